@@ -1,0 +1,1062 @@
+// TEST INFRASTRUCTURE — CPU FP64 restatement of the reference's ensemble
+// solve path, used only as the checker (tests/, smoke(), bench.py's CPU
+// baseline).  Never linked into the product.
+//
+// Parity status: pinned at the solution level against the reference's own
+// tolerance tests (tests/test_oracle.py); not pinned bit-for-bit against Julia
+// (the reference cannot run here).  Every routine cites the reference file it
+// restates; paths are relative to the OrdinaryDiffEq.jl checkout.
+//
+// Floating-point order: every `a*b + c` the reference writes under @muladd is
+// written here as fma(a, b, c) with the same nesting (MuladdMacro rewrites
+// `a1*k1 + a2*k2 + a3*k3` as muladd(a1,k1, muladd(a2,k2, a3*k3))).  The file
+// is compiled with -ffp-contract=off so no other contraction happens.
+#include "oracle.h"
+#include "oracle_tableaus.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------- helpers
+// Julia's min/max propagate NaN (Base.min/max on Float64).
+inline double jmin(double a, double b) { return (a != a || b != b) ? NAN : (a < b ? a : b); }
+inline double jmax(double a, double b) { return (a != a || b != b) ? NAN : (a > b ? a : b); }
+// Julia eps(x): spacing of doubles at |x|.
+inline double jeps(double x) {
+    double ax = std::fabs(x);
+    if (!std::isfinite(ax)) return NAN;
+    return std::nextafter(ax, INFINITY) - ax;
+}
+
+// x^y as used by the PI controller and initdt.  The reference calls
+// FastPower.fastpower (package FastPower, compat floor 1.1.2, not vendored;
+// lib/OrdinaryDiffEqCore/Project.toml:70), i.e. exp2(y*log2(x)).  Restated as
+// exp(y*ln x) with ln from the atanh series ln m = 2 atanh((m-1)/(m+1)) on
+// m in [1/sqrt2, sqrt2) and exp from range reduction by ln2 plus a Taylor
+// series (textbook methods, e.g. Muller, "Elementary Functions", ch. 5-6).
+const double LNC[13] = {2.0, 0.6666666666666666, 0.4, 0.2857142857142857, 0.2222222222222222,
+                        0.18181818181818182, 0.15384615384615385, 0.13333333333333333,
+                        0.11764705882352941, 0.10526315789473684, 0.09523809523809523,
+                        0.08695652173913043, 0.08};
+const double EXC[18] = {1.0, 1.0, 0.5, 0.16666666666666666, 0.041666666666666664,
+                        0.008333333333333333, 0.001388888888888889, 0.0001984126984126984,
+                        2.48015873015873e-05, 2.7557319223985893e-06, 2.755731922398589e-07,
+                        2.505210838544172e-08, 2.08767569878681e-09, 1.6059043836821613e-10,
+                        1.1470745597729725e-11, 7.647163731819816e-13, 4.779477332387385e-14,
+                        2.8114572543455206e-15};
+const double LN2 = 0.6931471805599453, LN2LO = 2.3190468138462996e-17;
+const double INVLN2 = 1.4426950408889634, SQRT1_2 = 0.7071067811865476;
+
+double series_ln(double x) {  // x > 0 finite
+    int e;
+    double m = std::frexp(x, &e);
+    if (m < SQRT1_2) { m = m * 2.0; e -= 1; }
+    double s = (m - 1.0) / (m + 1.0);
+    double s2 = s * s;
+    double poly = LNC[12];
+    for (int k = 11; k >= 0; --k) poly = std::fma(poly, s2, LNC[k]);
+    double de = (double)e;
+    return std::fma(de, LN2, std::fma(de, LN2LO, s * poly));
+}
+double series_exp(double t) {
+    if (t != t) return t;
+    if (t > 709.0) return INFINITY;
+    if (t < -745.0) return 0.0;
+    double k = std::rint(t * INVLN2);
+    double r = std::fma(-k, LN2, t);
+    r = std::fma(-k, LN2LO, r);
+    double e = EXC[17];
+    for (int i = 16; i >= 0; --i) e = std::fma(e, r, EXC[i]);
+    return std::ldexp(e, (int)k);
+}
+double ctrl_pow(double x, double y) {
+    if (x == 0.0) return 0.0;
+    if (x != x || y != y) return NAN;
+    if (std::isinf(x)) return INFINITY;
+    return series_exp(y * series_ln(x));
+}
+
+// ---------------------------------------------------------------- models
+// Lorenz: lib/OrdinaryDiffEqCore/src/precompilation_setup.jl:1-6 with p = (sigma, rho, beta).
+// Robertson: benchmark/benchmarks.jl:93-100 with p = (k1, k2, k3).
+// Duffing chain (defined by the workload, not the reference): N oscillators,
+//   state interleaved (x1, v1, ..., xN, vN), fixed walls x0 = x_{N+1} = 0,
+//   p = (k stiffness, delta damping, beta cubic):
+//   x_i' = v_i,  v_i' = (k*lap_i - delta*v_i) - beta*(x_i*x_i*x_i),
+//   lap_i = (x_{i-1} + x_{i+1}) - 2 x_i.
+// Brusselator 1-D periodic, 32 cells on [0,1), interleaved (u1, v1, ...),
+//   p = (A, B, alpha), ae = alpha*ncells^2 (alpha/dx^2 as in
+//   benchmark/benchmarks.jl:243-247):
+//   u' = ((A + u*u*v) - (B+1)*u) + ae*lap(u),  v' = (B*u - u*u*v) + ae*lap(v).
+// Linear: u_i' = p0 * u_i (prob_ode_linear with p0 = 1.01, test/Regression_I/ode_dense_tests.jl:30-38).
+void rhs(int model, int n, const double* u, const double* p, double t, double* du) {
+    (void)t;
+    switch (model) {
+    case ORC_LINEAR:
+        for (int i = 0; i < n; ++i) du[i] = p[0] * u[i];
+        break;
+    case ORC_LORENZ:
+        du[0] = p[0] * (u[1] - u[0]);
+        du[1] = u[0] * (p[1] - u[2]) - u[1];
+        du[2] = u[0] * u[1] - p[2] * u[2];
+        break;
+    case ORC_ROBERTSON: {
+        double y1 = u[0], y2 = u[1], y3 = u[2];
+        du[0] = -p[0] * y1 + p[2] * y2 * y3;
+        du[1] = p[0] * y1 - p[1] * (y2 * y2) - p[2] * y2 * y3;
+        du[2] = p[1] * (y2 * y2);
+        break;
+    }
+    case ORC_DUFFING: {
+        int N = n / 2;
+        for (int i = 0; i < N; ++i) {
+            double x = u[2 * i], v = u[2 * i + 1];
+            double xl = i > 0 ? u[2 * i - 2] : 0.0;
+            double xr = i < N - 1 ? u[2 * i + 2] : 0.0;
+            double lap = (xl + xr) - 2.0 * x;
+            du[2 * i] = v;
+            du[2 * i + 1] = (p[0] * lap - p[1] * v) - p[2] * (x * x * x);
+        }
+        break;
+    }
+    case ORC_BRUSSELATOR: {
+        int N = n / 2;
+        double ae = p[2] * ((double)N * (double)N);
+        for (int i = 0; i < N; ++i) {
+            int il = i == 0 ? N - 1 : i - 1, ir = i == N - 1 ? 0 : i + 1;
+            double uu = u[2 * i], vv = u[2 * i + 1];
+            double lu = (u[2 * il] + u[2 * ir]) - 2.0 * uu;
+            double lv = (u[2 * il + 1] + u[2 * ir + 1]) - 2.0 * vv;
+            double u2v = uu * uu * vv;
+            du[2 * i] = ((p[0] + u2v) - (p[1] + 1.0) * uu) + ae * lu;
+            du[2 * i + 1] = (p[1] * uu - u2v) + ae * lv;
+        }
+        break;
+    }
+    }
+}
+
+// Analytic Jacobians (row-major J[i*n + j] = d f_i / d u_j).
+void jac(int model, int n, const double* u, const double* p, double t, double* J) {
+    (void)t;
+    std::memset(J, 0, sizeof(double) * n * n);
+    switch (model) {
+    case ORC_LINEAR:
+        for (int i = 0; i < n; ++i) J[i * n + i] = p[0];
+        break;
+    case ORC_LORENZ:
+        J[0] = -p[0]; J[1] = p[0]; J[2] = 0.0;
+        J[3] = p[1] - u[2]; J[4] = -1.0; J[5] = -u[0];
+        J[6] = u[1]; J[7] = u[0]; J[8] = -p[2];
+        break;
+    case ORC_ROBERTSON: {
+        double y2 = u[1], y3 = u[2];
+        J[0] = -p[0]; J[1] = p[2] * y3; J[2] = p[2] * y2;
+        J[3] = p[0]; J[4] = -2.0 * p[1] * y2 - p[2] * y3; J[5] = -p[2] * y2;
+        J[6] = 0.0; J[7] = 2.0 * p[1] * y2; J[8] = 0.0;
+        break;
+    }
+    case ORC_DUFFING: {
+        int N = n / 2;
+        for (int i = 0; i < N; ++i) {
+            double x = u[2 * i];
+            int rx = 2 * i, rv = 2 * i + 1;
+            J[rx * n + rv] = 1.0;
+            J[rv * n + rx] = -2.0 * p[0] - p[2] * (3.0 * (x * x));
+            J[rv * n + rv] = -p[1];
+            if (i > 0) J[rv * n + rx - 2] = p[0];
+            if (i < N - 1) J[rv * n + rx + 2] = p[0];
+        }
+        break;
+    }
+    case ORC_BRUSSELATOR: {
+        int N = n / 2;
+        double ae = p[2] * ((double)N * (double)N);
+        for (int i = 0; i < N; ++i) {
+            int il = i == 0 ? N - 1 : i - 1, ir = i == N - 1 ? 0 : i + 1;
+            double uu = u[2 * i], vv = u[2 * i + 1];
+            int ru = 2 * i, rv = 2 * i + 1;
+            J[ru * n + ru] = (2.0 * uu * vv - (p[1] + 1.0)) - 2.0 * ae;
+            J[ru * n + rv] = uu * uu;
+            J[ru * n + 2 * il] += ae;
+            J[ru * n + 2 * ir] += ae;
+            J[rv * n + ru] = p[1] - 2.0 * uu * vv;
+            J[rv * n + rv] = -(uu * uu) - 2.0 * ae;
+            J[rv * n + 2 * il + 1] += ae;
+            J[rv * n + 2 * ir + 1] += ae;
+        }
+        break;
+    }
+    }
+}
+
+// ---------------------------------------------------------------- integrator
+struct Step {  // one accepted step for dense output
+    double tprev, dt;
+    std::vector<double> y0, y1, k;  // k: nk * n
+};
+
+struct Dense {
+    int alg, model, n;
+    std::vector<double> p;
+    std::vector<Step> steps;
+};
+
+struct Integ {
+    int alg, model, n;
+    const double* p;
+    double t0, tf;
+    orc_opts o;
+    double t, dt, tprev, dtpropose, dtcache;
+    double EEst, q11, errold;
+    double beta1, beta2, qmin, qmax, qmax_first, gamma, qsteady_min, qsteady_max, qoldinit;
+    int order;
+    int64_t iter, success_iter;
+    bool accept_step, next_step_tstop;
+    double tstop_target;
+    std::vector<double> u, uprev, tmp, utilde, atmp, fsalfirst, fsallast;
+    std::vector<double> k;  // up to 16 stage vectors (or Rodas dense k1..k3), row k[s*n + i]
+    int nk_valid;          // Vern7 lazy: 10 until extra stages computed
+    // Rodas
+    std::vector<double> J, W, dT, ks, rhs, du;
+    std::vector<int> piv;
+    bool have_J;
+    std::vector<double> tstops;  // ascending
+    size_t itstop;
+    std::vector<double> saveat;
+    size_t isave;
+    double* t_out;
+    double* u_out;
+    int cap, nsaved;
+    double last_saved_t;
+    orc_stats st;
+    Dense* dense;
+    std::vector<double> interp_out;
+};
+
+thread_local int64_t g_rhs_calls = 0;  // counts every RHS call (the reference's counting-wrapper tests)
+
+inline void f_eval(Integ& I, const double* u, double t, double* du) {
+    ++g_rhs_calls;
+    rhs(I.model, I.n, u, I.p, t, du);
+}
+
+// calculate_residuals + ODE_DEFAULT_NORM:
+// lib/DiffEqBase/src/calculate_residuals.jl:9-14,117-125 and
+// lib/DiffEqBase/src/common_defaults.jl:69-75 (sqrt(sum(abs2)/n)).
+double residual_norm(Integ& I, const double* ut, const double* u0, const double* u1) {
+    double acc = 0.0;
+    for (int i = 0; i < I.n; ++i) {
+        double sc = std::fma(jmax(std::fabs(u0[i]), std::fabs(u1[i])), I.o.reltol, I.o.abstol);
+        double e = ut[i] / sc;
+        acc = std::fma(e, e, acc);
+    }
+    return std::sqrt(acc / (double)(I.n > 1 ? I.n : 1));
+}
+
+// Hairer initial step: lib/OrdinaryDiffEqCore/src/initdt.jl:17-298 (iip).
+double initdt(Integ& I) {
+    int n = I.n;
+    const double* u0 = I.u.data();
+    double t = I.t;
+    double dtmax = I.o.dtmax;
+    double dtmin = std::nextafter(jmax(I.o.dtmin, jeps(t)), INFINITY);
+    double smalldt = jmax(dtmin, 1e-6);
+    std::vector<double> sk(n), f0(n), f1(n), u1(n), tmp(n);
+    for (int i = 0; i < n; ++i) sk[i] = std::fma(std::fabs(u0[i]), I.o.reltol, I.o.abstol);
+    f_eval(I, u0, t, f0.data());
+    if (I.alg == ORC_TSIT5) I.fsallast = f0;
+    auto nrm = [&](const std::vector<double>& v) {
+        double a = 0.0;
+        for (int i = 0; i < n; ++i) a = std::fma(v[i], v[i], a);
+        return std::sqrt(a / (double)n);
+    };
+    for (int i = 0; i < n; ++i) tmp[i] = u0[i] / sk[i];
+    double d0 = nrm(tmp);
+    for (int i = 0; i < n; ++i) tmp[i] = f0[i] / sk[i];
+    double d1 = nrm(tmp);
+    if (d1 != d1) return dtmin;
+    double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? smalldt : (d0 / d1) / 100.0;
+    dt0 = jmin(dt0, dtmax);
+    if (dt0 < 10.0 * 2.220446049250313e-16) return jmax(smalldt, dtmin);
+    for (int i = 0; i < n; ++i) u1[i] = std::fma(dt0, f0[i], u0[i]);
+    f_eval(I, u1.data(), t + dt0, f1.data());
+    bool same = true;
+    for (int i = 0; i < n; ++i) same = same && (f0[i] == f1[i]);
+    if (n > 0 && same) return jmax(dtmin, 100.0 * dt0);
+    for (int i = 0; i < n; ++i) tmp[i] = (f1[i] - f0[i]) / sk[i];
+    double d2 = nrm(tmp) / dt0;
+    double mx = jmax(d1, d2);
+    double dt1;
+    if (mx <= 1e-15) {
+        dt1 = jmax(1e-6, dt0 * 1e-3);
+    } else {
+        // 10^(-(2 + log10 mx)/order) = exp(-(2 ln10 + ln mx)/order)
+        const double LN10 = 2.302585092994046;
+        dt1 = series_exp(-(2.0 * LN10 + series_ln(mx)) / (double)I.order);
+    }
+    return jmax(dtmin, jmin(jmin(100.0 * dt0, dt1), dtmax));
+}
+
+// ---------------------------------------------------------------- Tsit5
+// perform_step!(::Tsit5Cache): lib/OrdinaryDiffEqTsit5/src/tsit_perform_step.jl:309-367.
+void tsit5_step(Integ& I) {
+    int n = I.n;
+    double t = I.t, dt = I.dt;
+    const double* up = I.uprev.data();
+    double* K = I.k.data();
+    auto k = [&](int s) { return K + (s - 1) * n; };
+    std::memcpy(k(1), I.fsalfirst.data(), sizeof(double) * n);
+    double* tmp = I.tmp.data();
+    double a = dt * TSIT5_A[2][1];
+    for (int i = 0; i < n; ++i) tmp[i] = std::fma(a, k(1)[i], up[i]);
+    f_eval(I, tmp, std::fma(TSIT5_c[2], dt, t), k(2));
+    for (int s = 3; s <= 7; ++s) {
+        for (int i = 0; i < n; ++i) {
+            double acc = TSIT5_A[s][s - 1] * k(s - 1)[i];
+            for (int j = s - 2; j >= 1; --j) acc = std::fma(TSIT5_A[s][j], k(j)[i], acc);
+            tmp[i] = std::fma(dt, acc, up[i]);
+        }
+        if (s < 7) {
+            f_eval(I, tmp, std::fma(TSIT5_c[s], dt, t), k(s));
+        } else {
+            std::memcpy(I.u.data(), tmp, sizeof(double) * n);
+            f_eval(I, I.u.data(), t + dt, k(7));
+        }
+    }
+    std::memcpy(I.fsallast.data(), k(7), sizeof(double) * n);
+    I.st.nf += 6;
+    if (I.o.adaptive) {
+        for (int i = 0; i < n; ++i) {
+            double acc = TSIT5_bt[7] * k(7)[i];
+            for (int j = 6; j >= 1; --j) acc = std::fma(TSIT5_bt[j], k(j)[i], acc);
+            I.utilde[i] = dt * acc;
+        }
+        I.EEst = residual_norm(I, I.utilde.data(), up, I.u.data());
+    }
+    I.nk_valid = 7;
+}
+
+// Tsit5 interpolant: lib/OrdinaryDiffEqTsit5/src/interpolants.jl:25-65 with
+// Tsit5Interp (tsit_tableaus.jl:244-276); @evalpoly is Horner with muladd.
+void tsit5_interp(double th, double dt, const double* y0, const double* K, int n, double* out) {
+    double b[8];
+    double th2 = th * th;
+    b[1] = th * std::fma(th, std::fma(th, std::fma(th, TSIT5_R[1][4], TSIT5_R[1][3]), TSIT5_R[1][2]), TSIT5_R[1][1]);
+    for (int s = 2; s <= 7; ++s)
+        b[s] = th2 * std::fma(th, std::fma(th, TSIT5_R[s][4], TSIT5_R[s][3]), TSIT5_R[s][2]);
+    for (int i = 0; i < n; ++i) {
+        double acc = K[6 * n + i] * b[7];
+        for (int s = 6; s >= 1; --s) acc = std::fma(K[(s - 1) * n + i], b[s], acc);
+        out[i] = std::fma(dt, acc, y0[i]);
+    }
+}
+
+// ---------------------------------------------------------------- Vern7 / Vern9
+// Generic explicit RK stage: tmp = uprev + dt * sum_{j in mask} A[s][j] k_j with
+// the reference's muladd nesting (last term is the innermost product).
+template <int S>
+void erk_stage(int n, const double (&A)[S][S], const unsigned char (&Am)[S][S], int s,
+               const double* K, const double* up, double dt, double* out) {
+    int js[S];
+    int nj = 0;
+    for (int j = 1; j < s; ++j)
+        if (Am[s][j]) js[nj++] = j;
+    for (int i = 0; i < n; ++i) {
+        double acc = A[s][js[nj - 1]] * K[(js[nj - 1] - 1) * n + i];
+        for (int q = nj - 2; q >= 0; --q) acc = std::fma(A[s][js[q]], K[(js[q] - 1) * n + i], acc);
+        out[i] = std::fma(dt, acc, up[i]);
+    }
+}
+
+template <int S>
+void erk_combo(int n, const double (&w)[S], const unsigned char (&wm)[S], const double* K,
+               double* out_acc) {
+    int js[S];
+    int nj = 0;
+    for (int j = 1; j < S; ++j)
+        if (wm[j]) js[nj++] = j;
+    for (int i = 0; i < n; ++i) {
+        double acc = w[js[nj - 1]] * K[(js[nj - 1] - 1) * n + i];
+        for (int q = nj - 2; q >= 0; --q) acc = std::fma(w[js[q]], K[(js[q] - 1) * n + i], acc);
+        out_acc[i] = acc;
+    }
+}
+
+// perform_step!(::Vern7Cache): lib/OrdinaryDiffEqVerner/src/verner_rk_perform_step.jl:412-570 (lazy).
+void vern7_step(Integ& I) {
+    int n = I.n;
+    double t = I.t, dt = I.dt;
+    const double* up = I.uprev.data();
+    double* K = I.k.data();
+    double* tmp = I.tmp.data();
+    f_eval(I, up, t, K);
+    double a = dt * VERN7_A[2][1];
+    for (int i = 0; i < n; ++i) tmp[i] = std::fma(a, K[i], up[i]);
+    f_eval(I, tmp, std::fma(VERN7_c[2], dt, t), K + n);
+    for (int s = 3; s <= 10; ++s) {
+        erk_stage<17>(n, VERN7_A, VERN7_A_m, s, K, up, dt, tmp);
+        double ts = (s <= 8) ? std::fma(VERN7_c[s], dt, t) : t + dt;
+        f_eval(I, tmp, ts, K + (s - 1) * n);
+    }
+    std::vector<double> acc(n);
+    erk_combo<17>(n, VERN7_b, VERN7_b_m, K, acc.data());
+    for (int i = 0; i < n; ++i) I.u[i] = std::fma(dt, acc[i], up[i]);
+    I.st.nf += 10;
+    if (I.o.adaptive) {
+        erk_combo<17>(n, VERN7_bt, VERN7_bt_m, K, acc.data());
+        for (int i = 0; i < n; ++i) I.utilde[i] = dt * acc[i];
+        I.EEst = residual_norm(I, I.utilde.data(), up, I.u.data());
+    }
+    I.nk_valid = 10;
+}
+
+// Lazy extra stages: lib/OrdinaryDiffEqVerner/src/verner_addsteps.jl:80-195
+// (called with tprev, uprev, dt of the step).  Not counted in nf.
+void vern7_extra(int model, int n, const double* p, double tprev, double dt, const double* up, double* K) {
+    std::vector<double> tmp(n);
+    for (int s = 11; s <= 16; ++s) {
+        erk_stage<17>(n, VERN7_A, VERN7_A_m, s, K, up, dt, tmp.data());
+        rhs(model, n, tmp.data(), p, std::fma(VERN7_c[s], dt, tprev), K + (s - 1) * n);
+    }
+}
+
+// Vern7 interpolant: lib/OrdinaryDiffEqVerner/src/interpolants.jl:183-252.
+void vern7_interp(double th, double dt, const double* y0, const double* K, int n, double* out) {
+    static const int idx[13] = {1, 4, 5, 6, 7, 8, 9, 11, 12, 13, 14, 15, 16};
+    double b[17];
+    double th2 = th * th;
+    {
+        double acc = VERN7_R[1][7];
+        for (int p = 6; p >= 1; --p) acc = std::fma(th, acc, VERN7_R[1][p]);
+        b[1] = th * acc;
+    }
+    for (int q = 1; q < 13; ++q) {
+        int s = idx[q];
+        double acc = VERN7_R[s][7];
+        for (int p = 6; p >= 2; --p) acc = std::fma(th, acc, VERN7_R[s][p]);
+        b[s] = th2 * acc;
+    }
+    for (int i = 0; i < n; ++i) {
+        double acc = K[(16 - 1) * n + i] * b[16];
+        for (int q = 11; q >= 0; --q) acc = std::fma(K[(idx[q] - 1) * n + i], b[idx[q]], acc);
+        out[i] = std::fma(dt, acc, y0[i]);
+    }
+}
+
+// perform_step!(::Vern9Cache): lib/OrdinaryDiffEqVerner/src/verner_rk_perform_step.jl:1272-1420
+// (used only as the high-accuracy ground truth; saves are hit as tstops).
+void vern9_step(Integ& I) {
+    int n = I.n;
+    double t = I.t, dt = I.dt;
+    const double* up = I.uprev.data();
+    double* K = I.k.data();
+    double* tmp = I.tmp.data();
+    f_eval(I, up, t, K);
+    double a = dt * VERN9_A[2][1];
+    for (int i = 0; i < n; ++i) tmp[i] = std::fma(a, K[i], up[i]);
+    f_eval(I, tmp, std::fma(VERN9_c[2], dt, t), K + n);
+    for (int s = 3; s <= 16; ++s) {
+        erk_stage<17>(n, VERN9_A, VERN9_A_m, s, K, up, dt, tmp);
+        double ts = (s <= 14) ? std::fma(VERN9_c[s], dt, t) : t + dt;
+        f_eval(I, tmp, ts, K + (s - 1) * n);
+    }
+    std::vector<double> acc(n);
+    erk_combo<17>(n, VERN9_b, VERN9_b_m, K, acc.data());
+    for (int i = 0; i < n; ++i) I.u[i] = std::fma(dt, acc[i], up[i]);
+    I.st.nf += 16;
+    if (I.o.adaptive) {
+        erk_combo<17>(n, VERN9_bt, VERN9_bt_m, K, acc.data());
+        for (int i = 0; i < n; ++i) I.utilde[i] = dt * acc[i];
+        I.EEst = residual_norm(I, I.utilde.data(), up, I.u.data());
+    }
+    I.nk_valid = 16;
+}
+
+// ---------------------------------------------------------------- Rodas5P
+// LU with partial pivoting (row of largest |pivot|, first on ties) and the
+// triangular solves; stands in for LinearSolve's dense LU (not vendored).
+bool lu_factor(int n, double* W, int* piv) {
+    bool ok = true;
+    for (int c = 0; c < n; ++c) {
+        int pr = c;
+        double best = std::fabs(W[c * n + c]);
+        for (int r = c + 1; r < n; ++r) {
+            double v = std::fabs(W[r * n + c]);
+            if (v > best) { best = v; pr = r; }
+        }
+        piv[c] = pr;
+        if (pr != c)
+            for (int j = 0; j < n; ++j) std::swap(W[c * n + j], W[pr * n + j]);
+        double d = W[c * n + c];
+        if (d == 0.0) { ok = false; continue; }
+        double inv = 1.0 / d;
+        for (int r = c + 1; r < n; ++r) {
+            double l = W[r * n + c] * inv;
+            W[r * n + c] = l;
+            for (int j = c + 1; j < n; ++j) W[r * n + j] = std::fma(-l, W[c * n + j], W[r * n + j]);
+        }
+    }
+    return ok;
+}
+void lu_solve(int n, const double* LU, const int* piv, double* b) {
+    for (int c = 0; c < n; ++c)
+        if (piv[c] != c) std::swap(b[c], b[piv[c]]);
+    for (int r = 1; r < n; ++r) {
+        double acc = b[r];
+        for (int j = 0; j < r; ++j) acc = std::fma(-LU[r * n + j], b[j], acc);
+        b[r] = acc;
+    }
+    for (int r = n - 1; r >= 0; --r) {
+        double acc = b[r];
+        for (int j = r + 1; j < n; ++j) acc = std::fma(-LU[r * n + j], b[j], acc);
+        b[r] = acc / LU[r * n + r];
+    }
+}
+
+// perform_step!(::RosenbrockCache): lib/OrdinaryDiffEqRosenbrock/src/rosenbrock_perform_step.jl:729-847,
+// fused helpers :581-727 (left-to-right muladd accumulation), W = J - I/dtgamma
+// (lib/OrdinaryDiffEqDifferentiation/src/derivative_utils.jl:663-685), J reused
+// after a rejected step (do_newJW, :535-557).  Autonomous models: dT = 0; the
+// reference evaluates it by AD (one counted f call per fresh J, :181-227).
+void rodas5p_step(Integ& I) {
+    int n = I.n;
+    double t = I.t, dt = I.dt;
+    const double* up = I.uprev.data();
+    double invdt = 1.0 / dt;
+    double dtC[8][7], dtd[8];
+    for (int s = 0; s < 8; ++s) {
+        for (int j = 0; j < 7; ++j) dtC[s][j] = RODAS5P_C[s][j] * invdt;
+        dtd[s] = dt * RODAS5P_d[s];
+    }
+    double dtgamma = dt * RODAS5P_GAMMA;
+    double* fsal = I.fsalfirst.data();
+    f_eval(I, up, t, fsal);
+    I.st.nf += 1;
+    bool errorfail = I.EEst > 1.0;
+    bool new_jac = !(I.iter > 1 && errorfail) || !I.have_J;
+    if (I.iter <= 1) new_jac = true;
+    if (new_jac) {
+        jac(I.model, n, up, I.p, t, I.J.data());
+        I.st.njacs += 1;
+        // The reference differentiates f in t by AD (one counted call); every
+        // model here is autonomous, so the derivative is exactly zero.
+        f_eval(I, up, t, I.du.data());
+        std::fill(I.dT.begin(), I.dT.end(), 0.0);
+        I.st.nf += 1;
+        I.have_J = true;
+    }
+    double invdtgamma = 1.0 / dtgamma;
+    for (int i = 0; i < n * n; ++i) I.W[i] = I.J[i];
+    for (int i = 0; i < n; ++i) I.W[i * n + i] = std::fma(-1.0, invdtgamma, I.J[i * n + i]);
+    I.st.nw += 1;
+    lu_factor(n, I.W.data(), I.piv.data());
+    double* ks = I.ks.data();
+    double* r = I.rhs.data();
+    for (int i = 0; i < n; ++i) r[i] = fsal[i] + dtd[0] * I.dT[i];
+    lu_solve(n, I.W.data(), I.piv.data(), r);
+    for (int i = 0; i < n; ++i) ks[i] = -r[i];
+    I.st.nsolve += 1;
+    double* u = I.u.data();
+    double* du = I.du.data();
+    for (int s = 1; s < 8; ++s) {
+        for (int i = 0; i < n; ++i) {
+            double acc = up[i];
+            for (int j = 0; j < s; ++j) acc = std::fma(RODAS5P_A[s][j], ks[j * n + i], acc);
+            u[i] = acc;
+        }
+        f_eval(I, u, std::fma(RODAS5P_cc[s], dt, t), du);
+        I.st.nf += 1;
+        for (int i = 0; i < n; ++i) {
+            double acc = std::fma(dtd[s], I.dT[i], du[i]);
+            for (int j = 0; j < s; ++j) acc = std::fma(dtC[s][j], ks[j * n + i], acc);
+            r[i] = acc;
+        }
+        lu_solve(n, I.W.data(), I.piv.data(), r);
+        for (int i = 0; i < n; ++i) ks[s * n + i] = -r[i];
+        I.st.nsolve += 1;
+    }
+    // b = (A[8,1:7]..., 1), btilde = e_8 (rosenbrock_tableaus.jl:64-72)
+    for (int i = 0; i < n; ++i) {
+        double acc = up[i];
+        for (int j = 0; j < 7; ++j) acc = std::fma(RODAS5P_A[7][j], ks[j * n + i], acc);
+        acc = std::fma(1.0, ks[7 * n + i], acc);
+        u[i] = acc;
+    }
+    if (I.o.adaptive) {
+        for (int i = 0; i < n; ++i) I.utilde[i] = ks[7 * n + i];
+        I.EEst = residual_norm(I, I.utilde.data(), up, u);
+    }
+    // dense k_j = sum_i H[j,i] ks_i
+    double* K = I.k.data();
+    for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < n; ++i) {
+            double acc = 0.0;
+            for (int q = 0; q < 8; ++q) acc = std::fma(RODAS5P_H[j][q], ks[q * n + i], acc);
+            K[j * n + i] = acc;
+        }
+    I.nk_valid = 3;
+}
+
+// Rodas interpolant (interp_order 3): lib/OrdinaryDiffEqRosenbrock/src/rosenbrock_interpolants.jl:172-206.
+void rodas_interp(double th, const double* y0, const double* y1, const double* K, int n, double* out) {
+    double th1 = 1.0 - th;
+    for (int i = 0; i < n; ++i) {
+        double inner = std::fma(th, K[2 * n + i], K[n + i]);            // k2 + th*k3
+        inner = std::fma(th, inner, K[i]);                              // k1 + th*(...)
+        double v = std::fma(th1, inner, y1[i]);                         // y1 + th1*(...)
+        out[i] = std::fma(th1, y0[i], th * v);                          // th1*y0 + th*(...)
+    }
+}
+
+void do_step(Integ& I) {
+    switch (I.alg) {
+    case ORC_TSIT5: tsit5_step(I); break;
+    case ORC_VERN7: vern7_step(I); break;
+    case ORC_VERN9: vern9_step(I); break;
+    case ORC_RODAS5P: rodas5p_step(I); break;
+    }
+}
+
+void interpolate(Integ& I, double th, double* out) {
+    int n = I.n;
+    switch (I.alg) {
+    case ORC_TSIT5: tsit5_interp(th, I.dt, I.uprev.data(), I.k.data(), n, out); break;
+    case ORC_VERN7:
+        if (I.nk_valid < 16) {
+            vern7_extra(I.model, n, I.p, I.tprev, I.dt, I.uprev.data(), I.k.data());
+            I.nk_valid = 16;
+        }
+        vern7_interp(th, I.dt, I.uprev.data(), I.k.data(), n, out);
+        break;
+    case ORC_RODAS5P: rodas_interp(th, I.uprev.data(), I.u.data(), I.k.data(), n, out); break;
+    default: {  // Vern9 ground truth: linear (only reached if a save is not a tstop)
+        for (int i = 0; i < n; ++i) out[i] = (1.0 - th) * I.uprev[i] + th * I.u[i];
+    }
+    }
+}
+
+void push_save(Integ& I, double t, const double* v) {
+    if (I.nsaved < I.cap) {
+        if (I.t_out) I.t_out[I.nsaved] = t;
+        if (I.u_out) std::memcpy(I.u_out + (size_t)I.nsaved * I.n, v, sizeof(double) * I.n);
+    }
+    I.nsaved++;
+    I.last_saved_t = t;
+}
+
+// _savevalues!: lib/OrdinaryDiffEqCore/src/integrators/integrator_utils.jl:340-414.
+void savevalues(Integ& I) {
+    while (I.isave < I.saveat.size() && I.saveat[I.isave] <= I.t) {
+        double curt = I.saveat[I.isave++];
+        if (curt != I.t) {
+            double th = (curt - I.tprev) / I.dt;
+            interpolate(I, th, I.interp_out.data());
+            push_save(I, curt, I.interp_out.data());
+        } else {
+            if (curt == I.tf && !I.o.save_end) continue;
+            push_save(I, I.t, I.u.data());
+        }
+    }
+    if (I.alg == ORC_VERN7 && I.nk_valid > 10) I.nk_valid = 10;  // post_savevalues! resize
+}
+
+// modify_dt_for_tstops!: integrator_utils.jl:268-324.
+void modify_dt_for_tstops(Integ& I) {
+    if (I.itstop >= I.tstops.size()) { I.next_step_tstop = false; return; }
+    double tstop = I.tstops[I.itstop];
+    double dist = std::fabs(tstop - I.t);
+    double tol = (std::isfinite(tstop) && std::isfinite(I.t)) ? 100.0 * jeps(jmax(std::fabs(I.t), std::fabs(tstop))) : 0.0;
+    if (I.o.adaptive) {
+        double orig = std::fabs(I.dt);
+        I.dtpropose = orig;
+        if (orig + tol < dist) {
+            I.next_step_tstop = false;
+        } else {
+            I.next_step_tstop = true;
+            I.tstop_target = tstop;
+        }
+        I.dt = jmin(orig, dist);
+    } else {
+        if (std::fabs(I.dtcache) + tol < dist) {
+            I.next_step_tstop = false;
+        } else {
+            I.next_step_tstop = true;
+            I.tstop_target = tstop;
+        }
+        I.dt = jmin(std::fabs(I.dtcache), dist);
+    }
+}
+
+inline double dtmin_t(const Integ& I) { return std::fabs(jmax(jeps(I.t), I.o.dtmin)); }
+
+// fix_dt_at_bounds!: integrator_utils.jl:1243-1256.
+void fix_dt_at_bounds(Integ& I) {
+    I.dt = jmin(I.o.dtmax, I.dt);
+    I.dt = jmax(I.dt, dtmin_t(I));
+}
+
+// PI controller: lib/OrdinaryDiffEqCore/src/integrators/controllers.jl:805-843.
+double stepsize_controller(Integ& I) {
+    double qmax = I.success_iter == 0 ? I.qmax_first : I.qmax;
+    double q;
+    if (I.EEst == 0.0) {
+        q = 1.0 / qmax;
+    } else {
+        double q11 = ctrl_pow(I.EEst, I.beta1);
+        q = q11 / ctrl_pow(I.errold, I.beta2);
+        I.q11 = q11;
+        double x = q / I.gamma, lo = 1.0 / qmax, hi = 1.0 / I.qmin;
+        q = x > hi ? hi : (x < lo ? lo : x);
+    }
+    return q;
+}
+
+void record_dense(Integ& I) {
+    if (!I.dense) return;
+    Step s;
+    s.tprev = I.tprev;
+    s.dt = I.dt;
+    s.y0 = I.uprev;
+    s.y1 = I.u;
+    if (I.alg == ORC_VERN7 && I.nk_valid < 16) {
+        vern7_extra(I.model, I.n, I.p, I.tprev, I.dt, I.uprev.data(), I.k.data());
+        I.nk_valid = 16;
+    }
+    int nk = I.alg == ORC_TSIT5 ? 7 : I.alg == ORC_VERN7 ? 16 : I.alg == ORC_RODAS5P ? 3 : 0;
+    s.k.assign(I.k.begin(), I.k.begin() + (size_t)nk * I.n);
+    I.dense->steps.push_back(std::move(s));
+}
+
+// _loopfooter!: integrator_utils.jl:597-677.
+void loopfooter(Integ& I) {
+    double ttmp = I.t + I.dt;
+    if (I.o.adaptive) {
+        double q = stepsize_controller(I);
+        I.accept_step = I.EEst <= 1.0;
+        if (I.accept_step) {
+            I.st.naccept++;
+            I.tprev = I.t;
+            if (I.next_step_tstop) I.dt = I.dtpropose;
+            if (I.next_step_tstop) {
+                I.next_step_tstop = false;
+                I.t = I.tstop_target;
+            } else {
+                I.t = ttmp;
+            }
+            if (I.qsteady_min <= q && q <= I.qsteady_max) q = 1.0;
+            I.errold = jmax(I.EEst, I.qoldinit);
+            double dtnew = I.dt / q;
+            double dtp = jmin(std::fabs(I.o.dtmax), std::fabs(dtnew));
+            dtp = jmax(std::fabs(dtp), dtmin_t(I));
+            I.dtpropose = dtp;
+            record_dense(I);
+            savevalues(I);
+        } else {
+            I.st.nreject++;
+        }
+    } else {
+        I.st.naccept++;
+        I.tprev = I.t;
+        if (I.next_step_tstop) {
+            I.next_step_tstop = false;
+            I.t = I.tstop_target;
+        } else {
+            I.t = ttmp;
+        }
+        I.accept_step = true;
+        I.dtpropose = I.dt;
+        record_dense(I);
+        savevalues(I);
+    }
+}
+
+// loopheader!: integrator_utils.jl:84-127 (apply_step! :175-203, handle_step_rejection! :130-150).
+void loopheader(Integ& I) {
+    if (I.iter > 0) {
+        if (!I.o.adaptive || I.accept_step) {
+            I.success_iter++;
+            I.uprev = I.u;
+            I.dt = I.dtpropose;
+            if (I.alg == ORC_TSIT5) I.fsalfirst = I.fsallast;
+            modify_dt_for_tstops(I);
+        } else {
+            I.dt = I.dt / jmin(1.0 / I.qmin, I.q11 / I.gamma);
+        }
+    }
+    I.iter++;
+    fix_dt_at_bounds(I);
+    modify_dt_for_tstops(I);
+}
+
+// de_check_error: lib/DiffEqBase/src/check_error.jl:70-118.
+int check_error(Integ& I) {
+    if (I.dt != I.dt) return ORC_RC_DTNAN;
+    if (I.iter > I.o.maxiters) return ORC_RC_MAXITERS;
+    bool acc = I.accept_step;
+    if (I.o.adaptive) {
+        double next_tstop = I.itstop < I.tstops.size() ? I.tstops[I.itstop] : INFINITY;
+        if (std::fabs(I.dt) <= std::fabs(I.o.dtmin) && (!acc || I.t + I.dt < next_tstop))
+            return ORC_RC_DTLESSTHANMIN;
+        if (!acc && std::fabs(I.dt) <= std::fabs(jeps(I.t))) return ORC_RC_UNSTABLE;
+    }
+    if (acc)
+        for (int i = 0; i < I.n; ++i)
+            if (!std::isfinite(I.u[i])) return ORC_RC_UNSTABLE;
+    return ORC_RC_SUCCESS;
+}
+
+// solution_endpoint_match_cur_integrator!: integrator_utils.jl:540-588.
+void postamble(Integ& I) {
+    if (!I.o.save_end) return;
+    bool need;
+    if (I.nsaved == 0) {
+        need = true;
+    } else {
+        bool in_saveat = false;
+        if (I.o.saveat_given) {
+            if (I.o.saveat_scalar) {
+                in_saveat = false;
+            } else {
+                for (double s : I.saveat) in_saveat = in_saveat || (s == I.t);
+            }
+        }
+        need = I.last_saved_t != I.t &&
+               (I.o.save_end_user == 1 || in_saveat || I.t == I.tf || !I.o.saveat_given);
+    }
+    if (need) push_save(I, I.t, I.u.data());
+}
+
+int solve_one(Integ& I, const double* u0) {
+    int n = I.n;
+    I.u.assign(u0, u0 + n);
+    I.uprev = I.u;
+    I.tmp.assign(n, 0.0);
+    I.utilde.assign(n, 0.0);
+    I.atmp.assign(n, 0.0);
+    I.fsalfirst.assign(n, 0.0);
+    I.fsallast.assign(n, 0.0);
+    I.k.assign((size_t)16 * n, 0.0);
+    I.interp_out.assign(n, 0.0);
+    if (I.alg == ORC_RODAS5P) {
+        I.J.assign((size_t)n * n, 0.0);
+        I.W.assign((size_t)n * n, 0.0);
+        I.dT.assign(n, 0.0);
+        I.ks.assign((size_t)8 * n, 0.0);
+        I.rhs.assign(n, 0.0);
+        I.du.assign(n, 0.0);
+        I.piv.assign(n, 0);
+        I.have_J = false;
+    }
+    I.t = I.t0;
+    I.tprev = I.t0;
+    I.nk_valid = 0;
+    I.iter = 0;
+    I.success_iter = 0;
+    I.accept_step = false;
+    I.next_step_tstop = false;
+    I.EEst = 1.0;
+    I.q11 = 1.0;
+    I.errold = I.qoldinit;
+    I.nsaved = 0;
+    I.last_saved_t = NAN;
+    std::memset(&I.st, 0, sizeof(I.st));
+    if (I.o.save_start) push_save(I, I.t0, I.u.data());
+    if (I.alg == ORC_TSIT5) {  // initialize!: FSAL pre-start (tsit_perform_step.jl:293-307)
+        f_eval(I, I.u.data(), I.t, I.fsalfirst.data());
+        I.st.nf += 1;
+    }
+    if (I.o.dt > 0.0) {
+        I.dt = I.o.dt;
+    } else {
+        I.dt = initdt(I);
+        I.st.nf += 2;
+    }
+    I.dtpropose = I.dt;
+    I.dtcache = I.dt;
+    int rc = ORC_RC_DEFAULT;
+    while (I.itstop < I.tstops.size()) {
+        double first_tstop = I.tstops[I.itstop];
+        while (I.t < first_tstop) {
+            loopheader(I);
+            int e = check_error(I);
+            if (e != ORC_RC_SUCCESS) {
+                postamble(I);
+                return e;
+            }
+            bool tiny = I.next_step_tstop && std::fabs(I.dt) < jeps(std::fabs(I.t));
+            if (!tiny) do_step(I);
+            bool should_exit = I.next_step_tstop;
+            loopfooter(I);
+            if (I.itstop >= I.tstops.size() || should_exit) break;
+        }
+        // handle_tstop!: integrator_utils.jl:1290-1314
+        if (I.itstop < I.tstops.size() && I.t == I.tstops[I.itstop]) {
+            while (I.itstop < I.tstops.size() && I.tstops[I.itstop] == I.t) I.itstop++;
+        }
+    }
+    postamble(I);
+    rc = ORC_RC_SUCCESS;
+    return rc;
+}
+
+void setup(Integ& I, int alg, int model, int n, const double* p, double t0, double tf, const orc_opts* o,
+           const double* saveat, int nsave, const double* tstops, int ntstops) {
+    I.alg = alg;
+    I.model = model;
+    I.n = n;
+    I.p = p;
+    I.t0 = t0;
+    I.tf = tf;
+    I.o = *o;
+    if (I.o.dtmax <= 0.0) I.o.dtmax = tf - t0;
+    if (I.o.maxiters <= 0) I.o.maxiters = 1000000;
+    I.order = alg == ORC_VERN7 ? 7 : alg == ORC_VERN9 ? 9 : 5;
+    // controller defaults: lib/OrdinaryDiffEqCore/src/alg_utils.jl:407-879
+    I.beta2 = 2.0 / (5.0 * I.order);
+    I.beta1 = 7.0 / (10.0 * I.order);
+    I.qmin = 0.2;
+    I.qmax = o->qmax > 0 ? o->qmax : 10.0;
+    I.qmax_first = o->qmax_first_step > 0 ? o->qmax_first_step : 10000.0;
+    I.gamma = 0.9;
+    I.qsteady_min = 1.0;
+    I.qsteady_max = alg == ORC_RODAS5P ? 1.2 : 1.0;
+    I.qoldinit = 1e-4;
+    I.tstops.clear();
+    for (int i = 0; i < ntstops; ++i)
+        if (tstops[i] > t0 && tstops[i] < tf) I.tstops.push_back(tstops[i]);
+    I.tstops.push_back(tf);
+    std::sort(I.tstops.begin(), I.tstops.end());
+    I.itstop = 0;
+    I.saveat.clear();
+    for (int i = 0; i < nsave; ++i)
+        if (saveat[i] > t0 && saveat[i] <= tf) I.saveat.push_back(saveat[i]);
+    std::sort(I.saveat.begin(), I.saveat.end());
+    I.isave = 0;
+    I.dense = nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t orc_rhs_calls(int reset) {
+    int64_t v = g_rhs_calls;
+    if (reset) g_rhs_calls = 0;
+    return v;
+}
+
+void orc_rhs(int model, int n, const double* u, const double* p, double t, double* du) {
+    rhs(model, n, u, p, t, du);
+}
+void orc_jac(int model, int n, const double* u, const double* p, double t, double* J) {
+    jac(model, n, u, p, t, J);
+}
+
+int orc_solve(int alg, int model, int n, const double* p, double t0, double tf, const double* u0,
+              const orc_opts* o, const double* saveat, int nsave_in, const double* tstops, int ntstops,
+              double* t_out, double* u_out, int cap, int32_t* retcode, orc_stats* st, void** dense_handle) {
+    Integ I;
+    setup(I, alg, model, n, p, t0, tf, o, saveat, nsave_in, tstops, ntstops);
+    I.t_out = t_out;
+    I.u_out = u_out;
+    I.cap = cap;
+    Dense* D = nullptr;
+    if (dense_handle) {
+        D = new Dense();
+        D->alg = alg;
+        D->model = model;
+        D->n = n;
+        int np = model == ORC_LINEAR ? 1 : 3;
+        D->p.assign(p, p + np);
+        I.dense = D;
+        *dense_handle = D;
+    }
+    int rc = solve_one(I, u0);
+    if (retcode) *retcode = rc;
+    if (st) *st = I.st;
+    return I.nsaved;
+}
+
+int orc_dense_nsteps(void* h) { return h ? (int)((Dense*)h)->steps.size() : 0; }
+
+int orc_dense_eval(void* h, const double* tq, int nq, double* out) {
+    Dense* D = (Dense*)h;
+    int n = D->n;
+    for (int q = 0; q < nq; ++q) {
+        double t = tq[q];
+        if (D->steps.empty()) return -1;
+        size_t s = 0;
+        if (t <= D->steps.front().tprev) {
+            std::memcpy(out + (size_t)q * n, D->steps.front().y0.data(), sizeof(double) * n);
+            continue;
+        }
+        while (s + 1 < D->steps.size() && D->steps[s].tprev + D->steps[s].dt < t) ++s;
+        const Step& S = D->steps[s];
+        double tend = S.tprev + S.dt;
+        if (t == tend) {
+            std::memcpy(out + (size_t)q * n, S.y1.data(), sizeof(double) * n);
+            continue;
+        }
+        double th = (t - S.tprev) / S.dt;
+        switch (D->alg) {
+        case ORC_TSIT5: tsit5_interp(th, S.dt, S.y0.data(), S.k.data(), n, out + (size_t)q * n); break;
+        case ORC_VERN7: vern7_interp(th, S.dt, S.y0.data(), S.k.data(), n, out + (size_t)q * n); break;
+        case ORC_RODAS5P: rodas_interp(th, S.y0.data(), S.y1.data(), S.k.data(), n, out + (size_t)q * n); break;
+        default:
+            for (int i = 0; i < n; ++i) out[(size_t)q * n + i] = (1.0 - th) * S.y0[i] + th * S.y1[i];
+        }
+    }
+    return 0;
+}
+
+void orc_dense_free(void* h) { delete (Dense*)h; }
+
+int orc_solve_ensemble(int alg, int model, int nmax, const int32_t* n_per_traj, int np, int64_t N,
+                       const double* u0, const double* p, const double* tspan, const orc_opts* o,
+                       const double* saveat, int nsave, int saveat_per_traj, double* t_out, double* u_out,
+                       int32_t* nsaved, int32_t* retcode, orc_stats* stats, int nthreads) {
+    if (nthreads <= 0) nthreads = (int)std::thread::hardware_concurrency();
+    if (nthreads <= 0) nthreads = 1;
+    int cap = nsave + 2;  // saveat points plus possible start and end saves
+    std::atomic<int64_t> next(0);
+    auto worker = [&]() {
+        std::vector<double> uj(nmax), pj(np), sv(nsave > 0 ? nsave : 1), tl(cap), ul((size_t)cap * nmax);
+        Integ I;
+        for (;;) {
+            int64_t j = next.fetch_add(1);
+            if (j >= N) break;
+            int n = n_per_traj ? n_per_traj[j] : nmax;
+            for (int i = 0; i < n; ++i) uj[i] = u0[(size_t)i * N + j];
+            for (int i = 0; i < np; ++i) pj[i] = p[(size_t)i * N + j];
+            for (int s = 0; s < nsave; ++s) sv[s] = saveat_per_traj ? saveat[(size_t)s * N + j] : saveat[s];
+            double t0 = tspan[j], tf = tspan[N + j];
+            setup(I, alg, model, n, pj.data(), t0, tf, o, sv.data(), nsave, nullptr, 0);
+            I.t_out = tl.data();
+            I.u_out = ul.data();
+            I.cap = cap;
+            int rc = solve_one(I, uj.data());
+            int ns = I.nsaved < cap ? I.nsaved : cap;
+            if (nsaved) nsaved[j] = ns;
+            if (retcode) retcode[j] = rc;
+            if (stats) stats[j] = I.st;
+            for (int s = 0; s < ns; ++s) {
+                if (t_out) t_out[(size_t)s * N + j] = tl[s];
+                if (u_out)
+                    for (int i = 0; i < n; ++i) u_out[((size_t)s * nmax + i) * N + j] = ul[(size_t)s * n + i];
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (int i = 0; i < nthreads; ++i) th.emplace_back(worker);
+    for (auto& x : th) x.join();
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,181 @@
+"""TEST INFRASTRUCTURE — ctypes binding of the CPU oracle (liboracle.so).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module, as the checker.  The product never imports it.  See oracle.h for what
+the oracle restates and how far its parity is pinned.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+TSIT5, VERN7, RODAS5P, VERN9 = 0, 1, 2, 3
+LINEAR, LORENZ, ROBERTSON, DUFFING, BRUSSELATOR = 0, 1, 2, 3, 4
+RC_DEFAULT, RC_SUCCESS, RC_MAXITERS, RC_DTNAN, RC_DTLESSTHANMIN, RC_UNSTABLE = range(6)
+
+
+class Stats(C.Structure):
+    _fields_ = [(k, C.c_int64) for k in ("nf", "njacs", "nw", "nsolve", "naccept", "nreject")]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Opts(C.Structure):
+    _fields_ = [
+        ("reltol", C.c_double), ("abstol", C.c_double), ("dtmax", C.c_double),
+        ("dtmin", C.c_double), ("dt", C.c_double), ("adaptive", C.c_int32),
+        ("maxiters", C.c_int64), ("save_start", C.c_int32), ("save_end", C.c_int32),
+        ("save_end_user", C.c_int32), ("saveat_given", C.c_int32), ("saveat_scalar", C.c_int32),
+        ("qmax_first_step", C.c_double), ("qmax", C.c_double),
+    ]
+
+
+def build():
+    subprocess.check_call(["make", "-s", "-C", HERE])
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        dp = C.POINTER(C.c_double)
+        L.orc_solve.restype = C.c_int
+        L.orc_solve.argtypes = [C.c_int, C.c_int, C.c_int, dp, C.c_double, C.c_double, dp,
+                                C.POINTER(Opts), dp, C.c_int, dp, C.c_int, dp, dp, C.c_int,
+                                C.POINTER(C.c_int32), C.POINTER(Stats), C.POINTER(C.c_void_p)]
+        L.orc_dense_eval.argtypes = [C.c_void_p, dp, C.c_int, dp]
+        L.orc_dense_free.argtypes = [C.c_void_p]
+        L.orc_dense_nsteps.argtypes = [C.c_void_p]
+        L.orc_solve_ensemble.restype = C.c_int
+        L.orc_solve_ensemble.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int32), C.c_int,
+                                         C.c_int64, dp, dp, dp, C.POINTER(Opts), dp, C.c_int, C.c_int,
+                                         dp, dp, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                         C.POINTER(Stats), C.c_int]
+        L.orc_rhs_calls.restype = C.c_int64
+        L.orc_rhs_calls.argtypes = [C.c_int]
+        L.orc_rhs.argtypes = [C.c_int, C.c_int, dp, dp, C.c_double, dp]
+        L.orc_jac.argtypes = [C.c_int, C.c_int, dp, dp, C.c_double, dp]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def make_opts(reltol=1e-3, abstol=1e-6, dtmax=0.0, dtmin=0.0, dt=0.0, adaptive=True,
+              maxiters=1000000, save_start=False, save_end=True, save_end_user=-1,
+              saveat_given=True, saveat_scalar=False, qmax_first_step=0.0, qmax=0.0):
+    return Opts(reltol, abstol, dtmax, dtmin, dt, int(adaptive), maxiters, int(save_start),
+                int(save_end), save_end_user, int(saveat_given), int(saveat_scalar),
+                qmax_first_step, qmax)
+
+
+def solve(alg, model, u0, p, tspan, saveat=(), tstops=(), dense=False, **kw):
+    """Solve one trajectory; returns dict(t, u, retcode, stats, dense)."""
+    L = lib()
+    u0 = np.ascontiguousarray(u0, dtype=np.float64)
+    p = np.ascontiguousarray(np.atleast_1d(p), dtype=np.float64)
+    n = u0.size
+    sv = np.ascontiguousarray(saveat, dtype=np.float64)
+    ts = np.ascontiguousarray(tstops, dtype=np.float64)
+    cap = sv.size + 2
+    if kw.get("saveat_given", True) is False or sv.size == 0:
+        cap = 4
+    t_out = np.zeros(cap)
+    u_out = np.zeros((cap, n))
+    rc = C.c_int32(0)
+    st = Stats()
+    h = C.c_void_p(0)
+    o = make_opts(**kw)
+    ns = L.orc_solve(alg, model, n, _dp(p), tspan[0], tspan[1], _dp(u0), C.byref(o),
+                     _dp(sv) if sv.size else None, sv.size, _dp(ts) if ts.size else None, ts.size,
+                     _dp(t_out), _dp(u_out), cap, C.byref(rc), C.byref(st),
+                     C.byref(h) if dense else None)
+    ns = min(ns, cap)
+    out = {"t": t_out[:ns].copy(), "u": u_out[:ns].copy(), "retcode": rc.value, "stats": st.as_dict()}
+    if dense:
+        out["dense"] = DenseSolution(h, n)
+    return out
+
+
+class DenseSolution:
+    def __init__(self, h, n):
+        self.h, self.n = h, n
+
+    def __call__(self, ts):
+        ts = np.ascontiguousarray(np.atleast_1d(ts), dtype=np.float64)
+        out = np.zeros((ts.size, self.n))
+        lib().orc_dense_eval(self.h, _dp(ts), ts.size, _dp(out))
+        return out
+
+    @property
+    def nsteps(self):
+        return lib().orc_dense_nsteps(self.h)
+
+    def __del__(self):
+        try:
+            lib().orc_dense_free(self.h)
+        except Exception:
+            pass
+
+
+def solve_ensemble(alg, model, u0, p, tspan, saveat, reltol, abstol, n_per_traj=None,
+                   saveat_per_traj=False, nthreads=0, **kw):
+    """SoA ensemble solve.  u0: (nmax, N), p: (np, N), tspan: (2, N),
+    saveat: (nsave,) or (nsave, N).  Returns dict of SoA outputs."""
+    L = lib()
+    u0 = np.ascontiguousarray(u0, dtype=np.float64)
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    tspan = np.ascontiguousarray(tspan, dtype=np.float64)
+    sv = np.ascontiguousarray(saveat, dtype=np.float64)
+    nmax, N = u0.shape
+    nsave = sv.shape[0]
+    cap = nsave + 2
+    t_out = np.full((cap, N), np.nan)
+    u_out = np.full((cap, nmax, N), np.nan)
+    nsaved = np.zeros(N, dtype=np.int32)
+    rc = np.zeros(N, dtype=np.int32)
+    stats = (Stats * N)()
+    npt = None
+    if n_per_traj is not None:
+        npt = np.ascontiguousarray(n_per_traj, dtype=np.int32)
+    o = make_opts(reltol=reltol, abstol=abstol, **kw)
+    L.orc_solve_ensemble(alg, model, nmax, npt.ctypes.data_as(C.POINTER(C.c_int32)) if npt is not None else None,
+                         p.shape[0], N, _dp(u0), _dp(p), _dp(tspan), C.byref(o), _dp(sv), nsave,
+                         int(saveat_per_traj), _dp(t_out), _dp(u_out),
+                         nsaved.ctypes.data_as(C.POINTER(C.c_int32)), rc.ctypes.data_as(C.POINTER(C.c_int32)),
+                         stats, nthreads)
+    st = np.array([[getattr(stats[j], k) for k, _ in Stats._fields_] for j in range(N)], dtype=np.int64)
+    return {"t": t_out, "u": u_out, "nsaved": nsaved, "retcode": rc,
+            "stats": {k: st[:, i] for i, (k, _) in enumerate(Stats._fields_)}}
+
+
+def rhs(model, u, p, t=0.0):
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    p = np.ascontiguousarray(np.atleast_1d(p), dtype=np.float64)
+    du = np.zeros_like(u)
+    lib().orc_rhs(model, u.size, _dp(u), _dp(p), t, _dp(du))
+    return du
+
+
+def jac(model, u, p, t=0.0):
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    p = np.ascontiguousarray(np.atleast_1d(p), dtype=np.float64)
+    J = np.zeros((u.size, u.size))
+    lib().orc_jac(model, u.size, _dp(u), _dp(p), t, _dp(J))
+    return J
+
+
+def rhs_calls(reset=False):
+    return lib().orc_rhs_calls(int(reset))

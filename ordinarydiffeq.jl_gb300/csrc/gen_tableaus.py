@@ -1,0 +1,116 @@
+#!/usr/bin/env python3
+"""Generate ``tableaus.h`` (method coefficients for the device kernels).
+
+The coefficients are data that must equal the reference's exactly, so they are
+read from the reference's Julia sources rather than retyped:
+
+* Tsit5:  lib/OrdinaryDiffEqTsit5/src/tsit_tableaus.jl:45-101 (Float64 branch of
+  ``Tsit5ConstantCacheActual``) and :244-276 (``Tsit5Interp``).
+* Vern7:  lib/OrdinaryDiffEqVerner/src/verner_tableaus.jl:1129-1205 (``Vern7Tableau``),
+  :648-716 (``Vern7ExtraStages``), :880-972 (``Vern7InterpolationCoefficients``).
+* Rodas5P: lib/OrdinaryDiffEqRosenbrock/src/rosenbrock_tableaus.jl:23-72
+  (``RODAS5PA/C/c/d/H`` and ``Rodas5PTableau``).
+
+Each Julia literal is copied verbatim as a C++ double literal, so the C++ parser
+rounds it to the same IEEE double as Julia's parser does.  Run once in a
+checkout that has the reference tree; the output is committed.
+
+usage: python gen_tableaus.py <reference-root> [out.h]
+"""
+import os
+import re
+import sys
+
+LIT = r"(-?[0-9][0-9_]*(?:\.[0-9]*)?(?:[eE][-+]?[0-9]+)?)"
+
+
+def fold_block(text, header_regex):
+    """Return the body of the first ``@fold function`` whose header matches."""
+    m = re.search(header_regex, text)
+    if not m:
+        raise SystemExit("block not found: " + header_regex)
+    start = m.end()
+    end = text.index("\nend", start)
+    return text[start:end]
+
+
+def assignments(body):
+    out = {}
+    for line in body.splitlines():
+        line = line.split("#", 1)[0].strip()
+        m = re.match(r"^(\w+)\s*=\s*convert\(\s*T2?\s*,\s*" + LIT + r"\s*\)$", line)
+        if m:
+            out[m.group(1)] = m.group(2).replace("_", "")
+    return out
+
+
+def julia_matrix(text, name):
+    m = re.search(r"const " + name + r" = \[(.*?)\n\]", text, re.S)
+    if not m:
+        raise SystemExit("matrix not found: " + name)
+    rows = []
+    for line in m.group(1).strip().splitlines():
+        vals = line.strip().rstrip(",").replace(",", " ").split()
+        rows.append([v for v in vals])
+    return rows
+
+
+def as_double(lit):
+    lit = lit.strip()
+    if re.fullmatch(r"-?[0-9]+", lit):
+        return lit + ".0"
+    return lit
+
+
+def main():
+    ref = sys.argv[1]
+    out = sys.argv[2] if len(sys.argv) > 2 else os.path.join(os.path.dirname(__file__), "tableaus.h")
+    tsit = open(os.path.join(ref, "lib/OrdinaryDiffEqTsit5/src/tsit_tableaus.jl")).read()
+    vern = open(os.path.join(ref, "lib/OrdinaryDiffEqVerner/src/verner_tableaus.jl")).read()
+    ros = open(os.path.join(ref, "lib/OrdinaryDiffEqRosenbrock/src/rosenbrock_tableaus.jl")).read()
+
+    compiled = r"where \{\s*T <: CompiledFloats,\s*T2 <: CompiledFloats,?\s*\}"
+    blocks = [
+        ("TSIT5", assignments(fold_block(tsit, r"@fold function Tsit5ConstantCacheActual\(\s*::Type\{T\},\s*::Type\{T2\}\s*\)\s*" + compiled))),
+        ("TSIT5I", assignments(fold_block(tsit, r"@fold function Tsit5Interp\(::Type\{T\}\) where \{T <: CompiledFloats\}"))),
+        ("VERN7", assignments(fold_block(vern, r"@fold function Vern7Tableau\(\s*::Type\{T\},\s*::Type\{T2\}\s*\)\s*" + compiled))),
+        ("VERN7X", assignments(fold_block(vern, r"@fold function Vern7ExtraStages\(\s*::Type\{T\},\s*::Type\{T2\}\s*\)\s*" + compiled))),
+        ("VERN7I", assignments(fold_block(vern, r"@fold function Vern7InterpolationCoefficients\(::Type\{T\}\) where \{T <: CompiledFloats\}"))),
+    ]
+    lines = [
+        "// Generated by gen_tableaus.py from the reference's Julia tableau sources; do not edit.",
+        "// Tsit5: lib/OrdinaryDiffEqTsit5/src/tsit_tableaus.jl:45-101,244-276",
+        "// Vern7: lib/OrdinaryDiffEqVerner/src/verner_tableaus.jl:648-716,880-972,1129-1205",
+        "// Rodas5P: lib/OrdinaryDiffEqRosenbrock/src/rosenbrock_tableaus.jl:23-72",
+        "#pragma once",
+        "namespace odegb {",
+        "namespace tab {",
+    ]
+    for prefix, vals in blocks:
+        lines.append("// " + prefix)
+        for k, v in vals.items():
+            lines.append("constexpr double %s_%s = %s;" % (prefix, k, as_double(v)))
+    A = julia_matrix(ros, "RODAS5PA")
+    C = julia_matrix(ros, "RODAS5PC")
+    H = julia_matrix(ros, "RODAS5PH")
+    c = re.search(r"const RODAS5Pc = \[(.*?)\]", ros, re.S).group(1).replace("\n", " ").split(",")
+    d = re.search(r"const RODAS5Pd = \[(.*?)\]", ros, re.S).group(1).replace("\n", " ").split(",")
+    c = [x.strip() for x in c if x.strip()]
+    d = [x.strip() for x in d if x.strip()]
+    gamma = re.search(r"function Rodas5PTableau\(.*?gamma = " + LIT, ros, re.S).group(1)
+    lines.append("// RODAS5P (8 stages): A lower triangular 8x8, C 8x7, c 8, d 8, H 3x8")
+    lines.append("constexpr double RODAS5P_GAMMA = %s;" % as_double(gamma))
+    lines.append("constexpr double RODAS5P_A[8][8] = {%s};" % ", ".join("{" + ", ".join(as_double(v) for v in r) + "}" for r in A))
+    lines.append("constexpr double RODAS5P_C[8][7] = {%s};" % ", ".join("{" + ", ".join(as_double(v) for v in r) + "}" for r in C))
+    lines.append("constexpr double RODAS5P_c[8] = {%s};" % ", ".join(as_double(v) for v in c))
+    lines.append("constexpr double RODAS5P_d[8] = {%s};" % ", ".join(as_double(v) for v in d))
+    lines.append("constexpr double RODAS5P_H[3][8] = {%s};" % ", ".join("{" + ", ".join(as_double(v) for v in r) + "}" for r in H))
+    lines.append("}  // namespace tab")
+    lines.append("}  // namespace odegb")
+    with open(out, "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+    print("wrote", out, sum(len(v) for _, v in blocks), "named coefficients")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,211 @@
+"""Pin the CPU oracle against the reference's own tests for this path.
+
+The reference (Julia) cannot run here and stores no trajectory values, so the
+oracle is pinned at the solution level by restating the reference tests that
+constrain it (each test cites the file it mirrors).
+"""
+import numpy as np
+import pytest
+
+import pyoracle as O
+
+LIN = dict(model=O.LINEAR, p=[1.01], tspan=(0.0, 1.0))  # prob_ode_linear (u' = 1.01u, u0 = 0.5)
+
+
+LAM, TEND = 4.0, 2.0  # u' = 4u on (0, 2): errors stay above FP64 round-off at these dts
+
+
+def observed_order(alg, ks):
+    errs = []
+    for k in ks:
+        r = O.solve(alg, O.LINEAR, [0.5], [LAM], (0.0, TEND), saveat=[], saveat_given=False,
+                    dt=2.0 ** -k, adaptive=False)
+        errs.append(abs(r["u"][-1][0] / (0.5 * np.exp(LAM * TEND)) - 1.0))
+    errs = np.array(errs)
+    return float(np.mean(-np.diff(np.log2(errs)))), errs
+
+
+# Order checks in the manner of DiffEqDevTools.test_convergence (fixed-step solves at
+# halving dt; lib/OrdinaryDiffEqVerner/test/ode_verner_tests.jl:61-66 uses BigFloat
+# for Vern7, here the problem is scaled so FP64 round-off stays below the error).
+@pytest.mark.parametrize("alg,order,ks", [
+    (O.TSIT5, 5, (6, 7, 8)),
+    (O.VERN7, 7, (3, 4, 5, 6)),
+    (O.VERN9, 9, (3, 4, 5)),
+    (O.RODAS5P, 5, (3, 4, 5, 6)),
+])
+def test_convergence_order(alg, order, ks):
+    slope, errs = observed_order(alg, ks)
+    if alg == O.RODAS5P:
+        # "observed order > 6" on prob_ode_linear
+        # (lib/OrdinaryDiffEqRosenbrock/test/ode_rosenbrock_tests.jl:195-199).
+        assert slope > order - 0.2, (slope, errs)
+    else:
+        assert abs(slope - order) < 0.3, (slope, errs)
+
+
+def test_vern9_ground_truth_matches_analytic():
+    r = O.solve(O.VERN9, O.LINEAR, [0.5], [1.01], (0.0, 1.0), saveat=[], saveat_given=False,
+                reltol=1e-14, abstol=1e-14)
+    assert abs(r["u"][-1][0] - 0.5 * np.exp(1.01)) < 1e-13
+
+
+# test/Regression_I/ode_dense_tests.jl:55-80,370,430,480: adaptive solve from dt = 1/4
+# with dense output, interpolated on 0:1/16:1, against a fixed dt = 1/16 solve.
+@pytest.mark.parametrize("alg,tol1d,tol2d", [
+    (O.TSIT5, 2.0e-6, 4.0e-6),
+    (O.VERN7, 3.0e-9, 5.0e-9),
+    (O.RODAS5P, 2.0e-5, 3.0e-5),
+])
+def test_dense_regression(alg, tol1d, tol2d):
+    pts = np.arange(17) / 16.0
+    rng = np.random.default_rng(3)
+    for u0, tol in (([0.5], tol1d), (list(rng.random(8)), tol2d)):
+        r = O.solve(alg, O.LINEAR, u0, [1.01], (0.0, 1.0), saveat=[], saveat_given=False,
+                    dt=0.25, dense=True, save_start=True)
+        interp = r["dense"](pts)
+        fixed = O.solve(alg, O.LINEAR, u0, [1.01], (0.0, 1.0), saveat=list(pts[1:]), dt=1 / 16,
+                        adaptive=False, save_start=True)
+        assert fixed["u"].shape == interp.shape
+        assert np.max(np.abs(fixed["u"] - interp)) < tol
+
+
+def test_interpolant_endpoint_consistency():
+    # At theta = 1 every interpolant reproduces the step's end value.
+    for alg in (O.TSIT5, O.VERN7, O.RODAS5P):
+        r = O.solve(alg, O.LORENZ, [1.0, 0.0, 0.0], [10.0, 20.0, 8 / 3], (0.0, 0.5), saveat=[],
+                    saveat_given=False, dense=True, reltol=1e-6, abstol=1e-6)
+        d = r["dense"]
+        assert d.nsteps > 3
+        end = d([0.5])[0]
+        assert np.allclose(end, r["u"][-1], rtol=1e-12, atol=1e-12)
+
+
+# test/InterfaceIII/stats_tests.jl:5-38: counting wrapper equals stats.nf.
+@pytest.mark.parametrize("alg", [O.TSIT5, O.VERN7, O.VERN9, O.RODAS5P])
+def test_nf_counts_rhs_calls(alg):
+    O.rhs_calls(reset=True)
+    r = O.solve(alg, O.LINEAR, [1.0, 1.0], [5.0], (0.0, 1.0), saveat=[], saveat_given=False)
+    calls = O.rhs_calls(reset=True)
+    assert r["retcode"] == O.RC_SUCCESS
+    assert calls == r["stats"]["nf"]
+    st = r["stats"]
+    att = st["naccept"] + st["nreject"]
+    per = {O.TSIT5: 6, O.VERN7: 10, O.VERN9: 16, O.RODAS5P: 8}[alg]
+    base = 3 if alg == O.TSIT5 else 2
+    extra = st["njacs"] if alg == O.RODAS5P else 0
+    assert st["nf"] == base + per * att + extra
+    if alg == O.RODAS5P:
+        assert st["nsolve"] == 8 * att and st["nw"] == att
+
+
+# test/InterfaceI/controllers.jl:29-50: exp(-100) with default and restricted qmax_first_step.
+@pytest.mark.parametrize("alg", [O.TSIT5, O.VERN7])
+@pytest.mark.parametrize("qfs", [0.0, 10.0])
+def test_qmax_first_step_exp_decay(alg, qfs):
+    r = O.solve(alg, O.LINEAR, [1.0], [-1.0], (0.0, 100.0), saveat=[], saveat_given=False,
+                qmax_first_step=qfs)
+    assert r["retcode"] == O.RC_SUCCESS
+    assert abs(r["u"][-1][0] - np.exp(-100.0)) < 1e-6
+
+
+def test_qmax_first_step_changes_first_growth():
+    # From a tiny user dt the first accepted step may grow 10^4x by default but only
+    # 10x when qmax_first_step = qmax (controllers.jl:288-293 get_current_qmax).
+    kw = dict(saveat=[], saveat_given=False, dt=1e-8, maxiters=2)
+    a = O.solve(O.TSIT5, O.LINEAR, [1.0], [-1.0], (0.0, 100.0), **kw)
+    b = O.solve(O.TSIT5, O.LINEAR, [1.0], [-1.0], (0.0, 100.0), qmax_first_step=10.0, **kw)
+    assert a["retcode"] == b["retcode"] == O.RC_MAXITERS
+    # two accepted steps: dt1 = 1e-8, then dt2 > 10*dt1 by default but exactly 10*dt1
+    # when the first-step growth is capped at qmax = 10.
+    assert a["t"][-1] - 1e-8 > 1e-7 * 1.5
+    assert np.isclose(b["t"][-1], 1e-8 + 1e-7, rtol=1e-12)
+
+
+# lib/OrdinaryDiffEqRosenbrock/test/ode_rosenbrock_tests.jl:201-203: few steps on prob_ode_linear.
+def test_rodas5p_few_steps():
+    r = O.solve(O.RODAS5P, O.LINEAR, [0.5], [1.01], (0.0, 1.0), saveat=[], saveat_given=False)
+    assert r["retcode"] == O.RC_SUCCESS
+    assert r["stats"]["naccept"] + 1 < 20
+
+
+# test/InterfaceI/ode_saveat_tests.jl:185-190: saveat = 4.0 on (0, 15) -> [0, 4, 8, 12, 15].
+def test_saveat_number_endpoint():
+    r = O.solve(O.TSIT5, O.LINEAR, [1.0], [1.0], (0.0, 15.0), saveat=[4.0, 8.0, 12.0],
+                save_start=True, save_end=True, saveat_scalar=True)
+    assert list(r["t"]) == [0.0, 4.0, 8.0, 12.0, 15.0]
+    assert np.allclose(r["u"][:, 0], np.exp(r["t"]), rtol=2e-3)
+
+
+def test_saveat_vector_endpoint_rules():
+    # ode_saveat_tests.jl:259-268: saveat = [0.2] on (0, 0.4)
+    f = dict(model=O.LINEAR, u0=[10.0], p=[-1.0], tspan=(0.0, 0.4))
+
+    def ts(**kw):
+        return list(O.solve(O.TSIT5, f["model"], f["u0"], f["p"], f["tspan"], saveat=[0.2], **kw)["t"])
+
+    assert ts(save_start=False, save_end=False) == [0.2]
+    assert ts(save_start=True, save_end=True, save_end_user=1) == [0.0, 0.2, 0.4]
+    # default: save_end resolves to (tf in saveat) = False
+    assert ts(save_start=False, save_end=False, save_end_user=-1) == [0.2]
+
+
+def test_maxiters_retcode_and_partial_saves():
+    # ode_saveat_tests.jl:214-217: maxiters = 3 stops early with MaxIters.
+    r = O.solve(O.TSIT5, O.LINEAR, [1.0], [1.0], (0.0, 1.0), saveat=[], saveat_given=False,
+                save_start=True, maxiters=3, reltol=1e-12, abstol=1e-12)
+    assert r["retcode"] == O.RC_MAXITERS
+    assert len(r["t"]) == 2  # start + the final state (no saveat given)
+
+
+def test_nan_parameter_gives_failure_retcode():
+    r = O.solve(O.TSIT5, O.LORENZ, [1.0, 0.0, 0.0], [np.nan, 20.0, 8 / 3], (0.0, 1.0),
+                saveat=[0.5, 1.0])
+    assert r["retcode"] in (O.RC_DTNAN, O.RC_UNSTABLE, O.RC_DTLESSTHANMIN)
+
+
+@pytest.mark.parametrize("model,n,p", [
+    (O.LORENZ, 3, [10.0, 17.0, 8 / 3]),
+    (O.ROBERTSON, 3, [0.04, 3e7, 1e4]),
+    (O.DUFFING, 8, [0.5, 0.3, 2.0]),
+    (O.BRUSSELATOR, 64, [1.0, 3.0, 0.01]),
+])
+def test_model_jacobian_matches_finite_difference(model, n, p):
+    rng = np.random.default_rng(0)
+    u = rng.random(n) * (1e-3 if model == O.ROBERTSON else 1.0)
+    J = O.jac(model, u, p)
+    Jfd = np.zeros((n, n))
+    for j in range(n):
+        h = 1e-6 * max(1.0, abs(u[j]))
+        e = np.zeros(n)
+        e[j] = h
+        Jfd[:, j] = (O.rhs(model, u + e, p) - O.rhs(model, u - e, p)) / (2 * h)
+    assert np.allclose(J, Jfd, rtol=1e-5, atol=1e-4 * max(1.0, np.abs(J).max()))
+
+
+def test_robertson_known_values():
+    # Classic ROBER reference values at t = 1e5 (Hairer & Wanner II, sec. IV.10).
+    r = O.solve(O.RODAS5P, O.ROBERTSON, [1.0, 0.0, 0.0], [0.04, 3e7, 1e4], (0.0, 1e5),
+                saveat=[1e5], reltol=1e-8, abstol=1e-12)
+    y = r["u"][-1]
+    assert abs(y[0] - 1.786592e-2) < 2e-6
+    assert abs(y[1] - 7.274753e-8) < 2e-11
+    assert abs(sum(y) - 1.0) < 1e-9
+
+
+def test_ensemble_matches_single_solves():
+    N = 7
+    rng = np.random.default_rng(1)
+    rho = rng.uniform(0, 21, N)
+    u0 = np.tile(np.array([[1.0], [0.0], [0.0]]), (1, N))
+    p = np.vstack([np.full(N, 10.0), rho, np.full(N, 8 / 3)])
+    tspan = np.vstack([np.zeros(N), np.ones(N)])
+    sv = np.arange(1, 11) / 10.0
+    ens = O.solve_ensemble(O.TSIT5, O.LORENZ, u0, p, tspan, sv, 1e-8, 1e-8, save_start=True, nthreads=3)
+    for j in range(N):
+        one = O.solve(O.TSIT5, O.LORENZ, u0[:, j], p[:, j], (0.0, 1.0), saveat=sv, reltol=1e-8,
+                      abstol=1e-8, save_start=True)
+        ns = ens["nsaved"][j]
+        assert ns == len(one["t"]) == 11
+        assert np.array_equal(ens["u"][:ns, :, j], one["u"])
+        assert ens["stats"]["naccept"][j] == one["stats"]["naccept"]
