@@ -1,0 +1,180 @@
+/* libode_b200.so — C ABI of the GB300 ensemble ODE integrator.
+ *
+ * The drop-in point is the reference's many-trajectory solve
+ *   solve(EnsembleProblem(prob; prob_func), alg, ensemblealg; trajectories, saveat,
+ *         reltol, abstol)
+ * where ensemblealg is a SciMLBase.EnsembleAlgorithm (SciMLBase is not
+ * vendored; the call shape is exercised in lib/DiffEqBase/test/downstream/
+ * ensemble.jl:15-42).  A Julia `EnsembleGB300 <: EnsembleAlgorithm` evaluates
+ * prob_func on the host, packs the per-trajectory u0/p/tspan structure-of-
+ * arrays, and calls ode_solve_ensemble through ccall; it then builds one
+ * ODESolution per trajectory from t_out/u_out/retcode/stats.
+ *
+ * Everything the per-trajectory `solve(prob_i, alg; kwargs...)` does
+ * (lib/OrdinaryDiffEqCore/src/solve.jl:1-12, 128-946) runs on the GPU:
+ * initdt, the step loop with the PI controller, saveat interpolation and the
+ * retcode checks, for Tsit5, Vern7 and Rodas5P.
+ *
+ * Conventions: plain C types, caller-owned host buffers, 0 = success and a
+ * negative ode_status on error (never aborts the process).  Layouts are
+ * structure-of-arrays with the trajectory index fastest:
+ *   u0[i*N + j]          state i of trajectory j            (n_states x N)
+ *   p[k*N + j]           parameter k of trajectory j        (n_params x N)
+ *   tspan[j], tspan[N+j] t0 and tf of trajectory j          (2 x N)
+ *   saveat[s] shared, or saveat[s*N + j] per trajectory     (nsave or nsave x N)
+ *   t_out[s*N + j], u_out[(s*n_states + i)*N + j]           (cap x N, cap x n_states x N)
+ * with cap = nsave + 2 save slots per trajectory (start and end saves).
+ */
+#ifndef ODE_GB300_H
+#define ODE_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ODE_ABI_VERSION 1
+
+typedef struct ode_handle ode_handle;
+
+/* Algorithms: Tsit5 (lib/OrdinaryDiffEqTsit5/src/algorithms.jl:16-21),
+ * Vern7 (lib/OrdinaryDiffEqVerner/src/algorithms.jl:44-50, lazy = true),
+ * Rodas5P (lib/OrdinaryDiffEqRosenbrock/src/algorithms.jl:83-87). */
+enum ode_alg { ODE_TSIT5 = 0, ODE_VERN7 = 1, ODE_RODAS5P = 2 };
+
+/* Registered right-hand sides (with analytic Jacobians).  The reference takes
+ * an arbitrary f(du,u,p,t); device code cannot call Julia closures, so models
+ * are compiled in and chosen by id. */
+enum ode_model {
+    ODE_MODEL_LINEAR = 0,         /* u' = p0 u, any n                                 */
+    ODE_MODEL_LORENZ = 1,         /* n = 3, p = (sigma, rho, beta)                     */
+    ODE_MODEL_ROBERTSON = 2,      /* n = 3, p = (k1, k2, k3)                           */
+    ODE_MODEL_DUFFING_CHAIN = 3,  /* n = 2N, interleaved (x_i, v_i), p = (k, delta, beta) */
+    ODE_MODEL_BRUSSELATOR_1D = 4  /* n = 2*cells, interleaved (u_i, v_i), p = (A, B, alpha) */
+};
+
+/* FP64: every operation in double (the reference's arithmetic).
+ * MIXED: state and stage arithmetic in FP32 (and, for Rodas5P, the W
+ * factorisation in FP32 with FP64-residual iterative refinement); t, dt, the
+ * error-norm accumulator and the step-size controller stay FP64. */
+enum ode_precision { ODE_PREC_FP64 = 0, ODE_PREC_MIXED = 1 };
+
+/* Per-trajectory return codes, SciMLBase.ReturnCode meanings
+ * (lib/DiffEqBase/src/check_error.jl:70-118). */
+enum ode_retcode {
+    ODE_RC_DEFAULT = 0, ODE_RC_SUCCESS = 1, ODE_RC_MAXITERS = 2, ODE_RC_DTNAN = 3,
+    ODE_RC_DTLESSTHANMIN = 4, ODE_RC_UNSTABLE = 5,
+    ODE_RC_ABORTED = 6 /* stopped by ode_abort(); no reference counterpart */
+};
+
+enum ode_status {
+    ODE_OK = 0, ODE_E_INVALID = -1, ODE_E_CUDA = -2, ODE_E_NOMEM = -3,
+    ODE_E_UNSUPPORTED = -4, ODE_E_BUSY = -5, ODE_E_TIMEOUT = -6, ODE_E_NOTFOUND = -7
+};
+
+/* Per-trajectory counters; mirrors DiffEqBase.Stats (lib/DiffEqBase/src/stats.jl:30-44). */
+typedef struct {
+    int64_t nf, njacs, nw, nsolve, naccept, nreject;
+} ode_stats;
+
+typedef struct {
+    int32_t model_id;    /* ode_model */
+    int32_t alg_id;      /* ode_alg */
+    int32_t n_states;    /* state stride (the largest state count when n_per_traj is given) */
+    int32_t n_params;    /* parameters per trajectory */
+    int32_t precision;   /* ode_precision */
+    int32_t reserved;
+} ode_problem_desc;
+
+/* Solver keyword arguments (lib/OrdinaryDiffEqCore/src/solve.jl:128-202).
+ * The save_* flags arrive already resolved by the caller with the reference's
+ * defaults (solve.jl:141-143, 596-599). */
+typedef struct {
+    double reltol, abstol;      /* reference defaults 1e-3, 1e-6 when not given */
+    double dtmax;               /* <= 0: tf - t0 */
+    double dtmin;               /* 0: eps(t) */
+    double dt;                  /* > 0: initial dt, skips the initial-step heuristic */
+    int64_t maxiters;           /* <= 0: 1e6 */
+    int32_t save_start, save_end;
+    int32_t save_end_user;      /* -1 not given, else 0/1 (endpoint rule, integrator_utils.jl:540-588) */
+    int32_t saveat_scalar;      /* saveat was a number (t0+dt:dt:tf) */
+    int32_t nsave;              /* saveat entries (0 = no saveat) */
+    int32_t saveat_per_traj;    /* 0: saveat[nsave] shared; 1: saveat[nsave*N] */
+    double qmax_first_step;     /* <= 0: 10000 */
+    double qmax;                /* <= 0: 10 */
+    int32_t lanes_per_traj;     /* 0: tuned choice; else 1,2,4,8,16,32 where compiled */
+    int32_t scheduler;          /* 0 auto, 1 static (one lane group per trajectory), 2 persistent queue */
+    int32_t block_size;         /* 0: tuned */
+    int32_t ir_sweeps;          /* MIXED Rodas5P refinement sweeps (< 0: default 1) */
+} ode_options;
+
+/* Fill o with the reference's defaults. */
+void ode_options_default(ode_options* o);
+
+/* Open device `device`; hbm_budget bytes caps device memory the handle may
+ * hold (0: 90% of free memory).  One CUDA stream per handle. */
+int ode_create(int device, size_t hbm_budget, ode_handle** out);
+void ode_destroy(ode_handle* h);
+const char* ode_last_error(const ode_handle* h);
+const char* ode_status_string(int status);
+int ode_abi_version(void);
+
+/* Synchronous ensemble solve on caller-owned HOST buffers (layouts above).
+ * n_per_traj (may be NULL) gives each trajectory's state count (<= n_states,
+ * DUFFING_CHAIN only); trajectories are grouped by size on the device.
+ * Outputs are written before return.  stats and t_out may be NULL. */
+int ode_solve_ensemble(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int64_t ntraj,
+                       const int32_t* n_per_traj, const double* u0, const double* p, const double* tspan,
+                       const double* saveat, double* t_out, double* u_out, int32_t* nsaved,
+                       int32_t* retcode, ode_stats* stats);
+
+/* Same solve on DEVICE buffers already resident in HBM, enqueued on
+ * `cuda_stream` (NULL: the handle's stream); returns once enqueued.  Device
+ * scratch (work queues, size-class buckets) is owned by the handle. */
+int ode_solve_ensemble_device(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int64_t ntraj,
+                              const int32_t* n_per_traj_dev, const double* u0, const double* p,
+                              const double* tspan, const double* saveat, double* t_out, double* u_out,
+                              int32_t* nsaved, int32_t* retcode, ode_stats* stats, void* cuda_stream);
+
+/* Continuous-batching serving API.  ode_submit copies the request's inputs
+ * into handle-owned pinned/device memory and returns a ticket at once; the
+ * request starts on the device as soon as a slot and enough of the HBM
+ * budget are free, overlapping with requests already running.  Outputs land
+ * in the caller's buffers (which must stay valid) when ode_poll/ode_wait
+ * report completion. */
+int ode_submit(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int64_t ntraj,
+               const int32_t* n_per_traj, const double* u0, const double* p, const double* tspan,
+               const double* saveat, double* t_out, double* u_out, int32_t* nsaved, int32_t* retcode,
+               ode_stats* stats, uint64_t* ticket);
+/* done = 1 when the request's outputs are in place. */
+int ode_poll(ode_handle* h, uint64_t ticket, int32_t* done);
+/* Wait at most timeout_s seconds (< 0: forever). */
+int ode_wait(ode_handle* h, uint64_t ticket, double timeout_s);
+
+typedef struct {
+    int64_t submitted, admitted, completed, rejected, queued, running;
+    int64_t hbm_in_use, hbm_budget;
+    int32_t slots;
+    int32_t reserved;
+} ode_serving_stats;
+int ode_serving_stats_get(ode_handle* h, ode_serving_stats* s);
+/* Number of concurrent device slots (streams) used by the serving loop (default 8). */
+int ode_set_serving_slots(ode_handle* h, int32_t slots);
+
+/* Ask running kernels of this handle to stop; affected trajectories report
+ * ODE_RC_ABORTED.  Cleared by the next solve. */
+int ode_abort(ode_handle* h);
+
+/* Kernel launches made by this handle so far, and the device time of the
+ * last ensemble launch measured with CUDA events on its stream. */
+int ode_kernel_launches(const ode_handle* h, int64_t* launches);
+int ode_last_kernel_ms(const ode_handle* h, double* ms);
+
+/* Compiled kernel variants for (alg, model, precision, n): lanes per
+ * trajectory, for tuning and diagnostics.  Returns the count written. */
+int ode_query_variants(int alg, int model, int precision, int n, int32_t* lanes, int32_t cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,135 @@
+// Device helpers shared by every integrator kernel.
+//
+// All kernels are compiled with -fmad=false: every fused multiply-add is
+// written explicitly (fma / fmaf) in the nesting the reference's @muladd code
+// produces, so the FP64 path follows the reference's operation order.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace odegb {
+
+// ------------------------------------------------------------------ scalars
+template <class T> struct Arith;
+template <> struct Arith<double> {
+    static __device__ __forceinline__ double fma_(double a, double b, double c) { return fma(a, b, c); }
+    static __device__ __forceinline__ double abs_(double a) { return fabs(a); }
+};
+template <> struct Arith<float> {
+    static __device__ __forceinline__ float fma_(float a, float b, float c) { return fmaf(a, b, c); }
+    static __device__ __forceinline__ float abs_(float a) { return fabsf(a); }
+};
+template <class T> __device__ __forceinline__ T FMA(T a, T b, T c) { return Arith<T>::fma_(a, b, c); }
+template <class T> __device__ __forceinline__ T ABS(T a) { return Arith<T>::abs_(a); }
+
+// Julia's Base.min/max on floats propagate NaN.
+__device__ __forceinline__ double jmin(double a, double b) { return (a != a || b != b) ? __longlong_as_double(0x7ff8000000000000LL) : (a < b ? a : b); }
+__device__ __forceinline__ double jmax(double a, double b) { return (a != a || b != b) ? __longlong_as_double(0x7ff8000000000000LL) : (a > b ? a : b); }
+template <class T> __device__ __forceinline__ T tmax(T a, T b) { return (a != a || b != b) ? a + b : (a > b ? a : b); }
+// Julia eps(x): spacing of doubles at |x|.
+__device__ __forceinline__ double jeps(double x) {
+    double ax = fabs(x);
+    if (!isfinite(ax)) return __longlong_as_double(0x7ff8000000000000LL);
+    return nextafter(ax, __longlong_as_double(0x7ff0000000000000LL)) - ax;
+}
+
+// x^y for the step-size controller and the initial-step heuristic: the
+// reference calls FastPower.fastpower (exp2(y*log2 x)).  Evaluated here as
+// exp(y ln x): ln from the atanh series ln m = 2 atanh((m-1)/(m+1)) with
+// m in [1/sqrt2, sqrt2), exp by reduction modulo ln2 and a Taylor series
+// (textbook methods; Muller, "Elementary Functions", ch. 5-6).  Only +, *,
+// fma, IEEE division and exact scaling are used, so the result is identical
+// on every IEEE-754 machine that evaluates the same sequence.
+__device__ __forceinline__ double series_ln(double x) {
+    const double LN2 = 0.6931471805599453, LN2LO = 2.3190468138462996e-17, SQRT1_2 = 0.7071067811865476;
+    int e;
+    double m = frexp(x, &e);
+    if (m < SQRT1_2) { m = m * 2.0; e -= 1; }
+    double s = (m - 1.0) / (m + 1.0);
+    double s2 = s * s;
+    double poly = 0.08;
+    poly = fma(poly, s2, 0.08695652173913043);
+    poly = fma(poly, s2, 0.09523809523809523);
+    poly = fma(poly, s2, 0.10526315789473684);
+    poly = fma(poly, s2, 0.11764705882352941);
+    poly = fma(poly, s2, 0.13333333333333333);
+    poly = fma(poly, s2, 0.15384615384615385);
+    poly = fma(poly, s2, 0.18181818181818182);
+    poly = fma(poly, s2, 0.2222222222222222);
+    poly = fma(poly, s2, 0.2857142857142857);
+    poly = fma(poly, s2, 0.4);
+    poly = fma(poly, s2, 0.6666666666666666);
+    poly = fma(poly, s2, 2.0);
+    double de = (double)e;
+    return fma(de, LN2, fma(de, LN2LO, s * poly));
+}
+__device__ __forceinline__ double series_exp(double t) {
+    const double LN2 = 0.6931471805599453, LN2LO = 2.3190468138462996e-17, INVLN2 = 1.4426950408889634;
+    if (t != t) return t;
+    if (t > 709.0) return __longlong_as_double(0x7ff0000000000000LL);
+    if (t < -745.0) return 0.0;
+    double k = rint(t * INVLN2);
+    double r = fma(-k, LN2, t);
+    r = fma(-k, LN2LO, r);
+    double e = 2.8114572543455206e-15;
+    e = fma(e, r, 4.779477332387385e-14);
+    e = fma(e, r, 7.647163731819816e-13);
+    e = fma(e, r, 1.1470745597729725e-11);
+    e = fma(e, r, 1.6059043836821613e-10);
+    e = fma(e, r, 2.08767569878681e-09);
+    e = fma(e, r, 2.505210838544172e-08);
+    e = fma(e, r, 2.755731922398589e-07);
+    e = fma(e, r, 2.7557319223985893e-06);
+    e = fma(e, r, 2.48015873015873e-05);
+    e = fma(e, r, 0.0001984126984126984);
+    e = fma(e, r, 0.001388888888888889);
+    e = fma(e, r, 0.008333333333333333);
+    e = fma(e, r, 0.041666666666666664);
+    e = fma(e, r, 0.16666666666666666);
+    e = fma(e, r, 0.5);
+    e = fma(e, r, 1.0);
+    e = fma(e, r, 1.0);
+    return ldexp(e, (int)k);
+}
+__device__ __forceinline__ double ctrl_pow(double x, double y) {
+    if (x == 0.0) return 0.0;
+    if (x != x || y != y) return __longlong_as_double(0x7ff8000000000000LL);
+    if (isinf(x)) return __longlong_as_double(0x7ff0000000000000LL);
+    return series_exp(y * series_ln(x));
+}
+
+// ------------------------------------------------------------------ lane groups
+// A trajectory is owned by a group of L consecutive lanes of one warp; each
+// lane holds C state components (component index = lane_in_group*C + c).
+template <int L> struct Group {
+    unsigned mask;
+    int lane;   // lane within the group
+    __device__ __forceinline__ Group() {
+        int wl = threadIdx.x & 31;
+        lane = wl % L;
+        int base = wl - lane;
+        mask = (L == 32) ? 0xffffffffu : (((1u << L) - 1u) << base);
+    }
+    template <class T> __device__ __forceinline__ T sum(T v) const {
+#pragma unroll
+        for (int off = L / 2; off > 0; off >>= 1) v += __shfl_xor_sync(mask, v, off, L);
+        return v;
+    }
+    template <class T> __device__ __forceinline__ T bcast(T v, int src) const {
+        if (L == 1) return v;
+        return __shfl_sync(mask, v, src, L);
+    }
+    template <class T> __device__ __forceinline__ T from(T v, int src_lane) const {
+        if (L == 1) return v;
+        return __shfl_sync(mask, v, src_lane, L);
+    }
+    __device__ __forceinline__ bool any(bool b) const {
+        if (L == 1) return b;
+        return __any_sync(mask, b);
+    }
+    __device__ __forceinline__ void sync() const {
+        if (L > 1) __syncwarp(mask);
+    }
+};
+
+}  // namespace odegb

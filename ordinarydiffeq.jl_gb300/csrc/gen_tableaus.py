@@ -83,6 +83,7 @@ def main():
         "// Vern7: lib/OrdinaryDiffEqVerner/src/verner_tableaus.jl:648-716,880-972,1129-1205",
         "// Rodas5P: lib/OrdinaryDiffEqRosenbrock/src/rosenbrock_tableaus.jl:23-72",
         "#pragma once",
+        "#include <cuda_runtime.h>",
         "namespace odegb {",
         "namespace tab {",
     ]
@@ -98,13 +99,28 @@ def main():
     c = [x.strip() for x in c if x.strip()]
     d = [x.strip() for x in d if x.strip()]
     gamma = re.search(r"function Rodas5PTableau\(.*?gamma = " + LIT, ros, re.S).group(1)
-    lines.append("// RODAS5P (8 stages): A lower triangular 8x8, C 8x7, c 8, d 8, H 3x8")
+    lines.append("// RODAS5P (8 stages): A lower triangular 8x8, C 8x7, c 8, d 8, H 3x8.")
+    lines.append("// Accessors are constexpr functions so device code folds them to immediates.")
     lines.append("constexpr double RODAS5P_GAMMA = %s;" % as_double(gamma))
-    lines.append("constexpr double RODAS5P_A[8][8] = {%s};" % ", ".join("{" + ", ".join(as_double(v) for v in r) + "}" for r in A))
-    lines.append("constexpr double RODAS5P_C[8][7] = {%s};" % ", ".join("{" + ", ".join(as_double(v) for v in r) + "}" for r in C))
-    lines.append("constexpr double RODAS5P_c[8] = {%s};" % ", ".join(as_double(v) for v in c))
-    lines.append("constexpr double RODAS5P_d[8] = {%s};" % ", ".join(as_double(v) for v in d))
-    lines.append("constexpr double RODAS5P_H[3][8] = {%s};" % ", ".join("{" + ", ".join(as_double(v) for v in r) + "}" for r in H))
+
+    def accessor(name, rows, two_d=True):
+        if two_d:
+            body = ", ".join("{" + ", ".join(as_double(v) for v in r) + "}" for r in rows)
+            lines.append("__host__ __device__ constexpr double %s(int i, int j) {" % name)
+            lines.append("    constexpr double t[%d][%d] = {%s};" % (len(rows), len(rows[0]), body))
+            lines.append("    return t[i][j];")
+        else:
+            body = ", ".join(as_double(v) for v in rows)
+            lines.append("__host__ __device__ constexpr double %s(int i) {" % name)
+            lines.append("    constexpr double t[%d] = {%s};" % (len(rows), body))
+            lines.append("    return t[i];")
+        lines.append("}")
+
+    accessor("RODAS5P_A", A)
+    accessor("RODAS5P_C", C)
+    accessor("RODAS5P_c", c, two_d=False)
+    accessor("RODAS5P_d", d, two_d=False)
+    accessor("RODAS5P_H", H)
     lines.append("}  // namespace tab")
     lines.append("}  // namespace odegb")
     with open(out, "w") as fh:

@@ -1,0 +1,171 @@
+// Registered right-hand sides and analytic Jacobians.
+//
+// The reference takes an arbitrary Julia f(du, u, p, t) (and optional jac);
+// a device ensemble cannot call Julia closures, so models are registered at
+// compile time and selected by model_id.  Each is written for a lane group:
+// a lane holds C consecutive state components, neighbours across lanes come
+// from warp shuffles.  Operation order matches the oracle's restatement
+// exactly (explicit products and sums, no contraction).
+//
+//  LINEAR       u_i' = p0 u_i                       (prob_ode_linear, test/Regression_I/ode_dense_tests.jl:30-38)
+//  LORENZ       lib/OrdinaryDiffEqCore/src/precompilation_setup.jl:1-6, p = (sigma, rho, beta)
+//  ROBERTSON    benchmark/benchmarks.jl:93-100, p = (k1, k2, k3)
+//  DUFFING      chain of N oscillators, interleaved (x_i, v_i), walls x_0 = x_{N+1} = 0,
+//               p = (k, delta, beta): v_i' = (k*lap_i - delta*v_i) - beta*x_i^3
+//  BRUSSELATOR  1-D periodic, interleaved (u_i, v_i), p = (A, B, alpha), ae = alpha*ncells^2:
+//               u' = ((A + u^2 v) - (B+1) u) + ae*lap u,  v' = (B u - u^2 v) + ae*lap v
+#pragma once
+#include "common.cuh"
+
+namespace odegb {
+
+enum ModelId { M_LINEAR = 0, M_LORENZ = 1, M_ROBERTSON = 2, M_DUFFING = 3, M_BRUSSELATOR = 4 };
+
+struct Linear {
+    static constexpr int NP = 1;
+    template <class R, int L, int C>
+    __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>&) {
+#pragma unroll
+        for (int c = 0; c < C; ++c) du[c] = p[0] * u[c];
+    }
+    template <class R, int N>
+    __device__ static void jac(R (*J)[N], const R*, const R* p, double) {
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+#pragma unroll
+            for (int j = 0; j < N; ++j) J[i][j] = (i == j) ? p[0] : R(0);
+    }
+};
+
+struct Lorenz {
+    static constexpr int NP = 3;
+    template <class R, int L, int C>
+    __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>&) {
+        static_assert(L == 1 && C == 3, "Lorenz has 3 states on one lane");
+        du[0] = p[0] * (u[1] - u[0]);
+        du[1] = u[0] * (p[1] - u[2]) - u[1];
+        du[2] = u[0] * u[1] - p[2] * u[2];
+    }
+    template <class R, int N>
+    __device__ static void jac(R (*J)[N], const R* u, const R* p, double) {
+        J[0][0] = -p[0]; J[0][1] = p[0]; J[0][2] = R(0);
+        J[1][0] = p[1] - u[2]; J[1][1] = R(-1); J[1][2] = -u[0];
+        J[2][0] = u[1]; J[2][1] = u[0]; J[2][2] = -p[2];
+    }
+};
+
+struct Robertson {
+    static constexpr int NP = 3;
+    template <class R, int L, int C>
+    __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>&) {
+        static_assert(L == 1 && C == 3, "Robertson has 3 states on one lane");
+        R y1 = u[0], y2 = u[1], y3 = u[2];
+        du[0] = -p[0] * y1 + p[2] * y2 * y3;
+        du[1] = p[0] * y1 - p[1] * (y2 * y2) - p[2] * y2 * y3;
+        du[2] = p[1] * (y2 * y2);
+    }
+    template <class R, int N>
+    __device__ static void jac(R (*J)[N], const R* u, const R* p, double) {
+        R y2 = u[1], y3 = u[2];
+        J[0][0] = -p[0]; J[0][1] = p[2] * y3; J[0][2] = p[2] * y2;
+        J[1][0] = p[0]; J[1][1] = R(-2) * p[1] * y2 - p[2] * y3; J[1][2] = -p[2] * y2;
+        J[2][0] = R(0); J[2][1] = R(2) * p[1] * y2; J[2][2] = R(0);
+    }
+};
+
+// Neighbour values across lanes for the chain models: x of the last pair of
+// the previous lane and of the first pair of the next lane (wrapping).
+template <class R, int L, int C>
+__device__ __forceinline__ void chain_halo(const R* u, const Group<L>& g, int off, R& left, R& right) {
+    left = g.from(u[C - 2 + off], (g.lane + L - 1) % L);
+    right = g.from(u[0 + off], (g.lane + 1) % L);
+}
+
+struct Duffing {
+    static constexpr int NP = 3;
+    template <class R, int L, int C>
+    __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>& g) {
+        static_assert(C % 2 == 0, "Duffing lanes hold whole (x, v) pairs");
+        R xl, xr;
+        chain_halo<R, L, C>(u, g, 0, xl, xr);
+        if (g.lane == 0) xl = R(0);
+        if (g.lane == L - 1) xr = R(0);
+#pragma unroll
+        for (int q = 0; q < C / 2; ++q) {
+            R x = u[2 * q], v = u[2 * q + 1];
+            R left = q > 0 ? u[2 * q - 2] : xl;
+            R right = q < C / 2 - 1 ? u[2 * q + 2] : xr;
+            R lap = (left + right) - R(2) * x;
+            du[2 * q] = v;
+            du[2 * q + 1] = (p[0] * lap - p[1] * v) - p[2] * (x * x * x);
+        }
+    }
+    template <class R, int N>
+    __device__ static void jac(R (*J)[N], const R* u, const R* p, double) {
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+#pragma unroll
+            for (int j = 0; j < N; ++j) J[i][j] = R(0);
+#pragma unroll
+        for (int i = 0; i < N / 2; ++i) {
+            R x = u[2 * i];
+            J[2 * i][2 * i + 1] = R(1);
+            J[2 * i + 1][2 * i] = R(-2) * p[0] - p[2] * (R(3) * (x * x));
+            J[2 * i + 1][2 * i + 1] = -p[1];
+            if (i > 0) J[2 * i + 1][2 * i - 2] = p[0];
+            if (i < N / 2 - 1) J[2 * i + 1][2 * i + 2] = p[0];
+        }
+    }
+};
+
+struct Brusselator {
+    static constexpr int NP = 3;
+    template <class R, int L, int C>
+    __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>& g) {
+        static_assert(C % 2 == 0, "Brusselator lanes hold whole (u, v) cells");
+        constexpr int NC = L * C / 2;
+        R ae = p[2] * (R(NC) * R(NC));
+        R ul, ur, vl, vr;
+        chain_halo<R, L, C>(u, g, 0, ul, ur);
+        chain_halo<R, L, C>(u, g, 1, vl, vr);
+#pragma unroll
+        for (int q = 0; q < C / 2; ++q) {
+            R uu = u[2 * q], vv = u[2 * q + 1];
+            R uL = q > 0 ? u[2 * q - 2] : ul, uR = q < C / 2 - 1 ? u[2 * q + 2] : ur;
+            R vL = q > 0 ? u[2 * q - 1] : vl, vR = q < C / 2 - 1 ? u[2 * q + 3] : vr;
+            R lu = (uL + uR) - R(2) * uu;
+            R lv = (vL + vR) - R(2) * vv;
+            R u2v = uu * uu * vv;
+            du[2 * q] = ((p[0] + u2v) - (p[1] + R(1)) * uu) + ae * lu;
+            du[2 * q + 1] = (p[1] * uu - u2v) + ae * lv;
+        }
+    }
+    // Row block of the Jacobian owned by one lane-row index i (0..n-1), written
+    // into a dense row `row[n]`; used by the shared-memory W build.
+    template <class R>
+    __device__ static void jac_row(R* row, int n, int i, const R* uvec, const R* p) {
+        int NC = n / 2;
+        R ae = p[2] * (R(NC) * R(NC));
+        for (int j = 0; j < n; ++j) row[j] = R(0);
+        int cell = i / 2, il = cell == 0 ? NC - 1 : cell - 1, ir = cell == NC - 1 ? 0 : cell + 1;
+        R uu = uvec[2 * cell], vv = uvec[2 * cell + 1];
+        if ((i & 1) == 0) {
+            row[2 * cell] = (R(2) * uu * vv - (p[1] + R(1))) - R(2) * ae;
+            row[2 * cell + 1] = uu * uu;
+            row[2 * il] += ae;
+            row[2 * ir] += ae;
+        } else {
+            row[2 * cell] = p[1] - R(2) * uu * vv;
+            row[2 * cell + 1] = -(uu * uu) - R(2) * ae;
+            row[2 * il + 1] += ae;
+            row[2 * ir + 1] += ae;
+        }
+    }
+    template <class R, int N>
+    __device__ static void jac(R (*J)[N], const R* u, const R* p, double) {
+#pragma unroll 1
+        for (int i = 0; i < N; ++i) jac_row<R>(J[i], N, i, u, p);
+    }
+};
+
+}  // namespace odegb

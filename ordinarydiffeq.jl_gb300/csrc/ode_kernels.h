@@ -1,0 +1,67 @@
+// Kernel-side parameter block and the launcher table shared by the CUDA
+// translation units and the host runtime (ode_capi.cu).  Plain C++ types only.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace odegb {
+
+struct OdeStatsDev {
+    long long nf, njacs, nw, nsolve, naccept, nreject;
+};
+
+// Everything one ensemble launch needs.  Device pointers; SoA layouts:
+//   u0[i*N + j], p[i*N + j], tspan[j] / tspan[N + j],
+//   saveat[s] (shared) or saveat[s*N + j] (per trajectory),
+//   t_out[s*N + j], u_out[(s*nmax + i)*N + j].
+struct EnsembleArgs {
+    long long N;            // trajectories in the arrays
+    long long count;        // trajectories this launch integrates (entries of order, or N)
+    const long long* order; // optional trajectory indices (size-class buckets); nullptr = identity
+    int nmax;               // state stride
+    const double* u0;
+    const double* p;
+    const double* tspan;
+    const double* saveat;
+    int nsave;
+    int saveat_per_traj;
+    int nsave_cap;          // save slots per trajectory in t_out/u_out
+    double* t_out;
+    double* u_out;
+    int32_t* nsaved;
+    int32_t* retcode;
+    OdeStatsDev* stats;
+    // options
+    double reltol, abstol, dtmax, dtmin, dt;
+    long long maxiters;
+    int save_start, save_end, save_end_user, saveat_given, saveat_scalar;
+    double qmax_first_step, qmax;
+    int ir_sweeps;          // mixed Rosenbrock: refinement sweeps per solve
+    // scheduling
+    int persistent;
+    unsigned long long* queue;     // persistent work counter (zeroed before launch)
+    const volatile int* abort_flag;  // host-settable early stop (nullptr: none)
+};
+
+// One compiled kernel variant.
+struct KernelVariant {
+    int alg, model, prec;   // ode_alg, ode_model, ode_precision
+    int n;                  // state count handled (lanes * comps)
+    int lanes;              // lanes per trajectory
+    int smem_per_group;     // dynamic shared memory per lane group (bytes)
+    const void* fn;         // __global__ function
+    void (*launch)(const EnsembleArgs&, int grid, int block, size_t smem, cudaStream_t);
+    const char* name;
+};
+
+// Registries filled by each translation unit (static arrays).
+const KernelVariant* tsit5_variants(int* count);
+const KernelVariant* vern7_variants(int* count);
+const KernelVariant* rodas_variants(int* count);
+
+template <class K>
+void launch_kernel(K kernel, const EnsembleArgs& a, int grid, int block, size_t smem, cudaStream_t s) {
+    kernel<<<grid, block, smem, s>>>(a);
+}
+
+}  // namespace odegb

@@ -1,0 +1,347 @@
+"""SciML-shaped host API over libode_b200.so.
+
+Mirrors the reference's ensemble call
+    solve(EnsembleProblem(prob; prob_func, output_func, reduction, u_init), alg,
+          EnsembleGB300(); trajectories, batch_size, saveat, reltol, abstol, ...)
+(SciMLBase semantics as exercised in lib/DiffEqBase/test/downstream/ensemble.jl:7-118
+and NEWS.md "Ensemble RNG redesign": prob_func(prob, ctx), output_func(sol, ctx)).
+prob_func runs on the host for every trajectory; the packed structure-of-arrays
+batch goes to the GPU in one call.  A vectorised form (u0s / ps / tspans
+arrays instead of prob_func) skips the per-trajectory Python work.
+"""
+import ctypes as C
+import time
+from dataclasses import dataclass, field
+from enum import IntEnum
+
+import numpy as np
+
+from . import _lib
+from .saveat import resolve_saveat
+
+
+class ReturnCode(IntEnum):
+    Default = 0
+    Success = 1
+    MaxIters = 2
+    DtNaN = 3
+    DtLessThanMin = 4
+    Unstable = 5
+    Aborted = 6
+
+
+MODELS = {"linear": _lib.MODEL_LINEAR, "lorenz": _lib.MODEL_LORENZ, "robertson": _lib.MODEL_ROBERTSON,
+          "duffing_chain": _lib.MODEL_DUFFING_CHAIN, "brusselator_1d": _lib.MODEL_BRUSSELATOR_1D}
+N_PARAMS = {_lib.MODEL_LINEAR: 1, _lib.MODEL_LORENZ: 3, _lib.MODEL_ROBERTSON: 3,
+            _lib.MODEL_DUFFING_CHAIN: 3, _lib.MODEL_BRUSSELATOR_1D: 3}
+
+
+class _Alg:
+    alg_id = -1
+
+    def __repr__(self):
+        return type(self).__name__ + "()"
+
+
+class Tsit5(_Alg):
+    """Tsitouras 5(4) (lib/OrdinaryDiffEqTsit5/src/algorithms.jl:16-21)."""
+    alg_id = _lib.ODE_TSIT5
+
+
+class Vern7(_Alg):
+    """Verner 7(6), lazy interpolation stages (lib/OrdinaryDiffEqVerner/src/algorithms.jl:44-50)."""
+    alg_id = _lib.ODE_VERN7
+
+
+class Rodas5P(_Alg):
+    """Rodas5P Rosenbrock method with the analytic Jacobian of the model
+    (lib/OrdinaryDiffEqRosenbrock/src/algorithms.jl:83-87)."""
+    alg_id = _lib.ODE_RODAS5P
+
+
+@dataclass
+class EnsembleGB300:
+    """Ensemble algorithm running every trajectory on one GB300.
+
+    precision: "fp64" (the reference's arithmetic) or "mixed" (FP32 stages and,
+    for Rodas5P, FP32 LU with FP64-residual refinement; FP64 t, dt, error norm
+    and controller).  scheduler: "auto" | "static" | "persistent".
+    """
+    precision: str = "fp64"
+    lanes_per_traj: int = 0
+    scheduler: str = "auto"
+    block_size: int = 0
+    ir_sweeps: int = -1
+    device: int = 0
+
+    def prec_id(self):
+        return {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}[self.precision]
+
+    def sched_id(self):
+        return {"auto": 0, "static": 1, "persistent": 2}[self.scheduler]
+
+
+@dataclass
+class ODEProblem:
+    """An ODE over a registered model.  `model` is a name ("lorenz",
+    "robertson", "duffing_chain", "brusselator_1d", "linear") or id."""
+    model: object
+    u0: np.ndarray
+    tspan: tuple
+    p: np.ndarray = None
+
+    def __post_init__(self):
+        if isinstance(self.model, str):
+            self.model = MODELS[self.model]
+        self.u0 = np.asarray(self.u0, dtype=np.float64).ravel()
+        self.p = np.asarray(self.p if self.p is not None else [], dtype=np.float64).ravel()
+        self.tspan = (float(self.tspan[0]), float(self.tspan[1]))
+
+
+def remake(prob, u0=None, p=None, tspan=None):
+    return ODEProblem(prob.model, prob.u0 if u0 is None else u0, prob.tspan if tspan is None else tspan,
+                      prob.p if p is None else p)
+
+
+@dataclass
+class EnsembleContext:
+    sim_id: int
+    repeat: int
+    rng: np.random.Generator
+
+    @property
+    def i(self):
+        return self.sim_id
+
+
+def _default_output(sol, ctx):
+    return sol, False
+
+
+def _default_reduction(u, batch, I):
+    return u + list(batch), False
+
+
+@dataclass
+class EnsembleProblem:
+    prob: ODEProblem
+    prob_func: object = None
+    output_func: object = None
+    reduction: object = None
+    u_init: object = None
+    safetycopy: bool = True
+    # vectorised inputs (trajectory index last): u0s (n, N), ps (np, N), tspans (2, N)
+    u0s: np.ndarray = None
+    ps: np.ndarray = None
+    tspans: np.ndarray = None
+    n_per_traj: np.ndarray = None
+
+
+class ODESolution:
+    """One trajectory's result: t, u (list of state vectors), retcode, stats."""
+
+    def __init__(self, t, u, retcode, stats, prob=None, alg=None):
+        self.t = t
+        self.u = u
+        self.retcode = ReturnCode(int(retcode))
+        self.stats = stats
+        self.prob = prob
+        self.alg = alg
+
+    def __repr__(self):
+        return "ODESolution(retcode=%s, %d saves)" % (self.retcode.name, len(self.t))
+
+
+class _LazySolutions:
+    """List-like view creating ODESolution objects on access (cheap for 1M trajectories)."""
+
+    def __init__(self, res, alg, n_per_traj=None):
+        self.r = res
+        self.alg = alg
+        self.npt = n_per_traj
+
+    def __len__(self):
+        return self.r["retcode"].shape[0]
+
+    def __getitem__(self, j):
+        if isinstance(j, slice):
+            return [self[k] for k in range(*j.indices(len(self)))]
+        if j < 0:
+            j += len(self)
+        r = self.r
+        ns = int(r["nsaved"][j])
+        n = r["u"].shape[1] if self.npt is None else int(self.npt[j])
+        t = r["t"][:ns, j].copy()
+        u = [r["u"][s, :n, j].copy() for s in range(ns)]
+        st = {k: int(r["stats"][k][j]) for k in r["stats"]}
+        return ODESolution(t, u, r["retcode"][j], st, alg=self.alg)
+
+    def __iter__(self):
+        for j in range(len(self)):
+            yield self[j]
+
+
+@dataclass
+class EnsembleSolution:
+    u: object
+    elapsedTime: float
+    converged: bool = True
+    raw: dict = field(default=None, repr=False)
+
+
+_handles = {}
+
+
+def get_handle(device=0):
+    h = _handles.get(device)
+    if h is None:
+        L = _lib.load()
+        hp = C.c_void_p(0)
+        _lib.check(L.ode_create(device, 0, C.byref(hp)))
+        h = hp
+        _handles[device] = h
+    return h
+
+
+def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax):
+    o = _lib.Options()
+    L = _lib.load()
+    L.ode_options_default(C.byref(o))
+    o.reltol, o.abstol = reltol, abstol
+    o.dt = dt or 0.0
+    o.dtmax = dtmax or 0.0
+    o.dtmin = dtmin or 0.0
+    o.maxiters = int(maxiters)
+    o.save_start, o.save_end, o.save_end_user = int(sv.save_start), int(sv.save_end), sv.save_end_user
+    o.saveat_scalar = int(sv.scalar)
+    o.nsave = sv.nsave
+    o.saveat_per_traj = int(sv.per_traj)
+    o.qmax_first_step = qmax_first_step or 0.0
+    o.qmax = qmax or 0.0
+    o.lanes_per_traj = ens.lanes_per_traj
+    o.scheduler = ens.sched_id()
+    o.block_size = ens.block_size
+    o.ir_sweeps = ens.ir_sweeps
+    return o
+
+
+def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=1e-6, dt=None,
+                 dtmax=None, dtmin=None, maxiters=1000000, save_start=None, save_end=None, n_per_traj=None,
+                 qmax_first_step=None, qmax=None, return_times=False):
+    """Solve a packed ensemble.  u0s (n, N), ps (np, N), tspans (2, N).  Returns the
+    raw structure-of-arrays outputs dict (t, u, nsaved, retcode, stats)."""
+    L = _lib.load()
+    if isinstance(model, str):
+        model = MODELS[model]
+    u0s = np.ascontiguousarray(u0s, dtype=np.float64)
+    ps = np.ascontiguousarray(ps, dtype=np.float64)
+    tspans = np.ascontiguousarray(tspans, dtype=np.float64)
+    n, N = u0s.shape
+    sv = resolve_saveat(saveat, tspans, save_start, save_end)
+    o = _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax)
+    d = _lib.ProblemDesc(model, alg.alg_id, n, ps.shape[0], ens.prec_id(), 0)
+    cap = sv.nsave + 2
+    t_out = np.full((cap, N), np.nan)
+    u_out = np.full((cap, n, N), np.nan)
+    nsaved = np.zeros(N, dtype=np.int32)
+    rc = np.zeros(N, dtype=np.int32)
+    stats = np.zeros((N, 6), dtype=np.int64)
+    npt = None
+    if n_per_traj is not None:
+        npt = np.ascontiguousarray(n_per_traj, dtype=np.int32)
+    h = get_handle(ens.device)
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))
+    t0 = time.perf_counter()
+    status = L.ode_solve_ensemble(h, C.byref(d), C.byref(o), N, ip(npt) if npt is not None else None,
+                                  dp(u0s), dp(ps), dp(tspans), dp(sv.values) if sv.nsave else None,
+                                  dp(t_out), dp(u_out), ip(nsaved), ip(rc),
+                                  stats.ctypes.data_as(C.POINTER(_lib.Stats)))
+    elapsed = time.perf_counter() - t0
+    _lib.check(status, h)
+    names = ("nf", "njacs", "nw", "nsolve", "naccept", "nreject")
+    out = {"t": t_out, "u": u_out, "nsaved": nsaved, "retcode": rc,
+           "stats": {k: stats[:, i] for i, k in enumerate(names)}, "elapsed": elapsed}
+    return out
+
+
+def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, saveat=None, reltol=1e-3,
+          abstol=1e-6, dt=None, dtmax=None, dtmin=None, maxiters=1000000, save_start=None, save_end=None,
+          seed=0, qmax_first_step=None, qmax=None):
+    """solve(EnsembleProblem, alg, EnsembleGB300(); trajectories, saveat, reltol, abstol, ...)."""
+    ens = ensemblealg or EnsembleGB300()
+    if not isinstance(ens, EnsembleGB300):
+        raise TypeError("ensemble algorithm must be EnsembleGB300")
+    prob = eprob.prob
+    t_start = time.perf_counter()
+    if eprob.u0s is not None:
+        N = eprob.u0s.shape[1]
+        if trajectories is not None and trajectories != N:
+            raise ValueError("trajectories does not match the packed inputs")
+        u0s = eprob.u0s
+        ps = eprob.ps if eprob.ps is not None else np.repeat(prob.p[:, None], N, axis=1)
+        tspans = eprob.tspans if eprob.tspans is not None else np.repeat(np.array(prob.tspan)[:, None], N, axis=1)
+        res = solve_arrays(prob.model, alg, ens, u0s, ps, tspans, saveat, reltol, abstol, dt, dtmax, dtmin,
+                           maxiters, save_start, save_end, eprob.n_per_traj, qmax_first_step, qmax)
+        sols = _LazySolutions(res, alg, eprob.n_per_traj)
+        return EnsembleSolution(sols, time.perf_counter() - t_start, True, res)
+    if trajectories is None:
+        raise ValueError("trajectories is required")
+    batch_size = batch_size or trajectories
+    output_func = eprob.output_func or _default_output
+    reduction = eprob.reduction or _default_reduction
+    u = eprob.u_init if eprob.u_init is not None else []
+    converged = False
+    root = np.random.SeedSequence(seed)
+    done = 0
+    while done < trajectories:
+        ids = list(range(done, min(trajectories, done + batch_size)))
+        outs = _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, dtmin, maxiters,
+                            save_start, save_end, output_func, qmax_first_step, qmax)
+        u, converged = reduction(u, outs, range(ids[0] + 1, ids[-1] + 2))
+        done = ids[-1] + 1
+        if converged:
+            break
+    return EnsembleSolution(u, time.perf_counter() - t_start, converged)
+
+
+def _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, dtmin, maxiters, save_start,
+                 save_end, output_func, qmax_first_step, qmax):
+    repeat = {i: 1 for i in ids}
+    results = {}
+    todo = list(ids)
+    while todo:
+        probs, ctxs = [], []
+        for i in todo:
+            rng = np.random.default_rng(np.random.SeedSequence([root.entropy, i, repeat[i]]))
+            ctx = EnsembleContext(i + 1, repeat[i], rng)
+            pi = eprob.prob_func(eprob.prob, ctx) if eprob.prob_func else eprob.prob
+            probs.append(pi)
+            ctxs.append(ctx)
+        n = max(pp.u0.size for pp in probs)
+        if any(pp.model != probs[0].model for pp in probs):
+            raise ValueError("all trajectories of an ensemble must use the same model")
+        N = len(probs)
+        u0s = np.zeros((n, N))
+        npt = None
+        if any(pp.u0.size != n for pp in probs):
+            npt = np.array([pp.u0.size for pp in probs], dtype=np.int32)
+        for k, pp in enumerate(probs):
+            u0s[:pp.u0.size, k] = pp.u0
+        ps = np.stack([pp.p for pp in probs], axis=1)
+        tspans = np.array([pp.tspan for pp in probs]).T
+        res = solve_arrays(probs[0].model, alg, ens, u0s, ps, tspans, saveat, reltol, abstol, dt, dtmax, dtmin,
+                           maxiters, save_start, save_end, npt, qmax_first_step, qmax)
+        sols = _LazySolutions(res, alg, npt)
+        again = []
+        for k, i in enumerate(todo):
+            s = sols[k]
+            s.prob = probs[k]
+            out, rerun = output_func(s, ctxs[k])
+            if rerun:
+                repeat[i] += 1
+                again.append(i)
+            else:
+                results[i] = out
+        todo = again
+    return [results[i] for i in ids]

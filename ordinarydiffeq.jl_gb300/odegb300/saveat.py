@@ -1,0 +1,127 @@
+"""saveat / save_start / save_end resolution with the reference's rules.
+
+* A number saveat d means the range (t0 + d):d:tf (lib/OrdinaryDiffEqCore/src/solve.jl:1103-1124),
+  evaluated like Julia's Float64 range: when start, step and stop have exact
+  small rational forms the elements are the correctly rounded rationals (so
+  0.1:0.1:1.0 gives 0.3, not 0.1 + 0.2).
+* A vector saveat keeps the entries in (t0, tf] (the device skips the rest).
+* Defaults (solve.jl:141-143, 596-599): save_start = isempty(saveat) || saveat is a
+  number || t0 in saveat; save_end = isempty(saveat) || saveat is a number ||
+  tf in saveat.  Saving every step (empty saveat in the reference) is not
+  offered: without saveat only the start and end points are returned.
+"""
+from dataclasses import dataclass
+from fractions import Fraction
+
+import numpy as np
+
+_MAXINTFLOAT32 = 16777216  # maxintfloat(Float32), the bound Base.rat uses for Float64
+
+
+def julia_rat(x):
+    """Base.rat(x::Float64): continued-fraction rational with |num|,|den| <= 2^24."""
+    y = x
+    a, d = 1, 1
+    b, c = 0, 0
+    m = _MAXINTFLOAT32
+    while abs(y) <= m:
+        f = int(y)  # trunc
+        y -= f
+        a, c = f * a + c, a
+        b, d = f * b + d, b
+        if max(abs(a), abs(b)) > m:
+            return c, d
+        if b != 0 and float(a) / float(b) == x:
+            break
+        if y == 0:
+            break
+        y = 1.0 / y
+    return a, b
+
+
+def julia_float_range(start, step, stop):
+    """Elements of Julia's start:step:stop for Float64 (Base (:) on IEEE floats)."""
+    if step == 0:
+        raise ValueError("range step cannot be zero")
+    sn, sd = julia_rat(step)
+    if sd != 0 and sn / sd == step:
+        an, ad = julia_rat(start)
+        zn, zd = julia_rat(stop)
+        if ad != 0 and zd != 0 and an / ad == start and zn / zd == stop:
+            den = ad * sd // np.gcd(ad, sd)
+            start_n = round(start * den)
+            step_n = round(step * den)
+            if step_n != 0:
+                length = max(0, (den * zn - zd * start_n + step_n * zd) // (step_n * zd))
+                last = Fraction(start_n + (length - 1) * step_n, den)
+                nxt = Fraction(start_n + length * step_n, den)
+                if length > 0 and (Fraction(start) <= last <= Fraction(stop) + Fraction(step) / 2 or length == 0) \
+                        and not (Fraction(start) <= nxt <= Fraction(stop)):
+                    return np.array([float(Fraction(start_n + k * step_n, den)) for k in range(length)])
+    lf = (stop - start) / step
+    if lf < 0:
+        n = 0
+    elif lf == 0:
+        n = 1
+    else:
+        n = int(round(lf)) + 1
+        stop2 = start + (n - 1) * step
+        n -= int(start < stop < stop2) + int(start > stop > stop2)
+    return np.array([start + k * step for k in range(n)])
+
+
+@dataclass
+class SaveSpec:
+    values: np.ndarray
+    nsave: int
+    per_traj: bool
+    scalar: bool
+    save_start: bool
+    save_end: bool
+    save_end_user: int
+
+
+def resolve_saveat(saveat, tspans, save_start=None, save_end=None):
+    """tspans: (2, N).  Returns the SaveSpec passed to the C ABI."""
+    tspans = np.asarray(tspans, dtype=np.float64)
+    t0s, tfs = tspans[0], tspans[1]
+    same_span = bool(np.all(t0s == t0s[0]) and np.all(tfs == tfs[0])) if tspans.shape[1] else True
+    seu = -1 if save_end is None else int(bool(save_end))
+    if saveat is None or (not np.isscalar(saveat) and np.size(saveat) == 0):
+        return SaveSpec(np.zeros(0), 0, False, False, True if save_start is None else bool(save_start),
+                        True if save_end is None else bool(save_end), seu)
+    if np.isscalar(saveat):
+        d = abs(float(saveat))
+        if same_span:
+            vals = julia_float_range(t0s[0] + d, d, tfs[0])
+            per = False
+        else:
+            rows = [julia_float_range(a + d, d, b) for a, b in zip(t0s, tfs)]
+            m = max(len(r) for r in rows)
+            vals = np.full((m, len(rows)), np.inf)
+            for j, r in enumerate(rows):
+                vals[:len(r), j] = r
+            per = True
+        return SaveSpec(np.ascontiguousarray(vals), vals.shape[0], per, True,
+                        True if save_start is None else bool(save_start),
+                        True if save_end is None else bool(save_end), seu)
+    arr = np.asarray(saveat, dtype=np.float64)
+    if arr.ndim == 1:
+        vals = np.sort(arr)
+        ss = [float(t0s[0]) in set(vals.tolist())] if same_span else [a in set(vals.tolist()) for a in t0s]
+        se = [float(tfs[0]) in set(vals.tolist())] if same_span else [b in set(vals.tolist()) for b in tfs]
+        per = False
+    else:
+        vals = np.sort(arr, axis=0)
+        ss = [t0s[j] in set(vals[:, j].tolist()) for j in range(vals.shape[1])]
+        se = [tfs[j] in set(vals[:, j].tolist()) for j in range(vals.shape[1])]
+        per = True
+    if save_start is None:
+        if len(set(ss)) > 1:
+            raise ValueError("save_start differs between trajectories; pass save_start explicitly")
+        save_start = ss[0] if ss else False
+    if save_end is None:
+        if len(set(se)) > 1:
+            raise ValueError("save_end differs between trajectories; pass save_end explicitly")
+        save_end = se[0] if se else False
+    return SaveSpec(np.ascontiguousarray(vals), vals.shape[0], per, False, bool(save_start), bool(save_end), seu)

@@ -1,0 +1,83 @@
+"""Shared helpers for the GPU parity tests: seeded workloads and comparisons."""
+import numpy as np
+
+import pyoracle as O
+from odegb300 import EnsembleGB300, Rodas5P, Tsit5, Vern7, solve_arrays
+from odegb300.saveat import resolve_saveat
+
+ALG = {"tsit5": (Tsit5(), O.TSIT5), "vern7": (Vern7(), O.VERN7), "rodas5p": (Rodas5P(), O.RODAS5P)}
+MODEL = {"linear": O.LINEAR, "lorenz": O.LORENZ, "robertson": O.ROBERTSON, "duffing_chain": O.DUFFING,
+         "brusselator_1d": O.BRUSSELATOR}
+
+
+def lorenz_inputs(N, seed=42):
+    """Lorenz workload: u0 = (1, 0, 0), sigma = 10, beta = 8/3, rho ~ U(0, 21)."""
+    rng = np.random.default_rng(seed)
+    u0 = np.tile(np.array([[1.0], [0.0], [0.0]]), (1, N))
+    p = np.vstack([np.full(N, 10.0), rng.uniform(0.0, 21.0, N), np.full(N, 8.0 / 3.0)])
+    tspan = np.vstack([np.zeros(N), np.ones(N)])
+    return u0, p, tspan
+
+
+def robertson_inputs(N, seed=42):
+    """ROBER: k = (0.04, 3e7, 1e4), each scaled by an independent log-uniform factor in [0.5, 2]."""
+    rng = np.random.default_rng(seed)
+    base = np.array([0.04, 3e7, 1e4])[:, None]
+    p = base * 2.0 ** rng.uniform(-1.0, 1.0, (3, N))
+    u0 = np.tile(np.array([[1.0], [0.0], [0.0]]), (1, N))
+    tspan = np.vstack([np.zeros(N), np.full(N, 1e5)])
+    return u0, p, tspan
+
+
+ROBER_SAVEAT = 10.0 ** np.linspace(-5.0, 5.0, 20)
+
+
+def duffing_inputs(N, n_osc, seed=42, tf_range=(1.0, 100.0)):
+    """Duffing chain: k, delta ~ U(0.1, 1), beta ~ U(0, 5), u0 ~ N(0, 1), tf log-uniform."""
+    rng = np.random.default_rng(seed)
+    if np.isscalar(n_osc):
+        npt = np.full(N, 2 * n_osc, dtype=np.int32)
+    else:
+        npt = (2 * rng.choice(np.asarray(n_osc), N)).astype(np.int32)
+    nmax = int(npt.max())
+    u0 = rng.standard_normal((nmax, N))
+    for j in range(N):
+        u0[npt[j]:, j] = 0.0
+    p = np.vstack([rng.uniform(0.1, 1.0, N), rng.uniform(0.1, 1.0, N), rng.uniform(0.0, 5.0, N)])
+    tf = 10.0 ** rng.uniform(np.log10(tf_range[0]), np.log10(tf_range[1]), N)
+    tspan = np.vstack([np.zeros(N), tf])
+    saveat = np.outer(np.arange(1, 17) / 16.0, tf)  # 16 uniform saves in (0, tf], tf included
+    return u0, p, tspan, saveat, npt
+
+
+def gpu(model, alg, u0, p, tspan, saveat, reltol, abstol, precision="fp64", **kw):
+    ens = EnsembleGB300(precision=precision, lanes_per_traj=kw.pop("lanes", 0), scheduler=kw.pop("scheduler", "auto"),
+                        ir_sweeps=kw.pop("ir_sweeps", -1))
+    return solve_arrays(model, ALG[alg][0], ens, u0, p, tspan, saveat, reltol, abstol, **kw)
+
+
+def oracle(model, alg, u0, p, tspan, saveat, reltol, abstol, n_per_traj=None, **kw):
+    sv = resolve_saveat(saveat, tspan, kw.pop("save_start", None), kw.pop("save_end", None))
+    return O.solve_ensemble(ALG[alg][1], MODEL[model], u0, p, tspan, sv.values, reltol, abstol,
+                            n_per_traj=n_per_traj, saveat_per_traj=sv.per_traj, save_start=sv.save_start,
+                            save_end=sv.save_end, save_end_user=sv.save_end_user, saveat_given=sv.nsave > 0,
+                            saveat_scalar=sv.scalar, **kw)
+
+
+def compare(g, o, reltol, abstol, factor=10.0, step_slack=1):
+    """Saves agree within factor*(reltol*|u| + abstol); accepted steps within step_slack.
+    Returns a dict of agreement statistics."""
+    assert np.array_equal(g["nsaved"], o["nsaved"]), "save counts differ"
+    assert np.array_equal(g["retcode"], o["retcode"]), "retcodes differ"
+    ns = int(g["nsaved"].max())
+    gu, ou = g["u"][:ns], o["u"][:ns]
+    mask = ~np.isnan(ou)
+    diff = np.abs(gu - ou)
+    bound = factor * (reltol * np.abs(ou) + abstol)
+    ok = (diff <= bound) | ~mask
+    worst = float(np.nanmax(np.where(mask, diff / np.maximum(bound, 1e-300), 0.0)))
+    dsteps = np.abs(g["stats"]["naccept"] - o["stats"]["naccept"])
+    identical = np.all((gu == ou) | ~mask, axis=(0, 1))
+    return {"ok": bool(ok.all()), "worst_ratio": worst, "max_step_diff": int(dsteps.max()),
+            "frac_bit_identical": float(identical.mean()),
+            "steps_ok": bool((dsteps <= step_slack).all())}

@@ -1,0 +1,94 @@
+"""CPU-side checks: the C-ABI library builds, loads and exports every declared
+entry point; host-side saveat/save_start/save_end resolution follows the
+reference's rules; error paths that need no GPU."""
+import ctypes as C
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+from odegb300 import _lib, build
+from odegb300.saveat import julia_float_range, julia_rat, resolve_saveat
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[\w\s\*]+?\b(ode_\w+)\s*\(", text, re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    path = build.build()
+    L = C.CDLL(path)
+    names = declared_functions()
+    assert "ode_solve_ensemble" in names and "ode_submit" in names
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+    # the Python binding declares a signature for every exported entry point
+    assert names <= set(_lib.SIGNATURES), names - set(_lib.SIGNATURES)
+
+
+def test_abi_version_and_defaults_without_gpu():
+    L = _lib.load()
+    assert L.ode_abi_version() == 1
+    o = _lib.Options()
+    L.ode_options_default(C.byref(o))
+    assert o.reltol == 1e-3 and o.abstol == 1e-6 and o.maxiters == 1000000
+    assert o.save_start == 1 and o.save_end == 1 and o.save_end_user == -1
+    assert L.ode_status_string(-4).decode().startswith("unsupported")
+
+
+def test_variant_registry_covers_the_workloads():
+    L = _lib.load()
+    buf = (C.c_int32 * 8)()
+    for alg, model, n in [(0, 1, 3), (1, 1, 3), (2, 2, 3), (1, 3, 4), (1, 3, 8), (1, 3, 16), (1, 3, 32),
+                          (1, 3, 64)]:
+        for prec in (0, 1):
+            assert L.ode_query_variants(alg, model, prec, n, buf, 8) >= 1, (alg, model, n, prec)
+
+
+def test_julia_range_semantics():
+    # 0.1:0.1:1.0 gives correctly rounded tenths (0.3 == 3/10, not 0.1 + 0.2)
+    r = julia_float_range(0.1, 0.1, 1.0)
+    assert len(r) == 10 and r[2] == 0.3 and r[-1] == 1.0
+    assert julia_float_range(4.0, 4.0, 15.0).tolist() == [4.0, 8.0, 12.0]
+    assert julia_rat(0.1) == (1, 10)
+    assert julia_float_range(0.0, 0.25, 1.0).tolist() == [0.0, 0.25, 0.5, 0.75, 1.0]
+
+
+def test_save_flags_follow_reference_defaults():
+    ts = np.array([[0.0], [0.4]])
+    # test/InterfaceI/ode_saveat_tests.jl:240-268
+    s = resolve_saveat(0.1, ts)
+    assert s.scalar and s.save_start and s.save_end and s.values.tolist() == [0.1, 0.2, 0.3, 0.4]
+    s = resolve_saveat([0.2], ts)
+    assert not s.save_start and not s.save_end and s.save_end_user == -1
+    s = resolve_saveat([0.2], ts, save_start=True, save_end=True)
+    assert s.save_start and s.save_end and s.save_end_user == 1
+    s = resolve_saveat(np.arange(0, 0.5, 0.1), ts)
+    assert s.save_start  # t0 in saveat
+    s = resolve_saveat(None, ts)
+    assert s.nsave == 0 and s.save_start and s.save_end
+
+
+def test_per_trajectory_saveat_for_uneven_spans():
+    tf = np.array([1.0, 2.0, 4.0])
+    ts = np.vstack([np.zeros(3), tf])
+    sv = np.outer(np.arange(1, 17) / 16.0, tf)
+    s = resolve_saveat(sv, ts)
+    assert s.per_traj and s.nsave == 16 and not s.save_start and s.save_end
+    s = resolve_saveat(0.5, ts)
+    assert s.per_traj and s.values.shape == (8, 3) and np.isinf(s.values[2:, 0]).all()
+
+
+def test_invalid_arguments_are_rejected_without_gpu():
+    L = _lib.load()
+    rc = L.ode_solve_ensemble(None, None, None, 0, None, None, None, None, None, None, None, None, None, None)
+    assert rc == -1

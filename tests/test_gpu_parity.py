@@ -1,0 +1,118 @@
+"""GPU parity: the CUDA kernels (through the C ABI) against the CPU oracle.
+
+Bar: per-trajectory saveat values within 10x the tolerance (10*(reltol*|u| + abstol))
+and accepted-step counts within 1 for the FP64 path; the mixed path is held to
+the same value tolerance against the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+from gpu_common import (ROBER_SAVEAT, compare, duffing_inputs, gpu, lorenz_inputs, oracle,
+                        robertson_inputs)
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from odegb300 import build
+    build.build()
+
+
+@pytest.mark.parametrize("alg", ["tsit5", "vern7"])
+def test_lorenz_fp64(alg):
+    N = 512
+    u0, p, ts = lorenz_inputs(N)
+    g = gpu("lorenz", alg, u0, p, ts, 0.1, 1e-8, 1e-8)
+    o = oracle("lorenz", alg, u0, p, ts, 0.1, 1e-8, 1e-8)
+    assert g["nsaved"].min() == 11
+    c = compare(g, o, 1e-8, 1e-8)
+    assert c["ok"] and c["steps_ok"], c
+    # same operation order on both sides: most trajectories are bit-identical
+    assert c["frac_bit_identical"] > 0.9, c
+
+
+def test_robertson_rodas5p_fp64():
+    N = 512
+    u0, p, ts = robertson_inputs(N)
+    g = gpu("robertson", "rodas5p", u0, p, ts, ROBER_SAVEAT, 1e-6, 1e-10)
+    o = oracle("robertson", "rodas5p", u0, p, ts, ROBER_SAVEAT, 1e-6, 1e-10)
+    assert (g["retcode"] == 1).all()
+    c = compare(g, o, 1e-6, 1e-10)
+    assert c["ok"] and c["steps_ok"], c
+    for k in ("nf", "njacs", "nw", "nsolve", "naccept", "nreject"):
+        assert np.abs(g["stats"][k] - o["stats"][k]).max() <= 16, k
+
+
+@pytest.mark.parametrize("ir", [1, 2])
+def test_robertson_rodas5p_mixed(ir):
+    N = 512
+    u0, p, ts = robertson_inputs(N)
+    g = gpu("robertson", "rodas5p", u0, p, ts, ROBER_SAVEAT, 1e-6, 1e-10, precision="mixed", ir_sweeps=ir)
+    o = oracle("robertson", "rodas5p", u0, p, ts, ROBER_SAVEAT, 1e-6, 1e-10)
+    assert (g["retcode"] == 1).all()
+    c = compare(g, o, 1e-6, 1e-10, step_slack=10 ** 9)
+    assert c["ok"], c
+
+
+@pytest.mark.parametrize("alg", ["tsit5", "vern7"])
+@pytest.mark.parametrize("n_osc", [2, 4, 8, 16, 32])
+def test_duffing_fp64_lane_groups(alg, n_osc):
+    N = 256
+    u0, p, ts, sv, _ = duffing_inputs(N, n_osc, tf_range=(1.0, 10.0))
+    g = gpu("duffing_chain", alg, u0, p, ts, sv, 1e-6, 1e-6)
+    o = oracle("duffing_chain", alg, u0, p, ts, sv, 1e-6, 1e-6)
+    c = compare(g, o, 1e-6, 1e-6)
+    assert c["ok"] and c["steps_ok"], c
+
+
+@pytest.mark.parametrize("alg", ["tsit5", "vern7"])
+def test_duffing_mixed(alg):
+    N = 256
+    u0, p, ts, sv, _ = duffing_inputs(N, 4, tf_range=(1.0, 10.0))
+    g = gpu("duffing_chain", alg, u0, p, ts, sv, 1e-6, 1e-6, precision="mixed")
+    o = oracle("duffing_chain", alg, u0, p, ts, sv, 1e-6, 1e-6)
+    c = compare(g, o, 1e-6, 1e-6, step_slack=10 ** 9)
+    assert c["ok"], c
+
+
+def test_duffing_uneven_sizes_bucketed():
+    N = 600
+    u0, p, ts, sv, npt = duffing_inputs(N, [2, 4, 8, 16, 32], tf_range=(1.0, 10.0))
+    g = gpu("duffing_chain", "vern7", u0, p, ts, sv, 1e-6, 1e-6, n_per_traj=npt)
+    o = oracle("duffing_chain", "vern7", u0, p, ts, sv, 1e-6, 1e-6, n_per_traj=npt)
+    c = compare(g, o, 1e-6, 1e-6)
+    assert c["ok"] and c["steps_ok"], c
+
+
+def test_static_and_persistent_schedulers_agree():
+    N = 1000
+    u0, p, ts = lorenz_inputs(N, seed=7)
+    a = gpu("lorenz", "tsit5", u0, p, ts, 0.1, 1e-8, 1e-8, scheduler="static")
+    b = gpu("lorenz", "tsit5", u0, p, ts, 0.1, 1e-8, 1e-8, scheduler="persistent")
+    assert np.array_equal(a["u"], b["u"], equal_nan=True)
+    assert np.array_equal(a["stats"]["naccept"], b["stats"]["naccept"])
+
+
+def test_retcodes_match_oracle():
+    N = 64
+    u0, p, ts = lorenz_inputs(N)
+    p[0, :8] = np.nan
+    g = gpu("lorenz", "tsit5", u0, p, ts, 0.1, 1e-8, 1e-8)
+    o = oracle("lorenz", "tsit5", u0, p, ts, 0.1, 1e-8, 1e-8)
+    assert np.array_equal(g["retcode"], o["retcode"])
+    assert (g["retcode"][:8] != 1).all() and (g["retcode"][8:] == 1).all()
+    g = gpu("lorenz", "tsit5", u0, p, ts, 0.1, 1e-8, 1e-8, maxiters=5)
+    o = oracle("lorenz", "tsit5", u0, p, ts, 0.1, 1e-8, 1e-8, maxiters=5)
+    assert np.array_equal(g["retcode"], o["retcode"])
+    assert (g["retcode"][8:] == 2).all()
+    assert np.array_equal(g["nsaved"], o["nsaved"])
+
+
+def test_empty_ensemble():
+    u0, p, ts = lorenz_inputs(0)
+    g = gpu("lorenz", "tsit5", u0, p, ts, 0.1, 1e-8, 1e-8)
+    assert g["retcode"].shape == (0,)
