@@ -1,0 +1,397 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 ensemble ODE integrator (libode_b200.so).
+
+Default workload (one "step" = one full ensemble solve): 100,000 Robertson
+trajectories, Rodas5P with the analytic Jacobian, reltol 1e-6, abstol 1e-10,
+tspan (0, 1e5), 20 log-spaced saves; rate constants log-uniform-scaled per
+trajectory (seeded synthetic inputs; no dataset exists for this path).
+
+Both GPU forms run: plain FP64 and mixed precision.  `value` is the
+trajectories/s of the mixed form when its saves agree with the FP64 oracle
+within 10x the tolerance on a checked sample (else the FP64 form), inputs
+resident in HBM.  `e2e` is the same metric through the public host-buffer
+call (host->device copies and results back inside the timed region).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--config robertson|lorenz|duffing|brusselator] [--trajectories N]
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "ordinarydiffeq.jl_gb300"))
+
+CONFIGS = {
+    "robertson": ("Robertson kinetics, Rodas5P + analytic J, reltol 1e-6 abstol 1e-10, tspan (0,1e5), "
+                  "20 log-spaced saves", 100_000),
+    "lorenz": ("Lorenz, Tsit5, reltol=abstol=1e-8, tspan (0,1), saveat 0.1", 10_000),
+    "duffing": ("uneven Duffing chains N in {2,4,8,16,32}, Vern7, reltol 1e-6, 16 saves, tf log-uniform [1,100]",
+                1_000_000),
+    "brusselator": ("Brusselator-1D 32 cells (64 states), Rodas5P, reltol 1e-5 abstol 1e-8, tspan (0,10)",
+                    65_536),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="robertson", choices=sorted(CONFIGS))
+    ap.add_argument("--trajectories", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU-baseline sample time")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-small", action="store_true",
+                    help="one small FP64+mixed solve pair for ncu captures (no JSON line)")
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        dist.init_process_group(backend)
+    return world, rank, local, dist
+
+
+def workload(name, N, seed):
+    from odegb300 import workloads as W
+    return {"robertson": W.robertson, "lorenz": W.lorenz, "duffing": W.duffing,
+            "brusselator": W.brusselator}[name](N, seed=seed)
+
+
+def oracle_solve(wl, idx, nthreads=0):
+    """CPU oracle (test infrastructure) on the trajectories `idx` of workload wl."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    from odegb300.saveat import resolve_saveat
+    alg = {"tsit5": O.TSIT5, "vern7": O.VERN7, "rodas5p": O.RODAS5P}[wl["alg"]]
+    model = {"lorenz": O.LORENZ, "robertson": O.ROBERTSON, "duffing_chain": O.DUFFING,
+             "brusselator_1d": O.BRUSSELATOR}[wl["model"]]
+    ts = wl["tspan"][:, idx]
+    sv = wl["saveat"]
+    if isinstance(sv, np.ndarray) and sv.ndim == 2:
+        sv = sv[:, idx]
+    spec = resolve_saveat(sv, ts)
+    npt = wl.get("n_per_traj")
+    return O.solve_ensemble(alg, model, wl["u0"][:, idx], wl["p"][:, idx], ts, spec.values, wl["reltol"],
+                            wl["abstol"], n_per_traj=None if npt is None else npt[idx],
+                            saveat_per_traj=spec.per_traj, save_start=spec.save_start, save_end=spec.save_end,
+                            save_end_user=spec.save_end_user, saveat_given=spec.nsave > 0,
+                            saveat_scalar=spec.scalar, nthreads=nthreads)
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons, power = [], None, set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for k, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(k)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+def compare_err(g_u, o, reltol, abstol):
+    """Per-trajectory worst save error in units of the tolerance (reltol*|u| + abstol):
+    max, p99 and median over the checked trajectories."""
+    ns = int(o["nsaved"].max())
+    ou = o["u"][:ns]
+    gu = g_u[:ns]
+    mask = ~np.isnan(ou)
+    r = np.where(mask, np.abs(gu - ou) / (reltol * np.abs(ou) + abstol), 0.0)
+    per = r.max(axis=(0, 1))
+    return {"max": float(per.max()), "p99": float(np.percentile(per, 99)), "median": float(np.median(per))}
+
+
+def run_gb300(args, world, rank, local, dist):
+    import torch
+    import odegb300
+    from odegb300 import _lib, workloads as W
+    from odegb300.ensemble import get_handle, _options, ALG_BY_NAME
+    from odegb300.saveat import resolve_saveat
+
+    torch.cuda.set_device(local)
+    L = _lib.load()
+    h = get_handle(local)
+    desc_name, N0 = CONFIGS[args.config]
+    N = args.trajectories or N0
+    wl = workload(args.config, N, seed=42 + rank)
+    alg = ALG_BY_NAME[wl["alg"]]
+    model = odegb300.ensemble.MODELS[wl["model"]]
+    dev = torch.device("cuda", local)
+    n, _ = wl["u0"].shape
+    sv = resolve_saveat(wl["saveat"], wl["tspan"])
+    cap = sv.nsave + 2
+    npt = wl.get("n_per_traj")
+    t_u0 = torch.from_numpy(np.ascontiguousarray(wl["u0"])).to(dev)
+    t_p = torch.from_numpy(np.ascontiguousarray(wl["p"])).to(dev)
+    t_ts = torch.from_numpy(np.ascontiguousarray(wl["tspan"])).to(dev)
+    t_sv = torch.from_numpy(np.ascontiguousarray(sv.values if sv.nsave else np.zeros(1))).to(dev)
+    t_npt = torch.from_numpy(npt).to(dev) if npt is not None else None
+    t_out = torch.empty((cap, N), dtype=torch.float64, device=dev)
+    u_out = torch.empty((cap, n, N), dtype=torch.float64, device=dev)
+    ns_out = torch.empty(N, dtype=torch.int32, device=dev)
+    rc_out = torch.empty(N, dtype=torch.int32, device=dev)
+    st_out = torch.empty((N, 6), dtype=torch.int64, device=dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
+    # every launch, flush and event goes on one explicit stream (a null stream
+    # pointer would make the library fall back to its own stream)
+    work = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(work)
+    ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None
+
+    def solve_device(prec):
+        ens = odegb300.EnsembleGB300(precision=prec)
+        o = _options(wl["reltol"], wl["abstol"], None, None, None, 1000000, sv, ens, None, None)
+        d = _lib.ProblemDesc(model, alg.alg_id, n, wl["p"].shape[0], ens.prec_id(), 0)
+        stream = C.c_void_p(work.cuda_stream)
+        _lib.check(L.ode_solve_ensemble_device(h, C.byref(d), C.byref(o), N, ptr(t_npt), ptr(t_u0), ptr(t_p),
+                                               ptr(t_ts), ptr(t_sv), ptr(t_out), ptr(u_out), ptr(ns_out),
+                                               ptr(rc_out), ptr(st_out), stream), h)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    def launches():
+        v = C.c_int64(0)
+        L.ode_kernel_launches(h, C.byref(v))
+        return v.value
+
+    if args.profile_small:
+        for prec in ("fp64", "mixed"):
+            solve_device(prec)
+        torch.cuda.synchronize(dev)
+        print(json.dumps({"profile_small": True, "trajectories": N}))
+        return
+
+    # Accuracy sample against the CPU oracle (rank 0 only)
+    sample = np.arange(min(N, 256))
+    results = {}
+    clocks = Clocks(local)
+    for prec in ("fp64", "mixed"):
+        for _ in range(args.warmup):
+            flush.fill_(1.0)
+            solve_device(prec)
+        barrier()
+        if prec == "mixed":
+            clocks.start()
+        l0 = launches()
+        times = []
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        t_wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0.record()
+            solve_device(prec)
+            e1.record()
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        barrier()
+        wall = time.perf_counter() - t_wall0
+        if prec == "mixed":
+            clk = clocks.stop()
+        nl = launches() - l0
+        ms = float(np.mean(times))
+        if dist is not None:
+            tt = torch.tensor([ms], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            ms = float(tt.item())
+        st = st_out.cpu().numpy()
+        rc = rc_out.cpu().numpy()
+        attempts = int(st[:, 4].sum() + st[:, 5].sum())
+        results[prec] = {"ms": ms, "times": times, "launches": nl, "attempts": attempts,
+                         "success": float((rc == 1).mean()), "u": u_out[:, :, sample].cpu().numpy(),
+                         "naccept_mean": float(st[:, 4].mean()), "wall_s": wall}
+
+    acc = {}
+    o = None
+    if rank == 0:
+        o = oracle_solve(wl, sample)
+        for prec in ("fp64", "mixed"):
+            acc[prec] = compare_err(results[prec]["u"], o, wl["reltol"], wl["abstol"])
+    best = "mixed" if acc.get("mixed", {"max": 1e9})["max"] <= 10.0 else "fp64"
+    R = results[best]
+    value = world * N / (R["ms"] * 1e-3)
+
+    # roofline of the dominant kernel (the chosen form's integrator kernel)
+    peak = C.c_double(0)
+    L.ode_measure_fma_peak(local, 0 if best == "fp64" else 1, C.byref(peak))
+    nmean = float(np.mean(npt)) if npt is not None else n
+    fl = W.attempt_flops(wl["alg"], wl["model"], int(round(nmean)))
+    nsaves = sv.nsave if sv.nsave else 2
+    total_flops = R["attempts"] * fl + N * nsaves * W.save_flops(wl["alg"], wl["model"], int(round(nmean)))
+    achieved = total_flops / (R["ms"] * 1e-3)
+    fp64_peak = C.c_double(0)
+    L.ode_measure_fma_peak(local, 0, C.byref(fp64_peak))
+
+    # end-to-end through the public host-buffer call
+    from odegb300.ensemble import solve_arrays
+    ens = odegb300.EnsembleGB300(precision=best)
+    kw = dict(n_per_traj=npt) if npt is not None else {}
+    for _ in range(max(1, min(args.warmup, 2))):
+        solve_arrays(wl["model"], alg, ens, wl["u0"], wl["p"], wl["tspan"], wl["saveat"], wl["reltol"],
+                     wl["abstol"], **kw)
+    e2e_t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        solve_arrays(wl["model"], alg, ens, wl["u0"], wl["p"], wl["tspan"], wl["saveat"], wl["reltol"],
+                     wl["abstol"], **kw)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = float(np.mean(e2e_t))
+    h2d = wl["u0"].nbytes + wl["p"].nbytes + wl["tspan"].nbytes + (sv.values.nbytes if sv.nsave else 0) + \
+        (npt.nbytes if npt is not None else 0)
+    d2h = cap * N * 8 + cap * n * N * 8 + N * 8 + N * 48
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(wl, N, args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": "trajectories/sec at equal accuracy, mixed vs plain FP64 GPU; p50/p99 latency",
+            "value": value, "unit": "trajectories/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": R["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if best == "fp64" else "f32 stages + f64 t/dt/error norm",
+            "data": "synthetic (seeded, config distributions)",
+            "config": {"workload": desc_name, "trajectories": N, "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "256 MB buffer written between timed steps", "precision_chosen": best},
+            "forms": {p: {"trajectories_per_s": world * N / (results[p]["ms"] * 1e-3), "ms": results[p]["ms"],
+                          "err_vs_fp64_oracle_x_tol": acc.get(p), "success_frac": results[p]["success"],
+                          "mean_accepted_steps": results[p]["naccept_mean"]} for p in results},
+            "speedup_mixed_vs_fp64": results["fp64"]["ms"] / results["mixed"]["ms"],
+            "e2e": {"value": world * N / e2e_s, "unit": "trajectories/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "roofline": {"bound": "fp64 pipe" if best == "fp64" else "fp32 pipe", "achieved": achieved / 1e12,
+                         "peak": peak.value / 1e12, "unit": "TFLOP/s", "frac": achieved / peak.value if peak.value else None,
+                         "traffic": None, "flops_per_attempt": fl, "attempted_steps": R["attempts"],
+                         "peak_source": "ode_measure_fma_peak (FMA-chain kernel, this GPU)",
+                         "fp64_peak_tflops": fp64_peak.value / 1e12},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": R["launches"],
+        }
+        print(json.dumps(line))
+
+
+def cpu_baseline(wl, N, target_s):
+    """CPU restatement of the reference (the oracle), all host threads, bounded sample."""
+    ncores = os.cpu_count() or 1
+    k = min(N, 2048)
+    t0 = time.perf_counter()
+    oracle_solve(wl, np.arange(k), nthreads=ncores)
+    t1 = time.perf_counter() - t0
+    m = int(min(N, max(k, k * target_s / max(t1, 1e-3))))
+    if m > k:
+        t0 = time.perf_counter()
+        oracle_solve(wl, np.arange(m), nthreads=ncores)
+        t1 = time.perf_counter() - t0
+        k = m
+    return {"value": k / t1, "unit": "trajectories/s", "cores": ncores, "kind": "port",
+            "sample": "%d of %d trajectories of the same workload, oracle with %d threads (%.1f s)" % (k, N, ncores, t1)}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    desc_name, N0 = CONFIGS[args.config]
+    N = args.trajectories or N0
+    wl = workload(args.config, N, seed=42)
+    ncores = os.cpu_count() or 1
+    k = min(N, 2048)
+    t0 = time.perf_counter()
+    oracle_solve(wl, np.arange(k), nthreads=ncores)
+    t1 = time.perf_counter() - t0
+    per_step_target = 20.0 / max(1, args.steps + args.warmup)
+    m = int(min(N, max(256, k * per_step_target / max(t1, 1e-3))))
+    for _ in range(args.warmup):
+        oracle_solve(wl, np.arange(m), nthreads=ncores)
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle_solve(wl, np.arange(m), nthreads=ncores)
+        ts.append(time.perf_counter() - t0)
+    v = m / float(np.mean(ts))
+    sample = "%d of %d trajectories per step, CPU restatement of the reference (Julia is not installed), %d threads" % (
+        m, N, ncores)
+    print(json.dumps({
+        "impl": "reference", "metric": "trajectories/sec at equal accuracy, mixed vs plain FP64 GPU; p50/p99 latency",
+        "value": v, "unit": "trajectories/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": float(np.mean(ts)) * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded, config distributions)",
+        "config": {"workload": desc_name, "trajectories": N},
+        "cpu_baseline": {"value": v, "unit": "trajectories/s", "cores": ncores, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "trajectories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
+def main():
+    args = parse()
+    world, rank, local, dist = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gb300(args, world, rank, local, dist)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

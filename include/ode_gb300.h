@@ -174,6 +174,11 @@ int ode_last_kernel_ms(const ode_handle* h, double* ms);
  * trajectory, for tuning and diagnostics.  Returns the count written. */
 int ode_query_variants(int alg, int model, int precision, int n, int32_t* lanes, int32_t cap);
 
+/* Measured FMA throughput (FLOP/s, 2 per FMA) of the FP64 (precision =
+ * ODE_PREC_FP64) or FP32 (ODE_PREC_MIXED) pipe of `device`: the roofline
+ * denominator for the integrator kernels, which are bound by that pipe. */
+int ode_measure_fma_peak(int device, int precision, double* flops_per_s);
+
 #ifdef __cplusplus
 }
 #endif

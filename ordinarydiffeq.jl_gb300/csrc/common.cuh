@@ -98,6 +98,87 @@ __device__ __forceinline__ double ctrl_pow(double x, double y) {
     return series_exp(y * series_ln(x));
 }
 
+// ------------------------------------------------------------------ solution accumulator
+// The state u is carried as a pair (hi, lo).  In FP64 mode lo is always zero
+// and every formula reduces to the reference's single-rounding expression.
+// In the mixed mode (R = float) the pair is a compensated FP32 sum
+// (hi + lo, about 48 significant bits, Dekker/Knuth two-sum): stage values and
+// increments are FP32, but the running solution does not lose a float ulp per
+// step, which at reltol 1e-6 would otherwise dominate the error.  On GB300 a
+// two-sum costs a handful of FP32 instructions where an FP64 add runs on a
+// far slower pipe.
+template <class R> struct Acc;
+template <> struct Acc<double> {
+    // stage input uprev + d*S (reference: muladd(d, S, uprev))
+    static __device__ __forceinline__ double stage(double d, double S, double up, double) { return fma(d, S, up); }
+    // new solution u = uprev + d*S
+    static __device__ __forceinline__ void update(double& hi, double& lo, double d, double S, double up, double) {
+        hi = fma(d, S, up);
+        lo = 0.0;
+    }
+    // u = uprev + inc where inc was accumulated starting from uprev already
+    static __device__ __forceinline__ void set(double& hi, double& lo, double v) { hi = v; lo = 0.0; }
+    static __device__ __forceinline__ void set_pair(double& hi, double& lo, double v) { hi = v; lo = 0.0; }
+    static __device__ __forceinline__ void split(double x, double& hi, double& lo) { hi = x; lo = 0.0; }
+    static __device__ __forceinline__ double join(double hi, double) { return hi; }
+};
+template <> struct Acc<float> {
+    static __device__ __forceinline__ float stage(float d, float S, float up, float uplo) {
+        return fmaf(d, S, up) + uplo;
+    }
+    static __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+        s = a + b;
+        float bb = s - a;
+        e = (a - (s - bb)) + (b - bb);
+    }
+    static __device__ __forceinline__ void update(float& hi, float& lo, float d, float S, float up, float uplo) {
+        float inc = d * S + uplo;
+        two_sum(up, inc, hi, lo);
+    }
+    static __device__ __forceinline__ void set(float& hi, float& lo, float v) { hi = v; lo = 0.0f; }
+    static __device__ __forceinline__ void split(double x, float& hi, float& lo) {
+        hi = (float)x;
+        lo = (float)(x - (double)hi);
+    }
+    static __device__ __forceinline__ double join(float hi, float lo) { return (double)hi + (double)lo; }
+};
+
+// ------------------------------------------------------------------ double-float
+// An unevaluated sum hi + lo of two floats (about 48 significant bits),
+// evaluated with error-free transformations on the FP32 pipe (Dekker 1971;
+// Joldes, Muller, Popescu 2017, "Tight and rigorous error bounds for basic
+// building blocks of double-word arithmetic", algorithms 1-4 and 10-12).  The
+// mixed Rosenbrock path evaluates stiff right-hand sides in it: their terms
+// cancel (ROBER's k1 y1 - k2 y2^2 - k3 y2 y3), and FP32 arithmetic there alone
+// leaves ~70x reltol of error at reltol 1e-6.
+struct ff {
+    float hi, lo;
+    __device__ __forceinline__ ff() : hi(0.0f), lo(0.0f) {}
+    __device__ __forceinline__ ff(float h) : hi(h), lo(0.0f) {}
+    __device__ __forceinline__ ff(int h) : hi((float)h), lo(0.0f) {}
+    __device__ __forceinline__ ff(float h, float l) : hi(h), lo(l) {}
+    __device__ __forceinline__ explicit ff(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
+    __device__ __forceinline__ float f() const { return hi + lo; }
+};
+__device__ __forceinline__ ff ff_fast2sum(float a, float b) {
+    float s = a + b;
+    return ff(s, b - (s - a));
+}
+__device__ __forceinline__ ff operator+(ff a, ff b) {
+    float s = a.hi + b.hi;
+    float bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b.hi - bb);
+    return ff_fast2sum(s, e + (a.lo + b.lo));
+}
+__device__ __forceinline__ ff operator-(ff a) { return ff(-a.hi, -a.lo); }
+__device__ __forceinline__ ff operator-(ff a, ff b) { return a + (-b); }
+__device__ __forceinline__ ff operator*(ff a, ff b) {
+    float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+    return ff_fast2sum(p, e);
+}
+
 // ------------------------------------------------------------------ lane groups
 // A trajectory is owned by a group of L consecutive lanes of one warp; each
 // lane holds C state components (component index = lane_in_group*C + c).
@@ -122,6 +203,10 @@ template <int L> struct Group {
     template <class T> __device__ __forceinline__ T from(T v, int src_lane) const {
         if (L == 1) return v;
         return __shfl_sync(mask, v, src_lane, L);
+    }
+    __device__ __forceinline__ ff from(ff v, int src_lane) const {
+        if (L == 1) return v;
+        return ff(__shfl_sync(mask, v.hi, src_lane, L), __shfl_sync(mask, v.lo, src_lane, L));
     }
     __device__ __forceinline__ bool any(bool b) const {
         if (L == 1) return b;

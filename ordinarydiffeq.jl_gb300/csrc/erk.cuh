@@ -5,15 +5,29 @@
 //  Vern7: perform_step!(::Vern7Cache)  lib/OrdinaryDiffEqVerner/src/verner_rk_perform_step.jl:412-570
 //         (lazy: extra stages only when a save falls in the step, verner_addsteps.jl:80-195),
 //         interpolant lib/OrdinaryDiffEqVerner/src/interpolants.jl:183-252.
-// Stage sums use the reference's @muladd nesting: uprev + dt*(a1 k1 + ... + am km)
-// = fma(dt, fma(a1,k1, fma(a2,k2, ... am*km)), uprev).
+// Stage sums come from rksum.cuh: reference nesting in FP64, compensated sums
+// with split coefficients in the mixed mode.
 #pragma once
 #include "integrator.cuh"
-#include "tableaus.h"
+#include "rksum.cuh"
 
 namespace odegb {
 
-#define T_(x) ((R)(tab::x))
+#define HDC __host__ __device__ static constexpr
+struct Tsit5Sol { HDC int last() { return 6; } HDC double w(int j) { return tab::TSIT5_A(7, j); } HDC bool m(int j) { return j >= 1 && j <= 6; } };
+struct Tsit5Err { HDC int last() { return 7; } HDC double w(int j) { return tab::TSIT5_BT(j); } HDC bool m(int j) { return j >= 1 && j <= 7; } };
+struct Vern7Sol { HDC int last() { return 9; } HDC double w(int j) { return tab::VERN7_B(j); } HDC bool m(int j) { return tab::VERN7_BM(j); } };
+struct Vern7Err { HDC int last() { return 10; } HDC double w(int j) { return tab::VERN7_BT(j); } HDC bool m(int j) { return tab::VERN7_BTM(j); } };
+#undef HDC
+
+// Interpolation weights b_i(theta): Horner in FP64 (the reference's @evalpoly).
+template <int NPOLY, class RF>
+__device__ __forceinline__ double interp_weight(double th, int i, RF r, bool first) {
+    double acc = r(i, NPOLY - 1);
+#pragma unroll
+    for (int q = NPOLY - 2; q >= (first ? 1 : 2); --q) acc = fma(th, acc, r(i, q));
+    return first ? th * acc : (th * th) * acc;
+}
 
 struct Tsit5Alg {
     static constexpr int ORDER = 5;
@@ -26,7 +40,7 @@ struct Tsit5Alg {
 
     template <class Model, class R, int L, int C>
     __device__ static void initialize(Cache<R, C>& c, const R* u, const R* p, double t, const Group<L>& g,
-                                      StepStats& st, const EnsembleArgs&) {
+                                      StepStats& st, const EnsembleArgs&, long long) {
         Model::template rhs<R, L, C>(c.k[0], u, p, t, g);
         st.nf += 1;
     }
@@ -37,228 +51,155 @@ struct Tsit5Alg {
     template <class R, int C> __device__ static void after_save(Cache<R, C>&) {}
 
     template <class Model, class R, int L, int C>
-    __device__ static double step(Cache<R, C>& c, R* u, const R* up, const R* p, double t, double dt,
-                                  R abstol, R reltol, long long, double, const Group<L>& g, StepStats& st) {
+    __device__ static typename Ctl<R>::T step(Cache<R, C>& c, R* u, R* ulo, const R* up, const R* uplo,
+                                             const R* p, double t, double dt, R abstol, R reltol, long long, bool,
+                                             const Group<L>& g, StepStats& st) {
+        using K = RK<Tsit5Tab, R, C>;
         const R d = (R)dt;
-        R (*k)[C] = c.k;
         R* tmp = c.tmp;
-        const R a = d * T_(TSIT5_a21);
+        K::template stage<2>(tmp, c.k, d, up, uplo);
+        Model::template rhs<R, L, C>(c.k[1], tmp, p, fma(Tsit5Tab::c(2), dt, t), g);
+        K::template stage<3>(tmp, c.k, d, up, uplo);
+        Model::template rhs<R, L, C>(c.k[2], tmp, p, fma(Tsit5Tab::c(3), dt, t), g);
+        K::template stage<4>(tmp, c.k, d, up, uplo);
+        Model::template rhs<R, L, C>(c.k[3], tmp, p, fma(Tsit5Tab::c(4), dt, t), g);
+        K::template stage<5>(tmp, c.k, d, up, uplo);
+        Model::template rhs<R, L, C>(c.k[4], tmp, p, fma(Tsit5Tab::c(5), dt, t), g);
+        K::template stage<6>(tmp, c.k, d, up, uplo);
+        Model::template rhs<R, L, C>(c.k[5], tmp, p, t + dt, g);
+        K::weights(tmp, c.k, Tsit5Sol());
 #pragma unroll
-        for (int i = 0; i < C; ++i) tmp[i] = FMA(a, k[0][i], up[i]);
-        Model::template rhs<R, L, C>(k[1], tmp, p, fma(tab::TSIT5_c1, dt, t), g);
-#pragma unroll
-        for (int i = 0; i < C; ++i) tmp[i] = FMA(d, FMA(T_(TSIT5_a31), k[0][i], T_(TSIT5_a32) * k[1][i]), up[i]);
-        Model::template rhs<R, L, C>(k[2], tmp, p, fma(tab::TSIT5_c2, dt, t), g);
-#pragma unroll
-        for (int i = 0; i < C; ++i)
-            tmp[i] = FMA(d, FMA(T_(TSIT5_a41), k[0][i], FMA(T_(TSIT5_a42), k[1][i], T_(TSIT5_a43) * k[2][i])), up[i]);
-        Model::template rhs<R, L, C>(k[3], tmp, p, fma(tab::TSIT5_c3, dt, t), g);
-#pragma unroll
-        for (int i = 0; i < C; ++i)
-            tmp[i] = FMA(d, FMA(T_(TSIT5_a51), k[0][i], FMA(T_(TSIT5_a52), k[1][i],
-                          FMA(T_(TSIT5_a53), k[2][i], T_(TSIT5_a54) * k[3][i]))), up[i]);
-        Model::template rhs<R, L, C>(k[4], tmp, p, fma(tab::TSIT5_c4, dt, t), g);
-#pragma unroll
-        for (int i = 0; i < C; ++i)
-            tmp[i] = FMA(d, FMA(T_(TSIT5_a61), k[0][i], FMA(T_(TSIT5_a62), k[1][i], FMA(T_(TSIT5_a63), k[2][i],
-                          FMA(T_(TSIT5_a64), k[3][i], T_(TSIT5_a65) * k[4][i])))), up[i]);
-        Model::template rhs<R, L, C>(k[5], tmp, p, t + dt, g);
-#pragma unroll
-        for (int i = 0; i < C; ++i)
-            u[i] = FMA(d, FMA(T_(TSIT5_a71), k[0][i], FMA(T_(TSIT5_a72), k[1][i], FMA(T_(TSIT5_a73), k[2][i],
-                       FMA(T_(TSIT5_a74), k[3][i], FMA(T_(TSIT5_a75), k[4][i], T_(TSIT5_a76) * k[5][i]))))), up[i]);
-        Model::template rhs<R, L, C>(k[6], u, p, t + dt, g);
+        for (int i = 0; i < C; ++i) Acc<R>::update(u[i], ulo[i], d, tmp[i], up[i], uplo[i]);
+        Model::template rhs<R, L, C>(c.k[6], u, p, t + dt, g);
         st.nf += 6;
+        K::weights(tmp, c.k, Tsit5Err());
 #pragma unroll
-        for (int i = 0; i < C; ++i)
-            tmp[i] = d * FMA(T_(TSIT5_btilde1), k[0][i], FMA(T_(TSIT5_btilde2), k[1][i], FMA(T_(TSIT5_btilde3), k[2][i],
-                         FMA(T_(TSIT5_btilde4), k[3][i], FMA(T_(TSIT5_btilde5), k[4][i],
-                         FMA(T_(TSIT5_btilde6), k[5][i], T_(TSIT5_btilde7) * k[6][i]))))));
+        for (int i = 0; i < C; ++i) tmp[i] = d * tmp[i];
         return error_norm<R, L, C>(tmp, up, u, abstol, reltol, g);
     }
 
     template <class Model, class R, int L, int C>
-    __device__ static void interpolate(Cache<R, C>& c, R* out, double thd, double dt, double, const R* y0, const R*,
-                                       const R*, const Group<L>&) {
-        const R th = (R)thd, th2 = th * th, d = (R)dt;
-        const R b1 = th * FMA(th, FMA(th, FMA(th, T_(TSIT5I_r14), T_(TSIT5I_r13)), T_(TSIT5I_r12)), T_(TSIT5I_r11));
-        const R b2 = th2 * FMA(th, FMA(th, T_(TSIT5I_r24), T_(TSIT5I_r23)), T_(TSIT5I_r22));
-        const R b3 = th2 * FMA(th, FMA(th, T_(TSIT5I_r34), T_(TSIT5I_r33)), T_(TSIT5I_r32));
-        const R b4 = th2 * FMA(th, FMA(th, T_(TSIT5I_r44), T_(TSIT5I_r43)), T_(TSIT5I_r42));
-        const R b5 = th2 * FMA(th, FMA(th, T_(TSIT5I_r54), T_(TSIT5I_r53)), T_(TSIT5I_r52));
-        const R b6 = th2 * FMA(th, FMA(th, T_(TSIT5I_r64), T_(TSIT5I_r63)), T_(TSIT5I_r62));
-        const R b7 = th2 * FMA(th, FMA(th, T_(TSIT5I_r74), T_(TSIT5I_r73)), T_(TSIT5I_r72));
-        R (*k)[C] = c.k;
+    __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, double th, double dt, double, const R* y0,
+                                       const R* y0lo, const R*, const R*, const R*, const Group<L>&) {
+        auto r = [](int i, int q) { return tab::TSIT5_R(i, q); };
+        double b[8];
+        b[1] = interp_weight<5>(th, 1, r, true);
 #pragma unroll
-        for (int i = 0; i < C; ++i)
-            out[i] = FMA(d, FMA(k[0][i], b1, FMA(k[1][i], b2, FMA(k[2][i], b3, FMA(k[3][i], b4,
-                          FMA(k[4][i], b5, FMA(k[5][i], b6, k[6][i] * b7)))))), y0[i]);
+        for (int i = 2; i <= 7; ++i) b[i] = interp_weight<5>(th, i, r, false);
+        const R d = (R)dt;
+#pragma unroll
+        for (int i = 0; i < C; ++i) {
+            R S;
+            if (sizeof(R) == 8) {
+                R acc = c.k[6][i] * (R)b[7];
+#pragma unroll
+                for (int s = 6; s >= 1; --s) acc = FMA(c.k[s - 1][i], (R)b[s], acc);
+                S = acc;
+            } else {
+                CSum cs;
+#pragma unroll
+                for (int s = 1; s <= 7; ++s) cs.add(b[s], (float)c.k[s - 1][i]);
+                S = (R)cs.value();
+            }
+            Acc<R>::update(out[i], outlo[i], d, S, y0[i], y0lo[i]);
+        }
     }
 };
 
 struct Vern7Alg {
     static constexpr int ORDER = 7;
     static constexpr bool IMPLICIT = false;
-    // Slots: k1..k10 in s[0..9]; on a save step the extra stages k11..k16 are
-    // computed into s[1], s[2], s[9] (k2, k3, k10 are not used by the
-    // interpolant or the extra stages) and s[10..12].
     template <class R, int C> struct Cache {
-        R s[13][C];
+        R s[13][C];   // slots, see Vern7Tab::slot
         R tmp[C];
         bool extra;
     };
     template <class R, int C> __device__ static R* fsal_slot(Cache<R, C>& c) { return c.tmp; }
     template <class Model, class R, int L, int C>
     __device__ static void initialize(Cache<R, C>& c, const R*, const R*, double, const Group<L>&, StepStats&,
-                                      const EnsembleArgs&) {
+                                      const EnsembleArgs&, long long) {
         c.extra = false;
     }
     template <class R, int C> __device__ static void on_accept(Cache<R, C>&) {}
     template <class R, int C> __device__ static void after_save(Cache<R, C>& c) { c.extra = false; }
 
+    template <int ROW, class Model, class R, int L, int C>
+    __device__ static void eval_stage(Cache<R, C>& c, const R* up, const R* uplo, const R* p, double tstage, R d,
+                                      const Group<L>& g) {
+        RK<Vern7Tab, R, C>::template stage<ROW>(c.tmp, c.s, d, up, uplo);
+        Model::template rhs<R, L, C>(c.s[Vern7Tab::slot(ROW)], c.tmp, p, tstage, g);
+    }
+
     template <class Model, class R, int L, int C>
-    __device__ static double step(Cache<R, C>& c, R* u, const R* up, const R* p, double t, double dt,
-                                  R abstol, R reltol, long long, double, const Group<L>& g, StepStats& st) {
+    __device__ static typename Ctl<R>::T step(Cache<R, C>& c, R* u, R* ulo, const R* up, const R* uplo,
+                                             const R* p, double t, double dt, R abstol, R reltol, long long, bool,
+                                             const Group<L>& g, StepStats& st) {
         const R d = (R)dt;
-        R (*k)[C] = c.s;
-        R* tmp = c.tmp;
         c.extra = false;
-        Model::template rhs<R, L, C>(k[0], up, p, t, g);
-        const R a = d * T_(VERN7_a021);
+        Model::template rhs<R, L, C>(c.s[0], up, p, t, g);
+        eval_stage<2, Model>(c, up, uplo, p, fma(Vern7Tab::c(2), dt, t), d, g);
+        eval_stage<3, Model>(c, up, uplo, p, fma(Vern7Tab::c(3), dt, t), d, g);
+        eval_stage<4, Model>(c, up, uplo, p, fma(Vern7Tab::c(4), dt, t), d, g);
+        eval_stage<5, Model>(c, up, uplo, p, fma(Vern7Tab::c(5), dt, t), d, g);
+        eval_stage<6, Model>(c, up, uplo, p, fma(Vern7Tab::c(6), dt, t), d, g);
+        eval_stage<7, Model>(c, up, uplo, p, fma(Vern7Tab::c(7), dt, t), d, g);
+        eval_stage<8, Model>(c, up, uplo, p, fma(Vern7Tab::c(8), dt, t), d, g);
+        eval_stage<9, Model>(c, up, uplo, p, t + dt, d, g);
+        eval_stage<10, Model>(c, up, uplo, p, t + dt, d, g);
+        RK<Vern7Tab, R, C>::weights(c.tmp, c.s, Vern7Sol());
 #pragma unroll
-        for (int i = 0; i < C; ++i) tmp[i] = FMA(a, k[0][i], up[i]);
-        Model::template rhs<R, L, C>(k[1], tmp, p, fma(tab::VERN7_c2, dt, t), g);
-#pragma unroll
-        for (int i = 0; i < C; ++i) tmp[i] = FMA(d, FMA(T_(VERN7_a031), k[0][i], T_(VERN7_a032) * k[1][i]), up[i]);
-        Model::template rhs<R, L, C>(k[2], tmp, p, fma(tab::VERN7_c3, dt, t), g);
-#pragma unroll
-        for (int i = 0; i < C; ++i) tmp[i] = FMA(d, FMA(T_(VERN7_a041), k[0][i], T_(VERN7_a043) * k[2][i]), up[i]);
-        Model::template rhs<R, L, C>(k[3], tmp, p, fma(tab::VERN7_c4, dt, t), g);
-#pragma unroll
-        for (int i = 0; i < C; ++i)
-            tmp[i] = FMA(d, FMA(T_(VERN7_a051), k[0][i], FMA(T_(VERN7_a053), k[2][i], T_(VERN7_a054) * k[3][i])), up[i]);
-        Model::template rhs<R, L, C>(k[4], tmp, p, fma(tab::VERN7_c5, dt, t), g);
-#pragma unroll
-        for (int i = 0; i < C; ++i)
-            tmp[i] = FMA(d, FMA(T_(VERN7_a061), k[0][i], FMA(T_(VERN7_a063), k[2][i], FMA(T_(VERN7_a064), k[3][i],
-                          T_(VERN7_a065) * k[4][i]))), up[i]);
-        Model::template rhs<R, L, C>(k[5], tmp, p, fma(tab::VERN7_c6, dt, t), g);
-#pragma unroll
-        for (int i = 0; i < C; ++i)
-            tmp[i] = FMA(d, FMA(T_(VERN7_a071), k[0][i], FMA(T_(VERN7_a073), k[2][i], FMA(T_(VERN7_a074), k[3][i],
-                          FMA(T_(VERN7_a075), k[4][i], T_(VERN7_a076) * k[5][i])))), up[i]);
-        Model::template rhs<R, L, C>(k[6], tmp, p, fma(tab::VERN7_c7, dt, t), g);
-#pragma unroll
-        for (int i = 0; i < C; ++i)
-            tmp[i] = FMA(d, FMA(T_(VERN7_a081), k[0][i], FMA(T_(VERN7_a083), k[2][i], FMA(T_(VERN7_a084), k[3][i],
-                          FMA(T_(VERN7_a085), k[4][i], FMA(T_(VERN7_a086), k[5][i], T_(VERN7_a087) * k[6][i]))))), up[i]);
-        Model::template rhs<R, L, C>(k[7], tmp, p, fma(tab::VERN7_c8, dt, t), g);
-#pragma unroll
-        for (int i = 0; i < C; ++i)
-            tmp[i] = FMA(d, FMA(T_(VERN7_a091), k[0][i], FMA(T_(VERN7_a093), k[2][i], FMA(T_(VERN7_a094), k[3][i],
-                          FMA(T_(VERN7_a095), k[4][i], FMA(T_(VERN7_a096), k[5][i], FMA(T_(VERN7_a097), k[6][i],
-                          T_(VERN7_a098) * k[7][i])))))), up[i]);
-        Model::template rhs<R, L, C>(k[8], tmp, p, t + dt, g);
-#pragma unroll
-        for (int i = 0; i < C; ++i)
-            tmp[i] = FMA(d, FMA(T_(VERN7_a101), k[0][i], FMA(T_(VERN7_a103), k[2][i], FMA(T_(VERN7_a104), k[3][i],
-                          FMA(T_(VERN7_a105), k[4][i], FMA(T_(VERN7_a106), k[5][i], T_(VERN7_a107) * k[6][i]))))), up[i]);
-        Model::template rhs<R, L, C>(k[9], tmp, p, t + dt, g);
-#pragma unroll
-        for (int i = 0; i < C; ++i)
-            u[i] = FMA(d, FMA(T_(VERN7_b1), k[0][i], FMA(T_(VERN7_b4), k[3][i], FMA(T_(VERN7_b5), k[4][i],
-                       FMA(T_(VERN7_b6), k[5][i], FMA(T_(VERN7_b7), k[6][i], FMA(T_(VERN7_b8), k[7][i],
-                       T_(VERN7_b9) * k[8][i])))))), up[i]);
+        for (int i = 0; i < C; ++i) Acc<R>::update(u[i], ulo[i], d, c.tmp[i], up[i], uplo[i]);
         st.nf += 10;
+        RK<Vern7Tab, R, C>::weights(c.tmp, c.s, Vern7Err());
 #pragma unroll
-        for (int i = 0; i < C; ++i)
-            tmp[i] = d * FMA(T_(VERN7_btilde1), k[0][i], FMA(T_(VERN7_btilde4), k[3][i], FMA(T_(VERN7_btilde5), k[4][i],
-                         FMA(T_(VERN7_btilde6), k[5][i], FMA(T_(VERN7_btilde7), k[6][i], FMA(T_(VERN7_btilde8), k[7][i],
-                         FMA(T_(VERN7_btilde9), k[8][i], T_(VERN7_btilde10) * k[9][i])))))));
-        return error_norm<R, L, C>(tmp, up, u, abstol, reltol, g);
+        for (int i = 0; i < C; ++i) c.tmp[i] = d * c.tmp[i];
+        return error_norm<R, L, C>(c.tmp, up, u, abstol, reltol, g);
     }
 
     // Extra stages k11..k16 (verner_addsteps.jl:80-195) at (tprev, uprev, dt).
     template <class Model, class R, int L, int C>
-    __device__ static void extra_stages(Cache<R, C>& c, double tprev, double dt, const R* up, const R* p,
-                                        const Group<L>& g) {
+    __device__ static void extra_stages(Cache<R, C>& c, double tprev, double dt, const R* up, const R* uplo,
+                                        const R* p, const Group<L>& g) {
         const R d = (R)dt;
-        R (*k)[C] = c.s;
-        R* tmp = c.tmp;
-        // k11 -> s[1]
-#pragma unroll
-        for (int i = 0; i < C; ++i)
-            tmp[i] = FMA(d, FMA(T_(VERN7X_a1101), k[0][i], FMA(T_(VERN7X_a1104), k[3][i], FMA(T_(VERN7X_a1105), k[4][i],
-                          FMA(T_(VERN7X_a1106), k[5][i], FMA(T_(VERN7X_a1107), k[6][i], FMA(T_(VERN7X_a1108), k[7][i],
-                          T_(VERN7X_a1109) * k[8][i])))))), up[i]);
-        Model::template rhs<R, L, C>(k[1], tmp, p, fma(tab::VERN7X_c11, dt, tprev), g);
-        // k12 -> s[2]
-#pragma unroll
-        for (int i = 0; i < C; ++i)
-            tmp[i] = FMA(d, FMA(T_(VERN7X_a1201), k[0][i], FMA(T_(VERN7X_a1204), k[3][i], FMA(T_(VERN7X_a1205), k[4][i],
-                          FMA(T_(VERN7X_a1206), k[5][i], FMA(T_(VERN7X_a1207), k[6][i], FMA(T_(VERN7X_a1208), k[7][i],
-                          FMA(T_(VERN7X_a1209), k[8][i], T_(VERN7X_a1211) * k[1][i]))))))), up[i]);
-        Model::template rhs<R, L, C>(k[2], tmp, p, fma(tab::VERN7X_c12, dt, tprev), g);
-        // k13 -> s[9]
-#pragma unroll
-        for (int i = 0; i < C; ++i)
-            tmp[i] = FMA(d, FMA(T_(VERN7X_a1301), k[0][i], FMA(T_(VERN7X_a1304), k[3][i], FMA(T_(VERN7X_a1305), k[4][i],
-                          FMA(T_(VERN7X_a1306), k[5][i], FMA(T_(VERN7X_a1307), k[6][i], FMA(T_(VERN7X_a1308), k[7][i],
-                          FMA(T_(VERN7X_a1309), k[8][i], FMA(T_(VERN7X_a1311), k[1][i], T_(VERN7X_a1312) * k[2][i])))))))), up[i]);
-        Model::template rhs<R, L, C>(k[9], tmp, p, fma(tab::VERN7X_c13, dt, tprev), g);
-        // k14 -> s[10]
-#pragma unroll
-        for (int i = 0; i < C; ++i)
-            tmp[i] = FMA(d, FMA(T_(VERN7X_a1401), k[0][i], FMA(T_(VERN7X_a1404), k[3][i], FMA(T_(VERN7X_a1405), k[4][i],
-                          FMA(T_(VERN7X_a1406), k[5][i], FMA(T_(VERN7X_a1407), k[6][i], FMA(T_(VERN7X_a1408), k[7][i],
-                          FMA(T_(VERN7X_a1409), k[8][i], FMA(T_(VERN7X_a1411), k[1][i], FMA(T_(VERN7X_a1412), k[2][i],
-                          T_(VERN7X_a1413) * k[9][i]))))))))), up[i]);
-        Model::template rhs<R, L, C>(k[10], tmp, p, fma(tab::VERN7X_c14, dt, tprev), g);
-        // k15 -> s[11]
-#pragma unroll
-        for (int i = 0; i < C; ++i)
-            tmp[i] = FMA(d, FMA(T_(VERN7X_a1501), k[0][i], FMA(T_(VERN7X_a1504), k[3][i], FMA(T_(VERN7X_a1505), k[4][i],
-                          FMA(T_(VERN7X_a1506), k[5][i], FMA(T_(VERN7X_a1507), k[6][i], FMA(T_(VERN7X_a1508), k[7][i],
-                          FMA(T_(VERN7X_a1509), k[8][i], FMA(T_(VERN7X_a1511), k[1][i], FMA(T_(VERN7X_a1512), k[2][i],
-                          T_(VERN7X_a1513) * k[9][i]))))))))), up[i]);
-        Model::template rhs<R, L, C>(k[11], tmp, p, fma(tab::VERN7X_c15, dt, tprev), g);
-        // k16 -> s[12]
-#pragma unroll
-        for (int i = 0; i < C; ++i)
-            tmp[i] = FMA(d, FMA(T_(VERN7X_a1601), k[0][i], FMA(T_(VERN7X_a1604), k[3][i], FMA(T_(VERN7X_a1605), k[4][i],
-                          FMA(T_(VERN7X_a1606), k[5][i], FMA(T_(VERN7X_a1607), k[6][i], FMA(T_(VERN7X_a1608), k[7][i],
-                          FMA(T_(VERN7X_a1609), k[8][i], FMA(T_(VERN7X_a1611), k[1][i], FMA(T_(VERN7X_a1612), k[2][i],
-                          T_(VERN7X_a1613) * k[9][i]))))))))), up[i]);
-        Model::template rhs<R, L, C>(k[12], tmp, p, fma(tab::VERN7X_c16, dt, tprev), g);
+        eval_stage<11, Model>(c, up, uplo, p, fma(Vern7Tab::c(11), dt, tprev), d, g);
+        eval_stage<12, Model>(c, up, uplo, p, fma(Vern7Tab::c(12), dt, tprev), d, g);
+        eval_stage<13, Model>(c, up, uplo, p, fma(Vern7Tab::c(13), dt, tprev), d, g);
+        eval_stage<14, Model>(c, up, uplo, p, fma(Vern7Tab::c(14), dt, tprev), d, g);
+        eval_stage<15, Model>(c, up, uplo, p, fma(Vern7Tab::c(15), dt, tprev), d, g);
+        eval_stage<16, Model>(c, up, uplo, p, fma(Vern7Tab::c(16), dt, tprev), d, g);
         c.extra = true;
     }
 
-    template <class R>
-    __device__ static R poly6(R th, R r2, R r3, R r4, R r5, R r6, R r7) {
-        return FMA(th, FMA(th, FMA(th, FMA(th, FMA(th, r7, r6), r5), r4), r3), r2);
-    }
-
     template <class Model, class R, int L, int C>
-    __device__ static void interpolate(Cache<R, C>& c, R* out, double thd, double dt, double tprev, const R* y0,
-                                       const R*, const R* p, const Group<L>& g) {
-        if (!c.extra) extra_stages<Model, R, L, C>(c, tprev, dt, y0, p, g);
-        const R th = (R)thd, th2 = th * th, d = (R)dt;
-        const R b1 = th * FMA(th, poly6<R>(th, T_(VERN7I_r012), T_(VERN7I_r013), T_(VERN7I_r014), T_(VERN7I_r015),
-                                          T_(VERN7I_r016), T_(VERN7I_r017)), T_(VERN7I_r011));
-#define VB(S) th2 * poly6<R>(th, T_(VERN7I_r##S##2), T_(VERN7I_r##S##3), T_(VERN7I_r##S##4), T_(VERN7I_r##S##5), \
-                              T_(VERN7I_r##S##6), T_(VERN7I_r##S##7))
-        const R b4 = VB(04), b5 = VB(05), b6 = VB(06), b7 = VB(07), b8 = VB(08), b9 = VB(09);
-        const R b11 = VB(11), b12 = VB(12), b13 = VB(13), b14 = VB(14), b15 = VB(15), b16 = VB(16);
-#undef VB
-        R (*k)[C] = c.s;
+    __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, double th, double dt, double tprev,
+                                       const R* y0, const R* y0lo, const R*, const R*, const R* p,
+                                       const Group<L>& g) {
+        if (!c.extra) extra_stages<Model, R, L, C>(c, tprev, dt, y0, y0lo, p, g);
+        // stages of the 7th-order interpolant, in the reference's summation order
+        constexpr int idx[13] = {1, 4, 5, 6, 7, 8, 9, 11, 12, 13, 14, 15, 16};
+        auto r = [](int i, int q) { return tab::VERN7_R(i, q); };
+        double b[13];
+        b[0] = interp_weight<8>(th, 1, r, true);
 #pragma unroll
-        for (int i = 0; i < C; ++i)
-            out[i] = FMA(d, FMA(k[0][i], b1, FMA(k[3][i], b4, FMA(k[4][i], b5, FMA(k[5][i], b6, FMA(k[6][i], b7,
-                          FMA(k[7][i], b8, FMA(k[8][i], b9, FMA(k[1][i], b11, FMA(k[2][i], b12, FMA(k[9][i], b13,
-                          FMA(k[10][i], b14, FMA(k[11][i], b15, k[12][i] * b16)))))))))))), y0[i]);
+        for (int q = 1; q < 13; ++q) b[q] = interp_weight<8>(th, idx[q], r, false);
+        const R d = (R)dt;
+#pragma unroll
+        for (int i = 0; i < C; ++i) {
+            R S;
+            if (sizeof(R) == 8) {
+                R acc = c.s[Vern7Tab::slot(16)][i] * (R)b[12];
+#pragma unroll
+                for (int q = 11; q >= 0; --q) acc = FMA(c.s[Vern7Tab::slot(idx[q])][i], (R)b[q], acc);
+                S = acc;
+            } else {
+                CSum cs;
+#pragma unroll
+                for (int q = 0; q < 13; ++q) cs.add(b[q], (float)c.s[Vern7Tab::slot(idx[q])][i]);
+                S = (R)cs.value();
+            }
+            Acc<R>::update(out[i], outlo[i], d, S, y0[i], y0lo[i]);
+        }
     }
 };
-
-#undef T_
 
 }  // namespace odegb

@@ -121,6 +121,72 @@ def main():
     accessor("RODAS5P_c", c, two_d=False)
     accessor("RODAS5P_d", d, two_d=False)
     accessor("RODAS5P_H", H)
+
+    # Dense 1-based explicit-RK tables (rows = stages, zero where the reference
+    # has no term) with presence masks, for the generic stage loops.
+    def erk_tables(prefix, vals, extra, S, row_digits, c_of_stage):
+        A = [["0.0"] * (S + 1) for _ in range(S + 1)]
+        M = [[0] * (S + 1) for _ in range(S + 1)]
+        for k, v in list(vals.items()) + list(extra.items()):
+            m = re.fullmatch(r"a(\d{%d})(\d+)" % row_digits, k) if row_digits else None
+            if k.startswith("a") and len(k) == 5 and prefix == "VERN7":  # a1101 style (extra stages)
+                m = re.fullmatch(r"a(\d\d)(\d\d)", k)
+            if m:
+                i, j = int(m.group(1)), int(m.group(2))
+                A[i][j] = as_double(v)
+                M[i][j] = 1
+        cvec = ["0.0"] * (S + 1)
+        for i in range(2, S + 1):
+            cvec[i] = as_double(c_of_stage(i))
+        accessor(prefix + "_A", A)
+        lines.append("__host__ __device__ constexpr bool %s_AM(int i, int j) {" % prefix)
+        lines.append("    constexpr bool t[%d][%d] = {%s};" % (S + 1, S + 1, ", ".join("{" + ", ".join("true" if x else "false" for x in r) + "}" for r in M)))
+        lines.append("    return t[i][j];")
+        lines.append("}")
+        accessor(prefix + "_CS", cvec, two_d=False)
+
+    tv = dict(blocks[0][1])
+    # Tsit5: a<i><j> single digits, stage i at c_{i-1}; row 7 is the solution (FSAL)
+    erk_tables("TSIT5", tv, {}, 7, 1, lambda i: tv["c%d" % (i - 1)] if i <= 7 else "1")
+    bt = ["0.0"] * 8
+    for j in range(1, 8):
+        bt[j] = as_double(tv["btilde%d" % j])
+    accessor("TSIT5_BT", bt, two_d=False)
+    ti = dict(blocks[1][1])
+    R = [[as_double(ti.get("r%d%d" % (i, q), "0")) for q in range(5)] for i in range(8)]
+    accessor("TSIT5_R", R)
+    vv = dict(blocks[2][1])
+    vx = dict(blocks[3][1])
+    def vern_c(i):
+        if i <= 8:
+            return vv["c%d" % i]
+        if i <= 10:
+            return "1"
+        return vx["c%d" % i]
+    erk_tables("VERN7", vv, vx, 16, 2, vern_c)
+    b = ["0.0"] * 17
+    bm = [0] * 17
+    btl = ["0.0"] * 17
+    btm = [0] * 17
+    for k, v in vv.items():
+        m = re.fullmatch(r"b(\d+)", k)
+        if m:
+            b[int(m.group(1))] = as_double(v)
+            bm[int(m.group(1))] = 1
+        m = re.fullmatch(r"btilde(\d+)", k)
+        if m:
+            btl[int(m.group(1))] = as_double(v)
+            btm[int(m.group(1))] = 1
+    accessor("VERN7_B", b, two_d=False)
+    accessor("VERN7_BT", btl, two_d=False)
+    for name, mask in (("VERN7_BM", bm), ("VERN7_BTM", btm)):
+        lines.append("__host__ __device__ constexpr bool %s(int j) {" % name)
+        lines.append("    constexpr bool t[17] = {%s};" % ", ".join("true" if x else "false" for x in mask))
+        lines.append("    return t[j];")
+        lines.append("}")
+    vi = dict(blocks[4][1])
+    R7 = [[as_double(vi.get("r%02d%d" % (i, q), "0")) for q in range(8)] for i in range(17)]
+    accessor("VERN7_R", R7)
     lines.append("}  // namespace tab")
     lines.append("}  // namespace odegb")
     with open(out, "w") as fh:

@@ -17,9 +17,15 @@
 //   residual + norm            lib/DiffEqBase/src/calculate_residuals.jl:9-14, common_defaults.jl:69-75
 //   de_check_error             lib/DiffEqBase/src/check_error.jl:70-118
 //
-// Precision: t, dt, the error norm accumulator and the controller are always
-// FP64; the state and stage arithmetic use R (double, or float in the mixed
-// mode).  The only tstop is tf.
+// Precision policy.  t and dt are FP64 in both modes, and so is the error-
+// norm accumulator.  FP64 mode (R = double) evaluates the controller in FP64
+// like the reference.  Mixed mode (R = float) computes the controller's
+// powers and factors in FP32 and applies them to the FP64 dt with one
+// multiply: on GB300 an FP64 instruction occupies the FP64 pipe ~64x longer
+// than an FP32 one, so the per-step FP64 work is kept to t/dt updates and the
+// error accumulation.  min/max/eps of the (non-negative) time quantities run
+// on the integer pipe in both modes; they return exactly what Julia's
+// min/max/eps return, NaN propagation included.
 #pragma once
 #include "common.cuh"
 #include "ode_kernels.h"
@@ -33,7 +39,61 @@ struct StepStats {
     long long nf, njacs, nw, nsolve, naccept, nreject;
 };
 
-// Controller constants for one method (alg_utils.jl defaults).
+// ---------------------------------------------------------------- time helpers (integer pipe)
+__device__ __forceinline__ bool bits_nan(long long b) { return (b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL; }
+__device__ __forceinline__ double dnan() { return __longlong_as_double(0x7ff8000000000000LL); }
+// Julia min/max for non-negative doubles (NaN propagates).
+__device__ __forceinline__ double pmin(double a, double b) {
+    long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+    if (bits_nan(x) || bits_nan(y)) return dnan();
+    return x < y ? a : b;
+}
+__device__ __forceinline__ double pmax(double a, double b) {
+    long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+    if (bits_nan(x) || bits_nan(y)) return dnan();
+    return x > y ? a : b;
+}
+__device__ __forceinline__ double pabs(double a) {
+    return __longlong_as_double(__double_as_longlong(a) & 0x7fffffffffffffffLL);
+}
+// Julia eps(x): the spacing of doubles at |x|, built from the exponent bits.
+__device__ __forceinline__ double peps(double x) {
+    long long b = __double_as_longlong(x) & 0x7fffffffffffffffLL;
+    if (b >= 0x7ff0000000000000LL) return dnan();
+    int e = (int)(b >> 52);
+    if (e > 52) return __longlong_as_double((long long)(e - 52) << 52);
+    return __longlong_as_double(1LL << (e > 0 ? e - 1 : 0));
+}
+// a <= b and a < b for non-negative doubles (false when either is NaN, as in IEEE).
+__device__ __forceinline__ bool ple(double a, double b) {
+    long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+    return !bits_nan(x) && !bits_nan(y) && x <= y;
+}
+__device__ __forceinline__ bool plt(double a, double b) {
+    long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+    return !bits_nan(x) && !bits_nan(y) && x < y;
+}
+// 100 * eps(x), exactly: eps is a power of two 2^k and 100 * 2^k = 1.5625 * 2^(k+6).
+__device__ __forceinline__ double ptol100(double x) {
+    const double e = peps(x);
+    const int ex = (int)(__double_as_longlong(e) >> 52);
+    if (ex >= 1 && ex + 6 < 2047) return __longlong_as_double(((long long)(ex + 6) << 52) | 0x9000000000000LL);
+    return 100.0 * e;
+}
+
+// ---------------------------------------------------------------- controller policy
+template <class R> struct Ctl;
+template <> struct Ctl<double> {   // FP64: the reference's arithmetic
+    using T = double;
+    static __device__ __forceinline__ double pw(double x, double y) { return ctrl_pow(x, y); }
+    static __device__ __forceinline__ double scale_dt(double dt, double q) { return dt / q; }
+};
+template <> struct Ctl<float> {    // mixed: FP32 factors, FP64 dt
+    using T = float;
+    static __device__ __forceinline__ float pw(float x, float y) { return exp2f(y * log2f(x)); }
+    static __device__ __forceinline__ double scale_dt(double dt, float q) { return dt * (double)(1.0f / q); }
+};
+
 struct Ctrl {
     double beta1, beta2, qmin_inv, qmax, qmax_first, gamma, qsteady_max, qoldinit;
 };
@@ -52,11 +112,11 @@ __device__ __forceinline__ Ctrl make_ctrl(const EnsembleArgs& a) {
     return c;
 }
 
-// Residual norm sqrt(sum_i (ut_i / (abstol + max(|u0_i|,|u1_i|) reltol))^2 / n)
-// accumulated in FP64 (sequentially within a lane, then across the group).
+// Residual norm sqrt(sum_i (ut_i / (abstol + max(|u0_i|,|u1_i|) reltol))^2 / n),
+// the sum accumulated in FP64 (sequentially within a lane, then across the group).
 template <class R, int L, int C>
-__device__ __forceinline__ double error_norm(const R* ut, const R* u0, const R* u1, R abstol, R reltol,
-                                             const Group<L>& g) {
+__device__ __forceinline__ typename Ctl<R>::T error_norm(const R* ut, const R* u0, const R* u1, R abstol, R reltol,
+                                                         const Group<L>& g) {
     double acc = 0.0;
 #pragma unroll
     for (int c = 0; c < C; ++c) {
@@ -65,7 +125,8 @@ __device__ __forceinline__ double error_norm(const R* ut, const R* u0, const R* 
         acc = fma(e, e, acc);
     }
     acc = g.sum(acc);
-    return sqrt(acc / (double)(L * C));
+    if (sizeof(R) == 8) return (typename Ctl<R>::T)sqrt(acc / (double)(L * C));
+    return (typename Ctl<R>::T)sqrtf((float)acc * (1.0f / (float)(L * C)));
 }
 
 // Hairer's initial step (initdt.jl:17-298).  f0 is returned for FSAL methods.
@@ -112,6 +173,7 @@ __device__ double initdt(const R* u0, const R* p, double t, double dtmax, double
     if (mx <= 1e-15) {
         dt1 = jmax(1e-6, dt0 * 1e-3);
     } else {
+        // 10^(-(2 + log10 mx)/order) = exp(-(2 ln10 + ln mx)/order)
         const double LN10 = 2.302585092994046;
         dt1 = series_exp(-(2.0 * LN10 + series_ln(mx)) / (double)ORDER);
     }
@@ -122,31 +184,35 @@ __device__ double initdt(const R* u0, const R* p, double t, double dtmax, double
 // the step, the interpolant and the FSAL hooks.
 template <class Alg, class Model, class R, int L, int C>
 __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group<L>& g) {
+    using CT = typename Ctl<R>::T;
     constexpr int NP = Model::NP;
     const long long N = a.N;
-    R u[C], uprev[C];
+    R u[C], uprev[C], ulo[C], uprevlo[C];   // solution as (hi, lo) pairs, see Acc
     R p[NP];
 #pragma unroll
-    for (int c = 0; c < C; ++c) u[c] = (R)a.u0[(size_t)(g.lane * C + c) * N + j];
+    for (int c = 0; c < C; ++c) Acc<R>::split(a.u0[(size_t)(g.lane * C + c) * N + j], u[c], ulo[c]);
 #pragma unroll
     for (int i = 0; i < NP; ++i) p[i] = (R)a.p[(size_t)i * N + j];
     const double t0 = a.tspan[j], tf = a.tspan[N + j];
     const double dtmax = a.dtmax > 0 ? a.dtmax : tf - t0;
     const R abstol = (R)a.abstol, reltol = (R)a.reltol;
     const Ctrl K = make_ctrl<Alg::ORDER, Alg::IMPLICIT>(a);
+    const CT beta1 = (CT)K.beta1, beta2 = (CT)K.beta2, gam = (CT)K.gamma, qmin_inv = (CT)K.qmin_inv;
+    const CT qoldinit = (CT)K.qoldinit, qsteady_max = (CT)K.qsteady_max;
+    const CT inv_qmax = (CT)(1.0 / K.qmax), inv_qmax_first = (CT)(1.0 / K.qmax_first);
 
     typename Alg::template Cache<R, C> cache;
     StepStats st = {0, 0, 0, 0, 0, 0};
     int nsaved = 0;
     int isave = 0;
-    double last_saved_t = __longlong_as_double(0x7ff8000000000000LL);
+    double last_saved_t = dnan();
 
-    auto save_point = [&](double ts, const R* v) {
+    auto save_point = [&](double ts, const R* v, const R* vlo) {
         if (nsaved < a.nsave_cap) {
             if (g.lane == 0) a.t_out[(size_t)nsaved * N + j] = ts;
 #pragma unroll
             for (int c = 0; c < C; ++c)
-                a.u_out[((size_t)nsaved * a.nmax + g.lane * C + c) * N + j] = (double)v[c];
+                a.u_out[((size_t)nsaved * a.nmax + g.lane * C + c) * N + j] = Acc<R>::join(v[c], vlo[c]);
         }
         nsaved++;
         last_saved_t = ts;
@@ -159,11 +225,11 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
     while (isave < a.nsave && !(saveat_at(isave) > t0)) isave++;
 
 #pragma unroll
-    for (int c = 0; c < C; ++c) uprev[c] = u[c];
-    if (a.save_start) save_point(t0, u);
+    for (int c = 0; c < C; ++c) { uprev[c] = u[c]; uprevlo[c] = ulo[c]; }
+    if (a.save_start) save_point(t0, u, ulo);
 
     double t = t0, tprev = t0;
-    Alg::template initialize<Model, R, L, C>(cache, u, p, t, g, st, a);
+    Alg::template initialize<Model, R, L, C>(cache, u, p, t, g, st, a, j);
     double dt;
     if (a.dt > 0) {
         dt = a.dt;
@@ -173,54 +239,53 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
         st.nf += 2;
     }
     double dtpropose = dt;
-    double EEst = 1.0, q11 = 1.0, errold = K.qoldinit;
+    CT EEst = CT(1), q11 = CT(1), errold = qoldinit;
     long long iter = 0, success_iter = 0;
     bool accept = false, next_tstop = false;
     int rc = RC_DEFAULT;
 
     while (t < tf) {
         // ---- loopheader!
+        const double dist = tf - t;   // > 0 inside the loop; the only tstop is tf
         if (iter > 0) {
             if (accept) {
                 success_iter++;
 #pragma unroll
-                for (int c = 0; c < C; ++c) uprev[c] = u[c];
-                dt = dtpropose;
+                for (int c = 0; c < C; ++c) { uprev[c] = u[c]; uprevlo[c] = ulo[c]; }
+                // apply_step!: dt = dtpropose, then modify_dt_for_tstops! (whose flag and
+                // dtpropose the second call below overwrites; only the clip survives)
+                dt = pmin(dtpropose, dist);
                 Alg::template on_accept<R, C>(cache);
-                // modify_dt_for_tstops! (inside apply_step!)
-                double dist = fabs(tf - t);
-                double tol = 100.0 * jeps(jmax(fabs(t), fabs(tf)));
-                double orig = fabs(dt);
-                dtpropose = orig;
-                next_tstop = !(orig + tol < dist);
-                dt = jmin(orig, dist);
             } else {
-                dt = dt / jmin(K.qmin_inv, q11 / K.gamma);
+                // step_reject_controller!: dt /= min(1/qmin, q11/gamma)
+                const CT qq = q11 / gam;
+                const CT f = (qmin_inv != qmin_inv || qq != qq) ? qq + qmin_inv : (qmin_inv < qq ? qmin_inv : qq);
+                dt = Ctl<R>::scale_dt(dt, f);
             }
         }
         iter++;
         // fix_dt_at_bounds!
-        dt = jmin(dtmax, dt);
-        dt = jmax(dt, fabs(jmax(jeps(t), a.dtmin)));
+        dt = pmin(dtmax, dt);
+        dt = pmax(dt, pabs(pmax(peps(t), a.dtmin)));
         {   // modify_dt_for_tstops!
-            double dist = fabs(tf - t);
-            double tol = 100.0 * jeps(jmax(fabs(t), fabs(tf)));
-            double orig = fabs(dt);
+            const double tol = ptol100(pmax(pabs(t), pabs(tf)));
+            const double orig = pabs(dt);
             dtpropose = orig;
             next_tstop = !(orig + tol < dist);
-            dt = jmin(orig, dist);
+            dt = pmin(orig, dist);
         }
         // ---- check_error (de_check_error)
         {
             int e = RC_SUCCESS;
-            if (dt != dt) e = RC_DTNAN;
+            const long long db = __double_as_longlong(dt);
+            if (bits_nan(db)) e = RC_DTNAN;
             else if (iter > a.maxiters) e = RC_MAXITERS;
-            else if (fabs(dt) <= fabs(a.dtmin) && (!accept || t + dt < tf)) e = RC_DTLESSTHANMIN;
-            else if (!accept && fabs(dt) <= fabs(jeps(t))) e = RC_UNSTABLE;
+            else if (ple(pabs(dt), pabs(a.dtmin)) && (!accept || t + dt < tf)) e = RC_DTLESSTHANMIN;
+            else if (!accept && ple(pabs(dt), peps(t))) e = RC_UNSTABLE;
             else if (accept) {
                 bool bad = false;
 #pragma unroll
-                for (int c = 0; c < C; ++c) bad = bad || !isfinite((double)u[c]);
+                for (int c = 0; c < C; ++c) bad = bad || !isfinite(u[c]);
                 if (g.any(bad)) e = RC_UNSTABLE;
             }
             if (e == RC_SUCCESS && a.abort_flag != nullptr && (iter & 63) == 0 && *a.abort_flag != 0)
@@ -228,23 +293,24 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             if (e != RC_SUCCESS) { rc = e; break; }
         }
         // ---- perform_step! (skipped for a step below eps(t) onto the tstop)
-        if (!(next_tstop && fabs(dt) < jeps(fabs(t)))) {
-            EEst = Alg::template step<Model, R, L, C>(cache, u, uprev, p, t, dt, abstol, reltol, iter, EEst, g, st);
+        if (!(next_tstop && plt(pabs(dt), peps(t)))) {
+            EEst = Alg::template step<Model, R, L, C>(cache, u, ulo, uprev, uprevlo, p, t, dt, abstol, reltol, iter,
+                                                      EEst > CT(1), g, st);
         }
         // ---- loopfooter!
-        double ttmp = t + dt;
-        double qmaxc = success_iter == 0 ? K.qmax_first : K.qmax;
-        double q;
-        if (EEst == 0.0) {
-            q = 1.0 / qmaxc;
+        const double ttmp = t + dt;
+        const CT inv_qmaxc = success_iter == 0 ? inv_qmax_first : inv_qmax;
+        CT q;
+        if (EEst == CT(0)) {
+            q = inv_qmaxc;
         } else {
-            double qq = ctrl_pow(EEst, K.beta1);
-            q = qq / ctrl_pow(errold, K.beta2);
+            const CT qq = Ctl<R>::pw(EEst, beta1);
+            q = qq / Ctl<R>::pw(errold, beta2);
             q11 = qq;
-            double x = q / K.gamma, lo = 1.0 / qmaxc, hi = K.qmin_inv;
-            q = x > hi ? hi : (x < lo ? lo : x);
+            const CT x = q / gam;
+            q = x > qmin_inv ? qmin_inv : (x < inv_qmaxc ? inv_qmaxc : x);
         }
-        accept = EEst <= 1.0;
+        accept = EEst <= CT(1);
         if (accept) {
             st.naccept++;
             tprev = t;
@@ -255,11 +321,11 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             } else {
                 t = ttmp;
             }
-            if (1.0 <= q && q <= K.qsteady_max) q = 1.0;
-            errold = jmax(EEst, K.qoldinit);
-            double dtnew = dt / q;
-            double dtp = jmin(fabs(dtmax), fabs(dtnew));
-            dtpropose = jmax(fabs(dtp), fabs(jmax(jeps(t), a.dtmin)));
+            if (CT(1) <= q && q <= qsteady_max) q = CT(1);
+            errold = (EEst != EEst) ? EEst : (EEst > qoldinit ? EEst : qoldinit);
+            const double dtnew = Ctl<R>::scale_dt(dt, q);
+            const double dtp = pmin(pabs(dtmax), pabs(dtnew));
+            dtpropose = pmax(pabs(dtp), pabs(pmax(peps(t), a.dtmin)));
             // ---- savevalues!
             while (isave < a.nsave) {
                 double curt = saveat_at(isave);
@@ -267,12 +333,13 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
                 isave++;
                 if (curt != t) {
                     double th = (curt - tprev) / dt;
-                    R out[C];
-                    Alg::template interpolate<Model, R, L, C>(cache, out, th, dt, tprev, uprev, u, p, g);
-                    save_point(curt, out);
+                    R out[C], outlo[C];
+                    Alg::template interpolate<Model, R, L, C>(cache, out, outlo, th, dt, tprev, uprev, uprevlo, u,
+                                                              ulo, p, g);
+                    save_point(curt, out, outlo);
                 } else {
                     if (curt == tf && !a.save_end) continue;
-                    save_point(t, u);
+                    save_point(t, u, ulo);
                 }
             }
             Alg::template after_save<R, C>(cache);
@@ -292,7 +359,7 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
                 for (int s = 0; s < a.nsave; ++s) in_saveat = in_saveat || (saveat_at(s) == t);
             need = last_saved_t != t && (a.save_end_user == 1 || in_saveat || t == tf || !a.saveat_given);
         }
-        if (need) save_point(t, u);
+        if (need) save_point(t, u, ulo);
     }
     if (g.lane == 0) {
         a.nsaved[j] = nsaved < a.nsave_cap ? nsaved : a.nsave_cap;

@@ -46,10 +46,11 @@ const std::vector<KernelVariant>& all_variants() {
 
 int model_nparams(int model) { return model == ODE_MODEL_LINEAR ? 1 : 3; }
 
-// Default lanes per trajectory: one lane up to 8 states, else 4 states per lane.
+// Default lanes per trajectory: one lane for tiny systems (registers hold the
+// whole state and stage set), else 4 states per lane so the Vern7 stage set
+// stays in registers without spilling.
 int default_lanes(int alg, int n) {
-    (void)alg;
-    if (n <= 8) return 1;
+    if (n <= 4 || (n <= 8 && alg == ODE_RODAS5P)) return 1;
     return std::min(32, n / 4);
 }
 
@@ -194,7 +195,9 @@ EnsembleArgs make_args(ode_handle* h, const ode_problem_desc* d, const ode_optio
     a.saveat_scalar = o->saveat_scalar;
     a.qmax_first_step = o->qmax_first_step;
     a.qmax = o->qmax;
-    a.ir_sweeps = o->ir_sweeps < 0 ? 1 : o->ir_sweeps;
+    // Register-resident Rosenbrock solves (n <= 8) default to no refinement:
+    // their FP32 LU error is far below the tolerance; sweeps are available on request.
+    a.ir_sweeps = o->ir_sweeps < 0 ? 0 : o->ir_sweeps;
     a.abort_flag = h->d_abort;
     return a;
 }

@@ -12,9 +12,10 @@
 // the same algorithm the CPU oracle states; LinearSolve's LU (not vendored)
 // pivots the same way.
 //
-// Mixed precision (R = float): J, W and the LU are FP32; every solve W x = b
-// is followed by `a.ir_sweeps` refinement sweeps whose residual b - W x is
-// formed in FP64 from an FP64 copy of W.
+// Mixed precision (R = float): J, W, the LU, the solves and the stage sums are
+// FP32; the right-hand side is evaluated in double-float (ff) on the
+// compensated state, because stiff kinetics cancel inside f; `ir_sweeps`
+// optional refinement sweeps per solve form the residual b - W x in FP64.
 #pragma once
 #include "integrator.cuh"
 #include "tableaus.h"
@@ -85,11 +86,28 @@ __device__ __forceinline__ void lu_solve_reg(const R (*LU)[N], const int* piv, R
     }
 }
 
-#define RP_(x) ((R)(tab::x))
+// f(u) for a Rosenbrock stage: plain R in FP64 mode; in the mixed mode the
+// state (hi + lo) and the parameters are lifted to double-float, f runs in
+// double-float, and the result is rounded to FP32.
+template <class Model, class R, int L, int C, int NP>
+__device__ __forceinline__ void rhs_stage(R* du, const R* u, const R* ulo, const R* p, const ff* pff, double t,
+                                          const Group<L>& g) {
+    if (sizeof(R) == 8) {
+        Model::template rhs<R, L, C>(du, u, p, t, g);
+    } else {
+        ff uu[C], dd[C];
+#pragma unroll
+        for (int i = 0; i < C; ++i) uu[i] = ff_fast2sum((float)u[i], (float)ulo[i]);
+        Model::template rhs<ff, L, C>(dd, uu, pff, t, g);
+#pragma unroll
+        for (int i = 0; i < C; ++i) du[i] = (R)dd[i].f();
+    }
+}
 
 struct Rodas5PAlg {
     static constexpr int ORDER = 5;
     static constexpr bool IMPLICIT = true;
+    static constexpr int MAXP = 4;
     template <class R, int C> struct Cache {
         R J[C][C];
         R W[C][C];
@@ -97,23 +115,29 @@ struct Rodas5PAlg {
         R ks[8][C];
         R dk[3][C];   // dense k1..k3
         R scratch[C];
+        ff pff[MAXP];  // parameters in double-float (mixed mode)
         bool haveJ;
         int ir;
     };
     template <class R, int C> __device__ static R* fsal_slot(Cache<R, C>& c) { return c.scratch; }
     template <class Model, class R, int L, int C>
     __device__ static void initialize(Cache<R, C>& c, const R*, const R*, double, const Group<L>&, StepStats&,
-                                      const EnsembleArgs& a) {
+                                      const EnsembleArgs& a, long long j) {
         c.haveJ = false;
         c.ir = a.ir_sweeps;
+        if (sizeof(R) == 4) {
+#pragma unroll
+            for (int i = 0; i < Model::NP; ++i) c.pff[i] = ff(a.p[(size_t)i * a.N + j]);
+        }
     }
     template <class R, int C> __device__ static void on_accept(Cache<R, C>&) {}
     template <class R, int C> __device__ static void after_save(Cache<R, C>&) {}
 
-    // Solve W x = b in place (b -> x), with FP64-residual refinement in mixed mode.
+    // Solve W x = b in place (b -> x); in the mixed mode optionally refined with
+    // FP64 residuals b - (J - I/(dt*gamma)) x.
     template <class R, int C>
-    __device__ static void wsolve(Cache<R, C>& c, R* b, double invdtgamma, int sweeps) {
-        if (sizeof(R) == 8 || sweeps <= 0) {
+    __device__ static void wsolve(Cache<R, C>& c, R* b, double invdtgamma) {
+        if (sizeof(R) == 8 || c.ir <= 0) {
             lu_solve_reg<R, C>(c.W, c.piv, b);
             return;
         }
@@ -124,15 +148,15 @@ struct Rodas5PAlg {
         double x[C];
 #pragma unroll
         for (int i = 0; i < C; ++i) x[i] = (double)b[i];
-        for (int s = 0; s < sweeps; ++s) {
+        for (int s = 0; s < c.ir; ++s) {
             R r[C];
 #pragma unroll
             for (int i = 0; i < C; ++i) {
                 double acc = b64[i];
 #pragma unroll
-                for (int j = 0; j < C; ++j) {
-                    double wij = (double)c.J[i][j] - (i == j ? invdtgamma : 0.0);
-                    acc = fma(-wij, x[j], acc);
+                for (int jj = 0; jj < C; ++jj) {
+                    double wij = (double)c.J[i][jj] - (i == jj ? invdtgamma : 0.0);
+                    acc = fma(-wij, x[jj], acc);
                 }
                 r[i] = (R)acc;
             }
@@ -145,16 +169,20 @@ struct Rodas5PAlg {
     }
 
     template <class Model, class R, int L, int C>
-    __device__ static double step(Cache<R, C>& c, R* u, const R* up, const R* p, double t, double dt,
-                                  R abstol, R reltol, long long iter, double EEst_prev, const Group<L>& g,
-                                  StepStats& st) {
+    __device__ static typename Ctl<R>::T step(Cache<R, C>& c, R* u, R* ulo, const R* up, const R* uplo,
+                                             const R* p, double t, double dt, R abstol, R reltol, long long iter,
+                                             bool errorfail, const Group<L>& g, StepStats& st) {
         static_assert(L == 1, "register Rodas5P runs one trajectory per lane");
-        const double invdt = 1.0 / dt;
-        const double dtgamma = dt * tab::RODAS5P_GAMMA;
+        constexpr int NP = Model::NP;
+        // dt-derived coefficients: FP64 like the reference; in the mixed mode they
+        // scale FP32 stage terms, so they are formed in FP32 from dt (no FP64 work).
+        const R dr = (R)dt;
+        const R invdt = sizeof(R) == 8 ? R(1.0 / dt) : R(1) / dr;
+        const double invdtgamma = (sizeof(R) == 8 || c.ir > 0) ? 1.0 / (dt * tab::RODAS5P_GAMMA) : 0.0;
+        const R idg = sizeof(R) == 8 ? (R)invdtgamma : R(1) / (dr * (R)tab::RODAS5P_GAMMA);
         R* fsal = c.scratch;
-        Model::template rhs<R, L, C>(fsal, up, p, t, g);
+        rhs_stage<Model, R, L, C, NP>(fsal, up, uplo, p, c.pff, t, g);
         st.nf += 1;
-        bool errorfail = EEst_prev > 1.0;
         bool new_jac = !(iter > 1 && errorfail) || !c.haveJ;
         if (new_jac) {
             Model::template jac<R, C>(c.J, up, p, t);
@@ -162,53 +190,68 @@ struct Rodas5PAlg {
             st.nf += 1;   // the reference's AD time derivative (dT = 0 for autonomous models)
             c.haveJ = true;
         }
-        const double invdtgamma = 1.0 / dtgamma;
-        const R idg = (R)invdtgamma;
 #pragma unroll
         for (int i = 0; i < C; ++i)
 #pragma unroll
-            for (int j = 0; j < C; ++j) c.W[i][j] = (i == j) ? FMA(R(-1), idg, c.J[i][j]) : c.J[i][j];
+            for (int jj = 0; jj < C; ++jj) c.W[i][jj] = (i == jj) ? FMA(R(-1), idg, c.J[i][jj]) : c.J[i][jj];
         st.nw += 1;
         lu_factor_reg<R, C>(c.W, c.piv);
         R r[C];
 #pragma unroll
         for (int i = 0; i < C; ++i) r[i] = fsal[i];
-        wsolve<R, C>(c, r, invdtgamma, c.ir);
+        wsolve<R, C>(c, r, invdtgamma);
 #pragma unroll
         for (int i = 0; i < C; ++i) c.ks[0][i] = -r[i];
         st.nsolve += 1;
 #pragma unroll
         for (int s = 1; s < 8; ++s) {
+            R stlo[C];
 #pragma unroll
             for (int i = 0; i < C; ++i) {
                 R acc = up[i];
 #pragma unroll
                 for (int jj = 0; jj < s; ++jj) acc = FMA((R)tab::RODAS5P_A(s, jj), c.ks[jj][i], acc);
-                u[i] = acc;
+                if (sizeof(R) == 8) {
+                    u[i] = acc;
+                    stlo[i] = R(0);
+                } else {   // stage value as an exact pair: (up + sum) + uplo
+                    R sum = R(0);
+#pragma unroll
+                    for (int jj = 0; jj < s; ++jj) sum = FMA((R)tab::RODAS5P_A(s, jj), c.ks[jj][i], sum);
+                    Acc<R>::update(u[i], stlo[i], R(1), sum, up[i], uplo[i]);
+                }
             }
             R du[C];
-            Model::template rhs<R, L, C>(du, u, p, fma(tab::RODAS5P_c(s), dt, t), g);
+            rhs_stage<Model, R, L, C, NP>(du, u, stlo, p, c.pff, fma(tab::RODAS5P_c(s), dt, t), g);
             st.nf += 1;
 #pragma unroll
             for (int i = 0; i < C; ++i) {
                 R acc = du[i];
 #pragma unroll
-                for (int jj = 0; jj < s; ++jj) acc = FMA((R)(tab::RODAS5P_C(s, jj) * invdt), c.ks[jj][i], acc);
+                for (int jj = 0; jj < s; ++jj) acc = FMA((R)tab::RODAS5P_C(s, jj) * invdt, c.ks[jj][i], acc);
                 r[i] = acc;
             }
-            wsolve<R, C>(c, r, invdtgamma, c.ir);
+            wsolve<R, C>(c, r, invdtgamma);
 #pragma unroll
             for (int i = 0; i < C; ++i) c.ks[s][i] = -r[i];
             st.nsolve += 1;
         }
 #pragma unroll
         for (int i = 0; i < C; ++i) {
-            R acc = up[i];
+            if (sizeof(R) == 8) {   // reference order: acc = uprev; acc = muladd(b_j, ks_j, acc)
+                R acc = up[i];
 #pragma unroll
-            for (int jj = 0; jj < 7; ++jj) acc = FMA((R)tab::RODAS5P_A(7, jj), c.ks[jj][i], acc);
-            u[i] = FMA(R(1), c.ks[7][i], acc);
+                for (int jj = 0; jj < 7; ++jj) acc = FMA((R)tab::RODAS5P_A(7, jj), c.ks[jj][i], acc);
+                Acc<R>::set(u[i], ulo[i], FMA(R(1), c.ks[7][i], acc));
+            } else {                // increment in FP32, added to the compensated solution
+                R inc = R(0);
+#pragma unroll
+                for (int jj = 0; jj < 7; ++jj) inc = FMA((R)tab::RODAS5P_A(7, jj), c.ks[jj][i], inc);
+                inc = FMA(R(1), c.ks[7][i], inc);
+                Acc<R>::update(u[i], ulo[i], R(1), inc, up[i], uplo[i]);
+            }
         }
-        double EEst = error_norm<R, L, C>(c.ks[7], up, u, abstol, reltol, g);
+        const typename Ctl<R>::T EEst = error_norm<R, L, C>(c.ks[7], up, u, abstol, reltol, g);
 #pragma unroll
         for (int jd = 0; jd < 3; ++jd)
 #pragma unroll
@@ -222,19 +265,23 @@ struct Rodas5PAlg {
     }
 
     template <class Model, class R, int L, int C>
-    __device__ static void interpolate(Cache<R, C>& c, R* out, double thd, double, double, const R* y0,
-                                       const R* y1, const R*, const Group<L>&) {
+    __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, double thd, double, double, const R* y0,
+                                       const R* y0lo, const R* y1, const R* y1lo, const R*, const Group<L>&) {
         const R th = (R)thd, th1 = R(1) - th;
 #pragma unroll
         for (int i = 0; i < C; ++i) {
             R inner = FMA(th, c.dk[2][i], c.dk[1][i]);
             inner = FMA(th, inner, c.dk[0][i]);
-            R v = FMA(th1, inner, y1[i]);
-            out[i] = FMA(th1, y0[i], th * v);
+            if (sizeof(R) == 8) {
+                R v = FMA(th1, inner, y1[i]);
+                Acc<R>::set(out[i], outlo[i], FMA(th1, y0[i], th * v));
+            } else {   // a save is rare: combine the compensated end points in FP64
+                double t1 = 1.0 - thd;
+                double v = fma(t1, (double)inner, Acc<R>::join(y1[i], y1lo[i]));
+                Acc<R>::split(fma(t1, Acc<R>::join(y0[i], y0lo[i]), thd * v), out[i], outlo[i]);
+            }
         }
     }
 };
-
-#undef RP_
 
 }  // namespace odegb

@@ -65,6 +65,7 @@ SIGNATURES = {
     "ode_kernel_launches": (C.c_int, [_VP, C.POINTER(C.c_int64)]),
     "ode_last_kernel_ms": (C.c_int, [_VP, _DP]),
     "ode_query_variants": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _IP, C.c_int32]),
+    "ode_measure_fma_peak": (C.c_int, [C.c_int, C.c_int, _DP]),
 }
 
 _lib = None

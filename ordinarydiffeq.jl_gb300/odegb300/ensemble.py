@@ -59,6 +59,9 @@ class Rodas5P(_Alg):
     alg_id = _lib.ODE_RODAS5P
 
 
+ALG_BY_NAME = {"tsit5": Tsit5(), "vern7": Vern7(), "rodas5p": Rodas5P()}
+
+
 @dataclass
 class EnsembleGB300:
     """Ensemble algorithm running every trajectory on one GB300.

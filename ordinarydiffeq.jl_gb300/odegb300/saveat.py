@@ -87,6 +87,9 @@ def resolve_saveat(saveat, tspans, save_start=None, save_end=None):
     t0s, tfs = tspans[0], tspans[1]
     same_span = bool(np.all(t0s == t0s[0]) and np.all(tfs == tfs[0])) if tspans.shape[1] else True
     seu = -1 if save_end is None else int(bool(save_end))
+    if tspans.shape[1] == 0:  # empty ensemble: nothing to resolve
+        return SaveSpec(np.zeros(0), 0, False, np.isscalar(saveat), True if save_start is None else bool(save_start),
+                        True if save_end is None else bool(save_end), seu)
     if saveat is None or (not np.isscalar(saveat) and np.size(saveat) == 0):
         return SaveSpec(np.zeros(0), 0, False, False, True if save_start is None else bool(save_start),
                         True if save_end is None else bool(save_end), seu)

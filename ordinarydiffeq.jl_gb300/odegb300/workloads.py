@@ -1,0 +1,112 @@
+"""Seeded synthetic ensembles with the shapes of the benchmark configurations,
+and the algorithmic FLOP counts the roofline uses.
+
+No public dataset exists for this path; each workload is generated from a seed
+with the sizes and parameter distributions of the configuration it names.
+"""
+import numpy as np
+
+# ---------------------------------------------------------------- workloads
+
+
+def lorenz(N, seed=42):
+    """10k-style Lorenz ensemble: u0 = (1, 0, 0), sigma = 10, beta = 8/3, rho ~ U(0, 21),
+    tspan (0, 1), Tsit5, reltol = abstol = 1e-8, saveat 0.1."""
+    rng = np.random.default_rng(seed)
+    u0 = np.tile(np.array([[1.0], [0.0], [0.0]]), (1, N))
+    p = np.vstack([np.full(N, 10.0), rng.uniform(0.0, 21.0, N), np.full(N, 8.0 / 3.0)])
+    ts = np.vstack([np.zeros(N), np.ones(N)])
+    return dict(model="lorenz", alg="tsit5", u0=u0, p=p, tspan=ts, saveat=0.1, reltol=1e-8, abstol=1e-8)
+
+
+ROBER_SAVEAT = 10.0 ** np.linspace(-5.0, 5.0, 20)
+
+
+def robertson(N, seed=42):
+    """Robertson kinetics: k = (0.04, 3e7, 1e4) each scaled by 2^U(-1, 1) (log-uniform in
+    [0.5, 2]); u0 = (1, 0, 0); tspan (0, 1e5); 20 log-spaced saves in (0, 1e5];
+    Rodas5P with the analytic Jacobian, reltol 1e-6, abstol 1e-10."""
+    rng = np.random.default_rng(seed)
+    p = np.array([0.04, 3e7, 1e4])[:, None] * 2.0 ** rng.uniform(-1.0, 1.0, (3, N))
+    u0 = np.tile(np.array([[1.0], [0.0], [0.0]]), (1, N))
+    ts = np.vstack([np.zeros(N), np.full(N, 1e5)])
+    return dict(model="robertson", alg="rodas5p", u0=u0, p=p, tspan=ts, saveat=ROBER_SAVEAT, reltol=1e-6,
+                abstol=1e-10)
+
+
+def duffing(N, seed=42, sizes=(2, 4, 8, 16, 32), tf_range=(1.0, 100.0)):
+    """Uneven Duffing chains: N oscillators uniform in `sizes` (2N states), stiffness and
+    damping ~ U(0.1, 1), cubic ~ U(0, 5), u0 ~ N(0, 1), tf log-uniform in tf_range,
+    16 uniform saves in (0, tf]; Vern7, reltol = abstol = 1e-6."""
+    rng = np.random.default_rng(seed)
+    npt = (2 * rng.choice(np.asarray(sizes), N)).astype(np.int32)
+    nmax = int(npt.max())
+    u0 = rng.standard_normal((nmax, N))
+    u0[np.arange(nmax)[:, None] >= npt[None, :]] = 0.0
+    p = np.vstack([rng.uniform(0.1, 1.0, N), rng.uniform(0.1, 1.0, N), rng.uniform(0.0, 5.0, N)])
+    tf = 10.0 ** rng.uniform(np.log10(tf_range[0]), np.log10(tf_range[1]), N)
+    ts = np.vstack([np.zeros(N), tf])
+    saveat = np.outer(np.arange(1, 17) / 16.0, tf)
+    return dict(model="duffing_chain", alg="vern7", u0=u0, p=p, tspan=ts, saveat=saveat, reltol=1e-6,
+                abstol=1e-6, n_per_traj=npt)
+
+
+def brusselator(N, seed=42, cells=32):
+    """Brusselator 1-D, 32 periodic cells (64 states): A ~ U(0.5, 1.5), B ~ U(2, 4),
+    alpha log-uniform in [1e-3, 1e-1], u0 = steady state (A, B/A) + 0.1 N(0, 1);
+    tspan (0, 10), saves at 1.25:1.25:10; Rodas5P, reltol 1e-5, abstol 1e-8."""
+    rng = np.random.default_rng(seed)
+    A = rng.uniform(0.5, 1.5, N)
+    B = rng.uniform(2.0, 4.0, N)
+    alpha = 10.0 ** rng.uniform(-3.0, -1.0, N)
+    n = 2 * cells
+    u0 = np.empty((n, N))
+    u0[0::2] = A[None, :]
+    u0[1::2] = (B / A)[None, :]
+    u0 += 0.1 * rng.standard_normal((n, N))
+    p = np.vstack([A, B, alpha])
+    ts = np.vstack([np.zeros(N), np.full(N, 10.0)])
+    return dict(model="brusselator_1d", alg="rodas5p", u0=u0, p=p, tspan=ts, saveat=1.25, reltol=1e-5,
+                abstol=1e-8)
+
+
+# ---------------------------------------------------------------- FLOP model
+# Algorithmic floating-point operations per attempted step (an fma counts 2),
+# counted from the kernels' own arithmetic.  F: FLOPs of one RHS evaluation.
+
+RHS_FLOPS = {"linear": lambda n: n, "lorenz": lambda n: 9, "robertson": lambda n: 13,
+             "duffing_chain": lambda n: 9 * (n // 2), "brusselator_1d": lambda n: 13 * (n // 2)}
+JAC_FLOPS = {"linear": lambda n: 0, "lorenz": lambda n: 3, "robertson": lambda n: 10,
+             "duffing_chain": lambda n: 5 * (n // 2), "brusselator_1d": lambda n: 14 * (n // 2)}
+CONTROLLER_FLOPS = 150  # two series pow evaluations, clamp, dt update (FP64)
+
+
+def error_norm_flops(n):
+    return 6 * n + 4
+
+
+def attempt_flops(alg, model, n):
+    F = RHS_FLOPS[model](n)
+    if alg == "tsit5":
+        # 6 RHS; stage sums 21 fma + solution 6 fma (in the 21) + btilde 7 fma per state
+        return 6 * F + n * (2 * 21 + 2 * 7 + 6) + error_norm_flops(n) + CONTROLLER_FLOPS
+    if alg == "vern7":
+        # 10 RHS; 36 stage fma + 7 solution fma + 8 btilde fma per state
+        return 10 * F + n * (2 * 36 + 2 * 7 + 2 * 8 + 10) + error_norm_flops(n) + CONTROLLER_FLOPS
+    if alg == "rodas5p":
+        Jf = JAC_FLOPS[model](n)
+        lu = sum((n - c - 1) + 2 * (n - c - 1) ** 2 + 1 for c in range(n))
+        solve = 2 * n * n + n
+        return (8 * F + Jf + 2 * n + lu + 8 * solve + n * (2 * 28 + 2 * 28 + 2 * 8 + 2 * 24) + 28 + 8
+                + error_norm_flops(n) + CONTROLLER_FLOPS)
+    raise ValueError(alg)
+
+
+def save_flops(alg, model, n):
+    """Extra work of a step that holds saveat points (Vern7 lazy stages + interpolant)."""
+    F = RHS_FLOPS[model](n)
+    if alg == "vern7":
+        return 6 * F + n * 2 * (7 + 8 + 9 + 10 + 10 + 10) + n * 2 * 13
+    if alg == "tsit5":
+        return n * 2 * 7
+    return n * 2 * 5
