@@ -112,21 +112,47 @@ __device__ __forceinline__ Ctrl make_ctrl(const EnsembleArgs& a) {
     return c;
 }
 
-// Residual norm sqrt(sum_i (ut_i / (abstol + max(|u0_i|,|u1_i|) reltol))^2 / n),
-// the sum accumulated in FP64 (sequentially within a lane, then across the group).
+// Residual norm sqrt(sum_i (ut_i / (abstol + max(|u0_i|,|u1_i|) reltol))^2 / n).
+// FP64 mode: the sum in FP64 (sequentially within a lane, then across the
+// group).  Mixed mode: the same sum carried in double-float (an exact square
+// by fma, a two-sum per term; FP64-class precision on the FP32 pipe), since
+// on GB300 each FP64 add/fma or float<->double conversion per component would
+// cost the FP64 pipe more time than the whole FP32 stage work of a small system.
 template <class R, int L, int C>
 __device__ __forceinline__ typename Ctl<R>::T error_norm(const R* ut, const R* u0, const R* u1, R abstol, R reltol,
                                                          const Group<L>& g) {
-    double acc = 0.0;
+    if (sizeof(R) == 8) {
+        double acc = 0.0;
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            R sc = FMA(tmax(ABS(u0[c]), ABS(u1[c])), reltol, abstol);
+            double e = (double)(ut[c] / sc);
+            acc = fma(e, e, acc);
+        }
+        acc = g.sum(acc);
+        return (typename Ctl<R>::T)sqrt(acc / (double)(L * C));
+    }
+    float hi = 0.0f, lo = 0.0f;
 #pragma unroll
     for (int c = 0; c < C; ++c) {
-        R sc = FMA(tmax(ABS(u0[c]), ABS(u1[c])), reltol, abstol);
-        double e = (double)(ut[c] / sc);
-        acc = fma(e, e, acc);
+        const float sc = fmaf(tmax(fabsf((float)u0[c]), fabsf((float)u1[c])), (float)reltol, (float)abstol);
+        const float e = (float)ut[c] / sc;
+        const float p = e * e;
+        const float pe = fmaf(e, e, -p);
+        const float s = hi + p;
+        const float bb = s - hi;
+        lo += ((hi - (s - bb)) + (p - bb)) + pe;
+        hi = s;
     }
-    acc = g.sum(acc);
-    if (sizeof(R) == 8) return (typename Ctl<R>::T)sqrt(acc / (double)(L * C));
-    return (typename Ctl<R>::T)sqrtf((float)acc * (1.0f / (float)(L * C)));
+#pragma unroll
+    for (int off = L / 2; off > 0; off >>= 1) {
+        const float oh = __shfl_xor_sync(g.mask, hi, off, L), ol = __shfl_xor_sync(g.mask, lo, off, L);
+        const float s = hi + oh;
+        const float bb = s - hi;
+        lo = lo + ol + ((hi - (s - bb)) + (oh - bb));
+        hi = s;
+    }
+    return (typename Ctl<R>::T)sqrtf((hi + lo) * (1.0f / (float)(L * C)));
 }
 
 // Hairer's initial step (initdt.jl:17-298).  f0 is returned for FSAL methods.
@@ -374,7 +400,10 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
 // ensemble form) or persistent (groups pop trajectory indices from a device
 // counter until the ensemble is exhausted).
 template <class Alg, class Model, class R, int L, int C>
-__global__ void __launch_bounds__(128) ensemble_kernel(EnsembleArgs a) {
+#ifndef ODEGB_MIN_BLOCKS_F32
+#define ODEGB_MIN_BLOCKS_F32 1
+#endif
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? ODEGB_MIN_BLOCKS_F32 : 1) ensemble_kernel(EnsembleArgs a) {
     Group<L> g;
     const long long gid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / L;
     if (!a.persistent) {

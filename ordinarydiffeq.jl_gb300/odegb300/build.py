@@ -48,7 +48,9 @@ def up_to_date():
 
 def _compile(src, verbose):
     obj = os.path.join(OBJ_DIR, os.path.basename(src).replace(".cu", ".o"))
-    cmd = [nvcc()] + ARCH + NVCC_FLAGS + ["-c", src, "-o", obj]
+    # ODEGB_EXTRA_NVCC_FLAGS: tuning defines, e.g. -DODEGB_MIN_BLOCKS_F32=4
+    extra = os.environ.get("ODEGB_EXTRA_NVCC_FLAGS", "").split()
+    cmd = [nvcc()] + ARCH + NVCC_FLAGS + extra + ["-c", src, "-o", obj]
     if verbose:
         cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)
