@@ -1037,7 +1037,8 @@ int orc_solve_ensemble(int alg, int model, int nmax, const int32_t* n_per_traj, 
             for (int i = 0; i < np; ++i) pj[i] = p[(size_t)i * N + j];
             for (int s = 0; s < nsave; ++s) sv[s] = saveat_per_traj ? saveat[(size_t)s * N + j] : saveat[s];
             double t0 = tspan[j], tf = tspan[N + j];
-            setup(I, alg, model, n, pj.data(), t0, tf, o, sv.data(), nsave, nullptr, 0);
+            setup(I, alg, model, n, pj.data(), t0, tf, o, sv.data(), nsave, o->saveat_as_tstops ? sv.data() : nullptr,
+                  o->saveat_as_tstops ? nsave : 0);
             I.t_out = tl.data();
             I.u_out = ul.data();
             I.cap = cap;

@@ -43,6 +43,7 @@ typedef struct {
     int32_t saveat_scalar;  /* saveat was a Number (affects the endpoint rule) */
     double qmax_first_step; /* <= 0: 10000 */
     double qmax;            /* <= 0: 10 */
+    int32_t saveat_as_tstops; /* ensemble only: stop exactly at every save (ground-truth solves) */
 } orc_opts;
 
 /* Solve one trajectory.  saveat: nsave_in times in (t0, tf] sorted ascending.

@@ -31,7 +31,7 @@ class Opts(C.Structure):
         ("dtmin", C.c_double), ("dt", C.c_double), ("adaptive", C.c_int32),
         ("maxiters", C.c_int64), ("save_start", C.c_int32), ("save_end", C.c_int32),
         ("save_end_user", C.c_int32), ("saveat_given", C.c_int32), ("saveat_scalar", C.c_int32),
-        ("qmax_first_step", C.c_double), ("qmax", C.c_double),
+        ("qmax_first_step", C.c_double), ("qmax", C.c_double), ("saveat_as_tstops", C.c_int32),
     ]
 
 
@@ -75,10 +75,10 @@ def _dp(a):
 
 def make_opts(reltol=1e-3, abstol=1e-6, dtmax=0.0, dtmin=0.0, dt=0.0, adaptive=True,
               maxiters=1000000, save_start=False, save_end=True, save_end_user=-1,
-              saveat_given=True, saveat_scalar=False, qmax_first_step=0.0, qmax=0.0):
+              saveat_given=True, saveat_scalar=False, qmax_first_step=0.0, qmax=0.0, saveat_as_tstops=False):
     return Opts(reltol, abstol, dtmax, dtmin, dt, int(adaptive), maxiters, int(save_start),
                 int(save_end), save_end_user, int(saveat_given), int(saveat_scalar),
-                qmax_first_step, qmax)
+                qmax_first_step, qmax, int(saveat_as_tstops))
 
 
 def solve(alg, model, u0, p, tspan, saveat=(), tstops=(), dense=False, **kw):

@@ -75,6 +75,17 @@ struct CSum {
         hi = s;
         lo += e + e2;
     }
+    // weight given as a float pair wh + wl (a runtime product formed exactly)
+    __device__ __forceinline__ void add_pair(float wh, float wl, float k) {
+        float p = wh * k;
+        float e = fmaf(wh, k, -p);
+        e = fmaf(wl, k, e);
+        float s = hi + p;
+        float bb = s - hi;
+        float e2 = (hi - (s - bb)) + (p - bb);
+        hi = s;
+        lo += e + e2;
+    }
     __device__ __forceinline__ float value() const { return hi + lo; }
 };
 

@@ -18,6 +18,7 @@
 // optional refinement sweeps per solve form the residual b - W x in FP64.
 #pragma once
 #include "integrator.cuh"
+#include "rksum.cuh"
 #include "tableaus.h"
 
 namespace odegb {
@@ -208,17 +209,17 @@ struct Rodas5PAlg {
             R stlo[C];
 #pragma unroll
             for (int i = 0; i < C; ++i) {
-                R acc = up[i];
+                if (sizeof(R) == 8) {   // reference: acc = uprev; acc = muladd(A[s,j], ks_j, acc)
+                    R acc = up[i];
 #pragma unroll
-                for (int jj = 0; jj < s; ++jj) acc = FMA((R)tab::RODAS5P_A(s, jj), c.ks[jj][i], acc);
-                if (sizeof(R) == 8) {
+                    for (int jj = 0; jj < s; ++jj) acc = FMA((R)tab::RODAS5P_A(s, jj), c.ks[jj][i], acc);
                     u[i] = acc;
                     stlo[i] = R(0);
-                } else {   // stage value as an exact pair: (up + sum) + uplo
-                    R sum = R(0);
+                } else {   // compensated sum, then the stage value as an exact pair up + sum + uplo
+                    CSum cs;
 #pragma unroll
-                    for (int jj = 0; jj < s; ++jj) sum = FMA((R)tab::RODAS5P_A(s, jj), c.ks[jj][i], sum);
-                    Acc<R>::update(u[i], stlo[i], R(1), sum, up[i], uplo[i]);
+                    for (int jj = 0; jj < s; ++jj) cs.add(tab::RODAS5P_A(s, jj), (float)c.ks[jj][i]);
+                    Acc<R>::update(u[i], stlo[i], R(1), (R)cs.value(), up[i], uplo[i]);
                 }
             }
             R du[C];
@@ -226,10 +227,23 @@ struct Rodas5PAlg {
             st.nf += 1;
 #pragma unroll
             for (int i = 0; i < C; ++i) {
-                R acc = du[i];
+                if (sizeof(R) == 8) {
+                    R acc = du[i];
 #pragma unroll
-                for (int jj = 0; jj < s; ++jj) acc = FMA((R)tab::RODAS5P_C(s, jj) * invdt, c.ks[jj][i], acc);
-                r[i] = acc;
+                    for (int jj = 0; jj < s; ++jj) acc = FMA((R)tab::RODAS5P_C(s, jj) * invdt, c.ks[jj][i], acc);
+                    r[i] = acc;
+                } else {   // du + sum_j (C[s,j]/dt) ks_j with C split at compile time and 1/dt exact in FP32 pairs
+                    CSum cs;
+                    cs.hi = (float)du[i];
+#pragma unroll
+                    for (int jj = 0; jj < s; ++jj) {
+                        const float ch = f_hi(tab::RODAS5P_C(s, jj)), cl = f_lo(tab::RODAS5P_C(s, jj));
+                        const float wh = ch * (float)invdt;
+                        const float wl = fmaf(cl, (float)invdt, fmaf(ch, (float)invdt, -wh));
+                        cs.add_pair(wh, wl, (float)c.ks[jj][i]);
+                    }
+                    r[i] = (R)cs.value();
+                }
             }
             wsolve<R, C>(c, r, invdtgamma);
 #pragma unroll
@@ -243,30 +257,44 @@ struct Rodas5PAlg {
 #pragma unroll
                 for (int jj = 0; jj < 7; ++jj) acc = FMA((R)tab::RODAS5P_A(7, jj), c.ks[jj][i], acc);
                 Acc<R>::set(u[i], ulo[i], FMA(R(1), c.ks[7][i], acc));
-            } else {                // increment in FP32, added to the compensated solution
-                R inc = R(0);
+            } else {                // compensated increment, added to the compensated solution
+                CSum cs;
 #pragma unroll
-                for (int jj = 0; jj < 7; ++jj) inc = FMA((R)tab::RODAS5P_A(7, jj), c.ks[jj][i], inc);
-                inc = FMA(R(1), c.ks[7][i], inc);
-                Acc<R>::update(u[i], ulo[i], R(1), inc, up[i], uplo[i]);
+                for (int jj = 0; jj < 7; ++jj) cs.add(tab::RODAS5P_A(7, jj), (float)c.ks[jj][i]);
+                cs.add(1.0, (float)c.ks[7][i]);
+                Acc<R>::update(u[i], ulo[i], R(1), (R)cs.value(), up[i], uplo[i]);
             }
         }
-        const typename Ctl<R>::T EEst = error_norm<R, L, C>(c.ks[7], up, u, abstol, reltol, g);
+        return error_norm<R, L, C>(c.ks[7], up, u, abstol, reltol, g);
+    }
+
+    // Dense coefficients k_j = sum_i H[j,i] ks_i (rosenbrock_perform_step.jl:811-815),
+    // formed only on steps that interpolate a save (same operations as forming them
+    // every step, since ks is still the accepted step's).
+    template <class R, int C>
+    __device__ static void dense(Cache<R, C>& c) {
 #pragma unroll
         for (int jd = 0; jd < 3; ++jd)
 #pragma unroll
             for (int i = 0; i < C; ++i) {
-                R acc = R(0);
+                if (sizeof(R) == 8) {
+                    R acc = R(0);
 #pragma unroll
-                for (int q = 0; q < 8; ++q) acc = FMA((R)tab::RODAS5P_H(jd, q), c.ks[q][i], acc);
-                c.dk[jd][i] = acc;
+                    for (int q = 0; q < 8; ++q) acc = FMA((R)tab::RODAS5P_H(jd, q), c.ks[q][i], acc);
+                    c.dk[jd][i] = acc;
+                } else {
+                    CSum cs;
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) cs.add(tab::RODAS5P_H(jd, q), (float)c.ks[q][i]);
+                    c.dk[jd][i] = (R)cs.value();
+                }
             }
-        return EEst;
     }
 
     template <class Model, class R, int L, int C>
     __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, double thd, double, double, const R* y0,
                                        const R* y0lo, const R* y1, const R* y1lo, const R*, const Group<L>&) {
+        dense<R, C>(c);
         const R th = (R)thd, th1 = R(1) - th;
 #pragma unroll
         for (int i = 0; i < C; ++i) {

@@ -1,0 +1,125 @@
+"""
+    EnsembleGB300
+
+SciML ensemble algorithm that runs every trajectory of an `EnsembleProblem` on
+one GB300 through `libode_b200.so` (C ABI in `include/ode_gb300.h`).
+
+    using OrdinaryDiffEq, EnsembleGB300
+    prob = ODEProblem(GB300Model(:robertson), [1.0, 0.0, 0.0], (0.0, 1e5), [0.04, 3e7, 1e4])
+    eprob = EnsembleProblem(prob; prob_func = (prob, ctx) -> remake(prob; p = prob.p .* 2.0 .^ (2rand(ctx.rng, 3) .- 1)))
+    sim = solve(eprob, Rodas5P(), EnsembleGB300(); trajectories = 100_000,
+                saveat = 10 .^ range(-5, 5; length = 20), reltol = 1e-6, abstol = 1e-10)
+
+Right-hand sides are device functions compiled into the library and named by
+`GB300Model` (:linear, :lorenz, :robertson, :duffing_chain, :brusselator_1d);
+arbitrary Julia closures cannot run on the device.
+"""
+module EnsembleGB300Ext
+
+using SciMLBase
+import OrdinaryDiffEqTsit5: Tsit5
+import OrdinaryDiffEqVerner: Vern7
+import OrdinaryDiffEqRosenbrock: Rodas5P
+
+export EnsembleGB300, GB300Model
+
+const LIB = get(ENV, "ODE_GB300_LIB", joinpath(@__DIR__, "..", "lib", "libode_b200.so"))
+
+const MODEL_IDS = Dict(:linear => 0, :lorenz => 1, :robertson => 2, :duffing_chain => 3, :brusselator_1d => 4)
+const N_PARAMS = Dict(0 => 1, 1 => 3, 2 => 3, 3 => 3, 4 => 3)
+
+"""Marker right-hand side naming a model compiled into the library."""
+struct GB300Model
+    name::Symbol
+end
+(m::GB300Model)(du, u, p, t) = error("GB300Model($(m.name)) only runs on the device")
+
+struct EnsembleGB300 <: SciMLBase.EnsembleAlgorithm
+    precision::Symbol      # :fp64 or :mixed
+    device::Int
+    lanes_per_traj::Int
+    scheduler::Int
+end
+EnsembleGB300(; precision = :fp64, device = 0, lanes_per_traj = 0, scheduler = 0) =
+    EnsembleGB300(precision, device, lanes_per_traj, scheduler)
+
+# Mirrors of the C structs (include/ode_gb300.h).
+struct ProblemDesc
+    model_id::Int32; alg_id::Int32; n_states::Int32; n_params::Int32; precision::Int32; reserved::Int32
+end
+mutable struct Options
+    reltol::Float64; abstol::Float64; dtmax::Float64; dtmin::Float64; dt::Float64; maxiters::Int64
+    save_start::Int32; save_end::Int32; save_end_user::Int32; saveat_scalar::Int32; nsave::Int32
+    saveat_per_traj::Int32; qmax_first_step::Float64; qmax::Float64; lanes_per_traj::Int32
+    scheduler::Int32; block_size::Int32; ir_sweeps::Int32
+end
+struct Stats
+    nf::Int64; njacs::Int64; nw::Int64; nsolve::Int64; naccept::Int64; nreject::Int64
+end
+
+alg_id(::Tsit5) = Int32(0)
+alg_id(::Vern7) = Int32(1)
+alg_id(::Rodas5P) = Int32(2)
+
+const RETCODES = (SciMLBase.ReturnCode.Default, SciMLBase.ReturnCode.Success, SciMLBase.ReturnCode.MaxIters,
+                  SciMLBase.ReturnCode.DtNaN, SciMLBase.ReturnCode.DtLessThanMin, SciMLBase.ReturnCode.Unstable,
+                  SciMLBase.ReturnCode.Terminated)
+
+const HANDLES = Dict{Int, Ptr{Cvoid}}()
+function handle(dev)
+    get!(HANDLES, dev) do
+        h = Ref{Ptr{Cvoid}}(C_NULL)
+        rc = ccall((:ode_create, LIB), Cint, (Cint, Csize_t, Ref{Ptr{Cvoid}}), dev, 0, h)
+        rc == 0 || error("ode_create failed: ", unsafe_string(ccall((:ode_last_error, LIB), Cstring, (Ptr{Cvoid},), C_NULL)))
+        h[]
+    end
+end
+
+function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem, alg::Union{Tsit5, Vern7, Rodas5P},
+                           ens::EnsembleGB300; trajectories, saveat = Float64[], reltol = 1e-3, abstol = 1e-6,
+                           dt = 0.0, dtmax = 0.0, dtmin = 0.0, maxiters = 1_000_000, save_start = nothing,
+                           save_end = nothing, seed = 0, kwargs...)
+    t0 = time()
+    N = trajectories
+    probs = [eprob.prob_func(eprob.prob, SciMLBase.EnsembleContext(i, 1, seed)) for i in 1:N]
+    f = probs[1].f.f
+    f isa GB300Model || error("EnsembleGB300 needs an ODEFunction wrapping a GB300Model")
+    model = MODEL_IDS[f.name]
+    n = maximum(length(p.u0) for p in probs)
+    npar = N_PARAMS[model]
+    # C layout x[i*N + j] (trajectory fastest) is Julia's column-major (N, n) array
+    u0 = zeros(N, n); ps = zeros(N, npar); ts = zeros(N, 2)
+    for (j, p) in enumerate(probs)
+        u0[j, 1:length(p.u0)] .= p.u0
+        ps[j, :] .= p.p
+        ts[j, 1], ts[j, 2] = p.tspan
+    end
+    npt = all(length(p.u0) == n for p in probs) ? C_NULL : Int32[length(p.u0) for p in probs]
+    # saveat rules of lib/OrdinaryDiffEqCore/src/solve.jl:141-143,596-599,1103-1124
+    scalar = saveat isa Number
+    sv = scalar ? collect(probs[1].tspan[1] + saveat:saveat:probs[1].tspan[2]) : sort(collect(Float64, saveat))
+    ss = save_start === nothing ? (isempty(saveat) || scalar || probs[1].tspan[1] in sv) : save_start
+    se = save_end === nothing ? (isempty(saveat) || scalar || probs[1].tspan[2] in sv) : save_end
+    o = Options(reltol, abstol, dtmax, dtmin, dt, maxiters, ss, se, save_end === nothing ? -1 : Int32(save_end),
+                scalar, length(sv), 0, 0.0, 0.0, ens.lanes_per_traj, ens.scheduler, 0, -1)
+    d = ProblemDesc(model, alg_id(alg), n, npar, ens.precision === :mixed ? 1 : 0, 0)
+    cap = length(sv) + 2
+    t_out = fill(NaN, N, cap); u_out = fill(NaN, N, n, cap)   # [(s*n + i)*N + j] -> u_out[j, i, s]
+    nsaved = zeros(Int32, N); rc = zeros(Int32, N); st = Vector{Stats}(undef, N)
+    status = ccall((:ode_solve_ensemble, LIB), Cint,
+                   (Ptr{Cvoid}, Ref{ProblemDesc}, Ref{Options}, Int64, Ptr{Int32}, Ptr{Float64}, Ptr{Float64},
+                    Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Int32}, Ptr{Int32}, Ptr{Stats}),
+                   handle(ens.device), d, o, N, npt, u0, ps, ts, sv, t_out, u_out, nsaved, rc, st)
+    status == 0 || error("ode_solve_ensemble: ", unsafe_string(ccall((:ode_last_error, LIB), Cstring, (Ptr{Cvoid},), handle(ens.device))))
+    sols = map(1:N) do j
+        k = nsaved[j]
+        nj = length(probs[j].u0)
+        us = [u_out[j, 1:nj, s] for s in 1:k]
+        stats = SciMLBase.DEStats(st[j].nf, 0, 0, st[j].nsolve, st[j].nw, st[j].njacs, 0, 0, 0, 0,
+                                  st[j].naccept, st[j].nreject, 0.0)
+        SciMLBase.build_solution(probs[j], alg, t_out[j, 1:k], us; retcode = RETCODES[rc[j] + 1], stats)
+    end
+    SciMLBase.EnsembleSolution(sols, time() - t0, true)
+end
+
+end # module

@@ -64,6 +64,26 @@ def oracle(model, alg, u0, p, tspan, saveat, reltol, abstol, n_per_traj=None, **
                             saveat_scalar=sv.scalar, **kw)
 
 
+def truth(model, u0, p, tspan, saveat, n_per_traj=None, stiff=False):
+    """Ground truth: FP64 Vern9 at reltol = abstol = 1e-14 (Rodas5P at reltol 1e-12,
+    abstol 1e-16 for stiff models), every save hit exactly as a stop time."""
+    sv = resolve_saveat(saveat, tspan)
+    alg, rt, at = (O.RODAS5P, 1e-12, 1e-16) if stiff else (O.VERN9, 1e-14, 1e-14)
+    return O.solve_ensemble(alg, MODEL[model], u0, p, tspan, sv.values, rt, at, n_per_traj=n_per_traj,
+                            saveat_per_traj=sv.per_traj, save_start=sv.save_start, save_end=sv.save_end,
+                            save_end_user=sv.save_end_user, saveat_given=sv.nsave > 0, saveat_scalar=sv.scalar,
+                            saveat_as_tstops=True)
+
+
+def err_vs(g, ref, reltol, abstol):
+    """Per-trajectory worst save error of g against ref, in units of reltol*|ref| + abstol."""
+    ns = int(ref["nsaved"].max())
+    ru, gu = ref["u"][:ns], g["u"][:ns]
+    mask = ~np.isnan(ru)
+    r = np.where(mask, np.abs(gu - ru) / (reltol * np.abs(ru) + abstol), 0.0)
+    return r.max(axis=(0, 1))
+
+
 def compare(g, o, reltol, abstol, factor=10.0, step_slack=1):
     """Saves agree within factor*(reltol*|u| + abstol); accepted steps within step_slack.
     Returns a dict of agreement statistics."""
