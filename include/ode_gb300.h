@@ -174,6 +174,27 @@ int ode_last_kernel_ms(const ode_handle* h, double* ms);
  * trajectory, for tuning and diagnostics.  Returns the count written. */
 int ode_query_variants(int alg, int model, int precision, int n, int32_t* lanes, int32_t cap);
 
+/* Allocation-free ensemble solve on DEVICE buffers, enqueued on cuda_stream
+ * (NULL: the legacy default stream).  No counterpart in the reference: it is
+ * for callers that cannot call cudaMalloc (a framework's caching allocator
+ * owns the device, or the caller runs under a fixed memory budget), so it
+ * needs no handle and allocates nothing.  The work counters and the
+ * size-class index list of the persistent kernels live in one fixed device
+ * array inside the library (8 MiB + 256 B, held by every GPU that loads the
+ * library until exit), so n_per_traj_dev calls take at most 2^20
+ * trajectories (larger requests fail with ODE_E_INVALID); uniform-size calls
+ * have no limit.  The first call on a device resolves the array's address
+ * with that device current; make that first call before any stream capture.
+ * Every call shares the array: calls whose work overlaps on the GPU (two
+ * streams, or two host threads) race on it and must be serialised by the
+ * caller.  Same layouts and results as ode_solve_ensemble_device; returns
+ * once the work is enqueued (uneven-size calls synchronise the stream once
+ * to size the buckets). */
+int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_options* o, int64_t ntraj,
+                               const int32_t* n_per_traj_dev, const double* u0, const double* p,
+                               const double* tspan, const double* saveat, double* t_out, double* u_out,
+                               int32_t* nsaved, int32_t* retcode, ode_stats* stats, void* cuda_stream);
+
 /* Measured FMA throughput (FLOP/s, 2 per FMA) of the FP64 (precision =
  * ODE_PREC_FP64) or FP32 (ODE_PREC_MIXED) pipe of `device`: the roofline
  * denominator for the integrator kernels, which are bound by that pipe. */

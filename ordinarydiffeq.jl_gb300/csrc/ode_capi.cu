@@ -791,3 +791,160 @@ int ode_query_variants(int alg, int model, int precision, int n, int32_t* lanes,
 }
 
 }  // extern "C"
+
+// ============================================================== allocation-free entry point
+// For callers that must not allocate device memory: code running inside a
+// framework whose caching allocator owns the GPU, callers under a strict
+// memory budget, or hosts whose only device call surface is kernel launches
+// and copies.  The scratch the bucketed persistent kernels need (work
+// counters, per-size-class counts and offsets, the bucketed trajectory
+// indices) lives in one file-scope device array instead of handle-owned
+// cudaMalloc memory.
+namespace {
+
+// At most kNoAllocMaxTraj trajectories per call when per-trajectory sizes are
+// given (the bucket index list); uniform-size calls only use the counters.
+constexpr long long kNoAllocMaxTraj = 1LL << 20;
+// [0, 8) work counters, [8, 16) class counts, [16, 24) class cursors,
+// [32, 32 + kNoAllocMaxTraj) bucketed trajectory indices.  8 MiB + 256 B,
+// held by every GPU that loads the library until the process exits.
+static __device__ __align__(256) unsigned long long g_noalloc_scratch[32 + kNoAllocMaxTraj];
+
+std::mutex g_noalloc_mu;
+unsigned long long* g_noalloc_ptr[64] = {};
+
+// Device address of the scratch for the current device, resolved once per
+// device (with that device current) and cached.
+int noalloc_scratch(int dev, unsigned long long** out) {
+    if (dev < 0 || dev >= 64) return fail(nullptr, ODE_E_INVALID, "device ordinal out of range");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess || ptr == nullptr)
+            return fail(nullptr, ODE_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = (unsigned long long*)ptr;
+    }
+    *out = g_noalloc_ptr[dev];
+    return ODE_OK;
+}
+
+int noalloc_launch(const KernelVariant* v, EnsembleArgs a, unsigned long long* queue, int sm_count, cudaStream_t s) {
+    if (a.count <= 0) return ODE_OK;
+    const int block = 128;
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v->fn, block, 0);
+    if (e != cudaSuccess) return fail(nullptr, ODE_E_CUDA, std::string("occupancy: ") + cudaGetErrorString(e));
+    if (per_sm <= 0) per_sm = 1;
+    long long want = (a.count * v->lanes + block - 1) / block;
+    int grid = (int)std::min<long long>((long long)per_sm * sm_count, want);
+    if (grid < 1) grid = 1;
+    a.persistent = 1;
+    a.queue = queue;
+    v->launch(a, grid, block, 0, s);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(nullptr, ODE_E_CUDA, std::string("launch ") + v->name + ": " + cudaGetErrorString(e));
+    return ODE_OK;
+}
+
+}  // namespace
+
+extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_options* o, int64_t N,
+                                          const int32_t* npt_dev, const double* u0, const double* p,
+                                          const double* tspan, const double* saveat, double* t_out,
+                                          double* u_out, int32_t* nsaved, int32_t* retcode, ode_stats* stats,
+                                          void* cuda_stream) {
+    if (!d || !o) return fail(nullptr, ODE_E_INVALID, "null problem or options");
+    if (N < 0) return fail(nullptr, ODE_E_INVALID, "negative trajectory count");
+    if (npt_dev && N > kNoAllocMaxTraj) {
+        char buf[160];
+        std::snprintf(buf, sizeof buf,
+                      "ode_solve_ensemble_noalloc: %lld trajectories with per-trajectory sizes exceed the "
+                      "fixed scratch maximum of %lld",
+                      (long long)N, (long long)kNoAllocMaxTraj);
+        return fail(nullptr, ODE_E_INVALID, buf);
+    }
+    if (d->alg_id < ODE_TSIT5 || d->alg_id > ODE_RODAS5P ||
+        (d->precision != ODE_PREC_FP64 && d->precision != ODE_PREC_MIXED) ||
+        d->model_id < ODE_MODEL_LINEAR || d->model_id > ODE_MODEL_BRUSSELATOR_1D || d->n_states <= 0 ||
+        d->n_params != model_nparams(d->model_id) || !(o->reltol > 0) || !(o->abstol >= 0) || o->nsave < 0)
+        return fail(nullptr, ODE_E_INVALID, "invalid problem description or options");
+    if (npt_dev && d->model_id != ODE_MODEL_DUFFING_CHAIN)
+        return fail(nullptr, ODE_E_UNSUPPORTED, "per-trajectory sizes are supported for DUFFING_CHAIN");
+    if (N == 0) return ODE_OK;
+    int dev = 0, sm_count = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return fail(nullptr, ODE_E_CUDA, std::string("device query: ") + cudaGetErrorString(e));
+    unsigned long long* scratch = nullptr;
+    int rc = noalloc_scratch(dev, &scratch);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)cuda_stream;
+
+    EnsembleArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.N = N;
+    a.count = N;
+    a.nmax = d->n_states;
+    a.u0 = u0;
+    a.p = p;
+    a.tspan = tspan;
+    a.saveat = saveat;
+    a.nsave = o->nsave;
+    a.saveat_per_traj = o->saveat_per_traj;
+    a.nsave_cap = o->nsave + 2;
+    a.t_out = t_out;
+    a.u_out = u_out;
+    a.nsaved = nsaved;
+    a.retcode = retcode;
+    a.stats = (OdeStatsDev*)stats;
+    a.reltol = o->reltol;
+    a.abstol = o->abstol;
+    a.dtmax = o->dtmax;
+    a.dtmin = o->dtmin;
+    a.dt = o->dt;
+    a.maxiters = o->maxiters > 0 ? o->maxiters : 1000000;
+    a.save_start = o->save_start;
+    a.save_end = o->save_end;
+    a.save_end_user = o->save_end_user;
+    a.saveat_given = o->nsave > 0;
+    a.saveat_scalar = o->saveat_scalar;
+    a.qmax_first_step = o->qmax_first_step;
+    a.qmax = o->qmax;
+    a.ir_sweeps = o->ir_sweeps < 0 ? 0 : o->ir_sweeps;
+    a.abort_flag = nullptr;
+
+    // Counters must start at zero on every call (the array keeps the last call's contents).
+    e = cudaMemsetAsync(scratch, 0, 32 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return fail(nullptr, ODE_E_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
+    if (npt_dev == nullptr) {
+        const KernelVariant* v = find_variant(d->alg_id, d->model_id, d->precision, d->n_states, o->lanes_per_traj);
+        if (!v) return fail(nullptr, ODE_E_UNSUPPORTED, "no compiled kernel for this problem");
+        return noalloc_launch(v, a, scratch, sm_count, s);
+    }
+    long long* order = (long long*)(scratch + 32);
+    const int gb = (int)((N + 255) / 256);
+    bucket_count<<<gb, 256, 0, s>>>(npt_dev, N, scratch + 8);
+    unsigned long long hc[8] = {0};
+    e = cudaMemcpyAsync(hc, scratch + 8, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(nullptr, ODE_E_CUDA, std::string("bucket counts: ") + cudaGetErrorString(e));
+    unsigned long long off[8] = {0};
+    unsigned long long acc = 0;
+    for (int k = 0; k < 5; ++k) { off[k] = acc; acc += hc[k]; }
+    e = cudaMemcpyAsync(scratch + 16, off, 5 * sizeof(unsigned long long), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(nullptr, ODE_E_CUDA, std::string("bucket offsets: ") + cudaGetErrorString(e));
+    bucket_scatter<<<gb, 256, 0, s>>>(npt_dev, N, scratch + 16, order);
+    for (int k = 0; k < 5; ++k) {
+        if (hc[k] == 0) continue;
+        const KernelVariant* v = find_variant(d->alg_id, d->model_id, d->precision, kClassN[k], 0);
+        if (!v) return fail(nullptr, ODE_E_UNSUPPORTED, "no compiled kernel for a Duffing size class");
+        EnsembleArgs ac = a;
+        ac.order = order + off[k];
+        ac.count = (long long)hc[k];
+        rc = noalloc_launch(v, ac, scratch + k, sm_count, s);
+        if (rc) return rc;
+    }
+    return ODE_OK;
+}

@@ -66,6 +66,8 @@ SIGNATURES = {
     "ode_last_kernel_ms": (C.c_int, [_VP, _DP]),
     "ode_query_variants": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _IP, C.c_int32]),
     "ode_measure_fma_peak": (C.c_int, [C.c_int, C.c_int, _DP]),
+    "ode_solve_ensemble_noalloc": (C.c_int, [C.POINTER(ProblemDesc), C.POINTER(Options), C.c_int64, _VP, _VP,
+                                             _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
 }
 
 _lib = None
