@@ -38,7 +38,57 @@ CONFIGS = {
                 1_000_000),
     "brusselator": ("Brusselator-1D 32 cells (64 states), Rodas5P, reltol 1e-5 abstol 1e-8, tspan (0,10)",
                     65_536),
+    "serving": ("open-loop Poisson request stream; each request 1-4096 trajectories (log-uniform) of Lorenz/Tsit5, "
+                "Robertson/Rodas5P or Brusselator-1D (8/16/32 cells)/Rodas5P, reltol 10^U(-8,-4)", 0),
 }
+SERVE_HBM_BUDGET = 8 << 30
+
+
+def serving_block(args, local, rates, seconds):
+    """Continuous-batching serving under open-loop Poisson arrivals (one Server,
+    fixed HBM budget, precision chosen per request from its reltol)."""
+    from odegb300.serving import MIXED_MIN_RELTOL, Server, run_open_loop, serving_mix
+    reqs = serving_mix(2000, seed=3)
+    out = []
+    with Server(device=local, hbm_budget=SERVE_HBM_BUDGET, slots=args.serve_slots) as srv:
+        run_open_loop(srv, reqs[-40:], rate=200.0, duration=0.2, drain_timeout=30.0)   # module load, pools
+        for r in rates:
+            out.append(run_open_loop(srv, reqs, rate=r, duration=seconds, drain_timeout=max(15.0, 3 * seconds)))
+        st = srv.stats()
+    return {"workload": CONFIGS["serving"][0], "hbm_budget_bytes": SERVE_HBM_BUDGET, "slots": args.serve_slots,
+            "precision": "mixed when reltol >= %g, else fp64" % MIXED_MIN_RELTOL,
+            "latency": "completion (outputs in the caller's host buffers) minus scheduled arrival",
+            "rates": out, "rejected_total": st["rejected"]}
+
+
+def run_serving(args, rank, local):
+    if rank != 0:
+        return
+    import torch
+    torch.cuda.set_device(local)
+    rates = [float(x) for x in (args.serve_rates or "100,300,1000,3000,10000").split(",")]
+    blk = serving_block(args, local, rates, args.serve_seconds or 5.0)
+    best = max(blk["rates"], key=lambda m: m["trajectories_per_s"] or 0.0)
+    reqs = sum(m["completed"] for m in blk["rates"])
+    print(json.dumps({
+        "metric": "trajectories/sec at equal accuracy, mixed vs plain FP64 GPU; p50/p99 latency",
+        "value": best["trajectories_per_s"], "unit": "trajectories/s", "n_gpus": 1, "steps": len(rates),
+        "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 / f32 stages per request", "data": "synthetic (seeded request mix)",
+        "config": {"workload": CONFIGS["serving"][0], "rates_req_per_s": rates,
+                   "seconds_per_rate": args.serve_seconds or 5.0},
+        "serving": blk,
+        "e2e": {"value": best["trajectories_per_s"], "unit": "trajectories/s", "note": "host buffers in and out",
+                "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
+        "gpu_launches": None, "requests_completed": reqs}))
+
+
+# DRAM bytes (read + write) per launch of the integrator kernel(s), from one ncu
+# capture of the same kernels (profiles/rodas5p_robertson_100k.md,
+# profiles/vern7_duffing_uneven_20k.md; the Duffing figure is the 20,000-
+# trajectory capture scaled by 50 to the 1,000,000-trajectory launch).
+NCU_TRAFFIC = {("robertson", "fp64"): 17.11e6, ("robertson", "mixed"): 17.07e6,
+               ("duffing", "fp64"): 50 * 369.4e6, ("duffing", "mixed"): 50 * 368.7e6}
 
 
 def parse():
@@ -53,6 +103,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-small", action="store_true",
                     help="one small FP64+mixed solve pair for ncu captures (no JSON line)")
+    ap.add_argument("--serve-rates", default="",
+                    help="comma-separated Poisson request rates (req/s) of the serving measurement")
+    ap.add_argument("--serve-seconds", type=float, default=0.0, help="arrival window per rate")
+    ap.add_argument("--serve-slots", type=int, default=32, help="concurrent device slots of the server")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
     return ap.parse_args()
 
 
@@ -202,7 +257,7 @@ def run_gb300(args, world, rank, local, dist):
     ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None
 
     def solve_device(prec):
-        ens = odegb300.EnsembleGB300(precision=prec)
+        ens = odegb300.EnsembleGB300(precision=prec, ir_sweeps=wl.get("ir_sweeps", -1) if prec == "mixed" else -1)
         o = _options(wl["reltol"], wl["abstol"], None, None, None, 1000000, sv, ens, None, None)
         d = _lib.ProblemDesc(model, alg.alg_id, n, wl["p"].shape[0], ens.prec_id(), 0)
         stream = C.c_void_p(work.cuda_stream)
@@ -296,7 +351,7 @@ def run_gb300(args, world, rank, local, dist):
 
     # end-to-end through the public host-buffer call
     from odegb300.ensemble import solve_arrays
-    ens = odegb300.EnsembleGB300(precision=best)
+    ens = odegb300.EnsembleGB300(precision=best, ir_sweeps=wl.get("ir_sweeps", -1) if best == "mixed" else -1)
     kw = dict(n_per_traj=npt) if npt is not None else {}
     for _ in range(max(1, min(args.warmup, 2))):
         solve_arrays(wl["model"], alg, ens, wl["u0"], wl["p"], wl["tspan"], wl["saveat"], wl["reltol"],
@@ -315,6 +370,11 @@ def run_gb300(args, world, rank, local, dist):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(wl, N, args.cpu_seconds)
+    serving = None
+    if rank == 0 and not args.no_serving and not args.profile_small:
+        rates = [float(x) for x in (args.serve_rates or "100,300").split(",")]
+        serving = serving_block(args, local, rates, args.serve_seconds or 2.0)
+    hbm_bytes = h2d + d2h   # bytes the kernel reads (inputs) and writes (outputs) per solve
 
     if rank == 0:
         line = {
@@ -334,12 +394,17 @@ def run_gb300(args, world, rank, local, dist):
                     "d2h_bytes_per_step": int(d2h)},
             "roofline": {"bound": "fp64 pipe" if best == "fp64" else "fp32 pipe", "achieved": achieved / 1e12,
                          "peak": peak.value / 1e12, "unit": "TFLOP/s", "frac": achieved / peak.value if peak.value else None,
-                         "traffic": None, "flops_per_attempt": fl, "attempted_steps": R["attempts"],
+                         "traffic": NCU_TRAFFIC.get((args.config, best)) if N == N0 else None,
+                         "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
+                         "flops_per_attempt": fl, "attempted_steps": R["attempts"],
                          "peak_source": "ode_measure_fma_peak (FMA-chain kernel, this GPU)",
                          "fp64_peak_tflops": fp64_peak.value / 1e12},
+            "hbm": {"achieved_gbs": hbm_bytes / (R["ms"] * 1e-3) / 1e9, "bytes_per_solve": int(hbm_bytes),
+                    "note": "algorithmic bytes (inputs read + outputs written) / device time; not the bound"},
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": R["launches"],
+            "serving": serving,
         }
         print(json.dumps(line))
 
@@ -363,6 +428,10 @@ def cpu_baseline(wl, N, target_s):
 
 def run_reference(args, world, rank):
     if rank != 0:
+        return
+    if args.config == "serving":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving loop (EnsembleThreads "
+                                                              "solves one ensemble per call)"}))
         return
     desc_name, N0 = CONFIGS[args.config]
     N = args.trajectories or N0
@@ -399,6 +468,8 @@ def main():
     world, rank, local, dist = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.config == "serving":
+        run_serving(args, rank, local)
     else:
         run_gb300(args, world, rank, local, dist)
     if dist is not None:

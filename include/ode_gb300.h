@@ -120,9 +120,13 @@ const char* ode_status_string(int status);
 int ode_abi_version(void);
 
 /* Synchronous ensemble solve on caller-owned HOST buffers (layouts above).
- * n_per_traj (may be NULL) gives each trajectory's state count (<= n_states,
- * DUFFING_CHAIN only); trajectories are grouped by size on the device.
- * Outputs are written before return.  stats and t_out may be NULL. */
+ * n_per_traj (may be NULL) gives each trajectory's state count (DUFFING_CHAIN
+ * only; each one of 4, 8, 16, 32, 64 and <= n_states): trajectories are
+ * bucketed by size on the device and every size class is integrated in one
+ * persistent launch.  On the device-buffer entry points a trajectory of any
+ * other size is not integrated (nsaved 0, retcode ODE_RC_DEFAULT); the host
+ * entry point rejects it.  Outputs are written before return.  stats and
+ * t_out may be NULL. */
 int ode_solve_ensemble(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int64_t ntraj,
                        const int32_t* n_per_traj, const double* u0, const double* p, const double* tspan,
                        const double* saveat, double* t_out, double* u_out, int32_t* nsaved,
@@ -150,6 +154,13 @@ int ode_submit(ode_handle* h, const ode_problem_desc* d, const ode_options* o, i
 int ode_poll(ode_handle* h, uint64_t ticket, int32_t* done);
 /* Wait at most timeout_s seconds (< 0: forever). */
 int ode_wait(ode_handle* h, uint64_t ticket, double timeout_s);
+/* The next finished request in completion order, waiting at most timeout_s
+ * seconds (< 0: forever, 0: do not wait).  *ticket = 0 when none finished in
+ * time.  status: the request's result code; times[0..2]: submit, start on
+ * the device and completion (outputs in place), CLOCK_MONOTONIC seconds.
+ * Releases the ticket like a completed ode_poll.  No reference counterpart
+ * (serving). */
+int ode_next_completed(ode_handle* h, double timeout_s, uint64_t* ticket, int32_t* status, double* times);
 
 typedef struct {
     int64_t submitted, admitted, completed, rejected, queued, running;
@@ -180,7 +191,7 @@ int ode_query_variants(int alg, int model, int precision, int n, int32_t* lanes,
  * owns the device, or the caller runs under a fixed memory budget), so it
  * needs no handle and allocates nothing.  The work counters and the
  * size-class index list of the persistent kernels live in one fixed device
- * array inside the library (8 MiB + 256 B, held by every GPU that loads the
+ * array inside the library (8 MiB + 512 B, held by every GPU that loads the
  * library until exit), so n_per_traj_dev calls take at most 2^20
  * trajectories (larger requests fail with ODE_E_INVALID); uniform-size calls
  * have no limit.  The first call on a device resolves the array's address
@@ -188,8 +199,8 @@ int ode_query_variants(int alg, int model, int precision, int n, int32_t* lanes,
  * Every call shares the array: calls whose work overlaps on the GPU (two
  * streams, or two host threads) race on it and must be serialised by the
  * caller.  Same layouts and results as ode_solve_ensemble_device; returns
- * once the work is enqueued (uneven-size calls synchronise the stream once
- * to size the buckets). */
+ * once the work is enqueued (uneven-size calls of a method without a
+ * one-launch class kernel synchronise the stream once to size the buckets). */
 int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_options* o, int64_t ntraj,
                                const int32_t* n_per_traj_dev, const double* u0, const double* p,
                                const double* tspan, const double* saveat, double* t_out, double* u_out,

@@ -185,11 +185,18 @@ __device__ __forceinline__ ff operator*(ff a, ff b) {
 template <int L> struct Group {
     unsigned mask;
     int lane;   // lane within the group
+    int base;   // warp lane of the group's lane 0
     __device__ __forceinline__ Group() {
         int wl = threadIdx.x & 31;
         lane = wl % L;
-        int base = wl - lane;
+        base = wl - lane;
         mask = (L == 32) ? 0xffffffffu : (((1u << L) - 1u) << base);
+    }
+    // bit l set when lane l of the group has b
+    __device__ __forceinline__ unsigned ballot(bool b) const {
+        if (L == 1) return b ? 1u : 0u;
+        unsigned m = __ballot_sync(mask, b);
+        return L == 32 ? m : (m >> base) & ((1u << L) - 1u);
     }
     template <class T> __device__ __forceinline__ T sum(T v) const {
 #pragma unroll

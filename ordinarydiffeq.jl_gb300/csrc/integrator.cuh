@@ -235,7 +235,7 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
 
     auto save_point = [&](double ts, const R* v, const R* vlo) {
         if (nsaved < a.nsave_cap) {
-            if (g.lane == 0) a.t_out[(size_t)nsaved * N + j] = ts;
+            if (g.lane == 0 && a.t_out) a.t_out[(size_t)nsaved * N + j] = ts;
 #pragma unroll
             for (int c = 0; c < C; ++c)
                 a.u_out[((size_t)nsaved * a.nmax + g.lane * C + c) * N + j] = Acc<R>::join(v[c], vlo[c]);
@@ -390,9 +390,11 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
     if (g.lane == 0) {
         a.nsaved[j] = nsaved < a.nsave_cap ? nsaved : a.nsave_cap;
         a.retcode[j] = rc;
-        OdeStatsDev* s = a.stats + j;
-        s->nf = st.nf; s->njacs = st.njacs; s->nw = st.nw; s->nsolve = st.nsolve;
-        s->naccept = st.naccept; s->nreject = st.nreject;
+        if (a.stats) {
+            OdeStatsDev* s = a.stats + j;
+            s->nf = st.nf; s->njacs = st.njacs; s->nw = st.nw; s->nsolve = st.nsolve;
+            s->naccept = st.naccept; s->nreject = st.nreject;
+        }
     }
 }
 
@@ -420,6 +422,37 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? ODEGB_MIN_BLOCKS_F32 : 1
         long long j = a.order ? a.order[idx] : (long long)idx;
         solve_trajectory<Alg, Model, R, L, C>(a, j, g);
     }
+}
+
+// Uneven-size ensembles in ONE persistent launch.  Trajectories were bucketed
+// on the device by state count; every warp works through the size classes
+// from the largest down (longest jobs first), its lane groups popping
+// trajectories of the current class from that class's device counter, so a
+// group that finishes a trajectory refills at once and the load balances
+// across classes.  At a class change the warp regroups its lanes (L depends
+// on the class), which needs the whole warp: __syncwarp between classes.
+template <class Alg, class Model, class R, int L, int C>
+__device__ __forceinline__ void drain_class(const EnsembleArgs& a, int cls) {
+    Group<L> g;
+    const unsigned long long cnt = a.class_count[cls], off = a.class_offset[cls];
+    for (;;) {
+        unsigned long long idx = 0;
+        if (g.lane == 0) idx = atomicAdd(a.class_next + cls, 1ull);
+        idx = g.bcast(idx, 0);
+        if (idx >= cnt) break;
+        solve_trajectory<Alg, Model, R, L, C>(a, a.order[off + idx], g);
+    }
+    __syncwarp();
+}
+
+// Classes n = 64, 32, 16, 8, 4 with C = 4 states per lane (L = n/4).
+template <class Alg, class Model, class R>
+__global__ void __launch_bounds__(128, 1) fused_class_kernel(EnsembleArgs a) {
+    drain_class<Alg, Model, R, 16, 4>(a, 4);
+    drain_class<Alg, Model, R, 8, 4>(a, 3);
+    drain_class<Alg, Model, R, 4, 4>(a, 2);
+    drain_class<Alg, Model, R, 2, 4>(a, 1);
+    drain_class<Alg, Model, R, 1, 4>(a, 0);
 }
 
 }  // namespace odegb

@@ -166,6 +166,49 @@ struct Brusselator {
 #pragma unroll 1
         for (int i = 0; i < N; ++i) jac_row<R>(J[i], N, i, u, p);
     }
+    // Nonzeros of the lane's own rows (cells lane*C/2 ...) of J(u), in the
+    // oracle's arithmetic; put(i, col, v) with i the lane-local row.  The
+    // neighbour columns are distinct from the cell's own for 3 cells or more.
+    template <class R, int L, int C, class Put>
+    __device__ static void jac_rows(const R* u, const R* p, const Group<L>& g, Put&& put) {
+        constexpr int NC = L * C / 2;
+        static_assert(NC >= 3, "group Jacobian assumes distinct neighbour cells");
+        const R ae = p[2] * (R(NC) * R(NC));
+#pragma unroll
+        for (int q = 0; q < C / 2; ++q) {
+            const int cell = g.lane * (C / 2) + q;
+            const int il = cell == 0 ? NC - 1 : cell - 1, ir = cell == NC - 1 ? 0 : cell + 1;
+            const R uu = u[2 * q], vv = u[2 * q + 1];
+            put(2 * q, 2 * cell, (R(2) * uu * vv - (p[1] + R(1))) - R(2) * ae);
+            put(2 * q, 2 * cell + 1, uu * uu);
+            put(2 * q, 2 * il, ae);
+            put(2 * q, 2 * ir, ae);
+            put(2 * q + 1, 2 * cell, p[1] - R(2) * uu * vv);
+            put(2 * q + 1, 2 * cell + 1, -(uu * uu) - R(2) * ae);
+            put(2 * q + 1, 2 * il + 1, ae);
+            put(2 * q + 1, 2 * ir + 1, ae);
+        }
+    }
+    // J(u) x in double-float for the lane's rows (x in FP32, u and p in
+    // double-float): the refinement residual of the mixed Rosenbrock solve.
+    template <int L, int C>
+    __device__ static void jvp(ff* out, const float* x, const ff* u, const ff* p, const Group<L>& g) {
+        constexpr int NC = L * C / 2;
+        const ff ae = p[2] * (ff(NC) * ff(NC));
+        float xul, xur, xvl, xvr;
+        chain_halo<float, L, C>(x, g, 0, xul, xur);
+        chain_halo<float, L, C>(x, g, 1, xvl, xvr);
+#pragma unroll
+        for (int q = 0; q < C / 2; ++q) {
+            const ff uu = u[2 * q], vv = u[2 * q + 1];
+            const float xuL = q > 0 ? x[2 * q - 2] : xul, xuR = q < C / 2 - 1 ? x[2 * q + 2] : xur;
+            const float xvL = q > 0 ? x[2 * q - 1] : xvl, xvR = q < C / 2 - 1 ? x[2 * q + 3] : xvr;
+            const ff uv2 = ff(2) * uu * vv, u2 = uu * uu, ae2 = ff(2) * ae;
+            const ff xu = ff(x[2 * q]), xv = ff(x[2 * q + 1]);
+            out[2 * q] = (((uv2 - (p[1] + ff(1))) - ae2) * xu + u2 * xv) + ae * (ff(xuL) + ff(xuR));
+            out[2 * q + 1] = ((p[1] - uv2) * xu - (u2 + ae2) * xv) + ae * (ff(xvL) + ff(xvR));
+        }
+    }
 };
 
 }  // namespace odegb

@@ -15,6 +15,7 @@
 #include <condition_variable>
 #include <cstdio>
 #include <cstring>
+#include <ctime>
 #include <deque>
 #include <map>
 #include <memory>
@@ -39,6 +40,8 @@ const std::vector<KernelVariant>& all_variants() {
         out.insert(out.end(), t, t + n);
         t = rodas_variants(&n);
         out.insert(out.end(), t, t + n);
+        t = rodas_group_variants(&n);
+        out.insert(out.end(), t, t + n);
         return out;
     }();
     return v;
@@ -47,10 +50,12 @@ const std::vector<KernelVariant>& all_variants() {
 int model_nparams(int model) { return model == ODE_MODEL_LINEAR ? 1 : 3; }
 
 // Default lanes per trajectory: one lane for tiny systems (registers hold the
-// whole state and stage set), else 4 states per lane so the Vern7 stage set
-// stays in registers without spilling.
+// whole state and stage set); explicit methods 4 states per lane so the Vern7
+// stage set stays in registers without spilling; Rodas5P above 8 states one
+// lane per 2 states (W in shared memory, rows spread over the group).
 int default_lanes(int alg, int n) {
     if (n <= 4 || (n <= 8 && alg == ODE_RODAS5P)) return 1;
+    if (alg == ODE_RODAS5P) return std::min(32, n / 2);
     return std::min(32, n / 4);
 }
 
@@ -114,6 +119,10 @@ struct ode_handle {
     long long n_submitted = 0, n_admitted = 0, n_completed = 0, n_rejected = 0;
     std::vector<Ctx> slot_ctx;
     std::vector<int> slot_busy;
+    std::vector<void*> slot_pinned;          // per-slot pinned staging (grow only)
+    std::vector<size_t> slot_pinned_cap;
+    std::vector<cudaEvent_t> slot_ev;        // end of the slot's current request
+    std::deque<uint64_t> completed;          // tickets in completion order
 };
 
 namespace {
@@ -202,38 +211,143 @@ EnsembleArgs make_args(ode_handle* h, const ode_problem_desc* d, const ode_optio
     return a;
 }
 
-// Bucket trajectories by state count on the device (histogram + scatter).
-__global__ void bucket_count(const int32_t* npt, long long N, unsigned long long* counts) {
-    long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= N) return;
-    int n = npt[j];
-    int c = n <= 4 ? 0 : n <= 8 ? 1 : n <= 16 ? 2 : n <= 32 ? 3 : 4;
-    atomicAdd(&counts[c], 1ull);
-}
-__global__ void bucket_scatter(const int32_t* npt, long long N, unsigned long long* cursor, long long* order) {
-    long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= N) return;
-    int n = npt[j];
-    int c = n <= 4 ? 0 : n <= 8 ? 1 : n <= 16 ? 2 : n <= 32 ? 3 : 4;
-    unsigned long long slot = atomicAdd(&cursor[c], 1ull);
-    order[slot] = j;
+// Size class of a state count: 4, 8, 16, 32, 64 -> 0..4; -1 for any other.
+__device__ __forceinline__ int size_class(int n) {
+    return n == 4 ? 0 : n == 8 ? 1 : n == 16 ? 2 : n == 32 ? 3 : n == 64 ? 4 : -1;
 }
 
-constexpr int kClassN[5] = {4, 8, 16, 32, 64};
+// Bucket trajectories by state count on the device: a histogram, then a
+// scatter of the indices into class order (class k at [offset[k],
+// offset[k] + count[k])).  Atomics are aggregated per warp (one per class).
+// Trajectories of any other size are not integrated: nsaved 0, retcode DEFAULT.
+__global__ void bucket_count(const int32_t* npt, long long N, unsigned long long* counts) {
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int c = j < N ? size_class(npt[j]) : -2;
+    if (c == -1) c = kNumClasses;
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k <= kNumClasses; ++k) {
+        const unsigned m = __ballot_sync(0xffffffffu, c == k);
+        if (m && lane == __ffs(m) - 1) atomicAdd(&counts[k], (unsigned long long)__popc(m));
+    }
+}
+__global__ void bucket_scatter(const int32_t* npt, long long N, const unsigned long long* counts,
+                               unsigned long long* cursor, unsigned long long* offsets, long long* order,
+                               int32_t* nsaved, int32_t* retcode) {
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long off[kNumClasses];
+    unsigned long long acc = 0;
+#pragma unroll
+    for (int k = 0; k < kNumClasses; ++k) { off[k] = acc; acc += counts[k]; }
+    if (blockIdx.x == 0 && threadIdx.x < kNumClasses) offsets[threadIdx.x] = off[threadIdx.x];
+    const int c = j < N ? size_class(npt[j]) : -2;
+    if (c == -1) {
+        nsaved[j] = 0;
+        retcode[j] = ODE_RC_DEFAULT;
+    }
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int k = 0; k < kNumClasses; ++k) {
+        const unsigned m = __ballot_sync(0xffffffffu, c == k);
+        if (!m) continue;
+        const int leader = __ffs(m) - 1;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(&cursor[k], (unsigned long long)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (c == k) order[off[k] + base + __popc(m & lt)] = j;
+    }
+}
+
+// Device counters of one context: [0] the work queue of a uniform launch,
+// then, for uneven ensembles, class counts (5 classes + invalid sizes), scatter
+// cursors, per-class work counters, class offsets and the per-class queues of
+// the one-kernel-per-class form.
+constexpr int kCounters = 64;
+constexpr int kOffCounts = 8, kOffCursor = 16, kOffNext = 24, kOffOffsets = 32, kOffClassQ = 40;
+constexpr const int* kClassN = kClassStates;
+
+const FusedVariant* find_fused(int alg, int model, int prec) {
+    static const std::vector<FusedVariant> all = [] {
+        std::vector<FusedVariant> out;
+        int n = 0;
+        const FusedVariant* t = fused_tsit5_variants(&n);
+        out.insert(out.end(), t, t + n);
+        t = fused_vern7_variants(&n);
+        out.insert(out.end(), t, t + n);
+        return out;
+    }();
+    for (const auto& v : all)
+        if (v.alg == alg && v.model == model && v.prec == prec) return &v;
+    return nullptr;
+}
+
+// Count + scatter of an uneven ensemble into class order (device only).
+void enqueue_bucketing(const int32_t* npt_dev, long long N, unsigned long long* ctr, long long* order,
+                       int32_t* nsaved, int32_t* retcode, cudaStream_t s) {
+    const int gb = (int)((N + 255) / 256);
+    bucket_count<<<gb, 256, 0, s>>>(npt_dev, N, ctr + kOffCounts);
+    bucket_scatter<<<gb, 256, 0, s>>>(npt_dev, N, ctr + kOffCounts, ctr + kOffCursor, ctr + kOffOffsets, order,
+                                      nsaved, retcode);
+}
+
+// Every size class in one persistent launch (grid = resident blocks x SMs).
+cudaError_t launch_fused(const FusedVariant* fv, EnsembleArgs a, unsigned long long* ctr, int sm_count,
+                         cudaStream_t s) {
+    const int block = 128;
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fv->fn, block, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm <= 0) per_sm = 1;
+    long long want = (a.N * 16 + block - 1) / block;   // enough groups for the largest class
+    int grid = (int)std::min<long long>((long long)per_sm * sm_count, std::max<long long>(want, 1));
+    a.persistent = 1;
+    a.class_count = ctr + kOffCounts;
+    a.class_offset = ctr + kOffOffsets;
+    a.class_next = ctr + kOffNext;
+    fv->launch(a, grid, block, 0, s);
+    return cudaGetLastError();
+}
 constexpr int kBlock = 128;
+
+// Block size and dynamic shared memory of a launch.  Variants that keep W in
+// shared memory default to one warp per block (finer occupancy steps).
+cudaError_t launch_geometry(const KernelVariant* v, int block, int* block_out, size_t* smem_out) {
+    if (v->lanes > 1 && block % 32 != 0) block = kBlock;
+    if (block <= 0) block = v->smem_per_group > 0 ? 32 : kBlock;
+    if (block > 128) block = 128;
+    if (v->smem_per_group > 0) {   // shrink the block until its groups' W fit in one SM
+        int dev = 0, max_optin = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (e != cudaSuccess) return e;
+        while (block > 32 && block > v->lanes && (size_t)(block / v->lanes) * v->smem_per_group > (size_t)max_optin)
+            block /= 2;
+    }
+    const size_t smem = (size_t)(block / v->lanes) * (size_t)v->smem_per_group;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(v->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    *block_out = block;
+    *smem_out = smem;
+    return cudaSuccess;
+}
 
 int launch_variant(ode_handle* h, const KernelVariant* v, EnsembleArgs a, int scheduler, int block,
                    unsigned long long* queue, cudaStream_t s) {
-    if (v->lanes > 1 && block % 32 != 0) block = kBlock;
     if (a.count <= 0) return ODE_OK;
-    if (block <= 0) block = kBlock;
-    if (block > 128) block = 128;
+    size_t smem = 0;
+    {
+        cudaError_t e = launch_geometry(v, block, &block, &smem);
+        if (e != cudaSuccess) return fail(h, ODE_E_CUDA, std::string("shared memory for ") + v->name + ": " + cudaGetErrorString(e));
+    }
     long long groups = a.count;
     bool persistent = scheduler == 2;
     int grid;
     if (persistent) {
         int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v->fn, block, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v->fn, block, smem);
         if (per_sm <= 0) per_sm = 1;
         long long want = (groups * v->lanes + block - 1) / block;
         grid = (int)std::min<long long>((long long)per_sm * h->sm_count, want);
@@ -246,7 +360,7 @@ int launch_variant(ode_handle* h, const KernelVariant* v, EnsembleArgs a, int sc
         grid = (int)((threads + block - 1) / block);
         a.persistent = 0;
     }
-    v->launch(a, grid, block, 0, s);
+    v->launch(a, grid, block, smem, s);
     h->launches++;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(h, ODE_E_CUDA, std::string("launch ") + v->name + ": " + cudaGetErrorString(e));
@@ -256,8 +370,8 @@ int launch_variant(ode_handle* h, const KernelVariant* v, EnsembleArgs a, int sc
 int ctx_init(ode_handle* h, Ctx& c, cudaStream_t s) {
     if (s) c.stream = s;
     else CUDA_TRY(h, cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
-    CUDA_TRY(h, cudaMalloc(&c.d_queue, 32 * sizeof(unsigned long long)));
-    CUDA_TRY(h, cudaMemset(c.d_queue, 0, 32 * sizeof(unsigned long long)));
+    CUDA_TRY(h, cudaMalloc(&c.d_queue, kCounters * sizeof(unsigned long long)));
+    CUDA_TRY(h, cudaMemset(c.d_queue, 0, kCounters * sizeof(unsigned long long)));
     CUDA_TRY(h, cudaEventCreate(&c.ev0));
     CUDA_TRY(h, cudaEventCreate(&c.ev1));
     for (int k = 0; k < 5; ++k) {
@@ -304,8 +418,9 @@ int run_ensemble(ode_handle* h, Ctx& c, const ode_problem_desc* d, const ode_opt
         CUDA_TRY(h, cudaEventRecord(c.ev1, s));
         return ODE_OK;
     }
-    // Uneven sizes: bucket by state count, then one persistent kernel per size
-    // class, run concurrently on the handle's class streams.
+    // Uneven sizes: bucket by state count on the device, then integrate every
+    // class in one persistent launch (no host round trip); without a fused
+    // kernel for this method, one persistent kernel per class on the class streams.
     if (d->model_id != ODE_MODEL_DUFFING_CHAIN)
         return fail(h, ODE_E_UNSUPPORTED, "per-trajectory sizes are supported for DUFFING_CHAIN");
     if ((size_t)N > c.order_cap) {
@@ -315,23 +430,29 @@ int run_ensemble(ode_handle* h, Ctx& c, const ode_problem_desc* d, const ode_opt
         CUDA_TRY(h, cudaMalloc(&c.d_order, sizeof(long long) * (size_t)N));
         c.order_cap = (size_t)N;
     }
-    unsigned long long* counts = c.d_queue + 8;
-    unsigned long long* cursor = c.d_queue + 16;
-    CUDA_TRY(h, cudaMemsetAsync(counts, 0, 8 * sizeof(unsigned long long), s));
-    int gb = (int)((N + 255) / 256);
-    bucket_count<<<gb, 256, 0, s>>>(npt_dev, N, counts);
-    unsigned long long hc[8] = {0};
-    CUDA_TRY(h, cudaMemcpyAsync(hc, counts, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(h, cudaStreamSynchronize(s));
-    unsigned long long off[5];
-    unsigned long long acc = 0;
-    for (int k = 0; k < 5; ++k) { off[k] = acc; acc += hc[k]; }
-    CUDA_TRY(h, cudaMemcpyAsync(cursor, off, 5 * sizeof(unsigned long long), cudaMemcpyHostToDevice, s));
-    bucket_scatter<<<gb, 256, 0, s>>>(npt_dev, N, cursor, c.d_order);
+    unsigned long long* ctr = c.d_queue;
+    CUDA_TRY(h, cudaMemsetAsync(ctr + kOffCounts, 0, (kCounters - kOffCounts) * sizeof(unsigned long long), s));
+    enqueue_bucketing(npt_dev, N, ctr, c.d_order, nsaved, retcode, s);
     h->launches += 2;
+    a.order = c.d_order;
+    const FusedVariant* fv = o->lanes_per_traj <= 0 ? find_fused(d->alg_id, d->model_id, d->precision) : nullptr;
+    if (fv) {
+        CUDA_TRY(h, cudaEventRecord(c.ev0, s));
+        cudaError_t e = launch_fused(fv, a, ctr, h->sm_count, s);
+        if (e != cudaSuccess) return fail(h, ODE_E_CUDA, std::string("launch ") + fv->name + ": " + cudaGetErrorString(e));
+        h->launches++;
+        CUDA_TRY(h, cudaEventRecord(c.ev1, s));
+        return ODE_OK;
+    }
+    unsigned long long hc[kNumClasses + 1] = {0};
+    CUDA_TRY(h, cudaMemcpyAsync(hc, ctr + kOffCounts, sizeof(hc), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(h, cudaStreamSynchronize(s));
+    unsigned long long off[kNumClasses];
+    unsigned long long acc = 0;
+    for (int k = 0; k < kNumClasses; ++k) { off[k] = acc; acc += hc[k]; }
     CUDA_TRY(h, cudaEventRecord(c.ev0, s));
     if (scheduler == 0) scheduler = 2;
-    for (int k = 0; k < 5; ++k) {
+    for (int k = 0; k < kNumClasses; ++k) {
         if (hc[k] == 0) continue;
         const KernelVariant* v = find_variant(d->alg_id, d->model_id, d->precision, kClassN[k], 0);
         if (!v) return fail(h, ODE_E_UNSUPPORTED, "no compiled kernel for a Duffing size class");
@@ -339,7 +460,7 @@ int run_ensemble(ode_handle* h, Ctx& c, const ode_problem_desc* d, const ode_opt
         EnsembleArgs ac = a;
         ac.order = c.d_order + off[k];
         ac.count = (long long)hc[k];
-        int rc = launch_variant(h, v, ac, scheduler, o->block_size, c.d_queue + k, c.class_streams[k]);
+        int rc = launch_variant(h, v, ac, scheduler, o->block_size, ctr + kOffClassQ + k, c.class_streams[k]);
         if (rc) return rc;
         CUDA_TRY(h, cudaEventRecord(c.class_events[k], c.class_streams[k]));
         CUDA_TRY(h, cudaStreamWaitEvent(s, c.class_events[k], 0));
@@ -349,6 +470,25 @@ int run_ensemble(ode_handle* h, Ctx& c, const ode_problem_desc* d, const ode_opt
 }
 
 size_t save_cap(const ode_options* o) { return (size_t)o->nsave + 2; }
+
+// Host-side check of per-trajectory sizes: each a size class and <= n_states.
+int check_sizes(ode_handle* h, const ode_problem_desc* d, const int32_t* npt, int64_t N) {
+    if (!npt) return ODE_OK;
+    if (d->model_id != ODE_MODEL_DUFFING_CHAIN)
+        return fail(h, ODE_E_UNSUPPORTED, "per-trajectory sizes are supported for DUFFING_CHAIN");
+    for (int64_t j = 0; j < N; ++j) {
+        const int n = npt[j];
+        bool cls = false;
+        for (int k = 0; k < kNumClasses; ++k) cls = cls || n == kClassStates[k];
+        if (!cls || n > d->n_states) {
+            char buf[160];
+            std::snprintf(buf, sizeof buf, "n_per_traj[%lld] = %d: sizes must be 4, 8, 16, 32 or 64 and <= n_states",
+                          (long long)j, n);
+            return fail(h, ODE_E_INVALID, buf);
+        }
+    }
+    return ODE_OK;
+}
 
 }  // namespace
 
@@ -374,113 +514,143 @@ struct Request {
     int slot = -1;
     size_t bytes = 0;
     void* dmem = nullptr;      // one device block for inputs and outputs
-    void* hout = nullptr;      // pinned staging for outputs
-    cudaEvent_t done_ev = nullptr;
+    double t_submit = 0, t_start = 0, t_done = 0;   // CLOCK_MONOTONIC seconds
 };
 
-size_t request_bytes(const Request& r) {
-    size_t n = (size_t)r.d.n_states, np = (size_t)r.d.n_params, cap = (size_t)r.o.nsave + 2, N = (size_t)r.N;
-    size_t in = (n + np + 2) * N * 8 + r.saveat.size() * 8 + r.npt.size() * 4;
-    size_t out = cap * N * 8 + cap * n * N * 8 + N * 8 + N * sizeof(ode_stats);
-    return in + out + 1024;
-}
-
-size_t output_bytes(const Request& r) {
-    size_t n = (size_t)r.d.n_states, cap = (size_t)r.o.nsave + 2, N = (size_t)r.N;
-    return cap * N * 8 + cap * n * N * 8 + N * 8 + N * sizeof(ode_stats) + 256;
+double mono_now() {
+    timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
 }
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-// Admit r on slot k: stage inputs, launch, copy outputs back (all async).
+// Byte offsets of one request's block: inputs first, then outputs, so each
+// direction is one contiguous copy.  The pinned staging of the slot and the
+// device block share this layout.
+struct Layout {
+    size_t u0, p, ts, sv, npt, in_end, t, u, ns, rc, st, total;
+};
+Layout layout(const Request& r) {
+    const size_t n = (size_t)r.d.n_states, np = (size_t)r.d.n_params, N = (size_t)r.N, cap = (size_t)r.o.nsave + 2;
+    Layout L;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += align256(bytes); return o; };
+    L.u0 = take(n * N * 8);
+    L.p = take(np * N * 8);
+    L.ts = take(2 * N * 8);
+    L.sv = take(std::max<size_t>(r.saveat.size(), 1) * 8);
+    L.npt = r.npt.empty() ? (size_t)-1 : take(N * 4);
+    L.in_end = off;
+    L.t = take(cap * N * 8);
+    L.u = take(cap * n * N * 8);
+    L.ns = take(N * 4);
+    L.rc = take(N * 4);
+    L.st = take(N * sizeof(ode_stats));
+    L.total = off;
+    return L;
+}
+
+size_t request_bytes(const Request& r) { return layout(r).total; }
+
+// Start r on slot k: stage the inputs in the slot's pinned buffer, one copy in,
+// the ensemble kernel(s), one copy of the outputs back, all on the slot's stream.
 int admit(ode_handle* h, Request& r, int k) {
     Ctx& c = h->slot_ctx[k];
     cudaStream_t s = c.stream;
-    const size_t n = (size_t)r.d.n_states, np = (size_t)r.d.n_params, N = (size_t)r.N, cap = (size_t)r.o.nsave + 2;
-    CUDA_TRY(h, cudaMallocAsync(&r.dmem, r.bytes, s));
+    const Layout L = layout(r);
+    const size_t n = (size_t)r.d.n_states, np = (size_t)r.d.n_params, N = (size_t)r.N;
+    if (h->slot_pinned_cap[k] < L.total) {
+        if (h->slot_pinned[k]) cudaFreeHost(h->slot_pinned[k]);
+        h->slot_pinned[k] = nullptr;
+        h->slot_pinned_cap[k] = 0;
+        const size_t want = std::max<size_t>(L.total, (size_t)1 << 20);
+        CUDA_TRY(h, cudaHostAlloc(&h->slot_pinned[k], want, cudaHostAllocDefault));
+        h->slot_pinned_cap[k] = want;
+    }
+    char* hs = (char*)h->slot_pinned[k];
+    std::memcpy(hs + L.u0, r.u0.data(), n * N * 8);
+    std::memcpy(hs + L.p, r.p.data(), np * N * 8);
+    std::memcpy(hs + L.ts, r.tspan.data(), 2 * N * 8);
+    if (!r.saveat.empty()) std::memcpy(hs + L.sv, r.saveat.data(), r.saveat.size() * 8);
+    if (!r.npt.empty()) std::memcpy(hs + L.npt, r.npt.data(), N * 4);
+    CUDA_TRY(h, cudaMallocAsync(&r.dmem, L.total, s));
     char* base = (char*)r.dmem;
-    size_t off = 0;
-    auto take = [&](size_t bytes) { char* q = base + off; off += align256(bytes); return q; };
-    double* du0 = (double*)take(n * N * 8);
-    double* dp = (double*)take(np * N * 8);
-    double* dts = (double*)take(2 * N * 8);
-    double* dsv = (double*)take(std::max<size_t>(r.saveat.size(), 1) * 8);
-    int32_t* dnpt = r.npt.empty() ? nullptr : (int32_t*)take(N * 4);
-    double* dt = (double*)take(cap * N * 8);
-    double* du = (double*)take(cap * n * N * 8);
-    int32_t* dns = (int32_t*)take(N * 4);
-    int32_t* drc = (int32_t*)take(N * 4);
-    ode_stats* dst = (ode_stats*)take(N * sizeof(ode_stats));
-    CUDA_TRY(h, cudaMemcpyAsync(du0, r.u0.data(), n * N * 8, cudaMemcpyHostToDevice, s));
-    CUDA_TRY(h, cudaMemcpyAsync(dp, r.p.data(), np * N * 8, cudaMemcpyHostToDevice, s));
-    CUDA_TRY(h, cudaMemcpyAsync(dts, r.tspan.data(), 2 * N * 8, cudaMemcpyHostToDevice, s));
-    if (!r.saveat.empty())
-        CUDA_TRY(h, cudaMemcpyAsync(dsv, r.saveat.data(), r.saveat.size() * 8, cudaMemcpyHostToDevice, s));
-    if (dnpt) CUDA_TRY(h, cudaMemcpyAsync(dnpt, r.npt.data(), N * 4, cudaMemcpyHostToDevice, s));
-    int rc = run_ensemble(h, c, &r.d, &r.o, r.N, dnpt, du0, dp, dts, dsv, dt, du, dns, drc, (OdeStatsDev*)dst, s);
+    CUDA_TRY(h, cudaMemcpyAsync(base, hs, L.in_end, cudaMemcpyHostToDevice, s));
+    int rc = run_ensemble(h, c, &r.d, &r.o, r.N, r.npt.empty() ? nullptr : (const int32_t*)(base + L.npt),
+                          (const double*)(base + L.u0), (const double*)(base + L.p), (const double*)(base + L.ts),
+                          (const double*)(base + L.sv), (double*)(base + L.t), (double*)(base + L.u),
+                          (int32_t*)(base + L.ns), (int32_t*)(base + L.rc), (OdeStatsDev*)(base + L.st), s);
     if (rc) return rc;
-    CUDA_TRY(h, cudaMallocHost(&r.hout, output_bytes(r)));
-    char* ho = (char*)r.hout;
-    CUDA_TRY(h, cudaMemcpyAsync(ho, dt, cap * N * 8, cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(h, cudaMemcpyAsync(ho + cap * N * 8, du, cap * n * N * 8, cudaMemcpyDeviceToHost, s));
-    size_t o2 = cap * N * 8 + cap * n * N * 8;
-    CUDA_TRY(h, cudaMemcpyAsync(ho + o2, dns, N * 4, cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(h, cudaMemcpyAsync(ho + o2 + N * 4, drc, N * 4, cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(h, cudaMemcpyAsync(ho + o2 + N * 8, dst, N * sizeof(ode_stats), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(h, cudaMemcpyAsync(hs + L.t, base + L.t, L.total - L.t, cudaMemcpyDeviceToHost, s));
     CUDA_TRY(h, cudaFreeAsync(r.dmem, s));
     r.dmem = nullptr;
-    CUDA_TRY(h, cudaEventCreateWithFlags(&r.done_ev, cudaEventDisableTiming));
-    CUDA_TRY(h, cudaEventRecord(r.done_ev, s));
+    CUDA_TRY(h, cudaEventRecord(h->slot_ev[k], s));
     return ODE_OK;
 }
 
-void finish(Request& r) {
+// Outputs from the slot's staging into the caller's buffers.
+void finish(ode_handle* h, Request& r) {
     const size_t n = (size_t)r.d.n_states, N = (size_t)r.N, cap = (size_t)r.o.nsave + 2;
-    if (r.status == ODE_OK && r.hout) {
-        char* ho = (char*)r.hout;
-        if (r.t_out) std::memcpy(r.t_out, ho, cap * N * 8);
-        std::memcpy(r.u_out, ho + cap * N * 8, cap * n * N * 8);
-        size_t o2 = cap * N * 8 + cap * n * N * 8;
-        std::memcpy(r.nsaved, ho + o2, N * 4);
-        std::memcpy(r.retcode, ho + o2 + N * 4, N * 4);
-        if (r.stats) std::memcpy(r.stats, ho + o2 + N * 8, N * sizeof(ode_stats));
+    if (r.status == ODE_OK && r.slot >= 0 && h->slot_pinned[r.slot]) {
+        const Layout L = layout(r);
+        const char* hs = (const char*)h->slot_pinned[r.slot];
+        if (r.t_out) std::memcpy(r.t_out, hs + L.t, cap * N * 8);
+        std::memcpy(r.u_out, hs + L.u, cap * n * N * 8);
+        std::memcpy(r.nsaved, hs + L.ns, N * 4);
+        std::memcpy(r.retcode, hs + L.rc, N * 4);
+        if (r.stats) std::memcpy(r.stats, hs + L.st, N * sizeof(ode_stats));
     }
-    if (r.hout) cudaFreeHost(r.hout);
-    r.hout = nullptr;
-    if (r.done_ev) cudaEventDestroy(r.done_ev);
-    r.done_ev = nullptr;
     r.u0.clear(); r.u0.shrink_to_fit();
     r.p.clear(); r.p.shrink_to_fit();
-    r.state = 2;
+    r.tspan.clear(); r.tspan.shrink_to_fit();
+}
+
+// Book-keeping of a finished request (lock held).
+void retire(ode_handle* h, const std::shared_ptr<Request>& r) {
+    if (r->slot >= 0) h->slot_busy[r->slot] = 0;
+    if (r->state == 1) h->hbm_in_use -= r->bytes;
+    r->state = 2;
+    r->t_done = mono_now();
+    h->n_completed++;
+    h->completed.push_back(r->ticket);
 }
 
 // The serving loop: retire finished requests, then admit queued ones (FIFO)
 // while a slot is free and the HBM budget allows.  A request larger than the
-// whole budget is rejected with ODE_E_NOMEM.
+// whole budget is rejected with ODE_E_NOMEM.  Copies into and out of the
+// pinned staging run without the lock, so submitters are not held up.
 void serve_loop(ode_handle* h) {
     cudaSetDevice(h->device);
     std::unique_lock<std::mutex> lk(h->mu);
+    std::vector<std::shared_ptr<Request>> batch;
+    std::vector<std::pair<std::shared_ptr<Request>, int>> starts;
     while (!h->stop) {
         bool progressed = false;
+        batch.clear();
         for (size_t i = 0; i < h->running.size();) {
             auto r = h->running[i];
-            cudaError_t q = cudaEventQuery(r->done_ev);
+            cudaError_t q = cudaEventQuery(h->slot_ev[r->slot]);
             if (q == cudaErrorNotReady) { ++i; continue; }
             if (q != cudaSuccess) r->status = ODE_E_CUDA;
-            finish(*r);
-            h->slot_busy[r->slot] = 0;
-            h->hbm_in_use -= r->bytes;
-            h->n_completed++;
+            batch.push_back(r);
             h->running.erase(h->running.begin() + i);
+        }
+        if (!batch.empty()) {
+            lk.unlock();
+            for (auto& r : batch) finish(h, *r);
+            lk.lock();
+            for (auto& r : batch) retire(h, r);
             progressed = true;
         }
+        starts.clear();
         while (!h->pending.empty()) {
             auto r = h->pending.front();
             if (r->bytes > h->budget) {
                 h->pending.pop_front();
                 r->status = ODE_E_NOMEM;
-                r->state = 2;
                 h->n_rejected++;
+                retire(h, r);
                 progressed = true;
                 continue;
             }
@@ -494,26 +664,32 @@ void serve_loop(ode_handle* h) {
             h->hbm_in_use += r->bytes;
             r->state = 1;
             h->n_admitted++;
-            int rc = admit(h, *r, k);
-            if (rc) {
-                r->status = rc;
-                cudaStreamSynchronize(h->slot_ctx[k].stream);
-                if (r->dmem) cudaFree(r->dmem);
-                r->dmem = nullptr;
-                finish(*r);
-                h->slot_busy[k] = 0;
-                h->hbm_in_use -= r->bytes;
-                h->n_completed++;
-            } else {
-                h->running.push_back(r);
+            starts.emplace_back(r, k);
+        }
+        if (!starts.empty()) {
+            lk.unlock();
+            for (auto& rk : starts) {
+                rk.first->t_start = mono_now();
+                int rc = admit(h, *rk.first, rk.second);
+                if (rc) {
+                    rk.first->status = rc;
+                    cudaStreamSynchronize(h->slot_ctx[rk.second].stream);
+                    if (rk.first->dmem) cudaFree(rk.first->dmem);
+                    rk.first->dmem = nullptr;
+                }
+            }
+            lk.lock();
+            for (auto& rk : starts) {
+                if (rk.first->status != ODE_OK) retire(h, rk.first);
+                else h->running.push_back(rk.first);
             }
             progressed = true;
         }
         if (progressed) h->cv.notify_all();
         if (h->running.empty() && h->pending.empty())
             h->cv.wait(lk, [&] { return h->stop || !h->pending.empty(); });
-        else
-            h->cv.wait_for(lk, std::chrono::microseconds(50));
+        else if (!progressed)
+            h->cv.wait_for(lk, std::chrono::microseconds(20));
     }
 }
 
@@ -521,9 +697,13 @@ int ensure_worker(ode_handle* h) {
     if (h->worker_started) return ODE_OK;
     h->slot_ctx.resize(h->slots);
     h->slot_busy.assign(h->slots, 0);
+    h->slot_pinned.assign(h->slots, nullptr);
+    h->slot_pinned_cap.assign(h->slots, 0);
+    h->slot_ev.assign(h->slots, nullptr);
     for (int k = 0; k < h->slots; ++k) {
         int rc = ctx_init(h, h->slot_ctx[k], nullptr);
         if (rc) return rc;
+        CUDA_TRY(h, cudaEventCreateWithFlags(&h->slot_ev[k], cudaEventDisableTiming));
     }
     h->worker = std::thread(serve_loop, h);
     h->worker_started = true;
@@ -594,12 +774,16 @@ void ode_destroy(ode_handle* h) {
     if (h->worker_started && h->worker.joinable()) h->worker.join();
     cudaSetDevice(h->device);
     cudaDeviceSynchronize();
-    for (auto& r : h->running) finish(*r);
+    for (auto& r : h->running) finish(h, *r);
     for (DevBuf* b : {&h->b_u0, &h->b_p, &h->b_tspan, &h->b_saveat, &h->b_t, &h->b_u, &h->b_ns, &h->b_rc,
                       &h->b_st, &h->b_npt})
         if (b->p) cudaFree(b->p);
     ctx_free(h->main);
     for (auto& c : h->slot_ctx) ctx_free(c);
+    for (void* q : h->slot_pinned)
+        if (q) cudaFreeHost(q);
+    for (cudaEvent_t e : h->slot_ev)
+        if (e) cudaEventDestroy(e);
     if (h->h_abort) cudaFreeHost(h->h_abort);
     delete h;
 }
@@ -610,6 +794,9 @@ int ode_solve_ensemble_device(ode_handle* h, const ode_problem_desc* d, const od
                               int32_t* retcode, ode_stats* stats, void* cuda_stream) {
     int rc = validate(h, d, o, N);
     if (rc) return rc;
+    if (N > 0 && (!u0 || !p || !tspan || !u_out || !nsaved || !retcode))
+        return fail(h, ODE_E_INVALID, "null input or output buffer");
+    if (o->nsave > 0 && !saveat) return fail(h, ODE_E_INVALID, "nsave > 0 but saveat is null");
     std::lock_guard<std::mutex> lk(h->api_mu);
     CUDA_TRY(h, cudaSetDevice(h->device));
     *h->h_abort = 0;
@@ -627,6 +814,7 @@ int ode_solve_ensemble(ode_handle* h, const ode_problem_desc* d, const ode_optio
     if (N > 0 && (!u0 || !p || !tspan || !u_out || !nsaved || !retcode))
         return fail(h, ODE_E_INVALID, "null input or output buffer");
     if (o->nsave > 0 && !saveat) return fail(h, ODE_E_INVALID, "nsave > 0 but saveat is null");
+    if ((rc = check_sizes(h, d, npt, N))) return rc;
     std::lock_guard<std::mutex> lk(h->api_mu);
     CUDA_TRY(h, cudaSetDevice(h->device));
     *h->h_abort = 0;
@@ -674,6 +862,7 @@ int ode_submit(ode_handle* h, const ode_problem_desc* d, const ode_options* o, i
     if (N > 0 && (!u0 || !p || !tspan || !u_out || !nsaved || !retcode))
         return fail(h, ODE_E_INVALID, "null input or output buffer");
     if (o->nsave > 0 && !saveat) return fail(h, ODE_E_INVALID, "nsave > 0 but saveat is null");
+    if ((rc = check_sizes(h, d, npt, N))) return rc;
     auto r = std::make_shared<Request>();
     r->d = *d;
     r->o = *o;
@@ -695,6 +884,7 @@ int ode_submit(ode_handle* h, const ode_problem_desc* d, const ode_options* o, i
     rc = ensure_worker(h);
     if (rc) return rc;
     r->ticket = h->next_ticket++;
+    r->t_submit = mono_now();
     h->tickets[r->ticket] = r;
     h->pending.push_back(r);
     h->n_submitted++;
@@ -731,6 +921,31 @@ int ode_wait(ode_handle* h, uint64_t ticket, double timeout_s) {
     }
     h->tickets.erase(ticket);
     return r->status;
+}
+
+int ode_next_completed(ode_handle* h, double timeout_s, uint64_t* ticket, int32_t* status, double* times) {
+    if (!h || !ticket) return fail(h, ODE_E_INVALID, "null handle or ticket pointer");
+    std::unique_lock<std::mutex> lk(h->mu);
+    *ticket = 0;
+    auto ready = [&] {
+        while (!h->completed.empty() && !h->tickets.count(h->completed.front())) h->completed.pop_front();
+        return !h->completed.empty();
+    };
+    if (timeout_s < 0) h->cv.wait(lk, ready);
+    else if (timeout_s > 0) h->cv.wait_for(lk, std::chrono::duration<double>(timeout_s), ready);
+    if (!ready()) return ODE_OK;
+    const uint64_t t = h->completed.front();
+    h->completed.pop_front();
+    auto r = h->tickets[t];
+    h->tickets.erase(t);
+    *ticket = t;
+    if (status) *status = r->status;
+    if (times) {
+        times[0] = r->t_submit;
+        times[1] = r->t_start;
+        times[2] = r->t_done;
+    }
+    return ODE_OK;
 }
 
 int ode_serving_stats_get(ode_handle* h, ode_serving_stats* s) {
@@ -805,10 +1020,10 @@ namespace {
 // At most kNoAllocMaxTraj trajectories per call when per-trajectory sizes are
 // given (the bucket index list); uniform-size calls only use the counters.
 constexpr long long kNoAllocMaxTraj = 1LL << 20;
-// [0, 8) work counters, [8, 16) class counts, [16, 24) class cursors,
-// [32, 32 + kNoAllocMaxTraj) bucketed trajectory indices.  8 MiB + 256 B,
-// held by every GPU that loads the library until the process exits.
-static __device__ __align__(256) unsigned long long g_noalloc_scratch[32 + kNoAllocMaxTraj];
+// [0, kCounters) the counters of a context (layout of kOff*), then
+// [kCounters, kCounters + kNoAllocMaxTraj) bucketed trajectory indices.
+// 8 MiB + 512 B, held by every GPU that loads the library until the process exits.
+static __device__ __align__(256) unsigned long long g_noalloc_scratch[kCounters + kNoAllocMaxTraj];
 
 std::mutex g_noalloc_mu;
 unsigned long long* g_noalloc_ptr[64] = {};
@@ -831,9 +1046,12 @@ int noalloc_scratch(int dev, unsigned long long** out) {
 
 int noalloc_launch(const KernelVariant* v, EnsembleArgs a, unsigned long long* queue, int sm_count, cudaStream_t s) {
     if (a.count <= 0) return ODE_OK;
-    const int block = 128;
+    int block = 0;
+    size_t smem = 0;
+    cudaError_t e = launch_geometry(v, 0, &block, &smem);
+    if (e != cudaSuccess) return fail(nullptr, ODE_E_CUDA, std::string("shared memory: ") + cudaGetErrorString(e));
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v->fn, block, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v->fn, block, smem);
     if (e != cudaSuccess) return fail(nullptr, ODE_E_CUDA, std::string("occupancy: ") + cudaGetErrorString(e));
     if (per_sm <= 0) per_sm = 1;
     long long want = (a.count * v->lanes + block - 1) / block;
@@ -841,7 +1059,7 @@ int noalloc_launch(const KernelVariant* v, EnsembleArgs a, unsigned long long* q
     if (grid < 1) grid = 1;
     a.persistent = 1;
     a.queue = queue;
-    v->launch(a, grid, block, 0, s);
+    v->launch(a, grid, block, smem, s);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(nullptr, ODE_E_CUDA, std::string("launch ") + v->name + ": " + cudaGetErrorString(e));
     return ODE_OK;
@@ -871,6 +1089,9 @@ extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_o
         return fail(nullptr, ODE_E_INVALID, "invalid problem description or options");
     if (npt_dev && d->model_id != ODE_MODEL_DUFFING_CHAIN)
         return fail(nullptr, ODE_E_UNSUPPORTED, "per-trajectory sizes are supported for DUFFING_CHAIN");
+    if (N > 0 && (!u0 || !p || !tspan || !u_out || !nsaved || !retcode))
+        return fail(nullptr, ODE_E_INVALID, "null input or output buffer");
+    if (o->nsave > 0 && !saveat) return fail(nullptr, ODE_E_INVALID, "nsave > 0 but saveat is null");
     if (N == 0) return ODE_OK;
     int dev = 0, sm_count = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -915,35 +1136,36 @@ extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_o
     a.abort_flag = nullptr;
 
     // Counters must start at zero on every call (the array keeps the last call's contents).
-    e = cudaMemsetAsync(scratch, 0, 32 * sizeof(unsigned long long), s);
+    e = cudaMemsetAsync(scratch, 0, kCounters * sizeof(unsigned long long), s);
     if (e != cudaSuccess) return fail(nullptr, ODE_E_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
     if (npt_dev == nullptr) {
         const KernelVariant* v = find_variant(d->alg_id, d->model_id, d->precision, d->n_states, o->lanes_per_traj);
         if (!v) return fail(nullptr, ODE_E_UNSUPPORTED, "no compiled kernel for this problem");
         return noalloc_launch(v, a, scratch, sm_count, s);
     }
-    long long* order = (long long*)(scratch + 32);
-    const int gb = (int)((N + 255) / 256);
-    bucket_count<<<gb, 256, 0, s>>>(npt_dev, N, scratch + 8);
-    unsigned long long hc[8] = {0};
-    e = cudaMemcpyAsync(hc, scratch + 8, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+    long long* order = (long long*)(scratch + kCounters);
+    enqueue_bucketing(npt_dev, N, scratch, order, nsaved, retcode, s);
+    a.order = order;
+    if (const FusedVariant* fv = find_fused(d->alg_id, d->model_id, d->precision)) {
+        e = launch_fused(fv, a, scratch, sm_count, s);
+        if (e != cudaSuccess) return fail(nullptr, ODE_E_CUDA, std::string("launch ") + fv->name + ": " + cudaGetErrorString(e));
+        return ODE_OK;
+    }
+    unsigned long long hc[kNumClasses + 1] = {0};
+    e = cudaMemcpyAsync(hc, scratch + kOffCounts, sizeof(hc), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return fail(nullptr, ODE_E_CUDA, std::string("bucket counts: ") + cudaGetErrorString(e));
-    unsigned long long off[8] = {0};
+    unsigned long long off[kNumClasses] = {0};
     unsigned long long acc = 0;
-    for (int k = 0; k < 5; ++k) { off[k] = acc; acc += hc[k]; }
-    e = cudaMemcpyAsync(scratch + 16, off, 5 * sizeof(unsigned long long), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return fail(nullptr, ODE_E_CUDA, std::string("bucket offsets: ") + cudaGetErrorString(e));
-    bucket_scatter<<<gb, 256, 0, s>>>(npt_dev, N, scratch + 16, order);
-    for (int k = 0; k < 5; ++k) {
+    for (int k = 0; k < kNumClasses; ++k) { off[k] = acc; acc += hc[k]; }
+    for (int k = 0; k < kNumClasses; ++k) {
         if (hc[k] == 0) continue;
         const KernelVariant* v = find_variant(d->alg_id, d->model_id, d->precision, kClassN[k], 0);
         if (!v) return fail(nullptr, ODE_E_UNSUPPORTED, "no compiled kernel for a Duffing size class");
         EnsembleArgs ac = a;
         ac.order = order + off[k];
         ac.count = (long long)hc[k];
-        rc = noalloc_launch(v, ac, scratch + k, sm_count, s);
+        rc = noalloc_launch(v, ac, scratch + kOffClassQ + k, sm_count, s);
         if (rc) return rc;
     }
     return ODE_OK;

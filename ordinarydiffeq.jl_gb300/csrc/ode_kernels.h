@@ -41,7 +41,16 @@ struct EnsembleArgs {
     int persistent;
     unsigned long long* queue;     // persistent work counter (zeroed before launch)
     const volatile int* abort_flag;  // host-settable early stop (nullptr: none)
+    // size classes of an uneven ensemble (one launch over all classes):
+    // class k holds class_count[k] trajectories at order[class_offset[k] ...]
+    const unsigned long long* class_count;
+    const unsigned long long* class_offset;
+    unsigned long long* class_next;  // per-class work counters (zeroed before launch)
 };
+
+// Size classes of uneven ensembles: state counts 4, 8, 16, 32, 64.
+constexpr int kNumClasses = 5;
+constexpr int kClassStates[kNumClasses] = {4, 8, 16, 32, 64};
 
 // One compiled kernel variant.
 struct KernelVariant {
@@ -54,10 +63,21 @@ struct KernelVariant {
     const char* name;
 };
 
+// One launch integrating every size class of an uneven ensemble.
+struct FusedVariant {
+    int alg, model, prec;
+    const void* fn;
+    void (*launch)(const EnsembleArgs&, int grid, int block, size_t smem, cudaStream_t);
+    const char* name;
+};
+
 // Registries filled by each translation unit (static arrays).
 const KernelVariant* tsit5_variants(int* count);
 const KernelVariant* vern7_variants(int* count);
 const KernelVariant* rodas_variants(int* count);
+const KernelVariant* rodas_group_variants(int* count);
+const FusedVariant* fused_tsit5_variants(int* count);
+const FusedVariant* fused_vern7_variants(int* count);
 
 template <class K>
 void launch_kernel(K kernel, const EnsembleArgs& a, int grid, int block, size_t smem, cudaStream_t s) {

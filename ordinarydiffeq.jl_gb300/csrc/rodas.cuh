@@ -1,4 +1,7 @@
-// Rodas5P on one lane per trajectory (small systems, W kept in registers).
+// Rodas5P, with the linear algebra as a policy:
+//   RegLA   one lane per trajectory, J, W and the LU in registers (n <= 8);
+//   SmemLA  a lane group per trajectory, W and the LU in shared memory
+//           (16 to 64 states, lu_group.cuh).
 //
 //  perform_step!(::RosenbrockCache)  lib/OrdinaryDiffEqRosenbrock/src/rosenbrock_perform_step.jl:729-847
 //      fused accumulation helpers :581-727 (acc = base; acc = muladd(c_i, k_i, acc), left to right)
@@ -18,6 +21,7 @@
 // optional refinement sweeps per solve form the residual b - W x in FP64.
 #pragma once
 #include "integrator.cuh"
+#include "lu_group.cuh"
 #include "rksum.cuh"
 #include "tableaus.h"
 
@@ -105,14 +109,80 @@ __device__ __forceinline__ void rhs_stage(R* du, const R* u, const R* ulo, const
     }
 }
 
-struct Rodas5PAlg {
+// J, W and the LU in one lane's registers.
+struct RegLA {
+    static constexpr bool FP64_RESIDUAL = true;   // refinement residual formed in FP64
+    template <class R, int C> struct Store {
+        R J[C][C];
+        R W[C][C];
+        int piv[C];
+    };
+    template <class R, int L, int C> __host__ __device__ static constexpr int smem_bytes() { return 0; }
+    template <class R, int L, int C> __device__ static void init(Store<R, C>&, const Group<L>&) {
+        static_assert(L == 1, "register Rodas5P runs one trajectory per lane");
+    }
+    // J(uprev); kept across a rejected step (fresh = false)
+    template <class Model, class R, int L, int C>
+    __device__ static void jacobian(Store<R, C>& s, const R* up, const R* p, double t, bool fresh, const Group<L>&) {
+        if (fresh) Model::template jac<R, C>(s.J, up, p, t);
+    }
+    // W = J - I/(dt*gamma), factorised in place
+    template <class R, int L, int C>
+    __device__ static void factor(Store<R, C>& s, R idg, const Group<L>&) {
+#pragma unroll
+        for (int i = 0; i < C; ++i)
+#pragma unroll
+            for (int jj = 0; jj < C; ++jj) s.W[i][jj] = (i == jj) ? FMA(R(-1), idg, s.J[i][jj]) : s.J[i][jj];
+        lu_factor_reg<R, C>(s.W, s.piv);
+    }
+    // Solve W x = b in place (b -> x); in the mixed mode optionally refined with
+    // FP64 residuals b - (J - I/(dt*gamma)) x.
+    template <class Model, class R, int L, int C>
+    __device__ static void wsolve(Store<R, C>& s, R* b, double invdtgamma, R, int ir, const R*, const R*,
+                                  const ff*, const Group<L>&) {
+        if constexpr (sizeof(R) == 8) {
+            lu_solve_reg<R, C>(s.W, s.piv, b);
+            return;
+        }
+        if (ir <= 0) {
+            lu_solve_reg<R, C>(s.W, s.piv, b);
+            return;
+        }
+        double b64[C];
+#pragma unroll
+        for (int i = 0; i < C; ++i) b64[i] = (double)b[i];
+        lu_solve_reg<R, C>(s.W, s.piv, b);
+        double x[C];
+#pragma unroll
+        for (int i = 0; i < C; ++i) x[i] = (double)b[i];
+        for (int sw = 0; sw < ir; ++sw) {
+            R r[C];
+#pragma unroll
+            for (int i = 0; i < C; ++i) {
+                double acc = b64[i];
+#pragma unroll
+                for (int jj = 0; jj < C; ++jj) {
+                    double wij = (double)s.J[i][jj] - (i == jj ? invdtgamma : 0.0);
+                    acc = fma(-wij, x[jj], acc);
+                }
+                r[i] = (R)acc;
+            }
+            lu_solve_reg<R, C>(s.W, s.piv, r);
+#pragma unroll
+            for (int i = 0; i < C; ++i) x[i] += (double)r[i];
+        }
+#pragma unroll
+        for (int i = 0; i < C; ++i) b[i] = (R)x[i];
+    }
+};
+
+template <class LA>
+struct Rodas5PT {
     static constexpr int ORDER = 5;
     static constexpr bool IMPLICIT = true;
     static constexpr int MAXP = 4;
     template <class R, int C> struct Cache {
-        R J[C][C];
-        R W[C][C];
-        int piv[C];
+        typename LA::template Store<R, C> la;
         R ks[8][C];
         R dk[3][C];   // dense k1..k3
         R scratch[C];
@@ -120,10 +190,14 @@ struct Rodas5PAlg {
         bool haveJ;
         int ir;
     };
+    template <class R, int L, int C> __host__ __device__ static constexpr int smem_bytes() {
+        return LA::template smem_bytes<R, L, C>();
+    }
     template <class R, int C> __device__ static R* fsal_slot(Cache<R, C>& c) { return c.scratch; }
     template <class Model, class R, int L, int C>
-    __device__ static void initialize(Cache<R, C>& c, const R*, const R*, double, const Group<L>&, StepStats&,
+    __device__ static void initialize(Cache<R, C>& c, const R*, const R*, double, const Group<L>& g, StepStats&,
                                       const EnsembleArgs& a, long long j) {
+        LA::template init<R, L, C>(c.la, g);
         c.haveJ = false;
         c.ir = a.ir_sweeps;
         if (sizeof(R) == 4) {
@@ -134,73 +208,34 @@ struct Rodas5PAlg {
     template <class R, int C> __device__ static void on_accept(Cache<R, C>&) {}
     template <class R, int C> __device__ static void after_save(Cache<R, C>&) {}
 
-    // Solve W x = b in place (b -> x); in the mixed mode optionally refined with
-    // FP64 residuals b - (J - I/(dt*gamma)) x.
-    template <class R, int C>
-    __device__ static void wsolve(Cache<R, C>& c, R* b, double invdtgamma) {
-        if (sizeof(R) == 8 || c.ir <= 0) {
-            lu_solve_reg<R, C>(c.W, c.piv, b);
-            return;
-        }
-        double b64[C];
-#pragma unroll
-        for (int i = 0; i < C; ++i) b64[i] = (double)b[i];
-        lu_solve_reg<R, C>(c.W, c.piv, b);
-        double x[C];
-#pragma unroll
-        for (int i = 0; i < C; ++i) x[i] = (double)b[i];
-        for (int s = 0; s < c.ir; ++s) {
-            R r[C];
-#pragma unroll
-            for (int i = 0; i < C; ++i) {
-                double acc = b64[i];
-#pragma unroll
-                for (int jj = 0; jj < C; ++jj) {
-                    double wij = (double)c.J[i][jj] - (i == jj ? invdtgamma : 0.0);
-                    acc = fma(-wij, x[jj], acc);
-                }
-                r[i] = (R)acc;
-            }
-            lu_solve_reg<R, C>(c.W, c.piv, r);
-#pragma unroll
-            for (int i = 0; i < C; ++i) x[i] += (double)r[i];
-        }
-#pragma unroll
-        for (int i = 0; i < C; ++i) b[i] = (R)x[i];
-    }
-
     template <class Model, class R, int L, int C>
     __device__ static typename Ctl<R>::T step(Cache<R, C>& c, R* u, R* ulo, const R* up, const R* uplo,
                                              const R* p, double t, double dt, R abstol, R reltol, long long iter,
                                              bool errorfail, const Group<L>& g, StepStats& st) {
-        static_assert(L == 1, "register Rodas5P runs one trajectory per lane");
         constexpr int NP = Model::NP;
         // dt-derived coefficients: FP64 like the reference; in the mixed mode they
         // scale FP32 stage terms, so they are formed in FP32 from dt (no FP64 work).
         const R dr = (R)dt;
         const R invdt = sizeof(R) == 8 ? R(1.0 / dt) : R(1) / dr;
-        const double invdtgamma = (sizeof(R) == 8 || c.ir > 0) ? 1.0 / (dt * tab::RODAS5P_GAMMA) : 0.0;
+        const double invdtgamma =
+            (sizeof(R) == 8 || (LA::FP64_RESIDUAL && c.ir > 0)) ? 1.0 / (dt * tab::RODAS5P_GAMMA) : 0.0;
         const R idg = sizeof(R) == 8 ? (R)invdtgamma : R(1) / (dr * (R)tab::RODAS5P_GAMMA);
         R* fsal = c.scratch;
         rhs_stage<Model, R, L, C, NP>(fsal, up, uplo, p, c.pff, t, g);
         st.nf += 1;
         bool new_jac = !(iter > 1 && errorfail) || !c.haveJ;
+        LA::template jacobian<Model, R, L, C>(c.la, up, p, t, new_jac, g);
         if (new_jac) {
-            Model::template jac<R, C>(c.J, up, p, t);
             st.njacs += 1;
             st.nf += 1;   // the reference's AD time derivative (dT = 0 for autonomous models)
             c.haveJ = true;
         }
-#pragma unroll
-        for (int i = 0; i < C; ++i)
-#pragma unroll
-            for (int jj = 0; jj < C; ++jj) c.W[i][jj] = (i == jj) ? FMA(R(-1), idg, c.J[i][jj]) : c.J[i][jj];
+        LA::template factor<R, L, C>(c.la, idg, g);
         st.nw += 1;
-        lu_factor_reg<R, C>(c.W, c.piv);
         R r[C];
 #pragma unroll
         for (int i = 0; i < C; ++i) r[i] = fsal[i];
-        wsolve<R, C>(c, r, invdtgamma);
+        LA::template wsolve<Model, R, L, C>(c.la, r, invdtgamma, idg, c.ir, up, uplo, c.pff, g);
 #pragma unroll
         for (int i = 0; i < C; ++i) c.ks[0][i] = -r[i];
         st.nsolve += 1;
@@ -245,7 +280,7 @@ struct Rodas5PAlg {
                     r[i] = (R)cs.value();
                 }
             }
-            wsolve<R, C>(c, r, invdtgamma);
+            LA::template wsolve<Model, R, L, C>(c.la, r, invdtgamma, idg, c.ir, up, uplo, c.pff, g);
 #pragma unroll
             for (int i = 0; i < C; ++i) c.ks[s][i] = -r[i];
             st.nsolve += 1;
@@ -311,5 +346,8 @@ struct Rodas5PAlg {
         }
     }
 };
+
+using Rodas5PAlg = Rodas5PT<RegLA>;
+using Rodas5PGroupAlg = Rodas5PT<SmemLA>;
 
 }  // namespace odegb

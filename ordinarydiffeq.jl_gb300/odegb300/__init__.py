@@ -9,8 +9,9 @@
 from .ensemble import (EnsembleContext, EnsembleGB300, EnsembleProblem, EnsembleSolution, ODEProblem,
                        ODESolution, ReturnCode, Rodas5P, Tsit5, Vern7, get_handle, remake, solve, solve_arrays)
 from .saveat import julia_float_range, resolve_saveat
+from .serving import Server, run_open_loop
 from . import _lib, build
 
 __all__ = ["EnsembleContext", "EnsembleGB300", "EnsembleProblem", "EnsembleSolution", "ODEProblem", "ODESolution",
            "ReturnCode", "Rodas5P", "Tsit5", "Vern7", "get_handle", "remake", "solve", "solve_arrays",
-           "julia_float_range", "resolve_saveat"]
+           "julia_float_range", "resolve_saveat", "Server", "run_open_loop"]

@@ -82,7 +82,10 @@ class SaveSpec:
 
 
 def resolve_saveat(saveat, tspans, save_start=None, save_end=None):
-    """tspans: (2, N).  Returns the SaveSpec passed to the C ABI."""
+    """tspans: (2, N).  Returns the SaveSpec passed to the C ABI (a SaveSpec is
+    returned unchanged)."""
+    if isinstance(saveat, SaveSpec):
+        return saveat
     tspans = np.asarray(tspans, dtype=np.float64)
     t0s, tfs = tspans[0], tspans[1]
     same_span = bool(np.all(t0s == t0s[0]) and np.all(tfs == tfs[0])) if tspans.shape[1] else True

@@ -50,6 +50,14 @@ def duffing_inputs(N, n_osc, seed=42, tf_range=(1.0, 100.0)):
     return u0, p, tspan, saveat, npt
 
 
+def brusselator_inputs(N, cells=32, seed=42):
+    """Brusselator-1D: A ~ U(0.5, 1.5), B ~ U(2, 4), alpha log-uniform in [1e-3, 1e-1],
+    u0 = steady state + 0.1 N(0, 1), tspan (0, 10)."""
+    from odegb300 import workloads
+    wl = workloads.brusselator(N, seed=seed, cells=cells)
+    return wl["u0"], wl["p"], wl["tspan"]
+
+
 def gpu(model, alg, u0, p, tspan, saveat, reltol, abstol, precision="fp64", **kw):
     ens = EnsembleGB300(precision=precision, lanes_per_traj=kw.pop("lanes", 0), scheduler=kw.pop("scheduler", "auto"),
                         ir_sweeps=kw.pop("ir_sweeps", -1))

@@ -10,8 +10,8 @@ the tolerance (all trajectories of the well-conditioned Robertson ensemble,
 import numpy as np
 import pytest
 
-from gpu_common import (ROBER_SAVEAT, compare, duffing_inputs, err_vs, gpu, lorenz_inputs, oracle,
-                        robertson_inputs, truth)
+from gpu_common import (ROBER_SAVEAT, brusselator_inputs, compare, duffing_inputs, err_vs, gpu, lorenz_inputs,
+                        oracle, robertson_inputs, truth)
 
 pytestmark = pytest.mark.gpu
 
@@ -105,13 +105,76 @@ def test_duffing_mixed(alg, n_osc):
     assert_equal_accuracy(g, g64, tr, 1e-6, 1e-6)
 
 
-def test_duffing_uneven_sizes_bucketed():
+@pytest.mark.parametrize("cells", [8, 16, 32])
+def test_brusselator_rodas5p_fp64_shared_memory_lu(cells):
+    # 16 to 64 states: one lane group per trajectory, W and its LU in shared memory
+    N = 128
+    u0, p, ts = brusselator_inputs(N, cells=cells)
+    g = gpu("brusselator_1d", "rodas5p", u0, p, ts, 1.25, 1e-5, 1e-8)
+    o = oracle("brusselator_1d", "rodas5p", u0, p, ts, 1.25, 1e-5, 1e-8)
+    assert (g["retcode"] == 1).all()
+    c = compare(g, o, 1e-5, 1e-8)
+    assert c["ok"] and c["steps_ok"], c
+    assert (g["stats"]["njacs"] == o["stats"]["njacs"]).mean() > 0.9
+
+
+def test_brusselator_lane_layouts_agree():
+    # 64 states on 32 lanes x 2 rows and on 16 lanes x 4 rows: same factorisation
+    N = 128
+    u0, p, ts = brusselator_inputs(N, cells=32, seed=3)
+    a = gpu("brusselator_1d", "rodas5p", u0, p, ts, 1.25, 1e-5, 1e-8, lanes=32)
+    b = gpu("brusselator_1d", "rodas5p", u0, p, ts, 1.25, 1e-5, 1e-8, lanes=16)
+    c = compare(a, b, 1e-5, 1e-8, factor=1.0)
+    assert c["ok"] and c["steps_ok"], c
+
+
+@pytest.mark.parametrize("ir", [0, 1])
+def test_brusselator_rodas5p_mixed(ir):
+    # FP32 W and LU; with ir = 1 each solve takes one refinement sweep whose
+    # residual is formed in double-float
+    N = 128
+    u0, p, ts = brusselator_inputs(N, cells=32)
+    g = gpu("brusselator_1d", "rodas5p", u0, p, ts, 1.25, 1e-5, 1e-8, precision="mixed", ir_sweeps=ir)
+    o = oracle("brusselator_1d", "rodas5p", u0, p, ts, 1.25, 1e-5, 1e-8)
+    assert (g["retcode"] == 1).all()
+    c = compare(g, o, 1e-5, 1e-8, step_slack=10 ** 9)
+    assert c["ok"], c
+    g64 = gpu("brusselator_1d", "rodas5p", u0, p, ts, 1.25, 1e-5, 1e-8)
+    tr = truth("brusselator_1d", u0, p, ts, 1.25, stiff=True)
+    assert_equal_accuracy(g, g64, tr, 1e-5, 1e-8)
+
+
+@pytest.mark.parametrize("alg", ["tsit5", "vern7"])
+def test_duffing_uneven_sizes_one_launch(alg):
+    # every size class in one persistent launch (device bucketing, no host round trip)
     N = 600
     u0, p, ts, sv, npt = duffing_inputs(N, [2, 4, 8, 16, 32], tf_range=(1.0, 10.0))
-    g = gpu("duffing_chain", "vern7", u0, p, ts, sv, 1e-6, 1e-6, n_per_traj=npt)
-    o = oracle("duffing_chain", "vern7", u0, p, ts, sv, 1e-6, 1e-6, n_per_traj=npt)
+    g = gpu("duffing_chain", alg, u0, p, ts, sv, 1e-6, 1e-6, n_per_traj=npt)
+    o = oracle("duffing_chain", alg, u0, p, ts, sv, 1e-6, 1e-6, n_per_traj=npt)
     c = compare(g, o, 1e-6, 1e-6)
     assert c["ok"] and c["steps_ok"], c
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_uneven_one_launch_equals_one_kernel_per_class(precision):
+    # lanes_per_traj > 0 selects the one-kernel-per-class form (same lane
+    # layout per class): results must be bit-identical to the single launch
+    N = 400
+    u0, p, ts, sv, npt = duffing_inputs(N, [2, 4, 8, 16, 32], tf_range=(1.0, 10.0), seed=11)
+    a = gpu("duffing_chain", "vern7", u0, p, ts, sv, 1e-6, 1e-6, precision=precision, n_per_traj=npt)
+    b = gpu("duffing_chain", "vern7", u0, p, ts, sv, 1e-6, 1e-6, precision=precision, n_per_traj=npt, lanes=4)
+    assert np.array_equal(a["u"], b["u"], equal_nan=True)
+    assert np.array_equal(a["stats"]["naccept"], b["stats"]["naccept"])
+
+
+def test_uneven_sizes_must_be_size_classes():
+    from odegb300 import _lib
+    N = 8
+    u0, p, ts, sv, npt = duffing_inputs(N, 2)
+    npt = npt.copy()
+    npt[3] = 6
+    with pytest.raises(_lib.OdeError, match="sizes must be"):
+        gpu("duffing_chain", "vern7", u0, p, ts, sv, 1e-6, 1e-6, n_per_traj=npt)
 
 
 def test_static_and_persistent_schedulers_agree():
