@@ -349,18 +349,35 @@ def run_gb300(args, world, rank, local, dist):
     fp64_peak = C.c_double(0)
     L.ode_measure_fma_peak(local, 0, C.byref(fp64_peak))
 
-    # end-to-end through the public host-buffer call
-    from odegb300.ensemble import solve_arrays
-    ens = odegb300.EnsembleGB300(precision=best, ir_sweeps=wl.get("ir_sweeps", -1) if best == "mixed" else -1)
-    kw = dict(n_per_traj=npt) if npt is not None else {}
+    # end-to-end through the public host-buffer call (ode_solve_ensemble): inputs
+    # in pinned host memory, outputs back into pinned host memory, every step
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+    h_u0, h_p, h_ts = pin(wl["u0"]), pin(wl["p"]), pin(wl["tspan"])
+    h_sv = pin(sv.values if sv.nsave else np.zeros(1))
+    h_npt = pin(npt) if npt is not None else None
+    h_t = torch.empty((cap, N), dtype=torch.float64).pin_memory()
+    h_u = torch.empty((cap, n, N), dtype=torch.float64).pin_memory()
+    h_ns = torch.empty(N, dtype=torch.int32).pin_memory()
+    h_rc = torch.empty(N, dtype=torch.int32).pin_memory()
+    h_st = torch.empty((N, 6), dtype=torch.int64).pin_memory()
+    ens_e2e = odegb300.EnsembleGB300(precision=best, ir_sweeps=wl.get("ir_sweeps", -1) if best == "mixed" else -1)
+    o_e2e = _options(wl["reltol"], wl["abstol"], None, None, None, 1000000, sv, ens_e2e, None, None)
+    d_e2e = _lib.ProblemDesc(model, alg.alg_id, n, wl["p"].shape[0], ens_e2e.prec_id(), 0)
+    hp = lambda t, ty=C.c_double: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(ty)) if t is not None else None
+
+    def solve_host():
+        _lib.check(L.ode_solve_ensemble(h, C.byref(d_e2e), C.byref(o_e2e), N, hp(h_npt, C.c_int32), hp(h_u0),
+                                        hp(h_p), hp(h_ts), hp(h_sv) if sv.nsave else None, hp(h_t), hp(h_u),
+                                        hp(h_ns, C.c_int32), hp(h_rc, C.c_int32), hp(h_st, _lib.Stats)), h)
+
     for _ in range(max(1, min(args.warmup, 2))):
-        solve_arrays(wl["model"], alg, ens, wl["u0"], wl["p"], wl["tspan"], wl["saveat"], wl["reltol"],
-                     wl["abstol"], **kw)
+        solve_host()
     e2e_t = []
     for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        solve_arrays(wl["model"], alg, ens, wl["u0"], wl["p"], wl["tspan"], wl["saveat"], wl["reltol"],
-                     wl["abstol"], **kw)
+        solve_host()
         e2e_t.append(time.perf_counter() - t0)
     e2e_s = float(np.mean(e2e_t))
     h2d = wl["u0"].nbytes + wl["p"].nbytes + wl["tspan"].nbytes + (sv.values.nbytes if sv.nsave else 0) + \

@@ -181,6 +181,16 @@ int ode_abort(ode_handle* h);
 int ode_kernel_launches(const ode_handle* h, int64_t* launches);
 int ode_last_kernel_ms(const ode_handle* h, double* ms);
 
+/* Autotuner (no reference counterpart): times every compiled kernel variant
+ * (lanes per trajectory), block size (32, 64, 128) and scheduler (static,
+ * persistent) on the given HOST sample of a uniform-size problem and keeps
+ * the fastest for this handle; later solves of the same (alg, model,
+ * precision, n_states) with lanes_per_traj, block_size and scheduler left at
+ * 0 use it.  Outputs: the chosen shape and its time per solve of the sample. */
+int ode_autotune(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int64_t ntraj, const double* u0,
+                 const double* p, const double* tspan, const double* saveat, int32_t* lanes, int32_t* block_size,
+                 int32_t* scheduler, double* ms);
+
 /* Compiled kernel variants for (alg, model, precision, n): lanes per
  * trajectory, for tuning and diagnostics.  Returns the count written. */
 int ode_query_variants(int alg, int model, int precision, int n, int32_t* lanes, int32_t cap);

@@ -22,6 +22,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 using namespace odegb;
@@ -85,6 +86,10 @@ struct Ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaStream_t class_streams[5] = {};
     cudaEvent_t class_events[5] = {};
+    // the last solve captured as a CUDA graph, replayed while its key matches
+    cudaGraphExec_t graph = nullptr;
+    std::vector<unsigned char> graph_key;
+    long long graph_kernels = 0;
 };
 
 struct Request;
@@ -123,6 +128,10 @@ struct ode_handle {
     std::vector<size_t> slot_pinned_cap;
     std::vector<cudaEvent_t> slot_ev;        // end of the slot's current request
     std::deque<uint64_t> completed;          // tickets in completion order
+    // autotuned launch shape per (alg, model, precision, n)
+    struct Tuned { int lanes, block, scheduler; double ms; };
+    std::map<std::tuple<int, int, int, int>, Tuned> tuned;
+    std::mutex tune_mu;
 };
 
 namespace {
@@ -390,60 +399,75 @@ void ctx_free(Ctx& c) {
     }
     if (c.ev0) cudaEventDestroy(c.ev0);
     if (c.ev1) cudaEventDestroy(c.ev1);
+    if (c.graph) cudaGraphExecDestroy(c.graph);
     if (c.stream) cudaStreamDestroy(c.stream);
     c = Ctx();
 }
 
-// Enqueue the whole ensemble on stream s using the scratch of ctx c.  All
-// pointers are device pointers.
-int run_ensemble(ode_handle* h, Ctx& c, const ode_problem_desc* d, const ode_options* o, int64_t N,
-                 const int32_t* npt_dev, const double* u0, const double* p, const double* tspan,
-                 const double* saveat, double* t_out, double* u_out, int32_t* nsaved, int32_t* retcode,
-                 OdeStatsDev* stats, cudaStream_t s) {
-    EnsembleArgs a = make_args(h, d, o, N, u0, p, tspan, saveat, t_out, u_out, nsaved, retcode, stats);
-    int scheduler = o->scheduler;
-    if (N == 0) return ODE_OK;
+// The kernels of one solve, chosen before anything is enqueued.
+struct Plan {
+    const KernelVariant* v = nullptr;   // uniform size
+    const FusedVariant* fv = nullptr;   // uneven sizes, one launch over all classes
+    int block = 0, scheduler = 0;
+    bool per_class = false;             // uneven sizes without a fused kernel
+};
+
+int make_plan(ode_handle* h, const ode_problem_desc* d, const ode_options* o, const int32_t* npt_dev, Plan* pl) {
+    *pl = Plan();
+    pl->scheduler = o->scheduler;
+    pl->block = o->block_size;
     if (npt_dev == nullptr) {
-        const KernelVariant* v = find_variant(d->alg_id, d->model_id, d->precision, d->n_states, o->lanes_per_traj);
-        if (!v) {
+        int lanes = o->lanes_per_traj;
+        if (lanes <= 0 && pl->block <= 0 && pl->scheduler == 0) {   // shape chosen by ode_autotune, if any
+            std::lock_guard<std::mutex> tl(h->tune_mu);
+            auto it = h->tuned.find(std::make_tuple(d->alg_id, d->model_id, d->precision, d->n_states));
+            if (it != h->tuned.end()) {
+                lanes = it->second.lanes;
+                pl->block = it->second.block;
+                pl->scheduler = it->second.scheduler;
+            }
+        }
+        pl->v = find_variant(d->alg_id, d->model_id, d->precision, d->n_states, lanes);
+        if (!pl->v) {
             char buf[160];
             std::snprintf(buf, sizeof buf, "no compiled kernel for alg %d model %d precision %d n %d lanes %d",
-                          d->alg_id, d->model_id, d->precision, d->n_states, o->lanes_per_traj);
+                          d->alg_id, d->model_id, d->precision, d->n_states, lanes);
             return fail(h, ODE_E_UNSUPPORTED, buf);
         }
-        if (scheduler == 0) scheduler = 1;
-        CUDA_TRY(h, cudaEventRecord(c.ev0, s));
-        int rc = launch_variant(h, v, a, scheduler, o->block_size, c.d_queue, s);
-        if (rc) return rc;
-        CUDA_TRY(h, cudaEventRecord(c.ev1, s));
+        if (pl->scheduler == 0) pl->scheduler = 1;
         return ODE_OK;
     }
-    // Uneven sizes: bucket by state count on the device, then integrate every
-    // class in one persistent launch (no host round trip); without a fused
-    // kernel for this method, one persistent kernel per class on the class streams.
     if (d->model_id != ODE_MODEL_DUFFING_CHAIN)
         return fail(h, ODE_E_UNSUPPORTED, "per-trajectory sizes are supported for DUFFING_CHAIN");
-    if ((size_t)N > c.order_cap) {
-        if (c.d_order) cudaFree(c.d_order);
-        c.d_order = nullptr;
-        c.order_cap = 0;
-        CUDA_TRY(h, cudaMalloc(&c.d_order, sizeof(long long) * (size_t)N));
-        c.order_cap = (size_t)N;
-    }
+    pl->fv = o->lanes_per_traj <= 0 ? find_fused(d->alg_id, d->model_id, d->precision) : nullptr;
+    pl->per_class = pl->fv == nullptr;
+    if (pl->scheduler == 0) pl->scheduler = 2;
+    return ODE_OK;
+}
+
+// Enqueue a uniform or one-launch uneven solve (device work only, no host
+// synchronisation: capturable in a CUDA graph).
+int enqueue_plan(ode_handle* h, Ctx& c, const Plan& pl, EnsembleArgs a, const int32_t* npt_dev, cudaStream_t s) {
+    if (pl.v) return launch_variant(h, pl.v, a, pl.scheduler, pl.block, c.d_queue, s);
     unsigned long long* ctr = c.d_queue;
     CUDA_TRY(h, cudaMemsetAsync(ctr + kOffCounts, 0, (kCounters - kOffCounts) * sizeof(unsigned long long), s));
-    enqueue_bucketing(npt_dev, N, ctr, c.d_order, nsaved, retcode, s);
+    enqueue_bucketing(npt_dev, a.N, ctr, c.d_order, a.nsaved, a.retcode, s);
     h->launches += 2;
     a.order = c.d_order;
-    const FusedVariant* fv = o->lanes_per_traj <= 0 ? find_fused(d->alg_id, d->model_id, d->precision) : nullptr;
-    if (fv) {
-        CUDA_TRY(h, cudaEventRecord(c.ev0, s));
-        cudaError_t e = launch_fused(fv, a, ctr, h->sm_count, s);
-        if (e != cudaSuccess) return fail(h, ODE_E_CUDA, std::string("launch ") + fv->name + ": " + cudaGetErrorString(e));
-        h->launches++;
-        CUDA_TRY(h, cudaEventRecord(c.ev1, s));
-        return ODE_OK;
-    }
+    cudaError_t e = launch_fused(pl.fv, a, ctr, h->sm_count, s);
+    if (e != cudaSuccess) return fail(h, ODE_E_CUDA, std::string("launch ") + pl.fv->name + ": " + cudaGetErrorString(e));
+    h->launches++;
+    return ODE_OK;
+}
+
+// Uneven sizes without a fused kernel: one persistent kernel per size class on
+// the class streams (the counts are read back to size the launches).
+int run_per_class(ode_handle* h, Ctx& c, const ode_problem_desc* d, const ode_options* o, const Plan& pl,
+                  EnsembleArgs a, const int32_t* npt_dev, cudaStream_t s) {
+    unsigned long long* ctr = c.d_queue;
+    CUDA_TRY(h, cudaMemsetAsync(ctr + kOffCounts, 0, (kCounters - kOffCounts) * sizeof(unsigned long long), s));
+    enqueue_bucketing(npt_dev, a.N, ctr, c.d_order, a.nsaved, a.retcode, s);
+    h->launches += 2;
     unsigned long long hc[kNumClasses + 1] = {0};
     CUDA_TRY(h, cudaMemcpyAsync(hc, ctr + kOffCounts, sizeof(hc), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(h, cudaStreamSynchronize(s));
@@ -451,7 +475,6 @@ int run_ensemble(ode_handle* h, Ctx& c, const ode_problem_desc* d, const ode_opt
     unsigned long long acc = 0;
     for (int k = 0; k < kNumClasses; ++k) { off[k] = acc; acc += hc[k]; }
     CUDA_TRY(h, cudaEventRecord(c.ev0, s));
-    if (scheduler == 0) scheduler = 2;
     for (int k = 0; k < kNumClasses; ++k) {
         if (hc[k] == 0) continue;
         const KernelVariant* v = find_variant(d->alg_id, d->model_id, d->precision, kClassN[k], 0);
@@ -460,11 +483,92 @@ int run_ensemble(ode_handle* h, Ctx& c, const ode_problem_desc* d, const ode_opt
         EnsembleArgs ac = a;
         ac.order = c.d_order + off[k];
         ac.count = (long long)hc[k];
-        int rc = launch_variant(h, v, ac, scheduler, o->block_size, ctr + kOffClassQ + k, c.class_streams[k]);
+        int rc = launch_variant(h, v, ac, pl.scheduler, o->block_size, ctr + kOffClassQ + k, c.class_streams[k]);
         if (rc) return rc;
         CUDA_TRY(h, cudaEventRecord(c.class_events[k], c.class_streams[k]));
         CUDA_TRY(h, cudaStreamWaitEvent(s, c.class_events[k], 0));
     }
+    CUDA_TRY(h, cudaEventRecord(c.ev1, s));
+    return ODE_OK;
+}
+
+// Enqueue the whole ensemble on stream s using the scratch of ctx c.  All
+// pointers are device pointers.  With `graph`, a solve whose arguments,
+// kernels and stream equal the previous one of this context replays that
+// solve's CUDA graph (memsets, bucketing and integrator launches as one
+// graph launch); a new solve is captured and instantiated once.
+int run_ensemble(ode_handle* h, Ctx& c, const ode_problem_desc* d, const ode_options* o, int64_t N,
+                 const int32_t* npt_dev, const double* u0, const double* p, const double* tspan,
+                 const double* saveat, double* t_out, double* u_out, int32_t* nsaved, int32_t* retcode,
+                 OdeStatsDev* stats, cudaStream_t s, bool graph = false) {
+    EnsembleArgs a = make_args(h, d, o, N, u0, p, tspan, saveat, t_out, u_out, nsaved, retcode, stats);
+    if (N == 0) return ODE_OK;
+    Plan pl;
+    int rc = make_plan(h, d, o, npt_dev, &pl);
+    if (rc) return rc;
+    if (npt_dev && (size_t)N > c.order_cap) {
+        if (c.d_order) cudaFree(c.d_order);
+        c.d_order = nullptr;
+        c.order_cap = 0;
+        CUDA_TRY(h, cudaMalloc(&c.d_order, sizeof(long long) * (size_t)N));
+        c.order_cap = (size_t)N;
+    }
+    if (pl.per_class) return run_per_class(h, c, d, o, pl, a, npt_dev, s);
+    if (!graph || s == nullptr) {
+        CUDA_TRY(h, cudaEventRecord(c.ev0, s));
+        rc = enqueue_plan(h, c, pl, a, npt_dev, s);
+        if (rc) return rc;
+        CUDA_TRY(h, cudaEventRecord(c.ev1, s));
+        return ODE_OK;
+    }
+    struct Key {
+        EnsembleArgs a;
+        const void* kernel;
+        const int32_t* npt;
+        cudaStream_t s;
+        int block, scheduler;
+    } key;
+    std::memset(&key, 0, sizeof(key));
+    key.a = a;
+    key.kernel = pl.v ? (const void*)pl.v : (const void*)pl.fv;
+    key.npt = npt_dev;
+    key.s = s;
+    key.block = pl.block;
+    key.scheduler = pl.scheduler;
+    const unsigned char* kb = reinterpret_cast<const unsigned char*>(&key);
+    const bool hit = c.graph && c.graph_key.size() == sizeof(key) && std::memcmp(c.graph_key.data(), kb, sizeof(key)) == 0;
+    if (!hit) {
+        if (c.graph) cudaGraphExecDestroy(c.graph);
+        c.graph = nullptr;
+        c.graph_key.clear();
+        const long long before = h->launches.load();
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            rc = enqueue_plan(h, c, pl, a, npt_dev, s);
+            e = cudaStreamEndCapture(s, &g);
+        }
+        const long long kernels = h->launches.load() - before;
+        h->launches -= kernels;   // captured, not launched yet
+        cudaGraphExec_t ex = nullptr;
+        if (rc == ODE_OK && e == cudaSuccess && g) e = cudaGraphInstantiate(&ex, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (rc != ODE_OK || e != cudaSuccess || !ex) {   // not capturable here: enqueue directly
+            if (ex) cudaGraphExecDestroy(ex);
+            cudaGetLastError();
+            CUDA_TRY(h, cudaEventRecord(c.ev0, s));
+            rc = enqueue_plan(h, c, pl, a, npt_dev, s);
+            if (rc) return rc;
+            CUDA_TRY(h, cudaEventRecord(c.ev1, s));
+            return ODE_OK;
+        }
+        c.graph = ex;
+        c.graph_key.assign(kb, kb + sizeof(key));
+        c.graph_kernels = kernels;
+    }
+    CUDA_TRY(h, cudaEventRecord(c.ev0, s));
+    CUDA_TRY(h, cudaGraphLaunch(c.graph, s));
+    h->launches += c.graph_kernels;
     CUDA_TRY(h, cudaEventRecord(c.ev1, s));
     return ODE_OK;
 }
@@ -802,7 +906,7 @@ int ode_solve_ensemble_device(ode_handle* h, const ode_problem_desc* d, const od
     *h->h_abort = 0;
     cudaStream_t s = cuda_stream ? (cudaStream_t)cuda_stream : h->main.stream;
     return run_ensemble(h, h->main, d, o, N, npt_dev, u0, p, tspan, saveat, t_out, u_out, nsaved, retcode,
-                        (OdeStatsDev*)stats, s);
+                        (OdeStatsDev*)stats, s, /*graph=*/true);
 }
 
 int ode_solve_ensemble(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int64_t N,
@@ -835,7 +939,7 @@ int ode_solve_ensemble(ode_handle* h, const ode_problem_desc* d, const ode_optio
     rc = run_ensemble(h, h->main, d, o, N, npt ? (const int32_t*)h->b_npt.p : nullptr, (const double*)h->b_u0.p,
                       (const double*)h->b_p.p, (const double*)h->b_tspan.p, (const double*)h->b_saveat.p,
                       (double*)h->b_t.p, (double*)h->b_u.p, (int32_t*)h->b_ns.p, (int32_t*)h->b_rc.p,
-                      (OdeStatsDev*)h->b_st.p, s);
+                      (OdeStatsDev*)h->b_st.p, s, /*graph=*/true);
     if (rc) {
         cudaStreamSynchronize(s);
         return rc;
@@ -992,6 +1096,83 @@ int ode_last_kernel_ms(const ode_handle* h, double* ms) {
         return ODE_OK;
     }
     *ms = h->last_ms;
+    return ODE_OK;
+}
+
+int ode_autotune(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int64_t N, const double* u0,
+                 const double* p, const double* tspan, const double* saveat, int32_t* lanes_out,
+                 int32_t* block_out, int32_t* scheduler_out, double* ms_out) {
+    int rc = validate(h, d, o, N);
+    if (rc) return rc;
+    if (N <= 0 || !u0 || !p || !tspan) return fail(h, ODE_E_INVALID, "autotune needs a non-empty sample");
+    if (o->nsave > 0 && !saveat) return fail(h, ODE_E_INVALID, "nsave > 0 but saveat is null");
+    std::lock_guard<std::mutex> lk(h->api_mu);
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    *h->h_abort = 0;
+    const size_t n = (size_t)d->n_states, np = (size_t)d->n_params, cap = save_cap(o);
+    const size_t nsv = (size_t)o->nsave * (o->saveat_per_traj ? (size_t)N : 1);
+    if ((rc = grow(h, h->b_u0, n * N * 8)) || (rc = grow(h, h->b_p, np * N * 8)) ||
+        (rc = grow(h, h->b_tspan, 2 * N * 8)) || (rc = grow(h, h->b_saveat, nsv * 8)) ||
+        (rc = grow(h, h->b_t, cap * N * 8)) || (rc = grow(h, h->b_u, cap * n * N * 8)) ||
+        (rc = grow(h, h->b_ns, N * 4)) || (rc = grow(h, h->b_rc, N * 4)) ||
+        (rc = grow(h, h->b_st, N * sizeof(ode_stats))))
+        return rc;
+    cudaStream_t s = h->main.stream;
+    CUDA_TRY(h, cudaMemcpyAsync(h->b_u0.p, u0, n * N * 8, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(h, cudaMemcpyAsync(h->b_p.p, p, np * N * 8, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(h, cudaMemcpyAsync(h->b_tspan.p, tspan, 2 * N * 8, cudaMemcpyHostToDevice, s));
+    if (nsv) CUDA_TRY(h, cudaMemcpyAsync(h->b_saveat.p, saveat, nsv * 8, cudaMemcpyHostToDevice, s));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CUDA_TRY(h, cudaEventCreate(&e0));
+    CUDA_TRY(h, cudaEventCreate(&e1));
+    Ctx& c = h->main;
+    double best = -1.0;
+    ode_handle::Tuned pick{0, 0, 0, 0.0};
+    const int blocks[3] = {32, 64, 128};
+    rc = ODE_OK;
+    for (const auto& v : all_variants()) {
+        if (v.alg != d->alg_id || v.model != d->model_id || v.prec != d->precision || v.n != d->n_states) continue;
+        for (int bi = 0; bi < 3 && rc == ODE_OK; ++bi) {
+            for (int sched = 1; sched <= 2 && rc == ODE_OK; ++sched) {
+                ode_options ot = *o;
+                ot.lanes_per_traj = v.lanes;
+                ot.block_size = blocks[bi];
+                ot.scheduler = sched;
+                double ms = 0.0;
+                for (int rep = 0; rep < 3 && rc == ODE_OK; ++rep) {   // one warm-up, two timed
+                    if (cudaEventRecord(e0, s) != cudaSuccess) { rc = fail(h, ODE_E_CUDA, "event record"); break; }
+                    rc = run_ensemble(h, c, d, &ot, N, nullptr, (const double*)h->b_u0.p, (const double*)h->b_p.p,
+                                      (const double*)h->b_tspan.p, (const double*)h->b_saveat.p, (double*)h->b_t.p,
+                                      (double*)h->b_u.p, (int32_t*)h->b_ns.p, (int32_t*)h->b_rc.p,
+                                      (OdeStatsDev*)h->b_st.p, s);
+                    if (rc) break;
+                    float f = 0.0f;
+                    if (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                        cudaEventElapsedTime(&f, e0, e1) != cudaSuccess) {
+                        rc = fail(h, ODE_E_CUDA, "autotune timing");
+                        break;
+                    }
+                    if (rep > 0) ms += 0.5 * f;
+                }
+                if (rc == ODE_OK && (best < 0.0 || ms < best)) {
+                    best = ms;
+                    pick = {v.lanes, blocks[bi], sched, ms};
+                }
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (best < 0.0) return fail(h, ODE_E_UNSUPPORTED, "no compiled kernel for this problem");
+    {
+        std::lock_guard<std::mutex> tl(h->tune_mu);
+        h->tuned[std::make_tuple(d->alg_id, d->model_id, d->precision, d->n_states)] = pick;
+    }
+    if (lanes_out) *lanes_out = pick.lanes;
+    if (block_out) *block_out = pick.block;
+    if (scheduler_out) *scheduler_out = pick.scheduler;
+    if (ms_out) *ms_out = pick.ms;
     return ODE_OK;
 }
 

@@ -59,6 +59,8 @@ SIGNATURES = {
                              _DP, _DP, _DP, _DP, _IP, _IP, C.POINTER(Stats), C.POINTER(C.c_uint64)]),
     "ode_poll": (C.c_int, [_VP, C.c_uint64, _IP]),
     "ode_wait": (C.c_int, [_VP, C.c_uint64, C.c_double]),
+    "ode_autotune": (C.c_int, [_VP, C.POINTER(ProblemDesc), C.POINTER(Options), C.c_int64, _DP, _DP, _DP, _DP,
+                               _IP, _IP, _IP, _DP]),
     "ode_next_completed": (C.c_int, [_VP, C.c_double, C.POINTER(C.c_uint64), _IP, C.POINTER(C.c_double)]),
     "ode_serving_stats_get": (C.c_int, [_VP, C.POINTER(ServingStats)]),
     "ode_set_serving_slots": (C.c_int, [_VP, C.c_int32]),

@@ -268,6 +268,31 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
     return out
 
 
+def autotune(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=1e-6):
+    """Time every compiled launch shape (lanes per trajectory, block size,
+    scheduler) on this sample and keep the fastest for later solves of the same
+    (alg, model, precision, n) on the ensemble's device handle (used when the
+    EnsembleGB300 leaves lanes_per_traj, block_size and scheduler at auto)."""
+    L = _lib.load()
+    if isinstance(model, str):
+        model = MODELS[model]
+    u0s = np.ascontiguousarray(u0s, dtype=np.float64)
+    ps = np.ascontiguousarray(ps, dtype=np.float64)
+    tspans = np.ascontiguousarray(tspans, dtype=np.float64)
+    n, N = u0s.shape
+    sv = resolve_saveat(saveat, tspans)
+    o = _options(reltol, abstol, None, None, None, 1000000, sv, ens, None, None)
+    d = _lib.ProblemDesc(model, alg.alg_id, n, ps.shape[0], ens.prec_id(), 0)
+    h = get_handle(ens.device)
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    lanes, block, sched, ms = C.c_int32(0), C.c_int32(0), C.c_int32(0), C.c_double(0)
+    _lib.check(L.ode_autotune(h, C.byref(d), C.byref(o), N, dp(u0s), dp(ps), dp(tspans),
+                              dp(sv.values) if sv.nsave else None, C.byref(lanes), C.byref(block),
+                              C.byref(sched), C.byref(ms)), h)
+    return {"lanes_per_traj": lanes.value, "block_size": block.value,
+            "scheduler": {1: "static", 2: "persistent"}.get(sched.value, sched.value), "ms": ms.value}
+
+
 def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, saveat=None, reltol=1e-3,
           abstol=1e-6, dt=None, dtmax=None, dtmin=None, maxiters=1000000, save_start=None, save_end=None,
           seed=0, qmax_first_step=None, qmax=None):
