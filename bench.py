@@ -111,16 +111,36 @@ def parse():
     return ap.parse_args()
 
 
-def dist_setup(args):
+def dist_setup(args, backend=None, timeout_s=300.0):
+    """One process per GPU (torchrun environment).  Replicas only: the ranks
+    meet at barriers and in one max-reduction of their times; a rank that dies
+    makes the others' next collective fail within timeout_s instead of hanging."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     dist = None
     if world > 1:
+        import datetime
         import torch.distributed as dist
-        backend = "nccl" if args.impl == "gb300" else "gloo"
-        dist.init_process_group(backend)
+        if backend is None:
+            backend = "nccl" if args.impl == "gb300" else "gloo"
+        dist.init_process_group(backend, timeout=datetime.timedelta(seconds=timeout_s))
     return world, rank, local, dist
+
+
+def max_over_ranks(x, dist, device="cpu"):
+    """The job's time is its slowest replica's: max of x over the ranks."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(world, n_per_rank, seconds):
+    """Whole-job throughput: every rank integrates n_per_rank trajectories."""
+    return world * n_per_rank / seconds
 
 
 def workload(name, N, seed):
@@ -310,11 +330,7 @@ def run_gb300(args, world, rank, local, dist):
         if prec == "mixed":
             clk = clocks.stop()
         nl = launches() - l0
-        ms = float(np.mean(times))
-        if dist is not None:
-            tt = torch.tensor([ms], device=dev)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            ms = float(tt.item())
+        ms = max_over_ranks(float(np.mean(times)), dist, dev)
         st = st_out.cpu().numpy()
         rc = rc_out.cpu().numpy()
         attempts = int(st[:, 4].sum() + st[:, 5].sum())
@@ -336,7 +352,7 @@ def run_gb300(args, world, rank, local, dist):
         equal = all(acc_truth["mixed"][q] <= 2.0 * acc_truth["fp64"][q] + 1.0 for q in ("median", "p99"))
     best = "mixed" if equal else "fp64"
     R = results[best]
-    value = world * N / (R["ms"] * 1e-3)
+    value = replica_rate(world, N, R["ms"] * 1e-3)
 
     # roofline of the dominant kernel (the chosen form's integrator kernel)
     peak = C.c_double(0)

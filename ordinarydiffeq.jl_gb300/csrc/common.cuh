@@ -172,6 +172,13 @@ __device__ __forceinline__ ff operator+(ff a, ff b) {
 }
 __device__ __forceinline__ ff operator-(ff a) { return ff(-a.hi, -a.lo); }
 __device__ __forceinline__ ff operator-(ff a, ff b) { return a + (-b); }
+// a * b for a float b (error-free product of the leading part plus the tail)
+__device__ __forceinline__ ff ff_mul_f(ff a, float b) {
+    const float p = a.hi * b;
+    float e = fmaf(a.hi, b, -p);
+    e = fmaf(a.lo, b, e);
+    return ff_fast2sum(p, e);
+}
 __device__ __forceinline__ ff operator*(ff a, ff b) {
     float p = a.hi * b.hi;
     float e = fmaf(a.hi, b.hi, -p);

@@ -28,6 +28,13 @@ __device__ __forceinline__ double interp_weight(double th, int i, RF r, bool fir
     for (int q = NPOLY - 2; q >= (first ? 1 : 2); --q) acc = fma(th, acc, r(i, q));
     return first ? th * acc : (th * th) * acc;
 }
+// Mixed form: the weights stay FP64 (a save is rare and the FP64 pipe is
+// otherwise idle there; a double-float Horner measured slower on the FP32
+// issue path) and are split once into float pairs for the compensated sums.
+__device__ __forceinline__ ff split_weight(double w) {
+    const float h = (float)w;
+    return ff(h, (float)(w - (double)h));
+}
 
 struct Tsit5Alg {
     static constexpr int ORDER = 5;
@@ -79,29 +86,34 @@ struct Tsit5Alg {
     }
 
     template <class Model, class R, int L, int C>
-    __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, double th, double dt, double, const R* y0,
-                                       const R* y0lo, const R*, const R*, const R*, const Group<L>&) {
+    __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, typename Ctl<R>::T th, double dt, double,
+                                       const R* y0, const R* y0lo, const R*, const R*, const R*, const Group<L>&) {
         auto r = [](int i, int q) { return tab::TSIT5_R(i, q); };
-        double b[8];
-        b[1] = interp_weight<5>(th, 1, r, true);
-#pragma unroll
-        for (int i = 2; i <= 7; ++i) b[i] = interp_weight<5>(th, i, r, false);
         const R d = (R)dt;
+        if constexpr (sizeof(R) == 8) {
+            double b[8];
+            b[1] = interp_weight<5>(th, 1, r, true);
 #pragma unroll
-        for (int i = 0; i < C; ++i) {
-            R S;
-            if (sizeof(R) == 8) {
+            for (int i = 2; i <= 7; ++i) b[i] = interp_weight<5>(th, i, r, false);
+#pragma unroll
+            for (int i = 0; i < C; ++i) {
                 R acc = c.k[6][i] * (R)b[7];
 #pragma unroll
                 for (int s = 6; s >= 1; --s) acc = FMA(c.k[s - 1][i], (R)b[s], acc);
-                S = acc;
-            } else {
+                Acc<R>::update(out[i], outlo[i], d, acc, y0[i], y0lo[i]);
+            }
+        } else {
+            ff b[8];
+            b[1] = split_weight(interp_weight<5>((double)th, 1, r, true));
+#pragma unroll
+            for (int i = 2; i <= 7; ++i) b[i] = split_weight(interp_weight<5>((double)th, i, r, false));
+#pragma unroll
+            for (int i = 0; i < C; ++i) {
                 CSum cs;
 #pragma unroll
-                for (int s = 1; s <= 7; ++s) cs.add(b[s], (float)c.k[s - 1][i]);
-                S = (R)cs.value();
+                for (int s = 1; s <= 7; ++s) cs.add_pair(b[s].hi, b[s].lo, (float)c.k[s - 1][i]);
+                Acc<R>::update(out[i], outlo[i], d, (R)cs.value(), y0[i], y0lo[i]);
             }
-            Acc<R>::update(out[i], outlo[i], d, S, y0[i], y0lo[i]);
         }
     }
 };
@@ -171,33 +183,38 @@ struct Vern7Alg {
     }
 
     template <class Model, class R, int L, int C>
-    __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, double th, double dt, double tprev,
-                                       const R* y0, const R* y0lo, const R*, const R*, const R* p,
+    __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, typename Ctl<R>::T th, double dt,
+                                       double tprev, const R* y0, const R* y0lo, const R*, const R*, const R* p,
                                        const Group<L>& g) {
         if (!c.extra) extra_stages<Model, R, L, C>(c, tprev, dt, y0, y0lo, p, g);
         // stages of the 7th-order interpolant, in the reference's summation order
         constexpr int idx[13] = {1, 4, 5, 6, 7, 8, 9, 11, 12, 13, 14, 15, 16};
         auto r = [](int i, int q) { return tab::VERN7_R(i, q); };
-        double b[13];
-        b[0] = interp_weight<8>(th, 1, r, true);
-#pragma unroll
-        for (int q = 1; q < 13; ++q) b[q] = interp_weight<8>(th, idx[q], r, false);
         const R d = (R)dt;
+        if constexpr (sizeof(R) == 8) {
+            double b[13];
+            b[0] = interp_weight<8>(th, 1, r, true);
 #pragma unroll
-        for (int i = 0; i < C; ++i) {
-            R S;
-            if (sizeof(R) == 8) {
+            for (int q = 1; q < 13; ++q) b[q] = interp_weight<8>(th, idx[q], r, false);
+#pragma unroll
+            for (int i = 0; i < C; ++i) {
                 R acc = c.s[Vern7Tab::slot(16)][i] * (R)b[12];
 #pragma unroll
                 for (int q = 11; q >= 0; --q) acc = FMA(c.s[Vern7Tab::slot(idx[q])][i], (R)b[q], acc);
-                S = acc;
-            } else {
+                Acc<R>::update(out[i], outlo[i], d, acc, y0[i], y0lo[i]);
+            }
+        } else {
+            ff b[13];
+            b[0] = split_weight(interp_weight<8>((double)th, 1, r, true));
+#pragma unroll
+            for (int q = 1; q < 13; ++q) b[q] = split_weight(interp_weight<8>((double)th, idx[q], r, false));
+#pragma unroll
+            for (int i = 0; i < C; ++i) {
                 CSum cs;
 #pragma unroll
-                for (int q = 0; q < 13; ++q) cs.add(b[q], (float)c.s[Vern7Tab::slot(idx[q])][i]);
-                S = (R)cs.value();
+                for (int q = 0; q < 13; ++q) cs.add_pair(b[q].hi, b[q].lo, (float)c.s[Vern7Tab::slot(idx[q])][i]);
+                Acc<R>::update(out[i], outlo[i], d, (R)cs.value(), y0[i], y0lo[i]);
             }
-            Acc<R>::update(out[i], outlo[i], d, S, y0[i], y0lo[i]);
         }
     }
 };

@@ -73,6 +73,18 @@ __device__ __forceinline__ bool plt(double a, double b) {
     long long x = __double_as_longlong(a), y = __double_as_longlong(b);
     return !bits_nan(x) && !bits_nan(y) && x < y;
 }
+// Order-preserving integer key of a double of either sign (-0 and +0 equal).
+__device__ __forceinline__ long long okey(double x) {
+    const long long b = __double_as_longlong(x);
+    return b >= 0 ? b : -(b & 0x7fffffffffffffffLL);
+}
+// a <= b and a == b for doubles of either sign, false when either is NaN (IEEE).
+__device__ __forceinline__ bool dle(double a, double b) {
+    return !bits_nan(__double_as_longlong(a)) && !bits_nan(__double_as_longlong(b)) && okey(a) <= okey(b);
+}
+__device__ __forceinline__ bool deq(double a, double b) {
+    return !bits_nan(__double_as_longlong(a)) && !bits_nan(__double_as_longlong(b)) && okey(a) == okey(b);
+}
 // 100 * eps(x), exactly: eps is a power of two 2^k and 100 * 2^k = 1.5625 * 2^(k+6).
 __device__ __forceinline__ double ptol100(double x) {
     const double e = peps(x);
@@ -87,11 +99,16 @@ template <> struct Ctl<double> {   // FP64: the reference's arithmetic
     using T = double;
     static __device__ __forceinline__ double pw(double x, double y) { return ctrl_pow(x, y); }
     static __device__ __forceinline__ double scale_dt(double dt, double q) { return dt / q; }
+    // interpolation abscissa theta = (t_save - tprev) / dt
+    static __device__ __forceinline__ double theta(double num, double dt) { return num / dt; }
 };
 template <> struct Ctl<float> {    // mixed: FP32 factors, FP64 dt
     using T = float;
     static __device__ __forceinline__ float pw(float x, float y) { return exp2f(y * log2f(x)); }
     static __device__ __forceinline__ double scale_dt(double dt, float q) { return dt * (double)(1.0f / q); }
+    // theta in FP32: a relative error of 6e-8 in theta moves a save by 6e-8 of
+    // one step's change, far below the tolerance
+    static __device__ __forceinline__ float theta(double num, double dt) { return (float)num / (float)dt; }
 };
 
 struct Ctrl {
@@ -297,7 +314,7 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             const double tol = ptol100(pmax(pabs(t), pabs(tf)));
             const double orig = pabs(dt);
             dtpropose = orig;
-            next_tstop = !(orig + tol < dist);
+            next_tstop = !plt(orig + tol, dist);
             dt = pmin(orig, dist);
         }
         // ---- check_error (de_check_error)
@@ -355,16 +372,16 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             // ---- savevalues!
             while (isave < a.nsave) {
                 double curt = saveat_at(isave);
-                if (!(curt <= t)) break;
+                if (!dle(curt, t)) break;
                 isave++;
-                if (curt != t) {
-                    double th = (curt - tprev) / dt;
+                if (!deq(curt, t)) {
+                    const CT th = Ctl<R>::theta(curt - tprev, dt);
                     R out[C], outlo[C];
                     Alg::template interpolate<Model, R, L, C>(cache, out, outlo, th, dt, tprev, uprev, uprevlo, u,
                                                               ulo, p, g);
                     save_point(curt, out, outlo);
                 } else {
-                    if (curt == tf && !a.save_end) continue;
+                    if (deq(curt, tf) && !a.save_end) continue;
                     save_point(t, u, ulo);
                 }
             }

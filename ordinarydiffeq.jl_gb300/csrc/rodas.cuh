@@ -327,21 +327,26 @@ struct Rodas5PT {
     }
 
     template <class Model, class R, int L, int C>
-    __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, double thd, double, double, const R* y0,
-                                       const R* y0lo, const R* y1, const R* y1lo, const R*, const Group<L>&) {
+    __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, typename Ctl<R>::T th, double, double,
+                                       const R* y0, const R* y0lo, const R* y1, const R* y1lo, const R*,
+                                       const Group<L>&) {
         dense<R, C>(c);
-        const R th = (R)thd, th1 = R(1) - th;
+        const R th1 = R(1) - th;
 #pragma unroll
         for (int i = 0; i < C; ++i) {
             R inner = FMA(th, c.dk[2][i], c.dk[1][i]);
             inner = FMA(th, inner, c.dk[0][i]);
-            if (sizeof(R) == 8) {
+            if constexpr (sizeof(R) == 8) {
                 R v = FMA(th1, inner, y1[i]);
                 Acc<R>::set(out[i], outlo[i], FMA(th1, y0[i], th * v));
-            } else {   // a save is rare: combine the compensated end points in FP64
-                double t1 = 1.0 - thd;
-                double v = fma(t1, (double)inner, Acc<R>::join(y1[i], y1lo[i]));
-                Acc<R>::split(fma(t1, Acc<R>::join(y0[i], y0lo[i]), thd * v), out[i], outlo[i]);
+            } else {   // (1-th) y0 + th (y1 + (1-th) inner) on the compensated end points, in double-float
+                float ph, pl;
+                ph = th1 * inner;
+                pl = fmaf(th1, inner, -ph);
+                const ff v = ff(y1[i], y1lo[i]) + ff_fast2sum(ph, pl);
+                const ff o = ff_mul_f(ff(y0[i], y0lo[i]), th1) + ff_mul_f(v, th);
+                out[i] = o.hi;
+                outlo[i] = o.lo;
             }
         }
     }

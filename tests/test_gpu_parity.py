@@ -237,3 +237,48 @@ def test_autotune_picks_a_compiled_shape():
     o = oracle("brusselator_1d", "rodas5p", u0, p, ts, 1.25, 1e-5, 1e-8)
     assert (g["retcode"] == 1).all()
     assert compare(g, o, 1e-5, 1e-8, step_slack=10 ** 9)["ok"]
+
+
+def test_abort_stops_running_kernels():
+    # ode_abort sets a host-mapped flag that the kernels poll every 64 steps;
+    # a solve that would run for seconds ends early with ODE_RC_ABORTED
+    import ctypes as C
+    import time
+    import torch
+    from odegb300 import EnsembleGB300, Tsit5, _lib
+    from odegb300.ensemble import MODELS, _options, get_handle
+    from odegb300.saveat import resolve_saveat
+    L = _lib.load()
+    h = get_handle(0)
+    N = 2048
+    u0, p, ts = lorenz_inputs(N, seed=9)
+    p[1, :] = 28.0 + 0.01 * np.arange(N) / N   # chaotic: steps stay small for the whole span
+    ts[1, :] = 1.0e5   # about 1e7 steps per trajectory: many seconds unaborted
+    sv = resolve_saveat(None, ts)
+    ens = EnsembleGB300()
+    o = _options(1e-8, 1e-8, None, None, None, 10 ** 8, sv, ens, None, None)
+    d = _lib.ProblemDesc(MODELS["lorenz"], Tsit5().alg_id, 3, 3, ens.prec_id(), 0)
+    dev = torch.device("cuda", 0)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    du0, dp, dts = t(u0), t(p), t(ts)
+    cap = sv.nsave + 2
+    tout = torch.empty((cap, N), dtype=torch.float64, device=dev)
+    uout = torch.empty((cap, 3, N), dtype=torch.float64, device=dev)
+    ns = torch.empty(N, dtype=torch.int32, device=dev)
+    rc = torch.empty(N, dtype=torch.int32, device=dev)
+    st = torch.empty((N, 6), dtype=torch.int64, device=dev)
+    stream = torch.cuda.Stream(dev)
+    vp = lambda x: C.c_void_p(x.data_ptr())
+    t0 = time.perf_counter()
+    _lib.check(L.ode_solve_ensemble_device(h, C.byref(d), C.byref(o), N, None, vp(du0), vp(dp), vp(dts), None,
+                                           vp(tout), vp(uout), vp(ns), vp(rc), vp(st),
+                                           C.c_void_p(stream.cuda_stream)), h)
+    time.sleep(0.05)
+    _lib.check(L.ode_abort(h), h)
+    stream.synchronize()
+    elapsed = time.perf_counter() - t0
+    r = rc.cpu().numpy()
+    assert (r == 6).all(), np.unique(r, return_counts=True)
+    assert elapsed < 5.0, elapsed
+    naccept = st.cpu().numpy()[:, 4]
+    assert (naccept > 0).all() and (naccept < 10 ** 7).all()
