@@ -22,6 +22,17 @@ template <> struct Arith<float> {
 template <class T> __device__ __forceinline__ T FMA(T a, T b, T c) { return Arith<T>::fma_(a, b, c); }
 template <class T> __device__ __forceinline__ T ABS(T a) { return Arith<T>::abs_(a); }
 
+// |x| as a bit pattern, on the integer pipe.  Written in inline PTX because
+// the optimizer recognises a masked sign bit as a floating-point abs (an FP64
+// instruction on GB300's narrow FP64 pipe) and masked-bit comparisons as
+// floating-point tests; the time and pivot helpers below rely on this.
+__device__ __forceinline__ long long abs_bits_i(long long b) {
+    long long r;
+    asm("and.b64 %0, %1, %2;" : "=l"(r) : "l"(b), "l"(0x7fffffffffffffffLL));
+    return r;
+}
+__device__ __forceinline__ long long abs_bits(double x) { return abs_bits_i(__double_as_longlong(x)); }
+
 // Julia's Base.min/max on floats propagate NaN.
 __device__ __forceinline__ double jmin(double a, double b) { return (a != a || b != b) ? __longlong_as_double(0x7ff8000000000000LL) : (a < b ? a : b); }
 __device__ __forceinline__ double jmax(double a, double b) { return (a != a || b != b) ? __longlong_as_double(0x7ff8000000000000LL) : (a > b ? a : b); }

@@ -14,10 +14,26 @@
 namespace odegb {
 
 #define HDC __host__ __device__ static constexpr
-struct Tsit5Sol { HDC int last() { return 6; } HDC double w(int j) { return tab::TSIT5_A(7, j); } HDC bool m(int j) { return j >= 1 && j <= 6; } };
-struct Tsit5Err { HDC int last() { return 7; } HDC double w(int j) { return tab::TSIT5_BT(j); } HDC bool m(int j) { return j >= 1 && j <= 7; } };
-struct Vern7Sol { HDC int last() { return 9; } HDC double w(int j) { return tab::VERN7_B(j); } HDC bool m(int j) { return tab::VERN7_BM(j); } };
-struct Vern7Err { HDC int last() { return 10; } HDC double w(int j) { return tab::VERN7_BT(j); } HDC bool m(int j) { return tab::VERN7_BTM(j); } };
+struct Tsit5Sol {
+    HDC int last() { return 6; } HDC bool m(int j) { return j >= 1 && j <= 6; }
+    HDC double w(int j) { return tab::TSIT5_A(7, j); }
+    HDC float whi(int j) { return tab::TSIT5_A_HI(7, j); } HDC float wlo(int j) { return tab::TSIT5_A_LO(7, j); }
+};
+struct Tsit5Err {
+    HDC int last() { return 7; } HDC bool m(int j) { return j >= 1 && j <= 7; }
+    HDC double w(int j) { return tab::TSIT5_BT(j); }
+    HDC float whi(int j) { return tab::TSIT5_BT_HI(j); } HDC float wlo(int j) { return tab::TSIT5_BT_LO(j); }
+};
+struct Vern7Sol {
+    HDC int last() { return 9; } HDC bool m(int j) { return tab::VERN7_BM(j); }
+    HDC double w(int j) { return tab::VERN7_B(j); }
+    HDC float whi(int j) { return tab::VERN7_B_HI(j); } HDC float wlo(int j) { return tab::VERN7_B_LO(j); }
+};
+struct Vern7Err {
+    HDC int last() { return 10; } HDC bool m(int j) { return tab::VERN7_BTM(j); }
+    HDC double w(int j) { return tab::VERN7_BT(j); }
+    HDC float whi(int j) { return tab::VERN7_BT_HI(j); } HDC float wlo(int j) { return tab::VERN7_BT_LO(j); }
+};
 #undef HDC
 
 // Interpolation weights b_i(theta): Horner in FP64 (the reference's @evalpoly).
@@ -65,19 +81,19 @@ struct Tsit5Alg {
         const R d = (R)dt;
         R* tmp = c.tmp;
         K::template stage<2>(tmp, c.k, d, up, uplo);
-        Model::template rhs<R, L, C>(c.k[1], tmp, p, fma(Tsit5Tab::c(2), dt, t), g);
+        Model::template rhs<R, L, C>(c.k[1], tmp, p, stage_time<Model>(Tsit5Tab::c(2), dt, t), g);
         K::template stage<3>(tmp, c.k, d, up, uplo);
-        Model::template rhs<R, L, C>(c.k[2], tmp, p, fma(Tsit5Tab::c(3), dt, t), g);
+        Model::template rhs<R, L, C>(c.k[2], tmp, p, stage_time<Model>(Tsit5Tab::c(3), dt, t), g);
         K::template stage<4>(tmp, c.k, d, up, uplo);
-        Model::template rhs<R, L, C>(c.k[3], tmp, p, fma(Tsit5Tab::c(4), dt, t), g);
+        Model::template rhs<R, L, C>(c.k[3], tmp, p, stage_time<Model>(Tsit5Tab::c(4), dt, t), g);
         K::template stage<5>(tmp, c.k, d, up, uplo);
-        Model::template rhs<R, L, C>(c.k[4], tmp, p, fma(Tsit5Tab::c(5), dt, t), g);
+        Model::template rhs<R, L, C>(c.k[4], tmp, p, stage_time<Model>(Tsit5Tab::c(5), dt, t), g);
         K::template stage<6>(tmp, c.k, d, up, uplo);
-        Model::template rhs<R, L, C>(c.k[5], tmp, p, t + dt, g);
+        Model::template rhs<R, L, C>(c.k[5], tmp, p, stage_time<Model>(1.0, dt, t), g);
         K::weights(tmp, c.k, Tsit5Sol());
 #pragma unroll
         for (int i = 0; i < C; ++i) Acc<R>::update(u[i], ulo[i], d, tmp[i], up[i], uplo[i]);
-        Model::template rhs<R, L, C>(c.k[6], u, p, t + dt, g);
+        Model::template rhs<R, L, C>(c.k[6], u, p, stage_time<Model>(1.0, dt, t), g);
         st.nf += 6;
         K::weights(tmp, c.k, Tsit5Err());
 #pragma unroll
@@ -149,15 +165,15 @@ struct Vern7Alg {
         const R d = (R)dt;
         c.extra = false;
         Model::template rhs<R, L, C>(c.s[0], up, p, t, g);
-        eval_stage<2, Model>(c, up, uplo, p, fma(Vern7Tab::c(2), dt, t), d, g);
-        eval_stage<3, Model>(c, up, uplo, p, fma(Vern7Tab::c(3), dt, t), d, g);
-        eval_stage<4, Model>(c, up, uplo, p, fma(Vern7Tab::c(4), dt, t), d, g);
-        eval_stage<5, Model>(c, up, uplo, p, fma(Vern7Tab::c(5), dt, t), d, g);
-        eval_stage<6, Model>(c, up, uplo, p, fma(Vern7Tab::c(6), dt, t), d, g);
-        eval_stage<7, Model>(c, up, uplo, p, fma(Vern7Tab::c(7), dt, t), d, g);
-        eval_stage<8, Model>(c, up, uplo, p, fma(Vern7Tab::c(8), dt, t), d, g);
-        eval_stage<9, Model>(c, up, uplo, p, t + dt, d, g);
-        eval_stage<10, Model>(c, up, uplo, p, t + dt, d, g);
+        eval_stage<2, Model>(c, up, uplo, p, stage_time<Model>(Vern7Tab::c(2), dt, t), d, g);
+        eval_stage<3, Model>(c, up, uplo, p, stage_time<Model>(Vern7Tab::c(3), dt, t), d, g);
+        eval_stage<4, Model>(c, up, uplo, p, stage_time<Model>(Vern7Tab::c(4), dt, t), d, g);
+        eval_stage<5, Model>(c, up, uplo, p, stage_time<Model>(Vern7Tab::c(5), dt, t), d, g);
+        eval_stage<6, Model>(c, up, uplo, p, stage_time<Model>(Vern7Tab::c(6), dt, t), d, g);
+        eval_stage<7, Model>(c, up, uplo, p, stage_time<Model>(Vern7Tab::c(7), dt, t), d, g);
+        eval_stage<8, Model>(c, up, uplo, p, stage_time<Model>(Vern7Tab::c(8), dt, t), d, g);
+        eval_stage<9, Model>(c, up, uplo, p, stage_time<Model>(1.0, dt, t), d, g);
+        eval_stage<10, Model>(c, up, uplo, p, stage_time<Model>(1.0, dt, t), d, g);
         RK<Vern7Tab, R, C>::weights(c.tmp, c.s, Vern7Sol());
 #pragma unroll
         for (int i = 0; i < C; ++i) Acc<R>::update(u[i], ulo[i], d, c.tmp[i], up[i], uplo[i]);
@@ -173,12 +189,12 @@ struct Vern7Alg {
     __device__ static void extra_stages(Cache<R, C>& c, double tprev, double dt, const R* up, const R* uplo,
                                         const R* p, const Group<L>& g) {
         const R d = (R)dt;
-        eval_stage<11, Model>(c, up, uplo, p, fma(Vern7Tab::c(11), dt, tprev), d, g);
-        eval_stage<12, Model>(c, up, uplo, p, fma(Vern7Tab::c(12), dt, tprev), d, g);
-        eval_stage<13, Model>(c, up, uplo, p, fma(Vern7Tab::c(13), dt, tprev), d, g);
-        eval_stage<14, Model>(c, up, uplo, p, fma(Vern7Tab::c(14), dt, tprev), d, g);
-        eval_stage<15, Model>(c, up, uplo, p, fma(Vern7Tab::c(15), dt, tprev), d, g);
-        eval_stage<16, Model>(c, up, uplo, p, fma(Vern7Tab::c(16), dt, tprev), d, g);
+        eval_stage<11, Model>(c, up, uplo, p, stage_time<Model>(Vern7Tab::c(11), dt, tprev), d, g);
+        eval_stage<12, Model>(c, up, uplo, p, stage_time<Model>(Vern7Tab::c(12), dt, tprev), d, g);
+        eval_stage<13, Model>(c, up, uplo, p, stage_time<Model>(Vern7Tab::c(13), dt, tprev), d, g);
+        eval_stage<14, Model>(c, up, uplo, p, stage_time<Model>(Vern7Tab::c(14), dt, tprev), d, g);
+        eval_stage<15, Model>(c, up, uplo, p, stage_time<Model>(Vern7Tab::c(15), dt, tprev), d, g);
+        eval_stage<16, Model>(c, up, uplo, p, stage_time<Model>(Vern7Tab::c(16), dt, tprev), d, g);
         c.extra = true;
     }
 

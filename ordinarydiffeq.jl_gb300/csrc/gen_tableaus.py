@@ -19,6 +19,8 @@ usage: python gen_tableaus.py <reference-root> [out.h]
 """
 import os
 import re
+
+import numpy as np
 import sys
 
 LIT = r"(-?[0-9][0-9_]*(?:\.[0-9]*)?(?:[eE][-+]?[0-9]+)?)"
@@ -103,18 +105,39 @@ def main():
     lines.append("// Accessors are constexpr functions so device code folds them to immediates.")
     lines.append("constexpr double RODAS5P_GAMMA = %s;" % as_double(gamma))
 
+    def f32_split(lit):
+        # x = hi + lo with hi = float(x) (round to nearest) and lo = float(x - hi),
+        # both written as exact hexadecimal float literals
+        x = float(as_double(lit))
+        hi = float(np.float32(x))
+        lo = float(np.float32(x - hi))
+        return hi.hex() + "f", lo.hex() + "f"
+
     def accessor(name, rows, two_d=True):
         if two_d:
             body = ", ".join("{" + ", ".join(as_double(v) for v in r) + "}" for r in rows)
             lines.append("__host__ __device__ constexpr double %s(int i, int j) {" % name)
             lines.append("    constexpr double t[%d][%d] = {%s};" % (len(rows), len(rows[0]), body))
             lines.append("    return t[i][j];")
+            lines.append("}")
+            for part, tag in ((0, "HI"), (1, "LO")):
+                body = ", ".join("{" + ", ".join(f32_split(v)[part] for v in r) + "}" for r in rows)
+                lines.append("__host__ __device__ constexpr float %s_%s(int i, int j) {" % (name, tag))
+                lines.append("    constexpr float t[%d][%d] = {%s};" % (len(rows), len(rows[0]), body))
+                lines.append("    return t[i][j];")
+                lines.append("}")
         else:
             body = ", ".join(as_double(v) for v in rows)
             lines.append("__host__ __device__ constexpr double %s(int i) {" % name)
             lines.append("    constexpr double t[%d] = {%s};" % (len(rows), body))
             lines.append("    return t[i];")
-        lines.append("}")
+            lines.append("}")
+            for part, tag in ((0, "HI"), (1, "LO")):
+                body = ", ".join(f32_split(v)[part] for v in rows)
+                lines.append("__host__ __device__ constexpr float %s_%s(int i) {" % (name, tag))
+                lines.append("    constexpr float t[%d] = {%s};" % (len(rows), body))
+                lines.append("    return t[i];")
+                lines.append("}")
 
     accessor("RODAS5P_A", A)
     accessor("RODAS5P_C", C)

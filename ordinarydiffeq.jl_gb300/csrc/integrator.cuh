@@ -40,7 +40,7 @@ struct StepStats {
 };
 
 // ---------------------------------------------------------------- time helpers (integer pipe)
-__device__ __forceinline__ bool bits_nan(long long b) { return (b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL; }
+__device__ __forceinline__ bool bits_nan(long long b) { return abs_bits_i(b) > 0x7ff0000000000000LL; }
 __device__ __forceinline__ double dnan() { return __longlong_as_double(0x7ff8000000000000LL); }
 // Julia min/max for non-negative doubles (NaN propagates).
 __device__ __forceinline__ double pmin(double a, double b) {
@@ -54,11 +54,11 @@ __device__ __forceinline__ double pmax(double a, double b) {
     return x > y ? a : b;
 }
 __device__ __forceinline__ double pabs(double a) {
-    return __longlong_as_double(__double_as_longlong(a) & 0x7fffffffffffffffLL);
+    return __longlong_as_double(abs_bits(a));
 }
 // Julia eps(x): the spacing of doubles at |x|, built from the exponent bits.
 __device__ __forceinline__ double peps(double x) {
-    long long b = __double_as_longlong(x) & 0x7fffffffffffffffLL;
+    long long b = abs_bits(x);
     if (b >= 0x7ff0000000000000LL) return dnan();
     int e = (int)(b >> 52);
     if (e > 52) return __longlong_as_double((long long)(e - 52) << 52);
@@ -76,7 +76,7 @@ __device__ __forceinline__ bool plt(double a, double b) {
 // Order-preserving integer key of a double of either sign (-0 and +0 equal).
 __device__ __forceinline__ long long okey(double x) {
     const long long b = __double_as_longlong(x);
-    return b >= 0 ? b : -(b & 0x7fffffffffffffffLL);
+    return b >= 0 ? b : -abs_bits_i(b);
 }
 // a <= b and a == b for doubles of either sign, false when either is NaN (IEEE).
 __device__ __forceinline__ bool dle(double a, double b) {
@@ -91,6 +91,15 @@ __device__ __forceinline__ double ptol100(double x) {
     const int ex = (int)(__double_as_longlong(e) >> 52);
     if (ex >= 1 && ex + 6 < 2047) return __longlong_as_double(((long long)(ex + 6) << 52) | 0x9000000000000LL);
     return 100.0 * e;
+}
+
+// Time argument of a stage's right-hand side, t + c dt.  Every registered
+// model is autonomous (f does not read t), so the sum is not formed: it would
+// be one FP64 instruction per stage for a value nobody reads.
+template <class Model>
+__device__ __forceinline__ double stage_time(double c, double dt, double t) {
+    if constexpr (Model::AUTONOMOUS) return t;
+    else return fma(c, dt, t);
 }
 
 // ---------------------------------------------------------------- controller policy

@@ -44,9 +44,9 @@ extern __shared__ __align__(16) unsigned char odegb_dyn_smem[];
 template <class R> struct Bits;
 template <> struct Bits<double> {
     using U = unsigned long long;
-    static __device__ __forceinline__ bool nz(double x) { return (__double_as_longlong(x) << 1) != 0; }
+    static __device__ __forceinline__ bool nz(double x) { return abs_bits(x) != 0; }
     static __device__ __forceinline__ U mag_key(double x) {
-        const U a = (U)__double_as_longlong(x) & 0x7fffffffffffffffULL;
+        const U a = (U)abs_bits(x);
         return a > 0x7ff0000000000000ULL ? U(0) : a;
     }
 };
@@ -93,7 +93,6 @@ __device__ __forceinline__ int group_argmax(unsigned long long key, int pos, con
 }
 
 struct SmemLA {
-    static constexpr bool FP64_RESIDUAL = false;   // refinement residual formed in double-float
     template <class R, int C> struct Store {
         R* W;        // n columns of stride n+1, component-major rows
         R* dinv;     // 1 / pivot, by position

@@ -23,6 +23,7 @@ enum ModelId { M_LINEAR = 0, M_LORENZ = 1, M_ROBERTSON = 2, M_DUFFING = 3, M_BRU
 
 struct Linear {
     static constexpr int NP = 1;
+    static constexpr bool AUTONOMOUS = true;   // f(u, p) does not read t
     template <class R, int L, int C>
     __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>&) {
 #pragma unroll
@@ -39,6 +40,7 @@ struct Linear {
 
 struct Lorenz {
     static constexpr int NP = 3;
+    static constexpr bool AUTONOMOUS = true;   // f(u, p) does not read t
     template <class R, int L, int C>
     __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>&) {
         static_assert(L == 1 && C == 3, "Lorenz has 3 states on one lane");
@@ -56,6 +58,7 @@ struct Lorenz {
 
 struct Robertson {
     static constexpr int NP = 3;
+    static constexpr bool AUTONOMOUS = true;   // f(u, p) does not read t
     template <class R, int L, int C>
     __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>&) {
         static_assert(L == 1 && C == 3, "Robertson has 3 states on one lane");
@@ -83,6 +86,7 @@ __device__ __forceinline__ void chain_halo(const R* u, const Group<L>& g, int of
 
 struct Duffing {
     static constexpr int NP = 3;
+    static constexpr bool AUTONOMOUS = true;   // f(u, p) does not read t
     template <class R, int L, int C>
     __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>& g) {
         static_assert(C % 2 == 0, "Duffing lanes hold whole (x, v) pairs");
@@ -120,6 +124,7 @@ struct Duffing {
 
 struct Brusselator {
     static constexpr int NP = 3;
+    static constexpr bool AUTONOMOUS = true;   // f(u, p) does not read t
     template <class R, int L, int C>
     __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>& g) {
         static_assert(C % 2 == 0, "Brusselator lanes hold whole (u, v) cells");

@@ -20,6 +20,8 @@ namespace odegb {
 struct Tsit5Tab {
     static constexpr int S = 7;
     __host__ __device__ static constexpr double a(int i, int j) { return tab::TSIT5_A(i, j); }
+    __host__ __device__ static constexpr float ahi(int i, int j) { return tab::TSIT5_A_HI(i, j); }
+    __host__ __device__ static constexpr float alo(int i, int j) { return tab::TSIT5_A_LO(i, j); }
     __host__ __device__ static constexpr bool am(int i, int j) { return tab::TSIT5_AM(i, j); }
     __host__ __device__ static constexpr double c(int i) { return tab::TSIT5_CS(i); }
     __host__ __device__ static constexpr double bt(int j) { return tab::TSIT5_BT(j); }
@@ -30,6 +32,8 @@ struct Tsit5Tab {
 struct Vern7Tab {
     static constexpr int S = 16;
     __host__ __device__ static constexpr double a(int i, int j) { return tab::VERN7_A(i, j); }
+    __host__ __device__ static constexpr float ahi(int i, int j) { return tab::VERN7_A_HI(i, j); }
+    __host__ __device__ static constexpr float alo(int i, int j) { return tab::VERN7_A_LO(i, j); }
     __host__ __device__ static constexpr bool am(int i, int j) { return tab::VERN7_AM(i, j); }
     __host__ __device__ static constexpr double c(int i) { return tab::VERN7_CS(i); }
     __host__ __device__ static constexpr double b(int j) { return tab::VERN7_B(j); }
@@ -61,7 +65,9 @@ __host__ __device__ constexpr int row_terms(int row) {
 __host__ __device__ constexpr float f_hi(double x) { return (float)x; }
 __host__ __device__ constexpr float f_lo(double x) { return (float)(x - (double)(float)x); }
 
-// Compensated accumulator (hi, lo) for sum_j w_j k_j with w split into floats.
+// Compensated accumulator (hi, lo) for sum_j w_j k_j with w split into floats
+// (the tableau's split tables, hi = float(w), lo = float(w - hi), are
+// generated with the tables, so no split happens at run time).
 struct CSum {
     float hi = 0.0f, lo = 0.0f;
     __device__ __forceinline__ void add(double w, float k) {
@@ -150,13 +156,13 @@ template <class Tab, int C> struct RK<Tab, float, C> {
                 CSum s;
 #pragma unroll
                 for (int j = 1; j < ROW; ++j)
-                    if (Tab::am(ROW, j)) s.add(Tab::a(ROW, j), k[Tab::slot(j)][i]);
+                    if (Tab::am(ROW, j)) s.add_pair(Tab::ahi(ROW, j), Tab::alo(ROW, j), k[Tab::slot(j)][i]);
                 S = s.value();
             } else {
                 S = 0.0f;
 #pragma unroll
                 for (int j = 1; j < ROW; ++j)
-                    if (Tab::am(ROW, j)) S = fmaf((float)Tab::a(ROW, j), k[Tab::slot(j)][i], S);
+                    if (Tab::am(ROW, j)) S = fmaf(Tab::ahi(ROW, j), k[Tab::slot(j)][i], S);
             }
             out[i] = fmaf(d, S, up[i]) + uplo[i];
         }
@@ -169,7 +175,7 @@ template <class Tab, int C> struct RK<Tab, float, C> {
             CSum s;
 #pragma unroll
             for (int j = 1; j <= last; ++j)
-                if (W::m(j)) s.add(W::w(j), k[Tab::slot(j)][i]);
+                if (W::m(j)) s.add_pair(W::whi(j), W::wlo(j), k[Tab::slot(j)][i]);
             out[i] = s.value();
         }
     }

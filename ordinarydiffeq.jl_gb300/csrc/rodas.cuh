@@ -111,7 +111,6 @@ __device__ __forceinline__ void rhs_stage(R* du, const R* u, const R* ulo, const
 
 // J, W and the LU in one lane's registers.
 struct RegLA {
-    static constexpr bool FP64_RESIDUAL = true;   // refinement residual formed in FP64
     template <class R, int C> struct Store {
         R J[C][C];
         R W[C][C];
@@ -136,9 +135,9 @@ struct RegLA {
         lu_factor_reg<R, C>(s.W, s.piv);
     }
     // Solve W x = b in place (b -> x); in the mixed mode optionally refined with
-    // FP64 residuals b - (J - I/(dt*gamma)) x.
+    // FP64 residuals b - (J - idg I) x (idg = 1/(dt*gamma) as factored, in FP32).
     template <class Model, class R, int L, int C>
-    __device__ static void wsolve(Store<R, C>& s, R* b, double invdtgamma, R, int ir, const R*, const R*,
+    __device__ static void wsolve(Store<R, C>& s, R* b, double, R idg, int ir, const R*, const R*,
                                   const ff*, const Group<L>&) {
         if constexpr (sizeof(R) == 8) {
             lu_solve_reg<R, C>(s.W, s.piv, b);
@@ -148,6 +147,8 @@ struct RegLA {
             lu_solve_reg<R, C>(s.W, s.piv, b);
             return;
         }
+        // the residual of the matrix that was factored: J - idg*I with the FP32 idg
+        const double invdtgamma = (double)idg;
         double b64[C];
 #pragma unroll
         for (int i = 0; i < C; ++i) b64[i] = (double)b[i];
@@ -216,10 +217,14 @@ struct Rodas5PT {
         // dt-derived coefficients: FP64 like the reference; in the mixed mode they
         // scale FP32 stage terms, so they are formed in FP32 from dt (no FP64 work).
         const R dr = (R)dt;
-        const R invdt = sizeof(R) == 8 ? R(1.0 / dt) : R(1) / dr;
-        const double invdtgamma =
-            (sizeof(R) == 8 || (LA::FP64_RESIDUAL && c.ir > 0)) ? 1.0 / (dt * tab::RODAS5P_GAMMA) : 0.0;
-        const R idg = sizeof(R) == 8 ? (R)invdtgamma : R(1) / (dr * (R)tab::RODAS5P_GAMMA);
+        R invdt, idg;
+        if constexpr (sizeof(R) == 8) {
+            invdt = R(1.0 / dt);
+            idg = R(1.0 / (dt * tab::RODAS5P_GAMMA));
+        } else {
+            invdt = R(1) / dr;
+            idg = R(1) / (dr * (R)tab::RODAS5P_GAMMA);
+        }
         R* fsal = c.scratch;
         rhs_stage<Model, R, L, C, NP>(fsal, up, uplo, p, c.pff, t, g);
         st.nf += 1;
@@ -235,7 +240,7 @@ struct Rodas5PT {
         R r[C];
 #pragma unroll
         for (int i = 0; i < C; ++i) r[i] = fsal[i];
-        LA::template wsolve<Model, R, L, C>(c.la, r, invdtgamma, idg, c.ir, up, uplo, c.pff, g);
+        LA::template wsolve<Model, R, L, C>(c.la, r, dt, idg, c.ir, up, uplo, c.pff, g);
 #pragma unroll
         for (int i = 0; i < C; ++i) c.ks[0][i] = -r[i];
         st.nsolve += 1;
@@ -253,12 +258,12 @@ struct Rodas5PT {
                 } else {   // compensated sum, then the stage value as an exact pair up + sum + uplo
                     CSum cs;
 #pragma unroll
-                    for (int jj = 0; jj < s; ++jj) cs.add(tab::RODAS5P_A(s, jj), (float)c.ks[jj][i]);
+                    for (int jj = 0; jj < s; ++jj) cs.add_pair(tab::RODAS5P_A_HI(s, jj), tab::RODAS5P_A_LO(s, jj), (float)c.ks[jj][i]);
                     Acc<R>::update(u[i], stlo[i], R(1), (R)cs.value(), up[i], uplo[i]);
                 }
             }
             R du[C];
-            rhs_stage<Model, R, L, C, NP>(du, u, stlo, p, c.pff, fma(tab::RODAS5P_c(s), dt, t), g);
+            rhs_stage<Model, R, L, C, NP>(du, u, stlo, p, c.pff, stage_time<Model>(tab::RODAS5P_c(s), dt, t), g);
             st.nf += 1;
 #pragma unroll
             for (int i = 0; i < C; ++i) {
@@ -272,7 +277,7 @@ struct Rodas5PT {
                     cs.hi = (float)du[i];
 #pragma unroll
                     for (int jj = 0; jj < s; ++jj) {
-                        const float ch = f_hi(tab::RODAS5P_C(s, jj)), cl = f_lo(tab::RODAS5P_C(s, jj));
+                        const float ch = tab::RODAS5P_C_HI(s, jj), cl = tab::RODAS5P_C_LO(s, jj);
                         const float wh = ch * (float)invdt;
                         const float wl = fmaf(cl, (float)invdt, fmaf(ch, (float)invdt, -wh));
                         cs.add_pair(wh, wl, (float)c.ks[jj][i]);
@@ -280,7 +285,7 @@ struct Rodas5PT {
                     r[i] = (R)cs.value();
                 }
             }
-            LA::template wsolve<Model, R, L, C>(c.la, r, invdtgamma, idg, c.ir, up, uplo, c.pff, g);
+            LA::template wsolve<Model, R, L, C>(c.la, r, dt, idg, c.ir, up, uplo, c.pff, g);
 #pragma unroll
             for (int i = 0; i < C; ++i) c.ks[s][i] = -r[i];
             st.nsolve += 1;
@@ -295,8 +300,8 @@ struct Rodas5PT {
             } else {                // compensated increment, added to the compensated solution
                 CSum cs;
 #pragma unroll
-                for (int jj = 0; jj < 7; ++jj) cs.add(tab::RODAS5P_A(7, jj), (float)c.ks[jj][i]);
-                cs.add(1.0, (float)c.ks[7][i]);
+                for (int jj = 0; jj < 7; ++jj) cs.add_pair(tab::RODAS5P_A_HI(7, jj), tab::RODAS5P_A_LO(7, jj), (float)c.ks[jj][i]);
+                cs.add_pair(1.0f, 0.0f, (float)c.ks[7][i]);
                 Acc<R>::update(u[i], ulo[i], R(1), (R)cs.value(), up[i], uplo[i]);
             }
         }
@@ -320,7 +325,7 @@ struct Rodas5PT {
                 } else {
                     CSum cs;
 #pragma unroll
-                    for (int q = 0; q < 8; ++q) cs.add(tab::RODAS5P_H(jd, q), (float)c.ks[q][i]);
+                    for (int q = 0; q < 8; ++q) cs.add_pair(tab::RODAS5P_H_HI(jd, q), tab::RODAS5P_H_LO(jd, q), (float)c.ks[q][i]);
                     c.dk[jd][i] = (R)cs.value();
                 }
             }
