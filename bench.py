@@ -47,7 +47,7 @@ SERVE_HBM_BUDGET = 8 << 30
 def serving_block(args, local, rates, seconds):
     """Continuous-batching serving under open-loop Poisson arrivals (one Server,
     fixed HBM budget, precision chosen per request from its reltol)."""
-    from odegb300.serving import MIXED_MIN_RELTOL, Server, run_open_loop, serving_mix
+    from odegb300.serving import MIXED_MIN_RELTOL, MIXED_MIN_RELTOL_BY_MODEL, Server, run_open_loop, serving_mix
     reqs = serving_mix(2000, seed=3)
     out = []
     with Server(device=local, hbm_budget=SERVE_HBM_BUDGET, slots=args.serve_slots) as srv:
@@ -56,7 +56,8 @@ def serving_block(args, local, rates, seconds):
             out.append(run_open_loop(srv, reqs, rate=r, duration=seconds, drain_timeout=max(15.0, 3 * seconds)))
         st = srv.stats()
     return {"workload": CONFIGS["serving"][0], "hbm_budget_bytes": SERVE_HBM_BUDGET, "slots": args.serve_slots,
-            "precision": "mixed when reltol >= %g, else fp64" % MIXED_MIN_RELTOL,
+            "precision": "mixed when reltol >= %g (%s), else fp64" % (
+                MIXED_MIN_RELTOL, ", ".join("%s: %g" % kv for kv in MIXED_MIN_RELTOL_BY_MODEL.items())),
             "latency": "completion (outputs in the caller's host buffers) minus scheduled arrival",
             "rates": out, "rejected_total": st["rejected"]}
 

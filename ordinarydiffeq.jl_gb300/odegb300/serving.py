@@ -20,16 +20,22 @@ from . import _lib
 from .ensemble import MODELS, ALG_BY_NAME, EnsembleGB300, _options
 from .saveat import resolve_saveat
 
-# precision="auto": FP32 stages down to this reltol, FP64 below it (FP32 stage
-# arithmetic cannot carry tighter tolerances).
+# precision="auto": FP32 stages down to a model's reltol floor, FP64 below it
+# (FP32 stage arithmetic cannot carry tighter tolerances).  Measured on GB300
+# against ground-truth solves, the mixed form stays within 2x (+1 tol) of the
+# FP64 form's error at the median and p99 down to 1e-6 for Lorenz/Tsit5 and
+# Robertson/Rodas5P and down to 1e-7 for the Brusselator (Rodas5P with one
+# refinement sweep per solve); one decade further it does not.
 MIXED_MIN_RELTOL = 1e-6
+MIXED_MIN_RELTOL_BY_MODEL = {"brusselator_1d": 1e-7}
 
 _NAMES = ("nf", "njacs", "nw", "nsolve", "naccept", "nreject")
 
 
-def pick_precision(precision, reltol):
+def pick_precision(precision, reltol, model=None):
     if precision == "auto":
-        return "mixed" if reltol >= MIXED_MIN_RELTOL else "fp64"
+        floor = MIXED_MIN_RELTOL_BY_MODEL.get(model, MIXED_MIN_RELTOL)
+        return "mixed" if reltol >= floor * (1 - 1e-12) else "fp64"
     return precision
 
 
@@ -56,6 +62,7 @@ class Server:
     def submit(self, model, alg, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=1e-6, precision="fp64",
                ir_sweeps=-1, tag=None):
         """Queue one packed ensemble; returns its ticket at once."""
+        name = model if isinstance(model, str) else None
         if isinstance(model, str):
             model = MODELS[model]
         if isinstance(alg, str):
@@ -64,7 +71,7 @@ class Server:
         ps = np.ascontiguousarray(ps, dtype=np.float64)
         tspans = np.ascontiguousarray(tspans, dtype=np.float64)
         n, N = u0s.shape
-        prec = pick_precision(precision, reltol)
+        prec = pick_precision(precision, reltol, name)
         ens = EnsembleGB300(precision=prec, ir_sweeps=ir_sweeps if prec == "mixed" else -1)
         sv = saveat if hasattr(saveat, "nsave") else resolve_saveat(saveat, tspans)
         o = _options(reltol, abstol, None, None, None, 1000000, sv, ens, None, None)
