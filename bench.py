@@ -88,8 +88,8 @@ def run_serving(args, rank, local):
 # capture of the same kernels (profiles/rodas5p_robertson_100k.md,
 # profiles/vern7_duffing_uneven_20k.md; the Duffing figure is the 20,000-
 # trajectory capture scaled by 50 to the 1,000,000-trajectory launch).
-NCU_TRAFFIC = {("robertson", "fp64"): 17.11e6, ("robertson", "mixed"): 17.07e6,
-               ("duffing", "fp64"): 50 * 369.4e6, ("duffing", "mixed"): 50 * 368.7e6}
+NCU_TRAFFIC = {("robertson", "fp64"): 17.19e6, ("robertson", "mixed"): 17.56e6,
+               ("duffing", "fp64"): 50 * 326.7e6, ("duffing", "mixed"): 50 * 331.8e6}
 
 
 def parse():
