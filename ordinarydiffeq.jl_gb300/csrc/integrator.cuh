@@ -475,19 +475,20 @@ __device__ __forceinline__ void drain_class(const EnsembleArgs& a, int cls) {
     __syncwarp();
 }
 
-// Classes n = 64, 32, 16, 8, 4 with C = 4 states per lane (L = n/4).
+// Classes n = 64, 32, 16, 8, 4 with C states per lane (L = n/C).
 // The mixed one-launch kernel at 3 resident blocks (<= 168 registers, no
 // spills): 227 ms against 295 ms at 2 blocks for 1M uneven Duffing chains.
 #ifndef ODEGB_MIN_BLOCKS_FUSED_F32
 #define ODEGB_MIN_BLOCKS_FUSED_F32 3
 #endif
-template <class Alg, class Model, class R>
+template <class Alg, class Model, class R, int C>
 __global__ void __launch_bounds__(128, sizeof(R) == 4 ? ODEGB_MIN_BLOCKS_FUSED_F32 : 1) fused_class_kernel(EnsembleArgs a) {
-    drain_class<Alg, Model, R, 16, 4>(a, 4);
-    drain_class<Alg, Model, R, 8, 4>(a, 3);
-    drain_class<Alg, Model, R, 4, 4>(a, 2);
-    drain_class<Alg, Model, R, 2, 4>(a, 1);
-    drain_class<Alg, Model, R, 1, 4>(a, 0);
+    static_assert(C == 2 || C == 4, "class layouts hold 2 or 4 states per lane");
+    drain_class<Alg, Model, R, 64 / C, C>(a, 4);
+    drain_class<Alg, Model, R, 32 / C, C>(a, 3);
+    drain_class<Alg, Model, R, 16 / C, C>(a, 2);
+    drain_class<Alg, Model, R, 8 / C, C>(a, 1);
+    drain_class<Alg, Model, R, 4 / C, C>(a, 0);
 }
 
 }  // namespace odegb

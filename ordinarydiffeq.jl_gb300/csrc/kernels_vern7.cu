@@ -17,6 +17,10 @@ static const KernelVariant kVariants[] = {
     BOTH(Lorenz, M_LORENZ, 1, 3),
     BOTH(Duffing, M_DUFFING, 1, 4), BOTH(Duffing, M_DUFFING, 1, 8), BOTH(Duffing, M_DUFFING, 2, 4),
     BOTH(Duffing, M_DUFFING, 4, 4), BOTH(Duffing, M_DUFFING, 8, 4), BOTH(Duffing, M_DUFFING, 16, 4),
+    // mixed: 2 states per lane (the default layout, see default_lanes)
+    VAR(Duffing, M_DUFFING, float, 1, 2, 2), VAR(Duffing, M_DUFFING, float, 1, 4, 2),
+    VAR(Duffing, M_DUFFING, float, 1, 8, 2), VAR(Duffing, M_DUFFING, float, 1, 16, 2),
+    VAR(Duffing, M_DUFFING, float, 1, 32, 2),
 };
 
 const KernelVariant* vern7_variants(int* count) {

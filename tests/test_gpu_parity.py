@@ -282,3 +282,64 @@ def test_abort_stops_running_kernels():
     assert elapsed < 5.0, elapsed
     naccept = st.cpu().numpy()[:, 4]
     assert (naccept > 0).all() and (naccept < 10 ** 7).all()
+
+
+def _device_solve(model, alg, u0, p, ts, saveat, reltol, abstol, precision="fp64", npt=None):
+    """The same solve through ode_solve_ensemble_device on torch buffers."""
+    import ctypes as C
+    import torch
+    from gpu_common import ALG
+    from odegb300 import EnsembleGB300, _lib
+    from odegb300.ensemble import MODELS, _options, get_handle
+    from odegb300.saveat import resolve_saveat
+    L = _lib.load()
+    h = get_handle(0)
+    n, N = u0.shape
+    sv = resolve_saveat(saveat, ts)
+    ens = EnsembleGB300(precision=precision)
+    o = _options(reltol, abstol, None, None, None, 10 ** 6, sv, ens, None, None)
+    d = _lib.ProblemDesc(MODELS[model], ALG[alg][0].alg_id, n, p.shape[0], ens.prec_id(), 0)
+    dev = torch.device("cuda", 0)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    cap = sv.nsave + 2
+    bufs = [t(u0), t(p), t(ts), t(sv.values if sv.nsave else np.zeros(1)),
+            torch.empty((cap, N), dtype=torch.float64, device=dev),
+            torch.empty((cap, n, N), dtype=torch.float64, device=dev),
+            torch.empty(N, dtype=torch.int32, device=dev), torch.empty(N, dtype=torch.int32, device=dev),
+            torch.empty((N, 6), dtype=torch.int64, device=dev)]
+    dn = t(npt) if npt is not None else None
+    vp = lambda x: C.c_void_p(x.data_ptr()) if x is not None else None
+    stream = torch.cuda.Stream(dev)
+    _lib.check(L.ode_solve_ensemble_device(h, C.byref(d), C.byref(o), N, vp(dn), *[vp(b) for b in bufs],
+                                           C.c_void_p(stream.cuda_stream)), h)
+    stream.synchronize()
+    names = ("nf", "njacs", "nw", "nsolve", "naccept", "nreject")
+    st = bufs[8].cpu().numpy()
+    return {"t": bufs[4].cpu().numpy(), "u": bufs[5].cpu().numpy(), "nsaved": bufs[6].cpu().numpy(),
+            "retcode": bufs[7].cpu().numpy(), "stats": {k: st[:, i] for i, k in enumerate(names)}}
+
+
+def _same_saved(a, b):
+    ns = a["nsaved"]
+    assert np.array_equal(ns, b["nsaved"]) and np.array_equal(a["retcode"], b["retcode"])
+    m = np.arange(a["t"].shape[0])[:, None] < ns[None, :]
+    assert np.array_equal(a["t"][m], b["t"][m])
+    mu = np.broadcast_to(m[:, None, :], a["u"].shape)
+    assert np.array_equal(a["u"][mu], b["u"][mu])
+    assert np.array_equal(a["stats"]["naccept"], b["stats"]["naccept"])
+
+
+def test_pipelined_host_solve_equals_device_solve():
+    # host-buffer solves of 32768+ trajectories run as a 4-slice copy/compute
+    # pipeline; every trajectory must come out as in one device-buffer solve
+    N = 40000
+    u0, p, ts = lorenz_inputs(N, seed=21)
+    _same_saved(gpu("lorenz", "tsit5", u0, p, ts, 0.1, 1e-8, 1e-8),
+                _device_solve("lorenz", "tsit5", u0, p, ts, 0.1, 1e-8, 1e-8))
+
+
+def test_pipelined_uneven_host_solve_equals_device_solve():
+    N = 40000
+    u0, p, ts, sv, npt = duffing_inputs(N, [2, 4, 8, 16, 32], tf_range=(1.0, 3.0), seed=5)
+    _same_saved(gpu("duffing_chain", "vern7", u0, p, ts, sv, 1e-6, 1e-6, precision="mixed", n_per_traj=npt),
+                _device_solve("duffing_chain", "vern7", u0, p, ts, sv, 1e-6, 1e-6, precision="mixed", npt=npt))
