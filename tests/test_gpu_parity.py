@@ -329,9 +329,9 @@ def _same_saved(a, b):
     assert np.array_equal(a["stats"]["naccept"], b["stats"]["naccept"])
 
 
-def test_pipelined_host_solve_equals_device_solve():
-    # host-buffer solves of 32768+ trajectories run as a 4-slice copy/compute
-    # pipeline; every trajectory must come out as in one device-buffer solve
+def test_host_solve_equals_device_solve():
+    # the host-buffer entry point (copies + graph replay) and the device-buffer
+    # entry point give the same trajectories
     N = 40000
     u0, p, ts = lorenz_inputs(N, seed=21)
     _same_saved(gpu("lorenz", "tsit5", u0, p, ts, 0.1, 1e-8, 1e-8),
@@ -339,6 +339,9 @@ def test_pipelined_host_solve_equals_device_solve():
 
 
 def test_pipelined_uneven_host_solve_equals_device_solve():
+    # 32768+ trajectories with many output bytes each (64-state class slots,
+    # 18 saves) run as a 4-slice copy/compute pipeline; every trajectory must
+    # come out as in one device-buffer solve
     N = 40000
     u0, p, ts, sv, npt = duffing_inputs(N, [2, 4, 8, 16, 32], tf_range=(1.0, 3.0), seed=5)
     _same_saved(gpu("duffing_chain", "vern7", u0, p, ts, sv, 1e-6, 1e-6, precision="mixed", n_per_traj=npt),
