@@ -258,7 +258,7 @@ def run_gb300(args, world, rank, local, dist):
     dev = torch.device("cuda", local)
     n, _ = wl["u0"].shape
     sv = resolve_saveat(wl["saveat"], wl["tspan"])
-    cap = sv.nsave + 2
+    cap = sv.cap
     npt = wl.get("n_per_traj")
     t_u0 = torch.from_numpy(np.ascontiguousarray(wl["u0"])).to(dev)
     t_p = torch.from_numpy(np.ascontiguousarray(wl["p"])).to(dev)

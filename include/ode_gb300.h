@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define ODE_ABI_VERSION 1
+#define ODE_ABI_VERSION 2
 
 typedef struct ode_handle ode_handle;
 
@@ -105,7 +105,11 @@ typedef struct {
     int32_t lanes_per_traj;     /* 0: tuned choice; else 1,2,4,8,16,32 where compiled */
     int32_t scheduler;          /* 0 auto, 1 static (one lane group per trajectory), 2 persistent queue */
     int32_t block_size;         /* 0: tuned */
-    int32_t ir_sweeps;          /* MIXED Rodas5P refinement sweeps (< 0: default 1) */
+    int32_t ir_sweeps;          /* MIXED Rodas5P refinement sweeps (< 0: none) */
+    int32_t save_everystep;     /* 1: save every accepted step, the reference's default without saveat
+                                   (integrator_utils.jl:397-404); needs nsave == 0 */
+    int32_t max_step_saves;     /* save_everystep: step saves kept per trajectory; t_out/u_out hold
+                                   max_step_saves + 2 slots, and past that the last slot keeps the latest step */
 } ode_options;
 
 /* Fill o with the reference's defaults. */

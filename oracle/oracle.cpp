@@ -643,9 +643,10 @@ void interpolate(Integ& I, double th, double* out) {
 }
 
 void push_save(Integ& I, double t, const double* v) {
-    if (I.nsaved < I.cap) {
-        if (I.t_out) I.t_out[I.nsaved] = t;
-        if (I.u_out) std::memcpy(I.u_out + (size_t)I.nsaved * I.n, v, sizeof(double) * I.n);
+    const int slot = I.nsaved < I.cap ? I.nsaved : (I.o.save_everystep ? I.cap - 1 : -1);
+    if (slot >= 0) {
+        if (I.t_out) I.t_out[slot] = t;
+        if (I.u_out) std::memcpy(I.u_out + (size_t)slot * I.n, v, sizeof(double) * I.n);
     }
     I.nsaved++;
     I.last_saved_t = t;
@@ -664,6 +665,11 @@ void savevalues(Integ& I) {
             push_save(I, I.t, I.u.data());
         }
     }
+    // save_everystep: the accepted step unless it repeats the last save (t === sol.t[end]
+    // with dt != 0) or is tf with save_end off (integrator_utils.jl:397-404)
+    if (I.o.save_everystep &&
+        (I.nsaved == 0 || ((I.t != I.last_saved_t || I.dt == 0.0) && (I.o.save_end || I.t != I.tf))))
+        push_save(I, I.t, I.u.data());
     if (I.alg == ORC_VERN7 && I.nk_valid > 10) I.nk_valid = 10;  // post_savevalues! resize
 }
 
@@ -1024,7 +1030,7 @@ int orc_solve_ensemble(int alg, int model, int nmax, const int32_t* n_per_traj, 
                        int32_t* nsaved, int32_t* retcode, orc_stats* stats, int nthreads) {
     if (nthreads <= 0) nthreads = (int)std::thread::hardware_concurrency();
     if (nthreads <= 0) nthreads = 1;
-    int cap = nsave + 2;  // saveat points plus possible start and end saves
+    int cap = (o->save_everystep ? o->max_step_saves : nsave) + 2;  // saves plus possible start and end saves
     std::atomic<int64_t> next(0);
     auto worker = [&]() {
         std::vector<double> uj(nmax), pj(np), sv(nsave > 0 ? nsave : 1), tl(cap), ul((size_t)cap * nmax);

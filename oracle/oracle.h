@@ -44,6 +44,9 @@ typedef struct {
     double qmax_first_step; /* <= 0: 10000 */
     double qmax;            /* <= 0: 10 */
     int32_t saveat_as_tstops; /* ensemble only: stop exactly at every save (ground-truth solves) */
+    int32_t save_everystep;   /* save every accepted step (integrator_utils.jl:397-404) */
+    int32_t max_step_saves;   /* ensemble: slots are max_step_saves + 2; past them the last slot
+                                 keeps the latest step (the library's behaviour) */
 } orc_opts;
 
 /* Solve one trajectory.  saveat: nsave_in times in (t0, tf] sorted ascending.

@@ -32,6 +32,7 @@ class Opts(C.Structure):
         ("maxiters", C.c_int64), ("save_start", C.c_int32), ("save_end", C.c_int32),
         ("save_end_user", C.c_int32), ("saveat_given", C.c_int32), ("saveat_scalar", C.c_int32),
         ("qmax_first_step", C.c_double), ("qmax", C.c_double), ("saveat_as_tstops", C.c_int32),
+        ("save_everystep", C.c_int32), ("max_step_saves", C.c_int32),
     ]
 
 
@@ -75,10 +76,11 @@ def _dp(a):
 
 def make_opts(reltol=1e-3, abstol=1e-6, dtmax=0.0, dtmin=0.0, dt=0.0, adaptive=True,
               maxiters=1000000, save_start=False, save_end=True, save_end_user=-1,
-              saveat_given=True, saveat_scalar=False, qmax_first_step=0.0, qmax=0.0, saveat_as_tstops=False):
+              saveat_given=True, saveat_scalar=False, qmax_first_step=0.0, qmax=0.0, saveat_as_tstops=False,
+              save_everystep=False, max_step_saves=0):
     return Opts(reltol, abstol, dtmax, dtmin, dt, int(adaptive), maxiters, int(save_start),
                 int(save_end), save_end_user, int(saveat_given), int(saveat_scalar),
-                qmax_first_step, qmax, int(saveat_as_tstops))
+                qmax_first_step, qmax, int(saveat_as_tstops), int(save_everystep), int(max_step_saves))
 
 
 def solve(alg, model, u0, p, tspan, saveat=(), tstops=(), dense=False, **kw):
@@ -92,6 +94,8 @@ def solve(alg, model, u0, p, tspan, saveat=(), tstops=(), dense=False, **kw):
     cap = sv.size + 2
     if kw.get("saveat_given", True) is False or sv.size == 0:
         cap = 4
+    if kw.get("save_everystep"):
+        cap = kw.get("max_step_saves", 0) + 2
     t_out = np.zeros(cap)
     u_out = np.zeros((cap, n))
     rc = C.c_int32(0)
@@ -141,7 +145,7 @@ def solve_ensemble(alg, model, u0, p, tspan, saveat, reltol, abstol, n_per_traj=
     sv = np.ascontiguousarray(saveat, dtype=np.float64)
     nmax, N = u0.shape
     nsave = sv.shape[0]
-    cap = nsave + 2
+    cap = (kw.get("max_step_saves", 0) if kw.get("save_everystep") else nsave) + 2
     t_out = np.full((cap, N), np.nan)
     u_out = np.full((cap, nmax, N), np.nan)
     nsaved = np.zeros(N, dtype=np.int32)

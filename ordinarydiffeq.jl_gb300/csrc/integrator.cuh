@@ -260,11 +260,13 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
     double last_saved_t = dnan();
 
     auto save_point = [&](double ts, const R* v, const R* vlo) {
-        if (nsaved < a.nsave_cap) {
-            if (g.lane == 0 && a.t_out) a.t_out[(size_t)nsaved * N + j] = ts;
+        // past the capacity, step saves keep the latest point in the last slot
+        const int slot = nsaved < a.nsave_cap ? nsaved : (a.save_everystep ? a.nsave_cap - 1 : -1);
+        if (slot >= 0) {
+            if (g.lane == 0 && a.t_out) a.t_out[(size_t)slot * N + j] = ts;
 #pragma unroll
             for (int c = 0; c < C; ++c)
-                a.u_out[((size_t)nsaved * a.nmax + g.lane * C + c) * N + j] = Acc<R>::join(v[c], vlo[c]);
+                a.u_out[((size_t)slot * a.nmax + g.lane * C + c) * N + j] = Acc<R>::join(v[c], vlo[c]);
         }
         nsaved++;
         last_saved_t = ts;
@@ -394,6 +396,11 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
                     save_point(t, u, ulo);
                 }
             }
+            // save_everystep (_savevalues!, integrator_utils.jl:397-404): the accepted
+            // step, unless it repeats the last save or is tf with save_end off
+            if (a.save_everystep &&
+                (nsaved == 0 || ((!deq(t, last_saved_t) || abs_bits(dt) == 0) && (a.save_end || !deq(t, tf)))))
+                save_point(t, u, ulo);
             Alg::template after_save<R, C>(cache);
         } else {
             st.nreject++;

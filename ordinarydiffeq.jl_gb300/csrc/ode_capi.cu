@@ -181,8 +181,16 @@ int validate(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int
         return fail(h, ODE_E_INVALID, "this model has 3 states");
     if (!(o->reltol > 0) || !(o->abstol >= 0)) return fail(h, ODE_E_INVALID, "tolerances must be positive");
     if (o->nsave < 0) return fail(h, ODE_E_INVALID, "negative nsave");
+    if (o->save_everystep && o->nsave > 0)
+        return fail(h, ODE_E_UNSUPPORTED, "save_everystep together with saveat is not supported");
+    if (o->save_everystep && o->max_step_saves <= 0)
+        return fail(h, ODE_E_INVALID, "save_everystep needs max_step_saves > 0");
     return ODE_OK;
 }
+
+// Output slots per trajectory: the saveat points (or the kept step saves)
+// plus the start and end saves.
+size_t save_cap(const ode_options* o) { return (size_t)(o->save_everystep ? o->max_step_saves : o->nsave) + 2; }
 
 EnsembleArgs make_args(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int64_t N,
                        const double* u0, const double* p, const double* tspan, const double* saveat,
@@ -199,7 +207,8 @@ EnsembleArgs make_args(ode_handle* h, const ode_problem_desc* d, const ode_optio
     a.saveat = saveat;
     a.nsave = o->nsave;
     a.saveat_per_traj = o->saveat_per_traj;
-    a.nsave_cap = o->nsave + 2;
+    a.nsave_cap = (int)save_cap(o);
+    a.save_everystep = o->save_everystep;
     a.t_out = t_out;
     a.u_out = u_out;
     a.nsaved = nsaved;
@@ -579,7 +588,6 @@ int run_ensemble(ode_handle* h, Ctx& c, const ode_problem_desc* d, const ode_opt
     return ODE_OK;
 }
 
-size_t save_cap(const ode_options* o) { return (size_t)o->nsave + 2; }
 
 // Large host-buffer solves run as a pipeline of kPipeChunks trajectory slices:
 // slice k+1's inputs go in on one copy stream while slice k integrates and
@@ -723,7 +731,7 @@ struct Layout {
     size_t u0, p, ts, sv, npt, in_end, t, u, ns, rc, st, total;
 };
 Layout layout(const Request& r) {
-    const size_t n = (size_t)r.d.n_states, np = (size_t)r.d.n_params, N = (size_t)r.N, cap = (size_t)r.o.nsave + 2;
+    const size_t n = (size_t)r.d.n_states, np = (size_t)r.d.n_params, N = (size_t)r.N, cap = save_cap(&r.o);
     Layout L;
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off += align256(bytes); return o; };
@@ -782,7 +790,7 @@ int admit(ode_handle* h, Request& r, int k) {
 
 // Outputs from the slot's staging into the caller's buffers.
 void finish(ode_handle* h, Request& r) {
-    const size_t n = (size_t)r.d.n_states, N = (size_t)r.N, cap = (size_t)r.o.nsave + 2;
+    const size_t n = (size_t)r.d.n_states, N = (size_t)r.N, cap = save_cap(&r.o);
     if (r.status == ODE_OK && r.slot >= 0 && h->slot_pinned[r.slot]) {
         const Layout L = layout(r);
         const char* hs = (const char*)h->slot_pinned[r.slot];
@@ -1361,7 +1369,8 @@ extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_o
     if (d->alg_id < ODE_TSIT5 || d->alg_id > ODE_RODAS5P ||
         (d->precision != ODE_PREC_FP64 && d->precision != ODE_PREC_MIXED) ||
         d->model_id < ODE_MODEL_LINEAR || d->model_id > ODE_MODEL_BRUSSELATOR_1D || d->n_states <= 0 ||
-        d->n_params != model_nparams(d->model_id) || !(o->reltol > 0) || !(o->abstol >= 0) || o->nsave < 0)
+        d->n_params != model_nparams(d->model_id) || !(o->reltol > 0) || !(o->abstol >= 0) || o->nsave < 0 ||
+        (o->save_everystep && (o->nsave > 0 || o->max_step_saves <= 0)))
         return fail(nullptr, ODE_E_INVALID, "invalid problem description or options");
     if (npt_dev && d->model_id != ODE_MODEL_DUFFING_CHAIN)
         return fail(nullptr, ODE_E_UNSUPPORTED, "per-trajectory sizes are supported for DUFFING_CHAIN");
@@ -1389,7 +1398,8 @@ extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_o
     a.saveat = saveat;
     a.nsave = o->nsave;
     a.saveat_per_traj = o->saveat_per_traj;
-    a.nsave_cap = o->nsave + 2;
+    a.nsave_cap = (int)save_cap(o);
+    a.save_everystep = o->save_everystep;
     a.t_out = t_out;
     a.u_out = u_out;
     a.nsaved = nsaved;

@@ -35,6 +35,7 @@ struct EnsembleArgs {
     double reltol, abstol, dtmax, dtmin, dt;
     long long maxiters;
     int save_start, save_end, save_end_user, saveat_given, saveat_scalar;
+    int save_everystep;     // save every accepted step (saveat empty); nsave_cap bounds the slots
     double qmax_first_step, qmax;
     int ir_sweeps;          // mixed Rosenbrock: refinement sweeps per solve
     // scheduling

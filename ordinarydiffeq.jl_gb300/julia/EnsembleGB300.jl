@@ -51,7 +51,7 @@ mutable struct Options
     reltol::Float64; abstol::Float64; dtmax::Float64; dtmin::Float64; dt::Float64; maxiters::Int64
     save_start::Int32; save_end::Int32; save_end_user::Int32; saveat_scalar::Int32; nsave::Int32
     saveat_per_traj::Int32; qmax_first_step::Float64; qmax::Float64; lanes_per_traj::Int32
-    scheduler::Int32; block_size::Int32; ir_sweeps::Int32
+    scheduler::Int32; block_size::Int32; ir_sweeps::Int32; save_everystep::Int32; max_step_saves::Int32
 end
 struct Stats
     nf::Int64; njacs::Int64; nw::Int64; nsolve::Int64; naccept::Int64; nreject::Int64
@@ -78,7 +78,8 @@ end
 function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem, alg::Union{Tsit5, Vern7, Rodas5P},
                            ens::EnsembleGB300; trajectories, saveat = Float64[], reltol = 1e-3, abstol = 1e-6,
                            dt = 0.0, dtmax = 0.0, dtmin = 0.0, maxiters = 1_000_000, save_start = nothing,
-                           save_end = nothing, seed = 0, kwargs...)
+                           save_end = nothing, save_everystep = isempty(saveat), max_step_saves = 1024, seed = 0,
+                           kwargs...)
     t0 = time()
     N = trajectories
     probs = [eprob.prob_func(eprob.prob, SciMLBase.EnsembleContext(i, 1, seed)) for i in 1:N]
@@ -100,10 +101,12 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem, alg::Union{
     sv = scalar ? collect(probs[1].tspan[1] + saveat:saveat:probs[1].tspan[2]) : sort(collect(Float64, saveat))
     ss = save_start === nothing ? (isempty(saveat) || scalar || probs[1].tspan[1] in sv) : save_start
     se = save_end === nothing ? (isempty(saveat) || scalar || probs[1].tspan[2] in sv) : save_end
+    everystep = save_everystep && isempty(sv)
     o = Options(reltol, abstol, dtmax, dtmin, dt, maxiters, ss, se, save_end === nothing ? -1 : Int32(save_end),
-                scalar, length(sv), 0, 0.0, 0.0, ens.lanes_per_traj, ens.scheduler, 0, -1)
+                scalar, length(sv), 0, 0.0, 0.0, ens.lanes_per_traj, ens.scheduler, 0, -1, everystep,
+                everystep ? max_step_saves : 0)
     d = ProblemDesc(model, alg_id(alg), n, npar, ens.precision === :mixed ? 1 : 0, 0)
-    cap = length(sv) + 2
+    cap = (everystep ? max_step_saves : length(sv)) + 2
     t_out = fill(NaN, N, cap); u_out = fill(NaN, N, n, cap)   # [(s*n + i)*N + j] -> u_out[j, i, s]
     nsaved = zeros(Int32, N); rc = zeros(Int32, N); st = Vector{Stats}(undef, N)
     status = ccall((:ode_solve_ensemble, LIB), Cint,

@@ -27,7 +27,8 @@ class Options(C.Structure):
                 ("save_start", C.c_int32), ("save_end", C.c_int32), ("save_end_user", C.c_int32),
                 ("saveat_scalar", C.c_int32), ("nsave", C.c_int32), ("saveat_per_traj", C.c_int32),
                 ("qmax_first_step", C.c_double), ("qmax", C.c_double), ("lanes_per_traj", C.c_int32),
-                ("scheduler", C.c_int32), ("block_size", C.c_int32), ("ir_sweeps", C.c_int32)]
+                ("scheduler", C.c_int32), ("block_size", C.c_int32), ("ir_sweeps", C.c_int32),
+                ("save_everystep", C.c_int32), ("max_step_saves", C.c_int32)]
 
 
 class Stats(C.Structure):

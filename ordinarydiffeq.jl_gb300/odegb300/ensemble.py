@@ -11,6 +11,7 @@ arrays instead of prob_func) skips the per-trajectory Python work.
 """
 import ctypes as C
 import time
+import warnings
 from dataclasses import dataclass, field
 from enum import IntEnum
 
@@ -225,14 +226,19 @@ def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_ste
     o.scheduler = ens.sched_id()
     o.block_size = ens.block_size
     o.ir_sweeps = ens.ir_sweeps
+    o.save_everystep = int(sv.everystep)
+    o.max_step_saves = int(sv.max_step_saves)
     return o
 
 
 def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=1e-6, dt=None,
                  dtmax=None, dtmin=None, maxiters=1000000, save_start=None, save_end=None, n_per_traj=None,
-                 qmax_first_step=None, qmax=None, return_times=False):
+                 qmax_first_step=None, qmax=None, return_times=False, save_everystep=False, max_step_saves=1024):
     """Solve a packed ensemble.  u0s (n, N), ps (np, N), tspans (2, N).  Returns the
-    raw structure-of-arrays outputs dict (t, u, nsaved, retcode, stats)."""
+    raw structure-of-arrays outputs dict (t, u, nsaved, retcode, stats).
+    save_everystep (without saveat) keeps every accepted step, up to
+    max_step_saves per trajectory (past that the last slot holds the final
+    point and a warning is issued)."""
     L = _lib.load()
     if isinstance(model, str):
         model = MODELS[model]
@@ -240,10 +246,10 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
     ps = np.ascontiguousarray(ps, dtype=np.float64)
     tspans = np.ascontiguousarray(tspans, dtype=np.float64)
     n, N = u0s.shape
-    sv = resolve_saveat(saveat, tspans, save_start, save_end)
+    sv = resolve_saveat(saveat, tspans, save_start, save_end, save_everystep, max_step_saves)
     o = _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax)
     d = _lib.ProblemDesc(model, alg.alg_id, n, ps.shape[0], ens.prec_id(), 0)
-    cap = sv.nsave + 2
+    cap = sv.cap
     t_out = np.full((cap, N), np.nan)
     u_out = np.full((cap, n, N), np.nan)
     nsaved = np.zeros(N, dtype=np.int32)
@@ -263,6 +269,11 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
     elapsed = time.perf_counter() - t0
     _lib.check(status, h)
     names = ("nf", "njacs", "nw", "nsolve", "naccept", "nreject")
+    if sv.everystep:
+        lost = int(np.sum(stats[:, 4] + int(sv.save_start) > cap))
+        if lost:
+            warnings.warn("%d trajectories took more than max_step_saves=%d steps; their middle steps were "
+                          "dropped (the final point is kept)" % (lost, sv.max_step_saves))
     out = {"t": t_out, "u": u_out, "nsaved": nsaved, "retcode": rc,
            "stats": {k: stats[:, i] for i, k in enumerate(names)}, "elapsed": elapsed}
     return out
@@ -295,8 +306,12 @@ def autotune(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=
 
 def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, saveat=None, reltol=1e-3,
           abstol=1e-6, dt=None, dtmax=None, dtmin=None, maxiters=1000000, save_start=None, save_end=None,
-          seed=0, qmax_first_step=None, qmax=None):
-    """solve(EnsembleProblem, alg, EnsembleGB300(); trajectories, saveat, reltol, abstol, ...)."""
+          seed=0, qmax_first_step=None, qmax=None, save_everystep=None, max_step_saves=1024):
+    """solve(EnsembleProblem, alg, EnsembleGB300(); trajectories, saveat, reltol, abstol, ...).
+    As in the reference, save_everystep defaults to "no saveat given" (every
+    accepted step is kept, up to max_step_saves per trajectory)."""
+    if save_everystep is None:
+        save_everystep = saveat is None or (not np.isscalar(saveat) and np.size(saveat) == 0)
     ens = ensemblealg or EnsembleGB300()
     if not isinstance(ens, EnsembleGB300):
         raise TypeError("ensemble algorithm must be EnsembleGB300")
@@ -310,7 +325,8 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
         ps = eprob.ps if eprob.ps is not None else np.repeat(prob.p[:, None], N, axis=1)
         tspans = eprob.tspans if eprob.tspans is not None else np.repeat(np.array(prob.tspan)[:, None], N, axis=1)
         res = solve_arrays(prob.model, alg, ens, u0s, ps, tspans, saveat, reltol, abstol, dt, dtmax, dtmin,
-                           maxiters, save_start, save_end, eprob.n_per_traj, qmax_first_step, qmax)
+                           maxiters, save_start, save_end, eprob.n_per_traj, qmax_first_step, qmax,
+                           save_everystep=save_everystep, max_step_saves=max_step_saves)
         sols = _LazySolutions(res, alg, eprob.n_per_traj)
         return EnsembleSolution(sols, time.perf_counter() - t_start, True, res)
     if trajectories is None:
@@ -325,7 +341,7 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
     while done < trajectories:
         ids = list(range(done, min(trajectories, done + batch_size)))
         outs = _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, dtmin, maxiters,
-                            save_start, save_end, output_func, qmax_first_step, qmax)
+                            save_start, save_end, output_func, qmax_first_step, qmax, save_everystep, max_step_saves)
         u, converged = reduction(u, outs, range(ids[0] + 1, ids[-1] + 2))
         done = ids[-1] + 1
         if converged:
@@ -334,7 +350,7 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
 
 
 def _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, dtmin, maxiters, save_start,
-                 save_end, output_func, qmax_first_step, qmax):
+                 save_end, output_func, qmax_first_step, qmax, save_everystep=False, max_step_saves=1024):
     repeat = {i: 1 for i in ids}
     results = {}
     todo = list(ids)
@@ -359,7 +375,8 @@ def _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, 
         ps = np.stack([pp.p for pp in probs], axis=1)
         tspans = np.array([pp.tspan for pp in probs]).T
         res = solve_arrays(probs[0].model, alg, ens, u0s, ps, tspans, saveat, reltol, abstol, dt, dtmax, dtmin,
-                           maxiters, save_start, save_end, npt, qmax_first_step, qmax)
+                           maxiters, save_start, save_end, npt, qmax_first_step, qmax,
+                           save_everystep=save_everystep, max_step_saves=max_step_saves)
         sols = _LazySolutions(res, alg, npt)
         again = []
         for k, i in enumerate(todo):

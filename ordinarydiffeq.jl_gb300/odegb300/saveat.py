@@ -79,13 +79,30 @@ class SaveSpec:
     save_start: bool
     save_end: bool
     save_end_user: int
+    everystep: bool = False      # save every accepted step (no saveat)
+    max_step_saves: int = 0      # step saves kept per trajectory when everystep
+
+    @property
+    def cap(self):
+        """Output slots per trajectory: t_out is (cap, N), u_out (cap, n, N)."""
+        return (self.max_step_saves if self.everystep else self.nsave) + 2
 
 
-def resolve_saveat(saveat, tspans, save_start=None, save_end=None):
+def resolve_saveat(saveat, tspans, save_start=None, save_end=None, save_everystep=False, max_step_saves=1024):
     """tspans: (2, N).  Returns the SaveSpec passed to the C ABI (a SaveSpec is
-    returned unchanged)."""
+    returned unchanged).  save_everystep (only without saveat) keeps every
+    accepted step, up to max_step_saves per trajectory."""
     if isinstance(saveat, SaveSpec):
         return saveat
+    no_saveat = saveat is None or (not np.isscalar(saveat) and np.size(saveat) == 0)
+    if save_everystep and not no_saveat:
+        raise ValueError("save_everystep together with saveat is not supported")
+    if save_everystep:
+        if max_step_saves <= 0:
+            raise ValueError("save_everystep needs max_step_saves > 0")
+        return SaveSpec(np.zeros(0), 0, False, False, True if save_start is None else bool(save_start),
+                        True if save_end is None else bool(save_end), -1 if save_end is None else int(bool(save_end)),
+                        True, int(max_step_saves))
     tspans = np.asarray(tspans, dtype=np.float64)
     t0s, tfs = tspans[0], tspans[1]
     same_span = bool(np.all(t0s == t0s[0]) and np.all(tfs == tfs[0])) if tspans.shape[1] else True

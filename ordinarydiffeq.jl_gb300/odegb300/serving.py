@@ -76,7 +76,7 @@ class Server:
         sv = saveat if hasattr(saveat, "nsave") else resolve_saveat(saveat, tspans)
         o = _options(reltol, abstol, None, None, None, 1000000, sv, ens, None, None)
         d = _lib.ProblemDesc(model, alg.alg_id, n, ps.shape[0], ens.prec_id(), 0)
-        cap = sv.nsave + 2
+        cap = sv.cap
         out = {"t": np.empty((cap, N)), "u": np.empty((cap, n, N)), "nsaved": np.empty(N, dtype=np.int32),
                "retcode": np.empty(N, dtype=np.int32), "stats": np.empty((N, 6), dtype=np.int64)}
         dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))

@@ -65,11 +65,13 @@ def gpu(model, alg, u0, p, tspan, saveat, reltol, abstol, precision="fp64", **kw
 
 
 def oracle(model, alg, u0, p, tspan, saveat, reltol, abstol, n_per_traj=None, **kw):
-    sv = resolve_saveat(saveat, tspan, kw.pop("save_start", None), kw.pop("save_end", None))
+    sv = resolve_saveat(saveat, tspan, kw.pop("save_start", None), kw.pop("save_end", None),
+                        kw.pop("save_everystep", False), kw.pop("max_step_saves", 1024))
     return O.solve_ensemble(ALG[alg][1], MODEL[model], u0, p, tspan, sv.values, reltol, abstol,
                             n_per_traj=n_per_traj, saveat_per_traj=sv.per_traj, save_start=sv.save_start,
                             save_end=sv.save_end, save_end_user=sv.save_end_user, saveat_given=sv.nsave > 0,
-                            saveat_scalar=sv.scalar, **kw)
+                            saveat_scalar=sv.scalar, save_everystep=sv.everystep,
+                            max_step_saves=sv.max_step_saves, **kw)
 
 
 def truth(model, u0, p, tspan, saveat, n_per_traj=None, stiff=False):

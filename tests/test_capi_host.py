@@ -37,7 +37,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_abi_version_and_defaults_without_gpu():
     L = _lib.load()
-    assert L.ode_abi_version() == 1
+    assert L.ode_abi_version() == 2
     o = _lib.Options()
     L.ode_options_default(C.byref(o))
     assert o.reltol == 1e-3 and o.abstol == 1e-6 and o.maxiters == 1000000

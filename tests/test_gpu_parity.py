@@ -261,7 +261,7 @@ def test_abort_stops_running_kernels():
     dev = torch.device("cuda", 0)
     t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
     du0, dp, dts = t(u0), t(p), t(ts)
-    cap = sv.nsave + 2
+    cap = sv.cap
     tout = torch.empty((cap, N), dtype=torch.float64, device=dev)
     uout = torch.empty((cap, 3, N), dtype=torch.float64, device=dev)
     ns = torch.empty(N, dtype=torch.int32, device=dev)
@@ -301,7 +301,7 @@ def _device_solve(model, alg, u0, p, ts, saveat, reltol, abstol, precision="fp64
     d = _lib.ProblemDesc(MODELS[model], ALG[alg][0].alg_id, n, p.shape[0], ens.prec_id(), 0)
     dev = torch.device("cuda", 0)
     t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
-    cap = sv.nsave + 2
+    cap = sv.cap
     bufs = [t(u0), t(p), t(ts), t(sv.values if sv.nsave else np.zeros(1)),
             torch.empty((cap, N), dtype=torch.float64, device=dev),
             torch.empty((cap, n, N), dtype=torch.float64, device=dev),
@@ -346,3 +346,29 @@ def test_pipelined_uneven_host_solve_equals_device_solve():
     u0, p, ts, sv, npt = duffing_inputs(N, [2, 4, 8, 16, 32], tf_range=(1.0, 3.0), seed=5)
     _same_saved(gpu("duffing_chain", "vern7", u0, p, ts, sv, 1e-6, 1e-6, precision="mixed", n_per_traj=npt),
                 _device_solve("duffing_chain", "vern7", u0, p, ts, sv, 1e-6, 1e-6, precision="mixed", npt=npt))
+
+
+@pytest.mark.parametrize("model,alg,rt,at", [("lorenz", "tsit5", 1e-8, 1e-8), ("lorenz", "vern7", 1e-8, 1e-8),
+                                             ("robertson", "rodas5p", 1e-6, 1e-10)])
+def test_save_everystep_matches_oracle(model, alg, rt, at):
+    # no saveat: every accepted step is saved (the reference's default)
+    N = 128
+    u0, p, ts = lorenz_inputs(N, seed=4) if model == "lorenz" else robertson_inputs(N, seed=4)
+    g = gpu(model, alg, u0, p, ts, None, rt, at, save_everystep=True, max_step_saves=4096)
+    o = oracle(model, alg, u0, p, ts, None, rt, at, save_everystep=True, max_step_saves=4096)
+    c = compare(g, o, rt, at)
+    assert c["ok"] and c["steps_ok"], c
+    # start + every accepted step (tf included)
+    assert np.array_equal(g["nsaved"], g["stats"]["naccept"] + 1)
+    last = g["t"][g["nsaved"] - 1, np.arange(N)]
+    assert np.array_equal(last, ts[1])
+
+
+def test_save_everystep_overflow_keeps_the_final_point():
+    N = 64
+    u0, p, ts = lorenz_inputs(N, seed=8)
+    g = gpu("lorenz", "tsit5", u0, p, ts, None, 1e-8, 1e-8, save_everystep=True, max_step_saves=5)
+    assert (g["nsaved"] == 7).all()
+    assert np.array_equal(g["t"][6], ts[1])   # the last slot holds tf
+    o = oracle("lorenz", "tsit5", u0, p, ts, None, 1e-8, 1e-8, save_everystep=True, max_step_saves=5)
+    assert np.allclose(g["u"][6], o["u"][6], rtol=1e-6, atol=1e-6)

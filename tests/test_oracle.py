@@ -209,3 +209,19 @@ def test_ensemble_matches_single_solves():
         assert ns == len(one["t"]) == 11
         assert np.array_equal(ens["u"][:ns, :, j], one["u"])
         assert ens["stats"]["naccept"][j] == one["stats"]["naccept"]
+
+
+def test_save_everystep_saves_start_and_every_accepted_step():
+    # integrator_utils.jl:397-404: with no saveat every accepted step is saved
+    # after the start point; tf is saved once (save_end), or dropped without it
+    r = O.solve_ensemble(O.TSIT5, O.LINEAR, np.array([[0.5]]), np.array([[1.01]]), np.array([[0.0], [1.0]]),
+                         np.zeros(0), 1e-6, 1e-6, save_start=True, save_end=True, saveat_given=False,
+                         save_everystep=True, max_step_saves=256)
+    k = int(r["nsaved"][0])
+    t = r["t"][:k, 0]
+    assert k == r["stats"]["naccept"][0] + 1
+    assert t[0] == 0.0 and t[-1] == 1.0 and np.all(np.diff(t) > 0)
+    r2 = O.solve_ensemble(O.TSIT5, O.LINEAR, np.array([[0.5]]), np.array([[1.01]]), np.array([[0.0], [1.0]]),
+                          np.zeros(0), 1e-6, 1e-6, save_start=True, save_end=False, saveat_given=False,
+                          save_everystep=True, max_step_saves=256)
+    assert int(r2["nsaved"][0]) == k - 1 and r2["t"][k - 2, 0] < 1.0

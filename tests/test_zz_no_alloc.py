@@ -30,7 +30,7 @@ def _device_solve(entry, model, alg_id, prec, u0, p, ts, saveat, reltol, abstol,
     dev = torch.device("cuda", 0)
     n, N = u0.shape
     sv = resolve_saveat(saveat, ts)
-    cap = sv.nsave + 2
+    cap = sv.cap
     ens = EnsembleGB300(precision=prec)
     o = _options(reltol, abstol, None, None, None, 1000000, sv, ens, None, None)
     d = _lib.ProblemDesc(model, alg_id, n, p.shape[0], ens.prec_id(), 0)
