@@ -145,32 +145,6 @@ struct Brusselator {
             du[2 * q + 1] = (p[1] * uu - u2v) + ae * lv;
         }
     }
-    // Row block of the Jacobian owned by one lane-row index i (0..n-1), written
-    // into a dense row `row[n]`; used by the shared-memory W build.
-    template <class R>
-    __device__ static void jac_row(R* row, int n, int i, const R* uvec, const R* p) {
-        int NC = n / 2;
-        R ae = p[2] * (R(NC) * R(NC));
-        for (int j = 0; j < n; ++j) row[j] = R(0);
-        int cell = i / 2, il = cell == 0 ? NC - 1 : cell - 1, ir = cell == NC - 1 ? 0 : cell + 1;
-        R uu = uvec[2 * cell], vv = uvec[2 * cell + 1];
-        if ((i & 1) == 0) {
-            row[2 * cell] = (R(2) * uu * vv - (p[1] + R(1))) - R(2) * ae;
-            row[2 * cell + 1] = uu * uu;
-            row[2 * il] += ae;
-            row[2 * ir] += ae;
-        } else {
-            row[2 * cell] = p[1] - R(2) * uu * vv;
-            row[2 * cell + 1] = -(uu * uu) - R(2) * ae;
-            row[2 * il + 1] += ae;
-            row[2 * ir + 1] += ae;
-        }
-    }
-    template <class R, int N>
-    __device__ static void jac(R (*J)[N], const R* u, const R* p, double) {
-#pragma unroll 1
-        for (int i = 0; i < N; ++i) jac_row<R>(J[i], N, i, u, p);
-    }
     // Nonzeros of the lane's own rows (cells lane*C/2 ...) of J(u), in the
     // oracle's arithmetic; put(i, col, v) with i the lane-local row.  The
     // neighbour columns are distinct from the cell's own for 3 cells or more.

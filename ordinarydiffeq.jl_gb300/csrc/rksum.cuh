@@ -62,26 +62,9 @@ __host__ __device__ constexpr int row_terms(int row) {
     return n;
 }
 
-__host__ __device__ constexpr float f_hi(double x) { return (float)x; }
-__host__ __device__ constexpr float f_lo(double x) { return (float)(x - (double)(float)x); }
-
-// Compensated accumulator (hi, lo) for sum_j w_j k_j with w split into floats
-// (the tableau's split tables, hi = float(w), lo = float(w - hi), are
-// generated with the tables, so no split happens at run time).
 struct CSum {
     float hi = 0.0f, lo = 0.0f;
-    __device__ __forceinline__ void add(double w, float k) {
-        const float wh = f_hi(w), wl = f_lo(w);
-        float p = wh * k;
-        float e = fmaf(wh, k, -p);
-        e = fmaf(wl, k, e);
-        float s = hi + p;
-        float bb = s - hi;
-        float e2 = (hi - (s - bb)) + (p - bb);
-        hi = s;
-        lo += e + e2;
-    }
-    // weight given as a float pair wh + wl (a runtime product formed exactly)
+    // weight given as a float pair wh + wl
     __device__ __forceinline__ void add_pair(float wh, float wl, float k) {
         float p = wh * k;
         float e = fmaf(wh, k, -p);
