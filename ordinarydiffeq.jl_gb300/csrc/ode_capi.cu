@@ -592,6 +592,21 @@ int run_ensemble(ode_handle* h, Ctx& c, const ode_problem_desc* d, const ode_opt
 }
 
 
+// Device address of a page-locked host buffer (mapped into the device's
+// address space), or nullptr for ordinary pageable memory.  On GB300 the GPU
+// reaches page-locked Grace memory over NVLink-C2C, so kernels can read their
+// inputs and write their saves there directly.
+template <class T> T* mapped_ptr(T* ptr) {
+    if (!ptr) return nullptr;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type != cudaMemoryTypeHost || at.devicePointer == nullptr) return nullptr;
+    return (T*)at.devicePointer;
+}
+
 // Large host-buffer solves run as a pipeline of kPipeChunks trajectory slices:
 // slice k+1's inputs go in on one copy stream while slice k integrates and
 // slice k-1's outputs come back on another, so the transfers hide behind the
@@ -1026,6 +1041,26 @@ int ode_solve_ensemble(ode_handle* h, const ode_problem_desc* d, const ode_optio
     std::lock_guard<std::mutex> lk(h->api_mu);
     CUDA_TRY(h, cudaSetDevice(h->device));
     *h->h_abort = 0;
+    if (N > 0) {   // every buffer page-locked: the kernels work in place, no staging copies
+        const double *mu0 = mapped_ptr(u0), *mp = mapped_ptr(p), *mts = mapped_ptr(tspan);
+        const double* msv = o->nsave > 0 ? mapped_ptr(saveat) : nullptr;
+        const int32_t* mnpt = npt ? mapped_ptr(npt) : nullptr;
+        double *mt = t_out ? mapped_ptr(t_out) : nullptr, *mu = mapped_ptr(u_out);
+        int32_t *mns = mapped_ptr(nsaved), *mrc = mapped_ptr(retcode);
+        ode_stats* mst = stats ? mapped_ptr(stats) : nullptr;
+        if (mu0 && mp && mts && mu && mns && mrc && (o->nsave == 0 || msv) && (!npt || mnpt) && (!t_out || mt) &&
+            (!stats || mst)) {
+            cudaStream_t s = h->main.stream;
+            rc = run_ensemble(h, h->main, d, o, N, mnpt, mu0, mp, mts, msv, mt, mu, mns, mrc, (OdeStatsDev*)mst, s,
+                              /*graph=*/true);
+            cudaError_t e = cudaStreamSynchronize(s);
+            if (rc) return rc;
+            if (e != cudaSuccess) return fail(h, ODE_E_CUDA, std::string("solve: ") + cudaGetErrorString(e));
+            float ms = 0;
+            if (cudaEventElapsedTime(&ms, h->main.ev0, h->main.ev1) == cudaSuccess) h->last_ms = ms;
+            return ODE_OK;
+        }
+    }
     const size_t n = (size_t)d->n_states, np = (size_t)d->n_params, cap = save_cap(o);
     const size_t nsv = (size_t)o->nsave * (o->saveat_per_traj ? (size_t)N : 1);
     if ((rc = grow(h, h->b_u0, n * N * 8)) || (rc = grow(h, h->b_p, np * N * 8)) ||

@@ -319,12 +319,17 @@ def _device_solve(model, alg, u0, p, ts, saveat, reltol, abstol, precision="fp64
             "retcode": bufs[7].cpu().numpy(), "stats": {k: st[:, i] for i, k in enumerate(names)}}
 
 
-def _same_saved(a, b):
+def _same_saved(a, b, npt=None):
+    """Equal saves; only the slots each trajectory wrote are compared (rows past
+    nsaved and, for uneven sizes, components past the trajectory's size are
+    unspecified)."""
     ns = a["nsaved"]
     assert np.array_equal(ns, b["nsaved"]) and np.array_equal(a["retcode"], b["retcode"])
     m = np.arange(a["t"].shape[0])[:, None] < ns[None, :]
     assert np.array_equal(a["t"][m], b["t"][m])
     mu = np.broadcast_to(m[:, None, :], a["u"].shape)
+    if npt is not None:
+        mu = mu & (np.arange(a["u"].shape[1])[None, :, None] < np.asarray(npt)[None, None, :])
     assert np.array_equal(a["u"][mu], b["u"][mu])
     assert np.array_equal(a["stats"]["naccept"], b["stats"]["naccept"])
 
@@ -345,7 +350,7 @@ def test_pipelined_uneven_host_solve_equals_device_solve():
     N = 40000
     u0, p, ts, sv, npt = duffing_inputs(N, [2, 4, 8, 16, 32], tf_range=(1.0, 3.0), seed=5)
     _same_saved(gpu("duffing_chain", "vern7", u0, p, ts, sv, 1e-6, 1e-6, precision="mixed", n_per_traj=npt),
-                _device_solve("duffing_chain", "vern7", u0, p, ts, sv, 1e-6, 1e-6, precision="mixed", npt=npt))
+                _device_solve("duffing_chain", "vern7", u0, p, ts, sv, 1e-6, 1e-6, precision="mixed", npt=npt), npt)
 
 
 @pytest.mark.parametrize("model,alg,rt,at", [("lorenz", "tsit5", 1e-8, 1e-8), ("lorenz", "vern7", 1e-8, 1e-8),
@@ -372,3 +377,48 @@ def test_save_everystep_overflow_keeps_the_final_point():
     assert np.array_equal(g["t"][6], ts[1])   # the last slot holds tf
     o = oracle("lorenz", "tsit5", u0, p, ts, None, 1e-8, 1e-8, save_everystep=True, max_step_saves=5)
     assert np.allclose(g["u"][6], o["u"][6], rtol=1e-6, atol=1e-6)
+
+
+@pytest.mark.parametrize("uneven", [False, True])
+def test_page_locked_host_buffers_solve_in_place(uneven):
+    # page-locked host buffers are read and written by the kernels directly
+    # (no staging copies); results must equal the staged path's
+    import ctypes as C
+    import torch
+    from gpu_common import ALG
+    from odegb300 import EnsembleGB300, _lib
+    from odegb300.ensemble import MODELS, _options, get_handle
+    from odegb300.saveat import resolve_saveat
+    if uneven:
+        u0, p, ts, sv, npt = duffing_inputs(3000, [2, 4, 8, 16, 32], tf_range=(1.0, 5.0), seed=13)
+        model, alg, rt, at, prec = "duffing_chain", "vern7", 1e-6, 1e-6, "mixed"
+    else:
+        u0, p, ts = robertson_inputs(3000, seed=13)
+        sv, npt = ROBER_SAVEAT, None
+        model, alg, rt, at, prec = "robertson", "rodas5p", 1e-6, 1e-10, "mixed"
+    ref = gpu(model, alg, u0, p, ts, sv, rt, at, precision=prec, n_per_traj=npt)
+    spec = resolve_saveat(sv, ts)
+    ens = EnsembleGB300(precision=prec)
+    o = _options(rt, at, None, None, None, 10 ** 6, spec, ens, None, None)
+    n, N = u0.shape
+    d = _lib.ProblemDesc(MODELS[model], ALG[alg][0].alg_id, n, p.shape[0], ens.prec_id(), 0)
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+    h_u0, h_p, h_ts, h_sv = pin(u0), pin(p), pin(ts), pin(spec.values)
+    h_npt = pin(npt) if npt is not None else None
+    cap = spec.cap
+    h_t = torch.empty((cap, N), dtype=torch.float64).pin_memory()
+    h_u = torch.empty((cap, n, N), dtype=torch.float64).pin_memory()
+    h_ns = torch.empty(N, dtype=torch.int32).pin_memory()
+    h_rc = torch.empty(N, dtype=torch.int32).pin_memory()
+    h_st = torch.empty((N, 6), dtype=torch.int64).pin_memory()
+    ptr = lambda t, ty=C.c_double: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(ty)) if t is not None else None
+    L = _lib.load()
+    h = get_handle(0)
+    _lib.check(L.ode_solve_ensemble(h, C.byref(d), C.byref(o), N, ptr(h_npt, C.c_int32), ptr(h_u0), ptr(h_p),
+                                    ptr(h_ts), ptr(h_sv), ptr(h_t), ptr(h_u), ptr(h_ns, C.c_int32),
+                                    ptr(h_rc, C.c_int32), ptr(h_st, _lib.Stats)), h)
+    names = ("nf", "njacs", "nw", "nsolve", "naccept", "nreject")
+    st = h_st.numpy()
+    got = {"t": h_t.numpy(), "u": h_u.numpy(), "nsaved": h_ns.numpy(), "retcode": h_rc.numpy(),
+           "stats": {k: st[:, i] for i, k in enumerate(names)}}
+    _same_saved(got, ref, npt)
