@@ -14,7 +14,8 @@ inputs resident in HBM.  `e2e` is the same metric through the public
 host-buffer call (host->device copies and results back inside the timed region).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                    [--config robertson|lorenz|duffing|brusselator] [--trajectories N]
+                    [--config robertson|lorenz|duffing|brusselator|robertson_ros23|lorenz_dense|serving]
+                    [--trajectories N]
 """
 import argparse
 import ctypes as C
@@ -38,6 +39,10 @@ CONFIGS = {
                 1_000_000),
     "brusselator": ("Brusselator-1D 32 cells (64 states), Rodas5P, reltol 1e-5 abstol 1e-8, tspan (0,10)",
                     65_536),
+    "robertson_ros23": ("Robertson kinetics, Rosenbrock23 + analytic J, reltol 1e-4 abstol 1e-8, tspan (0,1e5), "
+                        "20 log-spaced saves", 100_000),
+    "lorenz_dense": ("Lorenz, Tsit5, reltol=abstol=1e-8, tspan (0,1), dense output (every step with its "
+                     "interpolation vectors), then sol(t) at 101 times for every trajectory", 10_000),
     "serving": ("open-loop Poisson request stream; each request 1-4096 trajectories (log-uniform) of Lorenz/Tsit5, "
                 "Robertson/Rodas5P or Brusselator-1D (8/16/32 cells)/Rodas5P, reltol 10^U(-8,-4)", 0),
 }
@@ -146,8 +151,15 @@ def replica_rate(world, n_per_rank, seconds):
 
 def workload(name, N, seed):
     from odegb300 import workloads as W
+    if name == "robertson_ros23":
+        return W.robertson(N, seed=seed, alg="rosenbrock23", reltol=1e-4, abstol=1e-8)
+    if name == "lorenz_dense":   # no saveat: every step kept (the reference's dense default)
+        return dict(W.lorenz(N, seed=seed), saveat=None, everystep=True, max_step_saves=DENSE_MAX_STEPS)
     return {"robertson": W.robertson, "lorenz": W.lorenz, "duffing": W.duffing,
             "brusselator": W.brusselator}[name](N, seed=seed)
+
+
+DENSE_MAX_STEPS = 512   # step slots per trajectory of the dense workload (Lorenz at 1e-8 takes < 200)
 
 
 def oracle_solve(wl, idx, nthreads=0, truth=False):
@@ -157,23 +169,26 @@ def oracle_solve(wl, idx, nthreads=0, truth=False):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as O
     from odegb300.saveat import resolve_saveat
-    alg = {"tsit5": O.TSIT5, "vern7": O.VERN7, "rodas5p": O.RODAS5P}[wl["alg"]]
+    alg = {"tsit5": O.TSIT5, "vern7": O.VERN7, "rodas5p": O.RODAS5P, "rosenbrock23": O.ROSENBROCK23}[wl["alg"]]
     model = {"lorenz": O.LORENZ, "robertson": O.ROBERTSON, "duffing_chain": O.DUFFING,
              "brusselator_1d": O.BRUSSELATOR}[wl["model"]]
     ts = wl["tspan"][:, idx]
     sv = wl["saveat"]
     if isinstance(sv, np.ndarray) and sv.ndim == 2:
         sv = sv[:, idx]
-    spec = resolve_saveat(sv, ts)
+    every = bool(wl.get("everystep")) and not truth
+    spec = resolve_saveat(sv, ts, save_everystep=every, max_step_saves=wl.get("max_step_saves", 1024))
     npt = wl.get("n_per_traj")
     rt, at = wl["reltol"], wl["abstol"]
     if truth:
-        alg, rt, at = (O.RODAS5P, 1e-12, 1e-16) if wl["alg"] == "rodas5p" else (O.VERN9, 1e-14, 1e-14)
+        stiff = wl["alg"] in ("rodas5p", "rosenbrock23")
+        alg, rt, at = (O.RODAS5P, 1e-12, 1e-16) if stiff else (O.VERN9, 1e-14, 1e-14)
     return O.solve_ensemble(alg, model, wl["u0"][:, idx], wl["p"][:, idx], ts, spec.values, rt,
                             at, n_per_traj=None if npt is None else npt[idx], saveat_as_tstops=truth,
                             saveat_per_traj=spec.per_traj, save_start=spec.save_start, save_end=spec.save_end,
                             save_end_user=spec.save_end_user, saveat_given=spec.nsave > 0,
-                            saveat_scalar=spec.scalar, nthreads=nthreads)
+                            saveat_scalar=spec.scalar, save_everystep=spec.everystep,
+                            max_step_saves=spec.max_step_saves, nthreads=nthreads)
 
 
 class Clocks:
@@ -497,6 +512,159 @@ def run_reference(args, world, rank):
         "e2e": {"value": v, "unit": "trajectories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
+def measured_hbm_gbs():
+    """The machine's measured copy bandwidth (MEASURED_PEAKS.json, written by the
+    measurement job), or the recorded fallback of 6.8 TB/s."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback"
+
+
+def run_dense(args, world, rank, local, dist):
+    """Dense output through the public calls: ode_solve_ensemble_dense on
+    page-locked host buffers (every accepted step kept with its interpolation
+    vectors, written in place by the kernels), then sol(t) of every trajectory
+    at 101 times in one ode_dense_eval launch.  value: trajectories/s of the
+    dense solve on the device (its launch's CUDA-event time); e2e: the same
+    through the host call; dense_eval: (trajectory, time) pairs per second."""
+    import torch
+    import odegb300
+    from odegb300 import _lib, workloads as W
+    from odegb300.ensemble import ALG_BY_NAME, MODELS, _options, get_handle
+    from odegb300.saveat import resolve_saveat
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    L = _lib.load()
+    h = get_handle(local)
+    desc_name, N0 = CONFIGS[args.config]
+    N = args.trajectories or N0
+    wl = workload(args.config, N, seed=42 + rank)
+    n = wl["u0"].shape[0]
+    alg = ALG_BY_NAME[wl["alg"]]
+    sv = resolve_saveat(None, wl["tspan"], save_everystep=True, max_step_saves=wl["max_step_saves"])
+    cap = sv.cap
+    ens = odegb300.EnsembleGB300(precision="fp64")
+    o = _options(wl["reltol"], wl["abstol"], None, None, None, 1000000, sv, ens, None, None)
+    d = _lib.ProblemDesc(MODELS[wl["model"]], alg.alg_id, n, wl["p"].shape[0], 0, 0)
+    nk = L.ode_dense_nk(alg.alg_id)
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+    h_u0, h_p, h_ts = pin(wl["u0"]), pin(wl["p"]), pin(wl["tspan"])
+    h_t = torch.empty((cap, N), dtype=torch.float64).pin_memory()
+    h_u = torch.empty((cap, n, N), dtype=torch.float64).pin_memory()
+    h_k = torch.empty((cap, nk, n, N), dtype=torch.float64).pin_memory()
+    h_ns = torch.empty(N, dtype=torch.int32).pin_memory()
+    h_rc = torch.empty(N, dtype=torch.int32).pin_memory()
+    h_st = torch.empty((N, 6), dtype=torch.int64).pin_memory()
+    NQ = 101
+    tq = np.linspace(0.0, 1.0, NQ)
+    h_tq = pin(tq)
+    h_out = torch.empty((NQ, n, N), dtype=torch.float64).pin_memory()
+    hp = lambda t, ty=C.c_double: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(ty))
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    x = C.c_double(0)
+    cnt = C.c_int64(0)
+
+    def last_ms():
+        L.ode_last_kernel_ms(h, C.byref(x))
+        return x.value
+
+    def launches():
+        L.ode_kernel_launches(h, C.byref(cnt))
+        return cnt.value
+
+    def solve():
+        _lib.check(L.ode_solve_ensemble_dense(h, C.byref(d), C.byref(o), N, hp(h_u0), hp(h_p), hp(h_ts), hp(h_t),
+                                              hp(h_u), hp(h_k), hp(h_ns, C.c_int32), hp(h_rc, C.c_int32),
+                                              hp(h_st, _lib.Stats)), h)
+
+    def evaluate():
+        _lib.check(L.ode_dense_eval(h, C.byref(d), N, hp(h_p), hp(h_t), hp(h_u), hp(h_k), hp(h_ns, C.c_int32), cap,
+                                    NQ, hp(h_tq), 0, hp(h_out)), h)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+        dms, wall = [], []
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            fn()
+            wall.append(time.perf_counter() - t0)
+            dms.append(last_ms())
+        return max_over_ranks(float(np.mean(dms)), dist, dev), max_over_ranks(float(np.mean(wall)), dist, dev)
+
+    clocks = Clocks(local)
+    clocks.start()
+    l0 = launches()
+    ms, wall_s = timed(solve)
+    nl = launches() - l0
+    ev_ms, ev_wall = timed(evaluate)
+    clk = clocks.stop()
+    st = h_st.numpy()
+    ns = h_ns.numpy().astype(np.int64)
+    attempts = int(st[:, 4].sum() + st[:, 5].sum())
+    fl = W.attempt_flops(wl["alg"], wl["model"], n)
+    peak = C.c_double(0)
+    L.ode_measure_fma_peak(local, 0, C.byref(peak))
+    achieved = attempts * fl / (ms * 1e-3)
+    written = int(ns.sum()) * (1 + n + nk * n) * 8 + N * (8 + 48)
+    hbm_peak, hbm_src = measured_hbm_gbs()
+    # sol(t): per (trajectory, time) pair the interval search reads ~log2(steps)
+    # saved times, then u at both ends and the nk vectors (n each), and writes n values
+    pair_bytes = (int(np.ceil(np.log2(max(2.0, ns.mean())))) + 2 * n + nk * n + n) * 8
+    ev_gbs = NQ * N * pair_bytes / (ev_ms * 1e-3) / 1e9
+
+    acc, cpu = None, None
+    if rank == 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle as O
+        errs, same = [], 0
+        out = h_out.numpy()
+        for j in range(0, min(N, 64)):
+            r = O.solve(O.TSIT5, O.LORENZ, wl["u0"][:, j], wl["p"][:, j], wl["tspan"][:, j], dense=True,
+                        reltol=wl["reltol"], abstol=wl["abstol"], saveat_given=False, save_everystep=True,
+                        max_step_saves=wl["max_step_saves"], save_start=True, save_end=True)
+            ref = r["dense"](tq)
+            errs.append(float(np.max(np.abs(out[:, :, j] - ref) / (wl["reltol"] * np.abs(ref) + wl["abstol"]))))
+            same += int(r["dense"].nsteps + 1 == ns[j])
+        errs = np.array(errs)
+        acc = {"sol_t_err_vs_oracle_x_tol": {"max": float(errs.max()), "p99": float(np.percentile(errs, 99)),
+                                             "median": float(np.median(errs))},
+               "same_step_count_frac": same / len(errs), "checked": int(len(errs))}
+        if not args.no_cpu_baseline:
+            cpu = cpu_baseline(wl, N, args.cpu_seconds)
+        print(json.dumps({
+            "metric": "trajectories/sec, dense output (every step with its interpolation vectors), FP64",
+            "value": world * N / (ms * 1e-3), "unit": "trajectories/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, config distributions)",
+            "config": {"workload": desc_name, "trajectories": N, "max_step_saves": wl["max_step_saves"],
+                       "l2": "256 MB buffer written between timed steps",
+                       "buffers": "page-locked host buffers, written in place by the kernels"},
+            "e2e": {"value": world * N / wall_s, "unit": "trajectories/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0, "note": "page-locked buffers: the kernels read the inputs and write "
+                    "%d bytes of saves and vectors in place over NVLink-C2C" % written},
+            "dense_eval": {"queries_per_trajectory": NQ, "ms": ev_ms, "pairs_per_s": NQ * N / (ev_ms * 1e-3),
+                           "e2e_pairs_per_s": NQ * N / ev_wall, "algorithmic_gbs": ev_gbs,
+                           "hbm_peak_gbs": hbm_peak, "hbm_frac": ev_gbs / hbm_peak, "peak_source": hbm_src,
+                           "bytes_per_pair": pair_bytes},
+            "accuracy": acc,
+            "roofline": {"bound": "fp64 pipe", "achieved": achieved / 1e12, "peak": peak.value / 1e12,
+                         "unit": "TFLOP/s", "frac": achieved / peak.value if peak.value else None, "traffic": None,
+                         "flops_per_attempt": fl, "attempted_steps": attempts,
+                         "peak_source": "ode_measure_fma_peak (FMA-chain kernel, this GPU)"},
+            "hbm": {"bytes_written_per_solve": written, "achieved_gbs": written / (ms * 1e-3) / 1e9},
+            "mean_accepted_steps": float(st[:, 4].mean()),
+            "cpu_baseline": cpu, "clocks": clk, "gpu_launches": nl}))
+
+
 def main():
     args = parse()
     world, rank, local, dist = dist_setup(args)
@@ -504,6 +672,8 @@ def main():
         run_reference(args, world, rank)
     elif args.config == "serving":
         run_serving(args, rank, local)
+    elif args.config == "lorenz_dense":
+        run_dense(args, world, rank, local, dist)
     else:
         run_gb300(args, world, rank, local, dist)
     if dist is not None:

@@ -33,14 +33,16 @@
 extern "C" {
 #endif
 
-#define ODE_ABI_VERSION 2
+#define ODE_ABI_VERSION 3
 
 typedef struct ode_handle ode_handle;
 
 /* Algorithms: Tsit5 (lib/OrdinaryDiffEqTsit5/src/algorithms.jl:16-21),
  * Vern7 (lib/OrdinaryDiffEqVerner/src/algorithms.jl:44-50, lazy = true),
- * Rodas5P (lib/OrdinaryDiffEqRosenbrock/src/algorithms.jl:83-87). */
-enum ode_alg { ODE_TSIT5 = 0, ODE_VERN7 = 1, ODE_RODAS5P = 2 };
+ * Rodas5P (lib/OrdinaryDiffEqRosenbrock/src/algorithms.jl:83-87),
+ * Rosenbrock23 (lib/OrdinaryDiffEqRosenbrock/src/algorithms.jl:1-16,108-146, the
+ * default max_jac_age = 1: a fresh J and W on every step attempt). */
+enum ode_alg { ODE_TSIT5 = 0, ODE_VERN7 = 1, ODE_RODAS5P = 2, ODE_ROSENBROCK23 = 3 };
 
 /* Registered right-hand sides (with analytic Jacobians).  The reference takes
  * an arbitrary f(du,u,p,t); device code cannot call Julia closures, so models
@@ -143,6 +145,41 @@ int ode_solve_ensemble_device(ode_handle* h, const ode_problem_desc* d, const od
                               const int32_t* n_per_traj_dev, const double* u0, const double* p,
                               const double* tspan, const double* saveat, double* t_out, double* u_out,
                               int32_t* nsaved, int32_t* retcode, ode_stats* stats, void* cuda_stream);
+
+/* Dense output: the reference's dense = true, its default when no saveat is
+ * given (lib/OrdinaryDiffEqCore/src/solve.jl:145-146; sol.k filled by
+ * save_dense_at_t!, integrator_utils.jl:455-473).  ode_dense_nk: vectors
+ * stored per saved step, the method's interpolation data (integrator.k):
+ * Tsit5 7 (k1..k7), Vern7 7 (k1, k4..k9: its interpolant and lazy extra
+ * stages read no others), Rodas5P 3 (the dense k1..k3), Rosenbrock23 2 (k1,
+ * k2).  ODE_E_INVALID for an unknown alg. */
+int ode_dense_nk(int alg);
+
+/* Synchronous dense solve on HOST buffers: every accepted step is saved
+ * (o->save_everystep = 1, o->nsave = 0) and its vectors go to
+ * k_out[((s*nk + q)*n_states + i)*N + j], cap = max_step_saves + 2 slots.
+ * The start save's vectors are 0.  A trajectory with more steps than slots
+ * keeps its final point in the last slot with NaN vectors: its last interval
+ * cannot be interpolated.  Uniform sizes only (no n_per_traj).  Page-locked
+ * buffers are used in place, as in ode_solve_ensemble. */
+int ode_solve_ensemble_dense(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int64_t ntraj,
+                             const double* u0, const double* p, const double* tspan, double* t_out,
+                             double* u_out, double* k_out, int32_t* nsaved, int32_t* retcode, ode_stats* stats);
+
+/* sol_j(t) of a dense solve for every trajectory j at nq query times (tq[r]
+ * shared, or tq[r*N + j] per trajectory), evaluated on the device in FP64 from
+ * the solve's HOST outputs (t_saved, u_saved, k_saved with cap slots, layouts
+ * as above; p as given to the solve, read by Vern7's extra stages):
+ * out[(r*n_states + i)*N + j].  Follows ode_interpolation
+ * (lib/OrdinaryDiffEqCore/src/dense/generic_dense.jl:1094-1190): the left-
+ * continuous interval ts[i-] < t <= ts[i+], theta = (t - ts[i-]) /
+ * (ts[i+] - ts[i-]) and the method's interpolant with the vectors of the step
+ * ending at ts[i+] (Vern7 first forms its extra stages from them).  Times
+ * outside the saved range use the first or last step's polynomial, as
+ * ode_interpolation does; a trajectory with nsaved 0 gets NaN. */
+int ode_dense_eval(ode_handle* h, const ode_problem_desc* d, int64_t ntraj, const double* p,
+                   const double* t_saved, const double* u_saved, const double* k_saved, const int32_t* nsaved,
+                   int32_t cap, int32_t nq, const double* tq, int32_t tq_per_traj, double* out);
 
 /* Continuous-batching serving API.  ode_submit copies the request's inputs
  * into handle-owned pinned/device memory and returns a ticket at once; the

@@ -198,8 +198,8 @@ void jac(int model, int n, const double* u, const double* p, double t, double* J
 
 // ---------------------------------------------------------------- integrator
 struct Step {  // one accepted step for dense output
-    double tprev, dt;
-    std::vector<double> y0, y1, k;  // k: nk * n
+    double tprev, tend;
+    std::vector<double> y0, y1, k;  // k: nk * n (Vern7: k1..k10; the extra stages are formed when evaluated)
 };
 
 struct Dense {
@@ -615,12 +615,90 @@ void rodas_interp(double th, const double* y0, const double* y1, const double* K
     }
 }
 
+// perform_step!(::Rosenbrock23Cache): lib/OrdinaryDiffEqRosenbrock/src/rosenbrock_perform_step.jl:34-146,
+// tableau rosenbrock_tableaus.jl:6-10 (c32 = 6 + sqrt(2), d = 1/(2 + sqrt(2))).  A W-method
+// whose default max_jac_age = 1 (algorithms.jl:108-115) makes the reuse decision
+// (derivative_utils.jl:46-170) take a fresh J and W on every attempt, rejected or
+// not.  FSAL: fsalfirst is f(uprev), carried from the last accepted step.
+// Multiply-adds follow @muladd: a - b*c -> muladd(-b, c, a).
+void rosenbrock23_step(Integ& I) {
+    const int n = I.n;
+    const double t = I.t, dt = I.dt;
+    const double c32 = 6.0 + std::sqrt(2.0), d = 1.0 / (2.0 + std::sqrt(2.0));
+    const double* up = I.uprev.data();
+    const double dtgamma = dt * d;
+    const double neginvdtgamma = -(1.0 / dtgamma);
+    const double dto2 = dt / 2.0, dto6 = dt / 6.0;
+    jac(I.model, n, up, I.p, t, I.J.data());
+    I.st.njacs += 1;
+    // the reference differentiates f in t by AD (one counted call); autonomous models: dT = 0
+    f_eval(I, up, t, I.du.data());
+    std::fill(I.dT.begin(), I.dT.end(), 0.0);
+    I.st.nf += 1;
+    const double invdtgamma = 1.0 / dtgamma;
+    for (int i = 0; i < n * n; ++i) I.W[i] = I.J[i];
+    for (int i = 0; i < n; ++i) I.W[i * n + i] = std::fma(-1.0, invdtgamma, I.J[i * n + i]);
+    I.st.nw += 1;
+    lu_factor(n, I.W.data(), I.piv.data());
+    const double* fsal0 = I.fsalfirst.data();
+    double* r = I.rhs.data();
+    double* k1 = I.ks.data();
+    double* k2 = k1 + n;
+    double* k3 = k1 + 2 * n;
+    double* f1 = k1 + 3 * n;
+    for (int i = 0; i < n; ++i) r[i] = std::fma(dtgamma, I.dT[i], fsal0[i]);   // fsalfirst + dtd1 dT
+    lu_solve(n, I.W.data(), I.piv.data(), r);
+    for (int i = 0; i < n; ++i) k1[i] = r[i] * neginvdtgamma;
+    I.st.nsolve += 1;
+    double* u = I.u.data();
+    for (int i = 0; i < n; ++i) u[i] = std::fma(dto2, k1[i], up[i]);
+    f_eval(I, u, t + dto2, f1);
+    I.st.nf += 1;
+    for (int i = 0; i < n; ++i) r[i] = f1[i] - k1[i];
+    lu_solve(n, I.W.data(), I.piv.data(), r);
+    for (int i = 0; i < n; ++i) k2[i] = std::fma(r[i], neginvdtgamma, k1[i]);
+    I.st.nsolve += 1;
+    for (int i = 0; i < n; ++i) u[i] = std::fma(dt, k2[i], up[i]);
+    if (I.o.adaptive) {
+        double* fl = I.fsallast.data();
+        f_eval(I, u, t + dt, fl);
+        I.st.nf += 1;
+        for (int i = 0; i < n; ++i) {
+            double acc = std::fma(-c32, k2[i] - f1[i], fl[i]);
+            acc = std::fma(-2.0, k1[i] - fsal0[i], acc);
+            r[i] = std::fma(dt, I.dT[i], acc);
+        }
+        lu_solve(n, I.W.data(), I.piv.data(), r);
+        for (int i = 0; i < n; ++i) k3[i] = r[i] * neginvdtgamma;
+        I.st.nsolve += 1;
+        for (int i = 0; i < n; ++i) I.utilde[i] = dto6 * (std::fma(-2.0, k2[i], k1[i]) + k3[i]);
+        I.EEst = residual_norm(I, I.utilde.data(), up, u);
+    } else {
+        f_eval(I, u, t + dt, I.fsallast.data());
+        I.st.nf += 1;
+    }
+    // integrator.k = [k1, k2] (initialize!, rosenbrock_perform_step.jl:1-14)
+    std::memcpy(I.k.data(), k1, sizeof(double) * n);
+    std::memcpy(I.k.data() + n, k2, sizeof(double) * n);
+    I.nk_valid = 2;
+}
+
+// Rosenbrock23 interpolant: lib/OrdinaryDiffEqRosenbrock/src/rosenbrock_interpolants.jl:39-67
+// (c1 = th(1-th)/(1-2d), c2 = th(th-2d)/(1-2d); y0 + dt (c1 k1 + c2 k2)).
+void ros23_interp(double th, double dt, const double* y0, const double* K, int n, double* out) {
+    const double d = 1.0 / (2.0 + std::sqrt(2.0));
+    const double c1 = th * (1.0 - th) / (1.0 - 2.0 * d);
+    const double c2 = th * (th - 2.0 * d) / (1.0 - 2.0 * d);
+    for (int i = 0; i < n; ++i) out[i] = std::fma(dt, std::fma(c1, K[i], c2 * K[n + i]), y0[i]);
+}
+
 void do_step(Integ& I) {
     switch (I.alg) {
     case ORC_TSIT5: tsit5_step(I); break;
     case ORC_VERN7: vern7_step(I); break;
     case ORC_VERN9: vern9_step(I); break;
     case ORC_RODAS5P: rodas5p_step(I); break;
+    case ORC_ROSENBROCK23: rosenbrock23_step(I); break;
     }
 }
 
@@ -636,6 +714,7 @@ void interpolate(Integ& I, double th, double* out) {
         vern7_interp(th, I.dt, I.uprev.data(), I.k.data(), n, out);
         break;
     case ORC_RODAS5P: rodas_interp(th, I.uprev.data(), I.u.data(), I.k.data(), n, out); break;
+    case ORC_ROSENBROCK23: ros23_interp(th, I.dt, I.uprev.data(), I.k.data(), n, out); break;
     default: {  // Vern9 ground truth: linear (only reached if a save is not a tstop)
         for (int i = 0; i < n; ++i) out[i] = (1.0 - th) * I.uprev[i] + th * I.u[i];
     }
@@ -726,16 +805,14 @@ double stepsize_controller(Integ& I) {
 
 void record_dense(Integ& I) {
     if (!I.dense) return;
+    // sol.t / sol.u / sol.k of an every-step save (save_dense_at_t!, integrator_utils.jl:455-473)
     Step s;
     s.tprev = I.tprev;
-    s.dt = I.dt;
+    s.tend = I.t;
     s.y0 = I.uprev;
     s.y1 = I.u;
-    if (I.alg == ORC_VERN7 && I.nk_valid < 16) {
-        vern7_extra(I.model, I.n, I.p, I.tprev, I.dt, I.uprev.data(), I.k.data());
-        I.nk_valid = 16;
-    }
-    int nk = I.alg == ORC_TSIT5 ? 7 : I.alg == ORC_VERN7 ? 16 : I.alg == ORC_RODAS5P ? 3 : 0;
+    int nk = I.alg == ORC_TSIT5 ? 7 : I.alg == ORC_VERN7 ? 10 : I.alg == ORC_RODAS5P ? 3
+           : I.alg == ORC_ROSENBROCK23 ? 2 : 0;
     s.k.assign(I.k.begin(), I.k.begin() + (size_t)nk * I.n);
     I.dense->steps.push_back(std::move(s));
 }
@@ -790,7 +867,7 @@ void loopheader(Integ& I) {
             I.success_iter++;
             I.uprev = I.u;
             I.dt = I.dtpropose;
-            if (I.alg == ORC_TSIT5) I.fsalfirst = I.fsallast;
+            if (I.alg == ORC_TSIT5 || I.alg == ORC_ROSENBROCK23) I.fsalfirst = I.fsallast;
             modify_dt_for_tstops(I);
         } else {
             I.dt = I.dt / jmin(1.0 / I.qmin, I.q11 / I.gamma);
@@ -850,7 +927,7 @@ int solve_one(Integ& I, const double* u0) {
     I.fsallast.assign(n, 0.0);
     I.k.assign((size_t)16 * n, 0.0);
     I.interp_out.assign(n, 0.0);
-    if (I.alg == ORC_RODAS5P) {
+    if (I.alg == ORC_RODAS5P || I.alg == ORC_ROSENBROCK23) {
         I.J.assign((size_t)n * n, 0.0);
         I.W.assign((size_t)n * n, 0.0);
         I.dT.assign(n, 0.0);
@@ -874,7 +951,8 @@ int solve_one(Integ& I, const double* u0) {
     I.last_saved_t = NAN;
     std::memset(&I.st, 0, sizeof(I.st));
     if (I.o.save_start) push_save(I, I.t0, I.u.data());
-    if (I.alg == ORC_TSIT5) {  // initialize!: FSAL pre-start (tsit_perform_step.jl:293-307)
+    if (I.alg == ORC_TSIT5 || I.alg == ORC_ROSENBROCK23) {
+        // initialize!: FSAL pre-start (tsit_perform_step.jl:293-307, rosenbrock_perform_step.jl:1-14)
         f_eval(I, I.u.data(), I.t, I.fsalfirst.data());
         I.st.nf += 1;
     }
@@ -923,7 +1001,7 @@ void setup(Integ& I, int alg, int model, int n, const double* p, double t0, doub
     I.o = *o;
     if (I.o.dtmax <= 0.0) I.o.dtmax = tf - t0;
     if (I.o.maxiters <= 0) I.o.maxiters = 1000000;
-    I.order = alg == ORC_VERN7 ? 7 : alg == ORC_VERN9 ? 9 : 5;
+    I.order = alg == ORC_VERN7 ? 7 : alg == ORC_VERN9 ? 9 : alg == ORC_ROSENBROCK23 ? 2 : 5;
     // controller defaults: lib/OrdinaryDiffEqCore/src/alg_utils.jl:407-879
     I.beta2 = 2.0 / (5.0 * I.order);
     I.beta1 = 7.0 / (10.0 * I.order);
@@ -932,7 +1010,7 @@ void setup(Integ& I, int alg, int model, int n, const double* p, double t0, doub
     I.qmax_first = o->qmax_first_step > 0 ? o->qmax_first_step : 10000.0;
     I.gamma = 0.9;
     I.qsteady_min = 1.0;
-    I.qsteady_max = alg == ORC_RODAS5P ? 1.2 : 1.0;
+    I.qsteady_max = (alg == ORC_RODAS5P || alg == ORC_ROSENBROCK23) ? 1.2 : 1.0;   // AdaptiveImplicit: 6/5
     I.qoldinit = 1e-4;
     I.tstops.clear();
     for (int i = 0; i < ntstops; ++i)
@@ -992,34 +1070,65 @@ int orc_solve(int alg, int model, int n, const double* p, double t0, double tf, 
 
 int orc_dense_nsteps(void* h) { return h ? (int)((Dense*)h)->steps.size() : 0; }
 
+// sol(t) on the recorded steps: ode_interpolation(tval::Number, ...) with left
+// continuity (lib/OrdinaryDiffEqCore/src/dense/generic_dense.jl:1094-1190).  The
+// saved times are ts = [tprev of step 0, tend of each step]; i+ is the first
+// index >= 1 (0-based) with ts[i+] >= t, clamped to the last; dt = ts[i+] -
+// ts[i-] and theta = (t - ts[i-]) / dt; Vern7's extra stages are formed by
+// _ode_addsteps! with that dt (verner_addsteps.jl:137-193).
 int orc_dense_eval(void* h, const double* tq, int nq, double* out) {
     Dense* D = (Dense*)h;
-    int n = D->n;
+    const int n = D->n;
+    if (D->steps.empty()) return -1;
+    const size_t ns = D->steps.size() + 1;
+    auto ts = [&](size_t i) { return i == 0 ? D->steps[0].tprev : D->steps[i - 1].tend; };
+    std::vector<double> K;
     for (int q = 0; q < nq; ++q) {
-        double t = tq[q];
-        if (D->steps.empty()) return -1;
-        size_t s = 0;
-        if (t <= D->steps.front().tprev) {
-            std::memcpy(out + (size_t)q * n, D->steps.front().y0.data(), sizeof(double) * n);
-            continue;
-        }
-        while (s + 1 < D->steps.size() && D->steps[s].tprev + D->steps[s].dt < t) ++s;
-        const Step& S = D->steps[s];
-        double tend = S.tprev + S.dt;
-        if (t == tend) {
-            std::memcpy(out + (size_t)q * n, S.y1.data(), sizeof(double) * n);
-            continue;
-        }
-        double th = (t - S.tprev) / S.dt;
+        const double t = tq[q];
+        size_t ip = 1;
+        while (ip < ns && ts(ip) < t) ++ip;
+        if (ip > ns - 1) ip = ns - 1;
+        const size_t im = ip - 1;
+        const Step& S = D->steps[ip - 1];
+        const double dt = ts(ip) - ts(im);
+        const double th = dt == 0.0 ? 1.0 : (t - ts(im)) / dt;
+        double* o = out + (size_t)q * n;
         switch (D->alg) {
-        case ORC_TSIT5: tsit5_interp(th, S.dt, S.y0.data(), S.k.data(), n, out + (size_t)q * n); break;
-        case ORC_VERN7: vern7_interp(th, S.dt, S.y0.data(), S.k.data(), n, out + (size_t)q * n); break;
-        case ORC_RODAS5P: rodas_interp(th, S.y0.data(), S.y1.data(), S.k.data(), n, out + (size_t)q * n); break;
+        case ORC_TSIT5: tsit5_interp(th, dt, S.y0.data(), S.k.data(), n, o); break;
+        case ORC_VERN7:
+            K.assign((size_t)16 * n, 0.0);
+            std::copy(S.k.begin(), S.k.end(), K.begin());
+            vern7_extra(D->model, n, D->p.data(), ts(im), dt, S.y0.data(), K.data());
+            vern7_interp(th, dt, S.y0.data(), K.data(), n, o);
+            break;
+        case ORC_RODAS5P: rodas_interp(th, S.y0.data(), S.y1.data(), S.k.data(), n, o); break;
+        case ORC_ROSENBROCK23: ros23_interp(th, dt, S.y0.data(), S.k.data(), n, o); break;
         default:
-            for (int i = 0; i < n; ++i) out[(size_t)q * n + i] = (1.0 - th) * S.y0[i] + th * S.y1[i];
+            for (int i = 0; i < n; ++i) o[i] = (1.0 - th) * S.y0[i] + th * S.y1[i];
         }
     }
     return 0;
+}
+
+// Step s of a dense record: tprev and tend, y0, y1 (n each) and the stored
+// interpolation vectors in the library's order (Tsit5 k1..k7, Vern7 k1 and
+// k4..k9, Rodas5P dense k1..k3; q-major, n each).  Returns the vector count.
+int orc_dense_step(void* h, int s, double* t2, double* y0, double* y1, double* k) {
+    Dense* D = (Dense*)h;
+    if (s < 0 || (size_t)s >= D->steps.size()) return -1;
+    const Step& S = D->steps[s];
+    const int n = D->n;
+    t2[0] = S.tprev;
+    t2[1] = S.tend;
+    std::copy(S.y0.begin(), S.y0.end(), y0);
+    std::copy(S.y1.begin(), S.y1.end(), y1);
+    static const int vern7_stage[7] = {1, 4, 5, 6, 7, 8, 9};
+    const int nk = D->alg == ORC_VERN7 ? 7 : (int)(S.k.size() / (size_t)n);
+    for (int q = 0; q < nk; ++q) {
+        const int src = D->alg == ORC_VERN7 ? vern7_stage[q] - 1 : q;
+        std::copy(S.k.begin() + (size_t)src * n, S.k.begin() + (size_t)(src + 1) * n, k + (size_t)q * n);
+    }
+    return nk;
 }
 
 void orc_dense_free(void* h) { delete (Dense*)h; }

@@ -19,7 +19,7 @@
 extern "C" {
 #endif
 
-enum { ORC_TSIT5 = 0, ORC_VERN7 = 1, ORC_RODAS5P = 2, ORC_VERN9 = 3 };
+enum { ORC_TSIT5 = 0, ORC_VERN7 = 1, ORC_RODAS5P = 2, ORC_VERN9 = 3, ORC_ROSENBROCK23 = 4 };
 enum { ORC_LINEAR = 0, ORC_LORENZ = 1, ORC_ROBERTSON = 2, ORC_DUFFING = 3, ORC_BRUSSELATOR = 4 };
 /* SciMLBase ReturnCode subset used by this path (numbering of the C ABI). */
 enum { ORC_RC_DEFAULT = 0, ORC_RC_SUCCESS = 1, ORC_RC_MAXITERS = 2, ORC_RC_DTNAN = 3,
@@ -59,8 +59,12 @@ int orc_solve(int alg, int model, int n, const double* p, double t0, double tf,
               const double* tstops, int ntstops, double* t_out, double* u_out, int cap,
               int32_t* retcode, orc_stats* st, void** dense_handle);
 
-/* Evaluate the stored dense solution at nq times (out: nq*n). */
+/* Evaluate the stored dense solution at nq times (out: nq*n), as the
+ * reference's sol(t) does (ode_interpolation on the every-step saves). */
 int orc_dense_eval(void* dense_handle, const double* tq, int nq, double* out);
+/* Step s: t2 = (tprev, tend), y0, y1 (n each), k (returned count x n): the
+ * interpolation vectors in the library's dense order. */
+int orc_dense_step(void* dense_handle, int s, double* t2, double* y0, double* y1, double* k);
 void orc_dense_free(void* dense_handle);
 int orc_dense_nsteps(void* dense_handle);
 

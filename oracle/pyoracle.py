@@ -13,7 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 
-TSIT5, VERN7, RODAS5P, VERN9 = 0, 1, 2, 3
+TSIT5, VERN7, RODAS5P, VERN9, ROSENBROCK23 = 0, 1, 2, 3, 4
 LINEAR, LORENZ, ROBERTSON, DUFFING, BRUSSELATOR = 0, 1, 2, 3, 4
 RC_DEFAULT, RC_SUCCESS, RC_MAXITERS, RC_DTNAN, RC_DTLESSTHANMIN, RC_UNSTABLE = range(6)
 
@@ -57,6 +57,8 @@ def lib():
         L.orc_dense_eval.argtypes = [C.c_void_p, dp, C.c_int, dp]
         L.orc_dense_free.argtypes = [C.c_void_p]
         L.orc_dense_nsteps.argtypes = [C.c_void_p]
+        L.orc_dense_step.restype = C.c_int
+        L.orc_dense_step.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, dp]
         L.orc_solve_ensemble.restype = C.c_int
         L.orc_solve_ensemble.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int32), C.c_int,
                                          C.c_int64, dp, dp, dp, C.POINTER(Opts), dp, C.c_int, C.c_int,
@@ -126,6 +128,15 @@ class DenseSolution:
     @property
     def nsteps(self):
         return lib().orc_dense_nsteps(self.h)
+
+    def step(self, s):
+        """(tprev, tend, y0, y1, k) of step s; k (nk, n) in the library's dense order."""
+        t2, y0, y1 = np.zeros(2), np.zeros(self.n), np.zeros(self.n)
+        k = np.zeros((16, self.n))
+        nk = lib().orc_dense_step(self.h, s, _dp(t2), _dp(y0), _dp(y1), _dp(k))
+        if nk < 0:
+            raise IndexError(s)
+        return t2[0], t2[1], y0, y1, k[:nk].copy()
 
     def __del__(self):
         try:

@@ -73,6 +73,12 @@ struct Tsit5Alg {
     }
     template <class R, int C> __device__ static void after_save(Cache<R, C>&) {}
 
+    // Dense output (dense = true): the step's k1..k7, the reference's integrator.k
+    // for Tsit5 (tsit_perform_step.jl:293-307).
+    static constexpr int NDENSE = 7;
+    template <class R, int C> __device__ static void prepare_dense(Cache<R, C>&) {}
+    template <class R, int C> __device__ static R* dense_slot(Cache<R, C>& c, int q) { return c.k[q]; }
+
     template <class Model, class R, int L, int C>
     __device__ static typename Ctl<R>::T step(Cache<R, C>& c, R* u, R* ulo, const R* up, const R* uplo,
                                              const R* p, double t, double dt, R abstol, R reltol, long long, bool,
@@ -150,6 +156,16 @@ struct Vern7Alg {
     }
     template <class R, int C> __device__ static void on_accept(Cache<R, C>&) {}
     template <class R, int C> __device__ static void after_save(Cache<R, C>& c) { c.extra = false; }
+
+    // Dense output: k1, k4..k9, the stages that the interpolant and the lazy extra
+    // stages read (interpolants.jl:183-252, verner_addsteps.jl:137-193); of the
+    // reference's integrator.k[1..10], k2, k3 and k10 are read by neither.
+    static constexpr int NDENSE = 7;
+    __host__ __device__ static constexpr int dense_stage(int q) { return q == 0 ? 1 : q + 3; }
+    template <class R, int C> __device__ static void prepare_dense(Cache<R, C>&) {}
+    template <class R, int C> __device__ static R* dense_slot(Cache<R, C>& c, int q) {
+        return c.s[Vern7Tab::slot(dense_stage(q))];
+    }
 
     template <int ROW, class Model, class R, int L, int C>
     __device__ static void eval_stage(Cache<R, C>& c, const R* up, const R* uplo, const R* p, double tstage, R d,

@@ -10,6 +10,9 @@ read from the reference's Julia sources rather than retyped:
   :648-716 (``Vern7ExtraStages``), :880-972 (``Vern7InterpolationCoefficients``).
 * Rodas5P: lib/OrdinaryDiffEqRosenbrock/src/rosenbrock_tableaus.jl:23-72
   (``RODAS5PA/C/c/d/H`` and ``Rodas5PTableau``).
+* Rosenbrock23: rosenbrock_tableaus.jl:6-10 (``c32 = 6 + sqrt(2)``,
+  ``d = 1 / (2 + sqrt(2))``): expressions, evaluated here in IEEE double with
+  the same correctly rounded operations Julia's Float64 arithmetic performs.
 
 Each Julia literal is copied verbatim as a C++ double literal, so the C++ parser
 rounds it to the same IEEE double as Julia's parser does.  Run once in a
@@ -84,6 +87,7 @@ def main():
         "// Tsit5: lib/OrdinaryDiffEqTsit5/src/tsit_tableaus.jl:45-101,244-276",
         "// Vern7: lib/OrdinaryDiffEqVerner/src/verner_tableaus.jl:648-716,880-972,1129-1205",
         "// Rodas5P: lib/OrdinaryDiffEqRosenbrock/src/rosenbrock_tableaus.jl:23-72",
+        "// Rosenbrock23: lib/OrdinaryDiffEqRosenbrock/src/rosenbrock_tableaus.jl:6-10",
         "#pragma once",
         "#include <cuda_runtime.h>",
         "namespace odegb {",
@@ -210,6 +214,21 @@ def main():
     vi = dict(blocks[4][1])
     R7 = [[as_double(vi.get("r%02d%d" % (i, q), "0")) for q in range(8)] for i in range(17)]
     accessor("VERN7_R", R7)
+
+    # Rosenbrock23: the two expressions of Rosenbrock23Tableau, checked against the source
+    body = fold_block(ros, r"function Rosenbrock23Tableau\(::Type\{T\}\) where \{T\}")
+    if "convert(T, 6 + sqrt(2))" not in body or "convert(T, 1 / (2 + sqrt(2)))" not in body:
+        raise SystemExit("Rosenbrock23Tableau changed: " + body)
+    import math
+    c32 = 6.0 + math.sqrt(2.0)
+    dd = 1.0 / (2.0 + math.sqrt(2.0))
+    lines.append("// ROSENBROCK23: c32 = 6 + sqrt(2), d = 1 / (2 + sqrt(2)) in Float64")
+    for name, x in (("ROS23_C32", c32), ("ROS23_D", dd)):
+        hi = float(np.float32(x))
+        lo = float(np.float32(x - hi))
+        lines.append("constexpr double %s = %s;  // %r" % (name, x.hex(), x))
+        lines.append("constexpr float %s_HI = %sf;" % (name, hi.hex()))
+        lines.append("constexpr float %s_LO = %sf;" % (name, lo.hex()))
     lines.append("}  // namespace tab")
     lines.append("}  // namespace odegb")
     with open(out, "w") as fh:

@@ -271,6 +271,24 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
         nsaved++;
         last_saved_t = ts;
     };
+    // Dense output: the interpolation vectors of the step ending at the save about
+    // to be made (save_dense_at_t!, integrator_utils.jl:455-473), in the slot that
+    // save_point will use.  The start save has no step (zeros); a step save past the
+    // capacity overwrites the last slot, whose step no longer starts at the slot
+    // before it, so its vectors are NaN.
+    auto save_dense = [&](bool step) {
+        const bool over = nsaved >= a.nsave_cap;
+        const int slot = over ? a.nsave_cap - 1 : nsaved;
+        if (step) Alg::template prepare_dense<R, C>(cache);
+#pragma unroll
+        for (int q = 0; q < Alg::NDENSE; ++q) {
+            const R* kv = Alg::template dense_slot<R, C>(cache, q);
+#pragma unroll
+            for (int c = 0; c < C; ++c)
+                a.k_out[(((size_t)slot * Alg::NDENSE + q) * a.nmax + g.lane * C + c) * N + j] =
+                    !step ? 0.0 : over ? dnan() : (double)kv[c];
+        }
+    };
     auto saveat_at = [&](int s) -> double {
         return a.saveat_per_traj ? a.saveat[(size_t)s * N + j] : a.saveat[s];
     };
@@ -280,7 +298,10 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
 
 #pragma unroll
     for (int c = 0; c < C; ++c) { uprev[c] = u[c]; uprevlo[c] = ulo[c]; }
-    if (a.save_start) save_point(t0, u, ulo);
+    if (a.save_start) {
+        if (a.k_out) save_dense(false);
+        save_point(t0, u, ulo);
+    }
 
     double t = t0, tprev = t0;
     Alg::template initialize<Model, R, L, C>(cache, u, p, t, g, st, a, j);
@@ -399,8 +420,10 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             // save_everystep (_savevalues!, integrator_utils.jl:397-404): the accepted
             // step, unless it repeats the last save or is tf with save_end off
             if (a.save_everystep &&
-                (nsaved == 0 || ((!deq(t, last_saved_t) || abs_bits(dt) == 0) && (a.save_end || !deq(t, tf)))))
+                (nsaved == 0 || ((!deq(t, last_saved_t) || abs_bits(dt) == 0) && (a.save_end || !deq(t, tf))))) {
+                if (a.k_out) save_dense(true);
                 save_point(t, u, ulo);
+            }
             Alg::template after_save<R, C>(cache);
         } else {
             st.nreject++;
@@ -418,7 +441,10 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
                 for (int s = 0; s < a.nsave; ++s) in_saveat = in_saveat || (saveat_at(s) == t);
             need = last_saved_t != t && (a.save_end_user == 1 || in_saveat || t == tf || !a.saveat_given);
         }
-        if (need) save_point(t, u, ulo);
+        if (need) {
+            if (a.k_out) save_dense(st.naccept > 0);
+            save_point(t, u, ulo);
+        }
     }
     if (g.lane == 0) {
         a.nsaved[j] = nsaved < a.nsave_cap ? nsaved : a.nsave_cap;

@@ -1,0 +1,153 @@
+// Dense-output evaluation sol(t): the method's interpolant on the saved steps,
+// in FP64.
+//
+// Follows ode_interpolation(tval::Number, ...) (lib/OrdinaryDiffEqCore/src/dense/
+// generic_dense.jl:1094-1190) with left continuity: i+ is the first saved index
+// >= 2 (1-based) with ts[i+] >= t, clamped to the last index, i- = i+ - 1; dt =
+// ts[i+] - ts[i-]; theta = (t - ts[i-]) / dt (1 when dt is 0); then the
+// interpolant on (ts[i-], u[i-]) -> (ts[i+], u[i+]) with the vectors stored for
+// the step ending at i+ (ks[i+]).  Vern7's lazy extra stages are formed from
+// those vectors first, as _ode_addsteps! does (verner_addsteps.jl:137-193).
+// The interpolants themselves are the integrator's own (erk.cuh, rodas.cuh).
+#include "erk.cuh"
+#include "rodas.cuh"
+#include "ros23.cuh"
+#include "models.cuh"
+
+namespace odegb {
+
+static_assert(kDenseVectors[0] == Tsit5Alg::NDENSE && kDenseVectors[1] == Vern7Alg::NDENSE &&
+                  kDenseVectors[2] == Rodas5PAlg::NDENSE && kDenseVectors[3] == Rosenbrock23Alg::NDENSE,
+              "dense vector counts of the runtime and the kernels");
+
+struct Interval {
+    int im, ip;
+    double th, dt, tprev;
+};
+
+__device__ __forceinline__ Interval dense_locate(const DenseArgs& a, long long j, int ns, double t) {
+    const long long N = a.N;
+    int lo = 1, hi = ns;   // first s in [1, ns) with ts[s] >= t, else ns
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (a.ts[(size_t)mid * N + j] >= t) hi = mid;
+        else lo = mid + 1;
+    }
+    Interval v;
+    v.ip = lo < ns - 1 ? lo : ns - 1;
+    v.im = v.ip > 0 ? v.ip - 1 : v.ip;
+    v.tprev = a.ts[(size_t)v.im * N + j];
+    v.dt = a.ts[(size_t)v.ip * N + j] - v.tprev;
+    v.th = v.dt == 0.0 ? 1.0 : (t - v.tprev) / v.dt;
+    return v;
+}
+
+__device__ __forceinline__ double query_time(const DenseArgs& a, long long j, int r) {
+    return a.tq_per_traj ? a.tq[(size_t)r * a.N + j] : a.tq[r];
+}
+
+// Tsit5, Rodas5P and Rosenbrock23: componentwise interpolants, one thread per
+// (query, trajectory).
+template <int ALG>
+__global__ void dense_eval_pointwise(DenseArgs a) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= a.N * (long long)a.nq) return;
+    const long long N = a.N, j = idx % N;
+    const int r = (int)(idx / N), n = a.n;
+    const int ns = min(a.nsaved[j], a.cap);
+    if (ns <= 0) {
+        for (int i = 0; i < n; ++i) a.out[((size_t)r * n + i) * N + j] = dnan();
+        return;
+    }
+    const Interval v = dense_locate(a, j, ns, query_time(a, j, r));
+    constexpr int NK = kDenseVectors[ALG];
+    Group<1> g;
+    for (int i = 0; i < n; ++i) {
+        double y0 = a.us[((size_t)v.im * n + i) * N + j], y1 = a.us[((size_t)v.ip * n + i) * N + j];
+        double z = 0.0, o, olo;
+        const double* kp = a.ks + ((size_t)v.ip * NK * n + i) * N + j;
+        if constexpr (ALG == 0) {
+            Tsit5Alg::Cache<double, 1> c;
+#pragma unroll
+            for (int q = 0; q < NK; ++q) c.k[q][0] = kp[(size_t)q * n * N];
+            Tsit5Alg::interpolate<Linear, double, 1, 1>(c, &o, &olo, v.th, v.dt, v.tprev, &y0, &z, &y1, &z, nullptr,
+                                                        g);
+        } else if constexpr (ALG == 2) {
+            Rodas5PAlg::Cache<double, 1> c;
+#pragma unroll
+            for (int q = 0; q < NK; ++q) c.dk[q][0] = kp[(size_t)q * n * N];
+            Rodas5PAlg::interp_dense<double, 1>(c, &o, &olo, v.th, &y0, &z, &y1, &z);
+        } else {
+            Rosenbrock23Alg::Cache<double, 1> c;
+#pragma unroll
+            for (int q = 0; q < NK; ++q) c.k[q][0] = kp[(size_t)q * n * N];
+            Rosenbrock23Alg::interpolate<Linear, double, 1, 1>(c, &o, &olo, v.th, v.dt, v.tprev, &y0, &z, &y1, &z,
+                                                               nullptr, g);
+        }
+        a.out[((size_t)r * n + i) * N + j] = o;
+    }
+}
+
+// Vern7: the extra stages need the right-hand side, so one lane group (the
+// integrator's layout) per (query, trajectory).
+template <class Model, int L, int C>
+__global__ void dense_eval_vern7(DenseArgs a) {
+    Group<L> g;
+    const long long gid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / L;
+    if (gid >= a.N * (long long)a.nq) return;
+    const long long N = a.N, j = gid % N;
+    const int r = (int)(gid / N), n = a.n;
+    const int ns = min(a.nsaved[j], a.cap);
+    double out[C], outlo[C];
+    if (ns <= 0) {
+#pragma unroll
+        for (int c = 0; c < C; ++c) a.out[((size_t)r * n + g.lane * C + c) * N + j] = dnan();
+        return;
+    }
+    const Interval v = dense_locate(a, j, ns, query_time(a, j, r));
+    double p[Model::NP];
+#pragma unroll
+    for (int k = 0; k < Model::NP; ++k) p[k] = a.p[(size_t)k * N + j];
+    double y0[C], y1[C], z[C];
+    Vern7Alg::Cache<double, C> cache;
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        const int i = g.lane * C + c;
+        y0[c] = a.us[((size_t)v.im * n + i) * N + j];
+        y1[c] = a.us[((size_t)v.ip * n + i) * N + j];
+        z[c] = 0.0;
+#pragma unroll
+        for (int q = 0; q < Vern7Alg::NDENSE; ++q)
+            Vern7Alg::dense_slot<double, C>(cache, q)[c] =
+                a.ks[(((size_t)v.ip * Vern7Alg::NDENSE + q) * n + i) * N + j];
+    }
+    cache.extra = false;
+    Vern7Alg::interpolate<Model, double, L, C>(cache, out, outlo, v.th, v.dt, v.tprev, y0, z, y1, z, p, g);
+#pragma unroll
+    for (int c = 0; c < C; ++c) a.out[((size_t)r * n + g.lane * C + c) * N + j] = out[c];
+}
+
+#define PW(ALG, NAME)                                                                                  \
+    {ALG, -1, -1, 1,                                                                                   \
+     [](const DenseArgs& a, int g, int b, cudaStream_t st) { dense_eval_pointwise<ALG><<<g, b, 0, st>>>(a); }, \
+     "dense/" NAME}
+#define V7(MODEL, MID, L, C)                                                                           \
+    {1, MID, (L) * (C), L,                                                                             \
+     [](const DenseArgs& a, int g, int b, cudaStream_t st) { dense_eval_vern7<MODEL, L, C><<<g, b, 0, st>>>(a); }, \
+     "dense/vern7/" #MODEL "/L" #L "C" #C}
+
+// Vern7 shapes: the FP64 integrator's (kernels_vern7.cu).
+static const DenseVariant kDense[] = {
+    PW(0, "tsit5"), PW(2, "rodas5p"), PW(3, "rosenbrock23"),
+    V7(Linear, M_LINEAR, 1, 1), V7(Linear, M_LINEAR, 1, 2), V7(Linear, M_LINEAR, 1, 8),
+    V7(Lorenz, M_LORENZ, 1, 3),
+    V7(Duffing, M_DUFFING, 1, 4), V7(Duffing, M_DUFFING, 1, 8), V7(Duffing, M_DUFFING, 2, 4),
+    V7(Duffing, M_DUFFING, 4, 4), V7(Duffing, M_DUFFING, 8, 4), V7(Duffing, M_DUFFING, 16, 4),
+};
+
+const DenseVariant* dense_variants(int* count) {
+    *count = (int)(sizeof(kDense) / sizeof(kDense[0]));
+    return kDense;
+}
+
+}  // namespace odegb

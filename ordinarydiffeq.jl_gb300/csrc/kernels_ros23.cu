@@ -1,0 +1,26 @@
+// Rosenbrock23 kernel variants with W in registers (one lane per trajectory).
+#include "ros23.cuh"
+#include "models.cuh"
+
+namespace odegb {
+
+#define VAR(MODEL, MID, R, PREC, L, C)                                                              \
+    {3, MID, PREC, (L) * (C), L, 0, (const void*)ensemble_kernel<Rosenbrock23Alg, MODEL, R, L, C>,   \
+     [](const EnsembleArgs& a, int g, int b, size_t s, cudaStream_t st) {                           \
+         launch_kernel(ensemble_kernel<Rosenbrock23Alg, MODEL, R, L, C>, a, g, b, s, st);            \
+     },                                                                                             \
+     "rosenbrock23/" #MODEL "/" #R "/L" #L "C" #C}
+#define BOTH(MODEL, MID, L, C) VAR(MODEL, MID, double, 0, L, C), VAR(MODEL, MID, float, 1, L, C)
+
+static const KernelVariant kVariants[] = {
+    BOTH(Linear, M_LINEAR, 1, 1), BOTH(Linear, M_LINEAR, 1, 2),
+    BOTH(Lorenz, M_LORENZ, 1, 3), BOTH(Robertson, M_ROBERTSON, 1, 3),
+    BOTH(Duffing, M_DUFFING, 1, 4),
+};
+
+const KernelVariant* ros23_variants(int* count) {
+    *count = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
+    return kVariants;
+}
+
+}  // namespace odegb

@@ -43,6 +43,10 @@ const std::vector<KernelVariant>& all_variants() {
         out.insert(out.end(), t, t + n);
         t = rodas_group_variants(&n);
         out.insert(out.end(), t, t + n);
+        t = ros23_variants(&n);
+        out.insert(out.end(), t, t + n);
+        t = ros23_group_variants(&n);
+        out.insert(out.end(), t, t + n);
         return out;
     }();
     return v;
@@ -55,10 +59,12 @@ int model_nparams(int model) { return model == ODE_MODEL_LINEAR ? 1 : 3; }
 // stage set stays in registers without spilling, mixed Vern7 2 (a smaller
 // per-lane step: 1.2-1.5x faster measured); Rodas5P above 8 states one lane
 // per 2 states (W in shared memory, rows spread over the group).
+bool is_rosenbrock(int alg) { return alg == ODE_RODAS5P || alg == ODE_ROSENBROCK23; }
+
 int default_lanes(int alg, int n, int prec) {
     if (alg == ODE_VERN7 && prec == ODE_PREC_MIXED && n >= 4 && n % 2 == 0) return std::min(32, n / 2);
-    if (n <= 4 || (n <= 8 && alg == ODE_RODAS5P)) return 1;
-    if (alg == ODE_RODAS5P) return std::min(32, n / 2);
+    if (n <= 4 || (n <= 8 && is_rosenbrock(alg))) return 1;
+    if (is_rosenbrock(alg)) return std::min(32, n / 2);
     return std::min(32, n / 4);
 }
 
@@ -110,6 +116,7 @@ struct ode_handle {
     Ctx main;
     // staging for the synchronous host API
     DevBuf b_u0, b_p, b_tspan, b_saveat, b_t, b_u, b_ns, b_rc, b_st, b_npt;
+    DevBuf b_k, b_tq, b_out;                 // dense output and its evaluation
     // copy streams and events of the chunked host-API pipeline
     cudaStream_t copy_in = nullptr, copy_out = nullptr;
     cudaEvent_t pipe_in[4] = {}, pipe_done[4] = {};
@@ -169,7 +176,7 @@ int grow(ode_handle* h, DevBuf& b, size_t bytes) {
 int validate(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int64_t N) {
     if (!h || !d || !o) return fail(h, ODE_E_INVALID, "null handle, problem or options");
     if (N < 0) return fail(h, ODE_E_INVALID, "negative trajectory count");
-    if (d->alg_id < ODE_TSIT5 || d->alg_id > ODE_RODAS5P) return fail(h, ODE_E_INVALID, "unknown alg_id");
+    if (d->alg_id < ODE_TSIT5 || d->alg_id >= kNumAlgs) return fail(h, ODE_E_INVALID, "unknown alg_id");
     if (d->model_id < ODE_MODEL_LINEAR || d->model_id > ODE_MODEL_BRUSSELATOR_1D)
         return fail(h, ODE_E_INVALID, "unknown model_id");
     if (d->precision != ODE_PREC_FP64 && d->precision != ODE_PREC_MIXED)
@@ -517,8 +524,10 @@ int run_per_class(ode_handle* h, Ctx& c, const ode_problem_desc* d, const ode_op
 int run_ensemble(ode_handle* h, Ctx& c, const ode_problem_desc* d, const ode_options* o, int64_t N,
                  const int32_t* npt_dev, const double* u0, const double* p, const double* tspan,
                  const double* saveat, double* t_out, double* u_out, int32_t* nsaved, int32_t* retcode,
-                 OdeStatsDev* stats, cudaStream_t s, bool graph = false, int64_t stride = 0, bool timing = true) {
+                 OdeStatsDev* stats, cudaStream_t s, bool graph = false, int64_t stride = 0, bool timing = true,
+                 double* k_out = nullptr) {
     EnsembleArgs a = make_args(h, d, o, N, u0, p, tspan, saveat, t_out, u_out, nsaved, retcode, stats);
+    a.k_out = k_out;
     if (stride > 0) a.N = stride;   // a slice of a larger ensemble: N trajectories, arrays of row length stride
     if (N == 0) return ODE_OK;
     Plan pl;
@@ -703,6 +712,92 @@ int check_sizes(ode_handle* h, const ode_problem_desc* d, const int32_t* npt, in
                           (long long)j, n);
             return fail(h, ODE_E_INVALID, buf);
         }
+    }
+    return ODE_OK;
+}
+
+// Evaluation kernel for a dense solve: the model-free one for Tsit5 and
+// Rodas5P, the model's Vern7 one at the FP64 integrator's lane layout.
+const DenseVariant* find_dense(int alg, int model, int n) {
+    int cnt = 0;
+    const DenseVariant* all = dense_variants(&cnt);
+    const DenseVariant* best = nullptr;
+    for (int k = 0; k < cnt; ++k) {
+        const DenseVariant& v = all[k];
+        if (v.alg != alg) continue;
+        if (v.model < 0) return &v;
+        if (v.model != model || v.n != n) continue;
+        if (!best || v.lanes == default_lanes(alg, n, ODE_PREC_FP64)) best = &v;
+    }
+    return best;
+}
+
+// Synchronous solve on host buffers (validated by the caller); k_out: dense
+// output or nullptr.
+int solve_host(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int64_t N, const int32_t* npt,
+               const double* u0, const double* p, const double* tspan, const double* saveat, double* t_out,
+               double* u_out, double* k_out, int32_t* nsaved, int32_t* retcode, ode_stats* stats) {
+    int rc = ODE_OK;
+    std::lock_guard<std::mutex> lk(h->api_mu);
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    *h->h_abort = 0;
+    if (N > 0) {   // every buffer page-locked: the kernels work in place, no staging copies
+        const double *mu0 = mapped_ptr(u0), *mp = mapped_ptr(p), *mts = mapped_ptr(tspan);
+        const double* msv = o->nsave > 0 ? mapped_ptr(saveat) : nullptr;
+        const int32_t* mnpt = npt ? mapped_ptr(npt) : nullptr;
+        double *mt = t_out ? mapped_ptr(t_out) : nullptr, *mu = mapped_ptr(u_out);
+        int32_t *mns = mapped_ptr(nsaved), *mrc = mapped_ptr(retcode);
+        ode_stats* mst = stats ? mapped_ptr(stats) : nullptr;
+        double* mk = k_out ? mapped_ptr(k_out) : nullptr;
+        if (mu0 && mp && mts && mu && mns && mrc && (o->nsave == 0 || msv) && (!npt || mnpt) && (!t_out || mt) &&
+            (!stats || mst) && (!k_out || mk)) {
+            cudaStream_t s = h->main.stream;
+            rc = run_ensemble(h, h->main, d, o, N, mnpt, mu0, mp, mts, msv, mt, mu, mns, mrc, (OdeStatsDev*)mst, s,
+                              /*graph=*/true, 0, true, mk);
+            cudaError_t e = cudaStreamSynchronize(s);
+            if (rc) return rc;
+            if (e != cudaSuccess) return fail(h, ODE_E_CUDA, std::string("solve: ") + cudaGetErrorString(e));
+            float ms = 0;
+            if (cudaEventElapsedTime(&ms, h->main.ev0, h->main.ev1) == cudaSuccess) h->last_ms = ms;
+            return ODE_OK;
+        }
+    }
+    const size_t n = (size_t)d->n_states, np = (size_t)d->n_params, cap = save_cap(o);
+    const size_t nsv = (size_t)o->nsave * (o->saveat_per_traj ? (size_t)N : 1);
+    if ((rc = grow(h, h->b_u0, n * N * 8)) || (rc = grow(h, h->b_p, np * N * 8)) ||
+        (rc = grow(h, h->b_tspan, 2 * N * 8)) || (rc = grow(h, h->b_saveat, nsv * 8)) ||
+        (rc = grow(h, h->b_t, cap * N * 8)) || (rc = grow(h, h->b_u, cap * n * N * 8)) ||
+        (rc = grow(h, h->b_ns, N * 4)) || (rc = grow(h, h->b_rc, N * 4)) ||
+        (rc = grow(h, h->b_st, N * sizeof(ode_stats))) || (npt && (rc = grow(h, h->b_npt, N * 4))))
+        return rc;
+    const size_t kbytes = k_out ? cap * (size_t)kDenseVectors[d->alg_id] * n * N * 8 : 0;
+    if (k_out && (rc = grow(h, h->b_k, kbytes))) return rc;
+    cudaStream_t s = h->main.stream;
+    if (!k_out && N >= kPipeMin && (cap * (n + 1) + n + np + 2) * 8 >= kPipeMinBytesPerTraj)
+        return solve_chunked(h, d, o, N, npt, u0, p, tspan, saveat, t_out, u_out, nsaved, retcode, stats);
+    CUDA_TRY(h, cudaMemcpyAsync(h->b_u0.p, u0, n * N * 8, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(h, cudaMemcpyAsync(h->b_p.p, p, np * N * 8, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(h, cudaMemcpyAsync(h->b_tspan.p, tspan, 2 * N * 8, cudaMemcpyHostToDevice, s));
+    if (nsv) CUDA_TRY(h, cudaMemcpyAsync(h->b_saveat.p, saveat, nsv * 8, cudaMemcpyHostToDevice, s));
+    if (npt) CUDA_TRY(h, cudaMemcpyAsync(h->b_npt.p, npt, N * 4, cudaMemcpyHostToDevice, s));
+    rc = run_ensemble(h, h->main, d, o, N, npt ? (const int32_t*)h->b_npt.p : nullptr, (const double*)h->b_u0.p,
+                      (const double*)h->b_p.p, (const double*)h->b_tspan.p, (const double*)h->b_saveat.p,
+                      (double*)h->b_t.p, (double*)h->b_u.p, (int32_t*)h->b_ns.p, (int32_t*)h->b_rc.p,
+                      (OdeStatsDev*)h->b_st.p, s, /*graph=*/true, 0, true, k_out ? (double*)h->b_k.p : nullptr);
+    if (rc) {
+        cudaStreamSynchronize(s);
+        return rc;
+    }
+    if (t_out) CUDA_TRY(h, cudaMemcpyAsync(t_out, h->b_t.p, cap * N * 8, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(h, cudaMemcpyAsync(u_out, h->b_u.p, cap * n * N * 8, cudaMemcpyDeviceToHost, s));
+    if (k_out) CUDA_TRY(h, cudaMemcpyAsync(k_out, h->b_k.p, kbytes, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(h, cudaMemcpyAsync(nsaved, h->b_ns.p, N * 4, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(h, cudaMemcpyAsync(retcode, h->b_rc.p, N * 4, cudaMemcpyDeviceToHost, s));
+    if (stats) CUDA_TRY(h, cudaMemcpyAsync(stats, h->b_st.p, N * sizeof(ode_stats), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(h, cudaStreamSynchronize(s));
+    if (N > 0) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, h->main.ev0, h->main.ev1) == cudaSuccess) h->last_ms = ms;
     }
     return ODE_OK;
 }
@@ -1038,63 +1133,88 @@ int ode_solve_ensemble(ode_handle* h, const ode_problem_desc* d, const ode_optio
         return fail(h, ODE_E_INVALID, "null input or output buffer");
     if (o->nsave > 0 && !saveat) return fail(h, ODE_E_INVALID, "nsave > 0 but saveat is null");
     if ((rc = check_sizes(h, d, npt, N))) return rc;
+    return solve_host(h, d, o, N, npt, u0, p, tspan, saveat, t_out, u_out, nullptr, nsaved, retcode, stats);
+}
+
+int ode_dense_nk(int alg) {
+    return alg >= ODE_TSIT5 && alg < kNumAlgs ? kDenseVectors[alg] : ODE_E_INVALID;
+}
+
+int ode_solve_ensemble_dense(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int64_t N,
+                             const double* u0, const double* p, const double* tspan, double* t_out,
+                             double* u_out, double* k_out, int32_t* nsaved, int32_t* retcode, ode_stats* stats) {
+    int rc = validate(h, d, o, N);
+    if (rc) return rc;
+    if (!o->save_everystep || o->nsave != 0)
+        return fail(h, ODE_E_INVALID, "dense output saves every step: save_everystep = 1 and nsave = 0");
+    if (N > 0 && (!u0 || !p || !tspan || !u_out || !k_out || !nsaved || !retcode))
+        return fail(h, ODE_E_INVALID, "null input or output buffer");
+    return solve_host(h, d, o, N, nullptr, u0, p, tspan, nullptr, t_out, u_out, k_out, nsaved, retcode, stats);
+}
+
+int ode_dense_eval(ode_handle* h, const ode_problem_desc* d, int64_t N, const double* p, const double* t_saved,
+                   const double* u_saved, const double* k_saved, const int32_t* nsaved, int32_t cap, int32_t nq,
+                   const double* tq, int32_t tq_per_traj, double* out) {
+    if (!h || !d) return fail(h, ODE_E_INVALID, "null handle or problem");
+    ode_options o;
+    ode_options_default(&o);
+    int rc = validate(h, d, &o, N);
+    if (rc) return rc;
+    if (cap < 1 || nq < 0) return fail(h, ODE_E_INVALID, "cap must be >= 1 and nq >= 0");
+    if (N == 0 || nq == 0) return ODE_OK;
+    if (!p || !t_saved || !u_saved || !k_saved || !nsaved || !tq || !out)
+        return fail(h, ODE_E_INVALID, "null input or output buffer");
+    for (int64_t j = 0; j < N; ++j)
+        if (nsaved[j] < 0 || nsaved[j] > cap) return fail(h, ODE_E_INVALID, "nsaved outside [0, cap]");
+    const DenseVariant* v = find_dense(d->alg_id, d->model_id, d->n_states);
+    if (!v) {
+        char buf[128];
+        std::snprintf(buf, sizeof buf, "no dense evaluation kernel for alg %d model %d n %d", d->alg_id,
+                      d->model_id, d->n_states);
+        return fail(h, ODE_E_UNSUPPORTED, buf);
+    }
+    const size_t n = (size_t)d->n_states, np = (size_t)d->n_params, nk = (size_t)kDenseVectors[d->alg_id];
+    const size_t ntq = (size_t)nq * (tq_per_traj ? (size_t)N : 1);
     std::lock_guard<std::mutex> lk(h->api_mu);
     CUDA_TRY(h, cudaSetDevice(h->device));
-    *h->h_abort = 0;
-    if (N > 0) {   // every buffer page-locked: the kernels work in place, no staging copies
-        const double *mu0 = mapped_ptr(u0), *mp = mapped_ptr(p), *mts = mapped_ptr(tspan);
-        const double* msv = o->nsave > 0 ? mapped_ptr(saveat) : nullptr;
-        const int32_t* mnpt = npt ? mapped_ptr(npt) : nullptr;
-        double *mt = t_out ? mapped_ptr(t_out) : nullptr, *mu = mapped_ptr(u_out);
-        int32_t *mns = mapped_ptr(nsaved), *mrc = mapped_ptr(retcode);
-        ode_stats* mst = stats ? mapped_ptr(stats) : nullptr;
-        if (mu0 && mp && mts && mu && mns && mrc && (o->nsave == 0 || msv) && (!npt || mnpt) && (!t_out || mt) &&
-            (!stats || mst)) {
-            cudaStream_t s = h->main.stream;
-            rc = run_ensemble(h, h->main, d, o, N, mnpt, mu0, mp, mts, msv, mt, mu, mns, mrc, (OdeStatsDev*)mst, s,
-                              /*graph=*/true);
-            cudaError_t e = cudaStreamSynchronize(s);
-            if (rc) return rc;
-            if (e != cudaSuccess) return fail(h, ODE_E_CUDA, std::string("solve: ") + cudaGetErrorString(e));
-            float ms = 0;
-            if (cudaEventElapsedTime(&ms, h->main.ev0, h->main.ev1) == cudaSuccess) h->last_ms = ms;
-            return ODE_OK;
-        }
-    }
-    const size_t n = (size_t)d->n_states, np = (size_t)d->n_params, cap = save_cap(o);
-    const size_t nsv = (size_t)o->nsave * (o->saveat_per_traj ? (size_t)N : 1);
-    if ((rc = grow(h, h->b_u0, n * N * 8)) || (rc = grow(h, h->b_p, np * N * 8)) ||
-        (rc = grow(h, h->b_tspan, 2 * N * 8)) || (rc = grow(h, h->b_saveat, nsv * 8)) ||
-        (rc = grow(h, h->b_t, cap * N * 8)) || (rc = grow(h, h->b_u, cap * n * N * 8)) ||
-        (rc = grow(h, h->b_ns, N * 4)) || (rc = grow(h, h->b_rc, N * 4)) ||
-        (rc = grow(h, h->b_st, N * sizeof(ode_stats))) || (npt && (rc = grow(h, h->b_npt, N * 4))))
+    if ((rc = grow(h, h->b_p, np * N * 8)) || (rc = grow(h, h->b_t, (size_t)cap * N * 8)) ||
+        (rc = grow(h, h->b_u, (size_t)cap * n * N * 8)) || (rc = grow(h, h->b_k, (size_t)cap * nk * n * N * 8)) ||
+        (rc = grow(h, h->b_ns, N * 4)) || (rc = grow(h, h->b_tq, ntq * 8)) ||
+        (rc = grow(h, h->b_out, (size_t)nq * n * N * 8)))
         return rc;
     cudaStream_t s = h->main.stream;
-    if (N >= kPipeMin && (cap * (n + 1) + n + np + 2) * 8 >= kPipeMinBytesPerTraj)
-        return solve_chunked(h, d, o, N, npt, u0, p, tspan, saveat, t_out, u_out, nsaved, retcode, stats);
-    CUDA_TRY(h, cudaMemcpyAsync(h->b_u0.p, u0, n * N * 8, cudaMemcpyHostToDevice, s));
     CUDA_TRY(h, cudaMemcpyAsync(h->b_p.p, p, np * N * 8, cudaMemcpyHostToDevice, s));
-    CUDA_TRY(h, cudaMemcpyAsync(h->b_tspan.p, tspan, 2 * N * 8, cudaMemcpyHostToDevice, s));
-    if (nsv) CUDA_TRY(h, cudaMemcpyAsync(h->b_saveat.p, saveat, nsv * 8, cudaMemcpyHostToDevice, s));
-    if (npt) CUDA_TRY(h, cudaMemcpyAsync(h->b_npt.p, npt, N * 4, cudaMemcpyHostToDevice, s));
-    rc = run_ensemble(h, h->main, d, o, N, npt ? (const int32_t*)h->b_npt.p : nullptr, (const double*)h->b_u0.p,
-                      (const double*)h->b_p.p, (const double*)h->b_tspan.p, (const double*)h->b_saveat.p,
-                      (double*)h->b_t.p, (double*)h->b_u.p, (int32_t*)h->b_ns.p, (int32_t*)h->b_rc.p,
-                      (OdeStatsDev*)h->b_st.p, s, /*graph=*/true);
-    if (rc) {
-        cudaStreamSynchronize(s);
-        return rc;
-    }
-    if (t_out) CUDA_TRY(h, cudaMemcpyAsync(t_out, h->b_t.p, cap * N * 8, cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(h, cudaMemcpyAsync(u_out, h->b_u.p, cap * n * N * 8, cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(h, cudaMemcpyAsync(nsaved, h->b_ns.p, N * 4, cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(h, cudaMemcpyAsync(retcode, h->b_rc.p, N * 4, cudaMemcpyDeviceToHost, s));
-    if (stats) CUDA_TRY(h, cudaMemcpyAsync(stats, h->b_st.p, N * sizeof(ode_stats), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(h, cudaMemcpyAsync(h->b_t.p, t_saved, (size_t)cap * N * 8, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(h, cudaMemcpyAsync(h->b_u.p, u_saved, (size_t)cap * n * N * 8, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(h, cudaMemcpyAsync(h->b_k.p, k_saved, (size_t)cap * nk * n * N * 8, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(h, cudaMemcpyAsync(h->b_ns.p, nsaved, N * 4, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(h, cudaMemcpyAsync(h->b_tq.p, tq, ntq * 8, cudaMemcpyHostToDevice, s));
+    DenseArgs a;
+    a.N = N;
+    a.n = d->n_states;
+    a.nq = nq;
+    a.tq_per_traj = tq_per_traj ? 1 : 0;
+    a.cap = cap;
+    a.p = (const double*)h->b_p.p;
+    a.ts = (const double*)h->b_t.p;
+    a.us = (const double*)h->b_u.p;
+    a.ks = (const double*)h->b_k.p;
+    a.nsaved = (const int32_t*)h->b_ns.p;
+    a.tq = (const double*)h->b_tq.p;
+    a.out = (double*)h->b_out.p;
+    const int block = 128;
+    const long long threads = (long long)N * nq * v->lanes;
+    const long long grid = (threads + block - 1) / block;
+    if (grid > 0x7fffffffLL) return fail(h, ODE_E_INVALID, "too many (trajectory, query) pairs for one launch");
+    CUDA_TRY(h, cudaEventRecord(h->main.ev0, s));
+    v->launch(a, (int)grid, block, s);
+    CUDA_TRY(h, cudaGetLastError());
+    h->launches++;
+    CUDA_TRY(h, cudaEventRecord(h->main.ev1, s));
+    CUDA_TRY(h, cudaMemcpyAsync(out, h->b_out.p, (size_t)nq * n * N * 8, cudaMemcpyDeviceToHost, s));
     CUDA_TRY(h, cudaStreamSynchronize(s));
-    if (N > 0) {
-        float ms = 0;
-        if (cudaEventElapsedTime(&ms, h->main.ev0, h->main.ev1) == cudaSuccess) h->last_ms = ms;
-    }
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, h->main.ev0, h->main.ev1) == cudaSuccess) h->last_ms = ms;
     return ODE_OK;
 }
 
@@ -1404,7 +1524,7 @@ extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_o
                       (long long)N, (long long)kNoAllocMaxTraj);
         return fail(nullptr, ODE_E_INVALID, buf);
     }
-    if (d->alg_id < ODE_TSIT5 || d->alg_id > ODE_RODAS5P ||
+    if (d->alg_id < ODE_TSIT5 || d->alg_id >= kNumAlgs ||
         (d->precision != ODE_PREC_FP64 && d->precision != ODE_PREC_MIXED) ||
         d->model_id < ODE_MODEL_LINEAR || d->model_id > ODE_MODEL_BRUSSELATOR_1D || d->n_states <= 0 ||
         d->n_params != model_nparams(d->model_id) || !(o->reltol > 0) || !(o->abstol >= 0) || o->nsave < 0 ||

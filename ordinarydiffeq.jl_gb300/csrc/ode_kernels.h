@@ -36,6 +36,8 @@ struct EnsembleArgs {
     long long maxiters;
     int save_start, save_end, save_end_user, saveat_given, saveat_scalar;
     int save_everystep;     // save every accepted step (saveat empty); nsave_cap bounds the slots
+    double* k_out;          // dense output (nullptr: none): k_out[((s*NDENSE + q)*nmax + i)*N + j], the
+                            // method's NDENSE interpolation vectors of the step ending at save s
     double qmax_first_step, qmax;
     int ir_sweeps;          // mixed Rosenbrock: refinement sweeps per solve
     // scheduling
@@ -72,11 +74,42 @@ struct FusedVariant {
     const char* name;
 };
 
+// Dense-output evaluation sol(t) at query times (device pointers):
+//   ts[s*N + j], us[(s*n + i)*N + j], ks[((s*nk + q)*n + i)*N + j], nsaved[j],
+//   tq[r] (shared) or tq[r*N + j] (per trajectory), out[(r*n + i)*N + j].
+struct DenseArgs {
+    long long N;
+    int n, nq, tq_per_traj;
+    int cap;                // save slots per trajectory (nsaved is clamped to it)
+    const double* p;
+    const double* ts;
+    const double* us;
+    const double* ks;
+    const int32_t* nsaved;
+    const double* tq;
+    double* out;
+};
+
+// Dense vectors stored per step, by ode_alg (Tsit5, Vern7, Rodas5P, Rosenbrock23): NDENSE of each method.
+constexpr int kNumAlgs = 4;
+constexpr int kDenseVectors[kNumAlgs] = {7, 7, 3, 2};
+
+// One compiled evaluation kernel: model -1 for the model-free (componentwise)
+// interpolants, else the model whose right-hand side the interpolant needs.
+struct DenseVariant {
+    int alg, model, n, lanes;
+    void (*launch)(const DenseArgs&, int grid, int block, cudaStream_t);
+    const char* name;
+};
+const DenseVariant* dense_variants(int* count);
+
 // Registries filled by each translation unit (static arrays).
 const KernelVariant* tsit5_variants(int* count);
 const KernelVariant* vern7_variants(int* count);
 const KernelVariant* rodas_variants(int* count);
 const KernelVariant* rodas_group_variants(int* count);
+const KernelVariant* ros23_variants(int* count);
+const KernelVariant* ros23_group_variants(int* count);
 const FusedVariant* fused_tsit5_variants(int* count);
 const FusedVariant* fused_vern7_variants(int* count);
 

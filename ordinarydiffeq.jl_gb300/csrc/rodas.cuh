@@ -331,11 +331,24 @@ struct Rodas5PT {
             }
     }
 
+    // Dense output (dense = true): the step's dense k1..k3, the reference's
+    // integrator.k for Rodas5P (rosenbrock_perform_step.jl:811-815).
+    static constexpr int NDENSE = 3;
+    template <class R, int C> __device__ static void prepare_dense(Cache<R, C>& c) { dense<R, C>(c); }
+    template <class R, int C> __device__ static R* dense_slot(Cache<R, C>& c, int q) { return c.dk[q]; }
+
     template <class Model, class R, int L, int C>
     __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, typename Ctl<R>::T th, double, double,
                                        const R* y0, const R* y0lo, const R* y1, const R* y1lo, const R*,
                                        const Group<L>&) {
         dense<R, C>(c);
+        interp_dense<R, C>(c, out, outlo, th, y0, y0lo, y1, y1lo);
+    }
+
+    // Interpolant on formed dense coefficients (rosenbrock_interpolants.jl:172-206).
+    template <class R, int C>
+    __device__ static void interp_dense(const Cache<R, C>& c, R* out, R* outlo, typename Ctl<R>::T th, const R* y0,
+                                        const R* y0lo, const R* y1, const R* y1lo) {
         const R th1 = R(1) - th;
 #pragma unroll
         for (int i = 0; i < C; ++i) {

@@ -1,0 +1,178 @@
+// Rosenbrock23 (Shampine's ode23s pair), with the linear algebra as a policy
+// (RegLA: registers, n <= 8; SmemLA: shared memory, 16-64 states).
+//
+//  perform_step!(::Rosenbrock23Cache)  lib/OrdinaryDiffEqRosenbrock/src/rosenbrock_perform_step.jl:34-146
+//  initialize! (FSAL, k = [k1, k2])   rosenbrock_perform_step.jl:1-14
+//  tableau                             rosenbrock_tableaus.jl:6-10 (c32 = 6 + sqrt(2), d = 1/(2 + sqrt(2)))
+//  interpolant                         rosenbrock_interpolants.jl:39-74
+//  J and W on every attempt            a W-method whose default max_jac_age = 1
+//                                      (algorithms.jl:108-115) makes _rosenbrock_jac_reuse_decision
+//                                      (OrdinaryDiffEqDifferentiation/src/derivative_utils.jl:46-170)
+//                                      return a fresh J and W each time, rejected or not
+//  controller                          alg_order 2 (alg_utils.jl:1), qsteady_max 6/5 (AdaptiveImplicit)
+//
+// With W = J - I/(dt d) (the form the Rodas5P kernels factor), a solve x = W \ b
+// gives the stage k = -x/(dt d), the reference's `vecu * neginvdtγ`.
+// Multiply-adds follow @muladd: a - b*c -> muladd(-b, c, a).
+//
+// Mixed precision (R = float): J, W, the LU, the solves and the stages are FP32;
+// the right-hand side runs in double-float on the compensated state (rhs_stage),
+// the solution is a compensated pair, and the interpolation weights are FP64
+// split into float pairs.
+#pragma once
+#include "erk.cuh"
+#include "rodas.cuh"
+
+namespace odegb {
+
+template <class LA>
+struct Rosenbrock23T {
+    static constexpr int ORDER = 2;
+    static constexpr bool IMPLICIT = true;
+    static constexpr int MAXP = 4;
+    template <class R, int C> struct Cache {
+        typename LA::template Store<R, C> la;
+        R k[3][C];       // k1, k2 (the dense vectors), k3 (error estimate)
+        R f1[C];         // f at the half step
+        R fsal[C];       // f(uprev): FSAL from the last accepted step
+        R fsallast[C];   // f(u)
+        R scratch[C];
+        ff pff[MAXP];
+        int ir;
+    };
+    template <class R, int L, int C> __host__ __device__ static constexpr int smem_bytes() {
+        return LA::template smem_bytes<R, L, C>();
+    }
+    template <class R, int C> __device__ static R* fsal_slot(Cache<R, C>& c) { return c.scratch; }
+
+    template <class Model, class R, int L, int C>
+    __device__ static void initialize(Cache<R, C>& c, const R* u, const R* p, double t, const Group<L>& g,
+                                      StepStats& st, const EnsembleArgs& a, long long j) {
+        LA::template init<R, L, C>(c.la, g);
+        c.ir = a.ir_sweeps;
+        if (sizeof(R) == 4) {
+#pragma unroll
+            for (int i = 0; i < Model::NP; ++i) c.pff[i] = ff(a.p[(size_t)i * a.N + j]);
+        }
+        R zero[C];
+#pragma unroll
+        for (int i = 0; i < C; ++i) zero[i] = R(0);
+        // the start state is exact in the hi part (Acc::split of an FP64 u0 keeps
+        // the remainder in lo); f(u0) from the pair, as every later f
+        R ulo0[C];
+#pragma unroll
+        for (int i = 0; i < C; ++i) {
+            R hi;
+            Acc<R>::split(a.u0[(size_t)(g.lane * C + i) * a.N + j], hi, ulo0[i]);
+        }
+        rhs_stage<Model, R, L, C, Model::NP>(c.fsal, u, sizeof(R) == 4 ? ulo0 : zero, p, c.pff, t, g);
+        st.nf += 1;
+    }
+    template <class R, int C> __device__ static void on_accept(Cache<R, C>& c) {
+#pragma unroll
+        for (int i = 0; i < C; ++i) c.fsal[i] = c.fsallast[i];
+    }
+    template <class R, int C> __device__ static void after_save(Cache<R, C>&) {}
+
+    // Dense output: integrator.k = [k1, k2].
+    static constexpr int NDENSE = 2;
+    template <class R, int C> __device__ static void prepare_dense(Cache<R, C>&) {}
+    template <class R, int C> __device__ static R* dense_slot(Cache<R, C>& c, int q) { return c.k[q]; }
+
+    template <class Model, class R, int L, int C>
+    __device__ static typename Ctl<R>::T step(Cache<R, C>& c, R* u, R* ulo, const R* up, const R* uplo,
+                                             const R* p, double t, double dt, R abstol, R reltol, long long,
+                                             bool, const Group<L>& g, StepStats& st) {
+        constexpr int NP = Model::NP;
+        R dr, idg, ninv, dto2, dto6, c32;
+        if constexpr (sizeof(R) == 8) {
+            const double dtgamma = dt * tab::ROS23_D;
+            idg = 1.0 / dtgamma;
+            ninv = -idg;
+            dr = dt;
+            dto2 = dt / 2.0;
+            dto6 = dt / 6.0;
+            c32 = tab::ROS23_C32;
+        } else {   // dt-derived factors in FP32 (they scale FP32 stage terms)
+            dr = (R)dt;
+            idg = R(1) / (dr * tab::ROS23_D_HI);
+            ninv = -idg;
+            dto2 = dr * R(0.5);
+            dto6 = dr / R(6);
+            c32 = tab::ROS23_C32_HI;
+        }
+        LA::template jacobian<Model, R, L, C>(c.la, up, p, t, true, g);
+        st.njacs += 1;
+        st.nf += 1;   // the reference's AD time derivative (dT = 0 for autonomous models)
+        LA::template factor<R, L, C>(c.la, idg, g);
+        st.nw += 1;
+        R* k1 = c.k[0];
+        R* k2 = c.k[1];
+        R* k3 = c.k[2];
+        R r[C];
+#pragma unroll
+        for (int i = 0; i < C; ++i) r[i] = c.fsal[i];   // fsalfirst + dtd1 dT, dT = 0
+        LA::template wsolve<Model, R, L, C>(c.la, r, dt, idg, c.ir, up, uplo, c.pff, g);
+#pragma unroll
+        for (int i = 0; i < C; ++i) k1[i] = r[i] * ninv;
+        st.nsolve += 1;
+        R stlo[C];
+#pragma unroll
+        for (int i = 0; i < C; ++i) Acc<R>::update(u[i], stlo[i], dto2, k1[i], up[i], uplo[i]);
+        rhs_stage<Model, R, L, C, NP>(c.f1, u, stlo, p, c.pff, stage_time<Model>(0.5, dt, t), g);
+        st.nf += 1;
+#pragma unroll
+        for (int i = 0; i < C; ++i) r[i] = c.f1[i] - k1[i];
+        LA::template wsolve<Model, R, L, C>(c.la, r, dt, idg, c.ir, up, uplo, c.pff, g);
+#pragma unroll
+        for (int i = 0; i < C; ++i) k2[i] = FMA(r[i], ninv, k1[i]);
+        st.nsolve += 1;
+#pragma unroll
+        for (int i = 0; i < C; ++i) Acc<R>::update(u[i], ulo[i], dr, k2[i], up[i], uplo[i]);
+        rhs_stage<Model, R, L, C, NP>(c.fsallast, u, ulo, p, c.pff, stage_time<Model>(1.0, dt, t), g);
+        st.nf += 1;
+#pragma unroll
+        for (int i = 0; i < C; ++i) {
+            R acc = FMA(-c32, k2[i] - c.f1[i], c.fsallast[i]);
+            r[i] = FMA(R(-2), k1[i] - c.fsal[i], acc);   // + dt dT, dT = 0
+        }
+        LA::template wsolve<Model, R, L, C>(c.la, r, dt, idg, c.ir, up, uplo, c.pff, g);
+#pragma unroll
+        for (int i = 0; i < C; ++i) k3[i] = r[i] * ninv;
+        st.nsolve += 1;
+        R tmp[C];
+#pragma unroll
+        for (int i = 0; i < C; ++i) tmp[i] = dto6 * (FMA(R(-2), k2[i], k1[i]) + k3[i]);
+        return error_norm<R, L, C>(tmp, up, u, abstol, reltol, g);
+    }
+
+    // y0 + dt (c1 k1 + c2 k2), c1 = th (1 - th) / (1 - 2d), c2 = th (th - 2d) / (1 - 2d)
+    template <class Model, class R, int L, int C>
+    __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, typename Ctl<R>::T th, double dt, double,
+                                       const R* y0, const R* y0lo, const R*, const R*, const R*,
+                                       const Group<L>&) {
+        const double thd = (double)th;
+        const double d = tab::ROS23_D;
+        const double c1 = thd * (1.0 - thd) / (1.0 - 2.0 * d);
+        const double c2 = thd * (thd - 2.0 * d) / (1.0 - 2.0 * d);
+        if constexpr (sizeof(R) == 8) {
+#pragma unroll
+            for (int i = 0; i < C; ++i)
+                Acc<R>::update(out[i], outlo[i], dt, fma(c1, c.k[0][i], c2 * c.k[1][i]), y0[i], y0lo[i]);
+        } else {
+            const ff w1 = split_weight(c1), w2 = split_weight(c2);
+#pragma unroll
+            for (int i = 0; i < C; ++i) {
+                CSum cs;
+                cs.add_pair(w1.hi, w1.lo, (float)c.k[0][i]);
+                cs.add_pair(w2.hi, w2.lo, (float)c.k[1][i]);
+                Acc<R>::update(out[i], outlo[i], (R)dt, (R)cs.value(), y0[i], y0lo[i]);
+            }
+        }
+    }
+};
+
+using Rosenbrock23Alg = Rosenbrock23T<RegLA>;
+using Rosenbrock23GroupAlg = Rosenbrock23T<SmemLA>;
+
+}  // namespace odegb

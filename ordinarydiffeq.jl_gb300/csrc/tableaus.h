@@ -2,6 +2,7 @@
 // Tsit5: lib/OrdinaryDiffEqTsit5/src/tsit_tableaus.jl:45-101,244-276
 // Vern7: lib/OrdinaryDiffEqVerner/src/verner_tableaus.jl:648-716,880-972,1129-1205
 // Rodas5P: lib/OrdinaryDiffEqRosenbrock/src/rosenbrock_tableaus.jl:23-72
+// Rosenbrock23: lib/OrdinaryDiffEqRosenbrock/src/rosenbrock_tableaus.jl:6-10
 #pragma once
 #include <cuda_runtime.h>
 namespace odegb {
@@ -451,5 +452,12 @@ __host__ __device__ constexpr float VERN7_R_LO(int i, int j) {
     constexpr float t[17][8] = {{0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f}, {0x0.0p+0f, 0x0.0p+0f, 0x1.ae93600000000p-24f, -0x1.988f440000000p-20f, -0x1.f2c4b60000000p-21f, 0x1.60fa700000000p-20f, 0x1.c589f80000000p-20f, -0x1.be21d80000000p-22f}, {0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f}, {0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f}, {0x0.0p+0f, 0x0.0p+0f, 0x1.2207300000000p-24f, 0x1.c997560000000p-19f, -0x1.39a2c00000000p-24f, -0x1.f0a3e00000000p-18f, 0x1.f05c700000000p-18f, 0x1.ac1b400000000p-20f}, {0x0.0p+0f, 0x0.0p+0f, 0x1.354baa0000000p-22f, 0x1.9b478c0000000p-19f, -0x1.4542c60000000p-17f, 0x1.839d960000000p-16f, -0x1.587ba40000000p-16f, -0x1.40a1fa0000000p-19f}, {0x0.0p+0f, 0x0.0p+0f, -0x1.51e6700000000p-23f, -0x1.a0429e0000000p-20f, 0x1.388c4e0000000p-18f, -0x1.f50d7a0000000p-17f, -0x1.3be2fe0000000p-18f, 0x1.65fdaa0000000p-19f}, {0x0.0p+0f, 0x0.0p+0f, -0x1.37f3420000000p-22f, -0x1.a862bc0000000p-18f, -0x1.cbddf00000000p-20f, 0x1.ad76c20000000p-15f, 0x1.3fc4ac0000000p-20f, 0x1.a38ecc0000000p-17f}, {0x0.0p+0f, 0x0.0p+0f, 0x1.054cc20000000p-23f, 0x1.a5fe460000000p-19f, -0x1.00cb780000000p-17f, -0x1.553ece0000000p-20f, -0x1.876ba00000000p-22f, 0x1.0add480000000p-23f}, {0x0.0p+0f, 0x0.0p+0f, 0x1.4770aa0000000p-24f, 0x1.ada7120000000p-24f, 0x1.661a340000000p-20f, 0x1.95f4b00000000p-19f, -0x1.b0a12a0000000p-18f, 0x1.37cd1a0000000p-22f}, {0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f, 0x0.0p+0f}, {0x0.0p+0f, 0x0.0p+0f, -0x1.2caf340000000p-24f, -0x1.df15440000000p-21f, 0x1.a3abe20000000p-19f, -0x1.4bf5ea0000000p-19f, 0x1.dd7c6a0000000p-18f, 0x1.b9effa0000000p-21f}, {0x0.0p+0f, 0x0.0p+0f, -0x1.e801c80000000p-23f, -0x1.205dec0000000p-21f, -0x1.65e27c0000000p-24f, -0x1.40f6520000000p-24f, -0x1.4613900000000p-21f, 0x1.6a9a100000000p-22f}, {0x0.0p+0f, 0x0.0p+0f, -0x1.0580ca0000000p-22f, 0x1.33dc520000000p-20f, -0x1.482b240000000p-19f, 0x1.21c7d80000000p-24f, -0x1.fbc66c0000000p-20f, -0x1.787bea0000000p-20f}, {0x0.0p+0f, 0x0.0p+0f, -0x1.35f6640000000p-22f, -0x1.fdc9d40000000p-18f, -0x1.ccbc3a0000000p-17f, -0x1.ab1b2e0000000p-16f, 0x1.0f51ca0000000p-16f, 0x1.b38e8a0000000p-19f}, {0x0.0p+0f, 0x0.0p+0f, 0x1.876ec60000000p-24f, 0x1.7aa7c60000000p-20f, -0x1.0372c80000000p-18f, -0x1.c087460000000p-16f, -0x1.553d500000000p-23f, 0x1.2b721c0000000p-18f}, {0x0.0p+0f, 0x0.0p+0f, 0x1.3bb9ce0000000p-22f, 0x1.c893920000000p-22f, 0x1.1281540000000p-17f, 0x1.d5eaac0000000p-16f, -0x1.d996220000000p-17f, 0x1.463a1a0000000p-18f}};
     return t[i][j];
 }
+// ROSENBROCK23: c32 = 6 + sqrt(2), d = 1 / (2 + sqrt(2)) in Float64
+constexpr double ROS23_C32 = 0x1.da827999fcef3p+2;  // 7.414213562373095
+constexpr float ROS23_C32_HI = 0x1.da827a0000000p+2f;
+constexpr float ROS23_C32_LO = -0x1.980c440000000p-24f;
+constexpr double ROS23_D = 0x1.2bec333018867p-2;  // 0.2928932188134525
+constexpr float ROS23_D_HI = 0x1.2bec340000000p-2f;
+constexpr float ROS23_D_LO = -0x1.9fcef40000000p-27f;
 }  // namespace tab
 }  // namespace odegb

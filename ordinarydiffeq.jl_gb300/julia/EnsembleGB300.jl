@@ -19,7 +19,7 @@ module EnsembleGB300Ext
 using SciMLBase
 import OrdinaryDiffEqTsit5: Tsit5
 import OrdinaryDiffEqVerner: Vern7
-import OrdinaryDiffEqRosenbrock: Rodas5P
+import OrdinaryDiffEqRosenbrock: Rodas5P, Rosenbrock23
 
 export EnsembleGB300, GB300Model
 
@@ -60,10 +60,42 @@ end
 alg_id(::Tsit5) = Int32(0)
 alg_id(::Vern7) = Int32(1)
 alg_id(::Rodas5P) = Int32(2)
+alg_id(::Rosenbrock23) = Int32(3)
 
 const RETCODES = (SciMLBase.ReturnCode.Default, SciMLBase.ReturnCode.Success, SciMLBase.ReturnCode.MaxIters,
                   SciMLBase.ReturnCode.DtNaN, SciMLBase.ReturnCode.DtLessThanMin, SciMLBase.ReturnCode.Unstable,
                   SciMLBase.ReturnCode.Terminated)
+
+"""
+Interpolation of a dense GB300 solve (the reference's dense = true): sol(t)
+evaluates the method's interpolant on the saved steps on the device
+(ode_dense_eval), as ode_interpolation does on the host.  Holds one
+trajectory's saves t (ns), u (n x ns) and interpolation vectors k (n x nk x ns).
+"""
+struct GB300DenseInterpolation <: SciMLBase.AbstractDiffEqInterpolation
+    model::Int32
+    alg::Int32
+    p::Vector{Float64}
+    device::Int
+    t::Vector{Float64}
+    u::Matrix{Float64}
+    k::Array{Float64, 3}
+end
+
+function (id::GB300DenseInterpolation)(tvals, idxs, deriv, p, continuity::Symbol = :left)
+    deriv == Val{0} || error("GB300 dense output evaluates the solution (deriv = Val{0}) only")
+    tq = tvals isa Number ? [Float64(tvals)] : collect(Float64, tvals)
+    n, ns, nq = size(id.u, 1), length(id.t), length(tq)
+    d = ProblemDesc(id.model, id.alg, n, length(id.p), 0, 0)
+    out = zeros(n, nq)   # [(r*n + i)*N + j] with N = 1 -> out[i, r]
+    status = ccall((:ode_dense_eval, LIB), Cint,
+                   (Ptr{Cvoid}, Ref{ProblemDesc}, Int64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+                    Ptr{Int32}, Int32, Int32, Ptr{Float64}, Int32, Ptr{Float64}),
+                   handle(id.device), d, 1, id.p, id.t, id.u, id.k, Int32[ns], ns, nq, tq, 0, out)
+    status == 0 || error("ode_dense_eval: ", unsafe_string(ccall((:ode_last_error, LIB), Cstring, (Ptr{Cvoid},), handle(id.device))))
+    vals = [idxs === nothing ? out[:, r] : out[idxs, r] for r in 1:nq]
+    tvals isa Number ? vals[1] : vals
+end
 
 const HANDLES = Dict{Int, Ptr{Cvoid}}()
 function handle(dev)
@@ -75,11 +107,11 @@ function handle(dev)
     end
 end
 
-function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem, alg::Union{Tsit5, Vern7, Rodas5P},
+function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem, alg::Union{Tsit5, Vern7, Rodas5P, Rosenbrock23},
                            ens::EnsembleGB300; trajectories, saveat = Float64[], reltol = 1e-3, abstol = 1e-6,
                            dt = 0.0, dtmax = 0.0, dtmin = 0.0, maxiters = 1_000_000, save_start = nothing,
                            save_end = nothing, save_everystep = isempty(saveat), max_step_saves = 1024, seed = 0,
-                           kwargs...)
+                           dense = save_everystep && isempty(saveat), kwargs...)
     t0 = time()
     N = trajectories
     probs = [eprob.prob_func(eprob.prob, SciMLBase.EnsembleContext(i, 1, seed)) for i in 1:N]
@@ -109,10 +141,21 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem, alg::Union{
     cap = (everystep ? max_step_saves : length(sv)) + 2
     t_out = fill(NaN, N, cap); u_out = fill(NaN, N, n, cap)   # [(s*n + i)*N + j] -> u_out[j, i, s]
     nsaved = zeros(Int32, N); rc = zeros(Int32, N); st = Vector{Stats}(undef, N)
-    status = ccall((:ode_solve_ensemble, LIB), Cint,
-                   (Ptr{Cvoid}, Ref{ProblemDesc}, Ref{Options}, Int64, Ptr{Int32}, Ptr{Float64}, Ptr{Float64},
-                    Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Int32}, Ptr{Int32}, Ptr{Stats}),
-                   handle(ens.device), d, o, N, npt, u0, ps, ts, sv, t_out, u_out, nsaved, rc, st)
+    # dense output (solve.jl:145-146) for every-step saves of one state count
+    isdense = dense && everystep && npt == C_NULL
+    if isdense
+        nk = ccall((:ode_dense_nk, LIB), Cint, (Cint,), alg_id(alg))
+        k_out = zeros(N, n, nk, cap)   # [((s*nk + q)*n + i)*N + j] -> k_out[j, i, q, s]
+        status = ccall((:ode_solve_ensemble_dense, LIB), Cint,
+                       (Ptr{Cvoid}, Ref{ProblemDesc}, Ref{Options}, Int64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+                        Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Int32}, Ptr{Int32}, Ptr{Stats}),
+                       handle(ens.device), d, o, N, u0, ps, ts, t_out, u_out, k_out, nsaved, rc, st)
+    else
+        status = ccall((:ode_solve_ensemble, LIB), Cint,
+                       (Ptr{Cvoid}, Ref{ProblemDesc}, Ref{Options}, Int64, Ptr{Int32}, Ptr{Float64}, Ptr{Float64},
+                        Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Int32}, Ptr{Int32}, Ptr{Stats}),
+                       handle(ens.device), d, o, N, npt, u0, ps, ts, sv, t_out, u_out, nsaved, rc, st)
+    end
     status == 0 || error("ode_solve_ensemble: ", unsafe_string(ccall((:ode_last_error, LIB), Cstring, (Ptr{Cvoid},), handle(ens.device))))
     sols = map(1:N) do j
         k = nsaved[j]
@@ -120,7 +163,14 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem, alg::Union{
         us = [u_out[j, 1:nj, s] for s in 1:k]
         stats = SciMLBase.DEStats(st[j].nf, 0, 0, st[j].nsolve, st[j].nw, st[j].njacs, 0, 0, 0, 0,
                                   st[j].naccept, st[j].nreject, 0.0)
-        SciMLBase.build_solution(probs[j], alg, t_out[j, 1:k], us; retcode = RETCODES[rc[j] + 1], stats)
+        if isdense
+            interp = GB300DenseInterpolation(model, alg_id(alg), ps[j, :], ens.device, t_out[j, 1:k],
+                                             u_out[j, :, 1:k], k_out[j, :, :, 1:k])
+            SciMLBase.build_solution(probs[j], alg, t_out[j, 1:k], us; dense = true, interp,
+                                     retcode = RETCODES[rc[j] + 1], stats)
+        else
+            SciMLBase.build_solution(probs[j], alg, t_out[j, 1:k], us; retcode = RETCODES[rc[j] + 1], stats)
+        end
     end
     SciMLBase.EnsembleSolution(sols, time() - t0, true)
 end

@@ -9,7 +9,7 @@ import os
 
 from . import build as _build
 
-ODE_TSIT5, ODE_VERN7, ODE_RODAS5P = 0, 1, 2
+ODE_TSIT5, ODE_VERN7, ODE_RODAS5P, ODE_ROSENBROCK23 = 0, 1, 2, 3
 MODEL_LINEAR, MODEL_LORENZ, MODEL_ROBERTSON, MODEL_DUFFING_CHAIN, MODEL_BRUSSELATOR_1D = 0, 1, 2, 3, 4
 PREC_FP64, PREC_MIXED = 0, 1
 STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "out of device memory",
@@ -56,6 +56,11 @@ SIGNATURES = {
                                      _DP, _DP, _DP, _DP, _DP, _DP, _IP, _IP, C.POINTER(Stats)]),
     "ode_solve_ensemble_device": (C.c_int, [_VP, C.POINTER(ProblemDesc), C.POINTER(Options), C.c_int64,
                                             _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "ode_dense_nk": (C.c_int, [C.c_int]),
+    "ode_solve_ensemble_dense": (C.c_int, [_VP, C.POINTER(ProblemDesc), C.POINTER(Options), C.c_int64, _DP, _DP,
+                                           _DP, _DP, _DP, _DP, _IP, _IP, C.POINTER(Stats)]),
+    "ode_dense_eval": (C.c_int, [_VP, C.POINTER(ProblemDesc), C.c_int64, _DP, _DP, _DP, _DP, _IP, C.c_int32,
+                                 C.c_int32, _DP, C.c_int32, _DP]),
     "ode_submit": (C.c_int, [_VP, C.POINTER(ProblemDesc), C.POINTER(Options), C.c_int64, _IP, _DP, _DP,
                              _DP, _DP, _DP, _DP, _IP, _IP, C.POINTER(Stats), C.POINTER(C.c_uint64)]),
     "ode_poll": (C.c_int, [_VP, C.c_uint64, _IP]),

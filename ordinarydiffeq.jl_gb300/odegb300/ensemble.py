@@ -60,7 +60,14 @@ class Rodas5P(_Alg):
     alg_id = _lib.ODE_RODAS5P
 
 
-ALG_BY_NAME = {"tsit5": Tsit5(), "vern7": Vern7(), "rodas5p": Rodas5P()}
+class Rosenbrock23(_Alg):
+    """Rosenbrock23 (Shampine's ode23s W-method pair) with the analytic Jacobian of
+    the model, a fresh J and W on every step attempt (the reference's default
+    max_jac_age = 1; lib/OrdinaryDiffEqRosenbrock/src/algorithms.jl:108-146)."""
+    alg_id = _lib.ODE_ROSENBROCK23
+
+
+ALG_BY_NAME = {"tsit5": Tsit5(), "vern7": Vern7(), "rodas5p": Rodas5P(), "rosenbrock23": Rosenbrock23()}
 
 
 @dataclass
@@ -142,18 +149,49 @@ class EnsembleProblem:
 
 
 class ODESolution:
-    """One trajectory's result: t, u (list of state vectors), retcode, stats."""
+    """One trajectory's result: t, u (list of state vectors), retcode, stats.
+    sol(t) evaluates the solution between saves (see __call__)."""
 
-    def __init__(self, t, u, retcode, stats, prob=None, alg=None):
+    def __init__(self, t, u, retcode, stats, prob=None, alg=None, dense=None):
         self.t = t
         self.u = u
         self.retcode = ReturnCode(int(retcode))
         self.stats = stats
         self.prob = prob
         self.alg = alg
+        self._dense = dense   # (solve outputs, trajectory index) of a dense solve
+
+    @property
+    def dense(self):
+        return self._dense is not None
+
+    def __call__(self, t):
+        """sol(t) as ode_interpolation (generic_dense.jl:1094-1190) evaluates it:
+        the method's interpolant on the saved steps for a dense solve (on the
+        GPU), linear interpolation between saves otherwise.  Scalar t gives one
+        state vector, an array of times one row per time."""
+        tq = np.atleast_1d(np.asarray(t, dtype=np.float64))
+        if self._dense is not None:
+            res, j = self._dense
+            sub = {"t": res["t"][:, j:j + 1].copy(), "u": res["u"][:, :, j:j + 1].copy(),
+                   "k": res["k"][..., j:j + 1].copy(), "nsaved": res["nsaved"][j:j + 1].copy(),
+                   "dense": dict(res["dense"], p=res["dense"]["p"][:, j:j + 1].copy())}
+            vals = dense_eval(sub, tq)[:, :, 0]
+        else:
+            ts = np.asarray(self.t, dtype=np.float64)
+            us = np.asarray(self.u, dtype=np.float64)
+            vals = np.empty((tq.size, us.shape[1]))
+            for r, tv in enumerate(tq):
+                ip = min(len(ts) - 1, 1 + int(np.searchsorted(ts[1:], tv, side="left")))
+                im = ip - 1 if ip > 0 else ip
+                dt = ts[ip] - ts[im]
+                th = 1.0 if dt == 0 else (tv - ts[im]) / dt
+                vals[r] = (1 - th) * us[im] + th * us[ip]
+        return vals[0] if np.ndim(t) == 0 else vals
 
     def __repr__(self):
-        return "ODESolution(retcode=%s, %d saves)" % (self.retcode.name, len(self.t))
+        return "ODESolution(retcode=%s, %d saves%s)" % (self.retcode.name, len(self.t),
+                                                      ", dense" if self.dense else "")
 
 
 class _LazySolutions:
@@ -178,7 +216,7 @@ class _LazySolutions:
         t = r["t"][:ns, j].copy()
         u = [r["u"][s, :n, j].copy() for s in range(ns)]
         st = {k: int(r["stats"][k][j]) for k in r["stats"]}
-        return ODESolution(t, u, r["retcode"][j], st, alg=self.alg)
+        return ODESolution(t, u, r["retcode"][j], st, alg=self.alg, dense=(r, j) if r.get("dense") else None)
 
     def __iter__(self):
         for j in range(len(self)):
@@ -233,12 +271,14 @@ def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_ste
 
 def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=1e-6, dt=None,
                  dtmax=None, dtmin=None, maxiters=1000000, save_start=None, save_end=None, n_per_traj=None,
-                 qmax_first_step=None, qmax=None, return_times=False, save_everystep=False, max_step_saves=1024):
+                 qmax_first_step=None, qmax=None, return_times=False, save_everystep=False, max_step_saves=1024,
+                 dense=False):
     """Solve a packed ensemble.  u0s (n, N), ps (np, N), tspans (2, N).  Returns the
     raw structure-of-arrays outputs dict (t, u, nsaved, retcode, stats).
     save_everystep (without saveat) keeps every accepted step, up to
     max_step_saves per trajectory (past that the last slot holds the final
-    point and a warning is issued)."""
+    point and a warning is issued).  dense (with save_everystep) also keeps
+    each step's interpolation vectors, k (cap, nk, n, N), for dense_eval."""
     L = _lib.load()
     if isinstance(model, str):
         model = MODELS[model]
@@ -250,8 +290,13 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
     o = _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax)
     d = _lib.ProblemDesc(model, alg.alg_id, n, ps.shape[0], ens.prec_id(), 0)
     cap = sv.cap
+    if dense and not sv.everystep:
+        raise ValueError("dense output keeps every step: use it without saveat, with save_everystep")
+    if dense and n_per_traj is not None:
+        raise ValueError("dense output needs trajectories of one size")
     t_out = np.full((cap, N), np.nan)
     u_out = np.full((cap, n, N), np.nan)
+    k_out = np.empty((cap, L.ode_dense_nk(alg.alg_id), n, N)) if dense else None
     nsaved = np.zeros(N, dtype=np.int32)
     rc = np.zeros(N, dtype=np.int32)
     stats = np.zeros((N, 6), dtype=np.int64)
@@ -262,10 +307,15 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
     dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
     ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))
     t0 = time.perf_counter()
-    status = L.ode_solve_ensemble(h, C.byref(d), C.byref(o), N, ip(npt) if npt is not None else None,
-                                  dp(u0s), dp(ps), dp(tspans), dp(sv.values) if sv.nsave else None,
-                                  dp(t_out), dp(u_out), ip(nsaved), ip(rc),
-                                  stats.ctypes.data_as(C.POINTER(_lib.Stats)))
+    if dense:
+        status = L.ode_solve_ensemble_dense(h, C.byref(d), C.byref(o), N, dp(u0s), dp(ps), dp(tspans), dp(t_out),
+                                            dp(u_out), dp(k_out), ip(nsaved), ip(rc),
+                                            stats.ctypes.data_as(C.POINTER(_lib.Stats)))
+    else:
+        status = L.ode_solve_ensemble(h, C.byref(d), C.byref(o), N, ip(npt) if npt is not None else None,
+                                      dp(u0s), dp(ps), dp(tspans), dp(sv.values) if sv.nsave else None,
+                                      dp(t_out), dp(u_out), ip(nsaved), ip(rc),
+                                      stats.ctypes.data_as(C.POINTER(_lib.Stats)))
     elapsed = time.perf_counter() - t0
     _lib.check(status, h)
     names = ("nf", "njacs", "nw", "nsolve", "naccept", "nreject")
@@ -276,6 +326,34 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
                           "dropped (the final point is kept)" % (lost, sv.max_step_saves))
     out = {"t": t_out, "u": u_out, "nsaved": nsaved, "retcode": rc,
            "stats": {k: stats[:, i] for i, k in enumerate(names)}, "elapsed": elapsed}
+    if dense:
+        out["k"] = k_out
+        out["dense"] = {"model": model, "alg": alg.alg_id, "p": ps, "device": ens.device}
+    return out
+
+
+def dense_eval(res, tq, device=None):
+    """sol_j(t) of a dense solve (solve_arrays(..., dense=True)) for every
+    trajectory j at the query times tq, shared (nq,) or per trajectory (nq, N),
+    evaluated on the GPU in FP64 (ode_dense_eval).  Returns (nq, n, N)."""
+    info = res.get("dense")
+    if not info:
+        raise ValueError("not a dense solve: pass dense=True")
+    L = _lib.load()
+    t, u, k, ns = res["t"], res["u"], res["k"], res["nsaved"]
+    cap, n, N = u.shape
+    ps = np.ascontiguousarray(info["p"], dtype=np.float64)
+    tq = np.ascontiguousarray(np.atleast_1d(tq), dtype=np.float64)
+    per = tq.ndim == 2
+    if per and tq.shape[1] != N:
+        raise ValueError("per-trajectory query times must have shape (nq, N)")
+    nq = tq.shape[0]
+    out = np.empty((nq, n, N))
+    d = _lib.ProblemDesc(info["model"], info["alg"], n, ps.shape[0], 0, 0)
+    h = get_handle(info["device"] if device is None else device)
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    _lib.check(L.ode_dense_eval(h, C.byref(d), N, dp(ps), dp(t), dp(u), dp(k),
+                                ns.ctypes.data_as(C.POINTER(C.c_int32)), cap, nq, dp(tq), int(per), dp(out)), h)
     return out
 
 
@@ -306,12 +384,19 @@ def autotune(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=
 
 def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, saveat=None, reltol=1e-3,
           abstol=1e-6, dt=None, dtmax=None, dtmin=None, maxiters=1000000, save_start=None, save_end=None,
-          seed=0, qmax_first_step=None, qmax=None, save_everystep=None, max_step_saves=1024):
+          seed=0, qmax_first_step=None, qmax=None, save_everystep=None, max_step_saves=1024, dense=None):
     """solve(EnsembleProblem, alg, EnsembleGB300(); trajectories, saveat, reltol, abstol, ...).
-    As in the reference, save_everystep defaults to "no saveat given" (every
-    accepted step is kept, up to max_step_saves per trajectory)."""
+    As in the reference (solve.jl:138-146), save_everystep defaults to "no
+    saveat given" (every accepted step is kept, up to max_step_saves per
+    trajectory) and dense to save_everystep without saveat (each step's
+    interpolation vectors are kept too, so sol(t) uses the method's
+    interpolant); ensembles of uneven sizes are not dense by default."""
+    no_saveat = saveat is None or (not np.isscalar(saveat) and np.size(saveat) == 0)
     if save_everystep is None:
-        save_everystep = saveat is None or (not np.isscalar(saveat) and np.size(saveat) == 0)
+        save_everystep = no_saveat
+    dense_default = dense is None
+    if dense is None:
+        dense = bool(save_everystep and no_saveat)
     ens = ensemblealg or EnsembleGB300()
     if not isinstance(ens, EnsembleGB300):
         raise TypeError("ensemble algorithm must be EnsembleGB300")
@@ -326,7 +411,8 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
         tspans = eprob.tspans if eprob.tspans is not None else np.repeat(np.array(prob.tspan)[:, None], N, axis=1)
         res = solve_arrays(prob.model, alg, ens, u0s, ps, tspans, saveat, reltol, abstol, dt, dtmax, dtmin,
                            maxiters, save_start, save_end, eprob.n_per_traj, qmax_first_step, qmax,
-                           save_everystep=save_everystep, max_step_saves=max_step_saves)
+                           save_everystep=save_everystep, max_step_saves=max_step_saves,
+                           dense=dense and not (dense_default and eprob.n_per_traj is not None))
         sols = _LazySolutions(res, alg, eprob.n_per_traj)
         return EnsembleSolution(sols, time.perf_counter() - t_start, True, res)
     if trajectories is None:
@@ -341,7 +427,8 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
     while done < trajectories:
         ids = list(range(done, min(trajectories, done + batch_size)))
         outs = _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, dtmin, maxiters,
-                            save_start, save_end, output_func, qmax_first_step, qmax, save_everystep, max_step_saves)
+                            save_start, save_end, output_func, qmax_first_step, qmax, save_everystep, max_step_saves,
+                            dense, dense_default)
         u, converged = reduction(u, outs, range(ids[0] + 1, ids[-1] + 2))
         done = ids[-1] + 1
         if converged:
@@ -350,7 +437,8 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
 
 
 def _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, dtmin, maxiters, save_start,
-                 save_end, output_func, qmax_first_step, qmax, save_everystep=False, max_step_saves=1024):
+                 save_end, output_func, qmax_first_step, qmax, save_everystep=False, max_step_saves=1024,
+                 dense=False, dense_default=True):
     repeat = {i: 1 for i in ids}
     results = {}
     todo = list(ids)
@@ -376,7 +464,8 @@ def _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, 
         tspans = np.array([pp.tspan for pp in probs]).T
         res = solve_arrays(probs[0].model, alg, ens, u0s, ps, tspans, saveat, reltol, abstol, dt, dtmax, dtmin,
                            maxiters, save_start, save_end, npt, qmax_first_step, qmax,
-                           save_everystep=save_everystep, max_step_saves=max_step_saves)
+                           save_everystep=save_everystep, max_step_saves=max_step_saves,
+                           dense=dense and not (dense_default and npt is not None))
         sols = _LazySolutions(res, alg, npt)
         again = []
         for k, i in enumerate(todo):

@@ -22,16 +22,17 @@ def lorenz(N, seed=42):
 ROBER_SAVEAT = 10.0 ** np.linspace(-5.0, 5.0, 20)
 
 
-def robertson(N, seed=42):
+def robertson(N, seed=42, alg="rodas5p", reltol=1e-6, abstol=1e-10):
     """Robertson kinetics: k = (0.04, 3e7, 1e4) each scaled by 2^U(-1, 1) (log-uniform in
     [0.5, 2]); u0 = (1, 0, 0); tspan (0, 1e5); 20 log-spaced saves in (0, 1e5];
-    Rodas5P with the analytic Jacobian, reltol 1e-6, abstol 1e-10."""
+    Rodas5P with the analytic Jacobian, reltol 1e-6, abstol 1e-10 (or the given
+    Rosenbrock method and tolerances)."""
     rng = np.random.default_rng(seed)
     p = np.array([0.04, 3e7, 1e4])[:, None] * 2.0 ** rng.uniform(-1.0, 1.0, (3, N))
     u0 = np.tile(np.array([[1.0], [0.0], [0.0]]), (1, N))
     ts = np.vstack([np.zeros(N), np.full(N, 1e5)])
-    return dict(model="robertson", alg="rodas5p", u0=u0, p=p, tspan=ts, saveat=ROBER_SAVEAT, reltol=1e-6,
-                abstol=1e-10)
+    return dict(model="robertson", alg=alg, u0=u0, p=p, tspan=ts, saveat=ROBER_SAVEAT, reltol=reltol,
+                abstol=abstol)
 
 
 def duffing(N, seed=42, sizes=(2, 4, 8, 16, 32), tf_range=(1.0, 100.0)):
@@ -104,6 +105,16 @@ def attempt_flops(alg, model, n):
         solve = 2 * n * n + n
         return (8 * F + Jf + 2 * n + lu + 8 * solve + n * (2 * 28 + 2 * 28 + 2 * 8 + 2 * 24) + 28 + 8
                 + error_norm_flops(n) + CONTROLLER_FLOPS)
+    if alg == "rosenbrock23":
+        # 2 RHS (f at the half step, FSAL f(u)) + J, W, LU, 3 solves; per state the
+        # stage, FSAL-difference and error-estimate arithmetic: 19 flops
+        Jf = JAC_FLOPS[model](n)
+        if model == "brusselator_1d":
+            lu = lu_struct_flops(brusselator_pattern(n))
+        else:
+            lu = sum((n - c - 1) + 2 * (n - c - 1) ** 2 + 1 for c in range(n))
+        solve = 2 * n * n + n
+        return 2 * F + Jf + 2 * n + lu + 3 * solve + 19 * n + error_norm_flops(n) + CONTROLLER_FLOPS
     raise ValueError(alg)
 
 
@@ -140,4 +151,6 @@ def save_flops(alg, model, n):
         return 6 * F + n * 2 * (7 + 8 + 9 + 10 + 10 + 10) + n * 2 * 13
     if alg == "tsit5":
         return n * 2 * 7
+    if alg == "rosenbrock23":
+        return n * 2 * 2 + 8
     return n * 2 * 5

@@ -37,7 +37,9 @@ def test_library_exports_every_declared_symbol():
 
 def test_abi_version_and_defaults_without_gpu():
     L = _lib.load()
-    assert L.ode_abi_version() == 2
+    assert L.ode_abi_version() == 3
+    # dense vectors per step (Tsit5 k1..k7, Vern7 k1 and k4..k9, Rodas5P dense k1..k3)
+    assert [L.ode_dense_nk(a) for a in (0, 1, 2)] == [7, 7, 3] and L.ode_dense_nk(9) == -1
     o = _lib.Options()
     L.ode_options_default(C.byref(o))
     assert o.reltol == 1e-3 and o.abstol == 1e-6 and o.maxiters == 1000000

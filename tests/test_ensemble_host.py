@@ -22,7 +22,7 @@ def exact_linear(monkeypatch):
 
     def fake(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=1e-6, dt=None, dtmax=None,
              dtmin=None, maxiters=1000000, save_start=None, save_end=None, n_per_traj=None, qmax_first_step=None,
-             qmax=None, return_times=False, save_everystep=False, max_step_saves=1024):
+             qmax=None, return_times=False, save_everystep=False, max_step_saves=1024, dense=False):
         u0s, ps, tspans = np.asarray(u0s, float), np.asarray(ps, float), np.asarray(tspans, float)
         n, N = u0s.shape
         sv = resolve_saveat(saveat, tspans, save_start, save_end, save_everystep, max_step_saves)
@@ -39,7 +39,7 @@ def exact_linear(monkeypatch):
                 u[s, :, j] = u0s[:, j] * np.exp(ps[0, j] * (tt - tspans[0, j]))
             ns[j] = len(pts)
         calls.append(N)
-        fake.last = {"save_everystep": save_everystep, "max_step_saves": max_step_saves}
+        fake.last = {"save_everystep": save_everystep, "max_step_saves": max_step_saves, "dense": dense}
         names = ("nf", "njacs", "nw", "nsolve", "naccept", "nreject")
         return {"t": t, "u": u, "nsaved": ns, "retcode": np.ones(N, dtype=np.int32),
                 "stats": {k: np.zeros(N, dtype=np.int64) for k in names}, "elapsed": 0.0}
@@ -111,8 +111,32 @@ def test_packed_inputs_and_uneven_sizes(exact_linear):
 
 
 def test_no_saveat_defaults_to_every_step(exact_linear):
-    # the reference's default: save_everystep = isempty(saveat)
+    # the reference's defaults (solve.jl:138-146): save_everystep = isempty(saveat),
+    # dense = save_everystep && isempty(saveat)
     solve(EnsembleProblem(PROB), Tsit5(), EnsembleGB300(), trajectories=2)
-    assert E.solve_arrays.last["save_everystep"] is True
+    assert E.solve_arrays.last["save_everystep"] is True and E.solve_arrays.last["dense"] is True
     solve(EnsembleProblem(PROB), Tsit5(), EnsembleGB300(), trajectories=2, saveat=0.5)
-    assert E.solve_arrays.last["save_everystep"] is False
+    assert E.solve_arrays.last["save_everystep"] is False and E.solve_arrays.last["dense"] is False
+    solve(EnsembleProblem(PROB), Tsit5(), EnsembleGB300(), trajectories=2, dense=False)
+    assert E.solve_arrays.last["save_everystep"] is True and E.solve_arrays.last["dense"] is False
+
+
+def test_uneven_ensembles_are_not_dense_by_default(exact_linear):
+    npt = np.array([4, 8], dtype=np.int32)
+    ep = EnsembleProblem(ODEProblem("duffing_chain", np.ones(8), (0.0, 1.0), [0.5, 0.1, 0.0]),
+                         u0s=np.ones((8, 2)), ps=np.full((3, 2), 0.5), tspans=np.tile([[0.0], [1.0]], (1, 2)),
+                         n_per_traj=npt)
+    solve(ep, Tsit5(), EnsembleGB300())
+    assert E.solve_arrays.last["save_everystep"] is True and E.solve_arrays.last["dense"] is False
+
+
+def test_linear_interpolation_between_saves_without_dense():
+    # ode_interpolation's non-dense branch (generic_dense.jl:1121-1122, linear_interpolant :2119-2127)
+    from odegb300.ensemble import ODESolution
+    s = ODESolution(np.array([0.0, 1.0, 3.0]), [np.array([0.0, 10.0]), np.array([1.0, 20.0]),
+                                                 np.array([5.0, 0.0])], 1, {})
+    assert np.allclose(s(0.5), [0.5, 15.0]) and np.allclose(s(2.0), [3.0, 10.0])
+    assert np.allclose(s([0.0, 1.0, 3.0]), [[0.0, 10.0], [1.0, 20.0], [5.0, 0.0]])
+    # left continuity: t == ts[i] takes the interval ending at ts[i]; outside the
+    # range the first or last interval's line continues
+    assert np.allclose(s(4.0), [7.0, -10.0]) and np.allclose(s(-1.0), [-1.0, 0.0])

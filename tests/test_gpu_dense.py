@@ -1,0 +1,152 @@
+"""GPU parity of dense output (the reference's dense = true, its default without
+saveat): every accepted step is saved with the method's interpolation vectors
+(save_dense_at_t!, lib/OrdinaryDiffEqCore/src/integrators/integrator_utils.jl:455-473)
+and sol(t) evaluates the interpolant between saves as ode_interpolation does
+(lib/OrdinaryDiffEqCore/src/dense/generic_dense.jl:1094-1190).
+
+Checked against the oracle's dense record and its sol(t), and through
+properties that hold at any size: sol(t_i) reproduces the saved u_i, and sol(t)
+equals the saveat interpolant of a solve with the same steps.
+"""
+import numpy as np
+import pytest
+
+import pyoracle as O
+from gpu_common import ALG, MODEL, brusselator_inputs, duffing_inputs, gpu, lorenz_inputs, robertson_inputs
+from odegb300 import dense_eval
+
+pytestmark = pytest.mark.gpu
+
+
+def inputs(model, N, seed):
+    if model == "lorenz":
+        return lorenz_inputs(N, seed=seed)
+    if model == "robertson":
+        return robertson_inputs(N, seed=seed)
+    if model == "duffing_chain":
+        u0, p, ts, _, _ = duffing_inputs(N, 8, seed=seed, tf_range=(1.0, 10.0))
+        return u0, p, ts
+    return brusselator_inputs(N, cells=8, seed=seed)
+
+
+CASES = [("lorenz", "tsit5", 1e-8, 1e-8), ("lorenz", "vern7", 1e-8, 1e-8), ("robertson", "rodas5p", 1e-6, 1e-10),
+         ("duffing_chain", "vern7", 1e-6, 1e-6), ("brusselator_1d", "rodas5p", 1e-5, 1e-8)]
+
+
+@pytest.mark.parametrize("model,alg,rt,at", CASES)
+def test_dense_steps_and_sol_t_match_oracle(model, alg, rt, at):
+    N = 32
+    u0, p, ts = inputs(model, N, 5)
+    n = u0.shape[0]
+    g = gpu(model, alg, u0, p, ts, None, rt, at, save_everystep=True, max_step_saves=4096, dense=True)
+    rng = np.random.default_rng(1)
+    tq = ts[0] + (ts[1] - ts[0]) * rng.uniform(0.0, 1.0, (24, N))
+    tq[0], tq[1] = ts[0], ts[1]
+    ev = dense_eval(g, tq)
+    same_steps = 0
+    for j in range(N):
+        o = O.solve(ALG[alg][1], MODEL[model], u0[:, j], p[:, j], ts[:, j], dense=True, reltol=rt, abstol=at,
+                    saveat_given=False, save_everystep=True, max_step_saves=4096, save_start=True, save_end=True)
+        D = o["dense"]
+        ns = int(g["nsaved"][j])
+        # sol(t) at the queries: within 10 (reltol |u| + abstol) of the oracle's sol(t)
+        ref = D(tq[:, j])
+        assert np.all(np.abs(ev[:, :, j] - ref) <= 10 * (rt * np.abs(ref) + at)), (j, ev[:, :, j], ref)
+        if D.nsteps + 1 != ns:
+            continue
+        # FP64 on both sides, but FMA contraction (and the LU's rounding) differs: the
+        # step times drift apart slowly; compare the stored vectors step by step where
+        # the two step sequences still coincide to 1e-9
+        tends = np.array([D.step(s)[1] for s in range(ns - 1)])
+        if np.max(np.abs(g["t"][1:ns, j] - tends) / np.abs(tends).clip(1e-300)) > 1e-9:
+            continue
+        same_steps += 1
+        for s in range(1, ns):
+            tprev, tend, y0, y1, ko = D.step(s - 1)
+            kg = g["k"][s, :, :, j]
+            scale = np.abs(ko).max(axis=1, keepdims=True) + 1e-300
+            assert np.all(np.abs(kg - ko) <= 1e-5 * scale), (j, s, kg, ko)
+    assert same_steps >= 1
+    # the start save carries no step
+    assert np.all(g["k"][0] == 0.0)
+    # sol(t_i) reproduces the saved u_i (left continuity: theta = 1 on the step ending at t_i)
+    for j in range(0, N, 7):
+        ns = int(g["nsaved"][j])
+        at_saves = dense_eval({**g, "t": g["t"][:, j:j + 1].copy(), "u": g["u"][:, :, j:j + 1].copy(),
+                               "k": g["k"][..., j:j + 1].copy(), "nsaved": g["nsaved"][j:j + 1].copy(),
+                               "dense": dict(g["dense"], p=g["dense"]["p"][:, j:j + 1].copy())},
+                              g["t"][:ns, j])[:, :, 0]
+        saved = g["u"][:ns, :n, j]
+        assert np.all(np.abs(at_saves - saved) <= 1e-9 * (np.abs(saved) + np.abs(saved).max() + 1e-300))
+
+
+def test_dense_eval_equals_the_saveat_interpolant():
+    # saveat changes no step, so sol(t) of a dense solve and the saveat values of a
+    # saveat solve evaluate the same polynomial (up to theta's rounding), except in
+    # the final step clipped to tf, where the saveat path interpolates with the
+    # unclipped dt that the reference restores before savevalues!
+    # (integrator_utils.jl:626-631)
+    N = 256
+    u0, p, ts = lorenz_inputs(N, seed=9)
+    sv = np.arange(1, 20) * 0.05
+    a = gpu("lorenz", "tsit5", u0, p, ts, sv, 1e-8, 1e-8)
+    b = gpu("lorenz", "tsit5", u0, p, ts, None, 1e-8, 1e-8, save_everystep=True, max_step_saves=4096, dense=True)
+    assert np.array_equal(a["stats"]["naccept"], b["stats"]["naccept"])
+    ev = dense_eval(b, sv)
+    last_start = b["t"][b["nsaved"] - 2, np.arange(N)]
+    inner = sv[:, None] <= last_start[None, :]
+    got = np.transpose(ev, (0, 2, 1))[inner]
+    want = np.transpose(a["u"][:sv.size], (0, 2, 1))[inner]
+    assert inner.sum() > 0.8 * inner.size
+    assert np.all(np.abs(got - want) <= 1e-12 * (np.abs(want) + 1.0))
+
+
+def test_mixed_dense_is_within_tolerance_of_fp64():
+    N = 256
+    u0, p, ts = robertson_inputs(N, seed=11)
+    rt, at = 1e-6, 1e-10
+    f = gpu("robertson", "rodas5p", u0, p, ts, None, rt, at, save_everystep=True, max_step_saves=4096, dense=True)
+    m = gpu("robertson", "rodas5p", u0, p, ts, None, rt, at, precision="mixed", save_everystep=True,
+            max_step_saves=4096, dense=True)
+    tq = 10.0 ** np.linspace(-4.0, 5.0, 40)
+    a, b = dense_eval(f, tq), dense_eval(m, tq)
+    assert np.all(np.isfinite(b))
+    ratio = np.abs(a - b) / (rt * np.abs(a) + at)
+    assert np.percentile(ratio, 99) < 20.0 and ratio.max() < 200.0, (np.percentile(ratio, 99), ratio.max())
+
+
+def test_dense_overflow_marks_the_last_interval():
+    # more steps than slots: the last slot keeps the final point with NaN vectors,
+    # so sol(t) in the last (gapped) interval is NaN and elsewhere exact
+    N = 64
+    u0, p, ts = lorenz_inputs(N, seed=8)
+    with pytest.warns(UserWarning, match="max_step_saves"):
+        g = gpu("lorenz", "tsit5", u0, p, ts, None, 1e-8, 1e-8, save_everystep=True, max_step_saves=5, dense=True)
+    assert (g["nsaved"] == 7).all()
+    assert np.isnan(g["k"][6]).all() and np.isfinite(g["k"][1:6]).all()
+    full = gpu("lorenz", "tsit5", u0, p, ts, None, 1e-8, 1e-8, save_everystep=True, max_step_saves=4096, dense=True)
+    tq = np.vstack([0.5 * (g["t"][2] + g["t"][3]), 0.5 * (g["t"][5] + g["t"][6])])
+    ev, ref = dense_eval(g, tq), dense_eval(full, tq)
+    assert np.array_equal(ev[0], ref[0])
+    assert np.isnan(ev[1]).all()
+
+
+def test_solution_call_uses_the_dense_interpolant():
+    from odegb300 import EnsembleGB300, EnsembleProblem, ODEProblem, Vern7, remake, solve
+    prob = ODEProblem("lorenz", [1.0, 0.0, 0.0], (0.0, 1.0), [10.0, 14.0, 8.0 / 3.0])
+    ep = EnsembleProblem(prob, prob_func=lambda pr, ctx: remake(pr, p=[10.0, 10.0 + ctx.sim_id, 8.0 / 3.0]))
+    sim = solve(ep, Vern7(), EnsembleGB300(), trajectories=6, reltol=1e-8, abstol=1e-8)   # no saveat: dense
+    sol = sim.u[3]
+    assert sol.dense
+    tq = np.array([0.0, 0.123, 0.5, 0.999, 1.0])
+    vals = sol(tq)
+    assert vals.shape == (5, 3) and np.allclose(sol(0.5), vals[2], rtol=0, atol=0)
+    o = O.solve(O.VERN7, O.LORENZ, np.array([1.0, 0.0, 0.0]), np.array([10.0, 14.0, 8.0 / 3.0]), (0.0, 1.0),
+                dense=True, reltol=1e-8, abstol=1e-8, saveat_given=False, save_everystep=True,
+                max_step_saves=4096, save_start=True, save_end=True)
+    ref = o["dense"](tq)
+    assert np.all(np.abs(vals - ref) <= 10 * (1e-8 * np.abs(ref) + 1e-8))
+    # with saveat the solution is not dense: linear interpolation between saves
+    sim2 = solve(ep, Vern7(), EnsembleGB300(), trajectories=2, saveat=0.5, reltol=1e-8, abstol=1e-8)
+    s2 = sim2.u[0]
+    assert not s2.dense and np.allclose(s2(0.25), 0.5 * (np.asarray(s2.u[0]) + np.asarray(s2.u[1])))

@@ -1,0 +1,78 @@
+"""GPU parity of Rosenbrock23 (lib/OrdinaryDiffEqRosenbrock/src/rosenbrock_perform_step.jl:34-146)
+against the CPU oracle, through the C ABI: saves within 10x the tolerance,
+accepted steps within 1, the W-method's counters (a fresh J and W on every
+attempt at the default max_jac_age = 1), the mixed form's accuracy against a
+ground-truth solve, and dense output.
+"""
+import numpy as np
+import pytest
+
+from gpu_common import (ROBER_SAVEAT, brusselator_inputs, compare, duffing_inputs, err_vs, gpu, lorenz_inputs,
+                        oracle, robertson_inputs, truth)
+
+pytestmark = pytest.mark.gpu
+
+
+def _inputs(model, N, seed=3):
+    if model == "robertson":
+        return robertson_inputs(N, seed=seed), ROBER_SAVEAT, 1e-4, 1e-8
+    if model == "lorenz":
+        return lorenz_inputs(N, seed=seed), 0.1, 1e-5, 1e-7
+    if model == "duffing_chain":
+        u0, p, ts, sv, _ = duffing_inputs(N, 2, seed=seed, tf_range=(1.0, 10.0))
+        return (u0, p, ts), sv, 1e-4, 1e-6
+    u0, p, ts = brusselator_inputs(N, cells=8, seed=seed)
+    return (u0, p, ts), np.linspace(1.25, 10.0, 8), 1e-4, 1e-7
+
+
+@pytest.mark.parametrize("model", ["robertson", "lorenz", "duffing_chain", "brusselator_1d"])
+def test_rosenbrock23_fp64_matches_oracle(model):
+    N = 256
+    (u0, p, ts), sv, rt, at = _inputs(model, N)
+    g = gpu(model, "rosenbrock23", u0, p, ts, sv, rt, at)
+    o = oracle(model, "rosenbrock23", u0, p, ts, sv, rt, at)
+    assert (g["retcode"] == 1).all()
+    c = compare(g, o, rt, at)
+    assert c["ok"] and c["steps_ok"], c
+    st = g["stats"]
+    att = st["naccept"] + st["nreject"]
+    # W-method at max_jac_age = 1: J and W on every attempt, three solves
+    assert np.array_equal(st["njacs"], att) and np.array_equal(st["nw"], att)
+    assert np.array_equal(st["nsolve"], 3 * att)
+    for k in ("nf", "njacs", "nw", "nsolve", "naccept", "nreject"):
+        assert np.abs(st[k] - o["stats"][k]).max() <= 16, k
+
+
+@pytest.mark.parametrize("model", ["robertson", "brusselator_1d"])
+def test_rosenbrock23_mixed_equal_accuracy(model):
+    N = 256
+    (u0, p, ts), sv, rt, at = _inputs(model, N, seed=7)
+    gmx = gpu(model, "rosenbrock23", u0, p, ts, sv, rt, at, precision="mixed")
+    g64 = gpu(model, "rosenbrock23", u0, p, ts, sv, rt, at)
+    assert (gmx["retcode"] == 1).all()
+    tr = truth(model, u0, p, ts, sv, stiff=True)
+    emx, e64 = err_vs(gmx, tr, rt, at), err_vs(g64, tr, rt, at)
+    for q in (50, 90):
+        a, b = np.percentile(emx, q), np.percentile(e64, q)
+        assert a <= 2.0 * b + 1.0, (q, a, b)
+
+
+def test_rosenbrock23_dense_and_everystep():
+    import pyoracle as O
+    from odegb300 import dense_eval
+    N = 64
+    u0, p, ts = robertson_inputs(N, seed=5)
+    rt, at = 1e-4, 1e-8
+    g = gpu("robertson", "rosenbrock23", u0, p, ts, None, rt, at, save_everystep=True, max_step_saves=4096,
+            dense=True)
+    o = oracle("robertson", "rosenbrock23", u0, p, ts, None, rt, at, save_everystep=True, max_step_saves=4096)
+    c = compare(g, o, rt, at)
+    assert c["ok"] and c["steps_ok"], c
+    assert g["k"].shape[1] == 2   # k1, k2
+    tq = 10.0 ** np.linspace(-5.0, 5.0, 33)
+    ev = dense_eval(g, tq)
+    for j in range(0, N, 9):
+        r = O.solve(O.ROSENBROCK23, O.ROBERTSON, u0[:, j], p[:, j], ts[:, j], dense=True, reltol=rt, abstol=at,
+                    saveat_given=False, save_everystep=True, max_step_saves=4096, save_start=True, save_end=True)
+        ref = r["dense"](tq)
+        assert np.all(np.abs(ev[:, :, j] - ref) <= 10 * (rt * np.abs(ref) + at)), j

@@ -44,6 +44,22 @@ def test_convergence_order(alg, order, ks):
         assert abs(slope - order) < 0.3, (slope, errs)
 
 
+# lib/OrdinaryDiffEqRosenbrock/test/ode_rosenbrock_tests.jl:18-35: Rosenbrock23 on
+# prob_ode_linear, fixed dts (1/2)^(6:-1:3) -> order 2 (atol 0.2); adaptive with the
+# default tolerances in fewer than 20 saves.
+def test_rosenbrock23_order_and_adaptivity():
+    errs = []
+    for k in (6, 5, 4, 3):
+        r = O.solve(O.ROSENBROCK23, O.LINEAR, [0.5], [1.01], (0.0, 1.0), saveat=[], saveat_given=False,
+                    dt=2.0 ** -k, adaptive=False)
+        errs.append(abs(r["u"][-1][0] - 0.5 * np.exp(1.01)))
+    slope = float(np.mean(np.diff(np.log2(errs))))
+    assert abs(slope - 2.0) < 0.2, (slope, errs)
+    r = O.solve(O.ROSENBROCK23, O.LINEAR, [0.5], [1.01], (0.0, 1.0), saveat=[], saveat_given=False,
+                save_everystep=True, max_step_saves=100, save_start=True)
+    assert r["retcode"] == O.RC_SUCCESS and len(r["t"]) < 20
+
+
 def test_vern9_ground_truth_matches_analytic():
     r = O.solve(O.VERN9, O.LINEAR, [0.5], [1.01], (0.0, 1.0), saveat=[], saveat_given=False,
                 reltol=1e-14, abstol=1e-14)
@@ -56,6 +72,7 @@ def test_vern9_ground_truth_matches_analytic():
     (O.TSIT5, 2.0e-6, 4.0e-6),
     (O.VERN7, 3.0e-9, 5.0e-9),
     (O.RODAS5P, 2.0e-5, 3.0e-5),
+    (O.ROSENBROCK23, 3.0e-3, 6.0e-3),   # ode_dense_tests.jl:452-453
 ])
 def test_dense_regression(alg, tol1d, tol2d):
     pts = np.arange(17) / 16.0
@@ -72,7 +89,7 @@ def test_dense_regression(alg, tol1d, tol2d):
 
 def test_interpolant_endpoint_consistency():
     # At theta = 1 every interpolant reproduces the step's end value.
-    for alg in (O.TSIT5, O.VERN7, O.RODAS5P):
+    for alg in (O.TSIT5, O.VERN7, O.RODAS5P, O.ROSENBROCK23):
         r = O.solve(alg, O.LORENZ, [1.0, 0.0, 0.0], [10.0, 20.0, 8 / 3], (0.0, 0.5), saveat=[],
                     saveat_given=False, dense=True, reltol=1e-6, abstol=1e-6)
         d = r["dense"]
@@ -82,7 +99,7 @@ def test_interpolant_endpoint_consistency():
 
 
 # test/InterfaceIII/stats_tests.jl:5-38: counting wrapper equals stats.nf.
-@pytest.mark.parametrize("alg", [O.TSIT5, O.VERN7, O.VERN9, O.RODAS5P])
+@pytest.mark.parametrize("alg", [O.TSIT5, O.VERN7, O.VERN9, O.RODAS5P, O.ROSENBROCK23])
 def test_nf_counts_rhs_calls(alg):
     O.rhs_calls(reset=True)
     r = O.solve(alg, O.LINEAR, [1.0, 1.0], [5.0], (0.0, 1.0), saveat=[], saveat_given=False)
@@ -91,12 +108,15 @@ def test_nf_counts_rhs_calls(alg):
     assert calls == r["stats"]["nf"]
     st = r["stats"]
     att = st["naccept"] + st["nreject"]
-    per = {O.TSIT5: 6, O.VERN7: 10, O.VERN9: 16, O.RODAS5P: 8}[alg]
-    base = 3 if alg == O.TSIT5 else 2
-    extra = st["njacs"] if alg == O.RODAS5P else 0
+    per = {O.TSIT5: 6, O.VERN7: 10, O.VERN9: 16, O.RODAS5P: 8, O.ROSENBROCK23: 2}[alg]
+    base = 3 if alg in (O.TSIT5, O.ROSENBROCK23) else 2   # FSAL methods evaluate f(u0) once more
+    extra = st["njacs"] if alg in (O.RODAS5P, O.ROSENBROCK23) else 0
     assert st["nf"] == base + per * att + extra
     if alg == O.RODAS5P:
         assert st["nsolve"] == 8 * att and st["nw"] == att
+    if alg == O.ROSENBROCK23:
+        # W-method with max_jac_age = 1: a fresh J and W on every attempt
+        assert st["nsolve"] == 3 * att and st["nw"] == att and st["njacs"] == att
 
 
 # test/InterfaceI/controllers.jl:29-50: exp(-100) with default and restricted qmax_first_step.
