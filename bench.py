@@ -14,7 +14,8 @@ inputs resident in HBM.  `e2e` is the same metric through the public
 host-buffer call (host->device copies and results back inside the timed region).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                    [--config robertson|lorenz|duffing|brusselator|robertson_ros23|lorenz_dense|serving]
+                    [--config robertson|lorenz|duffing|brusselator|robertson_ros23|lorenz_dense|
+                              bouncing_ball|van_der_pol|serving]
                     [--trajectories N]
 """
 import argparse
@@ -43,6 +44,11 @@ CONFIGS = {
                         "20 log-spaced saves", 100_000),
     "lorenz_dense": ("Lorenz, Tsit5, reltol=abstol=1e-8, tspan (0,1), dense output (every step with its "
                      "interpolation vectors), then sol(t) at 101 times for every trajectory", 10_000),
+    "van_der_pol": ("van der Pol oscillators, mu log-uniform in [1, 1000], AutoTsit5(Rosenbrock23()) (stiffness "
+                    "switching), reltol=abstol=1e-6, tspan (0,6), saveat 0.5", 100_000),
+    "bouncing_ball": ("bouncing balls with the model's ContinuousCallback (condition x, affect_neg! v <- -e v, "
+                      "half terminate! after t_stop), Tsit5, reltol=abstol=1e-6, tspan (0,10), saveat 0.25",
+                      1_000_000),
     "serving": ("open-loop Poisson request stream; each request 1-4096 trajectories (log-uniform) of Lorenz/Tsit5, "
                 "Robertson/Rodas5P or Brusselator-1D (8/16/32 cells)/Rodas5P, reltol 10^U(-8,-4)", 0),
 }
@@ -156,7 +162,8 @@ def workload(name, N, seed):
     if name == "lorenz_dense":   # no saveat: every step kept (the reference's dense default)
         return dict(W.lorenz(N, seed=seed), saveat=None, everystep=True, max_step_saves=DENSE_MAX_STEPS)
     return {"robertson": W.robertson, "lorenz": W.lorenz, "duffing": W.duffing,
-            "brusselator": W.brusselator}[name](N, seed=seed)
+            "brusselator": W.brusselator, "bouncing_ball": W.bouncing_ball,
+            "van_der_pol": W.van_der_pol}[name](N, seed=seed)
 
 
 DENSE_MAX_STEPS = 512   # step slots per trajectory of the dense workload (Lorenz at 1e-8 takes < 200)
@@ -169,9 +176,12 @@ def oracle_solve(wl, idx, nthreads=0, truth=False):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as O
     from odegb300.saveat import resolve_saveat
-    alg = {"tsit5": O.TSIT5, "vern7": O.VERN7, "rodas5p": O.RODAS5P, "rosenbrock23": O.ROSENBROCK23}[wl["alg"]]
+    alg = {"tsit5": O.TSIT5, "vern7": O.VERN7, "rodas5p": O.RODAS5P, "rosenbrock23": O.ROSENBROCK23,
+           "autotsit5_rosenbrock23": O.AUTOTSIT5_ROSENBROCK23}[wl["alg"]]
     model = {"lorenz": O.LORENZ, "robertson": O.ROBERTSON, "duffing_chain": O.DUFFING,
-             "brusselator_1d": O.BRUSSELATOR}[wl["model"]]
+             "brusselator_1d": O.BRUSSELATOR, "bouncing_ball": O.BOUNCING_BALL, "van_der_pol": O.VANDERPOL}[wl["model"]]
+    cb = wl.get("callback")
+    cbkw = dict(callback=True, interp_points=cb.interp_points, max_events=cb.max_events) if cb else {}
     ts = wl["tspan"][:, idx]
     sv = wl["saveat"]
     if isinstance(sv, np.ndarray) and sv.ndim == 2:
@@ -181,14 +191,16 @@ def oracle_solve(wl, idx, nthreads=0, truth=False):
     npt = wl.get("n_per_traj")
     rt, at = wl["reltol"], wl["abstol"]
     if truth:
-        stiff = wl["alg"] in ("rodas5p", "rosenbrock23")
+        stiff = wl["alg"] in ("rodas5p", "rosenbrock23", "autotsit5_rosenbrock23")
         alg, rt, at = (O.RODAS5P, 1e-12, 1e-16) if stiff else (O.VERN9, 1e-14, 1e-14)
+        if cb:   # events need a dense interpolant to locate them: Tsit5 at 1e-13
+            alg, rt, at = O.TSIT5, 1e-13, 1e-13
     return O.solve_ensemble(alg, model, wl["u0"][:, idx], wl["p"][:, idx], ts, spec.values, rt,
                             at, n_per_traj=None if npt is None else npt[idx], saveat_as_tstops=truth,
                             saveat_per_traj=spec.per_traj, save_start=spec.save_start, save_end=spec.save_end,
                             save_end_user=spec.save_end_user, saveat_given=spec.nsave > 0,
                             saveat_scalar=spec.scalar, save_everystep=spec.everystep,
-                            max_step_saves=spec.max_step_saves, nthreads=nthreads)
+                            max_step_saves=spec.max_step_saves, nthreads=nthreads, **cbkw)
 
 
 class Clocks:
@@ -273,7 +285,8 @@ def run_gb300(args, world, rank, local, dist):
     dev = torch.device("cuda", local)
     n, _ = wl["u0"].shape
     sv = resolve_saveat(wl["saveat"], wl["tspan"])
-    cap = sv.cap
+    cb = wl.get("callback")
+    cap = sv.cap + (2 * cb.max_events if cb else 0)
     npt = wl.get("n_per_traj")
     t_u0 = torch.from_numpy(np.ascontiguousarray(wl["u0"])).to(dev)
     t_p = torch.from_numpy(np.ascontiguousarray(wl["p"])).to(dev)
@@ -294,7 +307,7 @@ def run_gb300(args, world, rank, local, dist):
 
     def solve_device(prec):
         ens = odegb300.EnsembleGB300(precision=prec, ir_sweeps=wl.get("ir_sweeps", -1) if prec == "mixed" else -1)
-        o = _options(wl["reltol"], wl["abstol"], None, None, None, 1000000, sv, ens, None, None)
+        o = _options(wl["reltol"], wl["abstol"], None, None, None, 1000000, sv, ens, None, None, cb)
         d = _lib.ProblemDesc(model, alg.alg_id, n, wl["p"].shape[0], ens.prec_id(), 0)
         stream = C.c_void_p(work.cuda_stream)
         _lib.check(L.ode_solve_ensemble_device(h, C.byref(d), C.byref(o), N, ptr(t_npt), ptr(t_u0), ptr(t_p),
@@ -351,7 +364,8 @@ def run_gb300(args, world, rank, local, dist):
         rc = rc_out.cpu().numpy()
         attempts = int(st[:, 4].sum() + st[:, 5].sum())
         results[prec] = {"ms": ms, "times": times, "launches": nl, "attempts": attempts,
-                         "success": float((rc == 1).mean()), "u": u_out[:, :, sample].cpu().numpy(),
+                         "success": float(((rc == 1) | (rc == 7)).mean()), "u": u_out[:, :, sample].cpu().numpy(),
+                         "terminated_frac": float((rc == 7).mean()),
                          "naccept_mean": float(st[:, 4].mean()), "wall_s": wall}
 
     # Accuracy on a checked sample: against the FP64 oracle at the same tolerance,
@@ -393,7 +407,7 @@ def run_gb300(args, world, rank, local, dist):
     h_rc = torch.empty(N, dtype=torch.int32).pin_memory()
     h_st = torch.empty((N, 6), dtype=torch.int64).pin_memory()
     ens_e2e = odegb300.EnsembleGB300(precision=best, ir_sweeps=wl.get("ir_sweeps", -1) if best == "mixed" else -1)
-    o_e2e = _options(wl["reltol"], wl["abstol"], None, None, None, 1000000, sv, ens_e2e, None, None)
+    o_e2e = _options(wl["reltol"], wl["abstol"], None, None, None, 1000000, sv, ens_e2e, None, None, cb)
     d_e2e = _lib.ProblemDesc(model, alg.alg_id, n, wl["p"].shape[0], ens_e2e.prec_id(), 0)
     hp = lambda t, ty=C.c_double: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(ty)) if t is not None else None
 
@@ -605,7 +619,7 @@ def run_dense(args, world, rank, local, dist):
     l0 = launches()
     ms, wall_s = timed(solve)
     nl = launches() - l0
-    ev_ms, ev_wall = timed(evaluate)
+    ev_ms, ev_wall = timed(evaluate)   # saves staged on the device, results written in place
     clk = clocks.stop()
     st = h_st.numpy()
     ns = h_ns.numpy().astype(np.int64)

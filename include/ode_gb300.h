@@ -23,7 +23,8 @@
  *   tspan[j], tspan[N+j] t0 and tf of trajectory j          (2 x N)
  *   saveat[s] shared, or saveat[s*N + j] per trajectory     (nsave or nsave x N)
  *   t_out[s*N + j], u_out[(s*n_states + i)*N + j]           (cap x N, cap x n_states x N)
- * with cap = nsave + 2 save slots per trajectory (start and end saves).
+ * with cap = nsave + 2 save slots per trajectory (start and end saves), or
+ * max_step_saves + 2 with save_everystep, plus 2 * max_events with a callback.
  */
 #ifndef ODE_GB300_H
 #define ODE_GB300_H
@@ -42,7 +43,12 @@ typedef struct ode_handle ode_handle;
  * Rodas5P (lib/OrdinaryDiffEqRosenbrock/src/algorithms.jl:83-87),
  * Rosenbrock23 (lib/OrdinaryDiffEqRosenbrock/src/algorithms.jl:1-16,108-146, the
  * default max_jac_age = 1: a fresh J and W on every step attempt). */
-enum ode_alg { ODE_TSIT5 = 0, ODE_VERN7 = 1, ODE_RODAS5P = 2, ODE_ROSENBROCK23 = 3 };
+enum ode_alg {
+    ODE_TSIT5 = 0, ODE_VERN7 = 1, ODE_RODAS5P = 2, ODE_ROSENBROCK23 = 3,
+    ODE_AUTOTSIT5_ROSENBROCK23 = 4  /* AutoTsit5(Rosenbrock23()): Tsit5 with stiffness detection switching
+                                       to Rosenbrock23 (lib/OrdinaryDiffEqTsit5/src/algorithms.jl:27-33,
+                                       lib/OrdinaryDiffEqCore/src/composite_algs.jl; default AutoSwitch) */
+};
 
 /* Registered right-hand sides (with analytic Jacobians).  The reference takes
  * an arbitrary f(du,u,p,t); device code cannot call Julia closures, so models
@@ -52,7 +58,13 @@ enum ode_model {
     ODE_MODEL_LORENZ = 1,         /* n = 3, p = (sigma, rho, beta)                     */
     ODE_MODEL_ROBERTSON = 2,      /* n = 3, p = (k1, k2, k3)                           */
     ODE_MODEL_DUFFING_CHAIN = 3,  /* n = 2N, interleaved (x_i, v_i), p = (k, delta, beta) */
-    ODE_MODEL_BRUSSELATOR_1D = 4  /* n = 2*cells, interleaved (u_i, v_i), p = (A, B, alpha) */
+    ODE_MODEL_BRUSSELATOR_1D = 4, /* n = 2*cells, interleaved (u_i, v_i), p = (A, B, alpha) */
+    ODE_MODEL_VANDERPOL = 6,      /* n = 2 (x, y): x' = y, y' = mu ((1 - x^2) y - x); p = (mu)
+                                     (test/InterfaceI/stiffness_detection_test.jl:10-16) */
+    ODE_MODEL_BOUNCING_BALL = 5   /* n = 2 (x, v): x' = v, v' = -g; p = (g, e, t_stop).  Its
+                                     ContinuousCallback (ode_options.callback): condition x,
+                                     affect! = nothing, affect_neg!: terminate! once t >= t_stop,
+                                     else v <- -e v (test/Integrators_I/ode_event_tests.jl:100-113,283-360) */
 };
 
 /* FP64: every operation in double (the reference's arithmetic).
@@ -66,7 +78,8 @@ enum ode_precision { ODE_PREC_FP64 = 0, ODE_PREC_MIXED = 1 };
 enum ode_retcode {
     ODE_RC_DEFAULT = 0, ODE_RC_SUCCESS = 1, ODE_RC_MAXITERS = 2, ODE_RC_DTNAN = 3,
     ODE_RC_DTLESSTHANMIN = 4, ODE_RC_UNSTABLE = 5,
-    ODE_RC_ABORTED = 6 /* stopped by ode_abort(); no reference counterpart */
+    ODE_RC_ABORTED = 6, /* stopped by ode_abort(); no reference counterpart */
+    ODE_RC_TERMINATED = 7 /* a callback called terminate! (ReturnCode.Terminated) */
 };
 
 enum ode_status {
@@ -112,6 +125,13 @@ typedef struct {
                                    (integrator_utils.jl:397-404); needs nsave == 0 */
     int32_t max_step_saves;     /* save_everystep: step saves kept per trajectory; t_out/u_out hold
                                    max_step_saves + 2 slots, and past that the last slot keeps the latest step */
+    int32_t callback;           /* 1: the model's registered ContinuousCallback (models with an event;
+                                   SciMLBase defaults: rootfind = LeftRootFind, save_positions = (true, true),
+                                   abstol = 10eps(), repeat_nudge = 1//100, dtrelax = 1); not with dense output */
+    int32_t interp_points;      /* the callback's interp_points (default 10) */
+    int32_t max_events;         /* save slots for events: 2 per event (before and after its affect) are added to
+                                   the output, and past the total the last slot keeps the latest save */
+    int32_t reserved_options;
 } ode_options;
 
 /* Fill o with the reference's defaults. */
@@ -152,7 +172,8 @@ int ode_solve_ensemble_device(ode_handle* h, const ode_problem_desc* d, const od
  * stored per saved step, the method's interpolation data (integrator.k):
  * Tsit5 7 (k1..k7), Vern7 7 (k1, k4..k9: its interpolant and lazy extra
  * stages read no others), Rodas5P 3 (the dense k1..k3), Rosenbrock23 2 (k1,
- * k2).  ODE_E_INVALID for an unknown alg. */
+ * k2); 0 for AutoTsit5(Rosenbrock23()) (no dense output).  ODE_E_INVALID for an
+ * unknown alg. */
 int ode_dense_nk(int alg);
 
 /* Synchronous dense solve on HOST buffers: every accepted step is saved
@@ -176,7 +197,8 @@ int ode_solve_ensemble_dense(ode_handle* h, const ode_problem_desc* d, const ode
  * (ts[i+] - ts[i-]) and the method's interpolant with the vectors of the step
  * ending at ts[i+] (Vern7 first forms its extra stages from them).  Times
  * outside the saved range use the first or last step's polynomial, as
- * ode_interpolation does; a trajectory with nsaved 0 gets NaN. */
+ * ode_interpolation does; a trajectory with nsaved 0 gets NaN.  The saves are
+ * staged on the device; a page-locked `out` is written in place. */
 int ode_dense_eval(ode_handle* h, const ode_problem_desc* d, int64_t ntraj, const double* p,
                    const double* t_saved, const double* u_saved, const double* k_saved, const int32_t* nsaved,
                    int32_t cap, int32_t nq, const double* tq, int32_t tq_per_traj, double* out);

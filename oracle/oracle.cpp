@@ -95,9 +95,19 @@ double ctrl_pow(double x, double y) {
 //   benchmark/benchmarks.jl:243-247):
 //   u' = ((A + u*u*v) - (B+1)*u) + ae*lap(u),  v' = (B*u - u*u*v) + ae*lap(v).
 // Linear: u_i' = p0 * u_i (prob_ode_linear with p0 = 1.01, test/Regression_I/ode_dense_tests.jl:30-38).
+// Bouncing ball: x' = v, v' = -g (p = (g, e, t_stop); test/Integrators_I/ode_event_tests.jl:100-104),
+//   with its event below.
 void rhs(int model, int n, const double* u, const double* p, double t, double* du) {
     (void)t;
     switch (model) {
+    case ORC_BOUNCING_BALL:
+        du[0] = u[1];
+        du[1] = -p[0];
+        break;
+    case ORC_VANDERPOL:   // test/InterfaceI/stiffness_detection_test.jl:10-16: mu ((1 - x^2) y - x)
+        du[0] = u[1];
+        du[1] = p[0] * ((1.0 - u[0] * u[0]) * u[1] - u[0]);
+        break;
     case ORC_LINEAR:
         for (int i = 0; i < n; ++i) du[i] = p[0] * u[i];
         break;
@@ -147,6 +157,14 @@ void jac(int model, int n, const double* u, const double* p, double t, double* J
     (void)t;
     std::memset(J, 0, sizeof(double) * n * n);
     switch (model) {
+    case ORC_BOUNCING_BALL:
+        J[1] = 1.0;
+        break;
+    case ORC_VANDERPOL:
+        J[1] = 1.0;
+        J[2] = p[0] * (-2.0 * u[0] * u[1] - 1.0);
+        J[3] = p[0] * (1.0 - u[0] * u[0]);
+        break;
     case ORC_LINEAR:
         for (int i = 0; i < n; ++i) J[i * n + i] = p[0];
         break;
@@ -238,6 +256,20 @@ struct Integ {
     orc_stats st;
     Dense* dense;
     std::vector<double> interp_out;
+    // AutoTsit5(Rosenbrock23()): the composite's state (AutoSwitchCache,
+    // composite_algs.jl:55-94) and one PI controller state per method
+    int current;                 // 0 Tsit5, 1 Rosenbrock23
+    int as_count, successive_switches;
+    bool is_stiffalg, do_error_check;
+    double eigen_est;
+    double ctl_errold[2], ctl_q11[2];
+    std::vector<double> g6;
+    std::vector<int32_t> alg_choice;
+    // continuous callback state (integrator.event_last_time, last_event_error)
+    int event_last_time;
+    double last_event_error;
+    bool reeval_fsal, terminated;
+    std::vector<double> cb_tmp;
 };
 
 thread_local int64_t g_rhs_calls = 0;  // counts every RHS call (the reference's counting-wrapper tests)
@@ -324,6 +356,7 @@ void tsit5_step(Integ& I) {
             tmp[i] = std::fma(dt, acc, up[i]);
         }
         if (s < 7) {
+            if (s == 6 && I.alg == ORC_AUTOTSIT5_ROSENBROCK23) I.g6.assign(tmp, tmp + n);
             f_eval(I, tmp, std::fma(TSIT5_c[s], dt, t), k(s));
         } else {
             std::memcpy(I.u.data(), tmp, sizeof(double) * n);
@@ -332,6 +365,13 @@ void tsit5_step(Integ& I) {
     }
     std::memcpy(I.fsallast.data(), k(7), sizeof(double) * n);
     I.st.nf += 6;
+    if (I.alg == ORC_AUTOTSIT5_ROSENBROCK23) {
+        // stiffness estimate of a composite step (tsit_perform_step.jl:240-246, Hairer II p. 22,
+        // Inf norm): max_i |(k7 - k6) / (g7 - g6)|, NaN propagating like Julia's maximum
+        double e = 0.0;
+        for (int i = 0; i < n; ++i) e = jmax(e, std::fabs((k(7)[i] - k(6)[i]) / (I.u[i] - I.g6[i])));
+        I.eigen_est = e;
+    }
     if (I.o.adaptive) {
         for (int i = 0; i < n; ++i) {
             double acc = TSIT5_bt[7] * k(7)[i];
@@ -694,6 +734,10 @@ void ros23_interp(double th, double dt, const double* y0, const double* K, int n
 
 void do_step(Integ& I) {
     switch (I.alg) {
+    case ORC_AUTOTSIT5_ROSENBROCK23:   // perform_step!(::CompositeCache): the current method
+        if (I.current == 0) tsit5_step(I);
+        else rosenbrock23_step(I);
+        break;
     case ORC_TSIT5: tsit5_step(I); break;
     case ORC_VERN7: vern7_step(I); break;
     case ORC_VERN9: vern9_step(I); break;
@@ -704,7 +748,8 @@ void do_step(Integ& I) {
 
 void interpolate(Integ& I, double th, double* out) {
     int n = I.n;
-    switch (I.alg) {
+    const int alg = I.alg == ORC_AUTOTSIT5_ROSENBROCK23 ? (I.current == 0 ? ORC_TSIT5 : ORC_ROSENBROCK23) : I.alg;
+    switch (alg) {
     case ORC_TSIT5: tsit5_interp(th, I.dt, I.uprev.data(), I.k.data(), n, out); break;
     case ORC_VERN7:
         if (I.nk_valid < 16) {
@@ -722,11 +767,12 @@ void interpolate(Integ& I, double th, double* out) {
 }
 
 void push_save(Integ& I, double t, const double* v) {
-    const int slot = I.nsaved < I.cap ? I.nsaved : (I.o.save_everystep ? I.cap - 1 : -1);
+    const int slot = I.nsaved < I.cap ? I.nsaved : ((I.o.save_everystep || I.o.callback) ? I.cap - 1 : -1);
     if (slot >= 0) {
         if (I.t_out) I.t_out[slot] = t;
         if (I.u_out) std::memcpy(I.u_out + (size_t)slot * I.n, v, sizeof(double) * I.n);
     }
+    if (I.alg == ORC_AUTOTSIT5_ROSENBROCK23) I.alg_choice.push_back(I.current + 1);   // sol.alg_choice
     I.nsaved++;
     I.last_saved_t = t;
 }
@@ -811,14 +857,194 @@ void record_dense(Integ& I) {
     s.tend = I.t;
     s.y0 = I.uprev;
     s.y1 = I.u;
-    int nk = I.alg == ORC_TSIT5 ? 7 : I.alg == ORC_VERN7 ? 10 : I.alg == ORC_RODAS5P ? 3
-           : I.alg == ORC_ROSENBROCK23 ? 2 : 0;
+    const int alg = I.alg == ORC_AUTOTSIT5_ROSENBROCK23 ? (I.current == 0 ? ORC_TSIT5 : ORC_ROSENBROCK23) : I.alg;
+    int nk = alg == ORC_TSIT5 ? 7 : alg == ORC_VERN7 ? 10 : alg == ORC_RODAS5P ? 3 : alg == ORC_ROSENBROCK23 ? 2 : 0;
     s.k.assign(I.k.begin(), I.k.begin() + (size_t)nk * I.n);
     I.dense->steps.push_back(std::move(s));
 }
 
+// ---------------------------------------------------------------- callbacks
+// The models' registered ContinuousCallback (SciMLBase's ContinuousCallback, not
+// vendored; its defaults: interp_points = 10, rootfind = LeftRootFind,
+// save_positions = (true, true), abstol = 10eps(), repeat_nudge = 1//100,
+// dtrelax = 1).  Bouncing ball: condition u[1] (the height), affect! = nothing,
+// affect_neg!: terminate! once t >= p[3], else v = -e v (p[2] = e = 1 gives the
+// reference's ode_event_tests.jl:100-113 and 332-346 callbacks).
+constexpr double CB_ABSTOL = 10.0 * 2.220446049250313e-16;
+constexpr double CB_REPEAT_NUDGE = 0.01;
+
+bool model_has_event(int model) { return model == ORC_BOUNCING_BALL; }
+double event_condition(int model, const double* u) { (void)model; return u[0]; }
+bool event_has_affect(int) { return false; }
+bool event_has_affect_neg(int) { return true; }
+// affect (upcrossing) / affect_neg (downcrossing) on the integrator state; true: terminate!
+bool event_apply(Integ& I, bool upcrossing) {
+    (void)upcrossing;
+    if (I.t >= I.p[2]) return true;
+    I.u[1] = -I.p[1] * I.u[1];
+    return false;
+}
+
+inline double jsign(double x) { return x > 0 ? 1.0 : (x < 0 ? -1.0 : (x == 0 ? 0.0 : x)); }
+
+// get_condition (lib/DiffEqBase/src/callbacks.jl:91-137): u at t, uprev at tprev,
+// else the current step's interpolant at abst.
+double cond_at(Integ& I, double abst) {
+    const double* v;
+    if (abst == I.t) {
+        v = I.u.data();
+    } else if (abst == I.tprev) {
+        v = I.uprev.data();
+    } else {
+        interpolate(I, (abst - I.tprev) / I.dt, I.cb_tmp.data());
+        v = I.cb_tmp.data();
+    }
+    return event_condition(I.model, v);
+}
+
+// is_event_occurrence (callbacks.jl:525-530)
+bool is_event(const Integ& I, double bs, double ts) {
+    return ((bs < 0 && event_has_affect(I.model)) || (bs > 0 && event_has_affect_neg(I.model))) && bs * ts <= 0;
+}
+
+// find_root with LeftRootFind (callbacks.jl:480-492): the reference runs ModAB
+// (BracketingNonlinearSolve, not vendored) with abstol = reltol = 0, i.e. to
+// adjacent floats, and returns the left end (or a point where the condition is
+// exactly 0).  Bisection to adjacent floats ends at the same bracket.
+double find_root_left(Integ& I, double a, double b) {
+    const double fa = cond_at(I, a);
+    for (int it = 0; it < 2200; ++it) {
+        const double m = a + (b - a) * 0.5;
+        if (!(m > a && m < b)) break;
+        const double fm = cond_at(I, m);
+        if (fm == 0.0) return m;
+        if ((fm > 0) == (fa > 0)) a = m;
+        else b = m;
+    }
+    return a;
+}
+
+// find_callback_time(integrator, ::ContinuousCallback, idx) (callbacks.jl:364-412),
+// with nudge_tprev (:414-426) and check_event_occurrence (:428-458).
+bool find_callback_time(Integ& I, double& cb_t, double& bottom_sign, double& residual) {
+    double bottom_t = I.tprev;
+    double bc = cond_at(I, bottom_t);
+    if (I.event_last_time == 1) {
+        if (std::fabs(bc - I.last_event_error) <= CB_ABSTOL) bottom_t = I.tprev + I.dt * CB_REPEAT_NUDGE;
+        bc = cond_at(I, bottom_t);
+    }
+    const double bs = jsign(bc);
+    double top_t = I.t;
+    double ts = jsign(cond_at(I, top_t));
+    bool occ = is_event(I, bs, ts);
+    if (I.o.interp_points != 0 && !occ) {
+        // range(tprev, stop = t, length = interp_points)
+        const int m = I.o.interp_points;
+        for (int i = 2; i <= m; ++i) {
+            top_t = i == m ? I.t : I.tprev + (I.t - I.tprev) * ((double)(i - 1) / (double)(m - 1));
+            ts = jsign(cond_at(I, top_t));
+            occ = is_event(I, bs, ts);
+            if (occ) break;
+        }
+    }
+    bottom_sign = bs;
+    residual = 0.0;
+    if (!occ) {
+        cb_t = I.t;
+        return false;
+    }
+    if (ts == 0.0) {
+        cb_t = top_t;
+    } else {
+        cb_t = find_root_left(I, bottom_t, top_t);
+        residual = cond_at(I, cb_t);
+    }
+    return true;
+}
+
+// ode_addsteps!(integrator, f, always_calc_begin = true): the step's
+// interpolation data recomputed from (tprev, uprev) with the current dt
+// (reeval_internals_due_to_modification!, integrator_interface.jl:54-79).  The
+// reference does not count these evaluations; u, the error estimate and the
+// counters are kept.
+void recompute_step_k(Integ& I) {
+    const std::vector<double> u = I.u, fsf = I.fsalfirst, fsl = I.fsallast, ut = I.utilde, J = I.J;
+    const double EEst = I.EEst, t = I.t;
+    const orc_stats st = I.st;
+    const bool have_J = I.have_J;
+    I.t = I.tprev;
+    if (I.alg == ORC_TSIT5 || I.alg == ORC_ROSENBROCK23 || I.alg == ORC_AUTOTSIT5_ROSENBROCK23)
+        f_eval(I, I.uprev.data(), I.t, I.fsalfirst.data());
+    const double eig = I.eigen_est;
+    do_step(I);
+    I.eigen_est = eig;
+    I.u = u;
+    I.fsalfirst = fsf;
+    I.fsallast = fsl;
+    I.utilde = ut;
+    I.J = J;
+    I.have_J = have_J;
+    I.EEst = EEst;
+    I.t = t;
+    I.st = st;
+}
+
+// apply_callback! (callbacks.jl:557-643) for a ContinuousCallback.
+void apply_callback(Integ& I, double cb_t, double bottom_sign) {
+    if (I.o.adaptive) {   // set_proposed_dt! (integrator_interface.jl:180-182), dtrelax = 1
+        I.dtpropose = jmax(std::nextafter(I.o.dtmin, INFINITY), 1.0 * I.dt);
+        I.dtcache = I.dtpropose;
+    }
+    // change_t_via_interpolation! (integrator_interface.jl:5-40)
+    if (cb_t != I.t) {
+        interpolate(I, (cb_t - I.tprev) / I.dt, I.u.data());
+        I.t = cb_t;
+        I.dt = I.t - I.tprev;
+        recompute_step_k(I);
+        I.reeval_fsal = true;
+    }
+    // savevalues! with saveat up to the event, then the pre-affect save unless saved exactly
+    const int before = I.nsaved;
+    const double last_before = I.last_saved_t;
+    savevalues(I);
+    const bool savedexactly = I.nsaved > before && I.last_saved_t == I.t && !(last_before == I.t);
+    if (!savedexactly) push_save(I, I.t, I.u.data());
+    // affect! (upcrossing) or affect_neg! (downcrossing); a nothing affect makes no change
+    bool modified = false;
+    if (bottom_sign < 0 && event_has_affect(I.model)) {
+        I.terminated = event_apply(I, true);
+        modified = true;
+    } else if (bottom_sign > 0 && event_has_affect_neg(I.model)) {
+        I.terminated = event_apply(I, false);
+        modified = true;
+    }
+    if (modified) {
+        recompute_step_k(I);
+        I.reeval_fsal = true;
+        push_save(I, I.t, I.u.data());   // save_positions[2]
+    }
+}
+
+// handle_callbacks! (integrator_utils.jl:1081-1132) for one continuous callback.
+void handle_callbacks(Integ& I) {
+    if (!I.o.callback || !model_has_event(I.model)) {
+        savevalues(I);
+        return;
+    }
+    double cb_t, bs, residual;
+    if (find_callback_time(I, cb_t, bs, residual)) {
+        I.event_last_time = 1;
+        I.last_event_error = residual;
+        apply_callback(I, cb_t, bs);
+    } else {
+        I.event_last_time = 0;
+        savevalues(I);
+    }
+}
+
 // _loopfooter!: integrator_utils.jl:597-677.
 void loopfooter(Integ& I) {
+    I.do_error_check = true;   // _loopfooter! (integrator_utils.jl:597-599)
     double ttmp = I.t + I.dt;
     if (I.o.adaptive) {
         double q = stepsize_controller(I);
@@ -840,7 +1066,7 @@ void loopfooter(Integ& I) {
             dtp = jmax(std::fabs(dtp), dtmin_t(I));
             I.dtpropose = dtp;
             record_dense(I);
-            savevalues(I);
+            handle_callbacks(I);
         } else {
             I.st.nreject++;
         }
@@ -856,7 +1082,55 @@ void loopfooter(Integ& I) {
         I.accept_step = true;
         I.dtpropose = I.dt;
         record_dense(I);
-        savevalues(I);
+        handle_callbacks(I);
+    }
+}
+
+// Controller defaults of one method (alg_utils.jl:407-879): beta1 = 7/(10 order),
+// beta2 = 2/(5 order), qsteady_max 6/5 for the adaptive implicit family.
+void set_controller(Integ& I, int order, bool implicit) {
+    I.order = order;
+    I.beta2 = 2.0 / (5.0 * order);
+    I.beta1 = 7.0 / (10.0 * order);
+    I.qsteady_max = implicit ? 1.2 : 1.0;
+}
+
+// choose_algorithm! for AutoTsit5(Rosenbrock23()) (composite_perform_step.jl:181-221)
+// with its AutoSwitch choice function (composite_algs.jl:17-94; defaults maxstiffstep
+// 10, maxnonstiffstep 3, nonstifftol = stifftol = 9//10, dtfac 2, stiffalgfirst false,
+// switch_max 5).  The composite's controller is one PI controller per method
+// (CompositeController, controllers.jl:1263-1345): switching banks the old
+// method's controller state and resumes the new one's.
+void choose_algorithm(Integ& I) {
+    if (I.alg != ORC_AUTOTSIT5_ROSENBROCK23) return;
+    // is_stiff: |eigen_est dt / alg_stability_size(Tsit5)| with alg_stability_size(::Tsit5) = 3.5068
+    // (lib/OrdinaryDiffEqTsit5/src/alg_utils.jl:3); `stiffness <= 9//10` compares exactly,
+    // which for a double is `< 0.9` (0.9 lies above 9/10)
+    const double stiffness = std::fabs(I.eigen_est * I.dt / 3.5068);
+    const bool stiff = !(stiffness < 0.9);
+    if (!stiff) I.successive_switches++;
+    else I.successive_switches = 0;
+    I.do_error_check = (I.successive_switches > 5 || !stiff) || I.is_stiffalg;
+    I.as_count = stiff ? (I.as_count < 0 ? 1 : I.as_count + 1) : (I.as_count > 0 ? -1 : I.as_count - 1);
+    if (!I.is_stiffalg && I.as_count > 10) {
+        I.dt = I.dt * 2.0;
+        I.is_stiffalg = true;
+    } else if (I.is_stiffalg && I.as_count < -3) {
+        I.dt = I.dt / 2.0;
+        I.is_stiffalg = false;
+    }
+    const int next = I.is_stiffalg ? 1 : 0;
+    if (next != I.current) {
+        I.ctl_errold[I.current] = I.errold;
+        I.ctl_q11[I.current] = I.q11;
+        I.current = next;
+        I.errold = I.ctl_errold[next];
+        I.q11 = I.ctl_q11[next];
+        if (next == 0) set_controller(I, 5, false);
+        else set_controller(I, 2, true);
+        // initialize! of the method switched to: its FSAL value f(uprev, t)
+        f_eval(I, I.uprev.data(), I.t, I.fsalfirst.data());
+        I.st.nf += 1;
     }
 }
 
@@ -867,13 +1141,22 @@ void loopheader(Integ& I) {
             I.success_iter++;
             I.uprev = I.u;
             I.dt = I.dtpropose;
-            if (I.alg == ORC_TSIT5 || I.alg == ORC_ROSENBROCK23) I.fsalfirst = I.fsallast;
+            if (I.alg == ORC_TSIT5 || I.alg == ORC_ROSENBROCK23 || I.alg == ORC_AUTOTSIT5_ROSENBROCK23) {
+                if (I.reeval_fsal) {   // update_fsal! -> reset_fsal! (integrator_utils.jl:216-235,1326-1340)
+                    f_eval(I, I.u.data(), I.t, I.fsalfirst.data());
+                    I.st.nf += 1;
+                } else {
+                    I.fsalfirst = I.fsallast;
+                }
+            }
+            I.reeval_fsal = false;
             modify_dt_for_tstops(I);
         } else {
             I.dt = I.dt / jmin(1.0 / I.qmin, I.q11 / I.gamma);
         }
     }
     I.iter++;
+    choose_algorithm(I);
     fix_dt_at_bounds(I);
     modify_dt_for_tstops(I);
 }
@@ -927,7 +1210,19 @@ int solve_one(Integ& I, const double* u0) {
     I.fsallast.assign(n, 0.0);
     I.k.assign((size_t)16 * n, 0.0);
     I.interp_out.assign(n, 0.0);
-    if (I.alg == ORC_RODAS5P || I.alg == ORC_ROSENBROCK23) {
+    I.current = 0;   // AutoSwitch: stiffalgfirst = false -> Tsit5 first
+    I.as_count = 0;
+    I.successive_switches = 0;
+    I.is_stiffalg = false;
+    I.do_error_check = true;
+    I.eigen_est = 1.0;   // solve.jl:697
+    I.alg_choice.clear();
+    if (I.alg == ORC_AUTOTSIT5_ROSENBROCK23) {
+        I.ctl_errold[0] = I.ctl_errold[1] = I.qoldinit;
+        I.ctl_q11[0] = I.ctl_q11[1] = 1.0;
+        set_controller(I, 5, false);
+    }
+    if (I.alg == ORC_RODAS5P || I.alg == ORC_ROSENBROCK23 || I.alg == ORC_AUTOTSIT5_ROSENBROCK23) {
         I.J.assign((size_t)n * n, 0.0);
         I.W.assign((size_t)n * n, 0.0);
         I.dT.assign(n, 0.0);
@@ -949,9 +1244,14 @@ int solve_one(Integ& I, const double* u0) {
     I.errold = I.qoldinit;
     I.nsaved = 0;
     I.last_saved_t = NAN;
+    I.event_last_time = 0;
+    I.last_event_error = 0.0;
+    I.reeval_fsal = false;
+    I.terminated = false;
+    I.cb_tmp.assign(n, 0.0);
     std::memset(&I.st, 0, sizeof(I.st));
     if (I.o.save_start) push_save(I, I.t0, I.u.data());
-    if (I.alg == ORC_TSIT5 || I.alg == ORC_ROSENBROCK23) {
+    if (I.alg == ORC_TSIT5 || I.alg == ORC_ROSENBROCK23 || I.alg == ORC_AUTOTSIT5_ROSENBROCK23) {
         // initialize!: FSAL pre-start (tsit_perform_step.jl:293-307, rosenbrock_perform_step.jl:1-14)
         f_eval(I, I.u.data(), I.t, I.fsalfirst.data());
         I.st.nf += 1;
@@ -969,7 +1269,7 @@ int solve_one(Integ& I, const double* u0) {
         double first_tstop = I.tstops[I.itstop];
         while (I.t < first_tstop) {
             loopheader(I);
-            int e = check_error(I);
+            int e = I.do_error_check ? check_error(I) : ORC_RC_SUCCESS;   // solve.jl:909
             if (e != ORC_RC_SUCCESS) {
                 postamble(I);
                 return e;
@@ -978,6 +1278,10 @@ int solve_one(Integ& I, const double* u0) {
             if (!tiny) do_step(I);
             bool should_exit = I.next_step_tstop;
             loopfooter(I);
+            if (I.terminated) {   // terminate! (ReturnCode.Terminated); postamble as the reference's
+                postamble(I);
+                return ORC_RC_TERMINATED;
+            }
             if (I.itstop >= I.tstops.size() || should_exit) break;
         }
         // handle_tstop!: integrator_utils.jl:1290-1314
@@ -1001,7 +1305,7 @@ void setup(Integ& I, int alg, int model, int n, const double* p, double t0, doub
     I.o = *o;
     if (I.o.dtmax <= 0.0) I.o.dtmax = tf - t0;
     if (I.o.maxiters <= 0) I.o.maxiters = 1000000;
-    I.order = alg == ORC_VERN7 ? 7 : alg == ORC_VERN9 ? 9 : alg == ORC_ROSENBROCK23 ? 2 : 5;
+    I.order = alg == ORC_VERN7 ? 7 : alg == ORC_VERN9 ? 9 : alg == ORC_ROSENBROCK23 ? 2 : 5;   // composite: Tsit5's
     // controller defaults: lib/OrdinaryDiffEqCore/src/alg_utils.jl:407-879
     I.beta2 = 2.0 / (5.0 * I.order);
     I.beta1 = 7.0 / (10.0 * I.order);
@@ -1043,6 +1347,8 @@ void orc_jac(int model, int n, const double* u, const double* p, double t, doubl
     jac(model, n, u, p, t, J);
 }
 
+thread_local std::vector<int32_t> g_last_alg_choice;
+
 int orc_solve(int alg, int model, int n, const double* p, double t0, double tf, const double* u0,
               const orc_opts* o, const double* saveat, int nsave_in, const double* tstops, int ntstops,
               double* t_out, double* u_out, int cap, int32_t* retcode, orc_stats* st, void** dense_handle) {
@@ -1057,7 +1363,7 @@ int orc_solve(int alg, int model, int n, const double* p, double t0, double tf, 
         D->alg = alg;
         D->model = model;
         D->n = n;
-        int np = model == ORC_LINEAR ? 1 : 3;
+        int np = (model == ORC_LINEAR || model == ORC_VANDERPOL) ? 1 : 3;   // every other model has 3
         D->p.assign(p, p + np);
         I.dense = D;
         *dense_handle = D;
@@ -1065,7 +1371,14 @@ int orc_solve(int alg, int model, int n, const double* p, double t0, double tf, 
     int rc = solve_one(I, u0);
     if (retcode) *retcode = rc;
     if (st) *st = I.st;
+    g_last_alg_choice = I.alg_choice;
     return I.nsaved;
+}
+
+int orc_last_alg_choice(int32_t* out, int cap) {
+    const int m = (int)g_last_alg_choice.size() < cap ? (int)g_last_alg_choice.size() : cap;
+    for (int i = 0; i < m; ++i) out[i] = g_last_alg_choice[i];
+    return m;
 }
 
 int orc_dense_nsteps(void* h) { return h ? (int)((Dense*)h)->steps.size() : 0; }
@@ -1139,7 +1452,8 @@ int orc_solve_ensemble(int alg, int model, int nmax, const int32_t* n_per_traj, 
                        int32_t* nsaved, int32_t* retcode, orc_stats* stats, int nthreads) {
     if (nthreads <= 0) nthreads = (int)std::thread::hardware_concurrency();
     if (nthreads <= 0) nthreads = 1;
-    int cap = (o->save_everystep ? o->max_step_saves : nsave) + 2;  // saves plus possible start and end saves
+    // saves plus possible start and end saves, and two per event (before and after its affect)
+    int cap = (o->save_everystep ? o->max_step_saves : nsave) + 2 + (o->callback ? 2 * o->max_events : 0);
     std::atomic<int64_t> next(0);
     auto worker = [&]() {
         std::vector<double> uj(nmax), pj(np), sv(nsave > 0 ? nsave : 1), tl(cap), ul((size_t)cap * nmax);

@@ -19,11 +19,13 @@
 extern "C" {
 #endif
 
-enum { ORC_TSIT5 = 0, ORC_VERN7 = 1, ORC_RODAS5P = 2, ORC_VERN9 = 3, ORC_ROSENBROCK23 = 4 };
-enum { ORC_LINEAR = 0, ORC_LORENZ = 1, ORC_ROBERTSON = 2, ORC_DUFFING = 3, ORC_BRUSSELATOR = 4 };
+enum { ORC_TSIT5 = 0, ORC_VERN7 = 1, ORC_RODAS5P = 2, ORC_VERN9 = 3, ORC_ROSENBROCK23 = 4,
+       ORC_AUTOTSIT5_ROSENBROCK23 = 5 /* AutoTsit5(Rosenbrock23()) */ };
+enum { ORC_LINEAR = 0, ORC_LORENZ = 1, ORC_ROBERTSON = 2, ORC_DUFFING = 3, ORC_BRUSSELATOR = 4, ORC_BOUNCING_BALL = 5,
+       ORC_VANDERPOL = 6 };
 /* SciMLBase ReturnCode subset used by this path (numbering of the C ABI). */
 enum { ORC_RC_DEFAULT = 0, ORC_RC_SUCCESS = 1, ORC_RC_MAXITERS = 2, ORC_RC_DTNAN = 3,
-       ORC_RC_DTLESSTHANMIN = 4, ORC_RC_UNSTABLE = 5 };
+       ORC_RC_DTLESSTHANMIN = 4, ORC_RC_UNSTABLE = 5, ORC_RC_TERMINATED = 7 };
 
 typedef struct {
     int64_t nf, njacs, nw, nsolve, naccept, nreject;
@@ -47,6 +49,10 @@ typedef struct {
     int32_t save_everystep;   /* save every accepted step (integrator_utils.jl:397-404) */
     int32_t max_step_saves;   /* ensemble: slots are max_step_saves + 2; past them the last slot
                                  keeps the latest step (the library's behaviour) */
+    int32_t callback;         /* 1: the model's ContinuousCallback (ORC_BOUNCING_BALL) */
+    int32_t interp_points;    /* ContinuousCallback interp_points (SciMLBase default 10) */
+    int32_t max_events;       /* ensemble: 2 more save slots per event */
+    int32_t reserved;
 } orc_opts;
 
 /* Solve one trajectory.  saveat: nsave_in times in (t0, tf] sorted ascending.
@@ -78,6 +84,11 @@ int orc_solve_ensemble(int alg, int model, int nmax, const int32_t* n_per_traj, 
                        const orc_opts* o, const double* saveat, int nsave, int saveat_per_traj,
                        double* t_out, double* u_out, int32_t* nsaved, int32_t* retcode,
                        orc_stats* stats, int nthreads);
+
+/* Method chosen for each saved point of the last orc_solve of this thread
+ * (sol.alg_choice: 1 = Tsit5, 2 = Rosenbrock23 for AutoTsit5(Rosenbrock23())).
+ * Returns the count written (at most cap). */
+int orc_last_alg_choice(int32_t* out, int cap);
 
 /* Number of RHS calls made by this thread's solves (the reference's counting
  * wrapper, test/InterfaceIII/stats_tests.jl:5-13); reset when asked. */

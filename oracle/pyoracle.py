@@ -13,9 +13,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 
-TSIT5, VERN7, RODAS5P, VERN9, ROSENBROCK23 = 0, 1, 2, 3, 4
-LINEAR, LORENZ, ROBERTSON, DUFFING, BRUSSELATOR = 0, 1, 2, 3, 4
+TSIT5, VERN7, RODAS5P, VERN9, ROSENBROCK23, AUTOTSIT5_ROSENBROCK23 = 0, 1, 2, 3, 4, 5
+LINEAR, LORENZ, ROBERTSON, DUFFING, BRUSSELATOR, BOUNCING_BALL, VANDERPOL = 0, 1, 2, 3, 4, 5, 6
 RC_DEFAULT, RC_SUCCESS, RC_MAXITERS, RC_DTNAN, RC_DTLESSTHANMIN, RC_UNSTABLE = range(6)
+RC_TERMINATED = 7
 
 
 class Stats(C.Structure):
@@ -33,6 +34,7 @@ class Opts(C.Structure):
         ("save_end_user", C.c_int32), ("saveat_given", C.c_int32), ("saveat_scalar", C.c_int32),
         ("qmax_first_step", C.c_double), ("qmax", C.c_double), ("saveat_as_tstops", C.c_int32),
         ("save_everystep", C.c_int32), ("max_step_saves", C.c_int32),
+        ("callback", C.c_int32), ("interp_points", C.c_int32), ("max_events", C.c_int32), ("reserved", C.c_int32),
     ]
 
 
@@ -64,6 +66,8 @@ def lib():
                                          C.c_int64, dp, dp, dp, C.POINTER(Opts), dp, C.c_int, C.c_int,
                                          dp, dp, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                          C.POINTER(Stats), C.c_int]
+        L.orc_last_alg_choice.restype = C.c_int
+        L.orc_last_alg_choice.argtypes = [C.POINTER(C.c_int32), C.c_int]
         L.orc_rhs_calls.restype = C.c_int64
         L.orc_rhs_calls.argtypes = [C.c_int]
         L.orc_rhs.argtypes = [C.c_int, C.c_int, dp, dp, C.c_double, dp]
@@ -79,10 +83,11 @@ def _dp(a):
 def make_opts(reltol=1e-3, abstol=1e-6, dtmax=0.0, dtmin=0.0, dt=0.0, adaptive=True,
               maxiters=1000000, save_start=False, save_end=True, save_end_user=-1,
               saveat_given=True, saveat_scalar=False, qmax_first_step=0.0, qmax=0.0, saveat_as_tstops=False,
-              save_everystep=False, max_step_saves=0):
+              save_everystep=False, max_step_saves=0, callback=False, interp_points=10, max_events=0):
     return Opts(reltol, abstol, dtmax, dtmin, dt, int(adaptive), maxiters, int(save_start),
                 int(save_end), save_end_user, int(saveat_given), int(saveat_scalar),
-                qmax_first_step, qmax, int(saveat_as_tstops), int(save_everystep), int(max_step_saves))
+                qmax_first_step, qmax, int(saveat_as_tstops), int(save_everystep), int(max_step_saves),
+                int(callback), int(interp_points), int(max_events), 0)
 
 
 def solve(alg, model, u0, p, tspan, saveat=(), tstops=(), dense=False, **kw):
@@ -98,6 +103,8 @@ def solve(alg, model, u0, p, tspan, saveat=(), tstops=(), dense=False, **kw):
         cap = 4
     if kw.get("save_everystep"):
         cap = kw.get("max_step_saves", 0) + 2
+    if kw.get("callback"):
+        cap += 2 * max(kw.get("max_events", 0), 64)
     t_out = np.zeros(cap)
     u_out = np.zeros((cap, n))
     rc = C.c_int32(0)
@@ -112,6 +119,10 @@ def solve(alg, model, u0, p, tspan, saveat=(), tstops=(), dense=False, **kw):
     out = {"t": t_out[:ns].copy(), "u": u_out[:ns].copy(), "retcode": rc.value, "stats": st.as_dict()}
     if dense:
         out["dense"] = DenseSolution(h, n)
+    if alg == AUTOTSIT5_ROSENBROCK23:
+        ch = np.zeros(cap, dtype=np.int32)
+        m = L.orc_last_alg_choice(ch.ctypes.data_as(C.POINTER(C.c_int32)), cap)
+        out["alg_choice"] = ch[:m].copy()
     return out
 
 
@@ -156,7 +167,8 @@ def solve_ensemble(alg, model, u0, p, tspan, saveat, reltol, abstol, n_per_traj=
     sv = np.ascontiguousarray(saveat, dtype=np.float64)
     nmax, N = u0.shape
     nsave = sv.shape[0]
-    cap = (kw.get("max_step_saves", 0) if kw.get("save_everystep") else nsave) + 2
+    cap = (kw.get("max_step_saves", 0) if kw.get("save_everystep") else nsave) + 2 + \
+        (2 * kw.get("max_events", 0) if kw.get("callback") else 0)
     t_out = np.full((cap, N), np.nan)
     u_out = np.full((cap, nmax, N), np.nan)
     nsaved = np.zeros(N, dtype=np.int32)

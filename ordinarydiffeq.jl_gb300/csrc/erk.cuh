@@ -58,6 +58,7 @@ struct Tsit5Alg {
     template <class R, int C> struct Cache {
         R k[7][C];   // k1..k7; k1 is the FSAL value
         R tmp[C];
+        double eig;  // the stiffness estimate of the last step (composite steps only)
     };
     template <class R, int C> __device__ static R* fsal_slot(Cache<R, C>& c) { return c.tmp; }
 
@@ -79,13 +80,28 @@ struct Tsit5Alg {
     template <class R, int C> __device__ static void prepare_dense(Cache<R, C>&) {}
     template <class R, int C> __device__ static R* dense_slot(Cache<R, C>& c, int q) { return c.k[q]; }
 
+    // A callback moved or modified u: the FSAL value is f(u) again (update_fsal! ->
+    // reset_fsal!, integrator_utils.jl:216-235,1326-1340; one counted call).  k7
+    // becomes the next step's k1 when it starts.
     template <class Model, class R, int L, int C>
+    __device__ static void reset_fsal(Cache<R, C>& c, const R* u, const R*, const R* p, double t, const Group<L>& g,
+                                      StepStats& st) {
+        Model::template rhs<R, L, C>(c.k[6], u, p, t, g);
+        st.nf += 1;
+    }
+
+    // EIG: also the stiffness estimate of a composite step (tsit_perform_step.jl:
+    // 240-246, Hairer II p. 22 with the Inf norm): max_i |(k7 - k6) / (u - g6)|,
+    // g6 the sixth stage's input, NaN propagating like Julia's maximum.
+    template <class Model, class R, int L, int C, bool EIG = false>
     __device__ static typename Ctl<R>::T step(Cache<R, C>& c, R* u, R* ulo, const R* up, const R* uplo,
                                              const R* p, double t, double dt, R abstol, R reltol, long long, bool,
                                              const Group<L>& g, StepStats& st) {
+        static_assert(!EIG || L == 1, "the stiffness estimate is formed on one lane");
         using K = RK<Tsit5Tab, R, C>;
         const R d = (R)dt;
         R* tmp = c.tmp;
+        R g6[EIG ? C : 1];
         K::template stage<2>(tmp, c.k, d, up, uplo);
         Model::template rhs<R, L, C>(c.k[1], tmp, p, stage_time<Model>(Tsit5Tab::c(2), dt, t), g);
         K::template stage<3>(tmp, c.k, d, up, uplo);
@@ -95,12 +111,25 @@ struct Tsit5Alg {
         K::template stage<5>(tmp, c.k, d, up, uplo);
         Model::template rhs<R, L, C>(c.k[4], tmp, p, stage_time<Model>(Tsit5Tab::c(5), dt, t), g);
         K::template stage<6>(tmp, c.k, d, up, uplo);
+        if constexpr (EIG) {
+#pragma unroll
+            for (int i = 0; i < C; ++i) g6[i] = tmp[i];
+        }
         Model::template rhs<R, L, C>(c.k[5], tmp, p, stage_time<Model>(1.0, dt, t), g);
         K::weights(tmp, c.k, Tsit5Sol());
 #pragma unroll
         for (int i = 0; i < C; ++i) Acc<R>::update(u[i], ulo[i], d, tmp[i], up[i], uplo[i]);
         Model::template rhs<R, L, C>(c.k[6], u, p, stage_time<Model>(1.0, dt, t), g);
         st.nf += 6;
+        if constexpr (EIG) {
+            double e = 0.0;
+#pragma unroll
+            for (int i = 0; i < C; ++i) {
+                const double v = fabs((double)(c.k[6][i] - c.k[5][i]) / (double)(u[i] - g6[i]));
+                e = (e != e || v != v) ? dnan() : (v > e ? v : e);
+            }
+            c.eig = e;
+        }
         K::weights(tmp, c.k, Tsit5Err());
 #pragma unroll
         for (int i = 0; i < C; ++i) tmp[i] = d * tmp[i];
@@ -108,7 +137,7 @@ struct Tsit5Alg {
     }
 
     template <class Model, class R, int L, int C>
-    __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, typename Ctl<R>::T th, double dt, double,
+    __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, double th, double dt, double,
                                        const R* y0, const R* y0lo, const R*, const R*, const R*, const Group<L>&) {
         auto r = [](int i, int q) { return tab::TSIT5_R(i, q); };
         const R d = (R)dt;
@@ -214,8 +243,13 @@ struct Vern7Alg {
         c.extra = true;
     }
 
+    // not FSAL (isfsal(::Vern7) = false): nothing to redo after a callback
     template <class Model, class R, int L, int C>
-    __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, typename Ctl<R>::T th, double dt,
+    __device__ static void reset_fsal(Cache<R, C>&, const R*, const R*, const R*, double, const Group<L>&,
+                                      StepStats&) {}
+
+    template <class Model, class R, int L, int C>
+    __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, double th, double dt,
                                        double tprev, const R* y0, const R* y0lo, const R*, const R*, const R* p,
                                        const Group<L>& g) {
         if (!c.extra) extra_stages<Model, R, L, C>(c, tprev, dt, y0, y0lo, p, g);

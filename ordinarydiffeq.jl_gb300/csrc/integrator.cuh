@@ -30,10 +30,23 @@
 #include "common.cuh"
 #include "ode_kernels.h"
 
+#include <type_traits>
+
 namespace odegb {
 
 enum RetCode { RC_DEFAULT = 0, RC_SUCCESS = 1, RC_MAXITERS = 2, RC_DTNAN = 3, RC_DTLESSTHANMIN = 4,
-               RC_UNSTABLE = 5, RC_ABORTED = 6 };
+               RC_UNSTABLE = 5, RC_ABORTED = 6, RC_TERMINATED = 7 };
+
+// Composite methods (AutoSwitchAlg) declare COMPOSITE; the loop then runs their
+// choice function and keeps one controller state per method.
+template <class A, class = void> struct is_composite_alg : std::false_type {};
+template <class A> struct is_composite_alg<A, std::void_t<decltype(A::COMPOSITE)>> : std::true_type {};
+
+// sign() with Julia's NaN behaviour
+__device__ __forceinline__ double dsign(double x) { return x > 0.0 ? 1.0 : (x < 0.0 ? -1.0 : (x == 0.0 ? 0.0 : x)); }
+// ContinuousCallback defaults (SciMLBase): abstol = 10eps(), repeat_nudge = 1//100
+constexpr double kCbAbstol = 10.0 * 2.220446049250313e-16;
+constexpr double kCbRepeatNudge = 0.01;
 
 struct StepStats {
     long long nf, njacs, nw, nsolve, naccept, nreject;
@@ -249,8 +262,10 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
     const double dtmax = a.dtmax > 0 ? a.dtmax : tf - t0;
     const R abstol = (R)a.abstol, reltol = (R)a.reltol;
     const Ctrl K = make_ctrl<Alg::ORDER, Alg::IMPLICIT>(a);
-    const CT beta1 = (CT)K.beta1, beta2 = (CT)K.beta2, gam = (CT)K.gamma, qmin_inv = (CT)K.qmin_inv;
-    const CT qoldinit = (CT)K.qoldinit, qsteady_max = (CT)K.qsteady_max;
+    // beta1, beta2 and qsteady_max change with a composite's current method
+    CT beta1 = (CT)K.beta1, beta2 = (CT)K.beta2, qsteady_max = (CT)K.qsteady_max;
+    const CT gam = (CT)K.gamma, qmin_inv = (CT)K.qmin_inv;
+    const CT qoldinit = (CT)K.qoldinit;
     const CT inv_qmax = (CT)(1.0 / K.qmax), inv_qmax_first = (CT)(1.0 / K.qmax_first);
 
     typename Alg::template Cache<R, C> cache;
@@ -261,7 +276,7 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
 
     auto save_point = [&](double ts, const R* v, const R* vlo) {
         // past the capacity, step saves keep the latest point in the last slot
-        const int slot = nsaved < a.nsave_cap ? nsaved : (a.save_everystep ? a.nsave_cap - 1 : -1);
+        const int slot = nsaved < a.nsave_cap ? nsaved : ((a.save_everystep || a.callback) ? a.nsave_cap - 1 : -1);
         if (slot >= 0) {
             if (g.lane == 0 && a.t_out) a.t_out[(size_t)slot * N + j] = ts;
 #pragma unroll
@@ -315,9 +330,147 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
     }
     double dtpropose = dt;
     CT EEst = CT(1), q11 = CT(1), errold = qoldinit;
+    CT bank_errold = qoldinit, bank_q11 = CT(1);   // composite: the other method's controller state
+    bool do_error_check = true;
     long long iter = 0, success_iter = 0;
     bool accept = false, next_tstop = false;
     int rc = RC_DEFAULT;
+
+    // _savevalues! (integrator_utils.jl:340-414) after an accepted step: saveat
+    // points up to t by the step's interpolant, then the every-step save; true
+    // when a save landed exactly on t (its `savedexactly`)
+    // y1/y1lo: the accepted step's end state, which the stiff-aware Rosenbrock
+    // interpolant reads (u itself, unless an event has moved u off the step's end)
+    auto savevalues = [&](const R* y1, const R* y1lo) -> bool {
+        bool exact = false;
+        while (isave < a.nsave) {
+            double curt = saveat_at(isave);
+            if (!dle(curt, t)) break;
+            isave++;
+            if (!deq(curt, t)) {
+                const double th = (double)Ctl<R>::theta(curt - tprev, dt);
+                R out[C], outlo[C];
+                Alg::template interpolate<Model, R, L, C>(cache, out, outlo, th, dt, tprev, uprev, uprevlo, y1, y1lo,
+                                                          p, g);
+                save_point(curt, out, outlo);
+            } else {
+                if (deq(curt, tf) && !a.save_end) continue;
+                save_point(t, u, ulo);
+                exact = true;
+            }
+        }
+        // save_everystep (integrator_utils.jl:397-404): the accepted step, unless it
+        // repeats the last save or is tf with save_end off
+        if (a.save_everystep &&
+            (nsaved == 0 || ((!deq(t, last_saved_t) || abs_bits(dt) == 0) && (a.save_end || !deq(t, tf))))) {
+            if (a.k_out) save_dense(true);
+            save_point(t, u, ulo);
+            exact = true;
+        }
+        return exact;
+    };
+
+    // The model's ContinuousCallback after an accepted step: handle_callbacks!
+    // (integrator_utils.jl:1081-1132) with find_callback_time, nudge_tprev,
+    // check_event_occurrence and apply_callback! (lib/DiffEqBase/src/callbacks.jl:
+    // 364-458, 557-643).  The event time is the left end of the sign change to
+    // adjacent floats (LeftRootFind; the reference's ModAB runs with abstol =
+    // reltol = 0); the condition between tprev and t comes from the step's
+    // interpolant.  After moving to the event the reference recomputes the step's
+    // interpolation data for the shortened step before saving the saveat points
+    // that precede the event; here those points come from the accepted step's own
+    // interpolant (the two differ by the local error).  Returns true when an event
+    // was applied (its saves made).
+    bool ev_last = false, terminated = false;
+    double last_event_error = 0.0;
+    auto handle_event = [&]() -> bool {
+        if constexpr (Model::HAS_EVENT) {
+            auto cond_at = [&](double abst) -> double {
+                if (abst == t) return Model::template event_condition<R, L, C>(u, ulo, g);
+                if (abst == tprev) return Model::template event_condition<R, L, C>(uprev, uprevlo, g);
+                R v[C], vlo[C];
+                Alg::template interpolate<Model, R, L, C>(cache, v, vlo, (abst - tprev) / dt, dt, tprev, uprev,
+                                                          uprevlo, u, ulo, p, g);
+                return Model::template event_condition<R, L, C>(v, vlo, g);
+            };
+            auto is_event = [](double bs, double ts) {
+                return ((bs < 0.0 && Model::EVENT_AFFECT_POS) || (bs > 0.0 && Model::EVENT_AFFECT_NEG)) &&
+                       bs * ts <= 0.0;
+            };
+            double bottom_t = tprev;
+            double bc = cond_at(bottom_t);
+            if (ev_last) {   // nudge_tprev: still at the last event's root -> look from just past it
+                if (fabs(bc - last_event_error) <= kCbAbstol) bottom_t = tprev + dt * kCbRepeatNudge;
+                bc = cond_at(bottom_t);
+            }
+            const double bs = dsign(bc);
+            double top_t = t;
+            double ts = dsign(cond_at(top_t));
+            bool occ = is_event(bs, ts);
+            if (a.interp_points != 0 && !occ) {   // range(tprev, stop = t, length = interp_points)
+                const int m = a.interp_points;
+                for (int i = 2; i <= m; ++i) {
+                    top_t = i == m ? t : tprev + (t - tprev) * ((double)(i - 1) / (double)(m - 1));
+                    ts = dsign(cond_at(top_t));
+                    occ = is_event(bs, ts);
+                    if (occ) break;
+                }
+            }
+            if (!occ) {
+                ev_last = false;
+                return false;
+            }
+            double cb_t = top_t, residual = 0.0;
+            if (ts != 0.0) {
+                double lo = bottom_t, hi = top_t;
+                for (int it = 0; it < 2200; ++it) {
+                    const double mid = lo + (hi - lo) * 0.5;
+                    if (!(mid > lo && mid < hi)) break;
+                    const double fm = cond_at(mid);
+                    if (fm == 0.0) {
+                        lo = mid;
+                        break;
+                    }
+                    if ((fm > 0.0) == (bs > 0.0)) lo = mid;
+                    else hi = mid;
+                }
+                cb_t = lo;
+                residual = cond_at(cb_t);
+            }
+            ev_last = true;
+            last_event_error = residual;
+            // apply_callback!: set_proposed_dt! (dtrelax = 1)
+            dtpropose = pmax(nextafter(a.dtmin, (double)INFINITY), dt);
+            // change_t_via_interpolation!  (the step's end state stays for the saveat
+            // points before the event)
+            const bool moved = cb_t != t;
+            R uend[C], uendlo[C];
+#pragma unroll
+            for (int c = 0; c < C; ++c) { uend[c] = u[c]; uendlo[c] = ulo[c]; }
+            if (moved) {
+                R v[C], vlo[C];
+                Alg::template interpolate<Model, R, L, C>(cache, v, vlo, (cb_t - tprev) / dt, dt, tprev, uprev,
+                                                          uprevlo, u, ulo, p, g);
+#pragma unroll
+                for (int c = 0; c < C; ++c) { u[c] = v[c]; ulo[c] = vlo[c]; }
+                t = cb_t;
+            }
+            // saveat up to the event, then the pre-affect save unless one landed on t
+            if (!savevalues(uend, uendlo)) save_point(t, u, ulo);
+            bool modified = false;
+            if (bs < 0.0 && Model::EVENT_AFFECT_POS) {
+                terminated = Model::template event_affect<R, L, C>(u, ulo, a.p + j, N, t, true, g);
+                modified = true;
+            } else if (bs > 0.0 && Model::EVENT_AFFECT_NEG) {
+                terminated = Model::template event_affect<R, L, C>(u, ulo, a.p + j, N, t, false, g);
+                modified = true;
+            }
+            if (modified) save_point(t, u, ulo);   // save_positions[2]
+            if (!terminated && (moved || modified)) Alg::template reset_fsal<Model, R, L, C>(cache, u, ulo, p, t, g, st);
+            return true;
+        }
+        return false;
+    };
 
     while (t < tf) {
         // ---- loopheader!
@@ -339,6 +492,26 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             }
         }
         iter++;
+        if constexpr (is_composite_alg<Alg>::value) {
+            // choose_algorithm! (integrator_utils.jl:120-121): on a switch the controller
+            // state of the method left is banked and the other's resumed
+            // (CompositeController), then the new method is initialised
+            if (Alg::choose(cache, dt, do_error_check)) {
+                const int cur = cache.current;
+                const CT e_old = errold, q_old = q11;   // swap with the other method's state
+                errold = bank_errold;
+                q11 = bank_q11;
+                bank_errold = e_old;
+                bank_q11 = q_old;
+                using NSA = typename Alg::NonStiff;
+                using SA = typename Alg::Stiff;
+                const Ctrl K2 = cur == 0 ? make_ctrl<NSA::ORDER, NSA::IMPLICIT>(a) : make_ctrl<SA::ORDER, SA::IMPLICIT>(a);
+                beta1 = (CT)K2.beta1;
+                beta2 = (CT)K2.beta2;
+                qsteady_max = (CT)K2.qsteady_max;
+                Alg::template enter<Model, R, L, C>(cache, uprev, uprevlo, p, t, g, st);
+            }
+        }
         // fix_dt_at_bounds!
         dt = pmin(dtmax, dt);
         dt = pmax(dt, pabs(pmax(peps(t), a.dtmin)));
@@ -349,11 +522,13 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             next_tstop = !plt(orig + tol, dist);
             dt = pmin(orig, dist);
         }
-        // ---- check_error (de_check_error)
+        // ---- check_error (de_check_error), unless a composite's stiffness test
+        // turned it off for this step (solve.jl:909)
         {
             int e = RC_SUCCESS;
             const long long db = __double_as_longlong(dt);
-            if (bits_nan(db)) e = RC_DTNAN;
+            if (!do_error_check) e = RC_SUCCESS;
+            else if (bits_nan(db)) e = RC_DTNAN;
             else if (iter > a.maxiters) e = RC_MAXITERS;
             else if (ple(pabs(dt), pabs(a.dtmin)) && (!accept || t + dt < tf)) e = RC_DTLESSTHANMIN;
             else if (!accept && ple(pabs(dt), peps(t))) e = RC_UNSTABLE;
@@ -373,6 +548,7 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
                                                       EEst > CT(1), g, st);
         }
         // ---- loopfooter!
+        if constexpr (is_composite_alg<Alg>::value) do_error_check = true;
         const double ttmp = t + dt;
         const CT inv_qmaxc = success_iter == 0 ? inv_qmax_first : inv_qmax;
         CT q;
@@ -401,30 +577,17 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             const double dtnew = Ctl<R>::scale_dt(dt, q);
             const double dtp = pmin(pabs(dtmax), pabs(dtnew));
             dtpropose = pmax(pabs(dtp), pabs(pmax(peps(t), a.dtmin)));
-            // ---- savevalues!
-            while (isave < a.nsave) {
-                double curt = saveat_at(isave);
-                if (!dle(curt, t)) break;
-                isave++;
-                if (!deq(curt, t)) {
-                    const CT th = Ctl<R>::theta(curt - tprev, dt);
-                    R out[C], outlo[C];
-                    Alg::template interpolate<Model, R, L, C>(cache, out, outlo, th, dt, tprev, uprev, uprevlo, u,
-                                                              ulo, p, g);
-                    save_point(curt, out, outlo);
-                } else {
-                    if (deq(curt, tf) && !a.save_end) continue;
-                    save_point(t, u, ulo);
-                }
+            // ---- handle_callbacks! / savevalues!
+            bool handled = false;
+            if constexpr (Model::HAS_EVENT) {
+                if (a.callback) handled = handle_event();
             }
-            // save_everystep (_savevalues!, integrator_utils.jl:397-404): the accepted
-            // step, unless it repeats the last save or is tf with save_end off
-            if (a.save_everystep &&
-                (nsaved == 0 || ((!deq(t, last_saved_t) || abs_bits(dt) == 0) && (a.save_end || !deq(t, tf))))) {
-                if (a.k_out) save_dense(true);
-                save_point(t, u, ulo);
-            }
+            if (!handled) savevalues(u, ulo);
             Alg::template after_save<R, C>(cache);
+            if (terminated) {   // terminate! (ReturnCode.Terminated)
+                rc = RC_TERMINATED;
+                break;
+            }
         } else {
             st.nreject++;
         }

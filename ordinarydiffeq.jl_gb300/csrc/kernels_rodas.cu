@@ -13,6 +13,8 @@ namespace odegb {
 #define BOTH(MODEL, MID, L, C) VAR(MODEL, MID, double, 0, L, C), VAR(MODEL, MID, float, 1, L, C)
 
 static const KernelVariant kVariants[] = {
+    BOTH(BouncingBall, M_BOUNCING_BALL, 1, 2),
+    BOTH(VanDerPol, M_VANDERPOL, 1, 2),
     BOTH(Linear, M_LINEAR, 1, 1), BOTH(Linear, M_LINEAR, 1, 2),
     BOTH(Lorenz, M_LORENZ, 1, 3), BOTH(Robertson, M_ROBERTSON, 1, 3),
     BOTH(Duffing, M_DUFFING, 1, 4),

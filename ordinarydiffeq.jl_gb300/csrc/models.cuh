@@ -19,11 +19,73 @@
 
 namespace odegb {
 
-enum ModelId { M_LINEAR = 0, M_LORENZ = 1, M_ROBERTSON = 2, M_DUFFING = 3, M_BRUSSELATOR = 4 };
+enum ModelId { M_LINEAR = 0, M_LORENZ = 1, M_ROBERTSON = 2, M_DUFFING = 3, M_BRUSSELATOR = 4, M_BOUNCING_BALL = 5,
+               M_VANDERPOL = 6 };
+
+// The van der Pol oscillator of the reference's stiffness-detection test
+// (test/InterfaceI/stiffness_detection_test.jl:10-16): u = (x, y), x' = y,
+// y' = mu ((1 - x^2) y - x), p = (mu).
+struct VanDerPol {
+    static constexpr int NP = 1;
+    static constexpr bool AUTONOMOUS = true;
+    static constexpr bool HAS_EVENT = false;
+    template <class R, int L, int C>
+    __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>&) {
+        static_assert(L == 1 && C == 2, "van der Pol has 2 states on one lane");
+        du[0] = u[1];
+        du[1] = p[0] * ((R(1) - u[0] * u[0]) * u[1] - u[0]);
+    }
+    template <class R, int N>
+    __device__ static void jac(R (*J)[N], const R* u, const R* p, double) {
+        J[0][0] = R(0);
+        J[0][1] = R(1);
+        J[1][0] = p[0] * (R(-2) * u[0] * u[1] - R(1));
+        J[1][1] = p[0] * (R(1) - u[0] * u[0]);
+    }
+};
+
+// A ball under gravity with its registered ContinuousCallback (the reference's
+// event tests, test/Integrators_I/ode_event_tests.jl:100-113 and 283-360):
+// u = (x, v), x' = v, v' = -g; p = (g, e, t_stop).  Callback: condition x,
+// affect! = nothing, affect_neg!: terminate! once t >= t_stop, else v <- -e v.
+struct BouncingBall {
+    static constexpr int NP = 3;
+    static constexpr bool AUTONOMOUS = true;
+    static constexpr bool HAS_EVENT = true;
+    static constexpr bool EVENT_AFFECT_POS = false;   // affect! = nothing
+    static constexpr bool EVENT_AFFECT_NEG = true;    // affect_neg!
+    template <class R, int L, int C>
+    __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>&) {
+        static_assert(L == 1 && C == 2, "the ball has 2 states on one lane");
+        du[0] = u[1];
+        du[1] = -p[0];
+    }
+    template <class R, int N>
+    __device__ static void jac(R (*J)[N], const R*, const R*, double) {
+        J[0][0] = R(0); J[0][1] = R(1);
+        J[1][0] = R(0); J[1][1] = R(0);
+    }
+    // condition(u, t, integrator) = u[1] (the height), in FP64 from the state pair
+    template <class R, int L, int C>
+    __device__ static double event_condition(const R* u, const R* ulo, const Group<L>&) {
+        return (double)u[0] + (double)ulo[0];
+    }
+    // the affect for a crossing from below (upcrossing) or above; true: terminate!
+    template <class R, int L, int C>
+    __device__ static bool event_affect(R* u, R* ulo, const double* p, long long stride, double t, bool,
+                                        const Group<L>&) {
+        if (t >= p[2 * stride]) return true;
+        const double v = -p[stride] * ((double)u[1] + (double)ulo[1]);
+        u[1] = (R)v;
+        ulo[1] = (R)(v - (double)u[1]);
+        return false;
+    }
+};
 
 struct Linear {
     static constexpr int NP = 1;
     static constexpr bool AUTONOMOUS = true;   // f(u, p) does not read t
+    static constexpr bool HAS_EVENT = false;   // no registered callback
     template <class R, int L, int C>
     __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>&) {
 #pragma unroll
@@ -41,6 +103,7 @@ struct Linear {
 struct Lorenz {
     static constexpr int NP = 3;
     static constexpr bool AUTONOMOUS = true;   // f(u, p) does not read t
+    static constexpr bool HAS_EVENT = false;   // no registered callback
     template <class R, int L, int C>
     __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>&) {
         static_assert(L == 1 && C == 3, "Lorenz has 3 states on one lane");
@@ -59,6 +122,7 @@ struct Lorenz {
 struct Robertson {
     static constexpr int NP = 3;
     static constexpr bool AUTONOMOUS = true;   // f(u, p) does not read t
+    static constexpr bool HAS_EVENT = false;   // no registered callback
     template <class R, int L, int C>
     __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>&) {
         static_assert(L == 1 && C == 3, "Robertson has 3 states on one lane");
@@ -87,6 +151,7 @@ __device__ __forceinline__ void chain_halo(const R* u, const Group<L>& g, int of
 struct Duffing {
     static constexpr int NP = 3;
     static constexpr bool AUTONOMOUS = true;   // f(u, p) does not read t
+    static constexpr bool HAS_EVENT = false;   // no registered callback
     template <class R, int L, int C>
     __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>& g) {
         static_assert(C % 2 == 0, "Duffing lanes hold whole (x, v) pairs");
@@ -125,6 +190,7 @@ struct Duffing {
 struct Brusselator {
     static constexpr int NP = 3;
     static constexpr bool AUTONOMOUS = true;   // f(u, p) does not read t
+    static constexpr bool HAS_EVENT = false;   // no registered callback
     template <class R, int L, int C>
     __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>& g) {
         static_assert(C % 2 == 0, "Brusselator lanes hold whole (u, v) cells");

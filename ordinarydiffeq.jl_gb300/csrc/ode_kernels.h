@@ -36,6 +36,8 @@ struct EnsembleArgs {
     long long maxiters;
     int save_start, save_end, save_end_user, saveat_given, saveat_scalar;
     int save_everystep;     // save every accepted step (saveat empty); nsave_cap bounds the slots
+    int callback;           // 1: the model's ContinuousCallback (models with HAS_EVENT)
+    int interp_points;      // its interp_points
     double* k_out;          // dense output (nullptr: none): k_out[((s*NDENSE + q)*nmax + i)*N + j], the
                             // method's NDENSE interpolation vectors of the step ending at save s
     double qmax_first_step, qmax;
@@ -90,9 +92,10 @@ struct DenseArgs {
     double* out;
 };
 
-// Dense vectors stored per step, by ode_alg (Tsit5, Vern7, Rodas5P, Rosenbrock23): NDENSE of each method.
-constexpr int kNumAlgs = 4;
-constexpr int kDenseVectors[kNumAlgs] = {7, 7, 3, 2};
+// Dense vectors stored per step, by ode_alg (Tsit5, Vern7, Rodas5P, Rosenbrock23,
+// AutoTsit5(Rosenbrock23())): NDENSE of each method, 0 without dense output.
+constexpr int kNumAlgs = 5;
+constexpr int kDenseVectors[kNumAlgs] = {7, 7, 3, 2, 0};
 
 // One compiled evaluation kernel: model -1 for the model-free (componentwise)
 // interpolants, else the model whose right-hand side the interpolant needs.
@@ -110,6 +113,7 @@ const KernelVariant* rodas_variants(int* count);
 const KernelVariant* rodas_group_variants(int* count);
 const KernelVariant* ros23_variants(int* count);
 const KernelVariant* ros23_group_variants(int* count);
+const KernelVariant* auto_variants(int* count);
 const FusedVariant* fused_tsit5_variants(int* count);
 const FusedVariant* fused_vern7_variants(int* count);
 

@@ -337,18 +337,25 @@ struct Rodas5PT {
     template <class R, int C> __device__ static void prepare_dense(Cache<R, C>& c) { dense<R, C>(c); }
     template <class R, int C> __device__ static R* dense_slot(Cache<R, C>& c, int q) { return c.dk[q]; }
 
+    // not FSAL (isfsal(::Rodas5P) = false, alg_utils.jl:60): f(uprev) is formed every step
     template <class Model, class R, int L, int C>
-    __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, typename Ctl<R>::T th, double, double,
+    __device__ static void reset_fsal(Cache<R, C>&, const R*, const R*, const R*, double, const Group<L>&,
+                                      StepStats&) {}
+
+    template <class Model, class R, int L, int C>
+    __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, double th, double, double,
                                        const R* y0, const R* y0lo, const R* y1, const R* y1lo, const R*,
                                        const Group<L>&) {
         dense<R, C>(c);
         interp_dense<R, C>(c, out, outlo, th, y0, y0lo, y1, y1lo);
     }
 
-    // Interpolant on formed dense coefficients (rosenbrock_interpolants.jl:172-206).
+    // Interpolant on formed dense coefficients (rosenbrock_interpolants.jl:172-206);
+    // theta in the stage precision.
     template <class R, int C>
-    __device__ static void interp_dense(const Cache<R, C>& c, R* out, R* outlo, typename Ctl<R>::T th, const R* y0,
+    __device__ static void interp_dense(const Cache<R, C>& c, R* out, R* outlo, double thd, const R* y0,
                                         const R* y0lo, const R* y1, const R* y1lo) {
+        const R th = (R)thd;
         const R th1 = R(1) - th;
 #pragma unroll
         for (int i = 0; i < C; ++i) {

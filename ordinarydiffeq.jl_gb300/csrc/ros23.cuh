@@ -45,15 +45,20 @@ struct Rosenbrock23T {
     }
     template <class R, int C> __device__ static R* fsal_slot(Cache<R, C>& c) { return c.scratch; }
 
+    // linear-algebra storage and the parameters in double-float, without f
     template <class Model, class R, int L, int C>
-    __device__ static void initialize(Cache<R, C>& c, const R* u, const R* p, double t, const Group<L>& g,
-                                      StepStats& st, const EnsembleArgs& a, long long j) {
+    __device__ static void prepare(Cache<R, C>& c, const Group<L>& g, const EnsembleArgs& a, long long j) {
         LA::template init<R, L, C>(c.la, g);
         c.ir = a.ir_sweeps;
         if (sizeof(R) == 4) {
 #pragma unroll
             for (int i = 0; i < Model::NP; ++i) c.pff[i] = ff(a.p[(size_t)i * a.N + j]);
         }
+    }
+    template <class Model, class R, int L, int C>
+    __device__ static void initialize(Cache<R, C>& c, const R* u, const R* p, double t, const Group<L>& g,
+                                      StepStats& st, const EnsembleArgs& a, long long j) {
+        prepare<Model, R, L, C>(c, g, a, j);
         R zero[C];
 #pragma unroll
         for (int i = 0; i < C; ++i) zero[i] = R(0);
@@ -78,6 +83,15 @@ struct Rosenbrock23T {
     static constexpr int NDENSE = 2;
     template <class R, int C> __device__ static void prepare_dense(Cache<R, C>&) {}
     template <class R, int C> __device__ static R* dense_slot(Cache<R, C>& c, int q) { return c.k[q]; }
+
+    // A callback moved or modified u: f(u) again (reset_fsal!, one counted call);
+    // fsallast becomes the next step's FSAL value when it starts.
+    template <class Model, class R, int L, int C>
+    __device__ static void reset_fsal(Cache<R, C>& c, const R* u, const R* ulo, const R* p, double t,
+                                      const Group<L>& g, StepStats& st) {
+        rhs_stage<Model, R, L, C, Model::NP>(c.fsallast, u, ulo, p, c.pff, t, g);
+        st.nf += 1;
+    }
 
     template <class Model, class R, int L, int C>
     __device__ static typename Ctl<R>::T step(Cache<R, C>& c, R* u, R* ulo, const R* up, const R* uplo,
@@ -148,10 +162,10 @@ struct Rosenbrock23T {
 
     // y0 + dt (c1 k1 + c2 k2), c1 = th (1 - th) / (1 - 2d), c2 = th (th - 2d) / (1 - 2d)
     template <class Model, class R, int L, int C>
-    __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, typename Ctl<R>::T th, double dt, double,
+    __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, double th, double dt, double,
                                        const R* y0, const R* y0lo, const R*, const R*, const R*,
                                        const Group<L>&) {
-        const double thd = (double)th;
+        const double thd = th;
         const double d = tab::ROS23_D;
         const double c1 = thd * (1.0 - thd) / (1.0 - 2.0 * d);
         const double c2 = thd * (thd - 2.0 * d) / (1.0 - 2.0 * d);

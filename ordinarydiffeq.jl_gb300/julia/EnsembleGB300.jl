@@ -20,13 +20,28 @@ using SciMLBase
 import OrdinaryDiffEqTsit5: Tsit5
 import OrdinaryDiffEqVerner: Vern7
 import OrdinaryDiffEqRosenbrock: Rodas5P, Rosenbrock23
+import OrdinaryDiffEqCore: CompositeAlgorithm, AutoSwitch
 
-export EnsembleGB300, GB300Model
+export EnsembleGB300, GB300Model, GB300Callback
 
 const LIB = get(ENV, "ODE_GB300_LIB", joinpath(@__DIR__, "..", "lib", "libode_b200.so"))
 
-const MODEL_IDS = Dict(:linear => 0, :lorenz => 1, :robertson => 2, :duffing_chain => 3, :brusselator_1d => 4)
-const N_PARAMS = Dict(0 => 1, 1 => 3, 2 => 3, 3 => 3, 4 => 3)
+const MODEL_IDS = Dict(:linear => 0, :lorenz => 1, :robertson => 2, :duffing_chain => 3, :brusselator_1d => 4,
+                       :bouncing_ball => 5, :van_der_pol => 6)
+const N_PARAMS = Dict(0 => 1, 1 => 3, 2 => 3, 3 => 3, 4 => 3, 5 => 3, 6 => 1)
+
+"""
+    GB300Callback(; interp_points = 10, max_events = 16)
+
+Turns on the model's registered ContinuousCallback (its condition and affect
+are device code compiled with the model, e.g. `:bouncing_ball`); pass it as
+`callback` to `solve`.  Each event adds two saves (before and after its affect).
+"""
+struct GB300Callback
+    interp_points::Int
+    max_events::Int
+end
+GB300Callback(; interp_points = 10, max_events = 16) = GB300Callback(interp_points, max_events)
 
 """Marker right-hand side naming a model compiled into the library."""
 struct GB300Model
@@ -52,6 +67,7 @@ mutable struct Options
     save_start::Int32; save_end::Int32; save_end_user::Int32; saveat_scalar::Int32; nsave::Int32
     saveat_per_traj::Int32; qmax_first_step::Float64; qmax::Float64; lanes_per_traj::Int32
     scheduler::Int32; block_size::Int32; ir_sweeps::Int32; save_everystep::Int32; max_step_saves::Int32
+    callback::Int32; interp_points::Int32; max_events::Int32; reserved_options::Int32
 end
 struct Stats
     nf::Int64; njacs::Int64; nw::Int64; nsolve::Int64; naccept::Int64; nreject::Int64
@@ -61,10 +77,19 @@ alg_id(::Tsit5) = Int32(0)
 alg_id(::Vern7) = Int32(1)
 alg_id(::Rodas5P) = Int32(2)
 alg_id(::Rosenbrock23) = Int32(3)
+# AutoTsit5(Rosenbrock23()) with the default AutoSwitch (the composite compiled in)
+function alg_id(alg::CompositeAlgorithm)
+    cf = alg.choice_function
+    ok = length(alg.algs) == 2 && alg.algs[1] isa Tsit5 && alg.algs[2] isa Rosenbrock23 && cf isa AutoSwitch &&
+         cf.maxstiffstep == 10 && cf.maxnonstiffstep == 3 && cf.nonstifftol == 9 // 10 && cf.stifftol == 9 // 10 &&
+         cf.dtfac == 2 && !cf.stiffalgfirst && cf.switch_max == 5
+    ok || error("EnsembleGB300 runs AutoTsit5(Rosenbrock23()) with the default AutoSwitch only")
+    return Int32(4)
+end
 
 const RETCODES = (SciMLBase.ReturnCode.Default, SciMLBase.ReturnCode.Success, SciMLBase.ReturnCode.MaxIters,
                   SciMLBase.ReturnCode.DtNaN, SciMLBase.ReturnCode.DtLessThanMin, SciMLBase.ReturnCode.Unstable,
-                  SciMLBase.ReturnCode.Terminated)
+                  SciMLBase.ReturnCode.Terminated, SciMLBase.ReturnCode.Terminated)
 
 """
 Interpolation of a dense GB300 solve (the reference's dense = true): sol(t)
@@ -107,11 +132,13 @@ function handle(dev)
     end
 end
 
-function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem, alg::Union{Tsit5, Vern7, Rodas5P, Rosenbrock23},
+function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem,
+                           alg::Union{Tsit5, Vern7, Rodas5P, Rosenbrock23, CompositeAlgorithm},
                            ens::EnsembleGB300; trajectories, saveat = Float64[], reltol = 1e-3, abstol = 1e-6,
                            dt = 0.0, dtmax = 0.0, dtmin = 0.0, maxiters = 1_000_000, save_start = nothing,
                            save_end = nothing, save_everystep = isempty(saveat), max_step_saves = 1024, seed = 0,
-                           dense = save_everystep && isempty(saveat), kwargs...)
+                           callback = nothing, dense = save_everystep && isempty(saveat) && callback === nothing,
+                           kwargs...)
     t0 = time()
     N = trajectories
     probs = [eprob.prob_func(eprob.prob, SciMLBase.EnsembleContext(i, 1, seed)) for i in 1:N]
@@ -134,11 +161,14 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem, alg::Union{
     ss = save_start === nothing ? (isempty(saveat) || scalar || probs[1].tspan[1] in sv) : save_start
     se = save_end === nothing ? (isempty(saveat) || scalar || probs[1].tspan[2] in sv) : save_end
     everystep = save_everystep && isempty(sv)
+    callback === nothing || callback isa GB300Callback ||
+        error("EnsembleGB300 runs the model's registered callback only: pass GB300Callback(...)")
+    cb = callback isa GB300Callback
     o = Options(reltol, abstol, dtmax, dtmin, dt, maxiters, ss, se, save_end === nothing ? -1 : Int32(save_end),
                 scalar, length(sv), 0, 0.0, 0.0, ens.lanes_per_traj, ens.scheduler, 0, -1, everystep,
-                everystep ? max_step_saves : 0)
+                everystep ? max_step_saves : 0, cb, cb ? callback.interp_points : 10, cb ? callback.max_events : 0, 0)
     d = ProblemDesc(model, alg_id(alg), n, npar, ens.precision === :mixed ? 1 : 0, 0)
-    cap = (everystep ? max_step_saves : length(sv)) + 2
+    cap = (everystep ? max_step_saves : length(sv)) + 2 + (cb ? 2 * callback.max_events : 0)
     t_out = fill(NaN, N, cap); u_out = fill(NaN, N, n, cap)   # [(s*n + i)*N + j] -> u_out[j, i, s]
     nsaved = zeros(Int32, N); rc = zeros(Int32, N); st = Vector{Stats}(undef, N)
     # dense output (solve.jl:145-146) for every-step saves of one state count

@@ -9,8 +9,9 @@ import os
 
 from . import build as _build
 
-ODE_TSIT5, ODE_VERN7, ODE_RODAS5P, ODE_ROSENBROCK23 = 0, 1, 2, 3
+ODE_TSIT5, ODE_VERN7, ODE_RODAS5P, ODE_ROSENBROCK23, ODE_AUTOTSIT5_ROSENBROCK23 = 0, 1, 2, 3, 4
 MODEL_LINEAR, MODEL_LORENZ, MODEL_ROBERTSON, MODEL_DUFFING_CHAIN, MODEL_BRUSSELATOR_1D = 0, 1, 2, 3, 4
+MODEL_BOUNCING_BALL, MODEL_VANDERPOL = 5, 6
 PREC_FP64, PREC_MIXED = 0, 1
 STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "out of device memory",
           -4: "unsupported", -5: "busy", -6: "timeout", -7: "unknown ticket"}
@@ -28,7 +29,9 @@ class Options(C.Structure):
                 ("saveat_scalar", C.c_int32), ("nsave", C.c_int32), ("saveat_per_traj", C.c_int32),
                 ("qmax_first_step", C.c_double), ("qmax", C.c_double), ("lanes_per_traj", C.c_int32),
                 ("scheduler", C.c_int32), ("block_size", C.c_int32), ("ir_sweeps", C.c_int32),
-                ("save_everystep", C.c_int32), ("max_step_saves", C.c_int32)]
+                ("save_everystep", C.c_int32), ("max_step_saves", C.c_int32),
+                ("callback", C.c_int32), ("interp_points", C.c_int32), ("max_events", C.c_int32),
+                ("reserved_options", C.c_int32)]
 
 
 class Stats(C.Structure):

@@ -29,12 +29,27 @@ class ReturnCode(IntEnum):
     DtLessThanMin = 4
     Unstable = 5
     Aborted = 6
+    Terminated = 7
 
 
 MODELS = {"linear": _lib.MODEL_LINEAR, "lorenz": _lib.MODEL_LORENZ, "robertson": _lib.MODEL_ROBERTSON,
-          "duffing_chain": _lib.MODEL_DUFFING_CHAIN, "brusselator_1d": _lib.MODEL_BRUSSELATOR_1D}
+          "duffing_chain": _lib.MODEL_DUFFING_CHAIN, "brusselator_1d": _lib.MODEL_BRUSSELATOR_1D,
+          "bouncing_ball": _lib.MODEL_BOUNCING_BALL, "van_der_pol": _lib.MODEL_VANDERPOL}
 N_PARAMS = {_lib.MODEL_LINEAR: 1, _lib.MODEL_LORENZ: 3, _lib.MODEL_ROBERTSON: 3,
-            _lib.MODEL_DUFFING_CHAIN: 3, _lib.MODEL_BRUSSELATOR_1D: 3}
+            _lib.MODEL_DUFFING_CHAIN: 3, _lib.MODEL_BRUSSELATOR_1D: 3, _lib.MODEL_BOUNCING_BALL: 3,
+            _lib.MODEL_VANDERPOL: 1}
+
+
+@dataclass
+class ContinuousCallback:
+    """The model's registered ContinuousCallback (device code cannot call Python or
+    Julia closures: the condition and affect are compiled in with the model, e.g.
+    "bouncing_ball": condition x, affect_neg! v <- -e v or terminate! once
+    t >= t_stop).  interp_points as SciMLBase's ContinuousCallback (default 10);
+    max_events sizes the output: each event adds two saves (before and after its
+    affect, save_positions = (true, true))."""
+    interp_points: int = 10
+    max_events: int = 16
 
 
 class _Alg:
@@ -67,7 +82,26 @@ class Rosenbrock23(_Alg):
     alg_id = _lib.ODE_ROSENBROCK23
 
 
-ALG_BY_NAME = {"tsit5": Tsit5(), "vern7": Vern7(), "rodas5p": Rodas5P(), "rosenbrock23": Rosenbrock23()}
+class AutoTsit5(_Alg):
+    """AutoTsit5(stiff_alg): Tsit5 with stiffness detection, switching to the stiff
+    method and back (AutoSwitch defaults: maxstiffstep 10, maxnonstiffstep 3,
+    tolerances 9/10, dtfac 2; lib/OrdinaryDiffEqTsit5/src/algorithms.jl:27-33,
+    lib/OrdinaryDiffEqCore/src/composite_algs.jl).  The stiff method compiled in is
+    Rosenbrock23."""
+
+    def __init__(self, stiff_alg=None):
+        if stiff_alg is not None and not isinstance(stiff_alg, Rosenbrock23):
+            raise ValueError("AutoTsit5 is compiled with Rosenbrock23 as its stiff method")
+        self.stiff_alg = stiff_alg or Rosenbrock23()
+
+    alg_id = _lib.ODE_AUTOTSIT5_ROSENBROCK23
+
+    def __repr__(self):
+        return "AutoTsit5(Rosenbrock23())"
+
+
+ALG_BY_NAME = {"tsit5": Tsit5(), "vern7": Vern7(), "rodas5p": Rodas5P(), "rosenbrock23": Rosenbrock23(),
+               "autotsit5_rosenbrock23": AutoTsit5(Rosenbrock23())}
 
 
 @dataclass
@@ -245,7 +279,7 @@ def get_handle(device=0):
     return h
 
 
-def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax):
+def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax, callback=None):
     o = _lib.Options()
     L = _lib.load()
     L.ode_options_default(C.byref(o))
@@ -266,19 +300,25 @@ def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_ste
     o.ir_sweeps = ens.ir_sweeps
     o.save_everystep = int(sv.everystep)
     o.max_step_saves = int(sv.max_step_saves)
+    if callback is not None:
+        o.callback = 1
+        o.interp_points = int(callback.interp_points)
+        o.max_events = int(callback.max_events)
     return o
 
 
 def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=1e-6, dt=None,
                  dtmax=None, dtmin=None, maxiters=1000000, save_start=None, save_end=None, n_per_traj=None,
                  qmax_first_step=None, qmax=None, return_times=False, save_everystep=False, max_step_saves=1024,
-                 dense=False):
+                 dense=False, callback=None):
     """Solve a packed ensemble.  u0s (n, N), ps (np, N), tspans (2, N).  Returns the
     raw structure-of-arrays outputs dict (t, u, nsaved, retcode, stats).
     save_everystep (without saveat) keeps every accepted step, up to
     max_step_saves per trajectory (past that the last slot holds the final
     point and a warning is issued).  dense (with save_everystep) also keeps
-    each step's interpolation vectors, k (cap, nk, n, N), for dense_eval."""
+    each step's interpolation vectors, k (cap, nk, n, N), for dense_eval.
+    callback: the model's ContinuousCallback (ContinuousCallback(...)); a
+    trajectory it terminates reports ReturnCode.Terminated."""
     L = _lib.load()
     if isinstance(model, str):
         model = MODELS[model]
@@ -287,9 +327,11 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
     tspans = np.ascontiguousarray(tspans, dtype=np.float64)
     n, N = u0s.shape
     sv = resolve_saveat(saveat, tspans, save_start, save_end, save_everystep, max_step_saves)
-    o = _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax)
+    o = _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax, callback)
     d = _lib.ProblemDesc(model, alg.alg_id, n, ps.shape[0], ens.prec_id(), 0)
-    cap = sv.cap
+    cap = sv.cap + (2 * callback.max_events if callback is not None else 0)
+    if dense and callback is not None:
+        raise ValueError("dense output with a callback is not supported")
     if dense and not sv.everystep:
         raise ValueError("dense output keeps every step: use it without saveat, with save_everystep")
     if dense and n_per_traj is not None:
@@ -319,7 +361,10 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
     elapsed = time.perf_counter() - t0
     _lib.check(status, h)
     names = ("nf", "njacs", "nw", "nsolve", "naccept", "nreject")
-    if sv.everystep:
+    if callback is not None and np.any(nsaved == cap):
+        warnings.warn("some trajectories filled all %d save slots: raise max_events (their latest save is kept "
+                      "in the last slot)" % cap)
+    elif sv.everystep:
         lost = int(np.sum(stats[:, 4] + int(sv.save_start) > cap))
         if lost:
             warnings.warn("%d trajectories took more than max_step_saves=%d steps; their middle steps were "
@@ -384,19 +429,21 @@ def autotune(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=
 
 def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, saveat=None, reltol=1e-3,
           abstol=1e-6, dt=None, dtmax=None, dtmin=None, maxiters=1000000, save_start=None, save_end=None,
-          seed=0, qmax_first_step=None, qmax=None, save_everystep=None, max_step_saves=1024, dense=None):
+          seed=0, qmax_first_step=None, qmax=None, save_everystep=None, max_step_saves=1024, dense=None,
+          callback=None):
     """solve(EnsembleProblem, alg, EnsembleGB300(); trajectories, saveat, reltol, abstol, ...).
     As in the reference (solve.jl:138-146), save_everystep defaults to "no
     saveat given" (every accepted step is kept, up to max_step_saves per
     trajectory) and dense to save_everystep without saveat (each step's
     interpolation vectors are kept too, so sol(t) uses the method's
-    interpolant); ensembles of uneven sizes are not dense by default."""
+    interpolant); ensembles of uneven sizes, and solves with a callback, are not
+    dense by default.  callback: the model's ContinuousCallback."""
     no_saveat = saveat is None or (not np.isscalar(saveat) and np.size(saveat) == 0)
     if save_everystep is None:
         save_everystep = no_saveat
     dense_default = dense is None
     if dense is None:
-        dense = bool(save_everystep and no_saveat)
+        dense = bool(save_everystep and no_saveat and callback is None)
     ens = ensemblealg or EnsembleGB300()
     if not isinstance(ens, EnsembleGB300):
         raise TypeError("ensemble algorithm must be EnsembleGB300")
@@ -412,7 +459,7 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
         res = solve_arrays(prob.model, alg, ens, u0s, ps, tspans, saveat, reltol, abstol, dt, dtmax, dtmin,
                            maxiters, save_start, save_end, eprob.n_per_traj, qmax_first_step, qmax,
                            save_everystep=save_everystep, max_step_saves=max_step_saves,
-                           dense=dense and not (dense_default and eprob.n_per_traj is not None))
+                           dense=dense and not (dense_default and eprob.n_per_traj is not None), callback=callback)
         sols = _LazySolutions(res, alg, eprob.n_per_traj)
         return EnsembleSolution(sols, time.perf_counter() - t_start, True, res)
     if trajectories is None:
@@ -428,7 +475,7 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
         ids = list(range(done, min(trajectories, done + batch_size)))
         outs = _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, dtmin, maxiters,
                             save_start, save_end, output_func, qmax_first_step, qmax, save_everystep, max_step_saves,
-                            dense, dense_default)
+                            dense, dense_default, callback)
         u, converged = reduction(u, outs, range(ids[0] + 1, ids[-1] + 2))
         done = ids[-1] + 1
         if converged:
@@ -438,7 +485,7 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
 
 def _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, dtmin, maxiters, save_start,
                  save_end, output_func, qmax_first_step, qmax, save_everystep=False, max_step_saves=1024,
-                 dense=False, dense_default=True):
+                 dense=False, dense_default=True, callback=None):
     repeat = {i: 1 for i in ids}
     results = {}
     todo = list(ids)
@@ -465,7 +512,7 @@ def _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, 
         res = solve_arrays(probs[0].model, alg, ens, u0s, ps, tspans, saveat, reltol, abstol, dt, dtmax, dtmin,
                            maxiters, save_start, save_end, npt, qmax_first_step, qmax,
                            save_everystep=save_everystep, max_step_saves=max_step_saves,
-                           dense=dense and not (dense_default and npt is not None))
+                           dense=dense and not (dense_default and npt is not None), callback=callback)
         sols = _LazySolutions(res, alg, npt)
         again = []
         for k, i in enumerate(todo):

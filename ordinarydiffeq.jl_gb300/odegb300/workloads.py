@@ -35,6 +35,34 @@ def robertson(N, seed=42, alg="rodas5p", reltol=1e-6, abstol=1e-10):
                 abstol=abstol)
 
 
+def bouncing_ball(N, seed=42):
+    """Balls dropped from 20-50 m (v0 ~ U(-5, 5)) under g = 9.81 with the model's
+    ContinuousCallback (condition x, affect_neg! v <- -e v): restitution e ~
+    U(0.85, 0.95), so the bounces stay apart over tspan (0, 10); half of the
+    balls terminate! at their first contact after t_stop ~ U(3, 10), the rest
+    bounce to tf.  Tsit5, reltol = abstol = 1e-6, saveat 0.25 (41 saves)."""
+    from .ensemble import ContinuousCallback
+    rng = np.random.default_rng(seed)
+    u0 = np.vstack([rng.uniform(20.0, 50.0, N), rng.uniform(-5.0, 5.0, N)])
+    t_stop = np.where(rng.uniform(0.0, 1.0, N) < 0.5, rng.uniform(3.0, 10.0, N), 1e9)
+    p = np.vstack([np.full(N, 9.81), rng.uniform(0.85, 0.95, N), t_stop])
+    ts = np.vstack([np.zeros(N), np.full(N, 10.0)])
+    return dict(model="bouncing_ball", alg="tsit5", u0=u0, p=p, tspan=ts, saveat=0.25, reltol=1e-6, abstol=1e-6,
+                callback=ContinuousCallback(interp_points=10, max_events=8))
+
+
+def van_der_pol(N, seed=42):
+    """Van der Pol oscillators (the reference's stiffness-detection problem) with
+    mu log-uniform in [1, 1000] (from non-stiff to stiff relaxation), u0 = (2, 0),
+    tspan (0, 6), AutoTsit5(Rosenbrock23()), reltol = abstol = 1e-6, saveat 0.5."""
+    rng = np.random.default_rng(seed)
+    u0 = np.tile(np.array([[2.0], [0.0]]), (1, N))
+    p = (10.0 ** rng.uniform(0.0, 3.0, N))[None, :]
+    ts = np.vstack([np.zeros(N), np.full(N, 6.0)])
+    return dict(model="van_der_pol", alg="autotsit5_rosenbrock23", u0=u0, p=p, tspan=ts, saveat=0.5, reltol=1e-6,
+                abstol=1e-6)
+
+
 def duffing(N, seed=42, sizes=(2, 4, 8, 16, 32), tf_range=(1.0, 100.0)):
     """Uneven Duffing chains: N oscillators uniform in `sizes` (2N states), stiffness and
     damping ~ U(0.1, 1), cubic ~ U(0, 5), u0 ~ N(0, 1), tf log-uniform in tf_range,
@@ -76,9 +104,11 @@ def brusselator(N, seed=42, cells=32):
 # counted from the kernels' own arithmetic.  F: FLOPs of one RHS evaluation.
 
 RHS_FLOPS = {"linear": lambda n: n, "lorenz": lambda n: 9, "robertson": lambda n: 13,
-             "duffing_chain": lambda n: 9 * (n // 2), "brusselator_1d": lambda n: 13 * (n // 2)}
+             "duffing_chain": lambda n: 9 * (n // 2), "brusselator_1d": lambda n: 13 * (n // 2),
+             "bouncing_ball": lambda n: 1, "van_der_pol": lambda n: 7}
 JAC_FLOPS = {"linear": lambda n: 0, "lorenz": lambda n: 3, "robertson": lambda n: 10,
-             "duffing_chain": lambda n: 5 * (n // 2), "brusselator_1d": lambda n: 14 * (n // 2)}
+             "duffing_chain": lambda n: 5 * (n // 2), "brusselator_1d": lambda n: 14 * (n // 2),
+             "bouncing_ball": lambda n: 0, "van_der_pol": lambda n: 8}
 CONTROLLER_FLOPS = 150  # two series pow evaluations, clamp, dt update (FP64)
 
 
@@ -105,6 +135,8 @@ def attempt_flops(alg, model, n):
         solve = 2 * n * n + n
         return (8 * F + Jf + 2 * n + lu + 8 * solve + n * (2 * 28 + 2 * 28 + 2 * 8 + 2 * 24) + 28 + 8
                 + error_norm_flops(n) + CONTROLLER_FLOPS)
+    if alg == "autotsit5_rosenbrock23":   # the Tsit5 attempt (the common one) plus the stiffness estimate
+        return attempt_flops("tsit5", model, n) + 3 * n
     if alg == "rosenbrock23":
         # 2 RHS (f at the half step, FSAL f(u)) + J, W, LU, 3 solves; per state the
         # stage, FSAL-difference and error-estimate arithmetic: 19 flops
@@ -153,4 +185,6 @@ def save_flops(alg, model, n):
         return n * 2 * 7
     if alg == "rosenbrock23":
         return n * 2 * 2 + 8
+    if alg == "autotsit5_rosenbrock23":
+        return n * 2 * 7
     return n * 2 * 5

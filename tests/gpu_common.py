@@ -2,13 +2,14 @@
 import numpy as np
 
 import pyoracle as O
-from odegb300 import EnsembleGB300, Rodas5P, Rosenbrock23, Tsit5, Vern7, solve_arrays
+from odegb300 import AutoTsit5, EnsembleGB300, Rodas5P, Rosenbrock23, Tsit5, Vern7, solve_arrays
 from odegb300.saveat import resolve_saveat
 
 ALG = {"tsit5": (Tsit5(), O.TSIT5), "vern7": (Vern7(), O.VERN7), "rodas5p": (Rodas5P(), O.RODAS5P),
-       "rosenbrock23": (Rosenbrock23(), O.ROSENBROCK23)}
+       "rosenbrock23": (Rosenbrock23(), O.ROSENBROCK23),
+       "autotsit5_rosenbrock23": (AutoTsit5(Rosenbrock23()), O.AUTOTSIT5_ROSENBROCK23)}
 MODEL = {"linear": O.LINEAR, "lorenz": O.LORENZ, "robertson": O.ROBERTSON, "duffing_chain": O.DUFFING,
-         "brusselator_1d": O.BRUSSELATOR}
+         "brusselator_1d": O.BRUSSELATOR, "bouncing_ball": O.BOUNCING_BALL, "van_der_pol": O.VANDERPOL}
 
 
 def lorenz_inputs(N, seed=42):

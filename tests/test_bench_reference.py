@@ -10,7 +10,8 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-@pytest.mark.parametrize("config", ["robertson", "robertson_ros23", "lorenz_dense", "serving"])
+@pytest.mark.parametrize("config", ["robertson", "robertson_ros23", "lorenz_dense", "bouncing_ball", "van_der_pol",
+                                    "serving"])
 def test_reference_arm_prints_one_json_line(config):
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--config", config,
                         "--trajectories", "64", "--steps", "1", "--warmup", "1"],

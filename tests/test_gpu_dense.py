@@ -64,7 +64,9 @@ def test_dense_steps_and_sol_t_match_oracle(model, alg, rt, at):
         for s in range(1, ns):
             tprev, tend, y0, y1, ko = D.step(s - 1)
             kg = g["k"][s, :, :, j]
-            scale = np.abs(ko).max(axis=1, keepdims=True) + 1e-300
+            # relative to the step's largest vector: a cancelling combination (Rodas5P's
+            # third dense vector) is small next to the others and carries their rounding
+            scale = np.abs(ko).max() + 1e-300
             assert np.all(np.abs(kg - ko) <= 1e-5 * scale), (j, s, kg, ko)
     assert same_steps >= 1
     # the start save carries no step
@@ -150,3 +152,26 @@ def test_solution_call_uses_the_dense_interpolant():
     sim2 = solve(ep, Vern7(), EnsembleGB300(), trajectories=2, saveat=0.5, reltol=1e-8, abstol=1e-8)
     s2 = sim2.u[0]
     assert not s2.dense and np.allclose(s2(0.25), 0.5 * (np.asarray(s2.u[0]) + np.asarray(s2.u[1])))
+
+
+def test_page_locked_dense_eval_output_is_identical():
+    import ctypes as C
+    import torch
+    from odegb300 import _lib
+    from odegb300.ensemble import get_handle
+    N = 200
+    u0, p, ts = lorenz_inputs(N, seed=12)
+    g = gpu("lorenz", "tsit5", u0, p, ts, None, 1e-8, 1e-8, save_everystep=True, max_step_saves=512, dense=True)
+    tq = np.linspace(0.0, 1.0, 37)
+    staged = dense_eval(g, tq)
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+    h_p, h_t, h_u, h_k, h_ns, h_tq = (pin(g["dense"]["p"]), pin(g["t"]), pin(g["u"]), pin(g["k"]), pin(g["nsaved"]),
+                                      pin(tq))
+    h_out = torch.empty((tq.size, 3, N), dtype=torch.float64).pin_memory()
+    ptr = lambda t, ty=C.c_double: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(ty))
+    L = _lib.load()
+    h = get_handle(0)
+    d = _lib.ProblemDesc(g["dense"]["model"], g["dense"]["alg"], 3, 3, 0, 0)
+    _lib.check(L.ode_dense_eval(h, C.byref(d), N, ptr(h_p), ptr(h_t), ptr(h_u), ptr(h_k), ptr(h_ns, C.c_int32),
+                                g["t"].shape[0], tq.size, ptr(h_tq), 0, ptr(h_out)), h)
+    assert np.array_equal(h_out.numpy(), staged)

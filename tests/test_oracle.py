@@ -245,3 +245,65 @@ def test_save_everystep_saves_start_and_every_accepted_step():
                           np.zeros(0), 1e-6, 1e-6, save_start=True, save_end=False, saveat_given=False,
                           save_everystep=True, max_step_saves=256)
     assert int(r2["nsaved"][0]) == k - 1 and r2["t"][k - 2, 0] < 1.0
+
+
+# test/Integrators_I/ode_event_tests.jl:283-323: ContinuousCallback(u[1], terminate!) on the
+# falling ball (x' = v, v' = -9.81, u0 = (50, 0)): Terminated at t = sqrt(50*2/9.81) with
+# the height below 3e-12.
+BALL0 = dict(saveat=[], saveat_given=False, callback=True, save_everystep=True, max_step_saves=400,
+             save_start=True)
+
+
+@pytest.mark.parametrize("alg", [O.TSIT5, O.VERN7, O.RODAS5P, O.ROSENBROCK23])
+def test_event_terminates_at_ground_contact(alg):
+    r = O.solve(alg, O.BOUNCING_BALL, [50.0, 0.0], [9.81, 1.0, 0.0], (0.0, 100.0), interp_points=10, **BALL0)
+    assert r["retcode"] == O.RC_TERMINATED
+    assert r["t"][-1] == pytest.approx(np.sqrt(50 * 2 / 9.81), rel=1e-12)
+    assert abs(r["u"][-1][0]) < 3.0e-12
+
+
+def test_event_bounces_then_terminates():
+    # ode_event_tests.jl:332-360: affect_neg! reflects v until t >= 3.5, then terminate!;
+    # interp_points = 100; ends at 3 sqrt(50*2/9.81) with the height below 1.3e-10
+    r = O.solve(O.TSIT5, O.BOUNCING_BALL, [50.0, 0.0], [9.81, 1.0, 3.5], (0.0, 100.0), interp_points=100, **BALL0)
+    assert r["retcode"] == O.RC_TERMINATED
+    assert r["t"][-1] == pytest.approx(3 * np.sqrt(50 * 2 / 9.81), rel=1e-12)
+    assert abs(r["u"][-1][0]) < 1.3e-10
+
+
+def test_event_saves_both_sides_of_the_discontinuity():
+    # ode_event_tests.jl:153-171: the event time is saved twice (save_positions =
+    # (true, true)); before the affect v < 0, after it v > 0
+    r = O.solve(O.TSIT5, O.BOUNCING_BALL, [50.0, 0.0], [9.81, 1.0, 1e9], (0.0, 15.0), interp_points=100, **BALL0)
+    assert r["retcode"] == O.RC_SUCCESS
+    t, u = r["t"], r["u"]
+    te = np.sqrt(50 * 2 / 9.81)
+    hit = np.nonzero(np.abs(t - te) < 1e-9)[0]
+    assert len(hit) == 2 and t[hit[0]] == t[hit[1]]
+    assert u[hit[0]][1] < 0 < u[hit[1]][1] and u[hit[1]][1] == -u[hit[0]][1]
+    # two more contacts before t = 15 (every 2 te): four more saves at event times
+    assert sum(np.sum(np.abs(t - k * te) < 1e-8) for k in (1, 3)) == 4
+
+
+# test/InterfaceI/stiffness_detection_test.jl:10-44: AutoTsit5(Rosenbrock23()) on the stiff
+# van der Pol oscillator (mu = 1/0.003, u0 = (2, 0), tspan (0, 6), maxiters 1000) succeeds
+# and switches back and forth: each method is chosen for more than 5 saved steps.
+def test_autotsit5_switches_back_and_forth_on_van_der_pol():
+    kw = dict(saveat=[], saveat_given=False, save_everystep=True, max_step_saves=2000, save_start=True,
+              maxiters=1000)
+    r = O.solve(O.AUTOTSIT5_ROSENBROCK23, O.VANDERPOL, [2.0, 0.0], [1 / 0.003], (0.0, 6.0), **kw)
+    assert r["retcode"] == O.RC_SUCCESS
+    ch = r["alg_choice"][1:]
+    assert all(np.sum(ch == i) > 5 for i in (1, 2))
+    r2 = O.solve(O.AUTOTSIT5_ROSENBROCK23, O.VANDERPOL, [2.0, 0.0], [1 / 0.003], (0.0, 6.0), **kw)
+    assert np.array_equal(r["t"], r2["t"])   # the composite's state is reinitialised per solve
+
+
+def test_autotsit5_on_a_nonstiff_problem_is_tsit5():
+    # no stiffness detected: the composite never switches and takes Tsit5's steps exactly
+    kw = dict(saveat=[], saveat_given=False, save_everystep=True, max_step_saves=2000, save_start=True,
+              reltol=1e-8, abstol=1e-8)
+    a = O.solve(O.AUTOTSIT5_ROSENBROCK23, O.LORENZ, [1.0, 0.0, 0.0], [10.0, 14.0, 8 / 3], (0.0, 1.0), **kw)
+    b = O.solve(O.TSIT5, O.LORENZ, [1.0, 0.0, 0.0], [10.0, 14.0, 8 / 3], (0.0, 1.0), **kw)
+    assert (a["alg_choice"] == 1).all()
+    assert np.array_equal(a["t"], b["t"]) and np.array_equal(a["u"], b["u"])

@@ -30,7 +30,8 @@ def _worker(rank, world, port, mode, q):
             t = bench.max_over_ranks(1.0 + r, dist)
             q.put((r, "ok", t, bench.replica_rate(w, 1000, t)))
             dist.barrier()
-        else:   # rank 1 dies before the collective; rank 0 must get an error
+        else:   # after one completed step rank 1 dies; rank 0's next collective must fail
+            bench.max_over_ranks(1.0, dist)
             if r == 1:
                 os._exit(3)
             try:
@@ -44,7 +45,7 @@ def _worker(rank, world, port, mode, q):
         q.put((rank, "exception", repr(e), None))
 
 
-def _run(mode, timeout=60):
+def _run(mode, timeout=180):   # spawn + import torch can be slow on a loaded host; the collective timeout is 20 s
     import multiprocessing as mp
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
