@@ -469,9 +469,12 @@ int make_plan(ode_handle* h, const ode_problem_desc* d, const ode_options* o, co
             return fail(h, ODE_E_UNSUPPORTED, buf);
         }
         // auto: the persistent queue for the shared-memory kernels (measured 13%
-        // faster on the 64-state Brusselator: its many short waves leave tails),
-        // one group per trajectory otherwise
-        if (pl->scheduler == 0) pl->scheduler = pl->v->smem_per_group > 0 ? 2 : 1;
+        // faster on the 64-state Brusselator: its many short waves leave tails)
+        // and for AutoTsit5 (trajectories that turn stiff take ~100x the steps of
+        // the others, and a finished lane refills: 498 -> 295 ms on 100k van der
+        // Pol oscillators), one group per trajectory otherwise
+        if (pl->scheduler == 0)
+            pl->scheduler = (pl->v->smem_per_group > 0 || d->alg_id == ODE_AUTOTSIT5_ROSENBROCK23) ? 2 : 1;
         return ODE_OK;
     }
     if (d->model_id != ODE_MODEL_DUFFING_CHAIN)
