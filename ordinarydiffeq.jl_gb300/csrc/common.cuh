@@ -127,6 +127,14 @@ template <> struct Acc<double> {
         hi = fma(d, S, up);
         lo = 0.0;
     }
+    // u = uprev + dt*S with dt as a pair (dh, dl); in FP64 dl is 0 and this is update
+    static __device__ __forceinline__ void update2(double& hi, double& lo, double dh, double, double S, double up,
+                                                   double) {
+        hi = fma(dh, S, up);
+        lo = 0.0;
+    }
+    // the low part of dt as a float pair: none in FP64
+    static __device__ __forceinline__ double dt_lo(double, double) { return 0.0; }
     // u = uprev + inc where inc was accumulated starting from uprev already
     static __device__ __forceinline__ void set(double& hi, double& lo, double v) { hi = v; lo = 0.0; }
     static __device__ __forceinline__ void set_pair(double& hi, double& lo, double v) { hi = v; lo = 0.0; }
@@ -146,6 +154,16 @@ template <> struct Acc<float> {
         float inc = d * S + uplo;
         two_sum(up, inc, hi, lo);
     }
+    // u = uprev + dt*S with the FP64 dt as a float pair dh + dl (dh = float(dt)):
+    // the remainder dl*S joins the increment, so the state advances by the step
+    // that t advances by (with dh alone the state drifts by up to 2^-24 of each
+    // increment, which shifts event times and accumulates over long runs)
+    static __device__ __forceinline__ void update2(float& hi, float& lo, float dh, float dl, float S, float up,
+                                                   float uplo) {
+        float inc = fmaf(dh, S, fmaf(dl, S, uplo));
+        two_sum(up, inc, hi, lo);
+    }
+    static __device__ __forceinline__ float dt_lo(double dt, float dh) { return (float)(dt - (double)dh); }
     static __device__ __forceinline__ void set(float& hi, float& lo, float v) { hi = v; lo = 0.0f; }
     static __device__ __forceinline__ void split(double x, float& hi, float& lo) {
         hi = (float)x;

@@ -100,6 +100,7 @@ struct Tsit5Alg {
         static_assert(!EIG || L == 1, "the stiffness estimate is formed on one lane");
         using K = RK<Tsit5Tab, R, C>;
         const R d = (R)dt;
+        const R dl = Acc<R>::dt_lo(dt, d);
         R* tmp = c.tmp;
         R g6[EIG ? C : 1];
         K::template stage<2>(tmp, c.k, d, up, uplo);
@@ -118,7 +119,7 @@ struct Tsit5Alg {
         Model::template rhs<R, L, C>(c.k[5], tmp, p, stage_time<Model>(1.0, dt, t), g);
         K::weights(tmp, c.k, Tsit5Sol());
 #pragma unroll
-        for (int i = 0; i < C; ++i) Acc<R>::update(u[i], ulo[i], d, tmp[i], up[i], uplo[i]);
+        for (int i = 0; i < C; ++i) Acc<R>::update2(u[i], ulo[i], d, dl, tmp[i], up[i], uplo[i]);
         Model::template rhs<R, L, C>(c.k[6], u, p, stage_time<Model>(1.0, dt, t), g);
         st.nf += 6;
         if constexpr (EIG) {
@@ -154,6 +155,7 @@ struct Tsit5Alg {
                 Acc<R>::update(out[i], outlo[i], d, acc, y0[i], y0lo[i]);
             }
         } else {
+            const R dl = Acc<R>::dt_lo(dt, d);
             ff b[8];
             b[1] = split_weight(interp_weight<5>((double)th, 1, r, true));
 #pragma unroll
@@ -163,7 +165,7 @@ struct Tsit5Alg {
                 CSum cs;
 #pragma unroll
                 for (int s = 1; s <= 7; ++s) cs.add_pair(b[s].hi, b[s].lo, (float)c.k[s - 1][i]);
-                Acc<R>::update(out[i], outlo[i], d, (R)cs.value(), y0[i], y0lo[i]);
+                Acc<R>::update2(out[i], outlo[i], d, dl, (R)cs.value(), y0[i], y0lo[i]);
             }
         }
     }
@@ -220,8 +222,9 @@ struct Vern7Alg {
         eval_stage<9, Model>(c, up, uplo, p, stage_time<Model>(1.0, dt, t), d, g);
         eval_stage<10, Model>(c, up, uplo, p, stage_time<Model>(1.0, dt, t), d, g);
         RK<Vern7Tab, R, C>::weights(c.tmp, c.s, Vern7Sol());
+        const R dl = Acc<R>::dt_lo(dt, d);
 #pragma unroll
-        for (int i = 0; i < C; ++i) Acc<R>::update(u[i], ulo[i], d, c.tmp[i], up[i], uplo[i]);
+        for (int i = 0; i < C; ++i) Acc<R>::update2(u[i], ulo[i], d, dl, c.tmp[i], up[i], uplo[i]);
         st.nf += 10;
         RK<Vern7Tab, R, C>::weights(c.tmp, c.s, Vern7Err());
 #pragma unroll
@@ -270,6 +273,7 @@ struct Vern7Alg {
                 Acc<R>::update(out[i], outlo[i], d, acc, y0[i], y0lo[i]);
             }
         } else {
+            const R dl = Acc<R>::dt_lo(dt, d);
             ff b[13];
             b[0] = split_weight(interp_weight<8>((double)th, 1, r, true));
 #pragma unroll
@@ -279,7 +283,7 @@ struct Vern7Alg {
                 CSum cs;
 #pragma unroll
                 for (int q = 0; q < 13; ++q) cs.add_pair(b[q].hi, b[q].lo, (float)c.s[Vern7Tab::slot(idx[q])][i]);
-                Acc<R>::update(out[i], outlo[i], d, (R)cs.value(), y0[i], y0lo[i]);
+                Acc<R>::update2(out[i], outlo[i], d, dl, (R)cs.value(), y0[i], y0lo[i]);
             }
         }
     }

@@ -141,8 +141,9 @@ struct Rosenbrock23T {
 #pragma unroll
         for (int i = 0; i < C; ++i) k2[i] = FMA(r[i], ninv, k1[i]);
         st.nsolve += 1;
+        const R dl = Acc<R>::dt_lo(dt, dr);
 #pragma unroll
-        for (int i = 0; i < C; ++i) Acc<R>::update(u[i], ulo[i], dr, k2[i], up[i], uplo[i]);
+        for (int i = 0; i < C; ++i) Acc<R>::update2(u[i], ulo[i], dr, dl, k2[i], up[i], uplo[i]);
         rhs_stage<Model, R, L, C, NP>(c.fsallast, u, ulo, p, c.pff, stage_time<Model>(1.0, dt, t), g);
         st.nf += 1;
 #pragma unroll
@@ -175,12 +176,13 @@ struct Rosenbrock23T {
                 Acc<R>::update(out[i], outlo[i], dt, fma(c1, c.k[0][i], c2 * c.k[1][i]), y0[i], y0lo[i]);
         } else {
             const ff w1 = split_weight(c1), w2 = split_weight(c2);
+            const R dh = (R)dt, dl = Acc<R>::dt_lo(dt, dh);
 #pragma unroll
             for (int i = 0; i < C; ++i) {
                 CSum cs;
                 cs.add_pair(w1.hi, w1.lo, (float)c.k[0][i]);
                 cs.add_pair(w2.hi, w2.lo, (float)c.k[1][i]);
-                Acc<R>::update(out[i], outlo[i], (R)dt, (R)cs.value(), y0[i], y0lo[i]);
+                Acc<R>::update2(out[i], outlo[i], dh, dl, (R)cs.value(), y0[i], y0lo[i]);
             }
         }
     }
