@@ -136,6 +136,10 @@ typedef struct {
 
 /* Fill o with the reference's defaults. */
 void ode_options_default(ode_options* o);
+/* sizeof(ode_options) and sizeof(ode_problem_desc) as compiled: bindings that
+ * mirror the structs (Julia, Python) check their layout against these. */
+size_t ode_options_size(void);
+size_t ode_problem_desc_size(void);
 
 /* Open device `device`; hbm_budget bytes caps device memory the handle may
  * hold (0: 90% of free memory).  One CUDA stream per handle. */

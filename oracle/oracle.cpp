@@ -910,16 +910,42 @@ bool is_event(const Integ& I, double bs, double ts) {
 // find_root with LeftRootFind (callbacks.jl:480-492): the reference runs ModAB
 // (BracketingNonlinearSolve, not vendored) with abstol = reltol = 0, i.e. to
 // adjacent floats, and returns the left end (or a point where the condition is
-// exactly 0).  Bisection to adjacent floats ends at the same bracket.
-double find_root_left(Integ& I, double a, double b) {
-    const double fa = cond_at(I, a);
+// exactly 0).  Any bracketing method run to adjacent floats ends at the same
+// pair where the sign change is unique; this one is Anderson-Bjorck false
+// position (the secant point; when the same end is replaced twice in a row the
+// retained end's value is scaled by 1 - f_new/f_replaced, or 1/2 when that is
+// not positive) with a bisection whenever the bracket has not halved over two
+// steps or the secant point is not strictly inside.  fa = f(a), fb = f(b) of
+// opposite signs, nonzero.
+double find_root_left(Integ& I, double a, double b, double fa, double fb) {
+    int side = 0;
+    double w_prev = b - a, w_prev2 = 2.0 * (b - a);
     for (int it = 0; it < 2200; ++it) {
-        const double m = a + (b - a) * 0.5;
+        const double w = b - a;
+        double m = (w > 0.5 * w_prev2) ? a + w * 0.5 : a + w * (fa / (fa - fb));
+        if (!(m > a && m < b)) m = a + w * 0.5;
         if (!(m > a && m < b)) break;
         const double fm = cond_at(I, m);
         if (fm == 0.0) return m;
-        if ((fm > 0) == (fa > 0)) a = m;
-        else b = m;
+        w_prev2 = w_prev;
+        w_prev = w;
+        if ((fm > 0.0) == (fa > 0.0)) {
+            if (side == -1) {
+                const double g = 1.0 - fm / fa;
+                fb *= g > 0.0 ? g : 0.5;
+            }
+            a = m;
+            fa = fm;
+            side = -1;
+        } else {
+            if (side == +1) {
+                const double g = 1.0 - fm / fb;
+                fa *= g > 0.0 ? g : 0.5;
+            }
+            b = m;
+            fb = fm;
+            side = +1;
+        }
     }
     return a;
 }
@@ -935,14 +961,16 @@ bool find_callback_time(Integ& I, double& cb_t, double& bottom_sign, double& res
     }
     const double bs = jsign(bc);
     double top_t = I.t;
-    double ts = jsign(cond_at(I, top_t));
+    double tv = cond_at(I, top_t);
+    double ts = jsign(tv);
     bool occ = is_event(I, bs, ts);
     if (I.o.interp_points != 0 && !occ) {
         // range(tprev, stop = t, length = interp_points)
         const int m = I.o.interp_points;
         for (int i = 2; i <= m; ++i) {
             top_t = i == m ? I.t : I.tprev + (I.t - I.tprev) * ((double)(i - 1) / (double)(m - 1));
-            ts = jsign(cond_at(I, top_t));
+            tv = cond_at(I, top_t);
+            ts = jsign(tv);
             occ = is_event(I, bs, ts);
             if (occ) break;
         }
@@ -956,7 +984,7 @@ bool find_callback_time(Integ& I, double& cb_t, double& bottom_sign, double& res
     if (ts == 0.0) {
         cb_t = top_t;
     } else {
-        cb_t = find_root_left(I, bottom_t, top_t);
+        cb_t = find_root_left(I, bottom_t, top_t, bc, tv);
         residual = cond_at(I, cb_t);
     }
     return true;

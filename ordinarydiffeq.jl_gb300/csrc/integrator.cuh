@@ -42,6 +42,51 @@ enum RetCode { RC_DEFAULT = 0, RC_SUCCESS = 1, RC_MAXITERS = 2, RC_DTNAN = 3, RC
 template <class A, class = void> struct is_composite_alg : std::false_type {};
 template <class A> struct is_composite_alg<A, std::void_t<decltype(A::COMPOSITE)>> : std::true_type {};
 
+// The left end of a sign change of f in [lo, hi] narrowed to adjacent floats
+// (LeftRootFind: the reference solves IntervalNonlinearProblem with ModAB,
+// BracketingNonlinearSolve, at abstol = reltol = 0 and returns the left
+// bracket; any bracketing method run to adjacent floats ends at the same pair
+// where the sign change is unique).  Anderson-Bjorck false position: the
+// secant point of the bracket; when the same end is replaced twice in a row
+// the retained end's value is scaled by 1 - f_new/f_replaced (by 1/2 when that
+// is not positive); a bisection whenever the bracket has not halved over two
+// steps, or when the secant point is not strictly inside the bracket.  flo and fhi are
+// f(lo) and f(hi), of opposite signs and nonzero.  The oracle runs the same
+// iteration.
+template <class F>
+__device__ __forceinline__ double bracket_left_root(F&& f, double lo, double hi, double flo, double fhi) {
+    int side = 0;
+    double w_prev = hi - lo, w_prev2 = 2.0 * (hi - lo);
+    for (int it = 0; it < 2200; ++it) {
+        const double w = hi - lo;
+        double m = (w > 0.5 * w_prev2) ? lo + w * 0.5 : lo + w * (flo / (flo - fhi));
+        if (!(m > lo && m < hi)) m = lo + w * 0.5;
+        if (!(m > lo && m < hi)) break;   // adjacent floats
+        const double fm = f(m);
+        if (fm == 0.0) return m;
+        w_prev2 = w_prev;
+        w_prev = w;
+        if ((fm > 0.0) == (flo > 0.0)) {
+            if (side == -1) {
+                const double g = 1.0 - fm / flo;
+                fhi *= g > 0.0 ? g : 0.5;
+            }
+            lo = m;
+            flo = fm;
+            side = -1;
+        } else {
+            if (side == +1) {
+                const double g = 1.0 - fm / fhi;
+                flo *= g > 0.0 ? g : 0.5;
+            }
+            hi = m;
+            fhi = fm;
+            side = +1;
+        }
+    }
+    return lo;
+}
+
 // sign() with Julia's NaN behaviour
 __device__ __forceinline__ double dsign(double x) { return x > 0.0 ? 1.0 : (x < 0.0 ? -1.0 : (x == 0.0 ? 0.0 : x)); }
 // ContinuousCallback defaults (SciMLBase): abstol = 10eps(), repeat_nudge = 1//100
@@ -405,13 +450,15 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             }
             const double bs = dsign(bc);
             double top_t = t;
-            double ts = dsign(cond_at(top_t));
+            double tv = cond_at(top_t);
+            double ts = dsign(tv);
             bool occ = is_event(bs, ts);
             if (a.interp_points != 0 && !occ) {   // range(tprev, stop = t, length = interp_points)
                 const int m = a.interp_points;
                 for (int i = 2; i <= m; ++i) {
                     top_t = i == m ? t : tprev + (t - tprev) * ((double)(i - 1) / (double)(m - 1));
-                    ts = dsign(cond_at(top_t));
+                    tv = cond_at(top_t);
+                    ts = dsign(tv);
                     occ = is_event(bs, ts);
                     if (occ) break;
                 }
@@ -422,19 +469,7 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             }
             double cb_t = top_t, residual = 0.0;
             if (ts != 0.0) {
-                double lo = bottom_t, hi = top_t;
-                for (int it = 0; it < 2200; ++it) {
-                    const double mid = lo + (hi - lo) * 0.5;
-                    if (!(mid > lo && mid < hi)) break;
-                    const double fm = cond_at(mid);
-                    if (fm == 0.0) {
-                        lo = mid;
-                        break;
-                    }
-                    if ((fm > 0.0) == (bs > 0.0)) lo = mid;
-                    else hi = mid;
-                }
-                cb_t = lo;
+                cb_t = bracket_left_root(cond_at, bottom_t, top_t, bc, tv);
                 residual = cond_at(cb_t);
             }
             ev_last = true;

@@ -1074,6 +1074,9 @@ void ode_options_default(ode_options* o) {
     o->interp_points = 10;
 }
 
+size_t ode_options_size(void) { return sizeof(ode_options); }
+size_t ode_problem_desc_size(void) { return sizeof(ode_problem_desc); }
+
 int ode_create(int device, size_t hbm_budget, ode_handle** out) {
     if (!out) return fail(nullptr, ODE_E_INVALID, "null output pointer");
     *out = nullptr;

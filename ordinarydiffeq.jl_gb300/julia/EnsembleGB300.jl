@@ -125,6 +125,10 @@ end
 const HANDLES = Dict{Int, Ptr{Cvoid}}()
 function handle(dev)
     get!(HANDLES, dev) do
+        # the struct mirrors above must match the library's layout
+        ccall((:ode_options_size, LIB), Csize_t, ()) == sizeof(Options) &&
+            ccall((:ode_problem_desc_size, LIB), Csize_t, ()) == sizeof(ProblemDesc) ||
+            error("EnsembleGB300: Options/ProblemDesc do not match the library's ode_options/ode_problem_desc")
         h = Ref{Ptr{Cvoid}}(C_NULL)
         rc = ccall((:ode_create, LIB), Cint, (Cint, Csize_t, Ref{Ptr{Cvoid}}), dev, 0, h)
         rc == 0 || error("ode_create failed: ", unsafe_string(ccall((:ode_last_error, LIB), Cstring, (Ptr{Cvoid},), C_NULL)))

@@ -51,6 +51,8 @@ _IP = C.POINTER(C.c_int32)
 SIGNATURES = {
     "ode_abi_version": (C.c_int, []),
     "ode_options_default": (None, [C.POINTER(Options)]),
+    "ode_options_size": (C.c_size_t, []),
+    "ode_problem_desc_size": (C.c_size_t, []),
     "ode_create": (C.c_int, [C.c_int, C.c_size_t, C.POINTER(_VP)]),
     "ode_destroy": (None, [_VP]),
     "ode_last_error": (C.c_char_p, [_VP]),

@@ -35,6 +35,12 @@ def test_library_exports_every_declared_symbol():
     assert names <= set(_lib.SIGNATURES), names - set(_lib.SIGNATURES)
 
 
+def test_struct_layouts_match_the_bindings():
+    L = _lib.load()
+    assert L.ode_options_size() == C.sizeof(_lib.Options)
+    assert L.ode_problem_desc_size() == C.sizeof(_lib.ProblemDesc)
+
+
 def test_abi_version_and_defaults_without_gpu():
     L = _lib.load()
     assert L.ode_abi_version() == 3

@@ -42,6 +42,9 @@ def test_events_match_oracle_fp64(alg):
     gu, ou = g["u"][:ns], o["u"][:ns]
     mu = ~np.isnan(ou)
     assert np.all(np.abs(gu[mu] - ou[mu]) <= 10 * (rt * np.abs(ou[mu]) + at))
+    # counters: the FSAL re-evaluation after an event is counted on both sides
+    for k in ("nf", "naccept", "nreject", "njacs"):
+        assert np.abs(g["stats"][k] - o["stats"][k]).max() <= 16, k
 
 
 def test_events_mixed_match_fp64():
