@@ -106,6 +106,11 @@ def load(build_if_missing=True):
         fn = getattr(L, name)
         fn.restype = res
         fn.argtypes = args
+    # the ctypes mirrors must match the library's struct layouts
+    if L.ode_options_size() != C.sizeof(Options) or L.ode_problem_desc_size() != C.sizeof(ProblemDesc):
+        raise RuntimeError("odegb300: Options/ProblemDesc do not match the library's ode_options/ode_problem_desc "
+                           "(%d/%d vs %d/%d bytes)" % (C.sizeof(Options), C.sizeof(ProblemDesc),
+                                                       L.ode_options_size(), L.ode_problem_desc_size()))
     _lib = L
     return L
 
