@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define ODE_ABI_VERSION 3
+#define ODE_ABI_VERSION 4
 
 typedef struct ode_handle ode_handle;
 
@@ -131,7 +131,13 @@ typedef struct {
     int32_t interp_points;      /* the callback's interp_points (default 10) */
     int32_t max_events;         /* save slots for events: 2 per event (before and after its affect) are added to
                                    the output, and past the total the last slot keeps the latest save */
-    int32_t reserved_options;
+    int32_t ntstops;            /* the solve's tstops, shared by every trajectory (solve.jl:1021-1040): */
+    const double* tstops;       /* a trajectory stops exactly at each ts with t0 < ts < tf, as at tf
+                                   (modify_dt_for_tstops!, handle_tstop!); duplicates allowed.  Host
+                                   memory in any order (NaN rejected) for ode_solve_ensemble,
+                                   ode_solve_ensemble_dense, ode_submit and ode_autotune; device
+                                   memory sorted ascending for ode_solve_ensemble_device and
+                                   ode_solve_ensemble_noalloc (entries out of order or NaN are skipped) */
 } ode_options;
 
 /* Fill o with the reference's defaults. */

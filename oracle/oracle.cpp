@@ -1485,6 +1485,7 @@ int orc_solve_ensemble(int alg, int model, int nmax, const int32_t* n_per_traj, 
     std::atomic<int64_t> next(0);
     auto worker = [&]() {
         std::vector<double> uj(nmax), pj(np), sv(nsave > 0 ? nsave : 1), tl(cap), ul((size_t)cap * nmax);
+        std::vector<double> ts;
         Integ I;
         for (;;) {
             int64_t j = next.fetch_add(1);
@@ -1494,8 +1495,11 @@ int orc_solve_ensemble(int alg, int model, int nmax, const int32_t* n_per_traj, 
             for (int i = 0; i < np; ++i) pj[i] = p[(size_t)i * N + j];
             for (int s = 0; s < nsave; ++s) sv[s] = saveat_per_traj ? saveat[(size_t)s * N + j] : saveat[s];
             double t0 = tspan[j], tf = tspan[N + j];
-            setup(I, alg, model, n, pj.data(), t0, tf, o, sv.data(), nsave, o->saveat_as_tstops ? sv.data() : nullptr,
-                  o->saveat_as_tstops ? nsave : 0);
+            ts.clear();
+            if (o->saveat_as_tstops) ts.insert(ts.end(), sv.begin(), sv.begin() + nsave);
+            if (o->ntstops > 0 && o->tstops) ts.insert(ts.end(), o->tstops, o->tstops + o->ntstops);
+            setup(I, alg, model, n, pj.data(), t0, tf, o, sv.data(), nsave, ts.empty() ? nullptr : ts.data(),
+                  (int)ts.size());
             I.t_out = tl.data();
             I.u_out = ul.data();
             I.cap = cap;

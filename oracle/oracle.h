@@ -52,7 +52,8 @@ typedef struct {
     int32_t callback;         /* 1: the model's ContinuousCallback (ORC_BOUNCING_BALL) */
     int32_t interp_points;    /* ContinuousCallback interp_points (SciMLBase default 10) */
     int32_t max_events;       /* ensemble: 2 more save slots per event */
-    int32_t reserved;
+    int32_t ntstops;          /* ensemble: user tstops shared by every trajectory, */
+    const double* tstops;     /* kept where t0 < ts < tf (initialize_tstops) */
 } orc_opts;
 
 /* Solve one trajectory.  saveat: nsave_in times in (t0, tf] sorted ascending.

@@ -34,7 +34,8 @@ class Opts(C.Structure):
         ("save_end_user", C.c_int32), ("saveat_given", C.c_int32), ("saveat_scalar", C.c_int32),
         ("qmax_first_step", C.c_double), ("qmax", C.c_double), ("saveat_as_tstops", C.c_int32),
         ("save_everystep", C.c_int32), ("max_step_saves", C.c_int32),
-        ("callback", C.c_int32), ("interp_points", C.c_int32), ("max_events", C.c_int32), ("reserved", C.c_int32),
+        ("callback", C.c_int32), ("interp_points", C.c_int32), ("max_events", C.c_int32), ("ntstops", C.c_int32),
+        ("tstops", C.POINTER(C.c_double)),
     ]
 
 
@@ -83,11 +84,15 @@ def _dp(a):
 def make_opts(reltol=1e-3, abstol=1e-6, dtmax=0.0, dtmin=0.0, dt=0.0, adaptive=True,
               maxiters=1000000, save_start=False, save_end=True, save_end_user=-1,
               saveat_given=True, saveat_scalar=False, qmax_first_step=0.0, qmax=0.0, saveat_as_tstops=False,
-              save_everystep=False, max_step_saves=0, callback=False, interp_points=10, max_events=0):
-    return Opts(reltol, abstol, dtmax, dtmin, dt, int(adaptive), maxiters, int(save_start),
-                int(save_end), save_end_user, int(saveat_given), int(saveat_scalar),
-                qmax_first_step, qmax, int(saveat_as_tstops), int(save_everystep), int(max_step_saves),
-                int(callback), int(interp_points), int(max_events), 0)
+              save_everystep=False, max_step_saves=0, callback=False, interp_points=10, max_events=0,
+              tstops=()):
+    ts = np.ascontiguousarray(tstops, dtype=np.float64).ravel()
+    o = Opts(reltol, abstol, dtmax, dtmin, dt, int(adaptive), maxiters, int(save_start),
+             int(save_end), save_end_user, int(saveat_given), int(saveat_scalar),
+             qmax_first_step, qmax, int(saveat_as_tstops), int(save_everystep), int(max_step_saves),
+             int(callback), int(interp_points), int(max_events), int(ts.size), _dp(ts) if ts.size else None)
+    o._tstops = ts   # keeps the array alive as long as the options
+    return o
 
 
 def solve(alg, model, u0, p, tspan, saveat=(), tstops=(), dense=False, **kw):

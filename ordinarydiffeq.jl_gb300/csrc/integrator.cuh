@@ -507,9 +507,17 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
         return false;
     };
 
+    // the tstops heap (initialize_tstops, solve.jl:1021-1040): the shared ascending
+    // tstops inside (t0, tf), then tf.  Entries not after t leave it at each loop
+    // header: the ones at t0 and, after a step landed on a tstop, every copy of it
+    // (handle_tstop!, integrator_utils.jl:1290-1313); NaNs and out-of-order
+    // entries are dropped the same way.
+    int itst = 0;
     while (t < tf) {
         // ---- loopheader!
-        const double dist = tf - t;   // > 0 inside the loop; the only tstop is tf
+        while (itst < a.ntstops && !(a.tstops[itst] > t)) itst++;
+        const double tnext = (itst < a.ntstops && a.tstops[itst] < tf) ? a.tstops[itst] : tf;   // first_tstop
+        const double dist = tnext - t;   // > 0 inside the loop
         if (iter > 0) {
             if (accept) {
                 success_iter++;
@@ -551,7 +559,7 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
         dt = pmin(dtmax, dt);
         dt = pmax(dt, pabs(pmax(peps(t), a.dtmin)));
         {   // modify_dt_for_tstops!
-            const double tol = ptol100(pmax(pabs(t), pabs(tf)));
+            const double tol = ptol100(pmax(pabs(t), pabs(tnext)));
             const double orig = pabs(dt);
             dtpropose = orig;
             next_tstop = !plt(orig + tol, dist);
@@ -565,7 +573,7 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             if (!do_error_check) e = RC_SUCCESS;
             else if (bits_nan(db)) e = RC_DTNAN;
             else if (iter > a.maxiters) e = RC_MAXITERS;
-            else if (ple(pabs(dt), pabs(a.dtmin)) && (!accept || t + dt < tf)) e = RC_DTLESSTHANMIN;
+            else if (ple(pabs(dt), pabs(a.dtmin)) && (!accept || t + dt < tnext)) e = RC_DTLESSTHANMIN;
             else if (!accept && ple(pabs(dt), peps(t))) e = RC_UNSTABLE;
             else if (accept) {
                 bool bad = false;
@@ -603,7 +611,7 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             if (next_tstop) {
                 dt = dtpropose;
                 next_tstop = false;
-                t = tf;
+                t = tnext;   // the tstop target
             } else {
                 t = ttmp;
             }

@@ -120,6 +120,7 @@ struct ode_handle {
     // staging for the synchronous host API
     DevBuf b_u0, b_p, b_tspan, b_saveat, b_t, b_u, b_ns, b_rc, b_st, b_npt;
     DevBuf b_k, b_tq, b_out;                 // dense output and its evaluation
+    DevBuf b_tstops;                         // the host API's tstops, sorted
     // copy streams and events of the chunked host-API pipeline
     cudaStream_t copy_in = nullptr, copy_out = nullptr;
     cudaEvent_t pipe_in[4] = {}, pipe_done[4] = {};
@@ -201,6 +202,40 @@ int validate(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int
         return fail(h, ODE_E_UNSUPPORTED, "save_everystep together with saveat is not supported");
     if (o->save_everystep && o->max_step_saves <= 0)
         return fail(h, ODE_E_INVALID, "save_everystep needs max_step_saves > 0");
+    if (o->ntstops < 0 || (o->ntstops > 0 && !o->tstops))
+        return fail(h, ODE_E_INVALID, "ntstops < 0, or tstops is null");
+    return ODE_OK;
+}
+
+// The host entry points take tstops in host memory, in any order: checked for
+// NaN here, then sorted (the kernels walk them in ascending order).
+int check_host_tstops(ode_handle* h, const ode_options* o) {
+    for (int32_t i = 0; i < o->ntstops; ++i)
+        if (o->tstops[i] != o->tstops[i]) return fail(h, ODE_E_INVALID, "NaN in tstops");
+    return ODE_OK;
+}
+
+std::vector<double> sorted_tstops(const ode_options* o) {
+    std::vector<double> v;
+    if (o->ntstops > 0) v.assign(o->tstops, o->tstops + o->ntstops);
+    std::sort(v.begin(), v.end());
+    return v;
+}
+
+// Copy the sorted tstops into the handle's buffer on stream s (synchronously:
+// they are a few bytes) and return in ot the options with tstops pointing
+// there, the form the launch code takes.
+int stage_tstops(ode_handle* h, const ode_options* o, cudaStream_t s, ode_options* ot) {
+    *ot = *o;
+    ot->tstops = nullptr;
+    const std::vector<double> v = sorted_tstops(o);
+    ot->ntstops = (int32_t)v.size();
+    if (v.empty()) return ODE_OK;
+    int rc = grow(h, h->b_tstops, v.size() * 8);
+    if (rc) return rc;
+    CUDA_TRY(h, cudaMemcpyAsync(h->b_tstops.p, v.data(), v.size() * 8, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(h, cudaStreamSynchronize(s));
+    ot->tstops = (const double*)h->b_tstops.p;
     return ODE_OK;
 }
 
@@ -229,6 +264,8 @@ EnsembleArgs make_args(ode_handle* h, const ode_problem_desc* d, const ode_optio
     a.save_everystep = o->save_everystep;
     a.callback = o->callback ? 1 : 0;
     a.interp_points = o->interp_points;
+    a.tstops = o->ntstops > 0 ? o->tstops : nullptr;   // device memory, ascending, at this point
+    a.ntstops = o->ntstops > 0 ? o->ntstops : 0;
     a.t_out = t_out;
     a.u_out = u_out;
     a.nsaved = nsaved;
@@ -757,6 +794,9 @@ int solve_host(ode_handle* h, const ode_problem_desc* d, const ode_options* o, i
     std::lock_guard<std::mutex> lk(h->api_mu);
     CUDA_TRY(h, cudaSetDevice(h->device));
     *h->h_abort = 0;
+    ode_options ostaged;
+    if ((rc = stage_tstops(h, o, h->main.stream, &ostaged))) return rc;
+    o = &ostaged;
     if (N > 0) {   // every buffer page-locked: the kernels work in place, no staging copies
         const double *mu0 = mapped_ptr(u0), *mp = mapped_ptr(p), *mts = mapped_ptr(tspan);
         const double* msv = o->nsave > 0 ? mapped_ptr(saveat) : nullptr;
@@ -830,7 +870,7 @@ struct Request {
     ode_problem_desc d;
     ode_options o;
     int64_t N = 0;
-    std::vector<double> u0, p, tspan, saveat;
+    std::vector<double> u0, p, tspan, saveat, tstops;   // tstops sorted; o.tstops is unused
     std::vector<int32_t> npt;
     double* t_out = nullptr;
     double* u_out = nullptr;
@@ -857,7 +897,7 @@ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // direction is one contiguous copy.  The pinned staging of the slot and the
 // device block share this layout.
 struct Layout {
-    size_t u0, p, ts, sv, npt, in_end, t, u, ns, rc, st, total;
+    size_t u0, p, ts, sv, tst, npt, in_end, t, u, ns, rc, st, total;
 };
 Layout layout(const Request& r) {
     const size_t n = (size_t)r.d.n_states, np = (size_t)r.d.n_params, N = (size_t)r.N, cap = save_cap(&r.o);
@@ -868,6 +908,7 @@ Layout layout(const Request& r) {
     L.p = take(np * N * 8);
     L.ts = take(2 * N * 8);
     L.sv = take(std::max<size_t>(r.saveat.size(), 1) * 8);
+    L.tst = take(std::max<size_t>(r.tstops.size(), 1) * 8);
     L.npt = r.npt.empty() ? (size_t)-1 : take(N * 4);
     L.in_end = off;
     L.t = take(cap * N * 8);
@@ -901,11 +942,15 @@ int admit(ode_handle* h, Request& r, int k) {
     std::memcpy(hs + L.p, r.p.data(), np * N * 8);
     std::memcpy(hs + L.ts, r.tspan.data(), 2 * N * 8);
     if (!r.saveat.empty()) std::memcpy(hs + L.sv, r.saveat.data(), r.saveat.size() * 8);
+    if (!r.tstops.empty()) std::memcpy(hs + L.tst, r.tstops.data(), r.tstops.size() * 8);
     if (!r.npt.empty()) std::memcpy(hs + L.npt, r.npt.data(), N * 4);
     CUDA_TRY(h, cudaMallocAsync(&r.dmem, L.total, s));
     char* base = (char*)r.dmem;
     CUDA_TRY(h, cudaMemcpyAsync(base, hs, L.in_end, cudaMemcpyHostToDevice, s));
-    int rc = run_ensemble(h, c, &r.d, &r.o, r.N, r.npt.empty() ? nullptr : (const int32_t*)(base + L.npt),
+    ode_options o = r.o;
+    o.ntstops = (int32_t)r.tstops.size();
+    o.tstops = r.tstops.empty() ? nullptr : (const double*)(base + L.tst);
+    int rc = run_ensemble(h, c, &r.d, &o, r.N, r.npt.empty() ? nullptr : (const int32_t*)(base + L.npt),
                           (const double*)(base + L.u0), (const double*)(base + L.p), (const double*)(base + L.ts),
                           (const double*)(base + L.sv), (double*)(base + L.t), (double*)(base + L.u),
                           (int32_t*)(base + L.ns), (int32_t*)(base + L.rc), (OdeStatsDev*)(base + L.st), s);
@@ -1107,7 +1152,7 @@ void ode_destroy(ode_handle* h) {
     cudaSetDevice(h->device);
     cudaDeviceSynchronize();
     for (auto& r : h->running) finish(h, *r);
-    for (DevBuf* b : {&h->b_u0, &h->b_p, &h->b_tspan, &h->b_saveat, &h->b_t, &h->b_u, &h->b_ns, &h->b_rc,
+    for (DevBuf* b : {&h->b_u0, &h->b_p, &h->b_tspan, &h->b_saveat, &h->b_tstops, &h->b_t, &h->b_u, &h->b_ns, &h->b_rc,
                       &h->b_st, &h->b_npt})
         if (b->p) cudaFree(b->p);
     ctx_free(h->main);
@@ -1153,6 +1198,7 @@ int ode_solve_ensemble(ode_handle* h, const ode_problem_desc* d, const ode_optio
         return fail(h, ODE_E_INVALID, "null input or output buffer");
     if (o->nsave > 0 && !saveat) return fail(h, ODE_E_INVALID, "nsave > 0 but saveat is null");
     if ((rc = check_sizes(h, d, npt, N))) return rc;
+    if ((rc = check_host_tstops(h, o))) return rc;
     return solve_host(h, d, o, N, npt, u0, p, tspan, saveat, t_out, u_out, nullptr, nsaved, retcode, stats);
 }
 
@@ -1171,6 +1217,7 @@ int ode_solve_ensemble_dense(ode_handle* h, const ode_problem_desc* d, const ode
     if (kDenseVectors[d->alg_id] == 0) return fail(h, ODE_E_UNSUPPORTED, "no dense output for this method");
     if (N > 0 && (!u0 || !p || !tspan || !u_out || !k_out || !nsaved || !retcode))
         return fail(h, ODE_E_INVALID, "null input or output buffer");
+    if ((rc = check_host_tstops(h, o))) return rc;
     return solve_host(h, d, o, N, nullptr, u0, p, tspan, nullptr, t_out, u_out, k_out, nsaved, retcode, stats);
 }
 
@@ -1255,9 +1302,13 @@ int ode_submit(ode_handle* h, const ode_problem_desc* d, const ode_options* o, i
         return fail(h, ODE_E_INVALID, "null input or output buffer");
     if (o->nsave > 0 && !saveat) return fail(h, ODE_E_INVALID, "nsave > 0 but saveat is null");
     if ((rc = check_sizes(h, d, npt, N))) return rc;
+    if ((rc = check_host_tstops(h, o))) return rc;
     auto r = std::make_shared<Request>();
     r->d = *d;
     r->o = *o;
+    r->tstops = sorted_tstops(o);
+    r->o.tstops = nullptr;
+    r->o.ntstops = (int32_t)r->tstops.size();
     r->N = N;
     const size_t n = (size_t)d->n_states, np = (size_t)d->n_params;
     r->u0.assign(u0, u0 + n * N);
@@ -1394,9 +1445,13 @@ int ode_autotune(ode_handle* h, const ode_problem_desc* d, const ode_options* o,
     if (rc) return rc;
     if (N <= 0 || !u0 || !p || !tspan) return fail(h, ODE_E_INVALID, "autotune needs a non-empty sample");
     if (o->nsave > 0 && !saveat) return fail(h, ODE_E_INVALID, "nsave > 0 but saveat is null");
+    if ((rc = check_host_tstops(h, o))) return rc;
     std::lock_guard<std::mutex> lk(h->api_mu);
     CUDA_TRY(h, cudaSetDevice(h->device));
     *h->h_abort = 0;
+    ode_options ostaged;
+    if ((rc = stage_tstops(h, o, h->main.stream, &ostaged))) return rc;
+    o = &ostaged;
     const size_t n = (size_t)d->n_states, np = (size_t)d->n_params, cap = save_cap(o);
     const size_t nsv = (size_t)o->nsave * (o->saveat_per_traj ? (size_t)N : 1);
     if ((rc = grow(h, h->b_u0, n * N * 8)) || (rc = grow(h, h->b_p, np * N * 8)) ||
@@ -1556,7 +1611,8 @@ extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_o
         d->model_id < ODE_MODEL_LINEAR || d->model_id > ODE_MODEL_VANDERPOL || d->n_states <= 0 ||
         (o->callback && !model_has_event(d->model_id)) ||
         d->n_params != model_nparams(d->model_id) || !(o->reltol > 0) || !(o->abstol >= 0) || o->nsave < 0 ||
-        (o->save_everystep && (o->nsave > 0 || o->max_step_saves <= 0)))
+        (o->save_everystep && (o->nsave > 0 || o->max_step_saves <= 0)) ||
+        o->ntstops < 0 || (o->ntstops > 0 && !o->tstops))
         return fail(nullptr, ODE_E_INVALID, "invalid problem description or options");
     if (npt_dev && d->model_id != ODE_MODEL_DUFFING_CHAIN)
         return fail(nullptr, ODE_E_UNSUPPORTED, "per-trajectory sizes are supported for DUFFING_CHAIN");
@@ -1588,6 +1644,8 @@ extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_o
     a.save_everystep = o->save_everystep;
     a.callback = o->callback ? 1 : 0;
     a.interp_points = o->interp_points;
+    a.tstops = o->ntstops > 0 ? o->tstops : nullptr;   // device memory, ascending
+    a.ntstops = o->ntstops > 0 ? o->ntstops : 0;
     a.t_out = t_out;
     a.u_out = u_out;
     a.nsaved = nsaved;

@@ -38,6 +38,8 @@ struct EnsembleArgs {
     int save_everystep;     // save every accepted step (saveat empty); nsave_cap bounds the slots
     int callback;           // 1: the model's ContinuousCallback (models with HAS_EVENT)
     int interp_points;      // its interp_points
+    const double* tstops;   // the solve's tstops, ascending, shared by every trajectory
+    int ntstops;
     double* k_out;          // dense output (nullptr: none): k_out[((s*NDENSE + q)*nmax + i)*N + j], the
                             // method's NDENSE interpolation vectors of the step ending at save s
     double qmax_first_step, qmax;

@@ -67,7 +67,7 @@ mutable struct Options
     save_start::Int32; save_end::Int32; save_end_user::Int32; saveat_scalar::Int32; nsave::Int32
     saveat_per_traj::Int32; qmax_first_step::Float64; qmax::Float64; lanes_per_traj::Int32
     scheduler::Int32; block_size::Int32; ir_sweeps::Int32; save_everystep::Int32; max_step_saves::Int32
-    callback::Int32; interp_points::Int32; max_events::Int32; reserved_options::Int32
+    callback::Int32; interp_points::Int32; max_events::Int32; ntstops::Int32; tstops::Ptr{Float64}
 end
 struct Stats
     nf::Int64; njacs::Int64; nw::Int64; nsolve::Int64; naccept::Int64; nreject::Int64
@@ -142,7 +142,7 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem,
                            dt = 0.0, dtmax = 0.0, dtmin = 0.0, maxiters = 1_000_000, save_start = nothing,
                            save_end = nothing, save_everystep = isempty(saveat), max_step_saves = 1024, seed = 0,
                            callback = nothing, dense = save_everystep && isempty(saveat) && callback === nothing,
-                           kwargs...)
+                           tstops = Float64[], kwargs...)
     t0 = time()
     N = trajectories
     probs = [eprob.prob_func(eprob.prob, SciMLBase.EnsembleContext(i, 1, seed)) for i in 1:N]
@@ -168,16 +168,19 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem,
     callback === nothing || callback isa GB300Callback ||
         error("EnsembleGB300 runs the model's registered callback only: pass GB300Callback(...)")
     cb = callback isa GB300Callback
+    # the solve's tstops (solve.jl:1021-1040): the library keeps those inside each (t0, tf)
+    tst = collect(Float64, tstops)
     o = Options(reltol, abstol, dtmax, dtmin, dt, maxiters, ss, se, save_end === nothing ? -1 : Int32(save_end),
                 scalar, length(sv), 0, 0.0, 0.0, ens.lanes_per_traj, ens.scheduler, 0, -1, everystep,
-                everystep ? max_step_saves : 0, cb, cb ? callback.interp_points : 10, cb ? callback.max_events : 0, 0)
+                everystep ? max_step_saves : 0, cb, cb ? callback.interp_points : 10, cb ? callback.max_events : 0,
+                length(tst), isempty(tst) ? Ptr{Float64}(C_NULL) : pointer(tst))
     d = ProblemDesc(model, alg_id(alg), n, npar, ens.precision === :mixed ? 1 : 0, 0)
     cap = (everystep ? max_step_saves : length(sv)) + 2 + (cb ? 2 * callback.max_events : 0)
     t_out = fill(NaN, N, cap); u_out = fill(NaN, N, n, cap)   # [(s*n + i)*N + j] -> u_out[j, i, s]
     nsaved = zeros(Int32, N); rc = zeros(Int32, N); st = Vector{Stats}(undef, N)
     # dense output (solve.jl:145-146) for every-step saves of one state count
     isdense = dense && everystep && npt == C_NULL
-    if isdense
+    GC.@preserve tst if isdense   # o holds a pointer into tst
         nk = ccall((:ode_dense_nk, LIB), Cint, (Cint,), alg_id(alg))
         k_out = zeros(N, n, nk, cap)   # [((s*nk + q)*n + i)*N + j] -> k_out[j, i, q, s]
         status = ccall((:ode_solve_ensemble_dense, LIB), Cint,

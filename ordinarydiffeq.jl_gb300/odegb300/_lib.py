@@ -31,7 +31,7 @@ class Options(C.Structure):
                 ("scheduler", C.c_int32), ("block_size", C.c_int32), ("ir_sweeps", C.c_int32),
                 ("save_everystep", C.c_int32), ("max_step_saves", C.c_int32),
                 ("callback", C.c_int32), ("interp_points", C.c_int32), ("max_events", C.c_int32),
-                ("reserved_options", C.c_int32)]
+                ("ntstops", C.c_int32), ("tstops", C.POINTER(C.c_double))]
 
 
 class Stats(C.Structure):

@@ -279,7 +279,8 @@ def get_handle(device=0):
     return h
 
 
-def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax, callback=None):
+def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax, callback=None,
+             tstops=None):
     o = _lib.Options()
     L = _lib.load()
     L.ode_options_default(C.byref(o))
@@ -304,13 +305,20 @@ def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_ste
         o.callback = 1
         o.interp_points = int(callback.interp_points)
         o.max_events = int(callback.max_events)
+    if tstops is not None and np.size(tstops) > 0:
+        ts = np.ascontiguousarray(np.atleast_1d(tstops), dtype=np.float64).ravel()
+        if np.isnan(ts).any():
+            raise ValueError("tstops contain NaN")
+        o.ntstops = ts.size
+        o.tstops = ts.ctypes.data_as(C.POINTER(C.c_double))
+        o._tstops = ts   # the options hold the array while the call reads it
     return o
 
 
 def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=1e-6, dt=None,
                  dtmax=None, dtmin=None, maxiters=1000000, save_start=None, save_end=None, n_per_traj=None,
                  qmax_first_step=None, qmax=None, return_times=False, save_everystep=False, max_step_saves=1024,
-                 dense=False, callback=None):
+                 dense=False, callback=None, tstops=None):
     """Solve a packed ensemble.  u0s (n, N), ps (np, N), tspans (2, N).  Returns the
     raw structure-of-arrays outputs dict (t, u, nsaved, retcode, stats).
     save_everystep (without saveat) keeps every accepted step, up to
@@ -318,7 +326,9 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
     point and a warning is issued).  dense (with save_everystep) also keeps
     each step's interpolation vectors, k (cap, nk, n, N), for dense_eval.
     callback: the model's ContinuousCallback (ContinuousCallback(...)); a
-    trajectory it terminates reports ReturnCode.Terminated."""
+    trajectory it terminates reports ReturnCode.Terminated.  tstops: times every
+    trajectory steps to exactly (those inside its (t0, tf)), as the reference's
+    tstops keyword."""
     L = _lib.load()
     if isinstance(model, str):
         model = MODELS[model]
@@ -327,7 +337,7 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
     tspans = np.ascontiguousarray(tspans, dtype=np.float64)
     n, N = u0s.shape
     sv = resolve_saveat(saveat, tspans, save_start, save_end, save_everystep, max_step_saves)
-    o = _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax, callback)
+    o = _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax, callback, tstops)
     d = _lib.ProblemDesc(model, alg.alg_id, n, ps.shape[0], ens.prec_id(), 0)
     cap = sv.cap + (2 * callback.max_events if callback is not None else 0)
     if dense and callback is not None:
@@ -430,14 +440,15 @@ def autotune(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=
 def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, saveat=None, reltol=1e-3,
           abstol=1e-6, dt=None, dtmax=None, dtmin=None, maxiters=1000000, save_start=None, save_end=None,
           seed=0, qmax_first_step=None, qmax=None, save_everystep=None, max_step_saves=1024, dense=None,
-          callback=None):
+          callback=None, tstops=None):
     """solve(EnsembleProblem, alg, EnsembleGB300(); trajectories, saveat, reltol, abstol, ...).
     As in the reference (solve.jl:138-146), save_everystep defaults to "no
     saveat given" (every accepted step is kept, up to max_step_saves per
     trajectory) and dense to save_everystep without saveat (each step's
     interpolation vectors are kept too, so sol(t) uses the method's
     interpolant); ensembles of uneven sizes, and solves with a callback, are not
-    dense by default.  callback: the model's ContinuousCallback."""
+    dense by default.  callback: the model's ContinuousCallback.  tstops: times
+    every trajectory steps to exactly."""
     no_saveat = saveat is None or (not np.isscalar(saveat) and np.size(saveat) == 0)
     if save_everystep is None:
         save_everystep = no_saveat
@@ -459,7 +470,8 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
         res = solve_arrays(prob.model, alg, ens, u0s, ps, tspans, saveat, reltol, abstol, dt, dtmax, dtmin,
                            maxiters, save_start, save_end, eprob.n_per_traj, qmax_first_step, qmax,
                            save_everystep=save_everystep, max_step_saves=max_step_saves,
-                           dense=dense and not (dense_default and eprob.n_per_traj is not None), callback=callback)
+                           dense=dense and not (dense_default and eprob.n_per_traj is not None), callback=callback,
+                           tstops=tstops)
         sols = _LazySolutions(res, alg, eprob.n_per_traj)
         return EnsembleSolution(sols, time.perf_counter() - t_start, True, res)
     if trajectories is None:
@@ -475,7 +487,7 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
         ids = list(range(done, min(trajectories, done + batch_size)))
         outs = _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, dtmin, maxiters,
                             save_start, save_end, output_func, qmax_first_step, qmax, save_everystep, max_step_saves,
-                            dense, dense_default, callback)
+                            dense, dense_default, callback, tstops)
         u, converged = reduction(u, outs, range(ids[0] + 1, ids[-1] + 2))
         done = ids[-1] + 1
         if converged:
@@ -485,7 +497,7 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
 
 def _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, dtmin, maxiters, save_start,
                  save_end, output_func, qmax_first_step, qmax, save_everystep=False, max_step_saves=1024,
-                 dense=False, dense_default=True, callback=None):
+                 dense=False, dense_default=True, callback=None, tstops=None):
     repeat = {i: 1 for i in ids}
     results = {}
     todo = list(ids)
@@ -512,7 +524,8 @@ def _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, 
         res = solve_arrays(probs[0].model, alg, ens, u0s, ps, tspans, saveat, reltol, abstol, dt, dtmax, dtmin,
                            maxiters, save_start, save_end, npt, qmax_first_step, qmax,
                            save_everystep=save_everystep, max_step_saves=max_step_saves,
-                           dense=dense and not (dense_default and npt is not None), callback=callback)
+                           dense=dense and not (dense_default and npt is not None), callback=callback,
+                           tstops=tstops)
         sols = _LazySolutions(res, alg, npt)
         again = []
         for k, i in enumerate(todo):

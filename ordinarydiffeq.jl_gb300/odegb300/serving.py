@@ -60,8 +60,9 @@ class Server:
         self.close()
 
     def submit(self, model, alg, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=1e-6, precision="fp64",
-               ir_sweeps=-1, tag=None):
-        """Queue one packed ensemble; returns its ticket at once."""
+               ir_sweeps=-1, tag=None, tstops=None):
+        """Queue one packed ensemble; returns its ticket at once (the library
+        copies the inputs, tstops included, before this returns)."""
         name = model if isinstance(model, str) else None
         if isinstance(model, str):
             model = MODELS[model]
@@ -74,7 +75,7 @@ class Server:
         prec = pick_precision(precision, reltol, name)
         ens = EnsembleGB300(precision=prec, ir_sweeps=ir_sweeps if prec == "mixed" else -1)
         sv = saveat if hasattr(saveat, "nsave") else resolve_saveat(saveat, tspans)
-        o = _options(reltol, abstol, None, None, None, 1000000, sv, ens, None, None)
+        o = _options(reltol, abstol, None, None, None, 1000000, sv, ens, None, None, tstops=tstops)
         d = _lib.ProblemDesc(model, alg.alg_id, n, ps.shape[0], ens.prec_id(), 0)
         cap = sv.cap
         out = {"t": np.empty((cap, N)), "u": np.empty((cap, n, N)), "nsaved": np.empty(N, dtype=np.int32),

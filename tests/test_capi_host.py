@@ -43,14 +43,27 @@ def test_struct_layouts_match_the_bindings():
 
 def test_abi_version_and_defaults_without_gpu():
     L = _lib.load()
-    assert L.ode_abi_version() == 3
+    assert L.ode_abi_version() == 4
     # dense vectors per step (Tsit5 k1..k7, Vern7 k1 and k4..k9, Rodas5P dense k1..k3)
     assert [L.ode_dense_nk(a) for a in (0, 1, 2)] == [7, 7, 3] and L.ode_dense_nk(9) == -1
     o = _lib.Options()
     L.ode_options_default(C.byref(o))
     assert o.reltol == 1e-3 and o.abstol == 1e-6 and o.maxiters == 1000000
     assert o.save_start == 1 and o.save_end == 1 and o.save_end_user == -1
+    assert o.ntstops == 0 and not o.tstops and o.interp_points == 10
     assert L.ode_status_string(-4).decode().startswith("unsupported")
+
+
+def test_tstops_count_without_array_is_rejected_before_any_device_work():
+    # ode_solve_ensemble_noalloc validates its arguments on the host first
+    L = _lib.load()
+    o = _lib.Options()
+    L.ode_options_default(C.byref(o))
+    o.ntstops = 2   # and tstops left null
+    d = _lib.ProblemDesc(_lib.MODEL_LORENZ, _lib.ODE_TSIT5, 3, 3, _lib.PREC_FP64, 0)
+    assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == -1
+    o.ntstops = -1
+    assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == -1
 
 
 def test_variant_registry_covers_the_workloads():

@@ -307,3 +307,57 @@ def test_autotsit5_on_a_nonstiff_problem_is_tsit5():
     b = O.solve(O.TSIT5, O.LORENZ, [1.0, 0.0, 0.0], [10.0, 14.0, 8 / 3], (0.0, 1.0), **kw)
     assert (a["alg_choice"] == 1).all()
     assert np.array_equal(a["t"], b["t"]) and np.array_equal(a["u"], b["u"])
+
+
+# ---- tstops (test/InterfaceI/ode_tstops_tests.jl)
+
+def test_tstops_half_is_hit_with_tsit5():
+    # ode_tstops_tests.jl:8-9: solve(prob_ode_linear, Tsit5(), dt = 1//2^6, tstops = [1/2]); 1//2 in sol.t
+    r = O.solve(O.TSIT5, O.LINEAR, [0.5], [1.01], (0.0, 1.0), saveat=[], tstops=[0.5], saveat_given=False,
+                dt=2.0 ** -6, save_everystep=True, max_step_saves=4096, save_start=True)
+    assert 0.5 in r["t"]
+    assert r["retcode"] == 1
+
+
+@pytest.mark.parametrize("alg", [O.TSIT5, O.VERN7, O.RODAS5P, O.ROSENBROCK23])
+def test_every_tstop_is_in_sol_t(alg):
+    # ode_tstops_tests.jl:43-61 (forward direction): every added tstop, the endpoints
+    # included, appears in sol.t
+    ts = [0.0, 1 / 5, 1 / 4, 1 / 3, 1 / 2, 3 / 4, 1.0]
+    r = O.solve(alg, O.LINEAR, [0.5], [1.01], (0.0, 1.0), saveat=[], tstops=ts, saveat_given=False,
+                save_everystep=True, max_step_saves=4096, save_start=True)
+    for t in ts:
+        assert t in r["t"], t
+    assert np.all(np.diff(r["t"]) > 0)
+
+
+def test_tstops_from_a_range_are_a_subset_of_sol_t():
+    # ode_tstops_tests.jl:97-105 ("Late binding tstops"): 0:0.1:1 is a subset of sol.t
+    ts = np.arange(0, 11) * 0.1
+    r = O.solve(O.TSIT5, O.LINEAR, [1.0], [0.1], (0.0, 1.0), saveat=[], tstops=ts, saveat_given=False,
+                save_everystep=True, max_step_saves=4096, save_start=True)
+    assert set(ts.tolist()) <= set(r["t"].tolist())
+
+
+def test_ensemble_tstops_equal_single_solves():
+    # the shared-tstops ensemble entry point filters each trajectory's (t0, tf) and
+    # otherwise runs the single solve: duplicates, out-of-span and unsorted entries
+    rng = np.random.default_rng(5)
+    N = 12
+    u0 = np.tile(np.array([[1.0], [0.0], [0.0]]), (1, N))
+    p = np.vstack([np.full(N, 10.0), rng.uniform(0.0, 21.0, N), np.full(N, 8.0 / 3.0)])
+    tspan = np.vstack([rng.uniform(0.0, 0.2, N), rng.uniform(0.6, 1.0, N)])
+    ts = np.array([0.7, 0.05, 0.5, 0.5, 1.5, -1.0, 0.3333])
+    sv = np.array([])
+    e = O.solve_ensemble(O.TSIT5, O.LORENZ, u0, p, tspan, sv, 1e-6, 1e-8, saveat_given=False, save_everystep=True,
+                         max_step_saves=2048, save_start=True, tstops=ts)
+    for j in range(N):
+        r = O.solve(O.TSIT5, O.LORENZ, u0[:, j], p[:, j], tspan[:, j], saveat=[], tstops=ts, saveat_given=False,
+                    reltol=1e-6, abstol=1e-8, save_everystep=True, max_step_saves=2048, save_start=True)
+        ns = int(e["nsaved"][j])
+        assert ns == len(r["t"])
+        assert np.array_equal(e["t"][:ns, j], r["t"])
+        assert np.array_equal(e["u"][:ns, :, j], r["u"])
+        for t in ts:
+            if tspan[0, j] < t < tspan[1, j]:
+                assert t in r["t"]
