@@ -79,7 +79,9 @@ enum ode_retcode {
     ODE_RC_DEFAULT = 0, ODE_RC_SUCCESS = 1, ODE_RC_MAXITERS = 2, ODE_RC_DTNAN = 3,
     ODE_RC_DTLESSTHANMIN = 4, ODE_RC_UNSTABLE = 5,
     ODE_RC_ABORTED = 6, /* stopped by ode_abort(); no reference counterpart */
-    ODE_RC_TERMINATED = 7 /* a callback called terminate! (ReturnCode.Terminated) */
+    ODE_RC_TERMINATED = 7, /* a callback called terminate! (ReturnCode.Terminated) */
+    ODE_RC_INITIALFAILURE = 8 /* tf < t0 or a NaN time span: backward integration is not supported, the
+                                 trajectory is not stepped (ReturnCode.InitialFailure) */
 };
 
 enum ode_status {

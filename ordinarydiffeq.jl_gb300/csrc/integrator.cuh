@@ -35,7 +35,8 @@
 namespace odegb {
 
 enum RetCode { RC_DEFAULT = 0, RC_SUCCESS = 1, RC_MAXITERS = 2, RC_DTNAN = 3, RC_DTLESSTHANMIN = 4,
-               RC_UNSTABLE = 5, RC_ABORTED = 6, RC_TERMINATED = 7 };
+               RC_UNSTABLE = 5, RC_ABORTED = 6, RC_TERMINATED = 7,
+               RC_INITIALFAILURE = 8 };
 
 // Composite methods (AutoSwitchAlg) declare COMPOSITE; the loop then runs their
 // choice function and keeps one controller state per method.
@@ -379,7 +380,8 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
     bool do_error_check = true;
     long long iter = 0, success_iter = 0;
     bool accept = false, next_tstop = false;
-    int rc = RC_DEFAULT;
+    // forward integration only: tf < t0 (or a NaN span) is not stepped
+    int rc = (tf >= t0) ? RC_DEFAULT : RC_INITIALFAILURE;
 
     // _savevalues! (integrator_utils.jl:340-414) after an accepted step: saveat
     // points up to t by the step's interpolant, then the every-step save; true

@@ -89,7 +89,8 @@ end
 
 const RETCODES = (SciMLBase.ReturnCode.Default, SciMLBase.ReturnCode.Success, SciMLBase.ReturnCode.MaxIters,
                   SciMLBase.ReturnCode.DtNaN, SciMLBase.ReturnCode.DtLessThanMin, SciMLBase.ReturnCode.Unstable,
-                  SciMLBase.ReturnCode.Terminated, SciMLBase.ReturnCode.Terminated)
+                  SciMLBase.ReturnCode.Terminated, SciMLBase.ReturnCode.Terminated,
+                  SciMLBase.ReturnCode.InitialFailure)
 
 """
 Interpolation of a dense GB300 solve (the reference's dense = true): sol(t)

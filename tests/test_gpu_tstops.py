@@ -141,3 +141,20 @@ def test_tstops_device_entry_and_serving_match_host():
         out = got[3]
     assert np.array_equal(out["nsaved"], host["nsaved"])
     assert np.array_equal(out["u"][:k], host["u"][:k])
+
+
+def test_backward_span_reports_initial_failure():
+    # forward integration only: a trajectory with tf < t0 (or a NaN span) is not
+    # stepped and reports ReturnCode.InitialFailure; the others are unaffected
+    N = 64
+    u0, p, ts = lorenz_inputs(N)
+    ts = ts.copy()
+    ts[1, 3] = -1.0
+    ts[0, 7] = np.nan
+    g = gpu("lorenz", "tsit5", u0, p, ts, [0.5, 1.0], 1e-8, 1e-8)
+    assert g["retcode"][3] == 8 and g["retcode"][7] == 8
+    assert g["stats"]["naccept"][3] == 0
+    ok = np.setdiff1d(np.arange(N), [3, 7])
+    assert (g["retcode"][ok] == 1).all()
+    ref = gpu("lorenz", "tsit5", u0[:, ok], p[:, ok], ts[:, ok], [0.5, 1.0], 1e-8, 1e-8)
+    assert np.array_equal(g["u"][:, :, ok], ref["u"])
