@@ -61,6 +61,11 @@ enum ode_model {
     ODE_MODEL_BRUSSELATOR_1D = 4, /* n = 2*cells, interleaved (u_i, v_i), p = (A, B, alpha) */
     ODE_MODEL_VANDERPOL = 6,      /* n = 2 (x, y): x' = y, y' = mu ((1 - x^2) y - x); p = (mu)
                                      (test/InterfaceI/stiffness_detection_test.jl:10-16) */
+    ODE_MODEL_PK_ONE_COMPARTMENT = 7, /* n = 2 (depot, central): depot' = -ka depot,
+                                     central' = ka depot - ke central; p = (ka, ke, dose).  Its
+                                     DiscreteCallback (ode_options.callback): condition t in tstops
+                                     (the dose times, passed as the solve's tstops), affect!:
+                                     depot += dose; save_positions = (true, true) */
     ODE_MODEL_BOUNCING_BALL = 5   /* n = 2 (x, v): x' = v, v' = -g; p = (g, e, t_stop).  Its
                                      ContinuousCallback (ode_options.callback): condition x,
                                      affect! = nothing, affect_neg!: terminate! once t >= t_stop,

@@ -108,6 +108,10 @@ void rhs(int model, int n, const double* u, const double* p, double t, double* d
         du[0] = u[1];
         du[1] = p[0] * ((1.0 - u[0] * u[0]) * u[1] - u[0]);
         break;
+    case ORC_PK1:   // one-compartment PK, first-order absorption: p = (ka, ke, dose)
+        du[0] = -p[0] * u[0];
+        du[1] = p[0] * u[0] - p[1] * u[1];
+        break;
     case ORC_LINEAR:
         for (int i = 0; i < n; ++i) du[i] = p[0] * u[i];
         break;
@@ -164,6 +168,11 @@ void jac(int model, int n, const double* u, const double* p, double t, double* J
         J[1] = 1.0;
         J[2] = p[0] * (-2.0 * u[0] * u[1] - 1.0);
         J[3] = p[0] * (1.0 - u[0] * u[0]);
+        break;
+    case ORC_PK1:
+        J[0] = -p[0];
+        J[2] = p[0];
+        J[3] = -p[1];
         break;
     case ORC_LINEAR:
         for (int i = 0; i < n; ++i) J[i * n + i] = p[0];
@@ -247,6 +256,7 @@ struct Integ {
     bool have_J;
     std::vector<double> tstops;  // ascending
     size_t itstop;
+    std::vector<double> dtimes;  // the tstops as given, sorted: the discrete callback's times
     std::vector<double> saveat;
     size_t isave;
     double* t_out;
@@ -874,6 +884,8 @@ constexpr double CB_ABSTOL = 10.0 * 2.220446049250313e-16;
 constexpr double CB_REPEAT_NUDGE = 0.01;
 
 bool model_has_event(int model) { return model == ORC_BOUNCING_BALL; }
+// The dosing model's registered DiscreteCallback (condition t in tstops).
+bool model_has_discrete(int model) { return model == ORC_PK1; }
 double event_condition(int model, const double* u) { (void)model; return u[0]; }
 bool event_has_affect(int) { return false; }
 bool event_has_affect_neg(int) { return true; }
@@ -1053,8 +1065,32 @@ void apply_callback(Integ& I, double cb_t, double bottom_sign) {
     }
 }
 
+// apply_discrete_callback! (lib/DiffEqBase/src/callbacks.jl:645-682) for the
+// dosing model's DiscreteCallback: condition t in the dose times (the solve's
+// tstops as given), affect! depot += dose, save_positions = (true, true); the
+// modification sets reeval_fsal (reeval_internals_due_to_modification! with
+// continuous_modification = false: the step's k are kept).
+void apply_discrete_callback(Integ& I) {
+    if (!std::binary_search(I.dtimes.begin(), I.dtimes.end(), I.t)) {
+        savevalues(I);
+        return;
+    }
+    const int before = I.nsaved;
+    const double last_before = I.last_saved_t;
+    savevalues(I);
+    const bool savedexactly = I.nsaved > before && I.last_saved_t == I.t && !(last_before == I.t);
+    if (!savedexactly) push_save(I, I.t, I.u.data());
+    I.u[0] += I.p[2];
+    I.reeval_fsal = true;
+    push_save(I, I.t, I.u.data());
+}
+
 // handle_callbacks! (integrator_utils.jl:1081-1132) for one continuous callback.
 void handle_callbacks(Integ& I) {
+    if (I.o.callback && model_has_discrete(I.model)) {
+        apply_discrete_callback(I);
+        return;
+    }
     if (!I.o.callback || !model_has_event(I.model)) {
         savevalues(I);
         return;
@@ -1382,6 +1418,8 @@ int orc_solve(int alg, int model, int n, const double* p, double t0, double tf, 
               double* t_out, double* u_out, int cap, int32_t* retcode, orc_stats* st, void** dense_handle) {
     Integ I;
     setup(I, alg, model, n, p, t0, tf, o, saveat, nsave_in, tstops, ntstops);
+    I.dtimes.assign(tstops, tstops + (tstops ? ntstops : 0));
+    std::sort(I.dtimes.begin(), I.dtimes.end());
     I.t_out = t_out;
     I.u_out = u_out;
     I.cap = cap;
@@ -1500,6 +1538,8 @@ int orc_solve_ensemble(int alg, int model, int nmax, const int32_t* n_per_traj, 
             if (o->ntstops > 0 && o->tstops) ts.insert(ts.end(), o->tstops, o->tstops + o->ntstops);
             setup(I, alg, model, n, pj.data(), t0, tf, o, sv.data(), nsave, ts.empty() ? nullptr : ts.data(),
                   (int)ts.size());
+            I.dtimes.assign(o->tstops, o->tstops + (o->tstops ? o->ntstops : 0));
+            std::sort(I.dtimes.begin(), I.dtimes.end());
             I.t_out = tl.data();
             I.u_out = ul.data();
             I.cap = cap;

@@ -42,6 +42,10 @@ enum RetCode { RC_DEFAULT = 0, RC_SUCCESS = 1, RC_MAXITERS = 2, RC_DTNAN = 3, RC
 // choice function and keeps one controller state per method.
 template <class A, class = void> struct is_composite_alg : std::false_type {};
 template <class A> struct is_composite_alg<A, std::void_t<decltype(A::COMPOSITE)>> : std::true_type {};
+// models with a registered DiscreteCallback declare HAS_DISCRETE
+template <class M, class = void> struct has_discrete_callback : std::false_type {};
+template <class M>
+struct has_discrete_callback<M, std::void_t<decltype(M::HAS_DISCRETE)>> : std::bool_constant<M::HAS_DISCRETE> {};
 
 // The left end of a sign change of f in [lo, hi] narrowed to adjacent floats
 // (LeftRootFind: the reference solves IntervalNonlinearProblem with ModAB,
@@ -626,6 +630,21 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             bool handled = false;
             if constexpr (Model::HAS_EVENT) {
                 if (a.callback) handled = handle_event();
+            }
+            if constexpr (has_discrete_callback<Model>::value) {
+                // apply_discrete_callback! (lib/DiffEqBase/src/callbacks.jl:645-682) for the
+                // model's DiscreteCallback, condition t in tstops: the step landed on the
+                // tstop the index points at (entries before it were passed at the header)
+                if (a.callback && itst < a.ntstops && a.tstops[itst] == t) {
+                    // saveat up to t and the every-step save, then save_positions[1]
+                    // unless a save landed on t; affect!; save_positions[2]
+                    if (!savevalues(u, ulo)) save_point(t, u, ulo);
+                    Model::template discrete_affect<R, L, C>(u, ulo, a.p + j, N, g);
+                    save_point(t, u, ulo);
+                    // u changed: FSAL methods evaluate f(u) again (reeval_fsal)
+                    Alg::template reset_fsal<Model, R, L, C>(cache, u, ulo, p, t, g, st);
+                    handled = true;
+                }
             }
             if (!handled) savevalues(u, ulo);
             Alg::template after_save<R, C>(cache);

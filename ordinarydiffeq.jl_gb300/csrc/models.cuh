@@ -20,7 +20,7 @@
 namespace odegb {
 
 enum ModelId { M_LINEAR = 0, M_LORENZ = 1, M_ROBERTSON = 2, M_DUFFING = 3, M_BRUSSELATOR = 4, M_BOUNCING_BALL = 5,
-               M_VANDERPOL = 6 };
+               M_VANDERPOL = 6, M_PK1 = 7 };
 
 // The van der Pol oscillator of the reference's stiffness-detection test
 // (test/InterfaceI/stiffness_detection_test.jl:10-16): u = (x, y), x' = y,
@@ -41,6 +41,36 @@ struct VanDerPol {
         J[0][1] = R(1);
         J[1][0] = p[0] * (R(-2) * u[0] * u[1] - R(1));
         J[1][1] = p[0] * (R(1) - u[0] * u[0]);
+    }
+};
+
+// One-compartment pharmacokinetics with first-order absorption, dosed by its
+// registered DiscreteCallback: u = (depot, central), depot' = -ka depot,
+// central' = ka depot - ke central; p = (ka, ke, dose).  Callback: condition
+// t in tstops (the dose times are the solve's tstops, the pattern of
+// DiffEqCallbacks' PresetTimeCallback), affect!: depot += dose.
+struct PKOneCompartment {
+    static constexpr int NP = 3;
+    static constexpr bool AUTONOMOUS = true;
+    static constexpr bool HAS_EVENT = false;
+    static constexpr bool HAS_DISCRETE = true;
+    template <class R, int L, int C>
+    __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>&) {
+        static_assert(L == 1 && C == 2, "the one-compartment model has 2 states on one lane");
+        du[0] = -p[0] * u[0];
+        du[1] = p[0] * u[0] - p[1] * u[1];
+    }
+    template <class R, int N>
+    __device__ static void jac(R (*J)[N], const R*, const R* p, double) {
+        J[0][0] = -p[0]; J[0][1] = R(0);
+        J[1][0] = p[0];  J[1][1] = -p[1];
+    }
+    // affect!: the dose into the depot, in FP64 on the state pair
+    template <class R, int L, int C>
+    __device__ static void discrete_affect(R* u, R* ulo, const double* p, long long stride, const Group<L>&) {
+        const double v = ((double)u[0] + (double)ulo[0]) + p[2 * stride];
+        u[0] = (R)v;
+        ulo[0] = (R)(v - (double)u[0]);
     }
 };
 

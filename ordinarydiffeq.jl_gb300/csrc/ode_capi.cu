@@ -55,7 +55,8 @@ const std::vector<KernelVariant>& all_variants() {
 }
 
 int model_nparams(int model) { return (model == ODE_MODEL_LINEAR || model == ODE_MODEL_VANDERPOL) ? 1 : 3; }
-bool model_has_event(int model) { return model == ODE_MODEL_BOUNCING_BALL; }
+// models with a registered callback (continuous: the ball; discrete: the dosing model)
+bool model_has_event(int model) { return model == ODE_MODEL_BOUNCING_BALL || model == ODE_MODEL_PK_ONE_COMPARTMENT; }
 
 // Default lanes per trajectory: one lane for tiny systems (registers hold the
 // whole state and stage set); explicit methods 4 states per lane so the Vern7
@@ -181,7 +182,7 @@ int validate(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int
     if (!h || !d || !o) return fail(h, ODE_E_INVALID, "null handle, problem or options");
     if (N < 0) return fail(h, ODE_E_INVALID, "negative trajectory count");
     if (d->alg_id < ODE_TSIT5 || d->alg_id >= kNumAlgs) return fail(h, ODE_E_INVALID, "unknown alg_id");
-    if (d->model_id < ODE_MODEL_LINEAR || d->model_id > ODE_MODEL_VANDERPOL)
+    if (d->model_id < ODE_MODEL_LINEAR || d->model_id > ODE_MODEL_PK_ONE_COMPARTMENT)
         return fail(h, ODE_E_INVALID, "unknown model_id");
     if (d->precision != ODE_PREC_FP64 && d->precision != ODE_PREC_MIXED)
         return fail(h, ODE_E_INVALID, "unknown precision");
@@ -190,7 +191,8 @@ int validate(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int
         return fail(h, ODE_E_INVALID, "n_params does not match the model");
     if ((d->model_id == ODE_MODEL_LORENZ || d->model_id == ODE_MODEL_ROBERTSON) && d->n_states != 3)
         return fail(h, ODE_E_INVALID, "this model has 3 states");
-    if ((d->model_id == ODE_MODEL_BOUNCING_BALL || d->model_id == ODE_MODEL_VANDERPOL) && d->n_states != 2)
+    if ((d->model_id == ODE_MODEL_BOUNCING_BALL || d->model_id == ODE_MODEL_VANDERPOL ||
+         d->model_id == ODE_MODEL_PK_ONE_COMPARTMENT) && d->n_states != 2)
         return fail(h, ODE_E_INVALID, "this model has 2 states");
     if (o->callback && !model_has_event(d->model_id))
         return fail(h, ODE_E_UNSUPPORTED, "the model has no registered callback");
@@ -1608,7 +1610,7 @@ extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_o
     }
     if (d->alg_id < ODE_TSIT5 || d->alg_id >= kNumAlgs ||
         (d->precision != ODE_PREC_FP64 && d->precision != ODE_PREC_MIXED) ||
-        d->model_id < ODE_MODEL_LINEAR || d->model_id > ODE_MODEL_VANDERPOL || d->n_states <= 0 ||
+        d->model_id < ODE_MODEL_LINEAR || d->model_id > ODE_MODEL_PK_ONE_COMPARTMENT || d->n_states <= 0 ||
         (o->callback && !model_has_event(d->model_id)) ||
         d->n_params != model_nparams(d->model_id) || !(o->reltol > 0) || !(o->abstol >= 0) || o->nsave < 0 ||
         (o->save_everystep && (o->nsave > 0 || o->max_step_saves <= 0)) ||

@@ -27,15 +27,17 @@ export EnsembleGB300, GB300Model, GB300Callback
 const LIB = get(ENV, "ODE_GB300_LIB", joinpath(@__DIR__, "..", "lib", "libode_b200.so"))
 
 const MODEL_IDS = Dict(:linear => 0, :lorenz => 1, :robertson => 2, :duffing_chain => 3, :brusselator_1d => 4,
-                       :bouncing_ball => 5, :van_der_pol => 6)
-const N_PARAMS = Dict(0 => 1, 1 => 3, 2 => 3, 3 => 3, 4 => 3, 5 => 3, 6 => 1)
+                       :bouncing_ball => 5, :van_der_pol => 6, :pk_one_compartment => 7)
+const N_PARAMS = Dict(0 => 1, 1 => 3, 2 => 3, 3 => 3, 4 => 3, 5 => 3, 6 => 1, 7 => 3)
 
 """
     GB300Callback(; interp_points = 10, max_events = 16)
 
-Turns on the model's registered ContinuousCallback (its condition and affect
-are device code compiled with the model, e.g. `:bouncing_ball`); pass it as
-`callback` to `solve`.  Each event adds two saves (before and after its affect).
+Turns on the model's registered callback (its condition and affect are device
+code compiled with the model): the ContinuousCallback of `:bouncing_ball`, or
+the DiscreteCallback of `:pk_one_compartment` (condition `t in tstops`, the
+dose times passed as `solve`'s `tstops`); pass it as `callback` to `solve`.
+Each firing adds two saves (before and after its affect).
 """
 struct GB300Callback
     interp_points::Int

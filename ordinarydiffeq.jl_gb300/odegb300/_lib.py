@@ -11,7 +11,7 @@ from . import build as _build
 
 ODE_TSIT5, ODE_VERN7, ODE_RODAS5P, ODE_ROSENBROCK23, ODE_AUTOTSIT5_ROSENBROCK23 = 0, 1, 2, 3, 4
 MODEL_LINEAR, MODEL_LORENZ, MODEL_ROBERTSON, MODEL_DUFFING_CHAIN, MODEL_BRUSSELATOR_1D = 0, 1, 2, 3, 4
-MODEL_BOUNCING_BALL, MODEL_VANDERPOL = 5, 6
+MODEL_BOUNCING_BALL, MODEL_VANDERPOL, MODEL_PK_ONE_COMPARTMENT = 5, 6, 7
 PREC_FP64, PREC_MIXED = 0, 1
 STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "out of device memory",
           -4: "unsupported", -5: "busy", -6: "timeout", -7: "unknown ticket"}

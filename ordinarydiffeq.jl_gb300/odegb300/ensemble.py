@@ -35,10 +35,11 @@ class ReturnCode(IntEnum):
 
 MODELS = {"linear": _lib.MODEL_LINEAR, "lorenz": _lib.MODEL_LORENZ, "robertson": _lib.MODEL_ROBERTSON,
           "duffing_chain": _lib.MODEL_DUFFING_CHAIN, "brusselator_1d": _lib.MODEL_BRUSSELATOR_1D,
-          "bouncing_ball": _lib.MODEL_BOUNCING_BALL, "van_der_pol": _lib.MODEL_VANDERPOL}
+          "bouncing_ball": _lib.MODEL_BOUNCING_BALL, "van_der_pol": _lib.MODEL_VANDERPOL,
+          "pk_one_compartment": _lib.MODEL_PK_ONE_COMPARTMENT}
 N_PARAMS = {_lib.MODEL_LINEAR: 1, _lib.MODEL_LORENZ: 3, _lib.MODEL_ROBERTSON: 3,
             _lib.MODEL_DUFFING_CHAIN: 3, _lib.MODEL_BRUSSELATOR_1D: 3, _lib.MODEL_BOUNCING_BALL: 3,
-            _lib.MODEL_VANDERPOL: 1}
+            _lib.MODEL_VANDERPOL: 1, _lib.MODEL_PK_ONE_COMPARTMENT: 3}
 
 
 @dataclass
@@ -51,6 +52,17 @@ class ContinuousCallback:
     affect, save_positions = (true, true))."""
     interp_points: int = 10
     max_events: int = 16
+
+
+@dataclass
+class DiscreteCallback:
+    """The model's registered DiscreteCallback, e.g. "pk_one_compartment": condition
+    t in tstops (the dose times, passed as solve's tstops: the pattern of
+    DiffEqCallbacks' PresetTimeCallback), affect! depot += dose.  max_events
+    sizes the output: each firing adds two saves (before and after its affect,
+    save_positions = (true, true))."""
+    max_events: int = 16
+    interp_points = 10   # unused by a discrete callback; the options carry one field for both
 
 
 class _Alg:

@@ -361,3 +361,70 @@ def test_ensemble_tstops_equal_single_solves():
         for t in ts:
             if tspan[0, j] < t < tspan[1, j]:
                 assert t in r["t"]
+
+
+# ---- DiscreteCallback: the dosing model (apply_discrete_callback!, lib/DiffEqBase/src/callbacks.jl:645-682)
+
+def pk_exact(t, ka, ke, dose, doses, depot0=None):
+    """Closed form of the one-compartment model with first-order absorption:
+    every dose D at tau adds D e^{-ka (t - tau)} to the depot and
+    D ka / (ka - ke) (e^{-ke (t - tau)} - e^{-ka (t - tau)}) to the central
+    compartment (depot0 = dose at t = 0)."""
+    d0 = dose if depot0 is None else depot0
+    taus = [0.0] + [tau for tau in doses if tau <= t]
+    amts = [d0] + [dose] * (len(taus) - 1)
+    x1 = sum(a * np.exp(-ka * (t - tau)) for a, tau in zip(amts, taus))
+    x2 = sum(a * ka / (ka - ke) * (np.exp(-ke * (t - tau)) - np.exp(-ka * (t - tau))) for a, tau in zip(amts, taus))
+    return np.array([x1, x2])
+
+
+PK_P = [1.2, 0.15, 100.0]             # ka, ke (1/h), dose
+PK_DOSES = [12.0 * k for k in range(1, 14)]
+
+
+@pytest.mark.parametrize("alg", [O.TSIT5, O.VERN7, O.RODAS5P, O.ROSENBROCK23, O.AUTOTSIT5_ROSENBROCK23])
+def test_dosing_callback_matches_the_closed_form(alg):
+    ka, ke, dose = PK_P
+    sv = np.arange(0.5, 168.0, 1.0)
+    rt = 1e-5 if alg == O.ROSENBROCK23 else 1e-9
+    r = O.solve(alg, O.PK1, [dose, 0.0], PK_P, (0.0, 168.0), saveat=sv, tstops=PK_DOSES, reltol=rt, abstol=rt,
+                callback=True, max_events=32)
+    assert r["retcode"] == 1
+    t, u = r["t"], r["u"]
+    # save_positions = (true, true): the state before and after each dose
+    for tau in PK_DOSES:
+        at = np.flatnonzero(t == tau)
+        assert len(at) == 2 and at[1] == at[0] + 1, tau
+        assert abs((u[at[1], 0] - u[at[0], 0]) - dose) < 1e-9 * dose
+    for s in np.flatnonzero(np.isin(t, sv)):
+        ex = pk_exact(t[s], ka, ke, dose, PK_DOSES)
+        assert np.allclose(u[s], ex, rtol=200 * rt, atol=200 * rt), (t[s], u[s], ex)
+
+
+def test_dosing_needs_the_callback_and_its_tstops():
+    # condition t in tstops: without the callback the tstops only stop the
+    # integrator; without tstops the condition never holds (one dose at t0)
+    ka, ke, dose = PK_P
+    r = O.solve(O.TSIT5, O.PK1, [dose, 0.0], PK_P, (0.0, 48.0), saveat=[47.5], tstops=[12.0, 24.0, 36.0],
+                reltol=1e-10, abstol=1e-10)
+    assert list(r["t"]) == [47.5, 48.0]   # the tstops are stops, not saves
+    assert np.allclose(r["u"][r["t"] == 47.5][0], pk_exact(47.5, ka, ke, dose, []), rtol=1e-7)
+    r = O.solve(O.TSIT5, O.PK1, [dose, 0.0], PK_P, (0.0, 48.0), saveat=[47.5], reltol=1e-10, abstol=1e-10,
+                callback=True, max_events=8)
+    assert np.allclose(r["u"][r["t"] == 47.5][0], pk_exact(47.5, ka, ke, dose, []), rtol=1e-7)
+
+
+def test_dosing_with_every_step_saves_and_a_dose_at_tf():
+    # the every-step save at a dose time is its pre-affect save; a dose time equal
+    # to tf fires too (handle_callbacks! runs after the last step)
+    ka, ke, dose = PK_P
+    doses = [6.0, 12.0, 24.0]
+    r = O.solve(O.TSIT5, O.PK1, [dose, 0.0], PK_P, (0.0, 24.0), saveat=[], saveat_given=False, tstops=doses,
+                reltol=1e-10, abstol=1e-10, save_everystep=True, max_step_saves=4096, save_start=True,
+                callback=True, max_events=8)
+    t, u = r["t"], r["u"]
+    for tau in doses:
+        at = np.flatnonzero(t == tau)
+        assert len(at) == 2, (tau, at)
+    assert t[-1] == 24.0 and np.isclose(u[-1, 0] - u[-2, 0], dose)
+    assert np.allclose(u[-1], pk_exact(24.0, ka, ke, dose, doses), rtol=1e-7)
