@@ -15,7 +15,7 @@ host-buffer call (host->device copies and results back inside the timed region).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
                     [--config robertson|lorenz|duffing|brusselator|robertson_ros23|lorenz_dense|
-                              bouncing_ball|van_der_pol|serving]
+                              bouncing_ball|van_der_pol|pk_dosing|serving]
                     [--trajectories N]
 """
 import argparse
@@ -49,6 +49,9 @@ CONFIGS = {
     "bouncing_ball": ("bouncing balls with the model's ContinuousCallback (condition x, affect_neg! v <- -e v, "
                       "half terminate! after t_stop), Tsit5, reltol=abstol=1e-6, tspan (0,10), saveat 0.25",
                       1_000_000),
+    "pk_dosing": ("population PK: one-compartment model with first-order absorption, ka/ke log-normal, "
+                  "100 mg every 12 h for a week by the model's DiscreteCallback (t in tstops), Tsit5, "
+                  "reltol=abstol=1e-8, tspan (0,168), hourly saves", 1_000_000),
     "serving": ("open-loop Poisson request stream; each request 1-4096 trajectories (log-uniform) of Lorenz/Tsit5, "
                 "Robertson/Rodas5P or Brusselator-1D (8/16/32 cells)/Rodas5P, reltol 10^U(-8,-4)", 0),
 }
@@ -163,7 +166,7 @@ def workload(name, N, seed):
         return dict(W.lorenz(N, seed=seed), saveat=None, everystep=True, max_step_saves=DENSE_MAX_STEPS)
     return {"robertson": W.robertson, "lorenz": W.lorenz, "duffing": W.duffing,
             "brusselator": W.brusselator, "bouncing_ball": W.bouncing_ball,
-            "van_der_pol": W.van_der_pol}[name](N, seed=seed)
+            "van_der_pol": W.van_der_pol, "pk_dosing": W.pk_dosing}[name](N, seed=seed)
 
 
 DENSE_MAX_STEPS = 512   # step slots per trajectory of the dense workload (Lorenz at 1e-8 takes < 200)
@@ -179,9 +182,12 @@ def oracle_solve(wl, idx, nthreads=0, truth=False):
     alg = {"tsit5": O.TSIT5, "vern7": O.VERN7, "rodas5p": O.RODAS5P, "rosenbrock23": O.ROSENBROCK23,
            "autotsit5_rosenbrock23": O.AUTOTSIT5_ROSENBROCK23}[wl["alg"]]
     model = {"lorenz": O.LORENZ, "robertson": O.ROBERTSON, "duffing_chain": O.DUFFING,
-             "brusselator_1d": O.BRUSSELATOR, "bouncing_ball": O.BOUNCING_BALL, "van_der_pol": O.VANDERPOL}[wl["model"]]
+             "brusselator_1d": O.BRUSSELATOR, "bouncing_ball": O.BOUNCING_BALL, "van_der_pol": O.VANDERPOL,
+             "pk_one_compartment": O.PK1}[wl["model"]]
     cb = wl.get("callback")
     cbkw = dict(callback=True, interp_points=cb.interp_points, max_events=cb.max_events) if cb else {}
+    if wl.get("tstops") is not None:
+        cbkw["tstops"] = wl["tstops"]
     ts = wl["tspan"][:, idx]
     sv = wl["saveat"]
     if isinstance(sv, np.ndarray) and sv.ndim == 2:
@@ -193,7 +199,7 @@ def oracle_solve(wl, idx, nthreads=0, truth=False):
     if truth:
         stiff = wl["alg"] in ("rodas5p", "rosenbrock23", "autotsit5_rosenbrock23")
         alg, rt, at = (O.RODAS5P, 1e-12, 1e-16) if stiff else (O.VERN9, 1e-14, 1e-14)
-        if cb:   # events need a dense interpolant to locate them: Tsit5 at 1e-13
+        if cb and wl["model"] == "bouncing_ball":   # events need a dense interpolant: Tsit5 at 1e-13
             alg, rt, at = O.TSIT5, 1e-13, 1e-13
     return O.solve_ensemble(alg, model, wl["u0"][:, idx], wl["p"][:, idx], ts, spec.values, rt,
                             at, n_per_traj=None if npt is None else npt[idx], saveat_as_tstops=truth,
@@ -293,6 +299,8 @@ def run_gb300(args, world, rank, local, dist):
     t_ts = torch.from_numpy(np.ascontiguousarray(wl["tspan"])).to(dev)
     t_sv = torch.from_numpy(np.ascontiguousarray(sv.values if sv.nsave else np.zeros(1))).to(dev)
     t_npt = torch.from_numpy(npt).to(dev) if npt is not None else None
+    tst = wl.get("tstops")
+    t_tst = torch.from_numpy(np.sort(np.asarray(tst, dtype=np.float64))).to(dev) if tst is not None else None
     t_out = torch.empty((cap, N), dtype=torch.float64, device=dev)
     u_out = torch.empty((cap, n, N), dtype=torch.float64, device=dev)
     ns_out = torch.empty(N, dtype=torch.int32, device=dev)
@@ -308,6 +316,9 @@ def run_gb300(args, world, rank, local, dist):
     def solve_device(prec):
         ens = odegb300.EnsembleGB300(precision=prec, ir_sweeps=wl.get("ir_sweeps", -1) if prec == "mixed" else -1)
         o = _options(wl["reltol"], wl["abstol"], None, None, None, 1000000, sv, ens, None, None, cb)
+        if t_tst is not None:   # the device entry point takes tstops in device memory, sorted
+            o.ntstops = int(t_tst.numel())
+            o.tstops = C.cast(C.c_void_p(t_tst.data_ptr()), C.POINTER(C.c_double))
         d = _lib.ProblemDesc(model, alg.alg_id, n, wl["p"].shape[0], ens.prec_id(), 0)
         stream = C.c_void_p(work.cuda_stream)
         _lib.check(L.ode_solve_ensemble_device(h, C.byref(d), C.byref(o), N, ptr(t_npt), ptr(t_u0), ptr(t_p),
@@ -407,7 +418,8 @@ def run_gb300(args, world, rank, local, dist):
     h_rc = torch.empty(N, dtype=torch.int32).pin_memory()
     h_st = torch.empty((N, 6), dtype=torch.int64).pin_memory()
     ens_e2e = odegb300.EnsembleGB300(precision=best, ir_sweeps=wl.get("ir_sweeps", -1) if best == "mixed" else -1)
-    o_e2e = _options(wl["reltol"], wl["abstol"], None, None, None, 1000000, sv, ens_e2e, None, None, cb)
+    o_e2e = _options(wl["reltol"], wl["abstol"], None, None, None, 1000000, sv, ens_e2e, None, None, cb,
+                     tstops=wl.get("tstops"))
     d_e2e = _lib.ProblemDesc(model, alg.alg_id, n, wl["p"].shape[0], ens_e2e.prec_id(), 0)
     hp = lambda t, ty=C.c_double: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(ty)) if t is not None else None
 

@@ -51,6 +51,23 @@ def bouncing_ball(N, seed=42):
                 callback=ContinuousCallback(interp_points=10, max_events=8))
 
 
+def pk_dosing(N, seed=42):
+    """Population pharmacokinetics: a one-compartment model with first-order
+    absorption per patient, ka and ke log-normal (medians 1.2 and 0.15 per hour,
+    30% spread), a 100 mg dose at t = 0 and then every 12 h for a week by the
+    model's DiscreteCallback (condition t in tstops, tstops = the dose times),
+    Tsit5, reltol 1e-8, abstol 1e-8, hourly saves."""
+    from .ensemble import DiscreteCallback
+    rng = np.random.default_rng(seed)
+    ka = 1.2 * np.exp(0.3 * rng.standard_normal(N))
+    ke = 0.15 * np.exp(0.3 * rng.standard_normal(N))
+    dose = np.full(N, 100.0)
+    u0 = np.vstack([dose, np.zeros(N)])
+    ts = np.vstack([np.zeros(N), np.full(N, 168.0)])
+    return dict(model="pk_one_compartment", alg="tsit5", u0=u0, p=np.vstack([ka, ke, dose]), tspan=ts, saveat=1.0,
+                reltol=1e-8, abstol=1e-8, tstops=12.0 * np.arange(1, 14), callback=DiscreteCallback(max_events=14))
+
+
 def van_der_pol(N, seed=42):
     """Van der Pol oscillators (the reference's stiffness-detection problem) with
     mu log-uniform in [1, 1000] (from non-stiff to stiff relaxation), u0 = (2, 0),
@@ -105,10 +122,10 @@ def brusselator(N, seed=42, cells=32):
 
 RHS_FLOPS = {"linear": lambda n: n, "lorenz": lambda n: 9, "robertson": lambda n: 13,
              "duffing_chain": lambda n: 9 * (n // 2), "brusselator_1d": lambda n: 13 * (n // 2),
-             "bouncing_ball": lambda n: 1, "van_der_pol": lambda n: 7}
+             "bouncing_ball": lambda n: 1, "van_der_pol": lambda n: 7, "pk_one_compartment": lambda n: 5}
 JAC_FLOPS = {"linear": lambda n: 0, "lorenz": lambda n: 3, "robertson": lambda n: 10,
              "duffing_chain": lambda n: 5 * (n // 2), "brusselator_1d": lambda n: 14 * (n // 2),
-             "bouncing_ball": lambda n: 0, "van_der_pol": lambda n: 8}
+             "bouncing_ball": lambda n: 0, "van_der_pol": lambda n: 8, "pk_one_compartment": lambda n: 0}
 CONTROLLER_FLOPS = 150  # two series pow evaluations, clamp, dt update (FP64)
 
 
