@@ -51,7 +51,7 @@ CONFIGS = {
                       1_000_000),
     "pk_dosing": ("population PK: one-compartment model with first-order absorption, ka/ke log-normal, "
                   "100 mg every 12 h for a week by the model's DiscreteCallback (t in tstops), Tsit5, "
-                  "reltol=abstol=1e-8, tspan (0,168), hourly saves", 1_000_000),
+                  "reltol 1e-6 abstol 1e-8, tspan (0,168), hourly saves", 1_000_000),
     "serving": ("open-loop Poisson request stream; each request 1-4096 trajectories (log-uniform) of Lorenz/Tsit5, "
                 "Robertson/Rodas5P or Brusselator-1D (8/16/32 cells)/Rodas5P, reltol 10^U(-8,-4)", 0),
 }

@@ -5,7 +5,8 @@ handle_callbacks!, lib/OrdinaryDiffEqCore/src/integrators/integrator_utils.jl:
 1081-1132).  A population of 512 patients (ka, ke log-normal) dosed every 12 h
 for a week: FP64 saves within 10x the tolerance of the oracle with accepted
 steps within 1, two saves at every dose (before and after it), and the closed
-form within the tolerance; the mixed form as accurate as FP64 against it.
+form within the tolerance; the mixed form as accurate as FP64 against it at
+reltol 1e-6.
 """
 import numpy as np
 import pytest
@@ -45,9 +46,9 @@ def closed_form(t, ka, ke, dose):
     return np.array([x1, x2])
 
 
-def solve_pair(alg, precision="fp64", N=512):
+def solve_pair(alg, precision="fp64", N=512, tol=None):
     from odegb300 import DiscreteCallback
-    rt, at = TOL[alg]
+    rt, at = tol or TOL[alg]
     u0, p, ts = population(N)
     g = gpu("pk_one_compartment", alg, u0, p, ts, SAVEAT, rt, at, precision=precision, tstops=DOSES,
             callback=DiscreteCallback(max_events=16))
@@ -78,8 +79,10 @@ def test_dosing_fp64_matches_oracle(alg):
 
 @pytest.mark.parametrize("alg", ["tsit5", "rodas5p"])
 def test_dosing_mixed_is_as_accurate_as_fp64(alg):
-    g, o, p, rt, at = solve_pair(alg, precision="mixed")
-    g64 = solve_pair(alg)[0]
+    # at reltol 1e-6: the mixed form keeps the parameters in FP32 (ka, ke to
+    # ~3e-8 relative), so its bar is a tolerance well above that
+    g, o, p, rt, at = solve_pair(alg, precision="mixed", tol=(1e-6, 1e-8))
+    g64 = solve_pair(alg, tol=(1e-6, 1e-8))[0]
     assert (g["retcode"] == 1).all()
     assert np.array_equal(g["nsaved"], o["nsaved"])
     ns = int(g["nsaved"][0])
