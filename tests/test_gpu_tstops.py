@@ -151,10 +151,11 @@ def test_backward_span_reports_initial_failure():
     ts = ts.copy()
     ts[1, 3] = -1.0
     ts[0, 7] = np.nan
-    g = gpu("lorenz", "tsit5", u0, p, ts, [0.5, 1.0], 1e-8, 1e-8)
+    kw = dict(save_start=False, save_end=True)   # the spans differ, so the save flags are given
+    g = gpu("lorenz", "tsit5", u0, p, ts, [0.5, 1.0], 1e-8, 1e-8, **kw)
     assert g["retcode"][3] == 8 and g["retcode"][7] == 8
     assert g["stats"]["naccept"][3] == 0
     ok = np.setdiff1d(np.arange(N), [3, 7])
     assert (g["retcode"][ok] == 1).all()
-    ref = gpu("lorenz", "tsit5", u0[:, ok], p[:, ok], ts[:, ok], [0.5, 1.0], 1e-8, 1e-8)
+    ref = gpu("lorenz", "tsit5", u0[:, ok], p[:, ok], ts[:, ok], [0.5, 1.0], 1e-8, 1e-8, **kw)
     assert np.array_equal(g["u"][:, :, ok], ref["u"])
