@@ -1,22 +1,25 @@
 #!/usr/bin/env python3
 """Benchmark of the GB300 ensemble ODE integrator (libode_b200.so).
 
-Default workload (one "step" = one full ensemble solve): 100,000 Robertson
+Headline workload (one "step" = one full ensemble solve): 100,000 Robertson
 trajectories, Rodas5P with the analytic Jacobian, reltol 1e-6, abstol 1e-10,
 tspan (0, 1e5), 20 log-spaced saves; rate constants log-uniform-scaled per
 trajectory (seeded synthetic inputs; no dataset exists for this path).
 
-Both GPU forms run: plain FP64 and mixed precision.  `value` is the
-trajectories/s of the mixed form when it is as accurate as the FP64 form on a
-checked sample (its error against a ground-truth solve within 2x the FP64
-form's, +1 tolerance unit, at the median and p99), else of the FP64 form;
-inputs resident in HBM.  `e2e` is the same metric through the public
-host-buffer call (host->device copies and results back inside the timed region).
+Both GPU forms run: plain FP64 and mixed precision (and, for the headline, the
+mixed form with one refinement sweep per W solve).  `value` is the
+trajectories/s of the mixed form when it is as accurate as the FP64 form
+(its error against a ground-truth solve within 2x the FP64 form's, +1
+tolerance unit, at the median and p99; checked on the whole ensemble where the
+oracle allows), else of the FP64 form; inputs resident in HBM.  `e2e` is the
+same metric through the public host-buffer call.  `configs` holds the same
+block for 10k Lorenz/Tsit5, 1M uneven Duffing chains/Vern7 and 65,536
+Brusselators/Rodas5P; `serving` the open-loop request stream.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
                     [--config robertson|lorenz|duffing|brusselator|robertson_ros23|lorenz_dense|
                               bouncing_ball|van_der_pol|pk_dosing|serving]
-                    [--trajectories N]
+                    [--trajectories N] [--no-suite] [--no-serving]
 """
 import argparse
 import ctypes as C
@@ -86,7 +89,7 @@ def run_serving(args, rank, local):
     best = max(blk["rates"], key=lambda m: m["trajectories_per_s"] or 0.0)
     reqs = sum(m["completed"] for m in blk["rates"])
     print(json.dumps({
-        "metric": "trajectories/sec at equal accuracy, mixed vs plain FP64 GPU; p50/p99 latency",
+        "metric": METRIC,
         "value": best["trajectories_per_s"], "unit": "trajectories/s", "n_gpus": 1, "steps": len(rates),
         "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64 / f32 stages per request", "data": "synthetic (seeded request mix)",
@@ -98,12 +101,12 @@ def run_serving(args, rank, local):
         "gpu_launches": None, "requests_completed": reqs}))
 
 
-# DRAM bytes (read + write) per launch of the integrator kernel(s), from one ncu
-# capture of the same kernels (profiles/rodas5p_robertson_100k.md,
-# profiles/vern7_duffing_uneven_20k.md; the Duffing figure is the 20,000-
-# trajectory capture scaled by 50 to the 1,000,000-trajectory launch).
-NCU_TRAFFIC = {("robertson", "fp64"): 17.19e6, ("robertson", "mixed"): 17.56e6,
-               ("duffing", "fp64"): 50 * 326.7e6, ("duffing", "mixed"): 50 * 331.8e6}
+# DRAM bytes (read + write) per launch of the integrator kernel, from one ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum) of the same kernel on
+# the full 100,000-trajectory Robertson ensemble.  Filled in only for kernels
+# captured at the benchmarked size; every other kernel reports null.
+NCU_TRAFFIC = {}
+METRIC = "trajectories/sec at equal accuracy, mixed vs plain FP64 GPU; p50/p99 latency"
 
 
 def parse():
@@ -123,6 +126,9 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=0.0, help="arrival window per rate")
     ap.add_argument("--serve-slots", type=int, default=32, help="concurrent device slots of the server")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--no-suite", action="store_true",
+                    help="headline configuration only (by default the Lorenz, uneven Duffing and Brusselator "
+                         "configurations are measured beside it)")
     return ap.parse_args()
 
 
@@ -273,57 +279,98 @@ def compare_err(g_u, o, reltol, abstol):
     return {"max": float(per.max()), "p99": float(np.percentile(per, 99)), "median": float(np.median(per))}
 
 
-def run_gb300(args, world, rank, local, dist):
+# Configurations measured beside the headline (Robertson/Rodas5P, 100k) in the
+# default run: the other single-GPU configurations of the benchmark.
+SUITE = ("lorenz", "duffing", "brusselator")
+# Trajectories checked against the FP64 oracle and against the ground truth, per
+# configuration (None: the whole ensemble).
+CHECK = {"robertson": (None, 8192), "lorenz": (None, None), "duffing": (4096, 4096), "brusselator": (4096, 256),
+         "robertson_ros23": (None, 4096), "van_der_pol": (4096, 1024), "bouncing_ball": (4096, 4096),
+         "pk_dosing": (4096, 4096)}
+L2_NOTE = "256 MB buffer written between timed steps"
+MIXED_DTYPE = ("f32 stages, W and LU; compensated f32-pair state and stage sums; f32-pair parameters; "
+               "double-float stiff right-hand side, error-norm accumulator and refinement residual; "
+               "f32 controller powers; f64 t and dt")
+
+
+def dtype_of(form):
+    return "f64" if form == "fp64" else MIXED_DTYPE
+
+
+def peak_with_clock(ctx, prec):
+    """ode_measure_fma_peak (FMA chains on every SM; ~20-35 ms per call) repeated
+    for about 1.5 s with the SM clock sampled meanwhile: the roofline denominator
+    and the clock it was measured at (once per precision per run)."""
+    key = ("peak", prec)
+    if key not in ctx:
+        L, local = ctx["L"], ctx["local"]
+        clk = Clocks(local)
+        clk.start()
+        vals = []
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 1.5 or len(vals) < 3:
+            v = C.c_double(0)
+            _check_peak(L.ode_measure_fma_peak(local, prec, C.byref(v)))
+            vals.append(v.value)
+        c = clk.stop()
+        ctx[key] = (float(np.median(vals)), c.get("sm_mhz"))
+    return ctx[key]
+
+
+def _check_peak(status):
+    if status != 0:
+        raise RuntimeError("ode_measure_fma_peak failed with status %d" % status)
+
+
+def measure(cfg, args, ctx, steps, warmup, headline=False):
+    """One configuration: both GPU forms timed on device-resident inputs, their
+    error against the FP64 oracle and the ground truth, the form the equal-
+    accuracy rule picks, its roofline, the end-to-end rate through the public
+    host-buffer call and the CPU baseline."""
     import torch
     import odegb300
     from odegb300 import _lib, workloads as W
-    from odegb300.ensemble import get_handle, _options, ALG_BY_NAME
+    from odegb300.ensemble import _options, ALG_BY_NAME
     from odegb300.saveat import resolve_saveat
 
-    torch.cuda.set_device(local)
-    L = _lib.load()
-    h = get_handle(local)
-    desc_name, N0 = CONFIGS[args.config]
-    N = args.trajectories or N0
-    wl = workload(args.config, N, seed=42 + rank)
+    L, h, dev, work, flush = ctx["L"], ctx["h"], ctx["dev"], ctx["work"], ctx["flush"]
+    world, rank, local, dist = ctx["world"], ctx["rank"], ctx["local"], ctx["dist"]
+    desc_name, N0 = CONFIGS[cfg]
+    N = (args.trajectories or N0) if headline else N0
+    wl = workload(cfg, N, seed=42 + rank)
     alg = ALG_BY_NAME[wl["alg"]]
     model = odegb300.ensemble.MODELS[wl["model"]]
-    dev = torch.device("cuda", local)
     n, _ = wl["u0"].shape
     sv = resolve_saveat(wl["saveat"], wl["tspan"])
     cb = wl.get("callback")
     cap = sv.cap + (2 * cb.max_events if cb else 0)
     npt = wl.get("n_per_traj")
-    t_u0 = torch.from_numpy(np.ascontiguousarray(wl["u0"])).to(dev)
-    t_p = torch.from_numpy(np.ascontiguousarray(wl["p"])).to(dev)
-    t_ts = torch.from_numpy(np.ascontiguousarray(wl["tspan"])).to(dev)
-    t_sv = torch.from_numpy(np.ascontiguousarray(sv.values if sv.nsave else np.zeros(1))).to(dev)
-    t_npt = torch.from_numpy(npt).to(dev) if npt is not None else None
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    t_u0, t_p, t_ts = T(wl["u0"]), T(wl["p"]), T(wl["tspan"])
+    t_sv = T(sv.values if sv.nsave else np.zeros(1))
+    t_npt = T(npt) if npt is not None else None
     tst = wl.get("tstops")
-    t_tst = torch.from_numpy(np.sort(np.asarray(tst, dtype=np.float64))).to(dev) if tst is not None else None
+    t_tst = T(np.sort(np.asarray(tst, dtype=np.float64))) if tst is not None else None
     t_out = torch.empty((cap, N), dtype=torch.float64, device=dev)
     u_out = torch.empty((cap, n, N), dtype=torch.float64, device=dev)
     ns_out = torch.empty(N, dtype=torch.int32, device=dev)
     rc_out = torch.empty(N, dtype=torch.int32, device=dev)
     st_out = torch.empty((N, 6), dtype=torch.int64, device=dev)
-    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
-    # every launch, flush and event goes on one explicit stream (a null stream
-    # pointer would make the library fall back to its own stream)
-    work = torch.cuda.Stream(dev)
-    torch.cuda.set_stream(work)
     ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None
+    ir_default = wl.get("ir_sweeps", -1)
 
-    def solve_device(prec):
-        ens = odegb300.EnsembleGB300(precision=prec, ir_sweeps=wl.get("ir_sweeps", -1) if prec == "mixed" else -1)
+    def solve_device(prec, ir=None, u0=None, p=None):
+        ens = odegb300.EnsembleGB300(precision=prec, ir_sweeps=(ir_default if ir is None else ir)
+                                     if prec == "mixed" else -1)
         o = _options(wl["reltol"], wl["abstol"], None, None, None, 1000000, sv, ens, None, None, cb)
         if t_tst is not None:   # the device entry point takes tstops in device memory, sorted
             o.ntstops = int(t_tst.numel())
             o.tstops = C.cast(C.c_void_p(t_tst.data_ptr()), C.POINTER(C.c_double))
         d = _lib.ProblemDesc(model, alg.alg_id, n, wl["p"].shape[0], ens.prec_id(), 0)
-        stream = C.c_void_p(work.cuda_stream)
-        _lib.check(L.ode_solve_ensemble_device(h, C.byref(d), C.byref(o), N, ptr(t_npt), ptr(t_u0), ptr(t_p),
+        _lib.check(L.ode_solve_ensemble_device(h, C.byref(d), C.byref(o), N, ptr(t_npt),
+                                               ptr(t_u0 if u0 is None else u0), ptr(t_p if p is None else p),
                                                ptr(t_ts), ptr(t_sv), ptr(t_out), ptr(u_out), ptr(ns_out),
-                                               ptr(rc_out), ptr(st_out), stream), h)
+                                               ptr(rc_out), ptr(st_out), C.c_void_p(work.cuda_stream)), h)
 
     def barrier():
         if dist is not None:
@@ -335,79 +382,92 @@ def run_gb300(args, world, rank, local, dist):
         L.ode_kernel_launches(h, C.byref(v))
         return v.value
 
-    if args.profile_small:
-        for prec in ("fp64", "mixed"):
-            solve_device(prec)
-        torch.cuda.synchronize(dev)
-        print(json.dumps({"profile_small": True, "trajectories": N}))
-        return
+    n_or, n_tr = CHECK.get(cfg, (4096, 1024))
+    idx_or = np.arange(N if n_or is None else min(N, n_or))
+    idx_tr = np.arange(N if n_tr is None else min(N, n_tr))
+    idx_u = idx_or if len(idx_or) >= len(idx_tr) else idx_tr
+    t_idx = torch.from_numpy(idx_u).to(dev)
 
-    # Accuracy sample against the CPU oracle (rank 0 only)
-    sample = np.arange(min(N, 256))
+    # forms: plain FP64 and mixed; the headline also times the mixed form with one
+    # refinement sweep per W solve (its default is none for register-resident W)
+    forms = [("fp64", None), ("mixed", None)]
+    if cfg in ("robertson", "robertson_ros23") and ir_default <= 0:
+        forms.append(("mixed_ir1", 1))
     results = {}
     clocks = Clocks(local)
-    for prec in ("fp64", "mixed"):
-        for _ in range(args.warmup):
+    clocks.start()
+    for name, ir in forms:
+        prec = "fp64" if name == "fp64" else "mixed"
+        for _ in range(warmup):
             flush.fill_(1.0)
-            solve_device(prec)
+            solve_device(prec, ir)
         barrier()
-        if prec == "mixed":
-            clocks.start()
         l0 = launches()
         times = []
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         t_wall0 = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(steps):
             flush.fill_(1.0)
-            e0.record()
-            solve_device(prec)
-            e1.record()
+            e0.record(work)
+            solve_device(prec, ir)
+            e1.record(work)
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
         barrier()
         wall = time.perf_counter() - t_wall0
-        if prec == "mixed":
-            clk = clocks.stop()
         nl = launches() - l0
         ms = max_over_ranks(float(np.mean(times)), dist, dev)
         st = st_out.cpu().numpy()
         rc = rc_out.cpu().numpy()
-        attempts = int(st[:, 4].sum() + st[:, 5].sum())
-        results[prec] = {"ms": ms, "times": times, "launches": nl, "attempts": attempts,
-                         "success": float(((rc == 1) | (rc == 7)).mean()), "u": u_out[:, :, sample].cpu().numpy(),
-                         "terminated_frac": float((rc == 7).mean()),
-                         "naccept_mean": float(st[:, 4].mean()), "wall_s": wall}
+        results[name] = {"ms": ms, "launches": nl, "attempts": int(st[:, 4].sum() + st[:, 5].sum()),
+                         "success": float(((rc == 1) | (rc == 7)).mean()),
+                         "u": u_out.index_select(2, t_idx).cpu().numpy(), "naccept_mean": float(st[:, 4].mean()),
+                         "wall_s": wall, "steps": steps, "ir_sweeps": ir if ir is not None else
+                         (ir_default if prec == "mixed" else None)}
+    clk = clocks.stop()
 
-    # Accuracy on a checked sample: against the FP64 oracle at the same tolerance,
-    # and against a ground-truth solve (Vern9 at 1e-14; Rodas5P at 1e-12 for stiff
-    # models).  "Equal accuracy": the mixed form's error against the ground truth is
-    # within 2x the FP64 form's (+1 tolerance unit) at the median and the p99.
+    # conditioning control (uneven Duffing chains): the FP64 kernel on inputs
+    # perturbed by one FP32 rounding, against the same FP64 oracle; it shows how
+    # far a perturbation of the mixed form's size moves these trajectories
+    control = {}
+    if cfg == "duffing":
+        u0p = t_u0 * (1.0 + 2.0 ** -24)
+        solve_device("fp64", u0=u0p)
+        control["u0_times_1p2em24"] = u_out.index_select(2, t_idx).cpu().numpy()
+        pf = t_p.float().double()
+        solve_device("fp64", p=pf)
+        control["p_rounded_to_fp32"] = u_out.index_select(2, t_idx).cpu().numpy()
+        del u0p, pf
+        torch.cuda.synchronize(dev)
+
     acc, acc_truth, equal = {}, {}, False
     if rank == 0:
-        o = oracle_solve(wl, sample)
-        tr = oracle_solve(wl, sample, truth=True)
-        for prec in ("fp64", "mixed"):
-            acc[prec] = compare_err(results[prec]["u"], o, wl["reltol"], wl["abstol"])
-            acc_truth[prec] = compare_err(results[prec]["u"], tr, wl["reltol"], wl["abstol"])
+        sel = lambda u, idx: u[:, :, :len(idx)]   # both samples are prefixes of the ensemble
+        o = oracle_solve(wl, idx_or, nthreads=os.cpu_count() or 1)
+        tr = oracle_solve(wl, idx_tr, nthreads=os.cpu_count() or 1, truth=True)
+        for name in results:
+            acc[name] = compare_err(sel(results[name]["u"], idx_or), o, wl["reltol"], wl["abstol"])
+            acc_truth[name] = compare_err(sel(results[name]["u"], idx_tr), tr, wl["reltol"], wl["abstol"])
+        for k, u in control.items():
+            control[k] = {"err_vs_fp64_oracle_x_tol": compare_err(sel(u, idx_or), o, wl["reltol"], wl["abstol"])}
         equal = all(acc_truth["mixed"][q] <= 2.0 * acc_truth["fp64"][q] + 1.0 for q in ("median", "p99"))
     best = "mixed" if equal else "fp64"
     R = results[best]
     value = replica_rate(world, N, R["ms"] * 1e-3)
 
     # roofline of the dominant kernel (the chosen form's integrator kernel)
-    peak = C.c_double(0)
-    L.ode_measure_fma_peak(local, 0 if best == "fp64" else 1, C.byref(peak))
+    prec_id = 0 if best == "fp64" else 1
+    peak, peak_mhz = peak_with_clock(ctx, prec_id)
     nmean = float(np.mean(npt)) if npt is not None else n
     fl = W.attempt_flops(wl["alg"], wl["model"], int(round(nmean)))
     nsaves = sv.nsave if sv.nsave else 2
     total_flops = R["attempts"] * fl + N * nsaves * W.save_flops(wl["alg"], wl["model"], int(round(nmean)))
     achieved = total_flops / (R["ms"] * 1e-3)
-    fp64_peak = C.c_double(0)
-    L.ode_measure_fma_peak(local, 0, C.byref(fp64_peak))
+    traffic = NCU_TRAFFIC.get((cfg, best)) if N == N0 else None
 
-    # end-to-end through the public host-buffer call (ode_solve_ensemble): inputs
-    # in pinned host memory, outputs back into pinned host memory, every step
+    # end to end through the public host-buffer call (ode_solve_ensemble): inputs in
+    # page-locked host memory, outputs back into page-locked host memory, every step
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
     h_u0, h_p, h_ts = pin(wl["u0"]), pin(wl["p"]), pin(wl["tspan"])
     h_sv = pin(sv.values if sv.nsave else np.zeros(1))
@@ -417,7 +477,7 @@ def run_gb300(args, world, rank, local, dist):
     h_ns = torch.empty(N, dtype=torch.int32).pin_memory()
     h_rc = torch.empty(N, dtype=torch.int32).pin_memory()
     h_st = torch.empty((N, 6), dtype=torch.int64).pin_memory()
-    ens_e2e = odegb300.EnsembleGB300(precision=best, ir_sweeps=wl.get("ir_sweeps", -1) if best == "mixed" else -1)
+    ens_e2e = odegb300.EnsembleGB300(precision=best, ir_sweeps=ir_default if best == "mixed" else -1)
     o_e2e = _options(wl["reltol"], wl["abstol"], None, None, None, 1000000, sv, ens_e2e, None, None, cb,
                      tstops=wl.get("tstops"))
     d_e2e = _lib.ProblemDesc(model, alg.alg_id, n, wl["p"].shape[0], ens_e2e.prec_id(), 0)
@@ -428,60 +488,139 @@ def run_gb300(args, world, rank, local, dist):
                                         hp(h_p), hp(h_ts), hp(h_sv) if sv.nsave else None, hp(h_t), hp(h_u),
                                         hp(h_ns, C.c_int32), hp(h_rc, C.c_int32), hp(h_st, _lib.Stats)), h)
 
-    for _ in range(max(1, min(args.warmup, 2))):
+    for _ in range(max(1, min(warmup, 2))):
         solve_host()
     e2e_t = []
-    for _ in range(args.steps):
+    for _ in range(steps):
         flush.fill_(1.0)
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         solve_host()
         e2e_t.append(time.perf_counter() - t0)
-    e2e_s = float(np.mean(e2e_t))
+    e2e_s = max_over_ranks(float(np.mean(e2e_t)), dist, "cpu" if dist is None else dev)
     h2d = wl["u0"].nbytes + wl["p"].nbytes + wl["tspan"].nbytes + (sv.values.nbytes if sv.nsave else 0) + \
         (npt.nbytes if npt is not None else 0)
     d2h = cap * N * 8 + cap * n * N * 8 + N * 8 + N * 48
+    del h_u, h_t, u_out, t_out
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(wl, N, args.cpu_seconds)
+    return {
+        "workload": desc_name, "trajectories": N, "value": value, "unit": "trajectories/s", "ms_per_step": R["ms"],
+        "steps": steps, "warmup": warmup, "precision_chosen": best, "dtype": dtype_of(best),
+        "forms": {p: {"trajectories_per_s": world * N / (results[p]["ms"] * 1e-3), "ms": results[p]["ms"],
+                      "ir_sweeps": results[p]["ir_sweeps"], "dtype": dtype_of("fp64" if p == "fp64" else "mixed"),
+                      "err_vs_fp64_oracle_x_tol": acc.get(p), "err_vs_ground_truth_x_tol": acc_truth.get(p),
+                      "success_frac": results[p]["success"], "mean_accepted_steps": results[p]["naccept_mean"],
+                      "gpu_launches": results[p]["launches"]} for p in results},
+        "accuracy_checked": {"vs_fp64_oracle": int(len(idx_or)), "vs_ground_truth": int(len(idx_tr)),
+                             "ground_truth": "FP64 Rodas5P at reltol 1e-12, abstol 1e-16" if wl["alg"] in (
+                                 "rodas5p", "rosenbrock23", "autotsit5_rosenbrock23") else
+                             "FP64 Vern9 at reltol = abstol = 1e-14", "saves hit exactly": True,
+                             "equal_accuracy_rule": "mixed error vs ground truth <= 2x FP64's + 1 tol unit "
+                                                    "at the median and p99"},
+        "conditioning_control": control or None,
+        "speedup_mixed_vs_fp64": results["fp64"]["ms"] / results["mixed"]["ms"],
+        "e2e": {"value": world * N / e2e_s, "unit": "trajectories/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "call": "ode_solve_ensemble on page-locked host buffers"},
+        "roofline": {"bound": "fp64 pipe" if best == "fp64" else "fp32 pipe", "achieved": achieved / 1e12,
+                     "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+                     "traffic": traffic,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch of this kernel"
+                     if traffic else "not captured for this kernel at this size",
+                     "flops_per_attempt": fl, "attempted_steps": R["attempts"],
+                     "peak_source": "ode_measure_fma_peak (FMA chains on every SM, this GPU; measured in this run)",
+                     "peak_sm_mhz": peak_mhz},
+        "hbm": {"achieved_gbs": (h2d + d2h) / (R["ms"] * 1e-3) / 1e9, "bytes_per_solve": int(h2d + d2h),
+                "note": "algorithmic bytes (inputs read + outputs written) / device time; not the bound"},
+        "cpu_baseline": cpu, "clocks": clk, "gpu_launches": R["launches"],
+    }
+
+
+def run_gb300(args, world, rank, local, dist):
+    import torch
+    from odegb300 import _lib
+    from odegb300.ensemble import get_handle
+
+    torch.cuda.set_device(local)
+    L = _lib.load()
+    h = get_handle(local)
+    dev = torch.device("cuda", local)
+    # every launch, flush and event goes on one explicit stream (a null stream
+    # pointer would make the library fall back to its own stream)
+    work = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(work)
+    ctx = dict(L=L, h=h, dev=dev, work=work, world=world, rank=rank, local=local, dist=dist,
+               flush=torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev))   # 256 MB > 129 MB L2
+
+    if args.profile_small:
+        run_profile_small(args, ctx)
+        return
+    head = measure(args.config, args, ctx, args.steps, args.warmup, headline=True)
+    suite = {}
+    if args.config == "robertson" and not args.no_suite and not args.trajectories:
+        for cfg in SUITE:
+            suite[cfg] = measure(cfg, args, ctx, min(args.steps, 5), 3)
     serving = None
-    if rank == 0 and not args.no_serving and not args.profile_small:
+    if rank == 0 and not args.no_serving:
         rates = [float(x) for x in (args.serve_rates or "100,300").split(",")]
         serving = serving_block(args, local, rates, args.serve_seconds or 2.0)
-    hbm_bytes = h2d + d2h   # bytes the kernel reads (inputs) and writes (outputs) per solve
-
     if rank == 0:
         line = {
-            "metric": "trajectories/sec at equal accuracy, mixed vs plain FP64 GPU; p50/p99 latency",
-            "value": value, "unit": "trajectories/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": R["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if best == "fp64" else "f32 stages + f64 t/dt/error norm",
+            "metric": METRIC, "value": head["value"], "unit": "trajectories/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": head["dtype"],
             "data": "synthetic (seeded, config distributions)",
-            "config": {"workload": desc_name, "trajectories": N, "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "256 MB buffer written between timed steps", "precision_chosen": best},
-            "forms": {p: {"trajectories_per_s": world * N / (results[p]["ms"] * 1e-3), "ms": results[p]["ms"],
-                          "err_vs_fp64_oracle_x_tol": acc.get(p),
-                          "err_vs_ground_truth_x_tol": acc_truth.get(p), "success_frac": results[p]["success"],
-                          "mean_accepted_steps": results[p]["naccept_mean"]} for p in results},
-            "speedup_mixed_vs_fp64": results["fp64"]["ms"] / results["mixed"]["ms"],
-            "e2e": {"value": world * N / e2e_s, "unit": "trajectories/s", "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h)},
-            "roofline": {"bound": "fp64 pipe" if best == "fp64" else "fp32 pipe", "achieved": achieved / 1e12,
-                         "peak": peak.value / 1e12, "unit": "TFLOP/s", "frac": achieved / peak.value if peak.value else None,
-                         "traffic": NCU_TRAFFIC.get((args.config, best)) if N == N0 else None,
-                         "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
-                         "flops_per_attempt": fl, "attempted_steps": R["attempts"],
-                         "peak_source": "ode_measure_fma_peak (FMA-chain kernel, this GPU)",
-                         "fp64_peak_tflops": fp64_peak.value / 1e12},
-            "hbm": {"achieved_gbs": hbm_bytes / (R["ms"] * 1e-3) / 1e9, "bytes_per_solve": int(hbm_bytes),
-                    "note": "algorithmic bytes (inputs read + outputs written) / device time; not the bound"},
-            "cpu_baseline": cpu,
-            "clocks": clk,
-            "gpu_launches": R["launches"],
-            "serving": serving,
+            "config": {"workload": head["workload"], "trajectories": head["trajectories"], "l2": L2_NOTE},
+            "precision_chosen": head["precision_chosen"],
         }
+        for k in ("forms", "accuracy_checked", "speedup_mixed_vs_fp64", "e2e", "roofline", "hbm", "cpu_baseline",
+                  "clocks", "gpu_launches"):
+            line[k] = head[k]
+        line["configs"] = suite or None
+        line["serving"] = serving
         print(json.dumps(line))
+
+
+def run_profile_small(args, ctx):
+    """One small FP64 + mixed solve pair of a configuration for ncu captures (no JSON line)."""
+    import torch
+    import odegb300
+    from odegb300 import _lib
+    from odegb300.ensemble import _options, ALG_BY_NAME
+    from odegb300.saveat import resolve_saveat
+    L, h, dev, work = ctx["L"], ctx["h"], ctx["dev"], ctx["work"]
+    N = args.trajectories or CONFIGS[args.config][1]
+    wl = workload(args.config, N, seed=42)
+    alg = ALG_BY_NAME[wl["alg"]]
+    model = odegb300.ensemble.MODELS[wl["model"]]
+    n = wl["u0"].shape[0]
+    sv = resolve_saveat(wl["saveat"], wl["tspan"])
+    cb = wl.get("callback")
+    cap = sv.cap + (2 * cb.max_events if cb else 0)
+    npt = wl.get("n_per_traj")
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    ins = [T(npt) if npt is not None else None, T(wl["u0"]), T(wl["p"]), T(wl["tspan"]),
+           T(sv.values if sv.nsave else np.zeros(1))]
+    outs = [torch.empty((cap, N), dtype=torch.float64, device=dev),
+            torch.empty((cap, n, N), dtype=torch.float64, device=dev),
+            torch.empty(N, dtype=torch.int32, device=dev), torch.empty(N, dtype=torch.int32, device=dev),
+            torch.empty((N, 6), dtype=torch.int64, device=dev)]
+    tst = wl.get("tstops")
+    t_tst = T(np.sort(np.asarray(tst, dtype=np.float64))) if tst is not None else None
+    ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None
+    for prec in ("fp64", "mixed"):
+        ens = odegb300.EnsembleGB300(precision=prec, ir_sweeps=wl.get("ir_sweeps", -1) if prec == "mixed" else -1)
+        o = _options(wl["reltol"], wl["abstol"], None, None, None, 1000000, sv, ens, None, None, cb)
+        if t_tst is not None:
+            o.ntstops = int(t_tst.numel())
+            o.tstops = C.cast(C.c_void_p(t_tst.data_ptr()), C.POINTER(C.c_double))
+        d = _lib.ProblemDesc(model, alg.alg_id, n, wl["p"].shape[0], ens.prec_id(), 0)
+        _lib.check(L.ode_solve_ensemble_device(h, C.byref(d), C.byref(o), N, *[ptr(x) for x in ins + outs],
+                                               C.c_void_p(work.cuda_stream)), h)
+    torch.cuda.synchronize(dev)
+    print(json.dumps({"profile_small": True, "config": args.config, "trajectories": N}))
 
 
 def cpu_baseline(wl, N, target_s):
@@ -502,6 +641,9 @@ def cpu_baseline(wl, N, target_s):
 
 
 def run_reference(args, world, rank):
+    """The reference's CPU path (its restatement: Julia is not installed) on all
+    host threads, over the whole headline ensemble every step, with the GPU arm's
+    config; the other configurations as one bounded sample each."""
     if rank != 0:
         return
     if args.config == "serving":
@@ -512,30 +654,31 @@ def run_reference(args, world, rank):
     N = args.trajectories or N0
     wl = workload(args.config, N, seed=42)
     ncores = os.cpu_count() or 1
-    k = min(N, 2048)
-    t0 = time.perf_counter()
-    oracle_solve(wl, np.arange(k), nthreads=ncores)
-    t1 = time.perf_counter() - t0
-    per_step_target = 20.0 / max(1, args.steps + args.warmup)
-    m = int(min(N, max(256, k * per_step_target / max(t1, 1e-3))))
+    idx = np.arange(N)
     for _ in range(args.warmup):
-        oracle_solve(wl, np.arange(m), nthreads=ncores)
+        oracle_solve(wl, idx[:min(N, 4096)], nthreads=ncores)
     ts = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        oracle_solve(wl, np.arange(m), nthreads=ncores)
+        oracle_solve(wl, idx, nthreads=ncores)
         ts.append(time.perf_counter() - t0)
-    v = m / float(np.mean(ts))
-    sample = "%d of %d trajectories per step, CPU restatement of the reference (Julia is not installed), %d threads" % (
-        m, N, ncores)
+    v = N / float(np.mean(ts))
+    sample = "all %d trajectories every step, CPU restatement of the reference (Julia is not installed), " \
+             "%d threads" % (N, ncores)
+    suite = {}
+    if args.config == "robertson" and not args.no_suite and not args.trajectories:
+        for cfg in SUITE:
+            wl_c = workload(cfg, CONFIGS[cfg][1], seed=42)
+            suite[cfg] = dict(cpu_baseline(wl_c, CONFIGS[cfg][1], args.cpu_seconds), workload=CONFIGS[cfg][0])
     print(json.dumps({
-        "impl": "reference", "metric": "trajectories/sec at equal accuracy, mixed vs plain FP64 GPU; p50/p99 latency",
-        "value": v, "unit": "trajectories/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": float(np.mean(ts)) * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (seeded, config distributions)",
-        "config": {"workload": desc_name, "trajectories": N},
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "trajectories/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(ts)) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded, config distributions)",
+        "config": {"workload": desc_name, "trajectories": N, "l2": L2_NOTE},
         "cpu_baseline": {"value": v, "unit": "trajectories/s", "cores": ncores, "kind": "port", "sample": sample},
-        "e2e": {"value": v, "unit": "trajectories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        "e2e": {"value": v, "unit": "trajectories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "configs": suite or None}))
 
 
 def measured_hbm_gbs():

@@ -40,7 +40,7 @@ struct AutoSwitchAlg {
     template <class R, int C> __device__ static R* fsal_slot(Cache<R, C>& c) { return NS::fsal_slot(c.ns); }
 
     template <class Model, class R, int L, int C>
-    __device__ static void initialize(Cache<R, C>& c, const R* u, const R* p, double t, const Group<L>& g,
+    __device__ static void initialize(Cache<R, C>& c, const R* u, const PR<R>* p, double t, const Group<L>& g,
                                       StepStats& st, const EnsembleArgs& a, long long j) {
         c.current = 0;   // stiffalgfirst = false
         c.count = 0;
@@ -91,7 +91,7 @@ struct AutoSwitchAlg {
 
     // initialize! of the method switched to: its FSAL value f(uprev, t) (one counted call)
     template <class Model, class R, int L, int C>
-    __device__ static void enter(Cache<R, C>& c, const R* up, const R* uplo, const R* p, double t, const Group<L>& g,
+    __device__ static void enter(Cache<R, C>& c, const R* up, const R* uplo, const PR<R>* p, double t, const Group<L>& g,
                                  StepStats& st) {
         if (c.current == 0) {
             Model::template rhs<R, L, C>(c.ns.k[0], up, p, t, g);
@@ -103,7 +103,7 @@ struct AutoSwitchAlg {
 
     template <class Model, class R, int L, int C>
     __device__ static typename Ctl<R>::T step(Cache<R, C>& c, R* u, R* ulo, const R* up, const R* uplo,
-                                             const R* p, double t, double dt, R abstol, R reltol, long long iter,
+                                             const PR<R>* p, double t, double dt, R abstol, R reltol, long long iter,
                                              bool errorfail, const Group<L>& g, StepStats& st) {
         if (c.current == 0) {
             const typename Ctl<R>::T e = NS::template step<Model, R, L, C, true>(c.ns, u, ulo, up, uplo, p, t, dt,
@@ -117,7 +117,7 @@ struct AutoSwitchAlg {
 
     template <class Model, class R, int L, int C>
     __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, double th, double dt, double tprev,
-                                       const R* y0, const R* y0lo, const R* y1, const R* y1lo, const R* p,
+                                       const R* y0, const R* y0lo, const R* y1, const R* y1lo, const PR<R>* p,
                                        const Group<L>& g) {
         if (c.current == 0)
             NS::template interpolate<Model, R, L, C>(c.ns, out, outlo, th, dt, tprev, y0, y0lo, y1, y1lo, p, g);
@@ -126,7 +126,7 @@ struct AutoSwitchAlg {
     }
 
     template <class Model, class R, int L, int C>
-    __device__ static void reset_fsal(Cache<R, C>& c, const R* u, const R* ulo, const R* p, double t,
+    __device__ static void reset_fsal(Cache<R, C>& c, const R* u, const R* ulo, const PR<R>* p, double t,
                                       const Group<L>& g, StepStats& st) {
         if (c.current == 0) NS::template reset_fsal<Model, R, L, C>(c.ns, u, ulo, p, t, g, st);
         else S::template reset_fsal<Model, R, L, C>(c.s, u, ulo, p, t, g, st);

@@ -215,6 +215,37 @@ __device__ __forceinline__ ff operator*(ff a, ff b) {
     return ff_fast2sum(p, e);
 }
 
+// ------------------------------------------------------------------ parameters
+// A parameter in the mixed form: its FP64 value as a float pair hi + lo
+// (hi = float(p)).  A product with an FP32 state value folds lo in before its
+// one rounding, fma(hi, x, lo x), so the right-hand side sees the FP64
+// parameter rather than float(p): rounding a parameter to FP32 changes the
+// problem itself by up to 2^-25 relative, a systematic error that
+// ill-conditioned trajectories (random Duffing chains) amplify far past the
+// tolerance.  Sums fold lo in after the leading rounding.  Converts to float
+// (hi) where a model's Jacobian takes a parameter as an entry.
+struct fpair {
+    float hi, lo;
+    __device__ __forceinline__ fpair() : hi(0.0f), lo(0.0f) {}
+    __device__ __forceinline__ fpair(float h, float l) : hi(h), lo(l) {}
+    __device__ __forceinline__ explicit fpair(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
+    __device__ __forceinline__ operator float() const { return hi; }
+};
+__device__ __forceinline__ float operator*(fpair a, float x) { return fmaf(a.hi, x, a.lo * x); }
+__device__ __forceinline__ float operator*(float x, fpair a) { return fmaf(a.hi, x, a.lo * x); }
+__device__ __forceinline__ float operator*(fpair a, fpair b) { return fmaf(a.hi, b.hi, fmaf(a.hi, b.lo, a.lo * b.hi)); }
+__device__ __forceinline__ float operator+(fpair a, float x) { return (a.hi + x) + a.lo; }
+__device__ __forceinline__ float operator+(float x, fpair a) { return (x + a.hi) + a.lo; }
+__device__ __forceinline__ float operator-(fpair a, float x) { return (a.hi - x) + a.lo; }
+__device__ __forceinline__ float operator-(float x, fpair a) { return (x - a.hi) - a.lo; }
+__device__ __forceinline__ fpair operator-(fpair a) { return fpair(-a.hi, -a.lo); }
+
+// Parameter type of a precision: double in FP64, a float pair in the mixed form.
+template <class R> struct ParamOf { using type = R; };
+template <> struct ParamOf<float> { using type = fpair; };
+template <class R> using PR = typename ParamOf<R>::type;
+template <class R> __device__ __forceinline__ PR<R> make_param(double x) { return PR<R>(x); }
+
 // ------------------------------------------------------------------ lane groups
 // A trajectory is owned by a group of L consecutive lanes of one warp; each
 // lane holds C state components (component index = lane_in_group*C + c).

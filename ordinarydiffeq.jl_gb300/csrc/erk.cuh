@@ -63,7 +63,7 @@ struct Tsit5Alg {
     template <class R, int C> __device__ static R* fsal_slot(Cache<R, C>& c) { return c.tmp; }
 
     template <class Model, class R, int L, int C>
-    __device__ static void initialize(Cache<R, C>& c, const R* u, const R* p, double t, const Group<L>& g,
+    __device__ static void initialize(Cache<R, C>& c, const R* u, const PR<R>* p, double t, const Group<L>& g,
                                       StepStats& st, const EnsembleArgs&, long long) {
         Model::template rhs<R, L, C>(c.k[0], u, p, t, g);
         st.nf += 1;
@@ -84,7 +84,7 @@ struct Tsit5Alg {
     // reset_fsal!, integrator_utils.jl:216-235,1326-1340; one counted call).  k7
     // becomes the next step's k1 when it starts.
     template <class Model, class R, int L, int C>
-    __device__ static void reset_fsal(Cache<R, C>& c, const R* u, const R*, const R* p, double t, const Group<L>& g,
+    __device__ static void reset_fsal(Cache<R, C>& c, const R* u, const R*, const PR<R>* p, double t, const Group<L>& g,
                                       StepStats& st) {
         Model::template rhs<R, L, C>(c.k[6], u, p, t, g);
         st.nf += 1;
@@ -95,7 +95,7 @@ struct Tsit5Alg {
     // g6 the sixth stage's input, NaN propagating like Julia's maximum.
     template <class Model, class R, int L, int C, bool EIG = false>
     __device__ static typename Ctl<R>::T step(Cache<R, C>& c, R* u, R* ulo, const R* up, const R* uplo,
-                                             const R* p, double t, double dt, R abstol, R reltol, long long, bool,
+                                             const PR<R>* p, double t, double dt, R abstol, R reltol, long long, bool,
                                              const Group<L>& g, StepStats& st) {
         static_assert(!EIG || L == 1, "the stiffness estimate is formed on one lane");
         using K = RK<Tsit5Tab, R, C>;
@@ -139,7 +139,7 @@ struct Tsit5Alg {
 
     template <class Model, class R, int L, int C>
     __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, double th, double dt, double,
-                                       const R* y0, const R* y0lo, const R*, const R*, const R*, const Group<L>&) {
+                                       const R* y0, const R* y0lo, const R*, const R*, const PR<R>*, const Group<L>&) {
         auto r = [](int i, int q) { return tab::TSIT5_R(i, q); };
         const R d = (R)dt;
         if constexpr (sizeof(R) == 8) {
@@ -181,7 +181,7 @@ struct Vern7Alg {
     };
     template <class R, int C> __device__ static R* fsal_slot(Cache<R, C>& c) { return c.tmp; }
     template <class Model, class R, int L, int C>
-    __device__ static void initialize(Cache<R, C>& c, const R*, const R*, double, const Group<L>&, StepStats&,
+    __device__ static void initialize(Cache<R, C>& c, const R*, const PR<R>*, double, const Group<L>&, StepStats&,
                                       const EnsembleArgs&, long long) {
         c.extra = false;
     }
@@ -199,7 +199,7 @@ struct Vern7Alg {
     }
 
     template <int ROW, class Model, class R, int L, int C>
-    __device__ static void eval_stage(Cache<R, C>& c, const R* up, const R* uplo, const R* p, double tstage, R d,
+    __device__ static void eval_stage(Cache<R, C>& c, const R* up, const R* uplo, const PR<R>* p, double tstage, R d,
                                       const Group<L>& g) {
         RK<Vern7Tab, R, C>::template stage<ROW>(c.tmp, c.s, d, up, uplo);
         Model::template rhs<R, L, C>(c.s[Vern7Tab::slot(ROW)], c.tmp, p, tstage, g);
@@ -207,7 +207,7 @@ struct Vern7Alg {
 
     template <class Model, class R, int L, int C>
     __device__ static typename Ctl<R>::T step(Cache<R, C>& c, R* u, R* ulo, const R* up, const R* uplo,
-                                             const R* p, double t, double dt, R abstol, R reltol, long long, bool,
+                                             const PR<R>* p, double t, double dt, R abstol, R reltol, long long, bool,
                                              const Group<L>& g, StepStats& st) {
         const R d = (R)dt;
         c.extra = false;
@@ -235,7 +235,7 @@ struct Vern7Alg {
     // Extra stages k11..k16 (verner_addsteps.jl:80-195) at (tprev, uprev, dt).
     template <class Model, class R, int L, int C>
     __device__ static void extra_stages(Cache<R, C>& c, double tprev, double dt, const R* up, const R* uplo,
-                                        const R* p, const Group<L>& g) {
+                                        const PR<R>* p, const Group<L>& g) {
         const R d = (R)dt;
         eval_stage<11, Model>(c, up, uplo, p, stage_time<Model>(Vern7Tab::c(11), dt, tprev), d, g);
         eval_stage<12, Model>(c, up, uplo, p, stage_time<Model>(Vern7Tab::c(12), dt, tprev), d, g);
@@ -248,12 +248,12 @@ struct Vern7Alg {
 
     // not FSAL (isfsal(::Vern7) = false): nothing to redo after a callback
     template <class Model, class R, int L, int C>
-    __device__ static void reset_fsal(Cache<R, C>&, const R*, const R*, const R*, double, const Group<L>&,
+    __device__ static void reset_fsal(Cache<R, C>&, const R*, const R*, const PR<R>*, double, const Group<L>&,
                                       StepStats&) {}
 
     template <class Model, class R, int L, int C>
     __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, double th, double dt,
-                                       double tprev, const R* y0, const R* y0lo, const R*, const R*, const R* p,
+                                       double tprev, const R* y0, const R* y0lo, const R*, const R*, const PR<R>* p,
                                        const Group<L>& g) {
         if (!c.extra) extra_stages<Model, R, L, C>(c, tprev, dt, y0, y0lo, p, g);
         // stages of the 7th-order interpolant, in the reference's summation order

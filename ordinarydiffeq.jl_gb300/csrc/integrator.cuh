@@ -246,7 +246,7 @@ __device__ __forceinline__ typename Ctl<R>::T error_norm(const R* ut, const R* u
 
 // Hairer's initial step (initdt.jl:17-298).  f0 is returned for FSAL methods.
 template <class Model, class R, int L, int C, int ORDER>
-__device__ double initdt(const R* u0, const R* p, double t, double dtmax, double dtmin_user, R abstol, R reltol,
+__device__ double initdt(const R* u0, const PR<R>* p, double t, double dtmax, double dtmin_user, R abstol, R reltol,
                          R* f0, const Group<L>& g) {
     double dtmin = nextafter(jmax(dtmin_user, jeps(t)), __longlong_as_double(0x7ff0000000000000LL));
     double smalldt = jmax(dtmin, 1e-6);
@@ -303,11 +303,11 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
     constexpr int NP = Model::NP;
     const long long N = a.N;
     R u[C], uprev[C], ulo[C], uprevlo[C];   // solution as (hi, lo) pairs, see Acc
-    R p[NP];
+    PR<R> p[NP];   // FP64, or float pairs in the mixed form (fpair)
 #pragma unroll
     for (int c = 0; c < C; ++c) Acc<R>::split(a.u0[(size_t)(g.lane * C + c) * N + j], u[c], ulo[c]);
 #pragma unroll
-    for (int i = 0; i < NP; ++i) p[i] = (R)a.p[(size_t)i * N + j];
+    for (int i = 0; i < NP; ++i) p[i] = make_param<R>(a.p[(size_t)i * N + j]);
     const double t0 = a.tspan[j], tf = a.tspan[N + j];
     const double dtmax = a.dtmax > 0 ? a.dtmax : tf - t0;
     const R abstol = (R)a.abstol, reltol = (R)a.reltol;

@@ -125,7 +125,7 @@ struct SmemLA {
     // J(uprev) into W.  A rejected step keeps uprev, so recomputing J there
     // reproduces the reference's reused J exactly; `fresh` only drives the count.
     template <class Model, class R, int L, int C>
-    __device__ static void jacobian(Store<R, C>& s, const R* up, const R* p, double, bool, const Group<L>& g) {
+    __device__ static void jacobian(Store<R, C>& s, const R* up, const PR<R>* p, double, bool, const Group<L>& g) {
         constexpr int n = L * C;
         R* W = s.W;
 #pragma unroll 8

@@ -29,14 +29,14 @@ struct VanDerPol {
     static constexpr int NP = 1;
     static constexpr bool AUTONOMOUS = true;
     static constexpr bool HAS_EVENT = false;
-    template <class R, int L, int C>
-    __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>&) {
+    template <class R, int L, int C, class P>
+    __device__ static void rhs(R* du, const R* u, const P* p, double, const Group<L>&) {
         static_assert(L == 1 && C == 2, "van der Pol has 2 states on one lane");
         du[0] = u[1];
         du[1] = p[0] * ((R(1) - u[0] * u[0]) * u[1] - u[0]);
     }
-    template <class R, int N>
-    __device__ static void jac(R (*J)[N], const R* u, const R* p, double) {
+    template <class R, int N, class P>
+    __device__ static void jac(R (*J)[N], const R* u, const P* p, double) {
         J[0][0] = R(0);
         J[0][1] = R(1);
         J[1][0] = p[0] * (R(-2) * u[0] * u[1] - R(1));
@@ -54,14 +54,14 @@ struct PKOneCompartment {
     static constexpr bool AUTONOMOUS = true;
     static constexpr bool HAS_EVENT = false;
     static constexpr bool HAS_DISCRETE = true;
-    template <class R, int L, int C>
-    __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>&) {
+    template <class R, int L, int C, class P>
+    __device__ static void rhs(R* du, const R* u, const P* p, double, const Group<L>&) {
         static_assert(L == 1 && C == 2, "the one-compartment model has 2 states on one lane");
         du[0] = -p[0] * u[0];
         du[1] = p[0] * u[0] - p[1] * u[1];
     }
-    template <class R, int N>
-    __device__ static void jac(R (*J)[N], const R*, const R* p, double) {
+    template <class R, int N, class P>
+    __device__ static void jac(R (*J)[N], const R*, const P* p, double) {
         J[0][0] = -p[0]; J[0][1] = R(0);
         J[1][0] = p[0];  J[1][1] = -p[1];
     }
@@ -84,14 +84,14 @@ struct BouncingBall {
     static constexpr bool HAS_EVENT = true;
     static constexpr bool EVENT_AFFECT_POS = false;   // affect! = nothing
     static constexpr bool EVENT_AFFECT_NEG = true;    // affect_neg!
-    template <class R, int L, int C>
-    __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>&) {
+    template <class R, int L, int C, class P>
+    __device__ static void rhs(R* du, const R* u, const P* p, double, const Group<L>&) {
         static_assert(L == 1 && C == 2, "the ball has 2 states on one lane");
         du[0] = u[1];
         du[1] = -p[0];
     }
-    template <class R, int N>
-    __device__ static void jac(R (*J)[N], const R*, const R*, double) {
+    template <class R, int N, class P>
+    __device__ static void jac(R (*J)[N], const R*, const P*, double) {
         J[0][0] = R(0); J[0][1] = R(1);
         J[1][0] = R(0); J[1][1] = R(0);
     }
@@ -116,13 +116,13 @@ struct Linear {
     static constexpr int NP = 1;
     static constexpr bool AUTONOMOUS = true;   // f(u, p) does not read t
     static constexpr bool HAS_EVENT = false;   // no registered callback
-    template <class R, int L, int C>
-    __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>&) {
+    template <class R, int L, int C, class P>
+    __device__ static void rhs(R* du, const R* u, const P* p, double, const Group<L>&) {
 #pragma unroll
         for (int c = 0; c < C; ++c) du[c] = p[0] * u[c];
     }
-    template <class R, int N>
-    __device__ static void jac(R (*J)[N], const R*, const R* p, double) {
+    template <class R, int N, class P>
+    __device__ static void jac(R (*J)[N], const R*, const P* p, double) {
 #pragma unroll
         for (int i = 0; i < N; ++i)
 #pragma unroll
@@ -134,15 +134,15 @@ struct Lorenz {
     static constexpr int NP = 3;
     static constexpr bool AUTONOMOUS = true;   // f(u, p) does not read t
     static constexpr bool HAS_EVENT = false;   // no registered callback
-    template <class R, int L, int C>
-    __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>&) {
+    template <class R, int L, int C, class P>
+    __device__ static void rhs(R* du, const R* u, const P* p, double, const Group<L>&) {
         static_assert(L == 1 && C == 3, "Lorenz has 3 states on one lane");
         du[0] = p[0] * (u[1] - u[0]);
         du[1] = u[0] * (p[1] - u[2]) - u[1];
         du[2] = u[0] * u[1] - p[2] * u[2];
     }
-    template <class R, int N>
-    __device__ static void jac(R (*J)[N], const R* u, const R* p, double) {
+    template <class R, int N, class P>
+    __device__ static void jac(R (*J)[N], const R* u, const P* p, double) {
         J[0][0] = -p[0]; J[0][1] = p[0]; J[0][2] = R(0);
         J[1][0] = p[1] - u[2]; J[1][1] = R(-1); J[1][2] = -u[0];
         J[2][0] = u[1]; J[2][1] = u[0]; J[2][2] = -p[2];
@@ -153,16 +153,16 @@ struct Robertson {
     static constexpr int NP = 3;
     static constexpr bool AUTONOMOUS = true;   // f(u, p) does not read t
     static constexpr bool HAS_EVENT = false;   // no registered callback
-    template <class R, int L, int C>
-    __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>&) {
+    template <class R, int L, int C, class P>
+    __device__ static void rhs(R* du, const R* u, const P* p, double, const Group<L>&) {
         static_assert(L == 1 && C == 3, "Robertson has 3 states on one lane");
         R y1 = u[0], y2 = u[1], y3 = u[2];
         du[0] = -p[0] * y1 + p[2] * y2 * y3;
         du[1] = p[0] * y1 - p[1] * (y2 * y2) - p[2] * y2 * y3;
         du[2] = p[1] * (y2 * y2);
     }
-    template <class R, int N>
-    __device__ static void jac(R (*J)[N], const R* u, const R* p, double) {
+    template <class R, int N, class P>
+    __device__ static void jac(R (*J)[N], const R* u, const P* p, double) {
         R y2 = u[1], y3 = u[2];
         J[0][0] = -p[0]; J[0][1] = p[2] * y3; J[0][2] = p[2] * y2;
         J[1][0] = p[0]; J[1][1] = R(-2) * p[1] * y2 - p[2] * y3; J[1][2] = -p[2] * y2;
@@ -182,8 +182,8 @@ struct Duffing {
     static constexpr int NP = 3;
     static constexpr bool AUTONOMOUS = true;   // f(u, p) does not read t
     static constexpr bool HAS_EVENT = false;   // no registered callback
-    template <class R, int L, int C>
-    __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>& g) {
+    template <class R, int L, int C, class P>
+    __device__ static void rhs(R* du, const R* u, const P* p, double, const Group<L>& g) {
         static_assert(C % 2 == 0, "Duffing lanes hold whole (x, v) pairs");
         R xl, xr;
         chain_halo<R, L, C>(u, g, 0, xl, xr);
@@ -199,8 +199,8 @@ struct Duffing {
             du[2 * q + 1] = (p[0] * lap - p[1] * v) - p[2] * (x * x * x);
         }
     }
-    template <class R, int N>
-    __device__ static void jac(R (*J)[N], const R* u, const R* p, double) {
+    template <class R, int N, class P>
+    __device__ static void jac(R (*J)[N], const R* u, const P* p, double) {
 #pragma unroll
         for (int i = 0; i < N; ++i)
 #pragma unroll
@@ -221,8 +221,8 @@ struct Brusselator {
     static constexpr int NP = 3;
     static constexpr bool AUTONOMOUS = true;   // f(u, p) does not read t
     static constexpr bool HAS_EVENT = false;   // no registered callback
-    template <class R, int L, int C>
-    __device__ static void rhs(R* du, const R* u, const R* p, double, const Group<L>& g) {
+    template <class R, int L, int C, class P>
+    __device__ static void rhs(R* du, const R* u, const P* p, double, const Group<L>& g) {
         static_assert(C % 2 == 0, "Brusselator lanes hold whole (u, v) cells");
         constexpr int NC = L * C / 2;
         R ae = p[2] * (R(NC) * R(NC));
@@ -244,8 +244,8 @@ struct Brusselator {
     // Nonzeros of the lane's own rows (cells lane*C/2 ...) of J(u), in the
     // oracle's arithmetic; put(i, col, v) with i the lane-local row.  The
     // neighbour columns are distinct from the cell's own for 3 cells or more.
-    template <class R, int L, int C, class Put>
-    __device__ static void jac_rows(const R* u, const R* p, const Group<L>& g, Put&& put) {
+    template <class R, int L, int C, class P, class Put>
+    __device__ static void jac_rows(const R* u, const P* p, const Group<L>& g, Put&& put) {
         constexpr int NC = L * C / 2;
         static_assert(NC >= 3, "group Jacobian assumes distinct neighbour cells");
         const R ae = p[2] * (R(NC) * R(NC));

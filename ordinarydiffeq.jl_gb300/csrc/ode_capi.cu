@@ -178,35 +178,45 @@ int grow(ode_handle* h, DevBuf& b, size_t bytes) {
     return ODE_OK;
 }
 
-int validate(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int64_t N) {
-    if (!h || !d || !o) return fail(h, ODE_E_INVALID, "null handle, problem or options");
-    if (N < 0) return fail(h, ODE_E_INVALID, "negative trajectory count");
-    if (d->alg_id < ODE_TSIT5 || d->alg_id >= kNumAlgs) return fail(h, ODE_E_INVALID, "unknown alg_id");
+// Checks of a problem and its options that need no handle, shared by every
+// entry point (the allocation-free one included), so that each rejects the same
+// input with the same status.  Returns ODE_OK or the status, with the reason in *why.
+int check_problem(const ode_problem_desc* d, const ode_options* o, int64_t N, const char** why) {
+    auto bad = [&](int code, const char* msg) { *why = msg; return code; };
+    if (!d || !o) return bad(ODE_E_INVALID, "null problem or options");
+    if (N < 0) return bad(ODE_E_INVALID, "negative trajectory count");
+    if (d->alg_id < ODE_TSIT5 || d->alg_id >= kNumAlgs) return bad(ODE_E_INVALID, "unknown alg_id");
     if (d->model_id < ODE_MODEL_LINEAR || d->model_id > ODE_MODEL_PK_ONE_COMPARTMENT)
-        return fail(h, ODE_E_INVALID, "unknown model_id");
+        return bad(ODE_E_INVALID, "unknown model_id");
     if (d->precision != ODE_PREC_FP64 && d->precision != ODE_PREC_MIXED)
-        return fail(h, ODE_E_INVALID, "unknown precision");
-    if (d->n_states <= 0) return fail(h, ODE_E_INVALID, "n_states must be positive");
-    if (d->n_params != model_nparams(d->model_id))
-        return fail(h, ODE_E_INVALID, "n_params does not match the model");
+        return bad(ODE_E_INVALID, "unknown precision");
+    if (d->n_states <= 0) return bad(ODE_E_INVALID, "n_states must be positive");
+    if (d->n_params != model_nparams(d->model_id)) return bad(ODE_E_INVALID, "n_params does not match the model");
     if ((d->model_id == ODE_MODEL_LORENZ || d->model_id == ODE_MODEL_ROBERTSON) && d->n_states != 3)
-        return fail(h, ODE_E_INVALID, "this model has 3 states");
+        return bad(ODE_E_INVALID, "this model has 3 states");
     if ((d->model_id == ODE_MODEL_BOUNCING_BALL || d->model_id == ODE_MODEL_VANDERPOL ||
          d->model_id == ODE_MODEL_PK_ONE_COMPARTMENT) && d->n_states != 2)
-        return fail(h, ODE_E_INVALID, "this model has 2 states");
+        return bad(ODE_E_INVALID, "this model has 2 states");
     if (o->callback && !model_has_event(d->model_id))
-        return fail(h, ODE_E_UNSUPPORTED, "the model has no registered callback");
+        return bad(ODE_E_UNSUPPORTED, "the model has no registered callback");
     if (o->callback && (o->interp_points < 0 || o->max_events < 0))
-        return fail(h, ODE_E_INVALID, "interp_points and max_events must be >= 0");
-    if (!(o->reltol > 0) || !(o->abstol >= 0)) return fail(h, ODE_E_INVALID, "tolerances must be positive");
-    if (o->nsave < 0) return fail(h, ODE_E_INVALID, "negative nsave");
+        return bad(ODE_E_INVALID, "interp_points and max_events must be >= 0");
+    if (!(o->reltol > 0) || !(o->abstol >= 0)) return bad(ODE_E_INVALID, "tolerances must be positive");
+    if (o->nsave < 0) return bad(ODE_E_INVALID, "negative nsave");
     if (o->save_everystep && o->nsave > 0)
-        return fail(h, ODE_E_UNSUPPORTED, "save_everystep together with saveat is not supported");
+        return bad(ODE_E_UNSUPPORTED, "save_everystep together with saveat is not supported");
     if (o->save_everystep && o->max_step_saves <= 0)
-        return fail(h, ODE_E_INVALID, "save_everystep needs max_step_saves > 0");
+        return bad(ODE_E_INVALID, "save_everystep needs max_step_saves > 0");
     if (o->ntstops < 0 || (o->ntstops > 0 && !o->tstops))
-        return fail(h, ODE_E_INVALID, "ntstops < 0, or tstops is null");
+        return bad(ODE_E_INVALID, "ntstops < 0, or tstops is null");
     return ODE_OK;
+}
+
+int validate(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int64_t N) {
+    if (!h) return fail(h, ODE_E_INVALID, "null handle");
+    const char* why = "";
+    const int rc = check_problem(d, o, N, &why);
+    return rc ? fail(h, rc, why) : ODE_OK;
 }
 
 // The host entry points take tstops in host memory, in any order: checked for
@@ -347,7 +357,6 @@ __global__ void bucket_scatter(const int32_t* npt, long long N, const unsigned l
 // the one-kernel-per-class form.
 constexpr int kCounters = 64;
 constexpr int kOffCounts = 8, kOffCursor = 16, kOffNext = 24, kOffOffsets = 32, kOffClassQ = 40;
-constexpr const int* kClassN = kClassStates;
 
 const FusedVariant* find_fused(int alg, int model, int prec) {
     static const std::vector<FusedVariant> all = [] {
@@ -365,12 +374,37 @@ const FusedVariant* find_fused(int alg, int model, int prec) {
 }
 
 // Count + scatter of an uneven ensemble into class order (device only).
+void enqueue_count(const int32_t* npt_dev, long long N, unsigned long long* ctr, cudaStream_t s) {
+    bucket_count<<<(int)((N + 255) / 256), 256, 0, s>>>(npt_dev, N, ctr + kOffCounts);
+}
+void enqueue_scatter(const int32_t* npt_dev, long long N, unsigned long long* ctr, long long* order,
+                     int32_t* nsaved, int32_t* retcode, cudaStream_t s) {
+    bucket_scatter<<<(int)((N + 255) / 256), 256, 0, s>>>(npt_dev, N, ctr + kOffCounts, ctr + kOffCursor,
+                                                          ctr + kOffOffsets, order, nsaved, retcode);
+}
 void enqueue_bucketing(const int32_t* npt_dev, long long N, unsigned long long* ctr, long long* order,
                        int32_t* nsaved, int32_t* retcode, cudaStream_t s) {
-    const int gb = (int)((N + 255) / 256);
-    bucket_count<<<gb, 256, 0, s>>>(npt_dev, N, ctr + kOffCounts);
-    bucket_scatter<<<gb, 256, 0, s>>>(npt_dev, N, ctr + kOffCounts, ctr + kOffCursor, ctr + kOffOffsets, order,
-                                      nsaved, retcode);
+    enqueue_count(npt_dev, N, ctr, s);
+    enqueue_scatter(npt_dev, N, ctr, order, nsaved, retcode, s);
+}
+
+// The one-kernel-per-class form needs a compiled kernel for every size class
+// present (hc: the class counts read back); a missing one fails the solve
+// before the scatter, i.e. before anything is written to the outputs.
+int class_kernels(ode_handle* h, const ode_problem_desc* d, const unsigned long long* hc,
+                  const KernelVariant** vk) {
+    for (int k = 0; k < kNumClasses; ++k) {
+        vk[k] = nullptr;
+        if (hc[k] == 0) continue;
+        vk[k] = find_variant(d->alg_id, d->model_id, d->precision, kClassStates[k], 0);
+        if (!vk[k]) {
+            char buf[160];
+            std::snprintf(buf, sizeof buf, "no compiled kernel for alg %d on the %d-state Duffing size class",
+                          d->alg_id, kClassStates[k]);
+            return fail(h, ODE_E_UNSUPPORTED, buf);
+        }
+    }
+    return ODE_OK;
 }
 
 // Every size class in one persistent launch (grid = resident blocks x SMs).
@@ -540,29 +574,33 @@ int enqueue_plan(ode_handle* h, Ctx& c, const Plan& pl, EnsembleArgs a, const in
 }
 
 // Uneven sizes without a fused kernel: one persistent kernel per size class on
-// the class streams (the counts are read back to size the launches).
+// the class streams (the counts are read back to size the launches and to check
+// that every class present has a kernel before anything is written).
 int run_per_class(ode_handle* h, Ctx& c, const ode_problem_desc* d, const ode_options* o, const Plan& pl,
                   EnsembleArgs a, const int32_t* npt_dev, cudaStream_t s) {
     unsigned long long* ctr = c.d_queue;
     CUDA_TRY(h, cudaMemsetAsync(ctr + kOffCounts, 0, (kCounters - kOffCounts) * sizeof(unsigned long long), s));
-    enqueue_bucketing(npt_dev, a.count, ctr, c.d_order, a.nsaved, a.retcode, s);
-    h->launches += 2;
+    enqueue_count(npt_dev, a.count, ctr, s);
+    h->launches += 1;
     unsigned long long hc[kNumClasses + 1] = {0};
     CUDA_TRY(h, cudaMemcpyAsync(hc, ctr + kOffCounts, sizeof(hc), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(h, cudaStreamSynchronize(s));
+    const KernelVariant* vk[kNumClasses];
+    int rc = class_kernels(h, d, hc, vk);
+    if (rc) return rc;
+    enqueue_scatter(npt_dev, a.count, ctr, c.d_order, a.nsaved, a.retcode, s);
+    h->launches += 1;
     unsigned long long off[kNumClasses];
     unsigned long long acc = 0;
     for (int k = 0; k < kNumClasses; ++k) { off[k] = acc; acc += hc[k]; }
     CUDA_TRY(h, cudaEventRecord(c.ev0, s));
     for (int k = 0; k < kNumClasses; ++k) {
         if (hc[k] == 0) continue;
-        const KernelVariant* v = find_variant(d->alg_id, d->model_id, d->precision, kClassN[k], 0);
-        if (!v) return fail(h, ODE_E_UNSUPPORTED, "no compiled kernel for a Duffing size class");
         CUDA_TRY(h, cudaStreamWaitEvent(c.class_streams[k], c.ev0, 0));
         EnsembleArgs ac = a;
         ac.order = c.d_order + off[k];
         ac.count = (long long)hc[k];
-        int rc = launch_variant(h, v, ac, pl.scheduler, o->block_size, ctr + kOffClassQ + k, c.class_streams[k]);
+        rc = launch_variant(h, vk[k], ac, pl.scheduler, o->block_size, ctr + kOffClassQ + k, c.class_streams[k]);
         if (rc) return rc;
         CUDA_TRY(h, cudaEventRecord(c.class_events[k], c.class_streams[k]));
         CUDA_TRY(h, cudaStreamWaitEvent(s, c.class_events[k], 0));
@@ -1552,21 +1590,62 @@ constexpr long long kNoAllocMaxTraj = 1LL << 20;
 static __device__ __align__(256) unsigned long long g_noalloc_scratch[kCounters + kNoAllocMaxTraj];
 
 std::mutex g_noalloc_mu;
-unsigned long long* g_noalloc_ptr[64] = {};
+struct NoallocCache {
+    unsigned long long ctx_id = 0;   // the context the address was resolved in (0: none yet)
+    unsigned long long* ptr = nullptr;
+};
+NoallocCache g_noalloc_cache[64];
 
-// Device address of the scratch for the current device, resolved once per
-// device (with that device current) and cached.
+// Identity of the current context (cuCtxGetCurrent + cuCtxGetId, reached through
+// the runtime's driver entry points so the library needs no link to libcuda).
+// A device reset in the caller's process destroys the primary context; the next
+// one gets a new id, so the cached address is resolved again there.
+int current_context_id(unsigned long long* id) {
+    typedef int (*GetCurrent)(void**);
+    typedef int (*GetId)(void*, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    if (!get_current || !get_id) {
+        void* f0 = nullptr;
+        void* f1 = nullptr;
+        cudaDriverEntryPointQueryResult q0, q1;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0);
+        if (e == cudaSuccess)
+            e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1);
+        if (e != cudaSuccess || !f0 || !f1 || q0 != cudaDriverEntryPointSuccess || q1 != cudaDriverEntryPointSuccess)
+            return fail(nullptr, ODE_E_CUDA, "driver entry points cuCtxGetCurrent/cuCtxGetId not found");
+        get_current = (GetCurrent)f0;
+        get_id = (GetId)f1;
+    }
+    void* ctx = nullptr;
+    if (get_current(&ctx) != 0 || ctx == nullptr || get_id(ctx, id) != 0)
+        return fail(nullptr, ODE_E_CUDA, "no current CUDA context");
+    return ODE_OK;
+}
+
+// Device address of the scratch for the current device, resolved with that
+// device current and cached per device; resolved again when the device's
+// context changed since (after a cudaDeviceReset).  cudaSetDevice on the
+// current device makes its primary context current (initialising it if needed)
+// and allocates nothing.
 int noalloc_scratch(int dev, unsigned long long** out) {
     if (dev < 0 || dev >= 64) return fail(nullptr, ODE_E_INVALID, "device ordinal out of range");
+    cudaError_t e = cudaSetDevice(dev);
+    if (e != cudaSuccess) return fail(nullptr, ODE_E_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    unsigned long long id = 0;
+    int rc = current_context_id(&id);
+    if (rc) return rc;
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    NoallocCache& c = g_noalloc_cache[dev];
+    if (!c.ptr || c.ctx_id != id) {
         void* ptr = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
         if (e != cudaSuccess || ptr == nullptr)
             return fail(nullptr, ODE_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        g_noalloc_ptr[dev] = (unsigned long long*)ptr;
+        c.ptr = (unsigned long long*)ptr;
+        c.ctx_id = id;
     }
-    *out = g_noalloc_ptr[dev];
+    *out = c.ptr;
     return ODE_OK;
 }
 
@@ -1598,8 +1677,9 @@ extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_o
                                           const double* tspan, const double* saveat, double* t_out,
                                           double* u_out, int32_t* nsaved, int32_t* retcode, ode_stats* stats,
                                           void* cuda_stream) {
-    if (!d || !o) return fail(nullptr, ODE_E_INVALID, "null problem or options");
-    if (N < 0) return fail(nullptr, ODE_E_INVALID, "negative trajectory count");
+    const char* why = "";
+    int rc = check_problem(d, o, N, &why);
+    if (rc) return fail(nullptr, rc, why);
     if (npt_dev && N > kNoAllocMaxTraj) {
         char buf[160];
         std::snprintf(buf, sizeof buf,
@@ -1608,14 +1688,6 @@ extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_o
                       (long long)N, (long long)kNoAllocMaxTraj);
         return fail(nullptr, ODE_E_INVALID, buf);
     }
-    if (d->alg_id < ODE_TSIT5 || d->alg_id >= kNumAlgs ||
-        (d->precision != ODE_PREC_FP64 && d->precision != ODE_PREC_MIXED) ||
-        d->model_id < ODE_MODEL_LINEAR || d->model_id > ODE_MODEL_PK_ONE_COMPARTMENT || d->n_states <= 0 ||
-        (o->callback && !model_has_event(d->model_id)) ||
-        d->n_params != model_nparams(d->model_id) || !(o->reltol > 0) || !(o->abstol >= 0) || o->nsave < 0 ||
-        (o->save_everystep && (o->nsave > 0 || o->max_step_saves <= 0)) ||
-        o->ntstops < 0 || (o->ntstops > 0 && !o->tstops))
-        return fail(nullptr, ODE_E_INVALID, "invalid problem description or options");
     if (npt_dev && d->model_id != ODE_MODEL_DUFFING_CHAIN)
         return fail(nullptr, ODE_E_UNSUPPORTED, "per-trajectory sizes are supported for DUFFING_CHAIN");
     if (N > 0 && (!u0 || !p || !tspan || !u_out || !nsaved || !retcode))
@@ -1627,7 +1699,7 @@ extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_o
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return fail(nullptr, ODE_E_CUDA, std::string("device query: ") + cudaGetErrorString(e));
     unsigned long long* scratch = nullptr;
-    int rc = noalloc_scratch(dev, &scratch);
+    rc = noalloc_scratch(dev, &scratch);
     if (rc) return rc;
     cudaStream_t s = (cudaStream_t)cuda_stream;
 
@@ -1678,28 +1750,34 @@ extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_o
         return noalloc_launch(v, a, scratch, sm_count, s);
     }
     long long* order = (long long*)(scratch + kCounters);
-    enqueue_bucketing(npt_dev, N, scratch, order, nsaved, retcode, s);
-    a.order = order;
     if (const FusedVariant* fv = find_fused(d->alg_id, d->model_id, d->precision)) {
+        enqueue_bucketing(npt_dev, N, scratch, order, nsaved, retcode, s);
+        a.order = order;
         e = launch_fused(fv, a, scratch, sm_count, s);
         if (e != cudaSuccess) return fail(nullptr, ODE_E_CUDA, std::string("launch ") + fv->name + ": " + cudaGetErrorString(e));
         return ODE_OK;
     }
+    // one kernel per size class: the counts first, a kernel for every class
+    // present, and only then the scatter (which writes the outputs of
+    // trajectories of no class) and the launches
+    enqueue_count(npt_dev, N, scratch, s);
     unsigned long long hc[kNumClasses + 1] = {0};
     e = cudaMemcpyAsync(hc, scratch + kOffCounts, sizeof(hc), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return fail(nullptr, ODE_E_CUDA, std::string("bucket counts: ") + cudaGetErrorString(e));
+    const KernelVariant* vk[kNumClasses];
+    if ((rc = class_kernels(nullptr, d, hc, vk))) return rc;
+    enqueue_scatter(npt_dev, N, scratch, order, nsaved, retcode, s);
+    a.order = order;
     unsigned long long off[kNumClasses] = {0};
     unsigned long long acc = 0;
     for (int k = 0; k < kNumClasses; ++k) { off[k] = acc; acc += hc[k]; }
     for (int k = 0; k < kNumClasses; ++k) {
         if (hc[k] == 0) continue;
-        const KernelVariant* v = find_variant(d->alg_id, d->model_id, d->precision, kClassN[k], 0);
-        if (!v) return fail(nullptr, ODE_E_UNSUPPORTED, "no compiled kernel for a Duffing size class");
         EnsembleArgs ac = a;
         ac.order = order + off[k];
         ac.count = (long long)hc[k];
-        rc = noalloc_launch(v, ac, scratch + kOffClassQ + k, sm_count, s);
+        rc = noalloc_launch(vk[k], ac, scratch + kOffClassQ + k, sm_count, s);
         if (rc) return rc;
     }
     return ODE_OK;

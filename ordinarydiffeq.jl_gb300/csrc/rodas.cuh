@@ -95,7 +95,7 @@ __device__ __forceinline__ void lu_solve_reg(const R (*LU)[N], const int* piv, R
 // state (hi + lo) and the parameters are lifted to double-float, f runs in
 // double-float, and the result is rounded to FP32.
 template <class Model, class R, int L, int C, int NP>
-__device__ __forceinline__ void rhs_stage(R* du, const R* u, const R* ulo, const R* p, const ff* pff, double t,
+__device__ __forceinline__ void rhs_stage(R* du, const R* u, const R* ulo, const PR<R>* p, const ff* pff, double t,
                                           const Group<L>& g) {
     if (sizeof(R) == 8) {
         Model::template rhs<R, L, C>(du, u, p, t, g);
@@ -122,7 +122,7 @@ struct RegLA {
     }
     // J(uprev); kept across a rejected step (fresh = false)
     template <class Model, class R, int L, int C>
-    __device__ static void jacobian(Store<R, C>& s, const R* up, const R* p, double t, bool fresh, const Group<L>&) {
+    __device__ static void jacobian(Store<R, C>& s, const R* up, const PR<R>* p, double t, bool fresh, const Group<L>&) {
         if (fresh) Model::template jac<R, C>(s.J, up, p, t);
     }
     // W = J - I/(dt*gamma), factorised in place
@@ -196,7 +196,7 @@ struct Rodas5PT {
     }
     template <class R, int C> __device__ static R* fsal_slot(Cache<R, C>& c) { return c.scratch; }
     template <class Model, class R, int L, int C>
-    __device__ static void initialize(Cache<R, C>& c, const R*, const R*, double, const Group<L>& g, StepStats&,
+    __device__ static void initialize(Cache<R, C>& c, const R*, const PR<R>*, double, const Group<L>& g, StepStats&,
                                       const EnsembleArgs& a, long long j) {
         LA::template init<R, L, C>(c.la, g);
         c.haveJ = false;
@@ -211,7 +211,7 @@ struct Rodas5PT {
 
     template <class Model, class R, int L, int C>
     __device__ static typename Ctl<R>::T step(Cache<R, C>& c, R* u, R* ulo, const R* up, const R* uplo,
-                                             const R* p, double t, double dt, R abstol, R reltol, long long iter,
+                                             const PR<R>* p, double t, double dt, R abstol, R reltol, long long iter,
                                              bool errorfail, const Group<L>& g, StepStats& st) {
         constexpr int NP = Model::NP;
         // dt-derived coefficients: FP64 like the reference; in the mixed mode they
@@ -339,12 +339,12 @@ struct Rodas5PT {
 
     // not FSAL (isfsal(::Rodas5P) = false, alg_utils.jl:60): f(uprev) is formed every step
     template <class Model, class R, int L, int C>
-    __device__ static void reset_fsal(Cache<R, C>&, const R*, const R*, const R*, double, const Group<L>&,
+    __device__ static void reset_fsal(Cache<R, C>&, const R*, const R*, const PR<R>*, double, const Group<L>&,
                                       StepStats&) {}
 
     template <class Model, class R, int L, int C>
     __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, double th, double, double,
-                                       const R* y0, const R* y0lo, const R* y1, const R* y1lo, const R*,
+                                       const R* y0, const R* y0lo, const R* y1, const R* y1lo, const PR<R>*,
                                        const Group<L>&) {
         dense<R, C>(c);
         interp_dense<R, C>(c, out, outlo, th, y0, y0lo, y1, y1lo);

@@ -56,7 +56,7 @@ struct Rosenbrock23T {
         }
     }
     template <class Model, class R, int L, int C>
-    __device__ static void initialize(Cache<R, C>& c, const R* u, const R* p, double t, const Group<L>& g,
+    __device__ static void initialize(Cache<R, C>& c, const R* u, const PR<R>* p, double t, const Group<L>& g,
                                       StepStats& st, const EnsembleArgs& a, long long j) {
         prepare<Model, R, L, C>(c, g, a, j);
         R zero[C];
@@ -87,7 +87,7 @@ struct Rosenbrock23T {
     // A callback moved or modified u: f(u) again (reset_fsal!, one counted call);
     // fsallast becomes the next step's FSAL value when it starts.
     template <class Model, class R, int L, int C>
-    __device__ static void reset_fsal(Cache<R, C>& c, const R* u, const R* ulo, const R* p, double t,
+    __device__ static void reset_fsal(Cache<R, C>& c, const R* u, const R* ulo, const PR<R>* p, double t,
                                       const Group<L>& g, StepStats& st) {
         rhs_stage<Model, R, L, C, Model::NP>(c.fsallast, u, ulo, p, c.pff, t, g);
         st.nf += 1;
@@ -95,7 +95,7 @@ struct Rosenbrock23T {
 
     template <class Model, class R, int L, int C>
     __device__ static typename Ctl<R>::T step(Cache<R, C>& c, R* u, R* ulo, const R* up, const R* uplo,
-                                             const R* p, double t, double dt, R abstol, R reltol, long long,
+                                             const PR<R>* p, double t, double dt, R abstol, R reltol, long long,
                                              bool, const Group<L>& g, StepStats& st) {
         constexpr int NP = Model::NP;
         R dr, idg, ninv, dto2, dto6, c32;
@@ -164,7 +164,7 @@ struct Rosenbrock23T {
     // y0 + dt (c1 k1 + c2 k2), c1 = th (1 - th) / (1 - 2d), c2 = th (th - 2d) / (1 - 2d)
     template <class Model, class R, int L, int C>
     __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, double th, double dt, double,
-                                       const R* y0, const R* y0lo, const R*, const R*, const R*,
+                                       const R* y0, const R* y0lo, const R*, const R*, const PR<R>*,
                                        const Group<L>&) {
         const double thd = th;
         const double d = tab::ROS23_D;

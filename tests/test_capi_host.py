@@ -66,6 +66,26 @@ def test_tstops_count_without_array_is_rejected_before_any_device_work():
     assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == -1
 
 
+def test_noalloc_applies_the_shared_problem_checks():
+    # ode_solve_ensemble_noalloc and the handle entry points run the same checks, so
+    # both reject the same input with the same status (ODE_E_INVALID = -1) on the host
+    L = _lib.load()
+    o = _lib.Options()
+    L.ode_options_default(C.byref(o))
+    d = _lib.ProblemDesc(_lib.MODEL_BOUNCING_BALL, _lib.ODE_TSIT5, 2, 3, _lib.PREC_FP64, 0)
+    o.callback = 1
+    o.max_events = -1   # would size the save slots negatively
+    assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == -1
+    assert b"max_events" in L.ode_last_error(None)
+    o.max_events = 4
+    o.interp_points = -2
+    assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == -1
+    L.ode_options_default(C.byref(o))
+    d = _lib.ProblemDesc(_lib.MODEL_LORENZ, _lib.ODE_TSIT5, 4, 3, _lib.PREC_FP64, 0)   # Lorenz has 3 states
+    assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == -1
+    assert b"3 states" in L.ode_last_error(None)
+
+
 def test_variant_registry_covers_the_workloads():
     L = _lib.load()
     buf = (C.c_int32 * 8)()

@@ -105,6 +105,48 @@ def test_duffing_mixed(alg, n_osc):
     assert_equal_accuracy(g, g64, tr, 1e-6, 1e-6)
 
 
+def assert_within_conditioning(g, u0, p, ts, sv, reltol, abstol, npt=None, alg="vern7"):
+    """The mixed form against the FP64 oracle, next to a conditioning control: the
+    FP64 kernel on u0 perturbed by one FP32 rounding (1 + 2^-24) against the same
+    oracle.  The mixed form's spread may not exceed the control's by more than 2x
+    (+1 tolerance unit) at the median, p90 and p99, and 90% of its trajectories
+    stay within 10x the tolerance."""
+    o = oracle("duffing_chain", alg, u0, p, ts, sv, reltol, abstol, n_per_traj=npt)
+    kw = {"n_per_traj": npt} if npt is not None else {}
+    ctl = gpu("duffing_chain", alg, u0 * (1.0 + 2.0 ** -24), p, ts, sv, reltol, abstol, **kw)
+    d, dc = err_vs(g, o, reltol, abstol), err_vs(ctl, o, reltol, abstol)
+    for q in (50, 90, 99):
+        a, b = np.percentile(d, q), np.percentile(dc, q)
+        assert a <= 2.0 * b + 1.0, (q, a, b)
+    assert np.mean(d <= 10.0) >= 0.9, np.sort(d)[-10:]
+    return d, dc
+
+
+@pytest.mark.parametrize("n_osc", [8, 32])
+def test_duffing_mixed_vern7_long_spans(n_osc):
+    # the C3 distribution's long half: tf log-uniform in [1, 100] (step counts vary ~50x)
+    N = 512
+    u0, p, ts, sv, _ = duffing_inputs(N, n_osc, seed=21, tf_range=(1.0, 100.0))
+    g = gpu("duffing_chain", "vern7", u0, p, ts, sv, 1e-6, 1e-6, precision="mixed")
+    assert (g["retcode"] == 1).all()
+    assert_within_conditioning(g, u0, p, ts, sv, 1e-6, 1e-6)
+    g64 = gpu("duffing_chain", "vern7", u0, p, ts, sv, 1e-6, 1e-6)
+    tr = truth("duffing_chain", u0, p, ts, sv)
+    assert_equal_accuracy(g, g64, tr, 1e-6, 1e-6)
+
+
+def test_duffing_uneven_mixed_one_launch_against_oracle():
+    # the one-launch mixed kernel over every size class, tf up to 100, against the FP64 oracle
+    N = 2048
+    u0, p, ts, sv, npt = duffing_inputs(N, [2, 4, 8, 16, 32], seed=31, tf_range=(1.0, 100.0))
+    g = gpu("duffing_chain", "vern7", u0, p, ts, sv, 1e-6, 1e-6, precision="mixed", n_per_traj=npt)
+    assert (g["retcode"] == 1).all()
+    assert_within_conditioning(g, u0, p, ts, sv, 1e-6, 1e-6, npt=npt)
+    g64 = gpu("duffing_chain", "vern7", u0, p, ts, sv, 1e-6, 1e-6, n_per_traj=npt)
+    tr = truth("duffing_chain", u0, p, ts, sv, n_per_traj=npt)
+    assert_equal_accuracy(g, g64, tr, 1e-6, 1e-6)
+
+
 @pytest.mark.parametrize("cells", [8, 16, 32])
 def test_brusselator_rodas5p_fp64_shared_memory_lu(cells):
     # 16 to 64 states: one lane group per trajectory, W and its LU in shared memory

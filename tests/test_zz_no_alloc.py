@@ -96,6 +96,52 @@ def test_noalloc_uniform_matches_device_entry():
         assert np.array_equal(got["u"], ref["u"], equal_nan=True)
 
 
+@pytest.mark.parametrize("alg", ["rodas5p", "rosenbrock23"])
+def test_noalloc_per_class_kernels_match_device_entry(alg):
+    # methods without a one-launch class kernel run one kernel per size class,
+    # from per-class queues inside the fixed array
+    from odegb300 import _lib
+    alg_id = {"rodas5p": _lib.ODE_RODAS5P, "rosenbrock23": _lib.ODE_ROSENBROCK23}[alg]
+    N = 500
+    u0, p, ts, sv, npt = duffing_inputs(N, 2, seed=13, tf_range=(1.0, 10.0))
+    ref = _device_solve("device", _lib.MODEL_DUFFING_CHAIN, alg_id, "fp64", u0, p, ts, sv, 1e-6, 1e-6, npt)
+    for _ in range(2):
+        got = _device_solve("noalloc", _lib.MODEL_DUFFING_CHAIN, alg_id, "fp64", u0, p, ts, sv, 1e-6, 1e-6, npt)
+        assert np.array_equal(got["u"], ref["u"], equal_nan=True)
+        assert np.array_equal(got["nsaved"], ref["nsaved"]) and (got["retcode"] == 1).all()
+        assert np.array_equal(got["stats"]["naccept"], ref["stats"]["naccept"])
+
+
+def test_noalloc_size_class_without_kernel_is_rejected_before_outputs_are_written():
+    # Rodas5P is compiled for 4-state Duffing chains only: an ensemble with
+    # 8-state chains fails with ODE_E_UNSUPPORTED (-4), and the outputs keep the
+    # caller's contents (nothing was scattered or integrated)
+    import torch
+    from odegb300 import _lib
+    from odegb300.ensemble import EnsembleGB300, _options
+    from odegb300.saveat import resolve_saveat
+    L = _lib.load()
+    dev = torch.device("cuda", 0)
+    N = 64
+    u0, p, ts, sv, npt = duffing_inputs(N, [2, 4], seed=3, tf_range=(1.0, 2.0))
+    s = resolve_saveat(sv, ts)
+    o = _options(1e-6, 1e-6, None, None, None, 1000000, s, EnsembleGB300(), None, None)
+    d = _lib.ProblemDesc(_lib.MODEL_DUFFING_CHAIN, _lib.ODE_RODAS5P, u0.shape[0], 3, 0, 0)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    b_u0, b_p, b_ts, b_sv, b_npt = t(u0), t(p), t(ts), t(s.values), t(npt)
+    u_out = torch.full((s.cap, u0.shape[0], N), 7.0, dtype=torch.float64, device=dev)
+    ns = torch.full((N,), -5, dtype=torch.int32, device=dev)
+    rc = torch.full((N,), -5, dtype=torch.int32, device=dev)
+    ptr = lambda x: C.c_void_p(x.data_ptr())
+    status = L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), N, ptr(b_npt), ptr(b_u0), ptr(b_p), ptr(b_ts),
+                                          ptr(b_sv), None, ptr(u_out), ptr(ns), ptr(rc), None, None)
+    torch.cuda.synchronize()
+    assert status == -4, status
+    assert b"8-state" in L.ode_last_error(None)
+    assert (ns.cpu().numpy() == -5).all() and (rc.cpu().numpy() == -5).all()
+    assert (u_out.cpu().numpy() == 7.0).all()
+
+
 def test_noalloc_rejects_oversized_bucketed_request():
     from odegb300 import _lib
     L = _lib.load()
