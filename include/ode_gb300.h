@@ -66,10 +66,26 @@ enum ode_model {
                                      DiscreteCallback (ode_options.callback): condition t in tstops
                                      (the dose times, passed as the solve's tstops), affect!:
                                      depot += dose; save_positions = (true, true) */
-    ODE_MODEL_BOUNCING_BALL = 5   /* n = 2 (x, v): x' = v, v' = -g; p = (g, e, t_stop).  Its
+    ODE_MODEL_BOUNCING_BALL = 5,  /* n = 2 (x, v): x' = v, v' = -g; p = (g, e, t_stop).  Its
                                      ContinuousCallback (ode_options.callback): condition x,
                                      affect! = nothing, affect_neg!: terminate! once t >= t_stop,
                                      else v <- -e v (test/Integrators_I/ode_event_tests.jl:100-113,283-360) */
+    ODE_MODEL_FORCED_DUFFING = 8  /* n = 2 (x, v), non-autonomous: x' = v,
+                                     v' = ((g cos(w t) - delta v) - alpha x) - beta x^3;
+                                     p = (delta, alpha, beta, g, w); analytic J and tgrad (df/dt, which
+                                     the Rosenbrock methods use: derivative_utils.jl:181-227) */
+};
+
+/* Models registered at run time (ode_register_model) take ids from
+ * ODE_MODEL_USER_BASE up, in registration order. */
+#define ODE_MODEL_USER_BASE 1000
+
+/* Flags of ode_register_model. */
+enum ode_model_flags {
+    ODE_MODEL_HAS_JAC = 1,        /* the source defines NAME_jac (else the Rosenbrock methods take J by
+                                     forward-mode AD of NAME_f, one counted f call per Jacobian) */
+    ODE_MODEL_HAS_TGRAD = 2,      /* the source defines NAME_tgrad, df/dt */
+    ODE_MODEL_NONAUTONOMOUS = 4   /* NAME_f reads t (the Rosenbrock methods then need NAME_tgrad) */
 };
 
 /* FP64: every operation in double (the reference's arithmetic).
@@ -153,6 +169,26 @@ void ode_options_default(ode_options* o);
  * mirror the structs (Julia, Python) check their layout against these. */
 size_t ode_options_size(void);
 size_t ode_problem_desc_size(void);
+
+/* Register a right-hand side given as CUDA C++ source, the device form of the
+ * reference's f(du, u, p, t) with its optional jac and tgrad (ODEFunction; the
+ * solve entry lib/DiffEqBase/src/solve.jl:155-192 takes any user function).
+ * For a model named NAME (a C identifier) the source defines
+ *   template <class T, class P> __device__ void NAME_f(T* du, const T* u, const P* p, double t);
+ *   template <class T, class P> __device__ void NAME_jac(T* J, const T* u, const P* p, double t);   (optional,
+ *                                                                        row-major J[i*n + j] = df_i/du_j)
+ *   template <class T, class P> __device__ void NAME_tgrad(T* dT, const T* u, const P* p, double t); (optional)
+ * written for any arithmetic T and parameter type P (FP64 solves use double;
+ * mixed solves a float, a double-float pair or a dual number) with +, -, *, /
+ * and exp, log, sqrt, sin, cos, tanh, pow, fabs.  n_states: 1..32 (at most 8 for
+ * Rodas5P, Rosenbrock23 and AutoTsit5(Rosenbrock23())); n_params: 0..32.
+ * Returns the new model id (>= ODE_MODEL_USER_BASE) for ode_problem_desc.
+ * Kernels are compiled with NVRTC on the first solve of each (method,
+ * precision) and kept until the process exits; a compile error fails that solve
+ * with ODE_E_UNSUPPORTED and the compiler log in ode_last_error.  Uniform sizes
+ * only (no n_per_traj), no callback. */
+int ode_register_model(const char* source, const char* name, int32_t n_states, int32_t n_params, int32_t flags,
+                       int32_t* model_id);
 
 /* Open device `device`; hbm_budget bytes caps device memory the handle may
  * hold (0: 90% of free memory).  One CUDA stream per handle. */

@@ -97,9 +97,32 @@ double ctrl_pow(double x, double y) {
 // Linear: u_i' = p0 * u_i (prob_ode_linear with p0 = 1.01, test/Regression_I/ode_dense_tests.jl:30-38).
 // Bouncing ball: x' = v, v' = -g (p = (g, e, t_stop); test/Integrators_I/ode_event_tests.jl:100-104),
 //   with its event below.
+// Forced Duffing (non-autonomous, defined by this build's tests): x' = v,
+//   v' = ((g cos(w t) - delta v) - alpha x) - beta x^3, p = (delta, alpha, beta, g, w),
+//   with the analytic time derivative (tgrad) below.
+// Two models that the library does not compile in, for the tests of models
+// registered at run time (the GPU side gets them as source through
+// ode_register_model):
+//   Lotka-Volterra, benchmark/benchmarks.jl:13-26: x' = a x - b x y,
+//     y' = d x y - c y, p = (a, b, c, d);
+//   the Oregonator (Field-Koros-Noyes, the stiff test problem of Hairer and
+//     Wanner's "Solving ODEs II", sec. IV.10): y1' = s (y2 + y1 (1 - q y1 - y2)),
+//     y2' = (y3 - (1 + y1) y2) / s, y3' = w (y1 - y3), p = (s, w, q).
 void rhs(int model, int n, const double* u, const double* p, double t, double* du) {
-    (void)t;
     switch (model) {
+    case ORC_LOTKA_VOLTERRA:
+        du[0] = p[0] * u[0] - p[1] * u[0] * u[1];
+        du[1] = p[3] * u[0] * u[1] - p[2] * u[1];
+        break;
+    case ORC_OREGONATOR:
+        du[0] = p[0] * (u[1] + u[0] * (1.0 - p[2] * u[0] - u[1]));
+        du[1] = (u[2] - (1.0 + u[0]) * u[1]) / p[0];
+        du[2] = p[1] * (u[0] - u[2]);
+        break;
+    case ORC_FORCED_DUFFING:
+        du[0] = u[1];
+        du[1] = ((p[3] * std::cos(p[4] * t) - p[0] * u[1]) - p[1] * u[0]) - p[2] * (u[0] * u[0] * u[0]);
+        break;
     case ORC_BOUNCING_BALL:
         du[0] = u[1];
         du[1] = -p[0];
@@ -161,6 +184,20 @@ void jac(int model, int n, const double* u, const double* p, double t, double* J
     (void)t;
     std::memset(J, 0, sizeof(double) * n * n);
     switch (model) {
+    case ORC_LOTKA_VOLTERRA:
+        J[0] = p[0] - p[1] * u[1]; J[1] = -p[1] * u[0];
+        J[2] = p[3] * u[1];        J[3] = p[3] * u[0] - p[2];
+        break;
+    case ORC_OREGONATOR:
+        J[0] = p[0] * (1.0 - 2.0 * p[2] * u[0] - u[1]); J[1] = p[0] * (1.0 - u[0]); J[2] = 0.0;
+        J[3] = -u[1] / p[0]; J[4] = -(1.0 + u[0]) / p[0]; J[5] = 1.0 / p[0];
+        J[6] = p[1]; J[7] = 0.0; J[8] = -p[1];
+        break;
+    case ORC_FORCED_DUFFING:
+        J[1] = 1.0;
+        J[2] = -p[1] - p[2] * (3.0 * (u[0] * u[0]));
+        J[3] = -p[0];
+        break;
     case ORC_BOUNCING_BALL:
         J[1] = 1.0;
         break;
@@ -221,6 +258,17 @@ void jac(int model, int n, const double* u, const double* p, double t, double* J
         break;
     }
     }
+}
+
+// Analytic time derivative df/dt (ODEFunction's tgrad) of the non-autonomous
+// models; false for the others (autonomous: the reference differentiates f in t
+// by AD, one counted f call, and gets 0).
+bool tgrad(int model, int n, const double* u, const double* p, double t, double* dT) {
+    (void)u;
+    if (model != ORC_FORCED_DUFFING) return false;
+    std::fill(dT, dT + n, 0.0);
+    dT[1] = -(p[3] * p[4]) * std::sin(p[4] * t);
+    return true;
 }
 
 // ---------------------------------------------------------------- integrator
@@ -595,11 +643,14 @@ void rodas5p_step(Integ& I) {
     if (new_jac) {
         jac(I.model, n, up, I.p, t, I.J.data());
         I.st.njacs += 1;
-        // The reference differentiates f in t by AD (one counted call); every
-        // model here is autonomous, so the derivative is exactly zero.
-        f_eval(I, up, t, I.du.data());
-        std::fill(I.dT.begin(), I.dT.end(), 0.0);
-        I.st.nf += 1;
+        // calc_tderivative! (derivative_utils.jl:181-227), with a fresh J only
+        // (:1040): the model's tgrad, else the reference differentiates f in t by
+        // AD (one counted call), exactly zero for the autonomous models here.
+        if (!tgrad(I.model, n, up, I.p, t, I.dT.data())) {
+            f_eval(I, up, t, I.du.data());
+            std::fill(I.dT.begin(), I.dT.end(), 0.0);
+            I.st.nf += 1;
+        }
         I.have_J = true;
     }
     double invdtgamma = 1.0 / dtgamma;
@@ -681,10 +732,13 @@ void rosenbrock23_step(Integ& I) {
     const double dto2 = dt / 2.0, dto6 = dt / 6.0;
     jac(I.model, n, up, I.p, t, I.J.data());
     I.st.njacs += 1;
-    // the reference differentiates f in t by AD (one counted call); autonomous models: dT = 0
-    f_eval(I, up, t, I.du.data());
-    std::fill(I.dT.begin(), I.dT.end(), 0.0);
-    I.st.nf += 1;
+    // the model's tgrad, else the reference differentiates f in t by AD (one counted
+    // call; autonomous models: dT = 0)
+    if (!tgrad(I.model, n, up, I.p, t, I.dT.data())) {
+        f_eval(I, up, t, I.du.data());
+        std::fill(I.dT.begin(), I.dT.end(), 0.0);
+        I.st.nf += 1;
+    }
     const double invdtgamma = 1.0 / dtgamma;
     for (int i = 0; i < n * n; ++i) I.W[i] = I.J[i];
     for (int i = 0; i < n; ++i) I.W[i * n + i] = std::fma(-1.0, invdtgamma, I.J[i * n + i]);
@@ -696,7 +750,8 @@ void rosenbrock23_step(Integ& I) {
     double* k2 = k1 + n;
     double* k3 = k1 + 2 * n;
     double* f1 = k1 + 3 * n;
-    for (int i = 0; i < n; ++i) r[i] = std::fma(dtgamma, I.dT[i], fsal0[i]);   // fsalfirst + dtd1 dT
+    // fsalfirst + dtd1 dT: calc_tderivative! is not under @muladd (plain ops)
+    for (int i = 0; i < n; ++i) r[i] = fsal0[i] + dtgamma * I.dT[i];
     lu_solve(n, I.W.data(), I.piv.data(), r);
     for (int i = 0; i < n; ++i) k1[i] = r[i] * neginvdtgamma;
     I.st.nsolve += 1;
@@ -1409,6 +1464,9 @@ void orc_rhs(int model, int n, const double* u, const double* p, double t, doubl
 }
 void orc_jac(int model, int n, const double* u, const double* p, double t, double* J) {
     jac(model, n, u, p, t, J);
+}
+int orc_tgrad(int model, int n, const double* u, const double* p, double t, double* dT) {
+    return tgrad(model, n, u, p, t, dT) ? 1 : 0;
 }
 
 thread_local std::vector<int32_t> g_last_alg_choice;

@@ -22,7 +22,8 @@ extern "C" {
 enum { ORC_TSIT5 = 0, ORC_VERN7 = 1, ORC_RODAS5P = 2, ORC_VERN9 = 3, ORC_ROSENBROCK23 = 4,
        ORC_AUTOTSIT5_ROSENBROCK23 = 5 /* AutoTsit5(Rosenbrock23()) */ };
 enum { ORC_LINEAR = 0, ORC_LORENZ = 1, ORC_ROBERTSON = 2, ORC_DUFFING = 3, ORC_BRUSSELATOR = 4, ORC_BOUNCING_BALL = 5,
-       ORC_VANDERPOL = 6, ORC_PK1 = 7 };
+       ORC_VANDERPOL = 6, ORC_PK1 = 7, ORC_FORCED_DUFFING = 8,
+       ORC_LOTKA_VOLTERRA = 9, ORC_OREGONATOR = 10 };
 /* SciMLBase ReturnCode subset used by this path (numbering of the C ABI). */
 enum { ORC_RC_DEFAULT = 0, ORC_RC_SUCCESS = 1, ORC_RC_MAXITERS = 2, ORC_RC_DTNAN = 3,
        ORC_RC_DTLESSTHANMIN = 4, ORC_RC_UNSTABLE = 5, ORC_RC_TERMINATED = 7 };
@@ -98,6 +99,8 @@ int64_t orc_rhs_calls(int reset);
 /* Model right-hand side and Jacobian (for tests of the models themselves). */
 void orc_rhs(int model, int n, const double* u, const double* p, double t, double* du);
 void orc_jac(int model, int n, const double* u, const double* p, double t, double* J);
+/* df/dt of a non-autonomous model (its tgrad); returns 0 for the autonomous ones */
+int orc_tgrad(int model, int n, const double* u, const double* p, double t, double* dT);
 
 #ifdef __cplusplus
 }

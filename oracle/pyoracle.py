@@ -14,7 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 
 TSIT5, VERN7, RODAS5P, VERN9, ROSENBROCK23, AUTOTSIT5_ROSENBROCK23 = 0, 1, 2, 3, 4, 5
-LINEAR, LORENZ, ROBERTSON, DUFFING, BRUSSELATOR, BOUNCING_BALL, VANDERPOL, PK1 = 0, 1, 2, 3, 4, 5, 6, 7
+LINEAR, LORENZ, ROBERTSON, DUFFING, BRUSSELATOR, BOUNCING_BALL, VANDERPOL, PK1, FORCED_DUFFING = 0, 1, 2, 3, 4, 5, 6, 7, 8
+LOTKA_VOLTERRA, OREGONATOR = 9, 10
 RC_DEFAULT, RC_SUCCESS, RC_MAXITERS, RC_DTNAN, RC_DTLESSTHANMIN, RC_UNSTABLE = range(6)
 RC_TERMINATED = 7
 
@@ -73,6 +74,8 @@ def lib():
         L.orc_rhs_calls.argtypes = [C.c_int]
         L.orc_rhs.argtypes = [C.c_int, C.c_int, dp, dp, C.c_double, dp]
         L.orc_jac.argtypes = [C.c_int, C.c_int, dp, dp, C.c_double, dp]
+        L.orc_tgrad.restype = C.c_int
+        L.orc_tgrad.argtypes = [C.c_int, C.c_int, dp, dp, C.c_double, dp]
         _lib = L
     return _lib
 
@@ -207,6 +210,14 @@ def jac(model, u, p, t=0.0):
     J = np.zeros((u.size, u.size))
     lib().orc_jac(model, u.size, _dp(u), _dp(p), t, _dp(J))
     return J
+
+
+def tgrad(model, u, p, t=0.0):
+    """df/dt of a non-autonomous model, or None for an autonomous one."""
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    p = np.ascontiguousarray(np.atleast_1d(p), dtype=np.float64)
+    dT = np.zeros_like(u)
+    return dT if lib().orc_tgrad(model, u.size, _dp(u), _dp(p), t, _dp(dT)) else None
 
 
 def rhs_calls(reset=False):

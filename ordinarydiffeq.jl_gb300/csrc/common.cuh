@@ -4,10 +4,24 @@
 // written explicitly (fma / fmaf) in the nesting the reference's @muladd code
 // produces, so the FP64 path follows the reference's operation order.
 #pragma once
+// The device headers also compile under NVRTC (registered models' kernels are
+// compiled at run time), which has no standard or CUDA runtime headers.
+#ifndef __CUDACC_RTC__
 #include <cstdint>
 #include <cuda_runtime.h>
+#else
+typedef signed char int8_t;
+typedef int int32_t;
+typedef unsigned int uint32_t;
+typedef long long int64_t;
+typedef unsigned long long uint64_t;
+#endif
 
 namespace odegb {
+
+// the two type traits the kernels use (std's, which NVRTC lacks)
+template <bool B> struct bool_constant { static constexpr bool value = B; };
+template <class...> using void_t = void;
 
 // ------------------------------------------------------------------ scalars
 template <class T> struct Arith;
@@ -245,6 +259,14 @@ template <class R> struct ParamOf { using type = R; };
 template <> struct ParamOf<float> { using type = fpair; };
 template <class R> using PR = typename ParamOf<R>::type;
 template <class R> __device__ __forceinline__ PR<R> make_param(double x) { return PR<R>(x); }
+
+// A parameter's FP64 value from any precision's parameter type, and an FP64
+// value in a stage type (float, double-float or double).
+__device__ __forceinline__ double pdouble(double x) { return x; }
+__device__ __forceinline__ double pdouble(fpair x) { return (double)x.hi + (double)x.lo; }
+__device__ __forceinline__ double pdouble(ff x) { return (double)x.hi + (double)x.lo; }
+template <class R> __device__ __forceinline__ R from_double(double x) { return (R)x; }
+template <> __device__ __forceinline__ ff from_double<ff>(double x) { return ff(x); }
 
 // ------------------------------------------------------------------ lane groups
 // A trajectory is owned by a group of L consecutive lanes of one warp; each

@@ -89,7 +89,9 @@ def main():
         "// Rodas5P: lib/OrdinaryDiffEqRosenbrock/src/rosenbrock_tableaus.jl:23-72",
         "// Rosenbrock23: lib/OrdinaryDiffEqRosenbrock/src/rosenbrock_tableaus.jl:6-10",
         "#pragma once",
+        "#ifndef __CUDACC_RTC__",
         "#include <cuda_runtime.h>",
+        "#endif",
         "namespace odegb {",
         "namespace tab {",
     ]

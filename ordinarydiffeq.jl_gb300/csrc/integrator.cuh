@@ -28,9 +28,7 @@
 // min/max/eps return, NaN propagation included.
 #pragma once
 #include "common.cuh"
-#include "ode_kernels.h"
-
-#include <type_traits>
+#include "ensemble_args.h"
 
 namespace odegb {
 
@@ -40,12 +38,25 @@ enum RetCode { RC_DEFAULT = 0, RC_SUCCESS = 1, RC_MAXITERS = 2, RC_DTNAN = 3, RC
 
 // Composite methods (AutoSwitchAlg) declare COMPOSITE; the loop then runs their
 // choice function and keeps one controller state per method.
-template <class A, class = void> struct is_composite_alg : std::false_type {};
-template <class A> struct is_composite_alg<A, std::void_t<decltype(A::COMPOSITE)>> : std::true_type {};
+template <class A, class = void> struct is_composite_alg : bool_constant<false> {};
+template <class A> struct is_composite_alg<A, void_t<decltype(A::COMPOSITE)>> : bool_constant<true> {};
 // models with a registered DiscreteCallback declare HAS_DISCRETE
-template <class M, class = void> struct has_discrete_callback : std::false_type {};
+template <class M, class = void> struct has_discrete_callback : bool_constant<false> {};
 template <class M>
-struct has_discrete_callback<M, std::void_t<decltype(M::HAS_DISCRETE)>> : std::bool_constant<M::HAS_DISCRETE> {};
+struct has_discrete_callback<M, void_t<decltype(M::HAS_DISCRETE)>> : bool_constant<M::HAS_DISCRETE> {};
+
+// models with an analytic time derivative (ODEFunction's tgrad) declare HAS_TGRAD
+template <class M, class = void> struct has_tgrad : bool_constant<false> {};
+template <class M>
+struct has_tgrad<M, void_t<decltype(M::HAS_TGRAD)>> : bool_constant<M::HAS_TGRAD> {};
+
+// f calls a Jacobian evaluation is counted as (JAC_F_CALLS: 1 for a Jacobian
+// by forward-mode AD of f, as the reference counts its ForwardDiff chunk; 0 for
+// an analytic one)
+template <class M, class = void> struct jac_f_calls { static constexpr int value = 0; };
+template <class M> struct jac_f_calls<M, void_t<decltype(M::JAC_F_CALLS)>> {
+    static constexpr int value = M::JAC_F_CALLS;
+};
 
 // The left end of a sign change of f in [lo, hi] narrowed to adjacent floats
 // (LeftRootFind: the reference solves IntervalNonlinearProblem with ModAB,
@@ -156,9 +167,9 @@ __device__ __forceinline__ double ptol100(double x) {
     return 100.0 * e;
 }
 
-// Time argument of a stage's right-hand side, t + c dt.  Every registered
-// model is autonomous (f does not read t), so the sum is not formed: it would
-// be one FP64 instruction per stage for a value nobody reads.
+// Time argument of a stage's right-hand side, t + c dt (the reference's
+// muladd(c, dt, t)).  For an autonomous model (f does not read t) the sum is not
+// formed: it would be one FP64 instruction per stage for a value nobody reads.
 template <class Model>
 __device__ __forceinline__ double stage_time(double c, double dt, double t) {
     if constexpr (Model::AUTONOMOUS) return t;
@@ -303,7 +314,7 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
     constexpr int NP = Model::NP;
     const long long N = a.N;
     R u[C], uprev[C], ulo[C], uprevlo[C];   // solution as (hi, lo) pairs, see Acc
-    PR<R> p[NP];   // FP64, or float pairs in the mixed form (fpair)
+    PR<R> p[NP > 0 ? NP : 1];   // FP64, or float pairs in the mixed form (fpair)
 #pragma unroll
     for (int c = 0; c < C; ++c) Acc<R>::split(a.u0[(size_t)(g.lane * C + c) * N + j], u[c], ulo[c]);
 #pragma unroll
@@ -481,7 +492,7 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             ev_last = true;
             last_event_error = residual;
             // apply_callback!: set_proposed_dt! (dtrelax = 1)
-            dtpropose = pmax(nextafter(a.dtmin, (double)INFINITY), dt);
+            dtpropose = pmax(nextafter(a.dtmin, __longlong_as_double(0x7ff0000000000000LL)), dt);
             // change_t_via_interpolation!  (the step's end state stays for the saveat
             // points before the event)
             const bool moved = cb_t != t;

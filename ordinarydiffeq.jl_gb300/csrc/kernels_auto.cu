@@ -1,5 +1,6 @@
 // AutoTsit5(Rosenbrock23()) kernel variants (one lane per trajectory; FP64 and mixed).
 #include "autoswitch.cuh"
+#include "ode_kernels.h"
 #include "models.cuh"
 
 namespace odegb {
@@ -15,6 +16,7 @@ namespace odegb {
 static const KernelVariant kVariants[] = {
     BOTH(VanDerPol, M_VANDERPOL, 1, 2), BOTH(Robertson, M_ROBERTSON, 1, 3), BOTH(Lorenz, M_LORENZ, 1, 3),
     BOTH(PKOneCompartment, M_PK1, 1, 2),
+    BOTH(ForcedDuffing, M_FORCED_DUFFING, 1, 2),
     BOTH(Linear, M_LINEAR, 1, 1),       BOTH(Linear, M_LINEAR, 1, 2),       BOTH(BouncingBall, M_BOUNCING_BALL, 1, 2),
 };
 

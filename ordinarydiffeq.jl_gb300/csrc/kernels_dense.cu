@@ -10,6 +10,7 @@
 // those vectors first, as _ode_addsteps! does (verner_addsteps.jl:137-193).
 // The interpolants themselves are the integrator's own (erk.cuh, rodas.cuh).
 #include "erk.cuh"
+#include "ode_kernels.h"
 #include "rodas.cuh"
 #include "ros23.cuh"
 #include "models.cuh"

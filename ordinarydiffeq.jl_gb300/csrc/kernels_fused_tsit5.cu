@@ -1,6 +1,7 @@
 // Tsit5 over every size class of an uneven ensemble in one persistent
 // launch (fused_class_kernel in integrator.cuh).
 #include "erk.cuh"
+#include "ode_kernels.h"
 #include "models.cuh"
 
 namespace odegb {

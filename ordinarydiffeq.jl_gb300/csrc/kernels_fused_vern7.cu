@@ -4,6 +4,7 @@
 // and more lanes per trajectory); the FP64 form 4, where the FP64 control path
 // is shared by more trajectories per warp.
 #include "erk.cuh"
+#include "ode_kernels.h"
 #include "models.cuh"
 
 namespace odegb {

@@ -1,6 +1,7 @@
 // Rodas5P kernel variants for 16 to 64 states: one lane group per trajectory,
 // W and its LU in shared memory (lu_group.cuh).
 #include "rodas.cuh"
+#include "ode_kernels.h"
 #include "models.cuh"
 
 namespace odegb {

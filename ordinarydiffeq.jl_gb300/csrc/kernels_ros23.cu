@@ -1,5 +1,6 @@
 // Rosenbrock23 kernel variants with W in registers (one lane per trajectory).
 #include "ros23.cuh"
+#include "ode_kernels.h"
 #include "models.cuh"
 
 namespace odegb {
@@ -16,6 +17,7 @@ static const KernelVariant kVariants[] = {
     BOTH(BouncingBall, M_BOUNCING_BALL, 1, 2),
     BOTH(VanDerPol, M_VANDERPOL, 1, 2),
     BOTH(PKOneCompartment, M_PK1, 1, 2),
+    BOTH(ForcedDuffing, M_FORCED_DUFFING, 1, 2),
     BOTH(Linear, M_LINEAR, 1, 1), BOTH(Linear, M_LINEAR, 1, 2),
     BOTH(Lorenz, M_LORENZ, 1, 3), BOTH(Robertson, M_ROBERTSON, 1, 3),
     BOTH(Duffing, M_DUFFING, 1, 4),

@@ -1,5 +1,6 @@
 // Vern7 kernel variants (FP64 and mixed, one lane or a lane group per trajectory).
 #include "erk.cuh"
+#include "ode_kernels.h"
 #include "models.cuh"
 
 namespace odegb {
@@ -15,6 +16,7 @@ namespace odegb {
 static const KernelVariant kVariants[] = {
     BOTH(BouncingBall, M_BOUNCING_BALL, 1, 2),
     BOTH(PKOneCompartment, M_PK1, 1, 2),
+    BOTH(ForcedDuffing, M_FORCED_DUFFING, 1, 2),
     BOTH(Linear, M_LINEAR, 1, 1),   BOTH(Linear, M_LINEAR, 1, 2),   BOTH(Linear, M_LINEAR, 1, 8),
     BOTH(Lorenz, M_LORENZ, 1, 3),
     BOTH(Duffing, M_DUFFING, 1, 4), BOTH(Duffing, M_DUFFING, 1, 8), BOTH(Duffing, M_DUFFING, 2, 4),

@@ -14,13 +14,53 @@
 //               p = (k, delta, beta): v_i' = (k*lap_i - delta*v_i) - beta*x_i^3
 //  BRUSSELATOR  1-D periodic, interleaved (u_i, v_i), p = (A, B, alpha), ae = alpha*ncells^2:
 //               u' = ((A + u^2 v) - (B+1) u) + ae*lap u,  v' = (B u - u^2 v) + ae*lap v
+//  FORCED_DUFFING  non-autonomous: x' = v, v' = ((g cos(w t) - delta v) - alpha x) - beta x^3,
+//               p = (delta, alpha, beta, g, w), with its analytic time derivative (tgrad)
 #pragma once
 #include "common.cuh"
 
 namespace odegb {
 
 enum ModelId { M_LINEAR = 0, M_LORENZ = 1, M_ROBERTSON = 2, M_DUFFING = 3, M_BRUSSELATOR = 4, M_BOUNCING_BALL = 5,
-               M_VANDERPOL = 6, M_PK1 = 7 };
+               M_VANDERPOL = 6, M_PK1 = 7, M_FORCED_DUFFING = 8 };
+
+// A forced (non-autonomous) Duffing oscillator, the standard driven nonlinear
+// oscillator: u = (x, v), x' = v, v' = ((g cos(w t) - delta v) - alpha x) - beta x^3;
+// p = (delta, alpha, beta, g, w).  With beta = 0 it is the driven damped linear
+// oscillator, whose closed-form solution pins the oracle.  The forcing is
+// evaluated in FP64 in every precision (t is FP64; w t in FP32 would lose the
+// phase after a few periods) and rounded to the stage type.  tgrad is the
+// analytic df/dt = (0, -g w sin(w t)) (ODEFunction's tgrad: the Rosenbrock
+// methods take it instead of differentiating f in t, so it is not an f call).
+struct ForcedDuffing {
+    static constexpr int NP = 5;
+    static constexpr bool AUTONOMOUS = false;
+    static constexpr bool HAS_EVENT = false;
+    static constexpr bool HAS_TGRAD = true;
+    template <class P> __device__ static double forcing(const P* p, double t) {
+        return pdouble(p[3]) * cos(pdouble(p[4]) * t);
+    }
+    template <class R, int L, int C, class P>
+    __device__ static void rhs(R* du, const R* u, const P* p, double t, const Group<L>&) {
+        static_assert(L == 1 && C == 2, "the forced oscillator has 2 states on one lane");
+        const R fo = from_double<R>(forcing(p, t));
+        du[0] = u[1];
+        du[1] = ((fo - p[0] * u[1]) - p[1] * u[0]) - p[2] * (u[0] * u[0] * u[0]);
+    }
+    template <class R, int N, class P>
+    __device__ static void jac(R (*J)[N], const R* u, const P* p, double) {
+        J[0][0] = R(0);
+        J[0][1] = R(1);
+        J[1][0] = -p[1] - p[2] * (R(3) * (u[0] * u[0]));
+        J[1][1] = -p[0];
+    }
+    template <class R, int C, class P>
+    __device__ static void tgrad(R* dT, const R*, const P* p, double t) {
+        const double w = pdouble(p[4]);
+        dT[0] = R(0);
+        dT[1] = from_double<R>(-(pdouble(p[3]) * w) * sin(w * t));
+    }
+};
 
 // The van der Pol oscillator of the reference's stiffness-detection test
 // (test/InterfaceI/stiffness_detection_test.jl:10-16): u = (x, y), x' = y,

@@ -8,6 +8,7 @@
 // variant the call fails with ODE_E_UNSUPPORTED.
 #include "ode_gb300.h"
 #include "ode_kernels.h"
+#include "rtc_models.h"
 
 #include <algorithm>
 #include <atomic>
@@ -54,7 +55,11 @@ const std::vector<KernelVariant>& all_variants() {
     return v;
 }
 
-int model_nparams(int model) { return (model == ODE_MODEL_LINEAR || model == ODE_MODEL_VANDERPOL) ? 1 : 3; }
+int model_nparams(int model) {
+    int np = 0;
+    if (model >= ODE_MODEL_USER_BASE) return rtc_lookup(model, nullptr, &np, nullptr) ? np : -1;
+    return (model == ODE_MODEL_LINEAR || model == ODE_MODEL_VANDERPOL) ? 1 : model == ODE_MODEL_FORCED_DUFFING ? 5 : 3;
+}
 // models with a registered callback (continuous: the ball; discrete: the dosing model)
 bool model_has_event(int model) { return model == ODE_MODEL_BOUNCING_BALL || model == ODE_MODEL_PK_ONE_COMPARTMENT; }
 
@@ -81,6 +86,41 @@ const KernelVariant* find_variant(int alg, int model, int prec, int n, int lanes
         if (lanes <= 0 && v.lanes == default_lanes(alg, n, prec)) best = &v;
     }
     return best;
+}
+
+// The kernel of a uniform-size problem: a compiled-in variant, or the run-time
+// compiled kernel of a registered model (compiled on its first use).  nullptr
+// with *rc and *why set when there is none.
+const KernelVariant* variant_for(const ode_problem_desc* d, int lanes, int* rc, std::string* why) {
+    *rc = ODE_OK;
+    if (d->model_id >= ODE_MODEL_USER_BASE) {
+        if (lanes > 1) {
+            *rc = ODE_E_UNSUPPORTED;
+            *why = "registered models run one lane per trajectory";
+            return nullptr;
+        }
+        return rtc_variant(d->alg_id, d->model_id, d->precision, rc, why);
+    }
+    const KernelVariant* v = find_variant(d->alg_id, d->model_id, d->precision, d->n_states, lanes);
+    if (!v) {
+        char buf[160];
+        std::snprintf(buf, sizeof buf, "no compiled kernel for alg %d model %d precision %d n %d lanes %d",
+                      d->alg_id, d->model_id, d->precision, d->n_states, lanes);
+        *rc = ODE_E_UNSUPPORTED;
+        *why = buf;
+    }
+    return v;
+}
+
+// Launch one ensemble kernel: through its typed launcher, or (a registered
+// model's run-time compiled kernel) through cudaLaunchKernel.
+void launch_any(const KernelVariant* v, const EnsembleArgs& a, int grid, int block, size_t smem, cudaStream_t s) {
+    if (v->launch) {
+        v->launch(a, grid, block, smem, s);
+        return;
+    }
+    void* args[] = {const_cast<EnsembleArgs*>(&a)};
+    cudaLaunchKernel(v->fn, dim3(grid), dim3(block), args, smem, s);
 }
 
 struct DevBuf {
@@ -186,8 +226,13 @@ int check_problem(const ode_problem_desc* d, const ode_options* o, int64_t N, co
     if (!d || !o) return bad(ODE_E_INVALID, "null problem or options");
     if (N < 0) return bad(ODE_E_INVALID, "negative trajectory count");
     if (d->alg_id < ODE_TSIT5 || d->alg_id >= kNumAlgs) return bad(ODE_E_INVALID, "unknown alg_id");
-    if (d->model_id < ODE_MODEL_LINEAR || d->model_id > ODE_MODEL_PK_ONE_COMPARTMENT)
+    if (d->model_id >= ODE_MODEL_USER_BASE) {
+        int n = 0;
+        if (!rtc_lookup(d->model_id, &n, nullptr, nullptr)) return bad(ODE_E_INVALID, "unknown model_id");
+        if (d->n_states != n) return bad(ODE_E_INVALID, "n_states does not match the registered model");
+    } else if (d->model_id < ODE_MODEL_LINEAR || d->model_id > ODE_MODEL_FORCED_DUFFING) {
         return bad(ODE_E_INVALID, "unknown model_id");
+    }
     if (d->precision != ODE_PREC_FP64 && d->precision != ODE_PREC_MIXED)
         return bad(ODE_E_INVALID, "unknown precision");
     if (d->n_states <= 0) return bad(ODE_E_INVALID, "n_states must be positive");
@@ -195,7 +240,8 @@ int check_problem(const ode_problem_desc* d, const ode_options* o, int64_t N, co
     if ((d->model_id == ODE_MODEL_LORENZ || d->model_id == ODE_MODEL_ROBERTSON) && d->n_states != 3)
         return bad(ODE_E_INVALID, "this model has 3 states");
     if ((d->model_id == ODE_MODEL_BOUNCING_BALL || d->model_id == ODE_MODEL_VANDERPOL ||
-         d->model_id == ODE_MODEL_PK_ONE_COMPARTMENT) && d->n_states != 2)
+         d->model_id == ODE_MODEL_PK_ONE_COMPARTMENT || d->model_id == ODE_MODEL_FORCED_DUFFING) &&
+        d->n_states != 2)
         return bad(ODE_E_INVALID, "this model has 2 states");
     if (o->callback && !model_has_event(d->model_id))
         return bad(ODE_E_UNSUPPORTED, "the model has no registered callback");
@@ -476,7 +522,7 @@ int launch_variant(ode_handle* h, const KernelVariant* v, EnsembleArgs a, int sc
         grid = (int)((threads + block - 1) / block);
         a.persistent = 0;
     }
-    v->launch(a, grid, block, smem, s);
+    launch_any(v, a, grid, block, smem, s);
     h->launches++;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(h, ODE_E_CUDA, std::string("launch ") + v->name + ": " + cudaGetErrorString(e));
@@ -534,13 +580,10 @@ int make_plan(ode_handle* h, const ode_problem_desc* d, const ode_options* o, co
                 pl->scheduler = it->second.scheduler;
             }
         }
-        pl->v = find_variant(d->alg_id, d->model_id, d->precision, d->n_states, lanes);
-        if (!pl->v) {
-            char buf[160];
-            std::snprintf(buf, sizeof buf, "no compiled kernel for alg %d model %d precision %d n %d lanes %d",
-                          d->alg_id, d->model_id, d->precision, d->n_states, lanes);
-            return fail(h, ODE_E_UNSUPPORTED, buf);
-        }
+        int rc = ODE_OK;
+        std::string why;
+        pl->v = variant_for(d, lanes, &rc, &why);
+        if (!pl->v) return fail(h, rc, why);
         // auto: the persistent queue for the shared-memory kernels (measured 13%
         // faster on the 64-state Brusselator: its many short waves leave tails)
         // and for AutoTsit5 (trajectories that turn stiff take ~100x the steps of
@@ -1559,6 +1602,17 @@ int ode_autotune(ode_handle* h, const ode_problem_desc* d, const ode_options* o,
     return ODE_OK;
 }
 
+int ode_register_model(const char* source, const char* name, int32_t n_states, int32_t n_params, int32_t flags,
+                       int32_t* model_id) {
+    if (!model_id) return fail(nullptr, ODE_E_INVALID, "null model_id pointer");
+    std::string why;
+    int id = 0;
+    const int rc = rtc_register(source, name, n_states, n_params, flags, &id, &why);
+    if (rc) return fail(nullptr, rc, why);
+    *model_id = id;
+    return ODE_OK;
+}
+
 int ode_query_variants(int alg, int model, int precision, int n, int32_t* lanes, int32_t cap) {
     int k = 0;
     for (const auto& v : all_variants())
@@ -1664,7 +1718,7 @@ int noalloc_launch(const KernelVariant* v, EnsembleArgs a, unsigned long long* q
     if (grid < 1) grid = 1;
     a.persistent = 1;
     a.queue = queue;
-    v->launch(a, grid, block, smem, s);
+    launch_any(v, a, grid, block, smem, s);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(nullptr, ODE_E_CUDA, std::string("launch ") + v->name + ": " + cudaGetErrorString(e));
     return ODE_OK;
@@ -1745,8 +1799,9 @@ extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_o
     e = cudaMemsetAsync(scratch, 0, kCounters * sizeof(unsigned long long), s);
     if (e != cudaSuccess) return fail(nullptr, ODE_E_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
     if (npt_dev == nullptr) {
-        const KernelVariant* v = find_variant(d->alg_id, d->model_id, d->precision, d->n_states, o->lanes_per_traj);
-        if (!v) return fail(nullptr, ODE_E_UNSUPPORTED, "no compiled kernel for this problem");
+        std::string why;
+        const KernelVariant* v = variant_for(d, o->lanes_per_traj, &rc, &why);
+        if (!v) return fail(nullptr, rc, why);
         return noalloc_launch(v, a, scratch, sm_count, s);
     }
     long long* order = (long long*)(scratch + kCounters);

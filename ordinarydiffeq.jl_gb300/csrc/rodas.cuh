@@ -8,8 +8,12 @@
 //  tableau                            lib/OrdinaryDiffEqRosenbrock/src/rosenbrock_tableaus.jl:23-72
 //  W = J - I/(dt*gamma)               lib/OrdinaryDiffEqDifferentiation/src/derivative_utils.jl:663-685
 //  J reuse after a rejected step      derivative_utils.jl:535-557 (do_newJW), :1011-1041
-//  time derivative                    derivative_utils.jl:181-227 (models are autonomous: dT = 0;
-//                                     the reference's AD evaluation is counted as one f call)
+//  time derivative                    derivative_utils.jl:181-227: the model's analytic tgrad
+//                                     (not an f call), formed with a fresh J only (:1040); an
+//                                     autonomous model without one has dT = 0, and the reference's
+//                                     AD evaluation of it is counted as one f call
+//  dT in the stages                   linsolve_tmp = fsalfirst + dtd1 dT (:227, plain ops), then
+//                                     muladd(dtd_s, dT, du) + sum dtC ks (_stage_rhs!, :637-652)
 //  interpolant (order 3)              rosenbrock_interpolants.jl:172-206
 // The LU is Doolittle with partial pivoting (largest |pivot|, first on ties),
 // the same algorithm the CPU oracle states; LinearSolve's LU (not vendored)
@@ -181,12 +185,15 @@ template <class LA>
 struct Rodas5PT {
     static constexpr int ORDER = 5;
     static constexpr bool IMPLICIT = true;
-    static constexpr int MAXP = 4;
+    // parameters kept in double-float (mixed mode); only the model's NP are
+    // touched, so the unused entries take no registers
+    static constexpr int MAXP = 32;
     template <class R, int C> struct Cache {
         typename LA::template Store<R, C> la;
         R ks[8][C];
         R dk[3][C];   // dense k1..k3
         R scratch[C];
+        R dT[C];       // df/dt at (uprev, t), non-autonomous models
         ff pff[MAXP];  // parameters in double-float (mixed mode)
         bool haveJ;
         int ir;
@@ -204,6 +211,7 @@ struct Rodas5PT {
         if (sizeof(R) == 4) {
 #pragma unroll
             for (int i = 0; i < Model::NP; ++i) c.pff[i] = ff(a.p[(size_t)i * a.N + j]);
+            static_assert(Model::NP <= MAXP, "too many parameters for the double-float copy");
         }
     }
     template <class R, int C> __device__ static void on_accept(Cache<R, C>&) {}
@@ -230,9 +238,13 @@ struct Rodas5PT {
         st.nf += 1;
         bool new_jac = !(iter > 1 && errorfail) || !c.haveJ;
         LA::template jacobian<Model, R, L, C>(c.la, up, p, t, new_jac, g);
+        static_assert(Model::AUTONOMOUS || has_tgrad<Model>::value, "a non-autonomous model needs its tgrad");
+        static_assert(Model::AUTONOMOUS || L == 1, "time derivatives are formed on one lane");
         if (new_jac) {
             st.njacs += 1;
-            st.nf += 1;   // the reference's AD time derivative (dT = 0 for autonomous models)
+            st.nf += jac_f_calls<Model>::value;
+            if constexpr (has_tgrad<Model>::value) Model::template tgrad<R, C>(c.dT, up, p, t);
+            else st.nf += 1;   // the reference's AD time derivative (dT = 0 for autonomous models)
             c.haveJ = true;
         }
         LA::template factor<R, L, C>(c.la, idg, g);
@@ -240,6 +252,11 @@ struct Rodas5PT {
         R r[C];
 #pragma unroll
         for (int i = 0; i < C; ++i) r[i] = fsal[i];
+        if constexpr (!Model::AUTONOMOUS) {   // fsalfirst + dtd1 dT
+            const R dtd0 = (R)(dt * tab::RODAS5P_d(0));
+#pragma unroll
+            for (int i = 0; i < C; ++i) r[i] = fsal[i] + dtd0 * c.dT[i];
+        }
         LA::template wsolve<Model, R, L, C>(c.la, r, dt, idg, c.ir, up, uplo, c.pff, g);
 #pragma unroll
         for (int i = 0; i < C; ++i) c.ks[0][i] = -r[i];
@@ -269,12 +286,18 @@ struct Rodas5PT {
             for (int i = 0; i < C; ++i) {
                 if (sizeof(R) == 8) {
                     R acc = du[i];
+                    if constexpr (!Model::AUTONOMOUS) acc = FMA((R)(dt * tab::RODAS5P_d(s)), c.dT[i], acc);
 #pragma unroll
                     for (int jj = 0; jj < s; ++jj) acc = FMA((R)tab::RODAS5P_C(s, jj) * invdt, c.ks[jj][i], acc);
                     r[i] = acc;
                 } else {   // du + sum_j (C[s,j]/dt) ks_j with C split at compile time and 1/dt exact in FP32 pairs
                     CSum cs;
                     cs.hi = (float)du[i];
+                    if constexpr (!Model::AUTONOMOUS) {   // + dtd_s dT, dtd_s = dt d_s as a float pair
+                        const double dd = dt * tab::RODAS5P_d(s);
+                        const float dh = (float)dd;
+                        cs.add_pair(dh, (float)(dd - (double)dh), (float)c.dT[i]);
+                    }
 #pragma unroll
                     for (int jj = 0; jj < s; ++jj) {
                         const float ch = tab::RODAS5P_C_HI(s, jj), cl = tab::RODAS5P_C_LO(s, jj);

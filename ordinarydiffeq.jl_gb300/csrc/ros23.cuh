@@ -29,7 +29,9 @@ template <class LA>
 struct Rosenbrock23T {
     static constexpr int ORDER = 2;
     static constexpr bool IMPLICIT = true;
-    static constexpr int MAXP = 4;
+    // parameters kept in double-float (mixed mode); only the model's NP are
+    // touched, so the unused entries take no registers
+    static constexpr int MAXP = 32;
     template <class R, int C> struct Cache {
         typename LA::template Store<R, C> la;
         R k[3][C];       // k1, k2 (the dense vectors), k3 (error estimate)
@@ -37,6 +39,7 @@ struct Rosenbrock23T {
         R fsal[C];       // f(uprev): FSAL from the last accepted step
         R fsallast[C];   // f(u)
         R scratch[C];
+        R dT[C];         // df/dt at (uprev, t), non-autonomous models
         ff pff[MAXP];
         int ir;
     };
@@ -53,6 +56,7 @@ struct Rosenbrock23T {
         if (sizeof(R) == 4) {
 #pragma unroll
             for (int i = 0; i < Model::NP; ++i) c.pff[i] = ff(a.p[(size_t)i * a.N + j]);
+            static_assert(Model::NP <= MAXP, "too many parameters for the double-float copy");
         }
     }
     template <class Model, class R, int L, int C>
@@ -115,9 +119,16 @@ struct Rosenbrock23T {
             dto6 = dr / R(6);
             c32 = tab::ROS23_C32_HI;
         }
+        static_assert(Model::AUTONOMOUS || has_tgrad<Model>::value, "a non-autonomous model needs its tgrad");
+        static_assert(Model::AUTONOMOUS || L == 1, "time derivatives are formed on one lane");
         LA::template jacobian<Model, R, L, C>(c.la, up, p, t, true, g);
         st.njacs += 1;
-        st.nf += 1;   // the reference's AD time derivative (dT = 0 for autonomous models)
+        st.nf += jac_f_calls<Model>::value;
+        // the time derivative (calc_tderivative!, derivative_utils.jl:181-227): the model's
+        // analytic tgrad (not an f call); else dT = 0 for an autonomous model, whose AD
+        // evaluation in the reference counts as one f call
+        if constexpr (has_tgrad<Model>::value) Model::template tgrad<R, C>(c.dT, up, p, t);
+        else st.nf += 1;
         LA::template factor<R, L, C>(c.la, idg, g);
         st.nw += 1;
         R* k1 = c.k[0];
@@ -125,7 +136,12 @@ struct Rosenbrock23T {
         R* k3 = c.k[2];
         R r[C];
 #pragma unroll
-        for (int i = 0; i < C; ++i) r[i] = c.fsal[i];   // fsalfirst + dtd1 dT, dT = 0
+        for (int i = 0; i < C; ++i) r[i] = c.fsal[i];   // fsalfirst + dtd1 dT (dT = 0: autonomous)
+        if constexpr (!Model::AUTONOMOUS) {
+            const R dtg = (R)(dt * tab::ROS23_D);
+#pragma unroll
+            for (int i = 0; i < C; ++i) r[i] = c.fsal[i] + dtg * c.dT[i];
+        }
         LA::template wsolve<Model, R, L, C>(c.la, r, dt, idg, c.ir, up, uplo, c.pff, g);
 #pragma unroll
         for (int i = 0; i < C; ++i) k1[i] = r[i] * ninv;
@@ -149,7 +165,8 @@ struct Rosenbrock23T {
 #pragma unroll
         for (int i = 0; i < C; ++i) {
             R acc = FMA(-c32, k2[i] - c.f1[i], c.fsallast[i]);
-            r[i] = FMA(R(-2), k1[i] - c.fsal[i], acc);   // + dt dT, dT = 0
+            r[i] = FMA(R(-2), k1[i] - c.fsal[i], acc);
+            if constexpr (!Model::AUTONOMOUS) r[i] = FMA(dr, c.dT[i], r[i]);   // + dt dT
         }
         LA::template wsolve<Model, R, L, C>(c.la, r, dt, idg, c.ir, up, uplo, c.pff, g);
 #pragma unroll

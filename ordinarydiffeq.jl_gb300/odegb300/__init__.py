@@ -8,12 +8,12 @@
 """
 from .ensemble import (AutoTsit5, ContinuousCallback, DiscreteCallback, EnsembleContext, EnsembleGB300,
                        EnsembleProblem, EnsembleSolution, ODEProblem, ODESolution, ReturnCode, Rodas5P, Rosenbrock23,
-                       Tsit5, Vern7, autotune, dense_eval, get_handle, remake, solve, solve_arrays)
+                       Tsit5, Vern7, autotune, dense_eval, get_handle, register_model, remake, solve, solve_arrays)
 from .saveat import julia_float_range, resolve_saveat
 from .serving import Server, run_open_loop
 from . import _lib, build
 
 __all__ = ["AutoTsit5", "ContinuousCallback", "DiscreteCallback", "EnsembleContext", "EnsembleGB300", "EnsembleProblem",
            "EnsembleSolution", "ODEProblem", "ODESolution", "ReturnCode", "Rodas5P", "Rosenbrock23", "Tsit5", "Vern7",
-           "autotune", "dense_eval", "get_handle", "remake", "solve", "solve_arrays", "julia_float_range",
+           "autotune", "dense_eval", "get_handle", "register_model", "remake", "solve", "solve_arrays", "julia_float_range",
            "resolve_saveat", "Server", "run_open_loop"]

@@ -11,7 +11,9 @@ from . import build as _build
 
 ODE_TSIT5, ODE_VERN7, ODE_RODAS5P, ODE_ROSENBROCK23, ODE_AUTOTSIT5_ROSENBROCK23 = 0, 1, 2, 3, 4
 MODEL_LINEAR, MODEL_LORENZ, MODEL_ROBERTSON, MODEL_DUFFING_CHAIN, MODEL_BRUSSELATOR_1D = 0, 1, 2, 3, 4
-MODEL_BOUNCING_BALL, MODEL_VANDERPOL, MODEL_PK_ONE_COMPARTMENT = 5, 6, 7
+MODEL_BOUNCING_BALL, MODEL_VANDERPOL, MODEL_PK_ONE_COMPARTMENT, MODEL_FORCED_DUFFING = 5, 6, 7, 8
+MODEL_USER_BASE = 1000   # ids of models registered at run time start here
+MODEL_HAS_JAC, MODEL_HAS_TGRAD, MODEL_NONAUTONOMOUS = 1, 2, 4
 PREC_FP64, PREC_MIXED = 0, 1
 STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "out of device memory",
           -4: "unsupported", -5: "busy", -6: "timeout", -7: "unknown ticket"}
@@ -79,6 +81,7 @@ SIGNATURES = {
     "ode_kernel_launches": (C.c_int, [_VP, C.POINTER(C.c_int64)]),
     "ode_last_kernel_ms": (C.c_int, [_VP, _DP]),
     "ode_query_variants": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _IP, C.c_int32]),
+    "ode_register_model": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int32, C.c_int32, C.c_int32, _IP]),
     "ode_measure_fma_peak": (C.c_int, [C.c_int, C.c_int, _DP]),
     "ode_solve_ensemble_noalloc": (C.c_int, [C.POINTER(ProblemDesc), C.POINTER(Options), C.c_int64, _VP, _VP,
                                              _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),

@@ -36,10 +36,10 @@ class ReturnCode(IntEnum):
 MODELS = {"linear": _lib.MODEL_LINEAR, "lorenz": _lib.MODEL_LORENZ, "robertson": _lib.MODEL_ROBERTSON,
           "duffing_chain": _lib.MODEL_DUFFING_CHAIN, "brusselator_1d": _lib.MODEL_BRUSSELATOR_1D,
           "bouncing_ball": _lib.MODEL_BOUNCING_BALL, "van_der_pol": _lib.MODEL_VANDERPOL,
-          "pk_one_compartment": _lib.MODEL_PK_ONE_COMPARTMENT}
+          "pk_one_compartment": _lib.MODEL_PK_ONE_COMPARTMENT, "forced_duffing": _lib.MODEL_FORCED_DUFFING}
 N_PARAMS = {_lib.MODEL_LINEAR: 1, _lib.MODEL_LORENZ: 3, _lib.MODEL_ROBERTSON: 3,
             _lib.MODEL_DUFFING_CHAIN: 3, _lib.MODEL_BRUSSELATOR_1D: 3, _lib.MODEL_BOUNCING_BALL: 3,
-            _lib.MODEL_VANDERPOL: 1, _lib.MODEL_PK_ONE_COMPARTMENT: 3}
+            _lib.MODEL_VANDERPOL: 1, _lib.MODEL_PK_ONE_COMPARTMENT: 3, _lib.MODEL_FORCED_DUFFING: 5}
 
 
 @dataclass
@@ -326,6 +326,30 @@ def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_ste
         o.tstops = ts.ctypes.data_as(C.POINTER(C.c_double))
         o._tstops = ts   # the options hold the array while the call reads it
     return o
+
+
+def register_model(source, name, n_states, n_params, jac=False, tgrad=False, nonautonomous=False):
+    """Register a model given as CUDA C++ source (ode_register_model): the device
+    form of the reference's f(du, u, p, t), with its optional jac and tgrad.  For a
+    model named `name` the source defines the templates
+
+        template <class T, class P> __device__ void NAME_f(T* du, const T* u, const P* p, double t);
+        template <class T, class P> __device__ void NAME_jac(T* J, const T* u, const P* p, double t);   # jac=True
+        template <class T, class P> __device__ void NAME_tgrad(T* dT, const T* u, const P* p, double t); # tgrad=True
+
+    (J row-major).  Without NAME_jac the Rosenbrock methods differentiate NAME_f
+    by forward-mode AD.  Returns the model id; the name also becomes a model name
+    for ODEProblem and solve_arrays.  The kernels are compiled on the first solve
+    of each method and precision."""
+    L = _lib.load()
+    flags = (_lib.MODEL_HAS_JAC if jac else 0) | (_lib.MODEL_HAS_TGRAD if tgrad else 0) | \
+        (_lib.MODEL_NONAUTONOMOUS if nonautonomous else 0)
+    mid = C.c_int32(0)
+    _lib.check(L.ode_register_model(source.encode(), name.encode(), int(n_states), int(n_params), flags,
+                                    C.byref(mid)))
+    MODELS[name] = mid.value
+    N_PARAMS[mid.value] = int(n_params)
+    return mid.value
 
 
 def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=1e-6, dt=None,

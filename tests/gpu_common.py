@@ -10,7 +10,7 @@ ALG = {"tsit5": (Tsit5(), O.TSIT5), "vern7": (Vern7(), O.VERN7), "rodas5p": (Rod
        "autotsit5_rosenbrock23": (AutoTsit5(Rosenbrock23()), O.AUTOTSIT5_ROSENBROCK23)}
 MODEL = {"linear": O.LINEAR, "lorenz": O.LORENZ, "robertson": O.ROBERTSON, "duffing_chain": O.DUFFING,
          "brusselator_1d": O.BRUSSELATOR, "bouncing_ball": O.BOUNCING_BALL, "van_der_pol": O.VANDERPOL,
-         "pk_one_compartment": O.PK1}
+         "pk_one_compartment": O.PK1, "forced_duffing": O.FORCED_DUFFING}
 
 
 def lorenz_inputs(N, seed=42):

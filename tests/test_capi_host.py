@@ -133,3 +133,32 @@ def test_invalid_arguments_are_rejected_without_gpu():
     L = _lib.load()
     rc = L.ode_solve_ensemble(None, None, None, 0, None, None, None, None, None, None, None, None, None, None)
     assert rc == -1
+
+
+def test_model_registration_checks_on_the_host():
+    # ode_register_model validates its arguments and stores the source; the
+    # kernels are compiled (NVRTC) on the first solve, which needs a GPU
+    L = _lib.load()
+    src = b"template <class T, class P> __device__ void m_f(T* du, const T* u, const P* p, double t) { du[0] = -u[0]; }"
+    mid = C.c_int32(0)
+    assert L.ode_register_model(src, b"m", 1, 0, 0, C.byref(mid)) == 0
+    assert mid.value >= _lib.MODEL_USER_BASE
+    mid2 = C.c_int32(0)
+    assert L.ode_register_model(src, b"m", 1, 0, 0, C.byref(mid2)) == 0 and mid2.value == mid.value + 1
+    assert L.ode_register_model(src, b"1m", 1, 0, 0, C.byref(mid)) == -1         # not an identifier
+    assert L.ode_register_model(src, b"m", 0, 0, 0, C.byref(mid)) == -1          # no states
+    assert L.ode_register_model(src, b"m", 33, 0, 0, C.byref(mid)) == -1         # too many for registers
+    assert L.ode_register_model(src, b"m", 1, 0, 64, C.byref(mid)) == -1         # unknown flag
+    assert L.ode_register_model(None, b"m", 1, 0, 0, C.byref(mid)) == -1
+    # a registered id is checked like a compiled-in model: state and parameter counts
+    o = _lib.Options()
+    L.ode_options_default(C.byref(o))
+    d = _lib.ProblemDesc(mid2.value, _lib.ODE_TSIT5, 2, 0, _lib.PREC_FP64, 0)
+    assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == -1
+    assert b"registered model" in L.ode_last_error(None)
+    d = _lib.ProblemDesc(mid2.value, _lib.ODE_TSIT5, 1, 3, _lib.PREC_FP64, 0)
+    assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == -1
+    d = _lib.ProblemDesc(_lib.MODEL_USER_BASE + 100000, _lib.ODE_TSIT5, 1, 0, _lib.PREC_FP64, 0)
+    assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == -1
+    d = _lib.ProblemDesc(mid2.value, _lib.ODE_TSIT5, 1, 0, _lib.PREC_FP64, 0)
+    assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == 0   # valid, nothing to do

@@ -428,3 +428,71 @@ def test_dosing_with_every_step_saves_and_a_dose_at_tf():
         assert len(at) == 2, (tau, at)
     assert t[-1] == 24.0 and np.isclose(u[-1, 0] - u[-2, 0], dose)
     assert np.allclose(u[-1], pk_exact(24.0, ka, ke, dose, doses), rtol=1e-7)
+
+
+# ---------------------------------------------------------------- non-autonomous problems
+# The forced Duffing oscillator x'' + delta x' + alpha x + beta x^3 = g cos(w t);
+# with beta = 0 it is the driven damped linear oscillator, whose closed form
+# (transient plus the steady-state response A cos wt + B sin wt) pins every
+# method's handling of t in the stages and, for the Rosenbrock methods, of the
+# time derivative dT (derivative_utils.jl:181-227): with dT left out Rodas5P
+# loses its order on this problem.
+def forced_exact(t, x0, v0, d, a, g, w):
+    den = (a - w * w) ** 2 + (d * w) ** 2
+    A, B = g * (a - w * w) / den, g * d * w / den
+    mu = np.sqrt(a - d * d / 4.0)
+    C1 = x0 - A
+    C2 = (v0 - B * w + d / 2.0 * C1) / mu
+    e = np.exp(-d * t / 2.0)
+    cs, sn = np.cos(mu * t), np.sin(mu * t)
+    x = e * (C1 * cs + C2 * sn) + A * np.cos(w * t) + B * np.sin(w * t)
+    v = e * (-d / 2.0) * (C1 * cs + C2 * sn) + e * mu * (C2 * cs - C1 * sn) - A * w * np.sin(w * t) + \
+        B * w * np.cos(w * t)
+    return np.stack([x, v], axis=-1)
+
+
+FORCED_P = [0.3, 2.0, 0.0, 1.5, 1.7]   # delta, alpha, beta, g, w
+
+
+@pytest.mark.parametrize("alg,rt,bound", [(O.TSIT5, 1e-10, 3.0), (O.VERN7, 1e-12, 3.0), (O.RODAS5P, 1e-9, 5.0),
+                                          (O.VERN9, 1e-13, 3.0)])
+def test_forced_oscillator_matches_the_closed_form(alg, rt, bound):
+    sv = np.linspace(1.0, 20.0, 20)
+    # Vern9 has no interpolant here: its saves are hit as tstops
+    r = O.solve(alg, O.FORCED_DUFFING, [0.4, -0.2], FORCED_P, (0.0, 20.0), saveat=sv, reltol=rt, abstol=rt,
+                tstops=sv if alg == O.VERN9 else ())
+    assert r["retcode"] == 1
+    ex = forced_exact(sv, 0.4, -0.2, 0.3, 2.0, 1.5, 1.7)
+    err = np.abs(r["u"][np.isin(r["t"], sv)] - ex).max() / rt
+    assert err < bound * 10, err
+
+
+def test_forced_oscillator_tgrad_matches_finite_difference():
+    u, p = np.array([0.3, -0.7]), [0.3, 2.0, 1.2, 1.5, 1.7]
+    for t in (0.0, 0.9, 12.3):
+        h = 1e-6
+        fd = (O.rhs(O.FORCED_DUFFING, u, p, t + h) - O.rhs(O.FORCED_DUFFING, u, p, t - h)) / (2 * h)
+        assert np.allclose(O.tgrad(O.FORCED_DUFFING, u, p, t), fd, rtol=1e-7, atol=1e-8)
+    assert O.tgrad(O.LORENZ, np.ones(3), [10.0, 28.0, 8 / 3]) is None   # autonomous
+
+
+def test_rosenbrock_order_on_the_forced_oscillator():
+    # fixed steps: Rodas5P keeps its high order on the non-autonomous problem
+    # only with the dtd*dT terms; Rosenbrock23 keeps order 2
+    for alg, lo in ((O.RODAS5P, 4.5), (O.ROSENBROCK23, 1.8)):
+        errs = []
+        for k in (5, 6, 7):
+            r = O.solve(alg, O.FORCED_DUFFING, [0.4, -0.2], FORCED_P, (0.0, 2.0), saveat=[], saveat_given=False,
+                        dt=2.0 ** -k, adaptive=False)
+            errs.append(np.abs(r["u"][-1] - forced_exact(2.0, 0.4, -0.2, 0.3, 2.0, 1.5, 1.7)).max())
+        slope = float(np.mean(np.diff(np.log2(errs))) * -1)
+        assert slope > lo, (alg, slope, errs)
+
+
+def test_tgrad_is_not_an_f_call():
+    # an analytic tgrad replaces the AD time derivative: Rodas5P makes 8 f calls
+    # per attempt (+ 2 for the initial step) with it, 9 per fresh J without it
+    r = O.solve(O.RODAS5P, O.FORCED_DUFFING, [0.4, -0.2], FORCED_P, (0.0, 5.0), saveat=[], saveat_given=False,
+                reltol=1e-6, abstol=1e-6)
+    st = r["stats"]
+    assert st["nf"] == 8 * (st["naccept"] + st["nreject"]) + 2, st
