@@ -154,8 +154,8 @@ def test_registered_forced_oscillator_equals_the_compiled_in_model(alg):
 def test_compile_errors_are_reported():
     from odegb300 import _lib, register_model
     bad = register_model("template <class T, class P> __device__ void broken_f(T* du, const T* u, const P* p, "
-                         "double t) { du[0] = undefined_symbol; }", "broken", 1, 0)
-    u0, p, ts = np.ones((1, 4)), np.zeros((0, 4)), np.vstack([np.zeros(4), np.ones(4)])
+                         "double t) { du[0] = undefined_symbol; }", "broken", 1, 1)
+    u0, p, ts = np.ones((1, 4)), np.ones((1, 4)), np.vstack([np.zeros(4), np.ones(4)])
     with pytest.raises(_lib.OdeError) as e:
         gpu(bad, "tsit5", u0, p, ts, 0.5, 1e-6, 1e-6)
     assert e.value.status == -4 and "undefined_symbol" in str(e.value)
