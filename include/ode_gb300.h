@@ -259,9 +259,13 @@ int ode_dense_eval(ode_handle* h, const ode_problem_desc* d, int64_t ntraj, cons
 /* Continuous-batching serving API.  ode_submit copies the request's inputs
  * into handle-owned pinned/device memory and returns a ticket at once; the
  * request starts on the device as soon as a slot and enough of the HBM
- * budget are free, overlapping with requests already running.  Outputs land
- * in the caller's buffers (which must stay valid) when ode_poll/ode_wait
- * report completion. */
+ * budget are free, overlapping with requests already running.  Queued
+ * requests that differ only in their trajectories and tolerances (same model,
+ * method, precision, sizes, options, saveat and tstops) are merged into one
+ * launch, each trajectory with its own request's tolerances; a request that
+ * does not fit the budget lets smaller ones behind it start, unless it has
+ * waited 0.25 s.  Outputs land in the caller's buffers (which must stay
+ * valid) when ode_poll/ode_wait report completion. */
 int ode_submit(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int64_t ntraj,
                const int32_t* n_per_traj, const double* u0, const double* p, const double* tspan,
                const double* saveat, double* t_out, double* u_out, int32_t* nsaved, int32_t* retcode,
@@ -279,14 +283,18 @@ int ode_wait(ode_handle* h, uint64_t ticket, double timeout_s);
 int ode_next_completed(ode_handle* h, double timeout_s, uint64_t* ticket, int32_t* status, double* times);
 
 typedef struct {
-    int64_t submitted, admitted, completed, rejected, queued, running;
+    int64_t submitted, admitted, completed, rejected, queued, running;  /* requests (running: launches) */
     int64_t hbm_in_use, hbm_budget;
     int32_t slots;
-    int32_t reserved;
+    int32_t launches;    /* launches so far; requests merged into one launch count once */
 } ode_serving_stats;
 int ode_serving_stats_get(ode_handle* h, ode_serving_stats* s);
 /* Number of concurrent device slots (streams) used by the serving loop (default 8). */
 int ode_set_serving_slots(ode_handle* h, int32_t slots);
+/* ode_submit answers ODE_E_BUSY, without queuing, while max_queued requests wait
+ * (0, the default: no limit): a server sheds load instead of queuing without
+ * bound.  No reference counterpart (serving). */
+int ode_set_serving_queue_limit(ode_handle* h, int64_t max_queued);
 
 /* Ask running kernels of this handle to stop; affected trajectories report
  * ODE_RC_ABORTED.  Cleared by the next solve. */

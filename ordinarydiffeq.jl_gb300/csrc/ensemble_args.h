@@ -35,6 +35,8 @@ struct EnsembleArgs {
     OdeStatsDev* stats;
     // options
     double reltol, abstol, dtmax, dtmin, dt;
+    const double* reltol_traj;   // per-trajectory tolerances (nullptr: reltol/abstol for all)
+    const double* abstol_traj;
     long long maxiters;
     int save_start, save_end, save_end_user, saveat_given, saveat_scalar;
     int save_everystep;     // save every accepted step (saveat empty); nsave_cap bounds the slots

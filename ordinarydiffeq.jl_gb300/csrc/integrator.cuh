@@ -321,7 +321,10 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
     for (int i = 0; i < NP; ++i) p[i] = make_param<R>(a.p[(size_t)i * N + j]);
     const double t0 = a.tspan[j], tf = a.tspan[N + j];
     const double dtmax = a.dtmax > 0 ? a.dtmax : tf - t0;
-    const R abstol = (R)a.abstol, reltol = (R)a.reltol;
+    // the ensemble's tolerances, or per trajectory (requests merged into one
+    // launch by the serving loop keep their own)
+    const R abstol = (R)(a.abstol_traj ? a.abstol_traj[j] : a.abstol);
+    const R reltol = (R)(a.reltol_traj ? a.reltol_traj[j] : a.reltol);
     const Ctrl K = make_ctrl<Alg::ORDER, Alg::IMPLICIT>(a);
     // beta1, beta2 and qsteady_max change with a composite's current method
     CT beta1 = (CT)K.beta1, beta2 = (CT)K.beta2, qsteady_max = (CT)K.qsteady_max;

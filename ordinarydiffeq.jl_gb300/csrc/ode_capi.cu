@@ -18,6 +18,7 @@
 #include <cstring>
 #include <ctime>
 #include <deque>
+#include <list>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -145,6 +146,7 @@ struct Ctx {
 };
 
 struct Request;
+struct Batch;
 
 }  // namespace
 
@@ -169,8 +171,8 @@ struct ode_handle {
     // serving
     std::mutex mu;
     std::condition_variable cv;
-    std::deque<std::shared_ptr<Request>> pending;
-    std::vector<std::shared_ptr<Request>> running;
+    std::list<std::shared_ptr<Request>> pending;
+    std::vector<std::shared_ptr<Batch>> running;
     std::map<uint64_t, std::shared_ptr<Request>> tickets;
     std::thread worker;
     bool stop = false;
@@ -178,7 +180,8 @@ struct ode_handle {
     int slots = 8;
     uint64_t next_ticket = 1;
     size_t hbm_in_use = 0;
-    long long n_submitted = 0, n_admitted = 0, n_completed = 0, n_rejected = 0;
+    long long n_submitted = 0, n_admitted = 0, n_completed = 0, n_rejected = 0, n_batches = 0;
+    size_t max_queued = 0;                   // ode_submit answers ODE_E_BUSY past this many queued (0: no limit)
     std::vector<Ctx> slot_ctx;
     std::vector<int> slot_busy;
     std::vector<void*> slot_pinned;          // per-slot pinned staging (grow only)
@@ -661,9 +664,11 @@ int run_ensemble(ode_handle* h, Ctx& c, const ode_problem_desc* d, const ode_opt
                  const int32_t* npt_dev, const double* u0, const double* p, const double* tspan,
                  const double* saveat, double* t_out, double* u_out, int32_t* nsaved, int32_t* retcode,
                  OdeStatsDev* stats, cudaStream_t s, bool graph = false, int64_t stride = 0, bool timing = true,
-                 double* k_out = nullptr) {
+                 double* k_out = nullptr, const double* reltol_traj = nullptr, const double* abstol_traj = nullptr) {
     EnsembleArgs a = make_args(h, d, o, N, u0, p, tspan, saveat, t_out, u_out, nsaved, retcode, stats);
     a.k_out = k_out;
+    a.reltol_traj = reltol_traj;
+    a.abstol_traj = abstol_traj;
     if (stride > 0) a.N = stride;   // a slice of a larger ensemble: N trajectories, arrays of row length stride
     if (N == 0) return ODE_OK;
     Plan pl;
@@ -962,10 +967,22 @@ struct Request {
     ode_stats* stats = nullptr;
     int state = 0;  // 0 queued, 1 running, 2 done
     int status = ODE_OK;
+    double t_submit = 0, t_start = 0, t_done = 0;   // CLOCK_MONOTONIC seconds
+};
+
+// One launch: a request, or several compatible ones merged into one ensemble
+// (continuous batching inside the kernel: their trajectories share the launch,
+// each with its own tolerances, and a lane group that finishes one request's
+// trajectory goes on with another's).
+struct Batch {
+    std::vector<std::shared_ptr<Request>> reqs;
+    std::vector<int64_t> offset;   // first trajectory of each request in the merged ensemble
+    int64_t N = 0;
     int slot = -1;
     size_t bytes = 0;
-    void* dmem = nullptr;      // one device block for inputs and outputs
-    double t_submit = 0, t_start = 0, t_done = 0;   // CLOCK_MONOTONIC seconds
+    void* dmem = nullptr;          // one device block for the inputs and outputs
+    int status = ODE_OK;
+    const Request& head() const { return *reqs.front(); }
 };
 
 double mono_now() {
@@ -976,23 +993,39 @@ double mono_now() {
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-// Byte offsets of one request's block: inputs first, then outputs, so each
+// Requests merge when they differ only in their trajectories and tolerances:
+// same model, method, precision and sizes, the same options otherwise, the
+// same shared saveat and tstops, and uniform sizes.
+bool mergeable(const Request& a, const Request& b) {
+    if (std::memcmp(&a.d, &b.d, sizeof(a.d)) != 0) return false;
+    if (!a.npt.empty() || !b.npt.empty() || a.o.saveat_per_traj || b.o.saveat_per_traj) return false;
+    ode_options x = a.o, y = b.o;
+    x.reltol = y.reltol = 0.0;
+    x.abstol = y.abstol = 0.0;
+    if (std::memcmp(&x, &y, sizeof(x)) != 0) return false;
+    return a.saveat == b.saveat && a.tstops == b.tstops;
+}
+
+// Byte offsets of one batch's block: inputs first, then outputs, so each
 // direction is one contiguous copy.  The pinned staging of the slot and the
-// device block share this layout.
+// device block share this layout.  Merged batches carry per-trajectory
+// tolerances.
 struct Layout {
-    size_t u0, p, ts, sv, tst, npt, in_end, t, u, ns, rc, st, total;
+    size_t u0, p, ts, rtol, atol, sv, tst, npt, in_end, t, u, ns, rc, st, total;
 };
-Layout layout(const Request& r) {
-    const size_t n = (size_t)r.d.n_states, np = (size_t)r.d.n_params, N = (size_t)r.N, cap = save_cap(&r.o);
+Layout layout(const Request& h, int64_t Ntot, bool per_traj_tol) {
+    const size_t n = (size_t)h.d.n_states, np = (size_t)h.d.n_params, N = (size_t)Ntot, cap = save_cap(&h.o);
     Layout L;
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off += align256(bytes); return o; };
     L.u0 = take(n * N * 8);
     L.p = take(np * N * 8);
     L.ts = take(2 * N * 8);
-    L.sv = take(std::max<size_t>(r.saveat.size(), 1) * 8);
-    L.tst = take(std::max<size_t>(r.tstops.size(), 1) * 8);
-    L.npt = r.npt.empty() ? (size_t)-1 : take(N * 4);
+    L.rtol = per_traj_tol ? take(N * 8) : (size_t)-1;
+    L.atol = per_traj_tol ? take(N * 8) : (size_t)-1;
+    L.sv = take(std::max<size_t>(h.saveat.size(), 1) * 8);
+    L.tst = take(std::max<size_t>(h.tstops.size(), 1) * 8);
+    L.npt = h.npt.empty() ? (size_t)-1 : take(N * 4);
     L.in_end = off;
     L.t = take(cap * N * 8);
     L.u = take(cap * n * N * 8);
@@ -1002,16 +1035,19 @@ Layout layout(const Request& r) {
     L.total = off;
     return L;
 }
+Layout layout(const Batch& b) { return layout(b.head(), b.N, b.reqs.size() > 1); }
 
-size_t request_bytes(const Request& r) { return layout(r).total; }
+size_t request_bytes(const Request& r) { return layout(r, r.N, false).total; }
 
-// Start r on slot k: stage the inputs in the slot's pinned buffer, one copy in,
-// the ensemble kernel(s), one copy of the outputs back, all on the slot's stream.
-int admit(ode_handle* h, Request& r, int k) {
+// Start batch b on slot k: stage every request's inputs at its offset in the
+// slot's pinned buffer, one copy in, the ensemble kernel(s), one copy of the
+// outputs back, all on the slot's stream.
+int admit(ode_handle* h, Batch& b, int k) {
     Ctx& c = h->slot_ctx[k];
     cudaStream_t s = c.stream;
-    const Layout L = layout(r);
-    const size_t n = (size_t)r.d.n_states, np = (size_t)r.d.n_params, N = (size_t)r.N;
+    const Request& r0 = b.head();
+    const Layout L = layout(b);
+    const size_t n = (size_t)r0.d.n_states, np = (size_t)r0.d.n_params, N = (size_t)b.N;
     if (h->slot_pinned_cap[k] < L.total) {
         if (h->slot_pinned[k]) cudaFreeHost(h->slot_pinned[k]);
         h->slot_pinned[k] = nullptr;
@@ -1021,89 +1057,130 @@ int admit(ode_handle* h, Request& r, int k) {
         h->slot_pinned_cap[k] = want;
     }
     char* hs = (char*)h->slot_pinned[k];
-    std::memcpy(hs + L.u0, r.u0.data(), n * N * 8);
-    std::memcpy(hs + L.p, r.p.data(), np * N * 8);
-    std::memcpy(hs + L.ts, r.tspan.data(), 2 * N * 8);
-    if (!r.saveat.empty()) std::memcpy(hs + L.sv, r.saveat.data(), r.saveat.size() * 8);
-    if (!r.tstops.empty()) std::memcpy(hs + L.tst, r.tstops.data(), r.tstops.size() * 8);
-    if (!r.npt.empty()) std::memcpy(hs + L.npt, r.npt.data(), N * 4);
-    CUDA_TRY(h, cudaMallocAsync(&r.dmem, L.total, s));
-    char* base = (char*)r.dmem;
+    // structure-of-arrays rows: request q's trajectories at columns [offset, offset + N_q)
+    auto pack = [&](size_t base, size_t rows, const std::vector<double>& src, const Request& r, int64_t off) {
+        for (size_t i = 0; i < rows; ++i)
+            std::memcpy(hs + base + (i * N + (size_t)off) * 8, src.data() + i * (size_t)r.N, (size_t)r.N * 8);
+    };
+    for (size_t q = 0; q < b.reqs.size(); ++q) {
+        const Request& r = *b.reqs[q];
+        const int64_t off = b.offset[q];
+        pack(L.u0, n, r.u0, r, off);
+        pack(L.p, np, r.p, r, off);
+        pack(L.ts, 2, r.tspan, r, off);
+        if (b.reqs.size() > 1) {
+            std::fill((double*)(hs + L.rtol) + off, (double*)(hs + L.rtol) + off + r.N, r.o.reltol);
+            std::fill((double*)(hs + L.atol) + off, (double*)(hs + L.atol) + off + r.N, r.o.abstol);
+        }
+    }
+    if (!r0.saveat.empty()) std::memcpy(hs + L.sv, r0.saveat.data(), r0.saveat.size() * 8);
+    if (!r0.tstops.empty()) std::memcpy(hs + L.tst, r0.tstops.data(), r0.tstops.size() * 8);
+    if (!r0.npt.empty()) std::memcpy(hs + L.npt, r0.npt.data(), N * 4);
+    CUDA_TRY(h, cudaMallocAsync(&b.dmem, L.total, s));
+    char* base = (char*)b.dmem;
     CUDA_TRY(h, cudaMemcpyAsync(base, hs, L.in_end, cudaMemcpyHostToDevice, s));
-    ode_options o = r.o;
-    o.ntstops = (int32_t)r.tstops.size();
-    o.tstops = r.tstops.empty() ? nullptr : (const double*)(base + L.tst);
-    int rc = run_ensemble(h, c, &r.d, &o, r.N, r.npt.empty() ? nullptr : (const int32_t*)(base + L.npt),
+    ode_options o = r0.o;
+    o.ntstops = (int32_t)r0.tstops.size();
+    o.tstops = r0.tstops.empty() ? nullptr : (const double*)(base + L.tst);
+    const bool pt = b.reqs.size() > 1;
+    int rc = run_ensemble(h, c, &r0.d, &o, b.N, r0.npt.empty() ? nullptr : (const int32_t*)(base + L.npt),
                           (const double*)(base + L.u0), (const double*)(base + L.p), (const double*)(base + L.ts),
                           (const double*)(base + L.sv), (double*)(base + L.t), (double*)(base + L.u),
-                          (int32_t*)(base + L.ns), (int32_t*)(base + L.rc), (OdeStatsDev*)(base + L.st), s);
+                          (int32_t*)(base + L.ns), (int32_t*)(base + L.rc), (OdeStatsDev*)(base + L.st), s,
+                          /*graph=*/false, 0, /*timing=*/false, nullptr,
+                          pt ? (const double*)(base + L.rtol) : nullptr, pt ? (const double*)(base + L.atol) : nullptr);
     if (rc) return rc;
     CUDA_TRY(h, cudaMemcpyAsync(hs + L.t, base + L.t, L.total - L.t, cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(h, cudaFreeAsync(r.dmem, s));
-    r.dmem = nullptr;
+    CUDA_TRY(h, cudaFreeAsync(b.dmem, s));
+    b.dmem = nullptr;
     CUDA_TRY(h, cudaEventRecord(h->slot_ev[k], s));
     return ODE_OK;
 }
 
-// Outputs from the slot's staging into the caller's buffers.
-void finish(ode_handle* h, Request& r) {
-    const size_t n = (size_t)r.d.n_states, N = (size_t)r.N, cap = save_cap(&r.o);
-    if (r.status == ODE_OK && r.slot >= 0 && h->slot_pinned[r.slot]) {
-        const Layout L = layout(r);
-        const char* hs = (const char*)h->slot_pinned[r.slot];
-        if (r.t_out) std::memcpy(r.t_out, hs + L.t, cap * N * 8);
-        std::memcpy(r.u_out, hs + L.u, cap * n * N * 8);
-        std::memcpy(r.nsaved, hs + L.ns, N * 4);
-        std::memcpy(r.retcode, hs + L.rc, N * 4);
-        if (r.stats) std::memcpy(r.stats, hs + L.st, N * sizeof(ode_stats));
+// Outputs from the slot's staging into each request's buffers.
+void finish(ode_handle* h, Batch& b) {
+    const Request& r0 = b.head();
+    const size_t n = (size_t)r0.d.n_states, N = (size_t)b.N, cap = save_cap(&r0.o);
+    if (b.status == ODE_OK && b.slot >= 0 && h->slot_pinned[b.slot]) {
+        const Layout L = layout(b);
+        const char* hs = (const char*)h->slot_pinned[b.slot];
+        for (size_t q = 0; q < b.reqs.size(); ++q) {
+            Request& r = *b.reqs[q];
+            const size_t off = (size_t)b.offset[q], m = (size_t)r.N;
+            if (r.t_out)
+                for (size_t i = 0; i < cap; ++i) std::memcpy(r.t_out + i * m, hs + L.t + (i * N + off) * 8, m * 8);
+            for (size_t i = 0; i < cap * n; ++i) std::memcpy(r.u_out + i * m, hs + L.u + (i * N + off) * 8, m * 8);
+            std::memcpy(r.nsaved, hs + L.ns + off * 4, m * 4);
+            std::memcpy(r.retcode, hs + L.rc + off * 4, m * 4);
+            if (r.stats) std::memcpy(r.stats, hs + L.st + off * sizeof(ode_stats), m * sizeof(ode_stats));
+        }
     }
-    r.u0.clear(); r.u0.shrink_to_fit();
-    r.p.clear(); r.p.shrink_to_fit();
-    r.tspan.clear(); r.tspan.shrink_to_fit();
+    for (auto& rp : b.reqs) {
+        Request& r = *rp;
+        if (r.status == ODE_OK) r.status = b.status;
+        r.u0.clear(); r.u0.shrink_to_fit();
+        r.p.clear(); r.p.shrink_to_fit();
+        r.tspan.clear(); r.tspan.shrink_to_fit();
+    }
 }
 
 // Book-keeping of a finished request (lock held).
 void retire(ode_handle* h, const std::shared_ptr<Request>& r) {
-    if (r->slot >= 0) h->slot_busy[r->slot] = 0;
-    if (r->state == 1) h->hbm_in_use -= r->bytes;
     r->state = 2;
     r->t_done = mono_now();
     h->n_completed++;
     h->completed.push_back(r->ticket);
 }
+void retire(ode_handle* h, Batch& b) {
+    if (b.slot >= 0) h->slot_busy[b.slot] = 0;
+    h->hbm_in_use -= b.bytes;
+    for (auto& r : b.reqs) retire(h, r);
+}
 
-// The serving loop: retire finished requests, then admit queued ones (FIFO)
-// while a slot is free and the HBM budget allows.  A request larger than the
-// whole budget is rejected with ODE_E_NOMEM.  Copies into and out of the
+// A request that has waited this long at the head of the queue holds back
+// the admission of the requests behind it until it fits (no starvation).
+constexpr double kServeAgingSeconds = 0.25;
+// At most this many trajectories are merged into one launch.
+constexpr int64_t kServeMaxBatchTraj = 1 << 17;
+
+// The serving loop: retire finished batches, then admit queued requests while
+// a slot is free and the HBM budget allows.  A request is merged with every
+// queued request it is compatible with (up to kServeMaxBatchTraj
+// trajectories); a request that does not fit does not block the smaller ones
+// behind it, unless it has waited kServeAgingSeconds.  A request larger than
+// the whole budget is rejected with ODE_E_NOMEM.  Copies into and out of the
 // pinned staging run without the lock, so submitters are not held up.
 void serve_loop(ode_handle* h) {
     cudaSetDevice(h->device);
     std::unique_lock<std::mutex> lk(h->mu);
-    std::vector<std::shared_ptr<Request>> batch;
-    std::vector<std::pair<std::shared_ptr<Request>, int>> starts;
+    std::vector<std::shared_ptr<Batch>> done;
+    std::vector<std::shared_ptr<Batch>> starts;
     while (!h->stop) {
         bool progressed = false;
-        batch.clear();
+        done.clear();
         for (size_t i = 0; i < h->running.size();) {
-            auto r = h->running[i];
-            cudaError_t q = cudaEventQuery(h->slot_ev[r->slot]);
+            auto b = h->running[i];
+            cudaError_t q = cudaEventQuery(h->slot_ev[b->slot]);
             if (q == cudaErrorNotReady) { ++i; continue; }
-            if (q != cudaSuccess) r->status = ODE_E_CUDA;
-            batch.push_back(r);
+            if (q != cudaSuccess) b->status = ODE_E_CUDA;
+            done.push_back(b);
             h->running.erase(h->running.begin() + i);
         }
-        if (!batch.empty()) {
+        if (!done.empty()) {
             lk.unlock();
-            for (auto& r : batch) finish(h, *r);
+            for (auto& b : done) finish(h, *b);
             lk.lock();
-            for (auto& r : batch) retire(h, r);
+            for (auto& b : done) retire(h, *b);
             progressed = true;
         }
         starts.clear();
-        while (!h->pending.empty()) {
-            auto r = h->pending.front();
-            if (r->bytes > h->budget) {
-                h->pending.pop_front();
+        const double now = mono_now();
+        for (auto it = h->pending.begin(); it != h->pending.end();) {
+            auto r = *it;
+            if (r->state != 0) { it = h->pending.erase(it); continue; }   // merged into an earlier batch
+            const size_t rb = request_bytes(*r);
+            if (rb > h->budget) {
+                it = h->pending.erase(it);
                 r->status = ODE_E_NOMEM;
                 h->n_rejected++;
                 retire(h, r);
@@ -1111,33 +1188,61 @@ void serve_loop(ode_handle* h) {
                 continue;
             }
             int k = -1;
-            for (int s = 0; s < (int)h->slot_ctx.size(); ++s)
-                if (!h->slot_busy[s]) { k = s; break; }
-            if (k < 0 || h->hbm_in_use + r->bytes > h->budget) break;
-            h->pending.pop_front();
-            r->slot = k;
-            h->slot_busy[k] = 1;
-            h->hbm_in_use += r->bytes;
+            for (int sl = 0; sl < (int)h->slot_ctx.size(); ++sl)
+                if (!h->slot_busy[sl]) { k = sl; break; }
+            if (k < 0) break;
+            if (h->hbm_in_use + rb > h->budget) {
+                if (now - r->t_submit > kServeAgingSeconds) break;   // it waits no longer behind others
+                ++it;
+                continue;
+            }
+            auto b = std::make_shared<Batch>();
+            b->reqs.push_back(r);
+            b->offset.push_back(0);
+            b->N = r->N;
+            b->bytes = rb;
             r->state = 1;
-            h->n_admitted++;
-            starts.emplace_back(r, k);
+            it = h->pending.erase(it);
+            // merge compatible requests queued behind it while the budget allows
+            for (auto jt = it; jt != h->pending.end() && b->N < kServeMaxBatchTraj; ++jt) {
+                auto& q = *jt;
+                if (q->state != 0 || !mergeable(*r, *q) || b->N + q->N > kServeMaxBatchTraj) continue;
+                const size_t nb = layout(*r, b->N + q->N, true).total;
+                if (h->hbm_in_use + nb > h->budget) continue;
+                b->offset.push_back(b->N);
+                b->reqs.push_back(q);
+                b->N += q->N;
+                b->bytes = nb;
+                q->state = 1;
+            }
+            b->slot = k;
+            h->slot_busy[k] = 1;
+            h->hbm_in_use += b->bytes;
+            h->n_admitted += (long long)b->reqs.size();
+            h->n_batches++;
+            starts.push_back(b);
         }
         if (!starts.empty()) {
             lk.unlock();
-            for (auto& rk : starts) {
-                rk.first->t_start = mono_now();
-                int rc = admit(h, *rk.first, rk.second);
+            for (auto& b : starts) {
+                const double t = mono_now();
+                for (auto& r : b->reqs) r->t_start = t;
+                int rc = admit(h, *b, b->slot);
                 if (rc) {
-                    rk.first->status = rc;
-                    cudaStreamSynchronize(h->slot_ctx[rk.second].stream);
-                    if (rk.first->dmem) cudaFree(rk.first->dmem);
-                    rk.first->dmem = nullptr;
+                    b->status = rc;
+                    cudaStreamSynchronize(h->slot_ctx[b->slot].stream);
+                    if (b->dmem) cudaFree(b->dmem);
+                    b->dmem = nullptr;
                 }
             }
             lk.lock();
-            for (auto& rk : starts) {
-                if (rk.first->status != ODE_OK) retire(h, rk.first);
-                else h->running.push_back(rk.first);
+            for (auto& b : starts) {
+                if (b->status != ODE_OK) {
+                    for (auto& r : b->reqs) r->status = b->status;
+                    retire(h, *b);
+                } else {
+                    h->running.push_back(b);
+                }
             }
             progressed = true;
         }
@@ -1404,8 +1509,9 @@ int ode_submit(ode_handle* h, const ode_problem_desc* d, const ode_options* o, i
     r->nsaved = nsaved;
     r->retcode = retcode;
     r->stats = stats;
-    r->bytes = request_bytes(*r);
     std::unique_lock<std::mutex> lk(h->mu);
+    if (h->max_queued > 0 && h->pending.size() >= h->max_queued)
+        return fail(h, ODE_E_BUSY, "serving queue full (ode_set_serving_queue_limit)");
     CUDA_TRY(h, cudaSetDevice(h->device));
     rc = ensure_worker(h);
     if (rc) return rc;
@@ -1486,7 +1592,14 @@ int ode_serving_stats_get(ode_handle* h, ode_serving_stats* s) {
     s->hbm_in_use = (int64_t)h->hbm_in_use;
     s->hbm_budget = (int64_t)h->budget;
     s->slots = h->slots;
-    s->reserved = 0;
+    s->launches = (int32_t)std::min<long long>(h->n_batches, 0x7fffffff);
+    return ODE_OK;
+}
+
+int ode_set_serving_queue_limit(ode_handle* h, int64_t max_queued) {
+    if (!h || max_queued < 0) return fail(h, ODE_E_INVALID, "null handle or negative limit");
+    std::unique_lock<std::mutex> lk(h->mu);
+    h->max_queued = (size_t)max_queued;
     return ODE_OK;
 }
 

@@ -10,9 +10,18 @@ one GB300 through `libode_b200.so` (C ABI in `include/ode_gb300.h`).
     sim = solve(eprob, Rodas5P(), EnsembleGB300(); trajectories = 100_000,
                 saveat = 10 .^ range(-5, 5; length = 20), reltol = 1e-6, abstol = 1e-10)
 
-Right-hand sides are device functions compiled into the library and named by
-`GB300Model` (:linear, :lorenz, :robertson, :duffing_chain, :brusselator_1d);
-arbitrary Julia closures cannot run on the device.
+Right-hand sides are device functions: compiled into the library and named by
+`GB300Model` (:linear, :lorenz, :robertson, :duffing_chain, :brusselator_1d,
+...), or registered at run time as CUDA C++ source with `register_model`
+(the library compiles them with NVRTC); arbitrary Julia closures cannot run
+on the device.
+
+    lv = register_model("""
+        template <class T, class P> __device__ void lv_f(T* du, const T* u, const P* p, double t) {
+            du[0] = p[0] * u[0] - p[1] * u[0] * u[1];
+            du[1] = p[3] * u[0] * u[1] - p[2] * u[1];
+        }""", :lv, 2, 4)
+    prob = ODEProblem(lv, [1.0, 1.0], (0.0, 10.0), [1.5, 1.0, 3.0, 1.0])
 """
 module EnsembleGB300Ext
 
@@ -22,13 +31,13 @@ import OrdinaryDiffEqVerner: Vern7
 import OrdinaryDiffEqRosenbrock: Rodas5P, Rosenbrock23
 import OrdinaryDiffEqCore: CompositeAlgorithm, AutoSwitch
 
-export EnsembleGB300, GB300Model, GB300Callback
+export EnsembleGB300, GB300Model, GB300Callback, register_model
 
 const LIB = get(ENV, "ODE_GB300_LIB", joinpath(@__DIR__, "..", "lib", "libode_b200.so"))
 
 const MODEL_IDS = Dict(:linear => 0, :lorenz => 1, :robertson => 2, :duffing_chain => 3, :brusselator_1d => 4,
-                       :bouncing_ball => 5, :van_der_pol => 6, :pk_one_compartment => 7)
-const N_PARAMS = Dict(0 => 1, 1 => 3, 2 => 3, 3 => 3, 4 => 3, 5 => 3, 6 => 1, 7 => 3)
+                       :bouncing_ball => 5, :van_der_pol => 6, :pk_one_compartment => 7, :forced_duffing => 8)
+const N_PARAMS = Dict(0 => 1, 1 => 3, 2 => 3, 3 => 3, 4 => 3, 5 => 3, 6 => 1, 7 => 3, 8 => 5)
 
 """
     GB300Callback(; interp_points = 10, max_events = 16)
@@ -45,11 +54,33 @@ struct GB300Callback
 end
 GB300Callback(; interp_points = 10, max_events = 16) = GB300Callback(interp_points, max_events)
 
-"""Marker right-hand side naming a model compiled into the library."""
+"""Marker right-hand side naming a model compiled into the library or registered with `register_model`."""
 struct GB300Model
     name::Symbol
 end
 (m::GB300Model)(du, u, p, t) = error("GB300Model($(m.name)) only runs on the device")
+
+"""
+    register_model(source, name, n_states, n_params; jac = false, tgrad = false, nonautonomous = false)
+
+Registers a right-hand side written as CUDA C++ (`ode_register_model`): the
+source defines `template <class T, class P> __device__ void NAME_f(T* du, const
+T* u, const P* p, double t)` and, with `jac`/`tgrad`, `NAME_jac(T* J, ...)`
+(row-major) and `NAME_tgrad(T* dT, ...)`; without `jac` the Rosenbrock methods
+differentiate `NAME_f` by forward-mode AD on the device.  Returns a
+`GB300Model` usable as the `f` of an `ODEProblem`.
+"""
+function register_model(source::AbstractString, name::Symbol, n_states::Integer, n_params::Integer;
+                        jac::Bool = false, tgrad::Bool = false, nonautonomous::Bool = false)
+    flags = Int32((jac ? 1 : 0) | (tgrad ? 2 : 0) | (nonautonomous ? 4 : 0))
+    id = Ref{Int32}(0)
+    st = ccall((:ode_register_model, LIB), Cint, (Cstring, Cstring, Int32, Int32, Int32, Ref{Int32}),
+               source, String(name), Int32(n_states), Int32(n_params), flags, id)
+    st == 0 || error("ode_register_model: " * unsafe_string(ccall((:ode_last_error, LIB), Cstring, (Ptr{Cvoid},), C_NULL)))
+    MODEL_IDS[name] = Int(id[])
+    N_PARAMS[Int(id[])] = Int(n_params)
+    return GB300Model(name)
+end
 
 struct EnsembleGB300 <: SciMLBase.EnsembleAlgorithm
     precision::Symbol      # :fp64 or :mixed

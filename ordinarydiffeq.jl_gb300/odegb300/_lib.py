@@ -43,7 +43,7 @@ class Stats(C.Structure):
 class ServingStats(C.Structure):
     _fields_ = [(k, C.c_int64) for k in ("submitted", "admitted", "completed", "rejected", "queued",
                                          "running", "hbm_in_use", "hbm_budget")] + \
-               [("slots", C.c_int32), ("reserved", C.c_int32)]
+               [("slots", C.c_int32), ("launches", C.c_int32)]
 
 
 # Every exported entry point of the C ABI with its ctypes signature.
@@ -77,6 +77,7 @@ SIGNATURES = {
     "ode_next_completed": (C.c_int, [_VP, C.c_double, C.POINTER(C.c_uint64), _IP, C.POINTER(C.c_double)]),
     "ode_serving_stats_get": (C.c_int, [_VP, C.POINTER(ServingStats)]),
     "ode_set_serving_slots": (C.c_int, [_VP, C.c_int32]),
+    "ode_set_serving_queue_limit": (C.c_int, [_VP, C.c_int64]),
     "ode_abort": (C.c_int, [_VP]),
     "ode_kernel_launches": (C.c_int, [_VP, C.POINTER(C.c_int64)]),
     "ode_last_kernel_ms": (C.c_int, [_VP, _DP]),

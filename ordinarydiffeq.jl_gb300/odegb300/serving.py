@@ -40,12 +40,16 @@ def pick_precision(precision, reltol, model=None):
 
 
 class Server:
-    def __init__(self, device=0, hbm_budget=0, slots=8):
+    """queue_limit > 0: submit() sheds a request (returns None) while that many
+    wait, instead of queuing without bound."""
+
+    def __init__(self, device=0, hbm_budget=0, slots=8, queue_limit=0):
         self.L = _lib.load()
         hp = C.c_void_p(0)
         _lib.check(self.L.ode_create(device, int(hbm_budget), C.byref(hp)))
         self.h = hp
         _lib.check(self.L.ode_set_serving_slots(self.h, int(slots)), self.h)
+        _lib.check(self.L.ode_set_serving_queue_limit(self.h, int(queue_limit)), self.h)
         self.live = {}
 
     def close(self):
@@ -62,7 +66,8 @@ class Server:
     def submit(self, model, alg, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=1e-6, precision="fp64",
                ir_sweeps=-1, tag=None, tstops=None):
         """Queue one packed ensemble; returns its ticket at once (the library
-        copies the inputs, tstops included, before this returns)."""
+        copies the inputs, tstops included, before this returns), or None when
+        the server's queue is full (the request was shed)."""
         name = model if isinstance(model, str) else None
         if isinstance(model, str):
             model = MODELS[model]
@@ -83,11 +88,13 @@ class Server:
         dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
         ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))
         ticket = C.c_uint64(0)
-        _lib.check(self.L.ode_submit(self.h, C.byref(d), C.byref(o), N, None, dp(u0s), dp(ps), dp(tspans),
-                                     dp(sv.values) if sv.nsave else None, dp(out["t"]), dp(out["u"]),
-                                     ip(out["nsaved"]), ip(out["retcode"]),
-                                     out["stats"].ctypes.data_as(C.POINTER(_lib.Stats)), C.byref(ticket)),
-                   self.h)
+        st = self.L.ode_submit(self.h, C.byref(d), C.byref(o), N, None, dp(u0s), dp(ps), dp(tspans),
+                               dp(sv.values) if sv.nsave else None, dp(out["t"]), dp(out["u"]),
+                               ip(out["nsaved"]), ip(out["retcode"]),
+                               out["stats"].ctypes.data_as(C.POINTER(_lib.Stats)), C.byref(ticket))
+        if st == -5:   # ODE_E_BUSY: queue full
+            return None
+        _lib.check(st, self.h)
         self.live[ticket.value] = (out, N, tag, prec)
         return ticket.value
 
@@ -140,14 +147,15 @@ def serving_mix(n_requests, seed=0, max_traj=4096):
 def run_open_loop(server, requests, rate, duration, seed=1, precision="auto", drain_timeout=120.0):
     """Poisson arrivals at `rate` requests/s for `duration` seconds, cycling
     through `requests`.  Latency = completion (outputs in the caller's
-    buffers) minus the scheduled arrival time."""
+    buffers) minus the scheduled arrival time.  Requests the server sheds
+    (queue full) are counted, not retried."""
     rng = np.random.default_rng(seed)
     clock = lambda: time.clock_gettime(time.CLOCK_MONOTONIC)
     t0 = clock() + 0.01
     end = t0 + duration
     nxt = t0 + rng.exponential(1.0 / rate)
     arrival = {}
-    lat, wait, ntraj_done, failures = [], [], 0, 0
+    lat, wait, ntraj_done, failures, shed = [], [], 0, 0, 0
     first_done, last_done = None, None
     i = 0
     submitted = 0
@@ -176,8 +184,11 @@ def run_open_loop(server, requests, rate, duration, seed=1, precision="auto", dr
             i += 1
             tk = server.submit(r["model"], r["alg"], r["u0s"], r["ps"], r["tspans"], r["saveat"], r["reltol"],
                                r["abstol"], precision=precision, ir_sweeps=r["ir_sweeps"])
-            arrival[tk] = nxt
-            submitted += 1
+            if tk is None:
+                shed += 1
+            else:
+                arrival[tk] = nxt
+                submitted += 1
             nxt += rng.exponential(1.0 / rate)
         collect(max(0.0, min(nxt, end) - clock()))
     deadline = clock() + drain_timeout
@@ -187,8 +198,10 @@ def run_open_loop(server, requests, rate, duration, seed=1, precision="auto", dr
     wait = np.array(wait)
     span = (last_done - t0) if last_done is not None else float("nan")
     pct = lambda a, q: float(np.percentile(a, q) * 1e3) if len(a) else None
+    st = server.stats()
     return {"offered_rate": rate, "duration_s": duration, "submitted": submitted, "completed": int(len(lat)),
-            "failed": failures, "unfinished": len(arrival),
+            "failed": failures, "unfinished": len(arrival), "shed_queue_full": shed,
+            "launches_total": st["launches"],
             "requests_per_s": len(lat) / span if span == span and span > 0 else None,
             "trajectories_per_s": ntraj_done / span if span == span and span > 0 else None,
             "latency_ms": {"p50": pct(lat, 50), "p90": pct(lat, 90), "p99": pct(lat, 99), "max": pct(lat, 100)},

@@ -114,3 +114,27 @@ def compare(g, o, reltol, abstol, factor=10.0, step_slack=1):
     return {"ok": bool(ok.all()), "worst_ratio": worst, "max_step_diff": int(dsteps.max()),
             "frac_bit_identical": float(identical.mean()),
             "steps_ok": bool((dsteps <= step_slack).all())}
+
+
+def assert_mixed_accuracy(model, alg, g, u0, p, ts, saveat, rt, at, stiff=False, n_per_traj=None):
+    """The mixed form's accuracy bar.  (1) Equal accuracy: its error against a
+    ground-truth solve is within 2x the FP64 form's (+1 tolerance unit) at the
+    median and p90.  (2) Against the FP64 oracle at the same tolerance it is no
+    further off than the FP64 kernel itself is when u0 is perturbed by one FP32
+    rounding (1 + 2^-24) -- the spread the problem's conditioning and the step
+    sequence give -- within 2x (+1 unit) at the median, p90 and p99.  Returns the
+    per-trajectory errors against the oracle."""
+    kw = {"n_per_traj": n_per_traj} if n_per_traj is not None else {}
+    g64 = gpu(model, alg, u0, p, ts, saveat, rt, at, **kw)
+    tr = truth(model, u0, p, ts, saveat, n_per_traj=n_per_traj, stiff=stiff)
+    emx, e64 = err_vs(g, tr, rt, at), err_vs(g64, tr, rt, at)
+    for q in (50, 90):
+        a, b = np.percentile(emx, q), np.percentile(e64, q)
+        assert a <= 2.0 * b + 1.0, ("vs ground truth", q, a, b)
+    o = oracle(model, alg, u0, p, ts, saveat, rt, at, n_per_traj=n_per_traj)
+    ctl = gpu(model, alg, u0 * (1.0 + 2.0 ** -24), p, ts, saveat, rt, at, **kw)
+    d, dc = err_vs(g, o, rt, at), err_vs(ctl, o, rt, at)
+    for q in (50, 90, 99):
+        a, b = np.percentile(d, q), np.percentile(dc, q)
+        assert a <= 2.0 * b + 1.0, ("vs FP64 oracle, beside the perturbed-u0 control", q, a, b)
+    return d
