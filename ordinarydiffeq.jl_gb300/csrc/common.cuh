@@ -22,6 +22,8 @@ namespace odegb {
 // the two type traits the kernels use (std's, which NVRTC lacks)
 template <bool B> struct bool_constant { static constexpr bool value = B; };
 template <class...> using void_t = void;
+template <class T> struct is_double : bool_constant<false> {};
+template <> struct is_double<double> : bool_constant<true> {};
 
 // ------------------------------------------------------------------ scalars
 template <class T> struct Arith;

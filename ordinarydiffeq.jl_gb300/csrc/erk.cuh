@@ -52,6 +52,55 @@ __device__ __forceinline__ ff split_weight(double w) {
     return ff(h, (float)(w - (double)h));
 }
 
+// Interpolation weights of a save computed lane-parallel within a lane group.
+// Every lane of a group needs the same NW weights b_q(theta) (Horner in FP64);
+// on GB300 an FP64 warp instruction occupies the FP64 pipe as long with one
+// active lane as with 32, so a group of L lanes evaluates them L at a time --
+// lane l the weights l, l + L, ... -- and shares them by shuffles: ceil(NW/L)
+// rounds of FP64 work per save instead of NW.  The arithmetic of each weight is
+// the sequential form's (interp_weight), so results are unchanged.  A table row
+// holds the polynomial's coefficients, read at run time by the lane that owns it.
+#define ODEGB_R5(i) {tab::TSIT5_R(i, 0), tab::TSIT5_R(i, 1), tab::TSIT5_R(i, 2), tab::TSIT5_R(i, 3), tab::TSIT5_R(i, 4)}
+#define ODEGB_R8(i)                                                                                      \
+    {tab::VERN7_R(i, 0), tab::VERN7_R(i, 1), tab::VERN7_R(i, 2), tab::VERN7_R(i, 3), tab::VERN7_R(i, 4), \
+     tab::VERN7_R(i, 5), tab::VERN7_R(i, 6), tab::VERN7_R(i, 7)}
+// weight q of Tsit5 belongs to stage q + 1; Vern7's 13 weights to stages 1, 4-9, 11-16
+static __device__ double kTsit5InterpR[7][5] = {ODEGB_R5(1), ODEGB_R5(2), ODEGB_R5(3), ODEGB_R5(4),
+                                                ODEGB_R5(5), ODEGB_R5(6), ODEGB_R5(7)};
+static __device__ double kVern7InterpR[13][8] = {ODEGB_R8(1),  ODEGB_R8(4),  ODEGB_R8(5),  ODEGB_R8(6), ODEGB_R8(7),
+                                                 ODEGB_R8(8),  ODEGB_R8(9),  ODEGB_R8(11), ODEGB_R8(12),
+                                                 ODEGB_R8(13), ODEGB_R8(14), ODEGB_R8(15), ODEGB_R8(16)};
+#undef ODEGB_R5
+#undef ODEGB_R8
+template <int NPOLY>
+__device__ __forceinline__ double interp_weight_row(double th, const double* r, bool first) {
+    double acc = r[NPOLY - 1];
+#pragma unroll
+    for (int q = NPOLY - 2; q >= 2; --q) acc = fma(th, acc, r[q]);
+    if (first) acc = fma(th, acc, r[1]);
+    return first ? th * acc : (th * th) * acc;
+}
+// b[q] for q < NW as double (FP64 form) or float pairs (mixed form); row(q) the
+// coefficient row of weight q; weight 0 is the `first` one (degree from 1).
+template <int NW, int NPOLY, int L, class B, class Row>
+__device__ __forceinline__ void group_weights(B* b, double th, const Group<L>& g, Row row) {
+#pragma unroll
+    for (int q0 = 0; q0 < NW; q0 += L) {
+        const int q = q0 + g.lane;
+        double w = 0.0;
+        if (q < NW) w = interp_weight_row<NPOLY>(th, row(q), q == 0);
+        if constexpr (is_double<B>::value) {
+#pragma unroll
+            for (int k = 0; k < L; ++k)
+                if (q0 + k < NW) b[q0 + k] = g.from(w, k);
+        } else {                          // float pair, split by the owning lane
+            const float hi = (float)w, lo = (float)(w - (double)hi);
+#pragma unroll
+            for (int k = 0; k < L; ++k)
+                if (q0 + k < NW) b[q0 + k] = ff(g.from(hi, k), g.from(lo, k));
+        }
+    }
+}
 struct Tsit5Alg {
     static constexpr int ORDER = 5;
     static constexpr bool IMPLICIT = false;
@@ -139,14 +188,19 @@ struct Tsit5Alg {
 
     template <class Model, class R, int L, int C>
     __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, double th, double dt, double,
-                                       const R* y0, const R* y0lo, const R*, const R*, const PR<R>*, const Group<L>&) {
+                                       const R* y0, const R* y0lo, const R*, const R*, const PR<R>*,
+                                       const Group<L>& g) {
         auto r = [](int i, int q) { return tab::TSIT5_R(i, q); };
         const R d = (R)dt;
         if constexpr (sizeof(R) == 8) {
             double b[8];
-            b[1] = interp_weight<5>(th, 1, r, true);
+            if constexpr (L > 1) {
+                group_weights<7, 5, L>(b + 1, th, g, [](int q) { return (const double*)kTsit5InterpR[q]; });
+            } else {
+                b[1] = interp_weight<5>(th, 1, r, true);
 #pragma unroll
-            for (int i = 2; i <= 7; ++i) b[i] = interp_weight<5>(th, i, r, false);
+                for (int i = 2; i <= 7; ++i) b[i] = interp_weight<5>(th, i, r, false);
+            }
 #pragma unroll
             for (int i = 0; i < C; ++i) {
                 R acc = c.k[6][i] * (R)b[7];
@@ -157,9 +211,13 @@ struct Tsit5Alg {
         } else {
             const R dl = Acc<R>::dt_lo(dt, d);
             ff b[8];
-            b[1] = split_weight(interp_weight<5>((double)th, 1, r, true));
+            if constexpr (L > 1) {
+                group_weights<7, 5, L>(b + 1, th, g, [](int q) { return (const double*)kTsit5InterpR[q]; });
+            } else {
+                b[1] = split_weight(interp_weight<5>((double)th, 1, r, true));
 #pragma unroll
-            for (int i = 2; i <= 7; ++i) b[i] = split_weight(interp_weight<5>((double)th, i, r, false));
+                for (int i = 2; i <= 7; ++i) b[i] = split_weight(interp_weight<5>((double)th, i, r, false));
+            }
 #pragma unroll
             for (int i = 0; i < C; ++i) {
                 CSum cs;
@@ -262,9 +320,13 @@ struct Vern7Alg {
         const R d = (R)dt;
         if constexpr (sizeof(R) == 8) {
             double b[13];
-            b[0] = interp_weight<8>(th, 1, r, true);
+            if constexpr (L > 1) {
+                group_weights<13, 8, L>(b, th, g, [](int q) { return (const double*)kVern7InterpR[q]; });
+            } else {
+                b[0] = interp_weight<8>(th, 1, r, true);
 #pragma unroll
-            for (int q = 1; q < 13; ++q) b[q] = interp_weight<8>(th, idx[q], r, false);
+                for (int q = 1; q < 13; ++q) b[q] = interp_weight<8>(th, idx[q], r, false);
+            }
 #pragma unroll
             for (int i = 0; i < C; ++i) {
                 R acc = c.s[Vern7Tab::slot(16)][i] * (R)b[12];
@@ -275,9 +337,13 @@ struct Vern7Alg {
         } else {
             const R dl = Acc<R>::dt_lo(dt, d);
             ff b[13];
-            b[0] = split_weight(interp_weight<8>((double)th, 1, r, true));
+            if constexpr (L > 1) {
+                group_weights<13, 8, L>(b, th, g, [](int q) { return (const double*)kVern7InterpR[q]; });
+            } else {
+                b[0] = split_weight(interp_weight<8>((double)th, 1, r, true));
 #pragma unroll
-            for (int q = 1; q < 13; ++q) b[q] = split_weight(interp_weight<8>((double)th, idx[q], r, false));
+                for (int q = 1; q < 13; ++q) b[q] = split_weight(interp_weight<8>((double)th, idx[q], r, false));
+            }
 #pragma unroll
             for (int i = 0; i < C; ++i) {
                 CSum cs;
