@@ -124,6 +124,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="robertson", choices=sorted(CONFIGS))
     ap.add_argument("--trajectories", type=int, default=0)
+    ap.add_argument("--lanes", type=int, default=0, help="lanes per trajectory of the device solves (0: default)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU-baseline sample time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-small", action="store_true",
@@ -368,7 +369,7 @@ def measure(cfg, args, ctx, steps, warmup, headline=False):
 
     def solve_device(prec, ir=None, u0=None, p=None):
         ens = odegb300.EnsembleGB300(precision=prec, ir_sweeps=(ir_default if ir is None else ir)
-                                     if prec == "mixed" else -1)
+                                     if prec == "mixed" else -1, lanes_per_traj=args.lanes)
         o = _options(wl["reltol"], wl["abstol"], None, None, None, 1000000, sv, ens, None, None, cb)
         if t_tst is not None:   # the device entry point takes tstops in device memory, sorted
             o.ntstops = int(t_tst.numel())

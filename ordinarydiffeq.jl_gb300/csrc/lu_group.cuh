@@ -233,14 +233,34 @@ struct SmemLA {
             // updates its rows.  Each row receives its updates in the same
             // column order as the column-by-column form (identical results)
             // with 1/C of the dependent shuffle rounds.
+            // The lane's C x C entries of block column q are loaded one round
+            // ahead (wn), so the shared-memory latency stays off the chain of
+            // dependent rounds (for C <= 2; wider rows would spill registers).
+            constexpr bool PF = C <= 2;
+            R wn[C][C];
+#pragma unroll
+            for (int i = 0; i < C; ++i)
+#pragma unroll
+                for (int k = 0; k < C; ++k) wn[i][k] = W[at<L, C>(i, g.lane, k)];
 #pragma unroll 1
             for (int q = 0; q < L; ++q) {
+                R w[C][C];
+#pragma unroll
+                for (int i = 0; i < C; ++i)
+#pragma unroll
+                    for (int k = 0; k < C; ++k) w[i][k] = PF ? wn[i][k] : W[at<L, C>(i, g.lane, q * C + k)];
+                if (PF && q + 1 < L) {
+#pragma unroll
+                    for (int i = 0; i < C; ++i)
+#pragma unroll
+                        for (int k = 0; k < C; ++k) wn[i][k] = W[at<L, C>(i, g.lane, (q + 1) * C + k)];
+                }
                 R y[C];
 #pragma unroll
                 for (int i = 0; i < C; ++i) {
                     R acc = b[i];
 #pragma unroll
-                    for (int k = 0; k < i; ++k) acc = FMA(-W[at<L, C>(i, g.lane, q * C + k)], y[k], acc);
+                    for (int k = 0; k < i; ++k) acc = FMA(-w[i][k], y[k], acc);
                     y[i] = acc;
                 }
 #pragma unroll
@@ -252,18 +272,40 @@ struct SmemLA {
 #pragma unroll
                     for (int i = 0; i < C; ++i)
 #pragma unroll
-                        for (int k = 0; k < C; ++k) b[i] = FMA(-W[at<L, C>(i, g.lane, q * C + k)], y[k], b[i]);
+                        for (int k = 0; k < C; ++k) b[i] = FMA(-w[i][k], y[k], b[i]);
                 }
             }
+#pragma unroll
+            for (int i = 0; i < C; ++i)
+#pragma unroll
+                for (int k = 0; k < C; ++k) wn[i][k] = W[at<L, C>(i, g.lane, (L - 1) * C + k)];
+            R dn[C];
+#pragma unroll
+            for (int i = 0; i < C; ++i) dn[i] = s.dinv[(L - 1) * C + i];
 #pragma unroll 1
             for (int q = L - 1; q >= 0; --q) {
+                R w[C][C], dv[C];
+#pragma unroll
+                for (int i = 0; i < C; ++i) {
+                    dv[i] = PF ? dn[i] : s.dinv[q * C + i];
+#pragma unroll
+                    for (int k = 0; k < C; ++k) w[i][k] = PF ? wn[i][k] : W[at<L, C>(i, g.lane, q * C + k)];
+                }
+                if (PF && q > 0) {
+#pragma unroll
+                    for (int i = 0; i < C; ++i) {
+                        dn[i] = s.dinv[(q - 1) * C + i];
+#pragma unroll
+                        for (int k = 0; k < C; ++k) wn[i][k] = W[at<L, C>(i, g.lane, (q - 1) * C + k)];
+                    }
+                }
                 R x[C];
 #pragma unroll
                 for (int i = C - 1; i >= 0; --i) {
                     R acc = b[i];
 #pragma unroll
-                    for (int k = C - 1; k > i; --k) acc = FMA(-W[at<L, C>(i, g.lane, q * C + k)], x[k], acc);
-                    x[i] = acc * s.dinv[q * C + i];
+                    for (int k = C - 1; k > i; --k) acc = FMA(-w[i][k], x[k], acc);
+                    x[i] = acc * dv[i];
                 }
 #pragma unroll
                 for (int k = 0; k < C; ++k) x[k] = g.from(x[k], q);
@@ -274,7 +316,7 @@ struct SmemLA {
 #pragma unroll
                     for (int i = 0; i < C; ++i)
 #pragma unroll
-                        for (int k = C - 1; k >= 0; --k) b[i] = FMA(-W[at<L, C>(i, g.lane, q * C + k)], x[k], b[i]);
+                        for (int k = C - 1; k >= 0; --k) b[i] = FMA(-w[i][k], x[k], b[i]);
                 }
             }
             return;
