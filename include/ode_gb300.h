@@ -85,8 +85,27 @@ enum ode_model_flags {
     ODE_MODEL_HAS_JAC = 1,        /* the source defines NAME_jac (else the Rosenbrock methods take J by
                                      forward-mode AD of NAME_f, one counted f call per Jacobian) */
     ODE_MODEL_HAS_TGRAD = 2,      /* the source defines NAME_tgrad, df/dt */
-    ODE_MODEL_NONAUTONOMOUS = 4   /* NAME_f reads t (the Rosenbrock methods then need NAME_tgrad) */
+    ODE_MODEL_NONAUTONOMOUS = 4,  /* NAME_f reads t (the Rosenbrock methods then need NAME_tgrad) */
+    /* Callbacks registered with the model (active when ode_options.callback = 1), each a plain
+     * FP64 device function of the state u (n), the parameters p and t:
+     *   ContinuousCallback:  double NAME_condition(const double* u, const double* p, double t);
+     *                        int NAME_affect(double* u, const double* p, double t, int upcrossing);
+     *   VectorContinuousCallback (len conditions):
+     *                        void NAME_vcondition(double* out, const double* u, const double* p, double t);
+     *                        int NAME_vaffect(double* u, const double* p, double t, const int* events);
+     *                        (events[k]: +1 upcrossing, -1 downcrossing, 0 not fired)
+     *   DiscreteCallback:    int NAME_dcondition(const double* u, const double* p, double t);
+     *                        int NAME_daffect(double* u, const double* p, double t);
+     * An affect that returns nonzero calls terminate! (ReturnCode.Terminated).  SciMLBase's
+     * defaults: save_positions = (true, true); continuous: interp_points (ode_options),
+     * LeftRootFind, abstol = 10eps(), repeat_nudge = 1//100. */
+    ODE_MODEL_CONTINUOUS_CALLBACK = 8,
+    ODE_MODEL_CALLBACK_AFFECT = 16,      /* the ContinuousCallback acts on upcrossings (affect!) */
+    ODE_MODEL_CALLBACK_AFFECT_NEG = 32,  /* ... and/or on downcrossings (affect_neg!) */
+    ODE_MODEL_VECTOR_CALLBACK = 64,      /* with ODE_MODEL_CALLBACK_LEN(len), 1 <= len <= 32 */
+    ODE_MODEL_DISCRETE_CALLBACK = 128
 };
+#define ODE_MODEL_CALLBACK_LEN(len) ((len) << 16)
 
 /* FP64: every operation in double (the reference's arithmetic).
  * MIXED: state and stage arithmetic in FP32 (and, for Rodas5P, the W

@@ -108,8 +108,26 @@ double ctrl_pow(double x, double y) {
 //   the Oregonator (Field-Koros-Noyes, the stiff test problem of Hairer and
 //     Wanner's "Solving ODEs II", sec. IV.10): y1' = s (y2 + y1 (1 - q y1 - y2)),
 //     y2' = (y3 - (1 + y1) y2) / s, y3' = w (y1 - y3), p = (s, w, q).
+// Two models for the tests of callbacks registered with a model (defined by
+// those tests, not the reference):
+//   a ball in a box, u = (x, y, vx, vy), p = (g, e, W): x' = vx, y' = vy,
+//     vx' = 0, vy' = -g, with a VectorContinuousCallback of three conditions
+//     (y: the floor; x and W - x: the walls) whose affect! reflects vy with
+//     restitution e at the floor and vx at a wall;
+//   a state-triggered dose, u = (c), p = (k, threshold, dose): c' = -k c, with a
+//     DiscreteCallback whose condition is c < threshold and whose affect! adds
+//     the dose.
 void rhs(int model, int n, const double* u, const double* p, double t, double* du) {
     switch (model) {
+    case ORC_BALL_BOX:
+        du[0] = u[2];
+        du[1] = u[3];
+        du[2] = 0.0;
+        du[3] = -p[0];
+        break;
+    case ORC_THRESHOLD_DOSE:
+        du[0] = -p[0] * u[0];
+        break;
     case ORC_LOTKA_VOLTERRA:
         du[0] = p[0] * u[0] - p[1] * u[0] * u[1];
         du[1] = p[3] * u[0] * u[1] - p[2] * u[1];
@@ -184,6 +202,13 @@ void jac(int model, int n, const double* u, const double* p, double t, double* J
     (void)t;
     std::memset(J, 0, sizeof(double) * n * n);
     switch (model) {
+    case ORC_BALL_BOX:
+        J[2] = 1.0;
+        J[7] = 1.0;
+        break;
+    case ORC_THRESHOLD_DOSE:
+        J[0] = -p[0];
+        break;
     case ORC_LOTKA_VOLTERRA:
         J[0] = p[0] - p[1] * u[1]; J[1] = -p[1] * u[0];
         J[2] = p[3] * u[1];        J[3] = p[3] * u[0] - p[2];
@@ -326,6 +351,7 @@ struct Integ {
     // continuous callback state (integrator.event_last_time, last_event_error)
     int event_last_time;
     double last_event_error;
+    bool prev_events[8];   // the components of the last vector event
     bool reeval_fsal, terminated;
     std::vector<double> cb_tmp;
 };
@@ -939,8 +965,9 @@ constexpr double CB_ABSTOL = 10.0 * 2.220446049250313e-16;
 constexpr double CB_REPEAT_NUDGE = 0.01;
 
 bool model_has_event(int model) { return model == ORC_BOUNCING_BALL; }
-// The dosing model's registered DiscreteCallback (condition t in tstops).
-bool model_has_discrete(int model) { return model == ORC_PK1; }
+// the ball in a box's VectorContinuousCallback, its number of conditions
+bool model_has_vector_event(int model) { return model == ORC_BALL_BOX; }
+constexpr int BOX_EVENTS = 3;
 double event_condition(int model, const double* u) { (void)model; return u[0]; }
 bool event_has_affect(int) { return false; }
 bool event_has_affect_neg(int) { return true; }
@@ -1140,25 +1167,216 @@ void apply_discrete_callback(Integ& I) {
     push_save(I, I.t, I.u.data());
 }
 
-// handle_callbacks! (integrator_utils.jl:1081-1132) for one continuous callback.
+// ---- VectorContinuousCallback (the ball in a box)
+void vector_conditions(Integ& I, const double* v, double* out) {
+    out[0] = v[1];
+    out[1] = v[0];
+    out[2] = I.p[2] - v[0];
+}
+// get_condition for a vector callback: u at t, uprev at tprev, else the interpolant
+void vcond_at(Integ& I, double abst, double* out) {
+    const double* v;
+    if (abst == I.t) {
+        v = I.u.data();
+    } else if (abst == I.tprev) {
+        v = I.uprev.data();
+    } else {
+        interpolate(I, (abst - I.tprev) / I.dt, I.cb_tmp.data());
+        v = I.cb_tmp.data();
+    }
+    vector_conditions(I, v, out);
+}
+// one component of the vector condition, as a function of t (find_root's zero_func)
+double find_root_left_component(Integ& I, int k, double a, double b, double fa, double fb) {
+    int side = 0;
+    double w_prev = b - a, w_prev2 = 2.0 * (b - a);
+    double o[BOX_EVENTS];
+    for (int it = 0; it < 2200; ++it) {
+        const double w = b - a;
+        double m = (w > 0.5 * w_prev2) ? a + w * 0.5 : a + w * (fa / (fa - fb));
+        if (!(m > a && m < b)) m = a + w * 0.5;
+        if (!(m > a && m < b)) break;
+        vcond_at(I, m, o);
+        const double fm = o[k];
+        if (fm == 0.0) return m;
+        w_prev2 = w_prev;
+        w_prev = w;
+        if ((fm > 0.0) == (fa > 0.0)) {
+            if (side == -1) {
+                const double g = 1.0 - fm / fa;
+                fb *= g > 0.0 ? g : 0.5;
+            }
+            a = m;
+            fa = fm;
+            side = -1;
+        } else {
+            if (side == +1) {
+                const double g = 1.0 - fm / fb;
+                fa *= g > 0.0 ? g : 0.5;
+            }
+            b = m;
+            fb = fm;
+            side = +1;
+        }
+    }
+    return a;
+}
+
+// find_callback_time(integrator, ::VectorContinuousCallback, idx)
+// (lib/DiffEqBase/src/callbacks.jl:239-362), check_event_occurrence (:428-458)
+// and findall_events! (:495-523).  events[k]: -sign(bottom sign) for the
+// components that fire at the earliest root, 0 else.
+bool find_vector_callback_time(Integ& I, double& cb_t, int* events, double& residual) {
+    const int M = BOX_EVENTS;
+    double bc[M], bs[M], nc[M], tc[M];
+    vcond_at(I, I.tprev, bc);
+    for (int i = 0; i < M; ++i) {
+        bs[i] = jsign(bc[i]);
+        nc[i] = bc[i];
+        events[i] = 0;
+    }
+    double nudged_t = I.tprev;
+    if (I.event_last_time == 1) {
+        double minc = 0.0, mina = INFINITY;
+        for (int i = 0; i < M; ++i)
+            if (I.prev_events[i] && std::fabs(bc[i]) < mina) {
+                mina = std::fabs(bc[i]);
+                minc = bc[i];
+            }
+        if (std::fabs(minc - I.last_event_error) <= CB_ABSTOL) nudged_t = I.tprev + I.dt * CB_REPEAT_NUDGE;
+        vcond_at(I, nudged_t, nc);
+        for (int i = 0; i < M; ++i)
+            if (I.prev_events[i]) bs[i] = jsign(nc[i]);
+    }
+    bool ev[M];
+    auto fire = [&](const double* top) {
+        bool any = false;
+        for (int i = 0; i < M; ++i) {
+            ev[i] = bs[i] != 0.0 && bs[i] * jsign(top[i]) <= 0.0;
+            any = any || ev[i];
+        }
+        return any;
+    };
+    double top_t = I.t;
+    vcond_at(I, top_t, tc);
+    bool occ = fire(tc);
+    bool any_zero = false;
+    for (int i = 0; i < M; ++i) any_zero = any_zero || !ev[i];
+    if (I.o.interp_points != 0 && any_zero) {
+        const int m = I.o.interp_points;
+        for (int i = 2; i <= m; ++i) {
+            top_t = i == m ? I.t : I.tprev + (I.t - I.tprev) * ((double)(i - 1) / (double)(m - 1));
+            vcond_at(I, top_t, tc);
+            occ = fire(tc);
+            if (occ) break;
+        }
+    }
+    residual = 0.0;
+    if (!occ) {
+        cb_t = I.t;
+        return false;
+    }
+    cb_t = std::nextafter(top_t, INFINITY);   // rightfloat(top_t, tdir)
+    for (int i = 0; i < M; ++i) {
+        if (!ev[i]) continue;
+        double cbi;
+        if (jsign(tc[i]) == 0.0) {
+            cbi = top_t;
+        } else if (I.event_last_time == 1 && I.prev_events[i]) {
+            cbi = find_root_left_component(I, i, nudged_t, top_t, nc[i], tc[i]);
+        } else {
+            cbi = find_root_left_component(I, i, I.tprev, top_t, bc[i], tc[i]);
+        }
+        if (cbi < cb_t)
+            for (int k = 0; k < M; ++k) events[k] = 0;
+        if (cbi <= cb_t) {
+            cb_t = cbi;
+            double o[M];
+            vcond_at(I, cbi, o);
+            residual = o[i];
+            events[i] = bs[i] < 0.0 ? 1 : -1;
+        }
+    }
+    return true;
+}
+
+// apply_callback! (callbacks.jl:557-643) for the VectorContinuousCallback: affect!
+// gets the events' directions; the ball reflects vy at the floor (restitution
+// e = p[2]) and vx at a wall.
+void apply_vector_callback(Integ& I, double cb_t, const int* events) {
+    if (I.o.adaptive) {
+        I.dtpropose = jmax(std::nextafter(I.o.dtmin, INFINITY), 1.0 * I.dt);
+        I.dtcache = I.dtpropose;
+    }
+    if (cb_t != I.t) {
+        interpolate(I, (cb_t - I.tprev) / I.dt, I.u.data());
+        I.t = cb_t;
+        I.dt = I.t - I.tprev;
+        recompute_step_k(I);
+        I.reeval_fsal = true;
+    }
+    const int before = I.nsaved;
+    const double last_before = I.last_saved_t;
+    savevalues(I);
+    const bool savedexactly = I.nsaved > before && I.last_saved_t == I.t && !(last_before == I.t);
+    if (!savedexactly) push_save(I, I.t, I.u.data());
+    if (events[0] != 0) I.u[3] = -I.p[1] * I.u[3];
+    if (events[1] != 0 || events[2] != 0) I.u[2] = -I.u[2];
+    recompute_step_k(I);
+    I.reeval_fsal = true;
+    push_save(I, I.t, I.u.data());
+}
+
+// apply_discrete_callback! (callbacks.jl:645-682) for the state-triggered dose:
+// condition c < threshold, affect! c += dose.  Returns saved_in_cb.
+bool apply_threshold_callback(Integ& I) {
+    if (!(I.u[0] < I.p[1])) return false;
+    const int before = I.nsaved;
+    const double last_before = I.last_saved_t;
+    savevalues(I);
+    const bool savedexactly = I.nsaved > before && I.last_saved_t == I.t && !(last_before == I.t);
+    if (!savedexactly) push_save(I, I.t, I.u.data());
+    I.u[0] += I.p[2];
+    I.reeval_fsal = true;
+    push_save(I, I.t, I.u.data());
+    return true;
+}
+
+// handle_callbacks! (integrator_utils.jl:1081-1132): the model's continuous
+// callback (scalar or vector), then its discrete one; savevalues! unless the
+// discrete callbacks (if any), else the continuous one, saved.
 void handle_callbacks(Integ& I) {
-    if (I.o.callback && model_has_discrete(I.model)) {
+    if (I.o.callback && I.model == ORC_PK1) {
         apply_discrete_callback(I);
         return;
     }
-    if (!I.o.callback || !model_has_event(I.model)) {
-        savevalues(I);
-        return;
+    bool saved_in_cb = false;
+    if (I.o.callback && model_has_event(I.model)) {
+        double cb_t, bs, residual;
+        if (find_callback_time(I, cb_t, bs, residual)) {
+            I.event_last_time = 1;
+            I.last_event_error = residual;
+            apply_callback(I, cb_t, bs);
+            saved_in_cb = true;
+        } else {
+            I.event_last_time = 0;
+        }
     }
-    double cb_t, bs, residual;
-    if (find_callback_time(I, cb_t, bs, residual)) {
-        I.event_last_time = 1;
-        I.last_event_error = residual;
-        apply_callback(I, cb_t, bs);
-    } else {
-        I.event_last_time = 0;
-        savevalues(I);
+    if (I.o.callback && model_has_vector_event(I.model)) {
+        double cb_t, residual;
+        int events[BOX_EVENTS];
+        if (find_vector_callback_time(I, cb_t, events, residual)) {
+            I.event_last_time = 1;
+            I.last_event_error = residual;
+            for (int k = 0; k < BOX_EVENTS; ++k) I.prev_events[k] = events[k] != 0;
+            apply_vector_callback(I, cb_t, events);
+            saved_in_cb = true;
+        } else {
+            I.event_last_time = 0;
+        }
     }
+    if (I.o.callback && I.model == ORC_THRESHOLD_DOSE) saved_in_cb = apply_threshold_callback(I);
+    if (!saved_in_cb) savevalues(I);
 }
 
 // _loopfooter!: integrator_utils.jl:597-677.
@@ -1365,6 +1583,7 @@ int solve_one(Integ& I, const double* u0) {
     I.last_saved_t = NAN;
     I.event_last_time = 0;
     I.last_event_error = 0.0;
+    for (bool& b : I.prev_events) b = false;
     I.reeval_fsal = false;
     I.terminated = false;
     I.cb_tmp.assign(n, 0.0);

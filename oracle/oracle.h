@@ -23,7 +23,7 @@ enum { ORC_TSIT5 = 0, ORC_VERN7 = 1, ORC_RODAS5P = 2, ORC_VERN9 = 3, ORC_ROSENBR
        ORC_AUTOTSIT5_ROSENBROCK23 = 5 /* AutoTsit5(Rosenbrock23()) */ };
 enum { ORC_LINEAR = 0, ORC_LORENZ = 1, ORC_ROBERTSON = 2, ORC_DUFFING = 3, ORC_BRUSSELATOR = 4, ORC_BOUNCING_BALL = 5,
        ORC_VANDERPOL = 6, ORC_PK1 = 7, ORC_FORCED_DUFFING = 8,
-       ORC_LOTKA_VOLTERRA = 9, ORC_OREGONATOR = 10 };
+       ORC_LOTKA_VOLTERRA = 9, ORC_OREGONATOR = 10, ORC_BALL_BOX = 11, ORC_THRESHOLD_DOSE = 12 };
 /* SciMLBase ReturnCode subset used by this path (numbering of the C ABI). */
 enum { ORC_RC_DEFAULT = 0, ORC_RC_SUCCESS = 1, ORC_RC_MAXITERS = 2, ORC_RC_DTNAN = 3,
        ORC_RC_DTLESSTHANMIN = 4, ORC_RC_UNSTABLE = 5, ORC_RC_TERMINATED = 7 };

@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(HERE, "liboracle.so")
 
 TSIT5, VERN7, RODAS5P, VERN9, ROSENBROCK23, AUTOTSIT5_ROSENBROCK23 = 0, 1, 2, 3, 4, 5
 LINEAR, LORENZ, ROBERTSON, DUFFING, BRUSSELATOR, BOUNCING_BALL, VANDERPOL, PK1, FORCED_DUFFING = 0, 1, 2, 3, 4, 5, 6, 7, 8
-LOTKA_VOLTERRA, OREGONATOR = 9, 10
+LOTKA_VOLTERRA, OREGONATOR, BALL_BOX, THRESHOLD_DOSE = 9, 10, 11, 12
 RC_DEFAULT, RC_SUCCESS, RC_MAXITERS, RC_DTNAN, RC_DTLESSTHANMIN, RC_UNSTABLE = range(6)
 RC_TERMINATED = 7
 

@@ -45,6 +45,16 @@ template <class M, class = void> struct has_discrete_callback : bool_constant<fa
 template <class M>
 struct has_discrete_callback<M, void_t<decltype(M::HAS_DISCRETE)>> : bool_constant<M::HAS_DISCRETE> {};
 
+// Continuous callbacks: a model with HAS_EVENT declares one ContinuousCallback
+// (EVENT_LEN = 1, the default) or one VectorContinuousCallback of EVENT_LEN
+// conditions.  A model's DiscreteCallback fires at the solve's tstops unless
+// the model declares DISCRETE_AT_TSTOPS = false and its own condition.
+template <class M, class = void> struct event_len { static constexpr int value = 1; };
+template <class M> struct event_len<M, void_t<decltype(M::EVENT_LEN)>> { static constexpr int value = M::EVENT_LEN; };
+template <class M, class = void> struct discrete_at_tstops : bool_constant<true> {};
+template <class M>
+struct discrete_at_tstops<M, void_t<decltype(M::DISCRETE_AT_TSTOPS)>> : bool_constant<M::DISCRETE_AT_TSTOPS> {};
+
 // models with an analytic time derivative (ODEFunction's tgrad) declare HAS_TGRAD
 template <class M, class = void> struct has_tgrad : bool_constant<false> {};
 template <class M>
@@ -449,14 +459,15 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
     bool ev_last = false, terminated = false;
     double last_event_error = 0.0;
     auto handle_event = [&]() -> bool {
-        if constexpr (Model::HAS_EVENT) {
+        if constexpr (Model::HAS_EVENT && event_len<Model>::value == 1) {
             auto cond_at = [&](double abst) -> double {
-                if (abst == t) return Model::template event_condition<R, L, C>(u, ulo, g);
-                if (abst == tprev) return Model::template event_condition<R, L, C>(uprev, uprevlo, g);
+                if (abst == t) return Model::template event_condition<R, L, C>(u, ulo, a.p + j, N, abst, g);
+                if (abst == tprev)
+                    return Model::template event_condition<R, L, C>(uprev, uprevlo, a.p + j, N, abst, g);
                 R v[C], vlo[C];
                 Alg::template interpolate<Model, R, L, C>(cache, v, vlo, (abst - tprev) / dt, dt, tprev, uprev,
                                                           uprevlo, u, ulo, p, g);
-                return Model::template event_condition<R, L, C>(v, vlo, g);
+                return Model::template event_condition<R, L, C>(v, vlo, a.p + j, N, abst, g);
             };
             auto is_event = [](double bs, double ts) {
                 return ((bs < 0.0 && Model::EVENT_AFFECT_POS) || (bs > 0.0 && Model::EVENT_AFFECT_NEG)) &&
@@ -522,6 +533,135 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             }
             if (modified) save_point(t, u, ulo);   // save_positions[2]
             if (!terminated && (moved || modified)) Alg::template reset_fsal<Model, R, L, C>(cache, u, ulo, p, t, g, st);
+            return true;
+        }
+        return false;
+    };
+
+    // The model's VectorContinuousCallback of M conditions after an accepted step:
+    // find_callback_time(integrator, ::VectorContinuousCallback, idx) (lib/DiffEqBase/
+    // src/callbacks.jl:239-362) and apply_callback! (:557-643).  The bottom signs come
+    // from tprev; the components of the last event (prev_mask) take theirs just past
+    // it (nudge_tprev on the one whose condition is closest to zero); a component
+    // fires on a sign change away from a nonzero bottom sign (findall_events!,
+    // :495-523), checked at t and, unless every component fired there, at the
+    // interp_points of the step; each firing component's root is bracketed to
+    // adjacent floats, the earliest wins and ties fire together; affect! gets the
+    // events' directions (+1 upcrossing, -1 downcrossing, 0 none).
+    int prev_mask = 0;
+    auto handle_vector_event = [&]() -> bool {
+        if constexpr (Model::HAS_EVENT && event_len<Model>::value > 1) {
+            constexpr int M = event_len<Model>::value;
+            static_assert(M <= 32, "at most 32 conditions");
+            auto conds_at = [&](double abst, double* out) {
+                if (abst == t) {
+                    Model::template event_conditions<R, L, C>(out, u, ulo, a.p + j, N, abst, g);
+                } else if (abst == tprev) {
+                    Model::template event_conditions<R, L, C>(out, uprev, uprevlo, a.p + j, N, abst, g);
+                } else {
+                    R v[C], vlo[C];
+                    Alg::template interpolate<Model, R, L, C>(cache, v, vlo, (abst - tprev) / dt, dt, tprev, uprev,
+                                                              uprevlo, u, ulo, p, g);
+                    Model::template event_conditions<R, L, C>(out, v, vlo, a.p + j, N, abst, g);
+                }
+            };
+            double bc[M], bs[M], nc[M], tc[M];
+            conds_at(tprev, bc);
+#pragma unroll
+            for (int i = 0; i < M; ++i) { bs[i] = dsign(bc[i]); nc[i] = bc[i]; }
+            double nudged_t = tprev;
+            if (ev_last) {
+                double minc = 0.0, mina = __longlong_as_double(0x7ff0000000000000LL);
+#pragma unroll
+                for (int i = 0; i < M; ++i)
+                    if (((prev_mask >> i) & 1) && fabs(bc[i]) < mina) { mina = fabs(bc[i]); minc = bc[i]; }
+                if (fabs(minc - last_event_error) <= kCbAbstol) nudged_t = tprev + dt * kCbRepeatNudge;
+                conds_at(nudged_t, nc);
+#pragma unroll
+                for (int i = 0; i < M; ++i)
+                    if ((prev_mask >> i) & 1) bs[i] = dsign(nc[i]);
+            }
+            auto fired = [&](const double* top) {
+                int m = 0;
+#pragma unroll
+                for (int i = 0; i < M; ++i)
+                    if (bs[i] != 0.0 && bs[i] * dsign(top[i]) <= 0.0) m |= 1 << i;
+                return m;
+            };
+            double top_t = t;
+            conds_at(top_t, tc);
+            int ev = fired(tc);
+            constexpr int all = M == 32 ? -1 : (1 << M) - 1;
+            if (a.interp_points != 0 && ev != all) {   // any(iszero, event_idx)
+                const int m = a.interp_points;
+                for (int i = 2; i <= m; ++i) {
+                    top_t = i == m ? t : tprev + (t - tprev) * ((double)(i - 1) / (double)(m - 1));
+                    conds_at(top_t, tc);
+                    ev = fired(tc);
+                    if (ev) break;
+                }
+            }
+            if (!ev) {
+                ev_last = false;
+                return false;
+            }
+            // the earliest root among the firing components (rightfloat(top_t) to start)
+            double cb_t = nextafter(top_t, __longlong_as_double(0x7ff0000000000000LL)), residual = 0.0;
+            int sim = 0, dir[M];
+#pragma unroll
+            for (int i = 0; i < M; ++i) dir[i] = 0;
+            // one copy of the root finder for every component (a rare path: events)
+#pragma unroll 1
+            for (int i = 0; i < M; ++i) {
+                if (!((ev >> i) & 1)) continue;
+                auto fi = [&](double s) {
+                    double o[M];
+                    conds_at(s, o);
+                    return o[i];
+                };
+                double cbi;
+                if (dsign(tc[i]) == 0.0) {
+                    cbi = top_t;
+                } else {
+                    const bool from_nudge = ev_last && ((prev_mask >> i) & 1);
+                    const double lo = from_nudge ? nudged_t : tprev;
+                    cbi = bracket_left_root(fi, lo, top_t, from_nudge ? nc[i] : bc[i], tc[i]);
+                }
+                if (cbi < cb_t) {
+                    sim = 0;
+#pragma unroll
+                    for (int k = 0; k < M; ++k) dir[k] = 0;
+                }
+                if (cbi <= cb_t) {
+                    cb_t = cbi;
+                    residual = fi(cbi);
+                    sim |= 1 << i;
+                    dir[i] = bs[i] < 0.0 ? 1 : -1;
+                }
+            }
+            ev_last = true;
+            last_event_error = residual;
+            prev_mask = sim;
+            // apply_callback!: set_proposed_dt! (dtrelax = 1), change_t_via_interpolation!,
+            // saveat up to the event, the pre-affect save unless one landed on t, affect!
+            // with the events' directions, the post-affect save
+            dtpropose = pmax(nextafter(a.dtmin, __longlong_as_double(0x7ff0000000000000LL)), dt);
+            const bool moved = cb_t != t;
+            R uend[C], uendlo[C];
+#pragma unroll
+            for (int c = 0; c < C; ++c) { uend[c] = u[c]; uendlo[c] = ulo[c]; }
+            if (moved) {
+                R v[C], vlo[C];
+                Alg::template interpolate<Model, R, L, C>(cache, v, vlo, (cb_t - tprev) / dt, dt, tprev, uprev,
+                                                          uprevlo, u, ulo, p, g);
+#pragma unroll
+                for (int c = 0; c < C; ++c) { u[c] = v[c]; ulo[c] = vlo[c]; }
+                t = cb_t;
+            }
+            if (!savevalues(uend, uendlo)) save_point(t, u, ulo);
+            terminated = Model::template vector_event_affect<R, L, C>(u, ulo, a.p + j, N, t, dir, g);
+            save_point(t, u, ulo);
+            if (!terminated) Alg::template reset_fsal<Model, R, L, C>(cache, u, ulo, p, t, g, st);
             return true;
         }
         return false;
@@ -641,24 +781,31 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             const double dtp = pmin(pabs(dtmax), pabs(dtnew));
             dtpropose = pmax(pabs(dtp), pabs(pmax(peps(t), a.dtmin)));
             // ---- handle_callbacks! / savevalues!
+            // handle_callbacks! (integrator_utils.jl:1081-1132): the continuous callback,
+            // then the discrete one; savevalues! unless the last of them saved
             bool handled = false;
             if constexpr (Model::HAS_EVENT) {
-                if (a.callback) handled = handle_event();
+                if (a.callback) handled = event_len<Model>::value == 1 ? handle_event() : handle_vector_event();
             }
             if constexpr (has_discrete_callback<Model>::value) {
-                // apply_discrete_callback! (lib/DiffEqBase/src/callbacks.jl:645-682) for the
-                // model's DiscreteCallback, condition t in tstops: the step landed on the
-                // tstop the index points at (entries before it were passed at the header)
-                if (a.callback && itst < a.ntstops && a.tstops[itst] == t) {
+                // apply_discrete_callback! (lib/DiffEqBase/src/callbacks.jl:645-682): the
+                // condition is t in tstops (the step landed on the tstop the index points
+                // at; entries before it were passed at the header) or the model's own
+                bool fire = false;
+                if (a.callback) {
+                    if constexpr (discrete_at_tstops<Model>::value) fire = itst < a.ntstops && a.tstops[itst] == t;
+                    else fire = Model::template discrete_condition<R, L, C>(u, ulo, a.p + j, N, t, g);
+                }
+                if (fire) {
                     // saveat up to t and the every-step save, then save_positions[1]
                     // unless a save landed on t; affect!; save_positions[2]
                     if (!savevalues(u, ulo)) save_point(t, u, ulo);
-                    Model::template discrete_affect<R, L, C>(u, ulo, a.p + j, N, g);
+                    terminated = Model::template discrete_affect<R, L, C>(u, ulo, a.p + j, N, t, g) || terminated;
                     save_point(t, u, ulo);
                     // u changed: FSAL methods evaluate f(u) again (reeval_fsal)
-                    Alg::template reset_fsal<Model, R, L, C>(cache, u, ulo, p, t, g, st);
-                    handled = true;
+                    if (!terminated) Alg::template reset_fsal<Model, R, L, C>(cache, u, ulo, p, t, g, st);
                 }
+                handled = fire;   // saved_in_cb is the discrete callbacks' verdict
             }
             if (!handled) savevalues(u, ulo);
             Alg::template after_save<R, C>(cache);

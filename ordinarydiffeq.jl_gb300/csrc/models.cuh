@@ -105,12 +105,14 @@ struct PKOneCompartment {
         J[0][0] = -p[0]; J[0][1] = R(0);
         J[1][0] = p[0];  J[1][1] = -p[1];
     }
-    // affect!: the dose into the depot, in FP64 on the state pair
+    // affect!: the dose into the depot, in FP64 on the state pair (no terminate!)
     template <class R, int L, int C>
-    __device__ static void discrete_affect(R* u, R* ulo, const double* p, long long stride, const Group<L>&) {
+    __device__ static bool discrete_affect(R* u, R* ulo, const double* p, long long stride, double,
+                                           const Group<L>&) {
         const double v = ((double)u[0] + (double)ulo[0]) + p[2 * stride];
         u[0] = (R)v;
         ulo[0] = (R)(v - (double)u[0]);
+        return false;
     }
 };
 
@@ -137,7 +139,8 @@ struct BouncingBall {
     }
     // condition(u, t, integrator) = u[1] (the height), in FP64 from the state pair
     template <class R, int L, int C>
-    __device__ static double event_condition(const R* u, const R* ulo, const Group<L>&) {
+    __device__ static double event_condition(const R* u, const R* ulo, const double*, long long, double,
+                                             const Group<L>&) {
         return (double)u[0] + (double)ulo[0];
     }
     // the affect for a crossing from below (upcrossing) or above; true: terminate!

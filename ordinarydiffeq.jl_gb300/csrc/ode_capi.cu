@@ -62,7 +62,13 @@ int model_nparams(int model) {
     return (model == ODE_MODEL_LINEAR || model == ODE_MODEL_VANDERPOL) ? 1 : model == ODE_MODEL_FORCED_DUFFING ? 5 : 3;
 }
 // models with a registered callback (continuous: the ball; discrete: the dosing model)
-bool model_has_event(int model) { return model == ODE_MODEL_BOUNCING_BALL || model == ODE_MODEL_PK_ONE_COMPARTMENT; }
+bool model_has_event(int model) {
+    int flags = 0;
+    if (model >= ODE_MODEL_USER_BASE)
+        return rtc_lookup(model, nullptr, nullptr, &flags) &&
+               (flags & (ODE_MODEL_CONTINUOUS_CALLBACK | ODE_MODEL_VECTOR_CALLBACK | ODE_MODEL_DISCRETE_CALLBACK));
+    return model == ODE_MODEL_BOUNCING_BALL || model == ODE_MODEL_PK_ONE_COMPARTMENT;
+}
 
 // Default lanes per trajectory: one lane for tiny systems (registers hold the
 // whole state and stage set); explicit methods 4 states per lane so the Vern7

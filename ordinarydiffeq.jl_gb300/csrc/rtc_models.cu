@@ -134,6 +134,9 @@ std::string program(const Registered& m) {
     const std::string& N = m.name;
     const bool jac = m.flags & ODE_MODEL_HAS_JAC, tg = m.flags & ODE_MODEL_HAS_TGRAD;
     const bool nonauto = m.flags & ODE_MODEL_NONAUTONOMOUS;
+    const bool ccb = m.flags & ODE_MODEL_CONTINUOUS_CALLBACK, vcb = m.flags & ODE_MODEL_VECTOR_CALLBACK;
+    const bool dcb = m.flags & ODE_MODEL_DISCRETE_CALLBACK;
+    const int vlen = (m.flags >> 16) & 0xff;
     std::string s;
     s += "#include \"erk.cuh\"\n#include \"rodas.cuh\"\n#include \"ros23.cuh\"\n#include \"autoswitch.cuh\"\n"
          "#include \"user_model.cuh\"\n";
@@ -144,7 +147,48 @@ std::string program(const Registered& m) {
     s += "struct Model {\n";
     s += "  static constexpr int NP = " + std::to_string(m.np) + ";\n";
     s += std::string("  static constexpr bool AUTONOMOUS = ") + (nonauto ? "false" : "true") + ";\n";
-    s += "  static constexpr bool HAS_EVENT = false;\n";
+    s += std::string("  static constexpr bool HAS_EVENT = ") + (ccb || vcb ? "true" : "false") + ";\n";
+    s += "  static constexpr int EVENT_LEN = " + std::to_string(vcb ? vlen : 1) + ";\n";
+    s += std::string("  static constexpr bool EVENT_AFFECT_POS = ") +
+         (m.flags & ODE_MODEL_CALLBACK_AFFECT ? "true" : "false") + ";\n";
+    s += std::string("  static constexpr bool EVENT_AFFECT_NEG = ") +
+         (m.flags & ODE_MODEL_CALLBACK_AFFECT_NEG ? "true" : "false") + ";\n";
+    s += std::string("  static constexpr bool HAS_DISCRETE = ") + (dcb ? "true" : "false") + ";\n";
+    s += "  static constexpr bool DISCRETE_AT_TSTOPS = false;\n";
+    // the callbacks see the state as FP64 (the pair hi + lo in the mixed form) and the
+    // parameters as FP64, and write the state back as a pair
+    s += "  template <class R, int C> __device__ static void gather(double* ud, double* pd, const R* u, "
+         "const R* ulo, const double* p, long long stride) {\n"
+         "    for (int c = 0; c < C; ++c) ud[c] = (double)u[c] + (double)ulo[c];\n"
+         "    for (int i = 0; i < NP; ++i) pd[i] = p[(long long)i * stride];\n  }\n";
+    s += "  template <class R, int C> __device__ static void scatter(R* u, R* ulo, const double* ud) {\n"
+         "    for (int c = 0; c < C; ++c) odegb::Acc<R>::split(ud[c], u[c], ulo[c]);\n  }\n";
+    const std::string args = "(const R* u, const R* ulo, const double* p, long long stride, double t, "
+                             "const odegb::Group<L>&)";
+    const std::string margs = "(R* u, R* ulo, const double* p, long long stride, double t, ";
+    const std::string locals = "double ud[C], pd[NP > 0 ? NP : 1]; gather<R, C>(ud, pd, u, ulo, p, stride); ";
+    if (ccb) {
+        s += "  template <class R, int L, int C> __device__ static double event_condition" + args + " { " + locals +
+             "return " + N + "_condition(ud, pd, t); }\n";
+        s += "  template <class R, int L, int C> __device__ static bool event_affect" + margs +
+             "bool up, const odegb::Group<L>&) { " + locals + "const int r = " + N +
+             "_affect(ud, pd, t, up ? 1 : 0); scatter<R, C>(u, ulo, ud); return r != 0; }\n";
+    }
+    if (vcb) {
+        s += "  template <class R, int L, int C> __device__ static void event_conditions(double* out, const R* u, "
+             "const R* ulo, const double* p, long long stride, double t, const odegb::Group<L>&) { " + locals +
+             N + "_vcondition(out, ud, pd, t); }\n";
+        s += "  template <class R, int L, int C> __device__ static bool vector_event_affect" + margs +
+             "const int* events, const odegb::Group<L>&) { " + locals + "const int r = " + N +
+             "_vaffect(ud, pd, t, events); scatter<R, C>(u, ulo, ud); return r != 0; }\n";
+    }
+    if (dcb) {
+        s += "  template <class R, int L, int C> __device__ static bool discrete_condition" + args + " { " + locals +
+             "return " + N + "_dcondition(ud, pd, t) != 0; }\n";
+        s += "  template <class R, int L, int C> __device__ static bool discrete_affect" + margs +
+             "const odegb::Group<L>&) { " + locals + "const int r = " + N +
+             "_daffect(ud, pd, t); scatter<R, C>(u, ulo, ud); return r != 0; }\n";
+    }
     s += std::string("  static constexpr bool HAS_TGRAD = ") + (tg ? "true" : "false") + ";\n";
     s += std::string("  static constexpr int JAC_F_CALLS = ") + (jac ? "0" : "1") + ";\n";
     s += "  template <class R, int L, int C, class P>\n  __device__ static void rhs(R* du, const R* u, const P* p, "
@@ -247,8 +291,26 @@ int rtc_register(const char* source, const char* name, int n, int np, int flags,
         *err = buf;
         return ODE_E_INVALID;
     }
-    if (flags & ~(ODE_MODEL_HAS_JAC | ODE_MODEL_HAS_TGRAD | ODE_MODEL_NONAUTONOMOUS)) {
+    const int known = ODE_MODEL_HAS_JAC | ODE_MODEL_HAS_TGRAD | ODE_MODEL_NONAUTONOMOUS |
+                      ODE_MODEL_CONTINUOUS_CALLBACK | ODE_MODEL_CALLBACK_AFFECT | ODE_MODEL_CALLBACK_AFFECT_NEG |
+                      ODE_MODEL_VECTOR_CALLBACK | ODE_MODEL_DISCRETE_CALLBACK | ODE_MODEL_CALLBACK_LEN(0xff);
+    if (flags & ~known) {
         *err = "unknown model flag";
+        return ODE_E_INVALID;
+    }
+    const int vlen = (flags >> 16) & 0xff;
+    if ((flags & ODE_MODEL_CONTINUOUS_CALLBACK) && (flags & ODE_MODEL_VECTOR_CALLBACK)) {
+        *err = "a model registers one continuous callback: scalar or vector";
+        return ODE_E_INVALID;
+    }
+    if ((flags & ODE_MODEL_CONTINUOUS_CALLBACK) &&
+        !(flags & (ODE_MODEL_CALLBACK_AFFECT | ODE_MODEL_CALLBACK_AFFECT_NEG))) {
+        *err = "a ContinuousCallback needs affect! (ODE_MODEL_CALLBACK_AFFECT) or affect_neg! "
+               "(ODE_MODEL_CALLBACK_AFFECT_NEG)";
+        return ODE_E_INVALID;
+    }
+    if ((flags & ODE_MODEL_VECTOR_CALLBACK) ? (vlen < 1 || vlen > 32) : vlen != 0) {
+        *err = "a VectorContinuousCallback takes ODE_MODEL_CALLBACK_LEN(len) with 1 <= len <= 32, and only it";
         return ODE_E_INVALID;
     }
     std::lock_guard<std::mutex> lk(g_mu);

@@ -26,6 +26,8 @@ namespace odegb {
 // the two type traits the kernels use (std's, which NVRTC lacks)
 template <bool B> struct bool_constant { static constexpr bool value = B; };
 template <class...> using void_t = void;
+template <class T> struct is_double : bool_constant<false> {};
+template <> struct is_double<double> : bool_constant<true> {};
 
 // ------------------------------------------------------------------ scalars
 template <class T> struct Arith;
@@ -428,6 +430,16 @@ template <class A> struct is_composite_alg<A, void_t<decltype(A::COMPOSITE)>> : 
 template <class M, class = void> struct has_discrete_callback : bool_constant<false> {};
 template <class M>
 struct has_discrete_callback<M, void_t<decltype(M::HAS_DISCRETE)>> : bool_constant<M::HAS_DISCRETE> {};
+
+// Continuous callbacks: a model with HAS_EVENT declares one ContinuousCallback
+// (EVENT_LEN = 1, the default) or one VectorContinuousCallback of EVENT_LEN
+// conditions.  A model's DiscreteCallback fires at the solve's tstops unless
+// the model declares DISCRETE_AT_TSTOPS = false and its own condition.
+template <class M, class = void> struct event_len { static constexpr int value = 1; };
+template <class M> struct event_len<M, void_t<decltype(M::EVENT_LEN)>> { static constexpr int value = M::EVENT_LEN; };
+template <class M, class = void> struct discrete_at_tstops : bool_constant<true> {};
+template <class M>
+struct discrete_at_tstops<M, void_t<decltype(M::DISCRETE_AT_TSTOPS)>> : bool_constant<M::DISCRETE_AT_TSTOPS> {};
 
 // models with an analytic time derivative (ODEFunction's tgrad) declare HAS_TGRAD
 template <class M, class = void> struct has_tgrad : bool_constant<false> {};
@@ -833,14 +845,15 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
     bool ev_last = false, terminated = false;
     double last_event_error = 0.0;
     auto handle_event = [&]() -> bool {
-        if constexpr (Model::HAS_EVENT) {
+        if constexpr (Model::HAS_EVENT && event_len<Model>::value == 1) {
             auto cond_at = [&](double abst) -> double {
-                if (abst == t) return Model::template event_condition<R, L, C>(u, ulo, g);
-                if (abst == tprev) return Model::template event_condition<R, L, C>(uprev, uprevlo, g);
+                if (abst == t) return Model::template event_condition<R, L, C>(u, ulo, a.p + j, N, abst, g);
+                if (abst == tprev)
+                    return Model::template event_condition<R, L, C>(uprev, uprevlo, a.p + j, N, abst, g);
                 R v[C], vlo[C];
                 Alg::template interpolate<Model, R, L, C>(cache, v, vlo, (abst - tprev) / dt, dt, tprev, uprev,
                                                           uprevlo, u, ulo, p, g);
-                return Model::template event_condition<R, L, C>(v, vlo, g);
+                return Model::template event_condition<R, L, C>(v, vlo, a.p + j, N, abst, g);
             };
             auto is_event = [](double bs, double ts) {
                 return ((bs < 0.0 && Model::EVENT_AFFECT_POS) || (bs > 0.0 && Model::EVENT_AFFECT_NEG)) &&
@@ -906,6 +919,135 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             }
             if (modified) save_point(t, u, ulo);   // save_positions[2]
             if (!terminated && (moved || modified)) Alg::template reset_fsal<Model, R, L, C>(cache, u, ulo, p, t, g, st);
+            return true;
+        }
+        return false;
+    };
+
+    // The model's VectorContinuousCallback of M conditions after an accepted step:
+    // find_callback_time(integrator, ::VectorContinuousCallback, idx) (lib/DiffEqBase/
+    // src/callbacks.jl:239-362) and apply_callback! (:557-643).  The bottom signs come
+    // from tprev; the components of the last event (prev_mask) take theirs just past
+    // it (nudge_tprev on the one whose condition is closest to zero); a component
+    // fires on a sign change away from a nonzero bottom sign (findall_events!,
+    // :495-523), checked at t and, unless every component fired there, at the
+    // interp_points of the step; each firing component's root is bracketed to
+    // adjacent floats, the earliest wins and ties fire together; affect! gets the
+    // events' directions (+1 upcrossing, -1 downcrossing, 0 none).
+    int prev_mask = 0;
+    auto handle_vector_event = [&]() -> bool {
+        if constexpr (Model::HAS_EVENT && event_len<Model>::value > 1) {
+            constexpr int M = event_len<Model>::value;
+            static_assert(M <= 32, "at most 32 conditions");
+            auto conds_at = [&](double abst, double* out) {
+                if (abst == t) {
+                    Model::template event_conditions<R, L, C>(out, u, ulo, a.p + j, N, abst, g);
+                } else if (abst == tprev) {
+                    Model::template event_conditions<R, L, C>(out, uprev, uprevlo, a.p + j, N, abst, g);
+                } else {
+                    R v[C], vlo[C];
+                    Alg::template interpolate<Model, R, L, C>(cache, v, vlo, (abst - tprev) / dt, dt, tprev, uprev,
+                                                              uprevlo, u, ulo, p, g);
+                    Model::template event_conditions<R, L, C>(out, v, vlo, a.p + j, N, abst, g);
+                }
+            };
+            double bc[M], bs[M], nc[M], tc[M];
+            conds_at(tprev, bc);
+#pragma unroll
+            for (int i = 0; i < M; ++i) { bs[i] = dsign(bc[i]); nc[i] = bc[i]; }
+            double nudged_t = tprev;
+            if (ev_last) {
+                double minc = 0.0, mina = __longlong_as_double(0x7ff0000000000000LL);
+#pragma unroll
+                for (int i = 0; i < M; ++i)
+                    if (((prev_mask >> i) & 1) && fabs(bc[i]) < mina) { mina = fabs(bc[i]); minc = bc[i]; }
+                if (fabs(minc - last_event_error) <= kCbAbstol) nudged_t = tprev + dt * kCbRepeatNudge;
+                conds_at(nudged_t, nc);
+#pragma unroll
+                for (int i = 0; i < M; ++i)
+                    if ((prev_mask >> i) & 1) bs[i] = dsign(nc[i]);
+            }
+            auto fired = [&](const double* top) {
+                int m = 0;
+#pragma unroll
+                for (int i = 0; i < M; ++i)
+                    if (bs[i] != 0.0 && bs[i] * dsign(top[i]) <= 0.0) m |= 1 << i;
+                return m;
+            };
+            double top_t = t;
+            conds_at(top_t, tc);
+            int ev = fired(tc);
+            constexpr int all = M == 32 ? -1 : (1 << M) - 1;
+            if (a.interp_points != 0 && ev != all) {   // any(iszero, event_idx)
+                const int m = a.interp_points;
+                for (int i = 2; i <= m; ++i) {
+                    top_t = i == m ? t : tprev + (t - tprev) * ((double)(i - 1) / (double)(m - 1));
+                    conds_at(top_t, tc);
+                    ev = fired(tc);
+                    if (ev) break;
+                }
+            }
+            if (!ev) {
+                ev_last = false;
+                return false;
+            }
+            // the earliest root among the firing components (rightfloat(top_t) to start)
+            double cb_t = nextafter(top_t, __longlong_as_double(0x7ff0000000000000LL)), residual = 0.0;
+            int sim = 0, dir[M];
+#pragma unroll
+            for (int i = 0; i < M; ++i) dir[i] = 0;
+            // one copy of the root finder for every component (a rare path: events)
+#pragma unroll 1
+            for (int i = 0; i < M; ++i) {
+                if (!((ev >> i) & 1)) continue;
+                auto fi = [&](double s) {
+                    double o[M];
+                    conds_at(s, o);
+                    return o[i];
+                };
+                double cbi;
+                if (dsign(tc[i]) == 0.0) {
+                    cbi = top_t;
+                } else {
+                    const bool from_nudge = ev_last && ((prev_mask >> i) & 1);
+                    const double lo = from_nudge ? nudged_t : tprev;
+                    cbi = bracket_left_root(fi, lo, top_t, from_nudge ? nc[i] : bc[i], tc[i]);
+                }
+                if (cbi < cb_t) {
+                    sim = 0;
+#pragma unroll
+                    for (int k = 0; k < M; ++k) dir[k] = 0;
+                }
+                if (cbi <= cb_t) {
+                    cb_t = cbi;
+                    residual = fi(cbi);
+                    sim |= 1 << i;
+                    dir[i] = bs[i] < 0.0 ? 1 : -1;
+                }
+            }
+            ev_last = true;
+            last_event_error = residual;
+            prev_mask = sim;
+            // apply_callback!: set_proposed_dt! (dtrelax = 1), change_t_via_interpolation!,
+            // saveat up to the event, the pre-affect save unless one landed on t, affect!
+            // with the events' directions, the post-affect save
+            dtpropose = pmax(nextafter(a.dtmin, __longlong_as_double(0x7ff0000000000000LL)), dt);
+            const bool moved = cb_t != t;
+            R uend[C], uendlo[C];
+#pragma unroll
+            for (int c = 0; c < C; ++c) { uend[c] = u[c]; uendlo[c] = ulo[c]; }
+            if (moved) {
+                R v[C], vlo[C];
+                Alg::template interpolate<Model, R, L, C>(cache, v, vlo, (cb_t - tprev) / dt, dt, tprev, uprev,
+                                                          uprevlo, u, ulo, p, g);
+#pragma unroll
+                for (int c = 0; c < C; ++c) { u[c] = v[c]; ulo[c] = vlo[c]; }
+                t = cb_t;
+            }
+            if (!savevalues(uend, uendlo)) save_point(t, u, ulo);
+            terminated = Model::template vector_event_affect<R, L, C>(u, ulo, a.p + j, N, t, dir, g);
+            save_point(t, u, ulo);
+            if (!terminated) Alg::template reset_fsal<Model, R, L, C>(cache, u, ulo, p, t, g, st);
             return true;
         }
         return false;
@@ -1025,24 +1167,31 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             const double dtp = pmin(pabs(dtmax), pabs(dtnew));
             dtpropose = pmax(pabs(dtp), pabs(pmax(peps(t), a.dtmin)));
             // ---- handle_callbacks! / savevalues!
+            // handle_callbacks! (integrator_utils.jl:1081-1132): the continuous callback,
+            // then the discrete one; savevalues! unless the last of them saved
             bool handled = false;
             if constexpr (Model::HAS_EVENT) {
-                if (a.callback) handled = handle_event();
+                if (a.callback) handled = event_len<Model>::value == 1 ? handle_event() : handle_vector_event();
             }
             if constexpr (has_discrete_callback<Model>::value) {
-                // apply_discrete_callback! (lib/DiffEqBase/src/callbacks.jl:645-682) for the
-                // model's DiscreteCallback, condition t in tstops: the step landed on the
-                // tstop the index points at (entries before it were passed at the header)
-                if (a.callback && itst < a.ntstops && a.tstops[itst] == t) {
+                // apply_discrete_callback! (lib/DiffEqBase/src/callbacks.jl:645-682): the
+                // condition is t in tstops (the step landed on the tstop the index points
+                // at; entries before it were passed at the header) or the model's own
+                bool fire = false;
+                if (a.callback) {
+                    if constexpr (discrete_at_tstops<Model>::value) fire = itst < a.ntstops && a.tstops[itst] == t;
+                    else fire = Model::template discrete_condition<R, L, C>(u, ulo, a.p + j, N, t, g);
+                }
+                if (fire) {
                     // saveat up to t and the every-step save, then save_positions[1]
                     // unless a save landed on t; affect!; save_positions[2]
                     if (!savevalues(u, ulo)) save_point(t, u, ulo);
-                    Model::template discrete_affect<R, L, C>(u, ulo, a.p + j, N, g);
+                    terminated = Model::template discrete_affect<R, L, C>(u, ulo, a.p + j, N, t, g) || terminated;
                     save_point(t, u, ulo);
                     // u changed: FSAL methods evaluate f(u) again (reeval_fsal)
-                    Alg::template reset_fsal<Model, R, L, C>(cache, u, ulo, p, t, g, st);
-                    handled = true;
+                    if (!terminated) Alg::template reset_fsal<Model, R, L, C>(cache, u, ulo, p, t, g, st);
                 }
+                handled = fire;   // saved_in_cb is the discrete callbacks' verdict
             }
             if (!handled) savevalues(u, ulo);
             Alg::template after_save<R, C>(cache);
@@ -1839,6 +1988,55 @@ __device__ __forceinline__ ff split_weight(double w) {
     return ff(h, (float)(w - (double)h));
 }
 
+// Interpolation weights of a save computed lane-parallel within a lane group.
+// Every lane of a group needs the same NW weights b_q(theta) (Horner in FP64);
+// on GB300 an FP64 warp instruction occupies the FP64 pipe as long with one
+// active lane as with 32, so a group of L lanes evaluates them L at a time --
+// lane l the weights l, l + L, ... -- and shares them by shuffles: ceil(NW/L)
+// rounds of FP64 work per save instead of NW.  The arithmetic of each weight is
+// the sequential form's (interp_weight), so results are unchanged.  A table row
+// holds the polynomial's coefficients, read at run time by the lane that owns it.
+#define ODEGB_R5(i) {tab::TSIT5_R(i, 0), tab::TSIT5_R(i, 1), tab::TSIT5_R(i, 2), tab::TSIT5_R(i, 3), tab::TSIT5_R(i, 4)}
+#define ODEGB_R8(i)                                                                                      \
+    {tab::VERN7_R(i, 0), tab::VERN7_R(i, 1), tab::VERN7_R(i, 2), tab::VERN7_R(i, 3), tab::VERN7_R(i, 4), \
+     tab::VERN7_R(i, 5), tab::VERN7_R(i, 6), tab::VERN7_R(i, 7)}
+// weight q of Tsit5 belongs to stage q + 1; Vern7's 13 weights to stages 1, 4-9, 11-16
+static __device__ double kTsit5InterpR[7][5] = {ODEGB_R5(1), ODEGB_R5(2), ODEGB_R5(3), ODEGB_R5(4),
+                                                ODEGB_R5(5), ODEGB_R5(6), ODEGB_R5(7)};
+static __device__ double kVern7InterpR[13][8] = {ODEGB_R8(1),  ODEGB_R8(4),  ODEGB_R8(5),  ODEGB_R8(6), ODEGB_R8(7),
+                                                 ODEGB_R8(8),  ODEGB_R8(9),  ODEGB_R8(11), ODEGB_R8(12),
+                                                 ODEGB_R8(13), ODEGB_R8(14), ODEGB_R8(15), ODEGB_R8(16)};
+#undef ODEGB_R5
+#undef ODEGB_R8
+template <int NPOLY>
+__device__ __forceinline__ double interp_weight_row(double th, const double* r, bool first) {
+    double acc = r[NPOLY - 1];
+#pragma unroll
+    for (int q = NPOLY - 2; q >= 2; --q) acc = fma(th, acc, r[q]);
+    if (first) acc = fma(th, acc, r[1]);
+    return first ? th * acc : (th * th) * acc;
+}
+// b[q] for q < NW as double (FP64 form) or float pairs (mixed form); row(q) the
+// coefficient row of weight q; weight 0 is the `first` one (degree from 1).
+template <int NW, int NPOLY, int L, class B, class Row>
+__device__ __forceinline__ void group_weights(B* b, double th, const Group<L>& g, Row row) {
+#pragma unroll
+    for (int q0 = 0; q0 < NW; q0 += L) {
+        const int q = q0 + g.lane;
+        double w = 0.0;
+        if (q < NW) w = interp_weight_row<NPOLY>(th, row(q), q == 0);
+        if constexpr (is_double<B>::value) {
+#pragma unroll
+            for (int k = 0; k < L; ++k)
+                if (q0 + k < NW) b[q0 + k] = g.from(w, k);
+        } else {                          // float pair, split by the owning lane
+            const float hi = (float)w, lo = (float)(w - (double)hi);
+#pragma unroll
+            for (int k = 0; k < L; ++k)
+                if (q0 + k < NW) b[q0 + k] = ff(g.from(hi, k), g.from(lo, k));
+        }
+    }
+}
 struct Tsit5Alg {
     static constexpr int ORDER = 5;
     static constexpr bool IMPLICIT = false;
@@ -1926,14 +2124,19 @@ struct Tsit5Alg {
 
     template <class Model, class R, int L, int C>
     __device__ static void interpolate(Cache<R, C>& c, R* out, R* outlo, double th, double dt, double,
-                                       const R* y0, const R* y0lo, const R*, const R*, const PR<R>*, const Group<L>&) {
+                                       const R* y0, const R* y0lo, const R*, const R*, const PR<R>*,
+                                       const Group<L>& g) {
         auto r = [](int i, int q) { return tab::TSIT5_R(i, q); };
         const R d = (R)dt;
         if constexpr (sizeof(R) == 8) {
             double b[8];
-            b[1] = interp_weight<5>(th, 1, r, true);
+            if constexpr (L > 1) {
+                group_weights<7, 5, L>(b + 1, th, g, [](int q) { return (const double*)kTsit5InterpR[q]; });
+            } else {
+                b[1] = interp_weight<5>(th, 1, r, true);
 #pragma unroll
-            for (int i = 2; i <= 7; ++i) b[i] = interp_weight<5>(th, i, r, false);
+                for (int i = 2; i <= 7; ++i) b[i] = interp_weight<5>(th, i, r, false);
+            }
 #pragma unroll
             for (int i = 0; i < C; ++i) {
                 R acc = c.k[6][i] * (R)b[7];
@@ -1944,9 +2147,13 @@ struct Tsit5Alg {
         } else {
             const R dl = Acc<R>::dt_lo(dt, d);
             ff b[8];
-            b[1] = split_weight(interp_weight<5>((double)th, 1, r, true));
+            if constexpr (L > 1) {
+                group_weights<7, 5, L>(b + 1, th, g, [](int q) { return (const double*)kTsit5InterpR[q]; });
+            } else {
+                b[1] = split_weight(interp_weight<5>((double)th, 1, r, true));
 #pragma unroll
-            for (int i = 2; i <= 7; ++i) b[i] = split_weight(interp_weight<5>((double)th, i, r, false));
+                for (int i = 2; i <= 7; ++i) b[i] = split_weight(interp_weight<5>((double)th, i, r, false));
+            }
 #pragma unroll
             for (int i = 0; i < C; ++i) {
                 CSum cs;
@@ -2049,9 +2256,13 @@ struct Vern7Alg {
         const R d = (R)dt;
         if constexpr (sizeof(R) == 8) {
             double b[13];
-            b[0] = interp_weight<8>(th, 1, r, true);
+            if constexpr (L > 1) {
+                group_weights<13, 8, L>(b, th, g, [](int q) { return (const double*)kVern7InterpR[q]; });
+            } else {
+                b[0] = interp_weight<8>(th, 1, r, true);
 #pragma unroll
-            for (int q = 1; q < 13; ++q) b[q] = interp_weight<8>(th, idx[q], r, false);
+                for (int q = 1; q < 13; ++q) b[q] = interp_weight<8>(th, idx[q], r, false);
+            }
 #pragma unroll
             for (int i = 0; i < C; ++i) {
                 R acc = c.s[Vern7Tab::slot(16)][i] * (R)b[12];
@@ -2062,9 +2273,13 @@ struct Vern7Alg {
         } else {
             const R dl = Acc<R>::dt_lo(dt, d);
             ff b[13];
-            b[0] = split_weight(interp_weight<8>((double)th, 1, r, true));
+            if constexpr (L > 1) {
+                group_weights<13, 8, L>(b, th, g, [](int q) { return (const double*)kVern7InterpR[q]; });
+            } else {
+                b[0] = split_weight(interp_weight<8>((double)th, 1, r, true));
 #pragma unroll
-            for (int q = 1; q < 13; ++q) b[q] = split_weight(interp_weight<8>((double)th, idx[q], r, false));
+                for (int q = 1; q < 13; ++q) b[q] = split_weight(interp_weight<8>((double)th, idx[q], r, false));
+            }
 #pragma unroll
             for (int i = 0; i < C; ++i) {
                 CSum cs;
@@ -2313,14 +2528,34 @@ struct SmemLA {
             // updates its rows.  Each row receives its updates in the same
             // column order as the column-by-column form (identical results)
             // with 1/C of the dependent shuffle rounds.
+            // The lane's C x C entries of block column q are loaded one round
+            // ahead (wn), so the shared-memory latency stays off the chain of
+            // dependent rounds (for C <= 2; wider rows would spill registers).
+            constexpr bool PF = C <= 2;
+            R wn[C][C];
+#pragma unroll
+            for (int i = 0; i < C; ++i)
+#pragma unroll
+                for (int k = 0; k < C; ++k) wn[i][k] = W[at<L, C>(i, g.lane, k)];
 #pragma unroll 1
             for (int q = 0; q < L; ++q) {
+                R w[C][C];
+#pragma unroll
+                for (int i = 0; i < C; ++i)
+#pragma unroll
+                    for (int k = 0; k < C; ++k) w[i][k] = PF ? wn[i][k] : W[at<L, C>(i, g.lane, q * C + k)];
+                if (PF && q + 1 < L) {
+#pragma unroll
+                    for (int i = 0; i < C; ++i)
+#pragma unroll
+                        for (int k = 0; k < C; ++k) wn[i][k] = W[at<L, C>(i, g.lane, (q + 1) * C + k)];
+                }
                 R y[C];
 #pragma unroll
                 for (int i = 0; i < C; ++i) {
                     R acc = b[i];
 #pragma unroll
-                    for (int k = 0; k < i; ++k) acc = FMA(-W[at<L, C>(i, g.lane, q * C + k)], y[k], acc);
+                    for (int k = 0; k < i; ++k) acc = FMA(-w[i][k], y[k], acc);
                     y[i] = acc;
                 }
 #pragma unroll
@@ -2332,18 +2567,40 @@ struct SmemLA {
 #pragma unroll
                     for (int i = 0; i < C; ++i)
 #pragma unroll
-                        for (int k = 0; k < C; ++k) b[i] = FMA(-W[at<L, C>(i, g.lane, q * C + k)], y[k], b[i]);
+                        for (int k = 0; k < C; ++k) b[i] = FMA(-w[i][k], y[k], b[i]);
                 }
             }
+#pragma unroll
+            for (int i = 0; i < C; ++i)
+#pragma unroll
+                for (int k = 0; k < C; ++k) wn[i][k] = W[at<L, C>(i, g.lane, (L - 1) * C + k)];
+            R dn[C];
+#pragma unroll
+            for (int i = 0; i < C; ++i) dn[i] = s.dinv[(L - 1) * C + i];
 #pragma unroll 1
             for (int q = L - 1; q >= 0; --q) {
+                R w[C][C], dv[C];
+#pragma unroll
+                for (int i = 0; i < C; ++i) {
+                    dv[i] = PF ? dn[i] : s.dinv[q * C + i];
+#pragma unroll
+                    for (int k = 0; k < C; ++k) w[i][k] = PF ? wn[i][k] : W[at<L, C>(i, g.lane, q * C + k)];
+                }
+                if (PF && q > 0) {
+#pragma unroll
+                    for (int i = 0; i < C; ++i) {
+                        dn[i] = s.dinv[(q - 1) * C + i];
+#pragma unroll
+                        for (int k = 0; k < C; ++k) wn[i][k] = W[at<L, C>(i, g.lane, (q - 1) * C + k)];
+                    }
+                }
                 R x[C];
 #pragma unroll
                 for (int i = C - 1; i >= 0; --i) {
                     R acc = b[i];
 #pragma unroll
-                    for (int k = C - 1; k > i; --k) acc = FMA(-W[at<L, C>(i, g.lane, q * C + k)], x[k], acc);
-                    x[i] = acc * s.dinv[q * C + i];
+                    for (int k = C - 1; k > i; --k) acc = FMA(-w[i][k], x[k], acc);
+                    x[i] = acc * dv[i];
                 }
 #pragma unroll
                 for (int k = 0; k < C; ++k) x[k] = g.from(x[k], q);
@@ -2354,7 +2611,7 @@ struct SmemLA {
 #pragma unroll
                     for (int i = 0; i < C; ++i)
 #pragma unroll
-                        for (int k = C - 1; k >= 0; --k) b[i] = FMA(-W[at<L, C>(i, g.lane, q * C + k)], x[k], b[i]);
+                        for (int k = C - 1; k >= 0; --k) b[i] = FMA(-w[i][k], x[k], b[i]);
                 }
             }
             return;

@@ -14,6 +14,12 @@ MODEL_LINEAR, MODEL_LORENZ, MODEL_ROBERTSON, MODEL_DUFFING_CHAIN, MODEL_BRUSSELA
 MODEL_BOUNCING_BALL, MODEL_VANDERPOL, MODEL_PK_ONE_COMPARTMENT, MODEL_FORCED_DUFFING = 5, 6, 7, 8
 MODEL_USER_BASE = 1000   # ids of models registered at run time start here
 MODEL_HAS_JAC, MODEL_HAS_TGRAD, MODEL_NONAUTONOMOUS = 1, 2, 4
+MODEL_CONTINUOUS_CALLBACK, MODEL_CALLBACK_AFFECT, MODEL_CALLBACK_AFFECT_NEG = 8, 16, 32
+MODEL_VECTOR_CALLBACK, MODEL_DISCRETE_CALLBACK = 64, 128
+
+
+def model_callback_len(n):
+    return n << 16
 PREC_FP64, PREC_MIXED = 0, 1
 STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "out of device memory",
           -4: "unsupported", -5: "busy", -6: "timeout", -7: "unknown ticket"}

@@ -328,7 +328,8 @@ def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_ste
     return o
 
 
-def register_model(source, name, n_states, n_params, jac=False, tgrad=False, nonautonomous=False):
+def register_model(source, name, n_states, n_params, jac=False, tgrad=False, nonautonomous=False,
+                   continuous_callback=None, vector_callback=0, discrete_callback=False):
     """Register a model given as CUDA C++ source (ode_register_model): the device
     form of the reference's f(du, u, p, t), with its optional jac and tgrad.  For a
     model named `name` the source defines the templates
@@ -338,12 +339,34 @@ def register_model(source, name, n_states, n_params, jac=False, tgrad=False, non
         template <class T, class P> __device__ void NAME_tgrad(T* dT, const T* u, const P* p, double t); # tgrad=True
 
     (J row-major).  Without NAME_jac the Rosenbrock methods differentiate NAME_f
-    by forward-mode AD.  Returns the model id; the name also becomes a model name
-    for ODEProblem and solve_arrays.  The kernels are compiled on the first solve
-    of each method and precision."""
+    by forward-mode AD.  Callbacks registered with the model (enabled per solve
+    by passing ContinuousCallback(...) / DiscreteCallback(...) as `callback`):
+
+        continuous_callback="up" | "down" | "both": a ContinuousCallback,
+            __device__ double NAME_condition(const double* u, const double* p, double t);
+            __device__ int NAME_affect(double* u, const double* p, double t, int upcrossing);
+            acting on upcrossings (affect!), downcrossings (affect_neg!) or both;
+        vector_callback=len: a VectorContinuousCallback of len conditions,
+            __device__ void NAME_vcondition(double* out, const double* u, const double* p, double t);
+            __device__ int NAME_vaffect(double* u, const double* p, double t, const int* events);
+        discrete_callback=True: a DiscreteCallback,
+            __device__ int NAME_dcondition(const double* u, const double* p, double t);
+            __device__ int NAME_daffect(double* u, const double* p, double t);
+
+    (an affect returning nonzero calls terminate!).  Returns the model id; the
+    name also becomes a model name for ODEProblem and solve_arrays.  The kernels
+    are compiled on the first solve of each method and precision."""
     L = _lib.load()
     flags = (_lib.MODEL_HAS_JAC if jac else 0) | (_lib.MODEL_HAS_TGRAD if tgrad else 0) | \
         (_lib.MODEL_NONAUTONOMOUS if nonautonomous else 0)
+    if continuous_callback is not None:
+        flags |= _lib.MODEL_CONTINUOUS_CALLBACK | {
+            "up": _lib.MODEL_CALLBACK_AFFECT, "down": _lib.MODEL_CALLBACK_AFFECT_NEG,
+            "both": _lib.MODEL_CALLBACK_AFFECT | _lib.MODEL_CALLBACK_AFFECT_NEG}[continuous_callback]
+    if vector_callback:
+        flags |= _lib.MODEL_VECTOR_CALLBACK | _lib.model_callback_len(int(vector_callback))
+    if discrete_callback:
+        flags |= _lib.MODEL_DISCRETE_CALLBACK
     mid = C.c_int32(0)
     _lib.check(L.ode_register_model(source.encode(), name.encode(), int(n_states), int(n_params), flags,
                                     C.byref(mid)))

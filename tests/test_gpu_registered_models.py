@@ -157,3 +157,100 @@ def test_compile_errors_are_reported():
     with pytest.raises(_lib.OdeError) as e:
         gpu(bad, "tsit5", u0, p, ts, 0.5, 1e-6, 1e-6)
     assert e.value.status == -4 and "undefined_symbol" in str(e.value)
+
+
+# ---------------------------------------------------------------- callbacks registered with a model
+BALL = r'''
+template <class T, class P> __device__ void rball_f(T* du, const T* u, const P* p, double t) {
+    du[0] = u[1];
+    du[1] = -p[0];
+}
+__device__ double rball_condition(const double* u, const double* p, double t) { return u[0]; }
+__device__ int rball_affect(double* u, const double* p, double t, int upcrossing) {
+    if (t >= p[2]) return 1;   // terminate!
+    u[1] = -p[1] * u[1];
+    return 0;
+}
+'''
+BOX = r'''
+template <class T, class P> __device__ void box_f(T* du, const T* u, const P* p, double t) {
+    du[0] = u[2]; du[1] = u[3]; du[2] = T(0); du[3] = -p[0];
+}
+__device__ void box_vcondition(double* out, const double* u, const double* p, double t) {
+    out[0] = u[1]; out[1] = u[0]; out[2] = p[2] - u[0];
+}
+__device__ int box_vaffect(double* u, const double* p, double t, const int* events) {
+    if (events[0] != 0) u[3] = -p[1] * u[3];
+    if (events[1] != 0 || events[2] != 0) u[2] = -u[2];
+    return 0;
+}
+'''
+THRESHOLD = r'''
+template <class T, class P> __device__ void thr_f(T* du, const T* u, const P* p, double t) { du[0] = -p[0] * u[0]; }
+__device__ int thr_dcondition(const double* u, const double* p, double t) { return u[0] < p[1]; }
+__device__ int thr_daffect(double* u, const double* p, double t) { u[0] += p[2]; return 0; }
+'''
+
+
+@pytest.fixture(scope="module")
+def with_callbacks():
+    from odegb300 import register_model
+    MODEL.setdefault("rball", O.BOUNCING_BALL)
+    MODEL.setdefault("box", O.BALL_BOX)
+    MODEL.setdefault("thr", O.THRESHOLD_DOSE)
+    return {"rball": register_model(BALL, "rball", 2, 3, continuous_callback="down"),
+            "box": register_model(BOX, "box", 4, 3, vector_callback=3),
+            "thr": register_model(THRESHOLD, "thr", 1, 3, discrete_callback=True)}
+
+
+def test_registered_continuous_callback_equals_the_compiled_in_ball(with_callbacks):
+    from odegb300 import workloads as W
+    from odegb300.saveat import resolve_saveat
+    wl = W.bouncing_ball(256, seed=4)
+    kw = dict(callback=wl["callback"])
+    a = gpu("rball", "tsit5", wl["u0"], wl["p"], wl["tspan"], wl["saveat"], 1e-6, 1e-6, **kw)
+    b = gpu("bouncing_ball", "tsit5", wl["u0"], wl["p"], wl["tspan"], wl["saveat"], 1e-6, 1e-6, **kw)
+    assert np.array_equal(a["u"], b["u"], equal_nan=True) and np.array_equal(a["retcode"], b["retcode"])
+    assert (a["retcode"] == 7).any()   # terminate! from the registered affect
+
+
+def box_inputs(N, seed=0):
+    rng = np.random.default_rng(seed)
+    W = rng.uniform(3.0, 6.0, N)
+    u0 = np.vstack([rng.uniform(0.5, 2.5, N), rng.uniform(3.0, 9.0, N), rng.uniform(-4.0, 4.0, N),
+                    rng.uniform(-2.0, 2.0, N)])
+    p = np.vstack([np.full(N, 9.81), rng.uniform(0.8, 1.0, N), W])
+    return u0, p, np.vstack([np.zeros(N), np.full(N, 6.0)])
+
+
+@pytest.mark.parametrize("alg", ["tsit5", "vern7"])
+def test_registered_vector_callback_matches_oracle(with_callbacks, alg):
+    from odegb300 import ContinuousCallback
+    N = 128
+    u0, p, ts = box_inputs(N)
+    cb = ContinuousCallback(interp_points=10, max_events=64)
+    g = gpu("box", alg, u0, p, ts, 0.25, 1e-8, 1e-8, callback=cb)
+    o = oracle_of_cb("box", alg, u0, p, ts, 0.25, 1e-8, 1e-8, cb)
+    c = compare(g, o, 1e-8, 1e-8)
+    assert c["ok"] and c["steps_ok"], c
+    assert (g["nsaved"] > 25).all()   # every trajectory hit a wall or the floor (two saves per event)
+
+
+def test_registered_discrete_callback_matches_oracle(with_callbacks):
+    from odegb300 import DiscreteCallback
+    N = 256
+    rng = np.random.default_rng(3)
+    p = np.vstack([rng.uniform(0.3, 1.0, N), rng.uniform(0.2, 0.5, N), np.ones(N)])
+    u0 = rng.uniform(0.8, 1.5, (1, N))
+    ts = np.vstack([np.zeros(N), np.full(N, 20.0)])
+    cb = DiscreteCallback(max_events=64)
+    g = gpu("thr", "tsit5", u0, p, ts, 0.5, 1e-8, 1e-10, callback=cb)
+    o = oracle_of_cb("thr", "tsit5", u0, p, ts, 0.5, 1e-8, 1e-10, cb)
+    c = compare(g, o, 1e-8, 1e-10)
+    assert c["ok"] and c["steps_ok"], c
+    assert (g["nsaved"] > 41).all()   # doses happened (two extra saves each)
+
+
+def oracle_of_cb(name, alg, u0, p, ts, saveat, rt, at, cb):
+    return oracle(name, alg, u0, p, ts, saveat, rt, at, callback=True, interp_points=cb.interp_points,
+                  max_events=cb.max_events)

@@ -496,3 +496,50 @@ def test_tgrad_is_not_an_f_call():
                 reltol=1e-6, abstol=1e-6)
     st = r["stats"]
     assert st["nf"] == 8 * (st["naccept"] + st["nreject"]) + 2, st
+
+
+# ---------------------------------------------------------------- vector and state-triggered callbacks
+# A ball in a box (x in [0, W], floor y = 0) with a VectorContinuousCallback of
+# three conditions (floor, left wall, right wall; lib/DiffEqBase/src/callbacks.jl:
+# 239-362 and 495-523); with restitution e = 1 both motions are exact: x(t) is
+# the unfolded straight line folded back into [0, W], y(t) a train of equal
+# parabolas after the first contact.
+def box_exact(t, x0, y0, vx, vy0, g, W):
+    s = np.mod(x0 + vx * t, 2 * W)
+    x = np.where(s <= W, s, 2 * W - s)
+    vb = np.sqrt(vy0 * vy0 + 2 * g * y0)
+    t1 = (vy0 + vb) / g
+    tau = np.mod(t - t1, 2 * vb / g)
+    y = np.where(t < t1, y0 + vy0 * t - 0.5 * g * t * t, vb * tau - 0.5 * g * tau * tau)
+    return x, y
+
+
+@pytest.mark.parametrize("alg", [O.TSIT5, O.VERN7])
+def test_ball_in_a_box_vector_callback_matches_the_closed_form(alg):
+    x0, y0, vx, vy0, g, W = 1.3, 7.0, 2.9, 1.5, 9.81, 4.0
+    sv = np.linspace(0.25, 10.0, 40)
+    r = O.solve(alg, O.BALL_BOX, [x0, y0, vx, vy0], [g, 1.0, W], (0.0, 10.0), saveat=sv, reltol=1e-10,
+                abstol=1e-10, callback=True, max_events=64)
+    assert r["retcode"] == 1
+    at = np.isin(r["t"], sv) & np.concatenate([[True], np.diff(r["t"]) != 0])
+    x, y = box_exact(r["t"][at], x0, y0, vx, vy0, g, W)
+    assert np.allclose(r["u"][at, 0], x, atol=1e-7) and np.allclose(r["u"][at, 1], y, atol=1e-6)
+    # the walls and the floor were each hit, and the saves bracket every event
+    ev = np.flatnonzero(np.diff(r["t"]) == 0)
+    assert len(ev) >= 8
+    assert np.all((np.abs(r["u"][ev, 0]) < 1e-8) | (np.abs(r["u"][ev, 0] - W) < 1e-8) | (np.abs(r["u"][ev, 1]) < 1e-8))
+
+
+def test_state_triggered_discrete_callback_doses_below_the_threshold():
+    k, thr, dose = 0.7, 0.4, 1.0
+    r = O.solve(O.TSIT5, O.THRESHOLD_DOSE, [1.2], [k, thr, dose], (0.0, 20.0), saveat=[], saveat_given=False,
+                reltol=1e-8, abstol=1e-10, save_everystep=True, max_step_saves=4096, save_start=True,
+                callback=True, max_events=64)
+    t, c = r["t"], r["u"][:, 0]
+    jumps = np.flatnonzero(np.diff(t) == 0)          # the pre- and post-affect saves share t
+    assert len(jumps) >= 5
+    assert np.allclose(c[jumps + 1] - c[jumps], dose)
+    assert np.all(c[jumps] < thr) and np.all(c[jumps] > thr * np.exp(-k))   # caught within a step
+    # between doses the decay is exact: c(t2) = c(t1) exp(-k (t2 - t1))
+    for a, b in zip(jumps[:-1] + 1, jumps[1:]):
+        assert abs(c[b] - c[a] * np.exp(-k * (t[b] - t[a]))) < 1e-7
