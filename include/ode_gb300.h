@@ -20,8 +20,9 @@
  * structure-of-arrays with the trajectory index fastest:
  *   u0[i*N + j]          state i of trajectory j            (n_states x N)
  *   p[k*N + j]           parameter k of trajectory j        (n_params x N)
- *   tspan[j], tspan[N+j] t0 and tf of trajectory j          (2 x N)
- *   saveat[s] shared, or saveat[s*N + j] per trajectory     (nsave or nsave x N)
+ *   tspan[j], tspan[N+j] t0 and tf of trajectory j          (2 x N; tf < t0 integrates backward)
+ *   saveat[s] shared, or saveat[s*N + j] per trajectory     (nsave or nsave x N; ascending in s
+ *                                                           whatever the direction)
  *   t_out[s*N + j], u_out[(s*n_states + i)*N + j]           (cap x N, cap x n_states x N)
  * with cap = nsave + 2 save slots per trajectory (start and end saves), or
  * max_step_saves + 2 with save_everystep, plus 2 * max_events with a callback.
@@ -120,8 +121,7 @@ enum ode_retcode {
     ODE_RC_DTLESSTHANMIN = 4, ODE_RC_UNSTABLE = 5,
     ODE_RC_ABORTED = 6, /* stopped by ode_abort(); no reference counterpart */
     ODE_RC_TERMINATED = 7, /* a callback called terminate! (ReturnCode.Terminated) */
-    ODE_RC_INITIALFAILURE = 8 /* tf < t0 or a NaN time span: backward integration is not supported, the
-                                 trajectory is not stepped (ReturnCode.InitialFailure) */
+    ODE_RC_INITIALFAILURE = 8 /* a NaN time span: the trajectory is not stepped (ReturnCode.InitialFailure) */
 };
 
 enum ode_status {
@@ -154,7 +154,7 @@ typedef struct {
     int64_t maxiters;           /* <= 0: 1e6 */
     int32_t save_start, save_end;
     int32_t save_end_user;      /* -1 not given, else 0/1 (endpoint rule, integrator_utils.jl:540-588) */
-    int32_t saveat_scalar;      /* saveat was a number (t0+dt:dt:tf) */
+    int32_t saveat_scalar;      /* saveat was a number ((t0 + tdir|d|):(tdir|d|):tf) */
     int32_t nsave;              /* saveat entries (0 = no saveat) */
     int32_t saveat_per_traj;    /* 0: saveat[nsave] shared; 1: saveat[nsave*N] */
     double qmax_first_step;     /* <= 0: 10000 */

@@ -197,6 +197,16 @@ void rhs(int model, int n, const double* u, const double* p, double t, double* d
     }
 }
 
+// Parameters each model reads (the dense record keeps a copy for the Vern7 extra stages).
+int model_nparams(int model) {
+    switch (model) {
+    case ORC_LINEAR: case ORC_VANDERPOL: return 1;
+    case ORC_LOTKA_VOLTERRA: return 4;
+    case ORC_FORCED_DUFFING: return 5;
+    default: return 3;   // ORC_THRESHOLD_DOSE and ORC_BALL_BOX read at most 3 (callbacks included)
+    }
+}
+
 // Analytic Jacobians (row-major J[i*n + j] = d f_i / d u_j).
 void jac(int model, int n, const double* u, const double* p, double t, double* J) {
     (void)t;
@@ -312,6 +322,7 @@ struct Integ {
     int alg, model, n;
     const double* p;
     double t0, tf;
+    double tdir;   // sign(tf - t0) (solve.jl:273); +1 for t0 == tf
     orc_opts o;
     double t, dt, tprev, dtpropose, dtcache;
     double EEst, q11, errold;
@@ -327,10 +338,10 @@ struct Integ {
     std::vector<double> J, W, dT, ks, rhs, du;
     std::vector<int> piv;
     bool have_J;
-    std::vector<double> tstops;  // ascending
+    std::vector<double> tstops;  // tdir * t, ascending (the reference's directional heap)
     size_t itstop;
     std::vector<double> dtimes;  // the tstops as given, sorted: the discrete callback's times
-    std::vector<double> saveat;
+    std::vector<double> saveat;  // tdir * t, ascending
     size_t isave;
     double* t_out;
     double* u_out;
@@ -357,9 +368,12 @@ struct Integ {
 };
 
 thread_local int64_t g_rhs_calls = 0;  // counts every RHS call (the reference's counting-wrapper tests)
+thread_local std::vector<double> g_eval_times;   // the t of every RHS call, while recording
+thread_local bool g_record_times = false;
 
 inline void f_eval(Integ& I, const double* u, double t, double* du) {
     ++g_rhs_calls;
+    if (g_record_times) g_eval_times.push_back(t);
     rhs(I.model, I.n, u, I.p, t, du);
 }
 
@@ -376,12 +390,17 @@ double residual_norm(Integ& I, const double* ut, const double* u0, const double*
     return std::sqrt(acc / (double)(I.n > 1 ? I.n : 1));
 }
 
-// Hairer initial step: lib/OrdinaryDiffEqCore/src/initdt.jl:17-298 (iip).
+// Hairer initial step: lib/OrdinaryDiffEqCore/src/initdt.jl:17-298 (iip); the
+// result carries the direction tdir.  Its dtmax is the distance to the first
+// tstop when that is smaller (_determine_initdt, integrator_interface.jl:644-656),
+// so the trial evaluation stays before it.
 double initdt(Integ& I) {
     int n = I.n;
     const double* u0 = I.u.data();
     double t = I.t;
-    double dtmax = I.o.dtmax;
+    const double tdir = I.tdir;
+    const double first_tstop = I.itstop < I.tstops.size() ? I.tstops[I.itstop] : tdir * I.tf;
+    double dtmax = jmin(std::fabs(I.o.dtmax), std::fabs(first_tstop - tdir * t));   // dtmax_tdir
     double dtmin = std::nextafter(jmax(I.o.dtmin, jeps(t)), INFINITY);
     double smalldt = jmax(dtmin, 1e-6);
     std::vector<double> sk(n), f0(n), f1(n), u1(n), tmp(n);
@@ -397,15 +416,16 @@ double initdt(Integ& I) {
     double d0 = nrm(tmp);
     for (int i = 0; i < n; ++i) tmp[i] = f0[i] / sk[i];
     double d1 = nrm(tmp);
-    if (d1 != d1) return dtmin;
+    if (d1 != d1) return tdir * dtmin;
     double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? smalldt : (d0 / d1) / 100.0;
     dt0 = jmin(dt0, dtmax);
-    if (dt0 < 10.0 * 2.220446049250313e-16) return jmax(smalldt, dtmin);
-    for (int i = 0; i < n; ++i) u1[i] = std::fma(dt0, f0[i], u0[i]);
-    f_eval(I, u1.data(), t + dt0, f1.data());
+    if (dt0 < 10.0 * 2.220446049250313e-16) return tdir * jmax(smalldt, dtmin);
+    const double dt0_tdir = tdir * dt0;
+    for (int i = 0; i < n; ++i) u1[i] = std::fma(dt0_tdir, f0[i], u0[i]);
+    f_eval(I, u1.data(), t + dt0_tdir, f1.data());
     bool same = true;
     for (int i = 0; i < n; ++i) same = same && (f0[i] == f1[i]);
-    if (n > 0 && same) return jmax(dtmin, 100.0 * dt0);
+    if (n > 0 && same) return tdir * jmax(dtmin, 100.0 * dt0);
     for (int i = 0; i < n; ++i) tmp[i] = (f1[i] - f0[i]) / sk[i];
     double d2 = nrm(tmp) / dt0;
     double mx = jmax(d1, d2);
@@ -417,7 +437,7 @@ double initdt(Integ& I) {
         const double LN10 = 2.302585092994046;
         dt1 = series_exp(-(2.0 * LN10 + series_ln(mx)) / (double)I.order);
     }
-    return jmax(dtmin, jmin(jmin(100.0 * dt0, dt1), dtmax));
+    return tdir * jmax(dtmin, jmin(jmin(100.0 * dt0, dt1), dtmax));
 }
 
 // ---------------------------------------------------------------- Tsit5
@@ -870,8 +890,8 @@ void push_save(Integ& I, double t, const double* v) {
 
 // _savevalues!: lib/OrdinaryDiffEqCore/src/integrators/integrator_utils.jl:340-414.
 void savevalues(Integ& I) {
-    while (I.isave < I.saveat.size() && I.saveat[I.isave] <= I.t) {
-        double curt = I.saveat[I.isave++];
+    while (I.isave < I.saveat.size() && I.saveat[I.isave] <= I.tdir * I.t) {
+        double curt = I.tdir * I.saveat[I.isave++];
         if (curt != I.t) {
             double th = (curt - I.tprev) / I.dt;
             interpolate(I, th, I.interp_out.data());
@@ -892,36 +912,45 @@ void savevalues(Integ& I) {
 // modify_dt_for_tstops!: integrator_utils.jl:268-324.
 void modify_dt_for_tstops(Integ& I) {
     if (I.itstop >= I.tstops.size()) { I.next_step_tstop = false; return; }
-    double tstop = I.tstops[I.itstop];
-    double dist = std::fabs(tstop - I.t);
-    double tol = (std::isfinite(tstop) && std::isfinite(I.t)) ? 100.0 * jeps(jmax(std::fabs(I.t), std::fabs(tstop))) : 0.0;
+    const double tdir_tstop = I.tstops[I.itstop];
+    const double tdir_t = I.tdir * I.t;
+    double dist = std::fabs(tdir_tstop - tdir_t);
+    double tol = (std::isfinite(tdir_tstop) && std::isfinite(I.t))
+                     ? 100.0 * jeps(jmax(std::fabs(I.t), std::fabs(tdir_tstop))) : 0.0;
     if (I.o.adaptive) {
         double orig = std::fabs(I.dt);
-        I.dtpropose = orig;
+        I.dtpropose = I.tdir * orig;
         if (orig + tol < dist) {
             I.next_step_tstop = false;
         } else {
             I.next_step_tstop = true;
-            I.tstop_target = tstop;
+            I.tstop_target = I.tdir * tdir_tstop;
         }
-        I.dt = jmin(orig, dist);
+        I.dt = I.tdir * jmin(orig, dist);
     } else {
         if (std::fabs(I.dtcache) + tol < dist) {
             I.next_step_tstop = false;
         } else {
             I.next_step_tstop = true;
-            I.tstop_target = tstop;
+            I.tstop_target = I.tdir * tdir_tstop;
         }
-        I.dt = jmin(std::fabs(I.dtcache), dist);
+        I.dt = I.tdir * jmin(std::fabs(I.dtcache), dist);
     }
 }
 
 inline double dtmin_t(const Integ& I) { return std::fabs(jmax(jeps(I.t), I.o.dtmin)); }
 
-// fix_dt_at_bounds!: integrator_utils.jl:1243-1256.
+// fix_dt_at_bounds!: integrator_utils.jl:1243-1256.  Backward, the reference
+// bounds dt by min(dt, dtmin) with the positive dtmin, which leaves a negative dt
+// as it is: the lower bound applies forward only.
 void fix_dt_at_bounds(Integ& I) {
-    I.dt = jmin(I.o.dtmax, I.dt);
-    I.dt = jmax(I.dt, dtmin_t(I));
+    if (I.tdir > 0) {
+        I.dt = jmin(I.o.dtmax, I.dt);
+        I.dt = jmax(I.dt, dtmin_t(I));
+    } else {
+        I.dt = jmax(I.o.dtmax, I.dt);
+        I.dt = jmin(I.dt, dtmin_t(I));
+    }
 }
 
 // PI controller: lib/OrdinaryDiffEqCore/src/integrators/controllers.jl:805-843.
@@ -1010,8 +1039,13 @@ bool is_event(const Integ& I, double bs, double ts) {
 // retained end's value is scaled by 1 - f_new/f_replaced, or 1/2 when that is
 // not positive) with a bisection whenever the bracket has not halved over two
 // steps or the secant point is not strictly inside.  fa = f(a), fb = f(b) of
-// opposite signs, nonzero.
+// opposite signs, nonzero.  a is the end first in the integration direction
+// (a > b backward); the iteration runs on tdir * t and returns the root's side
+// towards a.
 double find_root_left(Integ& I, double a, double b, double fa, double fb) {
+    const double d = I.tdir;
+    a *= d;
+    b *= d;
     int side = 0;
     double w_prev = b - a, w_prev2 = 2.0 * (b - a);
     for (int it = 0; it < 2200; ++it) {
@@ -1019,8 +1053,8 @@ double find_root_left(Integ& I, double a, double b, double fa, double fb) {
         double m = (w > 0.5 * w_prev2) ? a + w * 0.5 : a + w * (fa / (fa - fb));
         if (!(m > a && m < b)) m = a + w * 0.5;
         if (!(m > a && m < b)) break;
-        const double fm = cond_at(I, m);
-        if (fm == 0.0) return m;
+        const double fm = cond_at(I, d * m);
+        if (fm == 0.0) return d * m;
         w_prev2 = w_prev;
         w_prev = w;
         if ((fm > 0.0) == (fa > 0.0)) {
@@ -1041,7 +1075,7 @@ double find_root_left(Integ& I, double a, double b, double fa, double fb) {
             side = +1;
         }
     }
-    return a;
+    return d * a;
 }
 
 // find_callback_time(integrator, ::ContinuousCallback, idx) (callbacks.jl:364-412),
@@ -1114,7 +1148,7 @@ void recompute_step_k(Integ& I) {
 // apply_callback! (callbacks.jl:557-643) for a ContinuousCallback.
 void apply_callback(Integ& I, double cb_t, double bottom_sign) {
     if (I.o.adaptive) {   // set_proposed_dt! (integrator_interface.jl:180-182), dtrelax = 1
-        I.dtpropose = jmax(std::nextafter(I.o.dtmin, INFINITY), 1.0 * I.dt);
+        I.dtpropose = I.tdir * jmax(std::nextafter(I.o.dtmin, INFINITY), I.tdir * 1.0 * I.dt);
         I.dtcache = I.dtpropose;
     }
     // change_t_via_interpolation! (integrator_interface.jl:5-40)
@@ -1188,6 +1222,9 @@ void vcond_at(Integ& I, double abst, double* out) {
 }
 // one component of the vector condition, as a function of t (find_root's zero_func)
 double find_root_left_component(Integ& I, int k, double a, double b, double fa, double fb) {
+    const double d = I.tdir;
+    a *= d;
+    b *= d;
     int side = 0;
     double w_prev = b - a, w_prev2 = 2.0 * (b - a);
     double o[BOX_EVENTS];
@@ -1196,9 +1233,9 @@ double find_root_left_component(Integ& I, int k, double a, double b, double fa, 
         double m = (w > 0.5 * w_prev2) ? a + w * 0.5 : a + w * (fa / (fa - fb));
         if (!(m > a && m < b)) m = a + w * 0.5;
         if (!(m > a && m < b)) break;
-        vcond_at(I, m, o);
+        vcond_at(I, d * m, o);
         const double fm = o[k];
-        if (fm == 0.0) return m;
+        if (fm == 0.0) return d * m;
         w_prev2 = w_prev;
         w_prev = w;
         if ((fm > 0.0) == (fa > 0.0)) {
@@ -1219,7 +1256,7 @@ double find_root_left_component(Integ& I, int k, double a, double b, double fa, 
             side = +1;
         }
     }
-    return a;
+    return d * a;
 }
 
 // find_callback_time(integrator, ::VectorContinuousCallback, idx)
@@ -1276,7 +1313,7 @@ bool find_vector_callback_time(Integ& I, double& cb_t, int* events, double& resi
         cb_t = I.t;
         return false;
     }
-    cb_t = std::nextafter(top_t, INFINITY);   // rightfloat(top_t, tdir)
+    cb_t = std::nextafter(top_t, I.tdir * INFINITY);   // rightfloat(top_t, tdir)
     for (int i = 0; i < M; ++i) {
         if (!ev[i]) continue;
         double cbi;
@@ -1287,9 +1324,9 @@ bool find_vector_callback_time(Integ& I, double& cb_t, int* events, double& resi
         } else {
             cbi = find_root_left_component(I, i, I.tprev, top_t, bc[i], tc[i]);
         }
-        if (cbi < cb_t)
+        if (I.tdir * cbi < I.tdir * cb_t)
             for (int k = 0; k < M; ++k) events[k] = 0;
-        if (cbi <= cb_t) {
+        if (I.tdir * cbi <= I.tdir * cb_t) {
             cb_t = cbi;
             double o[M];
             vcond_at(I, cbi, o);
@@ -1305,7 +1342,7 @@ bool find_vector_callback_time(Integ& I, double& cb_t, int* events, double& resi
 // e = p[2]) and vx at a wall.
 void apply_vector_callback(Integ& I, double cb_t, const int* events) {
     if (I.o.adaptive) {
-        I.dtpropose = jmax(std::nextafter(I.o.dtmin, INFINITY), 1.0 * I.dt);
+        I.dtpropose = I.tdir * jmax(std::nextafter(I.o.dtmin, INFINITY), I.tdir * 1.0 * I.dt);
         I.dtcache = I.dtpropose;
     }
     if (cb_t != I.t) {
@@ -1398,9 +1435,9 @@ void loopfooter(Integ& I) {
             }
             if (I.qsteady_min <= q && q <= I.qsteady_max) q = 1.0;
             I.errold = jmax(I.EEst, I.qoldinit);
-            double dtnew = I.dt / q;
-            double dtp = jmin(std::fabs(I.o.dtmax), std::fabs(dtnew));
-            dtp = jmax(std::fabs(dtp), dtmin_t(I));
+            double dtnew = I.dt / q;   // calc_dt_propose! (integrator_utils.jl:1199-1209)
+            double dtp = I.tdir * jmin(std::fabs(I.o.dtmax), std::fabs(dtnew));
+            dtp = I.tdir * jmax(std::fabs(dtp), dtmin_t(I));
             I.dtpropose = dtp;
             record_dense(I);
             handle_callbacks(I);
@@ -1504,7 +1541,8 @@ int check_error(Integ& I) {
     if (I.iter > I.o.maxiters) return ORC_RC_MAXITERS;
     bool acc = I.accept_step;
     if (I.o.adaptive) {
-        double next_tstop = I.itstop < I.tstops.size() ? I.tstops[I.itstop] : INFINITY;
+        // t + dt < tdir * first(tstops), as the reference writes it for either direction
+        double next_tstop = I.itstop < I.tstops.size() ? I.tdir * I.tstops[I.itstop] : I.tdir * INFINITY;
         if (std::fabs(I.dt) <= std::fabs(I.o.dtmin) && (!acc || I.t + I.dt < next_tstop))
             return ORC_RC_DTLESSTHANMIN;
         if (!acc && std::fabs(I.dt) <= std::fabs(jeps(I.t))) return ORC_RC_UNSTABLE;
@@ -1527,7 +1565,7 @@ void postamble(Integ& I) {
             if (I.o.saveat_scalar) {
                 in_saveat = false;
             } else {
-                for (double s : I.saveat) in_saveat = in_saveat || (s == I.t);
+                for (double s : I.saveat) in_saveat = in_saveat || (I.tdir * s == I.t);
             }
         }
         need = I.last_saved_t != I.t &&
@@ -1595,7 +1633,7 @@ int solve_one(Integ& I, const double* u0) {
         I.st.nf += 1;
     }
     if (I.o.dt > 0.0) {
-        I.dt = I.o.dt;
+        I.dt = I.tdir * I.o.dt;   // a positive dt is taken in the direction (handle_dt!, solve.jl:949-966)
     } else {
         I.dt = initdt(I);
         I.st.nf += 2;
@@ -1605,7 +1643,7 @@ int solve_one(Integ& I, const double* u0) {
     int rc = ORC_RC_DEFAULT;
     while (I.itstop < I.tstops.size()) {
         double first_tstop = I.tstops[I.itstop];
-        while (I.t < first_tstop) {
+        while (I.tdir * I.t < first_tstop) {
             loopheader(I);
             int e = I.do_error_check ? check_error(I) : ORC_RC_SUCCESS;   // solve.jl:909
             if (e != ORC_RC_SUCCESS) {
@@ -1623,8 +1661,8 @@ int solve_one(Integ& I, const double* u0) {
             if (I.itstop >= I.tstops.size() || should_exit) break;
         }
         // handle_tstop!: integrator_utils.jl:1290-1314
-        if (I.itstop < I.tstops.size() && I.t == I.tstops[I.itstop]) {
-            while (I.itstop < I.tstops.size() && I.tstops[I.itstop] == I.t) I.itstop++;
+        if (I.itstop < I.tstops.size() && I.tdir * I.t == I.tstops[I.itstop]) {
+            while (I.itstop < I.tstops.size() && I.tstops[I.itstop] == I.tdir * I.t) I.itstop++;
         }
     }
     postamble(I);
@@ -1640,8 +1678,11 @@ void setup(Integ& I, int alg, int model, int n, const double* p, double t0, doub
     I.p = p;
     I.t0 = t0;
     I.tf = tf;
+    I.tdir = tf < t0 ? -1.0 : 1.0;
     I.o = *o;
+    // default tf - t0; a positive dtmax is taken in the direction (solve.jl:153,401)
     if (I.o.dtmax <= 0.0) I.o.dtmax = tf - t0;
+    else I.o.dtmax *= I.tdir;
     if (I.o.maxiters <= 0) I.o.maxiters = 1000000;
     I.order = alg == ORC_VERN7 ? 7 : alg == ORC_VERN9 ? 9 : alg == ORC_ROSENBROCK23 ? 2 : 5;   // composite: Tsit5's
     // controller defaults: lib/OrdinaryDiffEqCore/src/alg_utils.jl:407-879
@@ -1654,15 +1695,18 @@ void setup(Integ& I, int alg, int model, int n, const double* p, double t0, doub
     I.qsteady_min = 1.0;
     I.qsteady_max = (alg == ORC_RODAS5P || alg == ORC_ROSENBROCK23) ? 1.2 : 1.0;   // AdaptiveImplicit: 6/5
     I.qoldinit = 1e-4;
+    // initialize_tstops / initialize_saveat (solve.jl:1021-1040, 1103-1124): tdir * t
+    // inside the span, ascending
+    const double d = I.tdir, dt0 = d * t0, dtf = d * tf;
     I.tstops.clear();
     for (int i = 0; i < ntstops; ++i)
-        if (tstops[i] > t0 && tstops[i] < tf) I.tstops.push_back(tstops[i]);
-    I.tstops.push_back(tf);
+        if (dt0 < d * tstops[i] && d * tstops[i] < dtf) I.tstops.push_back(d * tstops[i]);
+    I.tstops.push_back(dtf);
     std::sort(I.tstops.begin(), I.tstops.end());
     I.itstop = 0;
     I.saveat.clear();
     for (int i = 0; i < nsave; ++i)
-        if (saveat[i] > t0 && saveat[i] <= tf) I.saveat.push_back(saveat[i]);
+        if (dt0 < d * saveat[i] && d * saveat[i] <= dtf) I.saveat.push_back(d * saveat[i]);
     std::sort(I.saveat.begin(), I.saveat.end());
     I.isave = 0;
     I.dense = nullptr;
@@ -1676,6 +1720,18 @@ int64_t orc_rhs_calls(int reset) {
     int64_t v = g_rhs_calls;
     if (reset) g_rhs_calls = 0;
     return v;
+}
+
+int orc_record_eval_times(int enable) {
+    g_record_times = enable != 0;
+    g_eval_times.clear();
+    return 0;
+}
+
+int orc_eval_times(double* out, int cap) {
+    const int m = (int)g_eval_times.size() < cap ? (int)g_eval_times.size() : cap;
+    for (int i = 0; i < m; ++i) out[i] = g_eval_times[i];
+    return (int)g_eval_times.size();
 }
 
 void orc_rhs(int model, int n, const double* u, const double* p, double t, double* du) {
@@ -1706,8 +1762,7 @@ int orc_solve(int alg, int model, int n, const double* p, double t0, double tf, 
         D->alg = alg;
         D->model = model;
         D->n = n;
-        int np = (model == ORC_LINEAR || model == ORC_VANDERPOL) ? 1 : 3;   // every other model has 3
-        D->p.assign(p, p + np);
+        D->p.assign(p, p + model_nparams(model));
         I.dense = D;
         *dense_handle = D;
     }
@@ -1738,11 +1793,12 @@ int orc_dense_eval(void* h, const double* tq, int nq, double* out) {
     if (D->steps.empty()) return -1;
     const size_t ns = D->steps.size() + 1;
     auto ts = [&](size_t i) { return i == 0 ? D->steps[0].tprev : D->steps[i - 1].tend; };
+    const double tdir = ts(ns - 1) < ts(0) ? -1.0 : 1.0;   // sign(ts[end] - ts[1])
     std::vector<double> K;
     for (int q = 0; q < nq; ++q) {
         const double t = tq[q];
         size_t ip = 1;
-        while (ip < ns && ts(ip) < t) ++ip;
+        while (ip < ns && tdir * ts(ip) < tdir * t) ++ip;
         if (ip > ns - 1) ip = ns - 1;
         const size_t im = ip - 1;
         const Step& S = D->steps[ip - 1];

@@ -96,6 +96,11 @@ int orc_last_alg_choice(int32_t* out, int cap);
  * wrapper, test/InterfaceIII/stats_tests.jl:5-13); reset when asked. */
 int64_t orc_rhs_calls(int reset);
 
+/* Record the t of every RHS call this thread makes (enable 1; also clears the
+ * record), and read it back: returns the number recorded, writes at most cap. */
+int orc_record_eval_times(int enable);
+int orc_eval_times(double* out, int cap);
+
 /* Model right-hand side and Jacobian (for tests of the models themselves). */
 void orc_rhs(int model, int n, const double* u, const double* p, double t, double* du);
 void orc_jac(int model, int n, const double* u, const double* p, double t, double* J);

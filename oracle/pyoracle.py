@@ -72,6 +72,9 @@ def lib():
         L.orc_last_alg_choice.argtypes = [C.POINTER(C.c_int32), C.c_int]
         L.orc_rhs_calls.restype = C.c_int64
         L.orc_rhs_calls.argtypes = [C.c_int]
+        L.orc_record_eval_times.argtypes = [C.c_int]
+        L.orc_eval_times.restype = C.c_int
+        L.orc_eval_times.argtypes = [dp, C.c_int]
         L.orc_rhs.argtypes = [C.c_int, C.c_int, dp, dp, C.c_double, dp]
         L.orc_jac.argtypes = [C.c_int, C.c_int, dp, dp, C.c_double, dp]
         L.orc_tgrad.restype = C.c_int
@@ -222,3 +225,15 @@ def tgrad(model, u, p, t=0.0):
 
 def rhs_calls(reset=False):
     return lib().orc_rhs_calls(int(reset))
+
+
+def record_eval_times(enable=True):
+    lib().orc_record_eval_times(int(enable))
+
+
+def eval_times():
+    """The t of every RHS call since record_eval_times() (this thread)."""
+    n = lib().orc_eval_times(None, 0)
+    out = np.zeros(n)
+    lib().orc_eval_times(_dp(out), n)
+    return out

@@ -266,9 +266,11 @@ __device__ __forceinline__ typename Ctl<R>::T error_norm(const R* ut, const R* u
 }
 
 // Hairer's initial step (initdt.jl:17-298).  f0 is returned for FSAL methods.
+// t is the model's time; bwd: the integration runs towards smaller t, so the
+// trial step goes to t - dt0 (dt0_tdir), and the magnitude is returned.
 template <class Model, class R, int L, int C, int ORDER>
-__device__ double initdt(const R* u0, const PR<R>* p, double t, double dtmax, double dtmin_user, R abstol, R reltol,
-                         R* f0, const Group<L>& g) {
+__device__ double initdt(const R* u0, const PR<R>* p, double t, bool bwd, double dtmax, double dtmin_user, R abstol,
+                         R reltol, R* f0, const Group<L>& g) {
     double dtmin = nextafter(jmax(dtmin_user, jeps(t)), __longlong_as_double(0x7ff0000000000000LL));
     double smalldt = jmax(dtmin, 1e-6);
     R sk[C], f1[C], u1[C];
@@ -289,10 +291,11 @@ __device__ double initdt(const R* u0, const PR<R>* p, double t, double dtmax, do
     double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? smalldt : (d0 / d1) / 100.0;
     dt0 = jmin(dt0, dtmax);
     if (dt0 < 10.0 * 2.220446049250313e-16) return jmax(smalldt, dtmin);
-    R dt0r = (R)dt0;
+    const double dt0_tdir = bwd ? -dt0 : dt0;
+    R dt0r = (R)dt0_tdir;
 #pragma unroll
     for (int c = 0; c < C; ++c) u1[c] = FMA(dt0r, f0[c], u0[c]);
-    Model::template rhs<R, L, C>(f1, u1, p, t + dt0, g);
+    Model::template rhs<R, L, C>(f1, u1, p, t + dt0_tdir, g);
     bool diff = false;
 #pragma unroll
     for (int c = 0; c < C; ++c) diff = diff || (f0[c] != f1[c]);
@@ -329,7 +332,15 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
     for (int c = 0; c < C; ++c) Acc<R>::split(a.u0[(size_t)(g.lane * C + c) * N + j], u[c], ulo[c]);
 #pragma unroll
     for (int i = 0; i < NP; ++i) p[i] = make_param<R>(a.p[(size_t)i * N + j]);
-    const double t0 = a.tspan[j], tf = a.tspan[N + j];
+    // Backward integration (tf < t0) runs the loop on s = -t: its times, steps,
+    // tstops and saveat points are those of the reference negated (the
+    // reference's own heaps hold tdir * t), every comparison on them is the
+    // reference's with tdir taken out, and the model and the method see the
+    // model's time TM(s) = -s and signed step DT(h) = -h, so each stage and each
+    // interpolation is the reference's arithmetic exactly (negation is exact).
+    const bool bwd = a.tspan[N + j] < a.tspan[j];
+    auto TM = [bwd](double x) -> double { return bwd ? -x : x; };
+    const double t0 = TM(a.tspan[j]), tf = TM(a.tspan[N + j]);
     const double dtmax = a.dtmax > 0 ? a.dtmax : tf - t0;
     // the ensemble's tolerances, or per trajectory (requests merged into one
     // launch by the serving loop keep their own)
@@ -352,7 +363,7 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
         // past the capacity, step saves keep the latest point in the last slot
         const int slot = nsaved < a.nsave_cap ? nsaved : ((a.save_everystep || a.callback) ? a.nsave_cap - 1 : -1);
         if (slot >= 0) {
-            if (g.lane == 0 && a.t_out) a.t_out[(size_t)slot * N + j] = ts;
+            if (g.lane == 0 && a.t_out) a.t_out[(size_t)slot * N + j] = TM(ts);
 #pragma unroll
             for (int c = 0; c < C; ++c)
                 a.u_out[((size_t)slot * a.nmax + g.lane * C + c) * N + j] = Acc<R>::join(v[c], vlo[c]);
@@ -378,9 +389,12 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
                     !step ? 0.0 : over ? dnan() : (double)kv[c];
         }
     };
+    // the saveat points ascend; backward they are read from the end, negated
     auto saveat_at = [&](int s) -> double {
-        return a.saveat_per_traj ? a.saveat[(size_t)s * N + j] : a.saveat[s];
+        const int k = bwd ? a.nsave - 1 - s : s;
+        return TM(a.saveat_per_traj ? a.saveat[(size_t)k * N + j] : a.saveat[k]);
     };
+    auto tstop_at = [&](int k) -> double { return TM(a.tstops[bwd ? a.ntstops - 1 - k : k]); };
 
     // saveat entries outside (t0, tf] are skipped (initialize_saveat, solve.jl:1103-1124)
     while (isave < a.nsave && !(saveat_at(isave) > t0)) isave++;
@@ -393,13 +407,18 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
     }
 
     double t = t0, tprev = t0;
-    Alg::template initialize<Model, R, L, C>(cache, u, p, t, g, st, a, j);
+    Alg::template initialize<Model, R, L, C>(cache, u, p, TM(t), g, st, a, j);
     double dt;
     if (a.dt > 0) {
         dt = a.dt;
     } else {
-        dt = initdt<Model, R, L, C, Alg::ORDER>(u, p, t, dtmax, a.dtmin, abstol, reltol,
-                                                 Alg::template fsal_slot<R, C>(cache), g);
+        // the initial step's dtmax is at most the distance to the first tstop
+        // (_determine_initdt, integrator_interface.jl:644-656)
+        int k0 = 0;
+        while (k0 < a.ntstops && !(tstop_at(k0) > t0)) k0++;
+        const double first_tstop = (k0 < a.ntstops && tstop_at(k0) < tf) ? tstop_at(k0) : tf;
+        dt = initdt<Model, R, L, C, Alg::ORDER>(u, p, TM(t), bwd, jmin(fabs(dtmax), fabs(first_tstop - t0)), a.dtmin,
+                                                 abstol, reltol, Alg::template fsal_slot<R, C>(cache), g);
         st.nf += 2;
     }
     double dtpropose = dt;
@@ -408,7 +427,7 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
     bool do_error_check = true;
     long long iter = 0, success_iter = 0;
     bool accept = false, next_tstop = false;
-    // forward integration only: tf < t0 (or a NaN span) is not stepped
+    // a NaN span is not stepped
     int rc = (tf >= t0) ? RC_DEFAULT : RC_INITIALFAILURE;
 
     // _savevalues! (integrator_utils.jl:340-414) after an accepted step: saveat
@@ -425,8 +444,8 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             if (!deq(curt, t)) {
                 const double th = (double)Ctl<R>::theta(curt - tprev, dt);
                 R out[C], outlo[C];
-                Alg::template interpolate<Model, R, L, C>(cache, out, outlo, th, dt, tprev, uprev, uprevlo, y1, y1lo,
-                                                          p, g);
+                Alg::template interpolate<Model, R, L, C>(cache, out, outlo, th, TM(dt), TM(tprev), uprev, uprevlo, y1,
+                                                          y1lo, p, g);
                 save_point(curt, out, outlo);
             } else {
                 if (deq(curt, tf) && !a.save_end) continue;
@@ -461,13 +480,13 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
     auto handle_event = [&]() -> bool {
         if constexpr (Model::HAS_EVENT && event_len<Model>::value == 1) {
             auto cond_at = [&](double abst) -> double {
-                if (abst == t) return Model::template event_condition<R, L, C>(u, ulo, a.p + j, N, abst, g);
+                if (abst == t) return Model::template event_condition<R, L, C>(u, ulo, a.p + j, N, TM(abst), g);
                 if (abst == tprev)
-                    return Model::template event_condition<R, L, C>(uprev, uprevlo, a.p + j, N, abst, g);
+                    return Model::template event_condition<R, L, C>(uprev, uprevlo, a.p + j, N, TM(abst), g);
                 R v[C], vlo[C];
-                Alg::template interpolate<Model, R, L, C>(cache, v, vlo, (abst - tprev) / dt, dt, tprev, uprev,
+                Alg::template interpolate<Model, R, L, C>(cache, v, vlo, (abst - tprev) / dt, TM(dt), TM(tprev), uprev,
                                                           uprevlo, u, ulo, p, g);
-                return Model::template event_condition<R, L, C>(v, vlo, a.p + j, N, abst, g);
+                return Model::template event_condition<R, L, C>(v, vlo, a.p + j, N, TM(abst), g);
             };
             auto is_event = [](double bs, double ts) {
                 return ((bs < 0.0 && Model::EVENT_AFFECT_POS) || (bs > 0.0 && Model::EVENT_AFFECT_NEG)) &&
@@ -515,7 +534,7 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             for (int c = 0; c < C; ++c) { uend[c] = u[c]; uendlo[c] = ulo[c]; }
             if (moved) {
                 R v[C], vlo[C];
-                Alg::template interpolate<Model, R, L, C>(cache, v, vlo, (cb_t - tprev) / dt, dt, tprev, uprev,
+                Alg::template interpolate<Model, R, L, C>(cache, v, vlo, (cb_t - tprev) / dt, TM(dt), TM(tprev), uprev,
                                                           uprevlo, u, ulo, p, g);
 #pragma unroll
                 for (int c = 0; c < C; ++c) { u[c] = v[c]; ulo[c] = vlo[c]; }
@@ -525,14 +544,14 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             if (!savevalues(uend, uendlo)) save_point(t, u, ulo);
             bool modified = false;
             if (bs < 0.0 && Model::EVENT_AFFECT_POS) {
-                terminated = Model::template event_affect<R, L, C>(u, ulo, a.p + j, N, t, true, g);
+                terminated = Model::template event_affect<R, L, C>(u, ulo, a.p + j, N, TM(t), true, g);
                 modified = true;
             } else if (bs > 0.0 && Model::EVENT_AFFECT_NEG) {
-                terminated = Model::template event_affect<R, L, C>(u, ulo, a.p + j, N, t, false, g);
+                terminated = Model::template event_affect<R, L, C>(u, ulo, a.p + j, N, TM(t), false, g);
                 modified = true;
             }
             if (modified) save_point(t, u, ulo);   // save_positions[2]
-            if (!terminated && (moved || modified)) Alg::template reset_fsal<Model, R, L, C>(cache, u, ulo, p, t, g, st);
+            if (!terminated && (moved || modified)) Alg::template reset_fsal<Model, R, L, C>(cache, u, ulo, p, TM(t), g, st);
             return true;
         }
         return false;
@@ -555,14 +574,14 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             static_assert(M <= 32, "at most 32 conditions");
             auto conds_at = [&](double abst, double* out) {
                 if (abst == t) {
-                    Model::template event_conditions<R, L, C>(out, u, ulo, a.p + j, N, abst, g);
+                    Model::template event_conditions<R, L, C>(out, u, ulo, a.p + j, N, TM(abst), g);
                 } else if (abst == tprev) {
-                    Model::template event_conditions<R, L, C>(out, uprev, uprevlo, a.p + j, N, abst, g);
+                    Model::template event_conditions<R, L, C>(out, uprev, uprevlo, a.p + j, N, TM(abst), g);
                 } else {
                     R v[C], vlo[C];
-                    Alg::template interpolate<Model, R, L, C>(cache, v, vlo, (abst - tprev) / dt, dt, tprev, uprev,
-                                                              uprevlo, u, ulo, p, g);
-                    Model::template event_conditions<R, L, C>(out, v, vlo, a.p + j, N, abst, g);
+                    Alg::template interpolate<Model, R, L, C>(cache, v, vlo, (abst - tprev) / dt, TM(dt), TM(tprev),
+                                                              uprev, uprevlo, u, ulo, p, g);
+                    Model::template event_conditions<R, L, C>(out, v, vlo, a.p + j, N, TM(abst), g);
                 }
             };
             double bc[M], bs[M], nc[M], tc[M];
@@ -652,16 +671,16 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             for (int c = 0; c < C; ++c) { uend[c] = u[c]; uendlo[c] = ulo[c]; }
             if (moved) {
                 R v[C], vlo[C];
-                Alg::template interpolate<Model, R, L, C>(cache, v, vlo, (cb_t - tprev) / dt, dt, tprev, uprev,
+                Alg::template interpolate<Model, R, L, C>(cache, v, vlo, (cb_t - tprev) / dt, TM(dt), TM(tprev), uprev,
                                                           uprevlo, u, ulo, p, g);
 #pragma unroll
                 for (int c = 0; c < C; ++c) { u[c] = v[c]; ulo[c] = vlo[c]; }
                 t = cb_t;
             }
             if (!savevalues(uend, uendlo)) save_point(t, u, ulo);
-            terminated = Model::template vector_event_affect<R, L, C>(u, ulo, a.p + j, N, t, dir, g);
+            terminated = Model::template vector_event_affect<R, L, C>(u, ulo, a.p + j, N, TM(t), dir, g);
             save_point(t, u, ulo);
-            if (!terminated) Alg::template reset_fsal<Model, R, L, C>(cache, u, ulo, p, t, g, st);
+            if (!terminated) Alg::template reset_fsal<Model, R, L, C>(cache, u, ulo, p, TM(t), g, st);
             return true;
         }
         return false;
@@ -675,8 +694,8 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
     int itst = 0;
     while (t < tf) {
         // ---- loopheader!
-        while (itst < a.ntstops && !(a.tstops[itst] > t)) itst++;
-        const double tnext = (itst < a.ntstops && a.tstops[itst] < tf) ? a.tstops[itst] : tf;   // first_tstop
+        while (itst < a.ntstops && !(tstop_at(itst) > t)) itst++;
+        const double tnext = (itst < a.ntstops && tstop_at(itst) < tf) ? tstop_at(itst) : tf;   // first_tstop
         const double dist = tnext - t;   // > 0 inside the loop
         if (iter > 0) {
             if (accept) {
@@ -712,12 +731,13 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
                 beta1 = (CT)K2.beta1;
                 beta2 = (CT)K2.beta2;
                 qsteady_max = (CT)K2.qsteady_max;
-                Alg::template enter<Model, R, L, C>(cache, uprev, uprevlo, p, t, g, st);
+                Alg::template enter<Model, R, L, C>(cache, uprev, uprevlo, p, TM(t), g, st);
             }
         }
-        // fix_dt_at_bounds!
+        // fix_dt_at_bounds!  (backward the reference takes min(dt, dtmin) of a negative
+        // dt and a positive dtmin: the lower bound applies forward only)
         dt = pmin(dtmax, dt);
-        dt = pmax(dt, pabs(pmax(peps(t), a.dtmin)));
+        if (!bwd) dt = pmax(dt, pabs(pmax(peps(t), a.dtmin)));
         {   // modify_dt_for_tstops!
             const double tol = ptol100(pmax(pabs(t), pabs(tnext)));
             const double orig = pabs(dt);
@@ -733,7 +753,9 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             if (!do_error_check) e = RC_SUCCESS;
             else if (bits_nan(db)) e = RC_DTNAN;
             else if (iter > a.maxiters) e = RC_MAXITERS;
-            else if (ple(pabs(dt), pabs(a.dtmin)) && (!accept || t + dt < tnext)) e = RC_DTLESSTHANMIN;
+            // t + dt < tdir * first(tstops) in the reference's own time
+            else if (ple(pabs(dt), pabs(a.dtmin)) && (!accept || (bwd ? t + dt > tnext : t + dt < tnext)))
+                e = RC_DTLESSTHANMIN;
             else if (!accept && ple(pabs(dt), peps(t))) e = RC_UNSTABLE;
             else if (accept) {
                 bool bad = false;
@@ -747,8 +769,8 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
         }
         // ---- perform_step! (skipped for a step below eps(t) onto the tstop)
         if (!(next_tstop && plt(pabs(dt), peps(t)))) {
-            EEst = Alg::template step<Model, R, L, C>(cache, u, ulo, uprev, uprevlo, p, t, dt, abstol, reltol, iter,
-                                                      EEst > CT(1), g, st);
+            EEst = Alg::template step<Model, R, L, C>(cache, u, ulo, uprev, uprevlo, p, TM(t), TM(dt), abstol, reltol,
+                                                      iter, EEst > CT(1), g, st);
         }
         // ---- loopfooter!
         if constexpr (is_composite_alg<Alg>::value) do_error_check = true;
@@ -793,17 +815,17 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
                 // at; entries before it were passed at the header) or the model's own
                 bool fire = false;
                 if (a.callback) {
-                    if constexpr (discrete_at_tstops<Model>::value) fire = itst < a.ntstops && a.tstops[itst] == t;
-                    else fire = Model::template discrete_condition<R, L, C>(u, ulo, a.p + j, N, t, g);
+                    if constexpr (discrete_at_tstops<Model>::value) fire = itst < a.ntstops && tstop_at(itst) == t;
+                    else fire = Model::template discrete_condition<R, L, C>(u, ulo, a.p + j, N, TM(t), g);
                 }
                 if (fire) {
                     // saveat up to t and the every-step save, then save_positions[1]
                     // unless a save landed on t; affect!; save_positions[2]
                     if (!savevalues(u, ulo)) save_point(t, u, ulo);
-                    terminated = Model::template discrete_affect<R, L, C>(u, ulo, a.p + j, N, t, g) || terminated;
+                    terminated = Model::template discrete_affect<R, L, C>(u, ulo, a.p + j, N, TM(t), g) || terminated;
                     save_point(t, u, ulo);
                     // u changed: FSAL methods evaluate f(u) again (reeval_fsal)
-                    if (!terminated) Alg::template reset_fsal<Model, R, L, C>(cache, u, ulo, p, t, g, st);
+                    if (!terminated) Alg::template reset_fsal<Model, R, L, C>(cache, u, ulo, p, TM(t), g, st);
                 }
                 handled = fire;   // saved_in_cb is the discrete callbacks' verdict
             }

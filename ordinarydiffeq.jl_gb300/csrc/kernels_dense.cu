@@ -3,7 +3,8 @@
 //
 // Follows ode_interpolation(tval::Number, ...) (lib/OrdinaryDiffEqCore/src/dense/
 // generic_dense.jl:1094-1190) with left continuity: i+ is the first saved index
-// >= 2 (1-based) with ts[i+] >= t, clamped to the last index, i- = i+ - 1; dt =
+// >= 2 (1-based) with tdir ts[i+] >= tdir t (tdir = sign(ts[end] - ts[1])),
+// clamped to the last index, i- = i+ - 1; dt =
 // ts[i+] - ts[i-]; theta = (t - ts[i-]) / dt (1 when dt is 0); then the
 // interpolant on (ts[i-], u[i-]) -> (ts[i+], u[i+]) with the vectors stored for
 // the step ending at i+ (ks[i+]).  Vern7's lazy extra stages are formed from
@@ -28,10 +29,13 @@ struct Interval {
 
 __device__ __forceinline__ Interval dense_locate(const DenseArgs& a, long long j, int ns, double t) {
     const long long N = a.N;
-    int lo = 1, hi = ns;   // first s in [1, ns) with ts[s] >= t, else ns
+    // the saved times run in the integration direction: sign(ts[end] - ts[1])
+    const bool bwd = a.ts[(size_t)(ns - 1) * N + j] < a.ts[j];
+    int lo = 1, hi = ns;   // first s in [1, ns) with tdir ts[s] >= tdir t, else ns
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        if (a.ts[(size_t)mid * N + j] >= t) hi = mid;
+        const double ts = a.ts[(size_t)mid * N + j];
+        if (bwd ? ts <= t : ts >= t) hi = mid;
         else lo = mid + 1;
     }
     Interval v;

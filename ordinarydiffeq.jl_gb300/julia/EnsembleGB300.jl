@@ -195,7 +195,10 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem,
     npt = all(length(p.u0) == n for p in probs) ? C_NULL : Int32[length(p.u0) for p in probs]
     # saveat rules of lib/OrdinaryDiffEqCore/src/solve.jl:141-143,596-599,1103-1124
     scalar = saveat isa Number
-    sv = scalar ? collect(probs[1].tspan[1] + saveat:saveat:probs[1].tspan[2]) : sort(collect(Float64, saveat))
+    # (t0 + tdir|d|):(tdir|d|):tf; the library takes the points ascending in either direction
+    t0, tf = probs[1].tspan
+    sd = (tf < t0 ? -1 : 1) * abs(saveat isa Number ? saveat : 0.0)
+    sv = scalar ? sort(collect(t0 + sd:sd:tf)) : sort(collect(Float64, saveat))
     ss = save_start === nothing ? (isempty(saveat) || scalar || probs[1].tspan[1] in sv) : save_start
     se = save_end === nothing ? (isempty(saveat) || scalar || probs[1].tspan[2] in sv) : save_end
     everystep = save_everystep && isempty(sv)

@@ -30,7 +30,7 @@ class ReturnCode(IntEnum):
     Unstable = 5
     Aborted = 6
     Terminated = 7
-    InitialFailure = 8   # tf < t0 or a NaN time span (backward integration is not supported)
+    InitialFailure = 8   # a NaN time span
 
 
 MODELS = {"linear": _lib.MODEL_LINEAR, "lorenz": _lib.MODEL_LORENZ, "robertson": _lib.MODEL_ROBERTSON,

@@ -1,10 +1,11 @@
 """saveat / save_start / save_end resolution with the reference's rules.
 
-* A number saveat d means the range (t0 + d):d:tf (lib/OrdinaryDiffEqCore/src/solve.jl:1103-1124),
+* A number saveat d means the range (t0 + tdir|d|):(tdir|d|):tf (lib/OrdinaryDiffEqCore/src/solve.jl:1103-1124),
   evaluated like Julia's Float64 range: when start, step and stop have exact
   small rational forms the elements are the correctly rounded rationals (so
   0.1:0.1:1.0 gives 0.3, not 0.1 + 0.2).
-* A vector saveat keeps the entries in (t0, tf] (the device skips the rest).
+* A vector saveat keeps the entries in (t0, tf] ([tf, t0) backward; the device skips
+  the rest).  The points are passed ascending whatever the direction.
 * Defaults (solve.jl:141-143, 596-599): save_start = isempty(saveat) || saveat is a
   number || t0 in saveat; save_end = isempty(saveat) || saveat is a number ||
   tf in saveat.  Saving every step (empty saveat in the reference) is not
@@ -39,6 +40,11 @@ def julia_rat(x):
     return a, b
 
 
+def _between(a, x, b):
+    # Base.isbetween: x between a and b in either order
+    return a <= x <= b or b <= x <= a
+
+
 def julia_float_range(start, step, stop):
     """Elements of Julia's start:step:stop for Float64 (Base (:) on IEEE floats)."""
     if step == 0:
@@ -55,8 +61,8 @@ def julia_float_range(start, step, stop):
                 length = max(0, (den * zn - zd * start_n + step_n * zd) // (step_n * zd))
                 last = Fraction(start_n + (length - 1) * step_n, den)
                 nxt = Fraction(start_n + length * step_n, den)
-                if length > 0 and (Fraction(start) <= last <= Fraction(stop) + Fraction(step) / 2 or length == 0) \
-                        and not (Fraction(start) <= nxt <= Fraction(stop)):
+                if length > 0 and _between(Fraction(start), last, Fraction(stop) + Fraction(step) / 2) \
+                        and not _between(Fraction(start), nxt, Fraction(stop)):
                     return np.array([float(Fraction(start_n + k * step_n, den)) for k in range(length)])
     lf = (stop - start) / step
     if lf < 0:
@@ -114,12 +120,15 @@ def resolve_saveat(saveat, tspans, save_start=None, save_end=None, save_everyste
         return SaveSpec(np.zeros(0), 0, False, False, True if save_start is None else bool(save_start),
                         True if save_end is None else bool(save_end), seu)
     if np.isscalar(saveat):
+        # (t0 + tdir|d|):(tdir|d|):tf, stored ascending (the device reads a
+        # backward trajectory's points from the end)
         d = abs(float(saveat))
+        sd = lambda a, b: -d if b < a else d
         if same_span:
-            vals = julia_float_range(t0s[0] + d, d, tfs[0])
+            vals = np.sort(julia_float_range(t0s[0] + sd(t0s[0], tfs[0]), sd(t0s[0], tfs[0]), tfs[0]))
             per = False
         else:
-            rows = [julia_float_range(a + d, d, b) for a, b in zip(t0s, tfs)]
+            rows = [np.sort(julia_float_range(a + sd(a, b), sd(a, b), b)) for a, b in zip(t0s, tfs)]
             m = max(len(r) for r in rows)
             vals = np.full((m, len(rows)), np.inf)
             for j, r in enumerate(rows):

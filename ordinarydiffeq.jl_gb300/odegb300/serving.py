@@ -148,9 +148,11 @@ def run_open_loop(server, requests, rate, duration, seed=1, precision="auto", dr
     """Poisson arrivals at `rate` requests/s for `duration` seconds, cycling
     through `requests`.  Latency = completion (outputs in the caller's
     buffers) minus the scheduled arrival time.  Requests the server sheds
-    (queue full) are counted, not retried."""
+    (queue full) are counted, not retried; `launches` counts the kernel
+    launches the server made for this run."""
     rng = np.random.default_rng(seed)
     clock = lambda: time.clock_gettime(time.CLOCK_MONOTONIC)
+    launches0 = server.stats()["launches"]
     t0 = clock() + 0.01
     end = t0 + duration
     nxt = t0 + rng.exponential(1.0 / rate)
@@ -201,7 +203,7 @@ def run_open_loop(server, requests, rate, duration, seed=1, precision="auto", dr
     st = server.stats()
     return {"offered_rate": rate, "duration_s": duration, "submitted": submitted, "completed": int(len(lat)),
             "failed": failures, "unfinished": len(arrival), "shed_queue_full": shed,
-            "launches_total": st["launches"],
+            "launches": st["launches"] - launches0,
             "requests_per_s": len(lat) / span if span == span and span > 0 else None,
             "trajectories_per_s": ntraj_done / span if span == span and span > 0 else None,
             "latency_ms": {"p50": pct(lat, 50), "p90": pct(lat, 90), "p99": pct(lat, 99), "max": pct(lat, 100)},

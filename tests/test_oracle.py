@@ -543,3 +543,113 @@ def test_state_triggered_discrete_callback_doses_below_the_threshold():
     # between doses the decay is exact: c(t2) = c(t1) exp(-k (t2 - t1))
     for a, b in zip(jumps[:-1] + 1, jumps[1:]):
         assert abs(c[b] - c[a] * np.exp(-k * (t[b] - t[a]))) < 1e-7
+
+
+# ---- backward integration (tdir = -1)
+
+def _steps(alg, tspan, **kw):
+    base = dict(saveat=[], saveat_given=False, save_everystep=True, max_step_saves=256, save_start=True)
+    base.update(kw)
+    return O.solve(alg, O.LINEAR, [0.5, 0.25], [1.01], tspan, **base)
+
+
+# test/InterfaceI/ode_backwards_test.jl: prob_ode_2Dlinear on (1, 0) with fixed steps of
+# 1/4 (a positive dt is taken in the direction) hits 0.75, 0.5, 0.25, 0; with tstops
+# [0.5, 0.33] the steps end at 0.5, 0.33, 0.08 and 0
+@pytest.mark.parametrize("alg", [O.TSIT5, O.VERN7, O.RODAS5P, O.ROSENBROCK23])
+def test_backward_fixed_steps_and_tstops(alg):
+    r = _steps(alg, (1.0, 0.0), adaptive=False, dt=0.25)
+    assert list(r["t"]) == [1.0, 0.75, 0.5, 0.25, 0.0]
+    r = _steps(alg, (1.0, 0.0), adaptive=False, dt=0.25, tstops=[0.5, 0.33])
+    assert np.allclose(r["t"], [1.0, 0.75, 0.5, 0.33, 0.08, 0.0], rtol=0, atol=1e-15)
+    assert 0.33 in r["t"]
+
+
+# ode_backwards_test.jl:8-9 (adaptive, dt = -1/4, tstops = [0.5]): the first step is the
+# given one, the tstop is hit, and the solve ends at 0 with the solution exp(1.01 (t - 1)) u0
+@pytest.mark.parametrize("alg", [O.TSIT5, O.VERN7, O.RODAS5P])
+def test_backward_adaptive_with_a_tstop(alg):
+    r = _steps(alg, (1.0, 0.0), dt=0.25, tstops=[0.5])
+    t = r["t"]
+    assert r["retcode"] == O.RC_SUCCESS and t[0] == 1.0 and t[1] == 0.75 and 0.5 in t and t[-1] == 0.0
+    assert np.all(np.diff(t) < 0)
+    ex = np.exp(1.01 * (t - 1.0))[:, None] * np.array([0.5, 0.25])
+    assert np.abs(r["u"] - ex).max() < 1e-3
+
+
+# test/InterfaceI/ode_saveat_tests.jl:5-42 on prob_reverse = (1.0, 0.0): the save times
+# mirror the forward ones
+def test_backward_saveat_rules():
+    from odegb300.saveat import resolve_saveat
+
+    def ts(saveat, **kw):
+        sv = resolve_saveat(saveat, np.array([[1.0], [0.0]]))
+        r = O.solve(O.TSIT5, O.LINEAR, [0.5], [1.01], (1.0, 0.0), saveat=sv.values, save_start=sv.save_start,
+                    save_end=sv.save_end, save_end_user=sv.save_end_user, saveat_given=sv.nsave > 0,
+                    saveat_scalar=sv.scalar, dt=0.25, **kw)
+        return list(r["t"])
+
+    assert ts(None) == [1.0, 0.0]
+    assert ts([0.5]) == [0.5]
+    assert ts([0.0, 0.5, 1.0]) == [1.0, 0.5, 0.0]
+    assert ts(0.5) == [1.0, 0.5, 0.0]
+    assert ts([0.5], tstops=[0.5]) == [0.5]
+    assert ts([0.0, 0.5, 1.0], tstops=[0.5]) == [1.0, 0.5, 0.0]
+    # saveat = 1/10 gives collect(1.0:-0.1:0.0): the correctly rounded tenths
+    assert ts(0.1, tstops=[0.5]) == [1.0, 0.9, 0.8, 0.7, 0.6, 0.5, 0.4, 0.3, 0.2, 0.1, 0.0]
+
+
+# test/InterfaceI/ode_initdt_tests.jl:134-153: the initial-dt probe stays before the first
+# tstop in either direction
+@pytest.mark.parametrize("tspan,tstop", [((0.0, 10.0), 1e-3), ((10.0, 0.0), 9.999)])
+def test_initdt_probe_respects_the_first_tstop(tspan, tstop):
+    tdir = np.sign(tspan[1] - tspan[0])
+    O.record_eval_times(True)
+    O.solve(O.TSIT5, O.LINEAR, [1.0], [-1.0], tspan, saveat=[], saveat_given=False, tstops=[tstop])
+    ev = O.eval_times()[:3]   # initialize! (FSAL) and the two evaluations of initdt
+    O.record_eval_times(False)
+    assert len(ev) == 3 and np.max(tdir * (ev - tstop)) <= 0
+
+
+# lib/OrdinaryDiffEqVerner/test/ode_verner_tests.jl:136-185 (backward solve, lazy
+# interpolation): du = (-u1, -2 u2) on (1, 0); the interpolant at each step's midpoint
+# (Vern7's extra stages formed with the step's signed dt) matches the solution
+def test_backward_dense_interpolation_inside_steps():
+    r = O.solve(O.VERN7, O.LINEAR, [1.0], [-1.0], (1.0, 0.0), saveat=[], saveat_given=False, dense=True,
+                save_everystep=True, max_step_saves=512, save_start=True, reltol=1e-12, abstol=1e-12)
+    d = r["dense"]
+    t = r["t"]
+    mids = 0.5 * (t[1:] + t[:-1])
+    got = d(mids)[:, 0]
+    assert np.abs(got - np.exp(-(mids - 1.0))).max() < 1e-10
+    # at the saved steps the interpolant reproduces the steps to round-off
+    assert np.allclose(d(t)[:, 0], r["u"][:, 0], rtol=1e-13, atol=0)
+
+
+# Backward over the whole span and forward again returns to the start (the forced
+# oscillator: t in every stage, the Rosenbrock time derivative with its sign)
+@pytest.mark.parametrize("alg,rt,bound", [(O.TSIT5, 1e-10, 50.0), (O.VERN7, 1e-12, 50.0), (O.RODAS5P, 1e-9, 50.0)])
+def test_backward_matches_the_closed_form(alg, rt, bound):
+    sv = np.linspace(0.0, 19.0, 20)
+    x20 = forced_exact(np.array([20.0]), 0.4, -0.2, 0.3, 2.0, 1.5, 1.7)[0]
+    r = O.solve(alg, O.FORCED_DUFFING, x20, FORCED_P, (20.0, 0.0), saveat=sv, reltol=rt, abstol=rt)
+    assert r["retcode"] == 1
+    assert np.all(np.diff(r["t"]) < 0) and list(r["t"]) == list(sv[::-1])
+    ex = forced_exact(r["t"], 0.4, -0.2, 0.3, 2.0, 1.5, 1.7)
+    # backward the damped oscillator's transient grows as e^{delta t / 2}: the bound scales with it
+    err = np.abs(r["u"] - ex).max() / (rt * np.exp(0.15 * 20.0))
+    assert err < bound, err
+
+
+def test_backward_bouncing_ball_event():
+    # the ball at height 50 moving up at 10: backward it falls back to the floor and bounces
+    # (affect_neg! on the downcrossing in integration order) at the closed-form times
+    r = O.solve(O.TSIT5, O.BOUNCING_BALL, [50.0, 10.0], [9.81, 1.0, 1e9], (10.0, 0.0), interp_points=10,
+                callback=True, saveat=[], saveat_given=False, save_start=True, max_events=8)
+    g = 9.81
+    # x(t) = 50 + 10 (t - 10) - g/2 (t - 10)^2: x = 0 first at t - 10 = (10 - sqrt(100 + 100 g)) / g
+    te = 10.0 + (10.0 - np.sqrt(100.0 + 2 * g * 50.0)) / g
+    hit = np.nonzero(np.abs(r["t"] - te) < 1e-9)[0]
+    assert r["retcode"] == O.RC_SUCCESS and len(hit) == 2
+    u = r["u"]
+    assert abs(u[hit[0]][0]) < 1e-9 and u[hit[0]][1] > 0 and u[hit[1]][1] == -u[hit[0]][1]
