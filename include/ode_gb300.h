@@ -169,7 +169,9 @@ typedef struct {
                                    max_step_saves + 2 slots, and past that the last slot keeps the latest step */
     int32_t callback;           /* 1: the model's registered ContinuousCallback (models with an event;
                                    SciMLBase defaults: rootfind = LeftRootFind, save_positions = (true, true),
-                                   abstol = 10eps(), repeat_nudge = 1//100, dtrelax = 1); not with dense output */
+                                   abstol = 10eps(), repeat_nudge = 1//100, dtrelax = 1).  An event moves t
+                                   back into the step and recomputes the step's interpolation data for the
+                                   shortened step (reeval_internals_due_to_modification!), as the reference */
     int32_t interp_points;      /* the callback's interp_points (default 10) */
     int32_t max_events;         /* save slots for events: 2 per event (before and after its affect) are added to
                                    the output, and past the total the last slot keeps the latest save */
@@ -253,8 +255,11 @@ int ode_dense_nk(int alg);
  * k_out[((s*nk + q)*n_states + i)*N + j], cap = max_step_saves + 2 slots.
  * The start save's vectors are 0.  A trajectory with more steps than slots
  * keeps its final point in the last slot with NaN vectors: its last interval
- * cannot be interpolated.  Uniform sizes only (no n_per_traj).  Page-locked
- * buffers are used in place, as in ode_solve_ensemble. */
+ * cannot be interpolated.  With a callback, its saves (before and after the
+ * affect, at the same t) store the step's vectors too; an event step's are
+ * those of the step shortened to the event.  Uniform sizes only (no
+ * n_per_traj).  Page-locked buffers are used in place, as in
+ * ode_solve_ensemble. */
 int ode_solve_ensemble_dense(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int64_t ntraj,
                              const double* u0, const double* p, const double* tspan, double* t_out,
                              double* u_out, double* k_out, int32_t* nsaved, int32_t* retcode, ode_stats* stats);

@@ -349,6 +349,7 @@ struct Integ {
     double last_saved_t;
     orc_stats st;
     Dense* dense;
+    std::vector<double> dense_last_u;   // u of the last save (the next dense interval's start)
     std::vector<double> interp_out;
     // AutoTsit5(Rosenbrock23()): the composite's state (AutoSwitchCache,
     // composite_algs.jl:55-94) and one PI controller state per method
@@ -877,7 +878,13 @@ void interpolate(Integ& I, double th, double* out) {
     }
 }
 
+void record_dense(Integ& I, double t, const double* v);
+
 void push_save(Integ& I, double t, const double* v) {
+    if (I.dense) {   // dense output saves every step: each save after the start is an interval
+        if (I.nsaved > 0) record_dense(I, t, v);
+        I.dense_last_u.assign(v, v + I.n);
+    }
     const int slot = I.nsaved < I.cap ? I.nsaved : ((I.o.save_everystep || I.o.callback) ? I.cap - 1 : -1);
     if (slot >= 0) {
         if (I.t_out) I.t_out[slot] = t;
@@ -969,14 +976,16 @@ double stepsize_controller(Integ& I) {
     return q;
 }
 
-void record_dense(Integ& I) {
-    if (!I.dense) return;
-    // sol.t / sol.u / sol.k of an every-step save (save_dense_at_t!, integrator_utils.jl:455-473)
+void record_dense(Integ& I, double t, const double* v) {
+    // sol.t / sol.u / sol.k of a step save or a callback's save (save_dense_at_t!,
+    // integrator_utils.jl:455-473; savevalues!(integrator, true) in apply_callback!):
+    // the interval from the previous save, with the interpolation data of the step
+    // as it stands (an event's step is the shortened one)
     Step s;
-    s.tprev = I.tprev;
-    s.tend = I.t;
-    s.y0 = I.uprev;
-    s.y1 = I.u;
+    s.tprev = I.last_saved_t;
+    s.tend = t;
+    s.y0 = I.dense_last_u;
+    s.y1.assign(v, v + I.n);
     const int alg = I.alg == ORC_AUTOTSIT5_ROSENBROCK23 ? (I.current == 0 ? ORC_TSIT5 : ORC_ROSENBROCK23) : I.alg;
     int nk = alg == ORC_TSIT5 ? 7 : alg == ORC_VERN7 ? 10 : alg == ORC_RODAS5P ? 3 : alg == ORC_ROSENBROCK23 ? 2 : 0;
     s.k.assign(I.k.begin(), I.k.begin() + (size_t)nk * I.n);
@@ -1439,7 +1448,6 @@ void loopfooter(Integ& I) {
             double dtp = I.tdir * jmin(std::fabs(I.o.dtmax), std::fabs(dtnew));
             dtp = I.tdir * jmax(std::fabs(dtp), dtmin_t(I));
             I.dtpropose = dtp;
-            record_dense(I);
             handle_callbacks(I);
         } else {
             I.st.nreject++;
@@ -1455,7 +1463,6 @@ void loopfooter(Integ& I) {
         }
         I.accept_step = true;
         I.dtpropose = I.dt;
-        record_dense(I);
         handle_callbacks(I);
     }
 }
@@ -1771,6 +1778,16 @@ int orc_solve(int alg, int model, int n, const double* p, double t0, double tf, 
     if (st) *st = I.st;
     g_last_alg_choice = I.alg_choice;
     return I.nsaved;
+}
+
+double orc_initdt(int alg, int model, int n, const double* p, double t0, double tf, const double* u0,
+                  const orc_opts* o, const double* tstops, int ntstops) {
+    Integ I;
+    setup(I, alg, model, n, p, t0, tf, o, nullptr, 0, tstops, tstops ? ntstops : 0);
+    I.u.assign(u0, u0 + n);
+    I.t = t0;
+    I.fsallast.assign(n, 0.0);
+    return initdt(I);
 }
 
 int orc_last_alg_choice(int32_t* out, int cap) {

@@ -67,6 +67,11 @@ int orc_solve(int alg, int model, int n, const double* p, double t0, double tf,
               const double* tstops, int ntstops, double* t_out, double* u_out, int cap,
               int32_t* retcode, orc_stats* st, void** dense_handle);
 
+/* The initial step the solve would take (ode_determine_initdt with tdir, its
+ * dtmax bounded by the first tstop), signed; counts its two f calls. */
+double orc_initdt(int alg, int model, int n, const double* p, double t0, double tf, const double* u0,
+                  const orc_opts* o, const double* tstops, int ntstops);
+
 /* Evaluate the stored dense solution at nq times (out: nq*n), as the
  * reference's sol(t) does (ode_interpolation on the every-step saves). */
 int orc_dense_eval(void* dense_handle, const double* tq, int nq, double* out);

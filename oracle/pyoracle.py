@@ -72,6 +72,9 @@ def lib():
         L.orc_last_alg_choice.argtypes = [C.POINTER(C.c_int32), C.c_int]
         L.orc_rhs_calls.restype = C.c_int64
         L.orc_rhs_calls.argtypes = [C.c_int]
+        L.orc_initdt.restype = C.c_double
+        L.orc_initdt.argtypes = [C.c_int, C.c_int, C.c_int, dp, C.c_double, C.c_double, dp, C.POINTER(Opts), dp,
+                                 C.c_int]
         L.orc_record_eval_times.argtypes = [C.c_int]
         L.orc_eval_times.restype = C.c_int
         L.orc_eval_times.argtypes = [dp, C.c_int]
@@ -102,8 +105,13 @@ def make_opts(reltol=1e-3, abstol=1e-6, dtmax=0.0, dtmin=0.0, dt=0.0, adaptive=T
 
 
 def solve(alg, model, u0, p, tspan, saveat=(), tstops=(), dense=False, **kw):
-    """Solve one trajectory; returns dict(t, u, retcode, stats, dense)."""
+    """Solve one trajectory; returns dict(t, u, retcode, stats, dense).  dense
+    keeps every step (the reference's dense output saves every step: its
+    default save_everystep = isempty(saveat))."""
     L = lib()
+    if dense and "save_everystep" not in kw:
+        kw["save_everystep"] = True
+        kw.setdefault("max_step_saves", 65536)
     u0 = np.ascontiguousarray(u0, dtype=np.float64)
     p = np.ascontiguousarray(np.atleast_1d(p), dtype=np.float64)
     n = u0.size
@@ -225,6 +233,16 @@ def tgrad(model, u, p, t=0.0):
 
 def rhs_calls(reset=False):
     return lib().orc_rhs_calls(int(reset))
+
+
+def initdt(alg, model, u0, p, tspan, tstops=(), **kw):
+    """The signed initial step of a solve (ode_determine_initdt)."""
+    u0 = np.ascontiguousarray(u0, dtype=np.float64)
+    p = np.ascontiguousarray(np.atleast_1d(p), dtype=np.float64)
+    ts = np.ascontiguousarray(tstops, dtype=np.float64)
+    o = make_opts(**kw)
+    return lib().orc_initdt(alg, model, u0.size, _dp(p), tspan[0], tspan[1], _dp(u0), C.byref(o),
+                            _dp(ts) if ts.size else None, ts.size)
 
 
 def record_eval_times(enable=True):

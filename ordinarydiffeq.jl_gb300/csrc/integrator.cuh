@@ -464,6 +464,33 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
         return exact;
     };
 
+    // After an event moved t back into the step (change_t_via_interpolation!,
+    // integrator_interface.jl:5-40): dt = t - tprev and the step's interpolation
+    // data recomputed for the shortened step from (tprev, uprev)
+    // (reeval_internals_due_to_modification! -> ode_addsteps! with
+    // always_calc_begin, :54-79), so the saveat points before the event and a
+    // dense save at it use the shortened step's interpolant, as the reference's
+    // do.  The reference does not count these evaluations; the state stays the
+    // interpolated one and a composite's stiffness estimate is kept.
+    auto recompute_step = [&]() {
+        if constexpr (Model::HAS_EVENT) {   // only event models move t
+            dt = t - tprev;
+            R ut[C], utlo[C];
+            StepStats uncounted = {0, 0, 0, 0, 0, 0};
+            double eig = 0.0;
+            if constexpr (is_composite_alg<Alg>::value) eig = cache.eigen_est;
+            Alg::template step<Model, R, L, C>(cache, ut, utlo, uprev, uprevlo, p, TM(tprev), TM(dt), abstol, reltol,
+                                               iter, false, g, uncounted);
+            if constexpr (is_composite_alg<Alg>::value) cache.eigen_est = eig;
+        }
+    };
+    // A save made by a callback (before or after its affect): with dense output it
+    // stores the step's interpolation vectors too (savevalues!(integrator, true)).
+    auto save_forced = [&]() {
+        if (a.k_out) save_dense(true);
+        save_point(t, u, ulo);
+    };
+
     // The model's ContinuousCallback after an accepted step: handle_callbacks!
     // (integrator_utils.jl:1081-1132) with find_callback_time, nudge_tprev,
     // check_event_occurrence and apply_callback! (lib/DiffEqBase/src/callbacks.jl:
@@ -526,12 +553,8 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             last_event_error = residual;
             // apply_callback!: set_proposed_dt! (dtrelax = 1)
             dtpropose = pmax(nextafter(a.dtmin, __longlong_as_double(0x7ff0000000000000LL)), dt);
-            // change_t_via_interpolation!  (the step's end state stays for the saveat
-            // points before the event)
+            // change_t_via_interpolation!
             const bool moved = cb_t != t;
-            R uend[C], uendlo[C];
-#pragma unroll
-            for (int c = 0; c < C; ++c) { uend[c] = u[c]; uendlo[c] = ulo[c]; }
             if (moved) {
                 R v[C], vlo[C];
                 Alg::template interpolate<Model, R, L, C>(cache, v, vlo, (cb_t - tprev) / dt, TM(dt), TM(tprev), uprev,
@@ -539,9 +562,10 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
 #pragma unroll
                 for (int c = 0; c < C; ++c) { u[c] = v[c]; ulo[c] = vlo[c]; }
                 t = cb_t;
+                recompute_step();
             }
             // saveat up to the event, then the pre-affect save unless one landed on t
-            if (!savevalues(uend, uendlo)) save_point(t, u, ulo);
+            if (!savevalues(u, ulo)) save_forced();
             bool modified = false;
             if (bs < 0.0 && Model::EVENT_AFFECT_POS) {
                 terminated = Model::template event_affect<R, L, C>(u, ulo, a.p + j, N, TM(t), true, g);
@@ -550,7 +574,7 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
                 terminated = Model::template event_affect<R, L, C>(u, ulo, a.p + j, N, TM(t), false, g);
                 modified = true;
             }
-            if (modified) save_point(t, u, ulo);   // save_positions[2]
+            if (modified) save_forced();   // save_positions[2]
             if (!terminated && (moved || modified)) Alg::template reset_fsal<Model, R, L, C>(cache, u, ulo, p, TM(t), g, st);
             return true;
         }
@@ -666,9 +690,6 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             // with the events' directions, the post-affect save
             dtpropose = pmax(nextafter(a.dtmin, __longlong_as_double(0x7ff0000000000000LL)), dt);
             const bool moved = cb_t != t;
-            R uend[C], uendlo[C];
-#pragma unroll
-            for (int c = 0; c < C; ++c) { uend[c] = u[c]; uendlo[c] = ulo[c]; }
             if (moved) {
                 R v[C], vlo[C];
                 Alg::template interpolate<Model, R, L, C>(cache, v, vlo, (cb_t - tprev) / dt, TM(dt), TM(tprev), uprev,
@@ -676,10 +697,11 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
 #pragma unroll
                 for (int c = 0; c < C; ++c) { u[c] = v[c]; ulo[c] = vlo[c]; }
                 t = cb_t;
+                recompute_step();
             }
-            if (!savevalues(uend, uendlo)) save_point(t, u, ulo);
+            if (!savevalues(u, ulo)) save_forced();
             terminated = Model::template vector_event_affect<R, L, C>(u, ulo, a.p + j, N, TM(t), dir, g);
-            save_point(t, u, ulo);
+            save_forced();
             if (!terminated) Alg::template reset_fsal<Model, R, L, C>(cache, u, ulo, p, TM(t), g, st);
             return true;
         }
@@ -821,9 +843,9 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
                 if (fire) {
                     // saveat up to t and the every-step save, then save_positions[1]
                     // unless a save landed on t; affect!; save_positions[2]
-                    if (!savevalues(u, ulo)) save_point(t, u, ulo);
+                    if (!savevalues(u, ulo)) save_forced();
                     terminated = Model::template discrete_affect<R, L, C>(u, ulo, a.p + j, N, TM(t), g) || terminated;
-                    save_point(t, u, ulo);
+                    save_forced();
                     // u changed: FSAL methods evaluate f(u) again (reeval_fsal)
                     if (!terminated) Alg::template reset_fsal<Model, R, L, C>(cache, u, ulo, p, TM(t), g, st);
                 }

@@ -144,6 +144,8 @@ __global__ void dense_eval_vern7(DenseArgs a) {
 // Vern7 shapes: the FP64 integrator's (kernels_vern7.cu).
 static const DenseVariant kDense[] = {
     PW(0, "tsit5"), PW(2, "rodas5p"), PW(3, "rosenbrock23"),
+    V7(BouncingBall, M_BOUNCING_BALL, 1, 2), V7(PKOneCompartment, M_PK1, 1, 2),
+    V7(ForcedDuffing, M_FORCED_DUFFING, 1, 2),
     V7(Linear, M_LINEAR, 1, 1), V7(Linear, M_LINEAR, 1, 2), V7(Linear, M_LINEAR, 1, 8),
     V7(Lorenz, M_LORENZ, 1, 3),
     V7(Duffing, M_DUFFING, 1, 4), V7(Duffing, M_DUFFING, 1, 8), V7(Duffing, M_DUFFING, 2, 4),

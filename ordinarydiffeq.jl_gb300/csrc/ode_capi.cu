@@ -1407,7 +1407,6 @@ int ode_solve_ensemble_dense(ode_handle* h, const ode_problem_desc* d, const ode
     if (rc) return rc;
     if (!o->save_everystep || o->nsave != 0)
         return fail(h, ODE_E_INVALID, "dense output saves every step: save_everystep = 1 and nsave = 0");
-    if (o->callback) return fail(h, ODE_E_UNSUPPORTED, "dense output with a callback is not supported");
     if (kDenseVectors[d->alg_id] == 0) return fail(h, ODE_E_UNSUPPORTED, "no dense output for this method");
     if (N > 0 && (!u0 || !p || !tspan || !u_out || !k_out || !nsaved || !retcode))
         return fail(h, ODE_E_INVALID, "null input or output buffer");

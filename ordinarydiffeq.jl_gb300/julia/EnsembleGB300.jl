@@ -175,7 +175,7 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem,
                            ens::EnsembleGB300; trajectories, saveat = Float64[], reltol = 1e-3, abstol = 1e-6,
                            dt = 0.0, dtmax = 0.0, dtmin = 0.0, maxiters = 1_000_000, save_start = nothing,
                            save_end = nothing, save_everystep = isempty(saveat), max_step_saves = 1024, seed = 0,
-                           callback = nothing, dense = save_everystep && isempty(saveat) && callback === nothing,
+                           callback = nothing, dense = save_everystep && isempty(saveat),
                            tstops = Float64[], kwargs...)
     t0 = time()
     N = trajectories

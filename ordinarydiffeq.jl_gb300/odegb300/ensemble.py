@@ -400,8 +400,6 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
     o = _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax, callback, tstops)
     d = _lib.ProblemDesc(model, alg.alg_id, n, ps.shape[0], ens.prec_id(), 0)
     cap = sv.cap + (2 * callback.max_events if callback is not None else 0)
-    if dense and callback is not None:
-        raise ValueError("dense output with a callback is not supported")
     if dense and not sv.everystep:
         raise ValueError("dense output keeps every step: use it without saveat, with save_everystep")
     if dense and n_per_traj is not None:
@@ -505,16 +503,15 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
     As in the reference (solve.jl:138-146), save_everystep defaults to "no
     saveat given" (every accepted step is kept, up to max_step_saves per
     trajectory) and dense to save_everystep without saveat (each step's
-    interpolation vectors are kept too, so sol(t) uses the method's
-    interpolant); ensembles of uneven sizes, and solves with a callback, are not
-    dense by default.  callback: the model's ContinuousCallback.  tstops: times
-    every trajectory steps to exactly."""
+    interpolant; a callback's saves keep them as well); ensembles of uneven
+    sizes are not dense by default.  callback: the model's ContinuousCallback or
+    DiscreteCallback.  tstops: times every trajectory steps to exactly."""
     no_saveat = saveat is None or (not np.isscalar(saveat) and np.size(saveat) == 0)
     if save_everystep is None:
         save_everystep = no_saveat
     dense_default = dense is None
     if dense is None:
-        dense = bool(save_everystep and no_saveat and callback is None)
+        dense = bool(save_everystep and no_saveat)
     ens = ensemblealg or EnsembleGB300()
     if not isinstance(ens, EnsembleGB300):
         raise TypeError("ensemble algorithm must be EnsembleGB300")

@@ -106,3 +106,31 @@ def test_reference_bounce_then_terminate_and_both_sides_saved():
                 reltol=1e-3, abstol=1e-6)
     assert len(r["t"]) == g["nsaved"][0]
     assert np.allclose(r["t"], t0, rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("alg", ["tsit5", "vern7", "rodas5p", "rosenbrock23"])
+def test_events_with_dense_output_match_oracle(alg):
+    # dense output with events: the event's step is recomputed shortened to the event
+    # (reeval_internals_due_to_modification!), every save keeps the step's vectors, and
+    # sol(t) on both sides of each contact matches the oracle's
+    from odegb300 import dense_eval
+    N = 64
+    wl = balls(N, seed=5)
+    rt = at = 1e-8 if alg != "rosenbrock23" else 1e-6
+    cb = ContinuousCallback(interp_points=10, max_events=16)
+    g = gpu("bouncing_ball", alg, wl["u0"], wl["p"], wl["tspan"], None, rt, at, callback=cb, save_everystep=True,
+            max_step_saves=4096, dense=True)
+    ts = wl["tspan"]
+    rng = np.random.default_rng(4)
+    tq = ts[0] + (ts[1] - ts[0]) * np.sort(rng.uniform(0.0, 1.0, (64, N)), axis=0)
+    ev = dense_eval(g, tq)
+    for j in range(N):
+        o = O.solve(ALG[alg][1], O.BOUNCING_BALL, wl["u0"][:, j], wl["p"][:, j], ts[:, j], dense=True, reltol=rt,
+                    abstol=at, saveat_given=False, save_everystep=True, max_step_saves=4096, save_start=True,
+                    callback=True, interp_points=10, max_events=16)
+        assert g["retcode"][j] == o["retcode"]
+        ns = int(g["nsaved"][j])
+        assert ns == len(o["t"])
+        assert np.all(np.abs(g["t"][:ns, j] - o["t"]) <= 1e-12 * np.abs(o["t"]) + 1e-14), j
+        ref = o["dense"](tq[:, j])
+        assert np.all(np.abs(ev[:, :, j] - ref) <= 10 * (rt * np.abs(ref) + at)), j

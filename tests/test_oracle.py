@@ -653,3 +653,84 @@ def test_backward_bouncing_ball_event():
     assert r["retcode"] == O.RC_SUCCESS and len(hit) == 2
     u = r["u"]
     assert abs(u[hit[0]][0]) < 1e-9 and u[hit[0]][1] > 0 and u[hit[1]][1] == -u[hit[0]][1]
+
+
+# test/ODEInterfaceRegression/init_dt_vs_dopri_tests.jl: the first step of a solve equals
+# that of Hairer's DOPRI5 code (prob_ode_linear forward and on (1, 0); prob_ode_2Dlinear
+# with the norms made to agree).  Restated here from the published starting-step algorithm
+# (Hairer, Norsett, Wanner, Solving ODEs I, sec. II.4, with the RMS norm the book and the
+# reference use); the oracle's initdt must give the same value.
+def hairer_initial_step(f, t0, y0, tdir, order, rtol, atol, hmax):
+    y0 = np.asarray(y0, dtype=float)
+    rms = lambda v: np.sqrt(np.mean(v * v))
+    sk = atol + rtol * np.abs(y0)
+    f0 = f(t0, y0)
+    d0, d1 = rms(y0 / sk), rms(f0 / sk)
+    h0 = 1e-6 if (d0 < 1e-5 or d1 < 1e-5) else 0.01 * d0 / d1
+    h0 = min(h0, hmax)
+    f1 = f(t0 + tdir * h0, y0 + tdir * h0 * f0)
+    d2 = rms((f1 - f0) / sk) / h0
+    m = max(d1, d2)
+    h1 = max(1e-6, h0 * 1e-3) if m <= 1e-15 else (0.01 / m) ** (1.0 / order)
+    return tdir * min(100 * h0, h1, hmax)
+
+
+@pytest.mark.parametrize("u0,tspan", [([0.5], (0.0, 1.0)), ([0.5], (1.0, 0.0)), ([0.5, 0.25], (0.0, 1.0)),
+                                      ([0.5, 0.25], (1.0, 0.0))])
+@pytest.mark.parametrize("alg,order", [(O.TSIT5, 5), (O.VERN7, 7), (O.RODAS5P, 5)])
+def test_initdt_matches_the_published_starting_step(u0, tspan, alg, order):
+    tdir = np.sign(tspan[1] - tspan[0])
+    want = hairer_initial_step(lambda t, y: 1.01 * y, tspan[0], u0, tdir, order, 1e-3, 1e-6,
+                               abs(tspan[1] - tspan[0]))
+    got = O.initdt(alg, O.LINEAR, u0, [1.01], tspan)
+    assert got == pytest.approx(want, rel=1e-12)
+
+
+def test_initdt_robust_to_zero_state_backward():
+    # ode_initdt_tests.jl:75-79: u0 = 0 with t0 = 20 on (20, 0): |dt| > eps(t)
+    dt = O.initdt(O.TSIT5, O.LINEAR, [0.0], [1.0], (20.0, 0.0))
+    assert dt < 0 and abs(dt) > np.spacing(20.0)
+
+
+# Dense output with a ContinuousCallback: every save stores the step's interpolation data,
+# an event's step being the one shortened to the event (change_t_via_interpolation! and
+# reeval_internals_due_to_modification!, integrator_interface.jl:5-79), so sol(t) follows
+# the solution on both sides of each bounce (the two saves at a contact make a zero-length
+# interval; left continuity gives the pre-affect state at the contact time itself).
+def ball_exact(t, h0, g, e):
+    tc, v, out = np.sqrt(2 * h0 / g), None, []
+    contacts = [tc]
+    v = g * tc
+    for _ in range(40):
+        v *= e
+        contacts.append(contacts[-1] + 2 * v / g)
+    contacts = np.array(contacts)
+    for s in np.atleast_1d(t):
+        k = int(np.searchsorted(contacts, s, side="left"))   # contacts before s (left-continuous)
+        if k == 0:
+            out.append([h0 - 0.5 * g * s * s, -g * s])
+        else:
+            t0, vk = contacts[k - 1], g * contacts[0] * e ** k
+            d = s - t0
+            out.append([vk * d - 0.5 * g * d * d, vk - g * d])
+    return np.array(out), contacts
+
+
+@pytest.mark.parametrize("alg", [O.TSIT5, O.VERN7, O.RODAS5P])
+def test_dense_output_with_events_follows_the_bounces(alg):
+    g, e = 9.81, 0.8
+    rt = 1e-10 if alg != O.RODAS5P else 1e-8
+    r = O.solve(alg, O.BOUNCING_BALL, [50.0, 0.0], [g, e, 1e9], (0.0, 12.0), saveat=[], saveat_given=False,
+                dense=True, save_start=True, callback=True, interp_points=10, reltol=rt, abstol=rt)
+    assert r["retcode"] == O.RC_SUCCESS
+    d = r["dense"]
+    tq = np.linspace(0.0, 12.0, 1201)
+    ex, contacts = ball_exact(tq, 50.0, g, e)
+    got = d(tq)
+    assert np.abs(got - ex).max() < 1e-5
+    # the saved times hold each contact twice, and sol(t) at the contact is the pre-affect state
+    t = r["t"]
+    for c in contacts[contacts < 12.0]:
+        hit = np.nonzero(np.abs(t - c) < 1e-8)[0]
+        assert len(hit) == 2
+        assert d([t[hit[0]]])[0][1] == pytest.approx(r["u"][hit[0]][1], rel=1e-12)
