@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define ODE_ABI_VERSION 4
+#define ODE_ABI_VERSION 5
 
 typedef struct ode_handle ode_handle;
 
@@ -182,6 +182,14 @@ typedef struct {
                                    ode_solve_ensemble_dense, ode_submit and ode_autotune; device
                                    memory sorted ascending for ode_solve_ensemble_device and
                                    ode_solve_ensemble_noalloc (entries out of order or NaN are skipped) */
+    int32_t max_jac_age;        /* Rosenbrock23 (a W-method) keeps J across accepted steps for at most this
+                                   many (Rosenbrock23(max_jac_age = ...), _rosenbrock_jac_reuse_decision,
+                                   OrdinaryDiffEqDifferentiation/src/derivative_utils.jl:46-170): 0 or 1, the
+                                   reference's default for Rosenbrock23, evaluates J on every attempt.
+                                   W = J - I/(dt gamma) and its LU are formed on every attempt either way */
+    int32_t reserved2;
+    double jac_reuse_gamma_tol; /* reuse only while |dtgamma / dtgamma_J - 1| <= this (reference default
+                                   0.03; < 0 means the default) */
 } ode_options;
 
 /* Fill o with the reference's defaults. */
@@ -279,6 +287,14 @@ int ode_solve_ensemble_dense(ode_handle* h, const ode_problem_desc* d, const ode
 int ode_dense_eval(ode_handle* h, const ode_problem_desc* d, int64_t ntraj, const double* p,
                    const double* t_saved, const double* u_saved, const double* k_saved, const int32_t* nsaved,
                    int32_t cap, int32_t nq, const double* tq, int32_t tq_per_traj, double* out);
+/* The same with the derivative order: deriv 0 is sol(t) (ode_dense_eval), 1 is
+ * sol(t, Val{1}), the time derivative of the method's interpolant on the same
+ * interval (Tsit5 interpolants.jl:143-178, Vern7 :305-334, Rodas5P
+ * rosenbrock_interpolants.jl:444-470, Rosenbrock23 :111-127).  Higher orders:
+ * ODE_E_UNSUPPORTED. */
+int ode_dense_eval_deriv(ode_handle* h, const ode_problem_desc* d, int64_t ntraj, const double* p,
+                         const double* t_saved, const double* u_saved, const double* k_saved, const int32_t* nsaved,
+                         int32_t cap, int32_t nq, const double* tq, int32_t tq_per_traj, int32_t deriv, double* out);
 
 /* Continuous-batching serving API.  ode_submit copies the request's inputs
  * into handle-owned pinned/device memory and returns a ticket at once; the

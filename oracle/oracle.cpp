@@ -338,6 +338,10 @@ struct Integ {
     std::vector<double> J, W, dT, ks, rhs, du;
     std::vector<int> piv;
     bool have_J;
+    // Rosenbrock23's JacReuseState (rosenbrock_caches.jl:25-60)
+    double jr_last_dtgamma, jr_pending_dtgamma;
+    int64_t jr_last_naccept, jr_last_step_iter;
+    bool recomputing;   // inside recompute_step_k (ode_addsteps! after an event)
     std::vector<double> tstops;  // tdir * t, ascending (the reference's directional heap)
     size_t itstop;
     std::vector<double> dtimes;  // the tstops as given, sorted: the discrete callback's times
@@ -763,6 +767,27 @@ void rodas_interp(double th, const double* y0, const double* y1, const double* K
     }
 }
 
+// _rosenbrock_jac_reuse_decision (lib/OrdinaryDiffEqDifferentiation/src/derivative_utils.jl:
+// 46-170) for Rosenbrock23, a W-method with reuse state, no mass matrix and not linear:
+// true when J (and W) must be fresh.  derivative_discontinuity is false here: the
+// callbacks' reeval_internals_due_to_modification! clears it before the next step.
+bool jac_reuse_decision(Integ& I, double dtgamma) {
+    if (I.iter <= 1) return true;
+    if (!I.o.adaptive) return true;
+    const int64_t naccept = I.st.naccept;
+    if (naccept > I.jr_last_naccept) I.jr_last_dtgamma = I.jr_pending_dtgamma;
+    if (I.jr_last_dtgamma == 0.0) return true;
+    if (I.jr_last_step_iter != 0 && I.iter > I.jr_last_step_iter + 1) return true;
+    if (I.EEst > 1.0) return true;
+    const double tol = I.o.jac_reuse_gamma_tol < 0 ? 0.03 : I.o.jac_reuse_gamma_tol;
+    if (std::fabs(dtgamma / I.jr_last_dtgamma - 1.0) > tol) return true;
+    if (naccept - I.jr_last_naccept >= I.o.max_jac_age) {
+        I.jr_last_naccept = naccept;
+        return true;
+    }
+    return false;
+}
+
 // perform_step!(::Rosenbrock23Cache): lib/OrdinaryDiffEqRosenbrock/src/rosenbrock_perform_step.jl:34-146,
 // tableau rosenbrock_tableaus.jl:6-10 (c32 = 6 + sqrt(2), d = 1/(2 + sqrt(2))).  A W-method
 // whose default max_jac_age = 1 (algorithms.jl:108-115) makes the reuse decision
@@ -777,14 +802,27 @@ void rosenbrock23_step(Integ& I) {
     const double dtgamma = dt * d;
     const double neginvdtgamma = -(1.0 / dtgamma);
     const double dto2 = dt / 2.0, dto6 = dt / 6.0;
-    jac(I.model, n, up, I.p, t, I.J.data());
-    I.st.njacs += 1;
-    // the model's tgrad, else the reference differentiates f in t by AD (one counted
-    // call; autonomous models: dT = 0)
-    if (!tgrad(I.model, n, up, I.p, t, I.dT.data())) {
-        f_eval(I, up, t, I.du.data());
-        std::fill(I.dT.begin(), I.dT.end(), 0.0);
-        I.st.nf += 1;
+    // calc_rosenbrock_differentiation! (derivative_utils.jl:1011-1041): the reuse
+    // decision (a composite always takes a fresh J); J and dT only when fresh.  An
+    // event's recomputation (the in-place ode_addsteps!) keeps the cached J and dT.
+    bool new_jac = true;
+    if (I.recomputing) {
+        new_jac = false;
+    } else if (I.alg == ORC_ROSENBROCK23) {
+        new_jac = jac_reuse_decision(I, dtgamma);
+        I.jr_last_step_iter = I.iter;
+        if (new_jac) I.jr_pending_dtgamma = dtgamma;
+    }
+    if (new_jac) {
+        jac(I.model, n, up, I.p, t, I.J.data());
+        I.st.njacs += 1;
+        // the model's tgrad, else the reference differentiates f in t by AD (one counted
+        // call; autonomous models: dT = 0)
+        if (!tgrad(I.model, n, up, I.p, t, I.dT.data())) {
+            f_eval(I, up, t, I.du.data());
+            std::fill(I.dT.begin(), I.dT.end(), 0.0);
+            I.st.nf += 1;
+        }
     }
     const double invdtgamma = 1.0 / dtgamma;
     for (int i = 0; i < n * n; ++i) I.W[i] = I.J[i];
@@ -842,6 +880,65 @@ void ros23_interp(double th, double dt, const double* y0, const double* K, int n
     const double c1 = th * (1.0 - th) / (1.0 - 2.0 * d);
     const double c2 = th * (th - 2.0 * d) / (1.0 - 2.0 * d);
     for (int i = 0; i < n; ++i) out[i] = std::fma(dt, std::fma(c1, K[i], c2 * K[n + i]), y0[i]);
+}
+
+// sol(t, Val{1}): the derivatives of the interpolants in t.
+// Tsit5 (lib/OrdinaryDiffEqTsit5/src/interpolants.jl:143-178): sum_i k_i b_i'(th) with
+// b1' = @evalpoly(th, r11, 2 r12, 3 r13, 4 r14), bi' = th @evalpoly(th, 2 ri2, 3 ri3, 4 ri4).
+void tsit5_interp_d1(double th, const double* K, int n, double* out) {
+    double b[8];
+    b[1] = std::fma(th, std::fma(th, std::fma(th, 4.0 * TSIT5_R[1][4], 3.0 * TSIT5_R[1][3]), 2.0 * TSIT5_R[1][2]),
+                    TSIT5_R[1][1]);
+    for (int s = 2; s <= 7; ++s)
+        b[s] = th * std::fma(th, std::fma(th, 4.0 * TSIT5_R[s][4], 3.0 * TSIT5_R[s][3]), 2.0 * TSIT5_R[s][2]);
+    for (int i = 0; i < n; ++i) {
+        double acc = K[6 * n + i] * b[7];
+        for (int s = 6; s >= 1; --s) acc = std::fma(K[(s - 1) * n + i], b[s], acc);
+        out[i] = acc;
+    }
+}
+
+// Vern7 (lib/OrdinaryDiffEqVerner/src/interpolants.jl:305-334), the extra stages formed.
+void vern7_interp_d1(double th, const double* K, int n, double* out) {
+    static const int idx[13] = {1, 4, 5, 6, 7, 8, 9, 11, 12, 13, 14, 15, 16};
+    double b[17];
+    {
+        double acc = 7.0 * VERN7_R[1][7];
+        for (int p = 6; p >= 1; --p) acc = std::fma(th, acc, (double)p * VERN7_R[1][p]);
+        b[1] = acc;
+    }
+    for (int q = 1; q < 13; ++q) {
+        const int s = idx[q];
+        double acc = 7.0 * VERN7_R[s][7];
+        for (int p = 6; p >= 2; --p) acc = std::fma(th, acc, (double)p * VERN7_R[s][p]);
+        b[s] = th * acc;
+    }
+    for (int i = 0; i < n; ++i) {
+        double acc = K[(16 - 1) * n + i] * b[16];
+        for (int q = 11; q >= 0; --q) acc = std::fma(K[(idx[q] - 1) * n + i], b[idx[q]], acc);
+        out[i] = acc;
+    }
+}
+
+// Rodas5P, interp_order 3 (lib/OrdinaryDiffEqRosenbrock/src/rosenbrock_interpolants.jl:444-470):
+// (k1 + th (-2 k1 + 2 k2 + th (-3 k2 + 3 k3 - 4 th k3)) - y0 + y1) / dt
+void rodas_interp_d1(double th, double dt, const double* y0, const double* y1, const double* K, int n,
+                     double* out) {
+    for (int i = 0; i < n; ++i) {
+        const double k1 = K[i], k2 = K[n + i], k3 = K[2 * n + i];
+        const double in2 = std::fma(-3.0, k2, std::fma(3.0, k3, -4.0 * th * k3));
+        const double in1 = std::fma(th, in2, std::fma(-2.0, k1, 2.0 * k2));
+        out[i] = ((std::fma(th, in1, k1) - y0[i]) + y1[i]) / dt;
+    }
+}
+
+// Rosenbrock23 (rosenbrock_interpolants.jl:111-127): c1' k1 + c2' k2 with
+// c1' = (1 - 2 th)/(1 - 2d), c2' = (2 th - 2d)/(1 - 2d).
+void ros23_interp_d1(double th, const double* K, int n, double* out) {
+    const double d = 1.0 / (2.0 + std::sqrt(2.0));
+    const double c1 = (1.0 - 2.0 * th) / (1.0 - 2.0 * d);
+    const double c2 = (2.0 * th - 2.0 * d) / (1.0 - 2.0 * d);
+    for (int i = 0; i < n; ++i) out[i] = std::fma(c1, K[i], c2 * K[n + i]);
 }
 
 void do_step(Integ& I) {
@@ -1141,7 +1238,9 @@ void recompute_step_k(Integ& I) {
     if (I.alg == ORC_TSIT5 || I.alg == ORC_ROSENBROCK23 || I.alg == ORC_AUTOTSIT5_ROSENBROCK23)
         f_eval(I, I.uprev.data(), I.t, I.fsalfirst.data());
     const double eig = I.eigen_est;
+    I.recomputing = true;
     do_step(I);
+    I.recomputing = false;
     I.eigen_est = eig;
     I.u = u;
     I.fsalfirst = fsf;
@@ -1614,6 +1713,9 @@ int solve_one(Integ& I, const double* u0) {
         I.piv.assign(n, 0);
         I.have_J = false;
     }
+    I.jr_last_dtgamma = I.jr_pending_dtgamma = 0.0;
+    I.jr_last_naccept = I.jr_last_step_iter = 0;
+    I.recomputing = false;
     I.t = I.t0;
     I.tprev = I.t0;
     I.nk_valid = 0;
@@ -1804,7 +1906,12 @@ int orc_dense_nsteps(void* h) { return h ? (int)((Dense*)h)->steps.size() : 0; }
 // index >= 1 (0-based) with ts[i+] >= t, clamped to the last; dt = ts[i+] -
 // ts[i-] and theta = (t - ts[i-]) / dt; Vern7's extra stages are formed by
 // _ode_addsteps! with that dt (verner_addsteps.jl:137-193).
-int orc_dense_eval(void* h, const double* tq, int nq, double* out) {
+int orc_dense_eval_deriv(void* h, const double* tq, int nq, int deriv, double* out);
+
+int orc_dense_eval(void* h, const double* tq, int nq, double* out) { return orc_dense_eval_deriv(h, tq, nq, 0, out); }
+
+int orc_dense_eval_deriv(void* h, const double* tq, int nq, int deriv, double* out) {
+    if (deriv < 0 || deriv > 1) return -2;
     Dense* D = (Dense*)h;
     const int n = D->n;
     if (D->steps.empty()) return -1;
@@ -1823,17 +1930,27 @@ int orc_dense_eval(void* h, const double* tq, int nq, double* out) {
         const double th = dt == 0.0 ? 1.0 : (t - ts(im)) / dt;
         double* o = out + (size_t)q * n;
         switch (D->alg) {
-        case ORC_TSIT5: tsit5_interp(th, dt, S.y0.data(), S.k.data(), n, o); break;
+        case ORC_TSIT5:
+            if (deriv) tsit5_interp_d1(th, S.k.data(), n, o);
+            else tsit5_interp(th, dt, S.y0.data(), S.k.data(), n, o);
+            break;
         case ORC_VERN7:
             K.assign((size_t)16 * n, 0.0);
             std::copy(S.k.begin(), S.k.end(), K.begin());
             vern7_extra(D->model, n, D->p.data(), ts(im), dt, S.y0.data(), K.data());
-            vern7_interp(th, dt, S.y0.data(), K.data(), n, o);
+            if (deriv) vern7_interp_d1(th, K.data(), n, o);
+            else vern7_interp(th, dt, S.y0.data(), K.data(), n, o);
             break;
-        case ORC_RODAS5P: rodas_interp(th, S.y0.data(), S.y1.data(), S.k.data(), n, o); break;
-        case ORC_ROSENBROCK23: ros23_interp(th, dt, S.y0.data(), S.k.data(), n, o); break;
+        case ORC_RODAS5P:
+            if (deriv) rodas_interp_d1(th, dt, S.y0.data(), S.y1.data(), S.k.data(), n, o);
+            else rodas_interp(th, S.y0.data(), S.y1.data(), S.k.data(), n, o);
+            break;
+        case ORC_ROSENBROCK23:
+            if (deriv) ros23_interp_d1(th, S.k.data(), n, o);
+            else ros23_interp(th, dt, S.y0.data(), S.k.data(), n, o);
+            break;
         default:
-            for (int i = 0; i < n; ++i) o[i] = (1.0 - th) * S.y0[i] + th * S.y1[i];
+            for (int i = 0; i < n; ++i) o[i] = deriv ? (S.y1[i] - S.y0[i]) / dt : (1.0 - th) * S.y0[i] + th * S.y1[i];
         }
     }
     return 0;

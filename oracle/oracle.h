@@ -55,6 +55,8 @@ typedef struct {
     int32_t max_events;       /* ensemble: 2 more save slots per event */
     int32_t ntstops;          /* ensemble: user tstops shared by every trajectory, */
     const double* tstops;     /* kept where t0 < ts < tf (initialize_tstops) */
+    int32_t max_jac_age;      /* Rosenbrock23: J kept for at most this many accepted steps (1: never) */
+    double jac_reuse_gamma_tol; /* ... while |dtgamma / dtgamma_J - 1| <= this (0.03) */
 } orc_opts;
 
 /* Solve one trajectory.  saveat: nsave_in times in (t0, tf] sorted ascending.
@@ -75,6 +77,8 @@ double orc_initdt(int alg, int model, int n, const double* p, double t0, double 
 /* Evaluate the stored dense solution at nq times (out: nq*n), as the
  * reference's sol(t) does (ode_interpolation on the every-step saves). */
 int orc_dense_eval(void* dense_handle, const double* tq, int nq, double* out);
+/* The same with the derivative order (0 the value, 1 sol(t, Val{1})). */
+int orc_dense_eval_deriv(void* dense_handle, const double* tq, int nq, int deriv, double* out);
 /* Step s: t2 = (tprev, tend), y0, y1 (n each), k (returned count x n): the
  * interpolation vectors in the library's dense order. */
 int orc_dense_step(void* dense_handle, int s, double* t2, double* y0, double* y1, double* k);

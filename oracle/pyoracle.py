@@ -36,7 +36,7 @@ class Opts(C.Structure):
         ("qmax_first_step", C.c_double), ("qmax", C.c_double), ("saveat_as_tstops", C.c_int32),
         ("save_everystep", C.c_int32), ("max_step_saves", C.c_int32),
         ("callback", C.c_int32), ("interp_points", C.c_int32), ("max_events", C.c_int32), ("ntstops", C.c_int32),
-        ("tstops", C.POINTER(C.c_double)),
+        ("tstops", C.POINTER(C.c_double)), ("max_jac_age", C.c_int32), ("jac_reuse_gamma_tol", C.c_double),
     ]
 
 
@@ -59,6 +59,7 @@ def lib():
                                 C.POINTER(Opts), dp, C.c_int, dp, C.c_int, dp, dp, C.c_int,
                                 C.POINTER(C.c_int32), C.POINTER(Stats), C.POINTER(C.c_void_p)]
         L.orc_dense_eval.argtypes = [C.c_void_p, dp, C.c_int, dp]
+        L.orc_dense_eval_deriv.argtypes = [C.c_void_p, dp, C.c_int, C.c_int, dp]
         L.orc_dense_free.argtypes = [C.c_void_p]
         L.orc_dense_nsteps.argtypes = [C.c_void_p]
         L.orc_dense_step.restype = C.c_int
@@ -94,12 +95,13 @@ def make_opts(reltol=1e-3, abstol=1e-6, dtmax=0.0, dtmin=0.0, dt=0.0, adaptive=T
               maxiters=1000000, save_start=False, save_end=True, save_end_user=-1,
               saveat_given=True, saveat_scalar=False, qmax_first_step=0.0, qmax=0.0, saveat_as_tstops=False,
               save_everystep=False, max_step_saves=0, callback=False, interp_points=10, max_events=0,
-              tstops=()):
+              tstops=(), max_jac_age=1, jac_reuse_gamma_tol=0.03):
     ts = np.ascontiguousarray(tstops, dtype=np.float64).ravel()
     o = Opts(reltol, abstol, dtmax, dtmin, dt, int(adaptive), maxiters, int(save_start),
              int(save_end), save_end_user, int(saveat_given), int(saveat_scalar),
              qmax_first_step, qmax, int(saveat_as_tstops), int(save_everystep), int(max_step_saves),
-             int(callback), int(interp_points), int(max_events), int(ts.size), _dp(ts) if ts.size else None)
+             int(callback), int(interp_points), int(max_events), int(ts.size), _dp(ts) if ts.size else None,
+             int(max_jac_age), float(jac_reuse_gamma_tol))
     o._tstops = ts   # keeps the array alive as long as the options
     return o
 
@@ -149,10 +151,10 @@ class DenseSolution:
     def __init__(self, h, n):
         self.h, self.n = h, n
 
-    def __call__(self, ts):
+    def __call__(self, ts, deriv=0):
         ts = np.ascontiguousarray(np.atleast_1d(ts), dtype=np.float64)
         out = np.zeros((ts.size, self.n))
-        lib().orc_dense_eval(self.h, _dp(ts), ts.size, _dp(out))
+        lib().orc_dense_eval_deriv(self.h, _dp(ts), ts.size, int(deriv), _dp(out))
         return out
 
     @property

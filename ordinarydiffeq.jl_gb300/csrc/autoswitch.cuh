@@ -49,6 +49,7 @@ struct AutoSwitchAlg {
         c.eigen_est = 1.0;
         NS::template initialize<Model, R, L, C>(c.ns, u, p, t, g, st, a, j);   // the current method's FSAL
         S::template prepare<Model, R, L, C>(c.s, g, a, j);
+        c.s.max_age = 1;   // a CompositeAlgorithm always takes a fresh J (derivative_utils.jl:104-108)
     }
     template <class R, int C> __device__ static void on_accept(Cache<R, C>& c) {
         if (c.current == 0) NS::on_accept(c.ns);

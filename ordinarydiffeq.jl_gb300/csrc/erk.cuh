@@ -44,6 +44,16 @@ __device__ __forceinline__ double interp_weight(double th, int i, RF r, bool fir
     for (int q = NPOLY - 2; q >= (first ? 1 : 2); --q) acc = fma(th, acc, r(i, q));
     return first ? th * acc : (th * th) * acc;
 }
+// Derivative weights b_i'(theta) of the reference's Val{1} interpolants: Horner
+// over the coefficients times their powers (b1: @evalpoly(th, r1, 2 r2, ...);
+// the others th * @evalpoly(th, 2 r2, 3 r3, ...)), in FP64.
+template <int NPOLY, class RF>
+__device__ __forceinline__ double interp_dweight(double th, int i, RF r, bool first) {
+    double acc = (double)(NPOLY - 1) * r(i, NPOLY - 1);
+#pragma unroll
+    for (int q = NPOLY - 2; q >= (first ? 1 : 2); --q) acc = fma(th, acc, (double)q * r(i, q));
+    return first ? acc : th * acc;
+}
 // Mixed form: the weights stay FP64 (a save is rare and the FP64 pipe is
 // otherwise idle there; a double-float Horner measured slower on the FP32
 // issue path) and are split once into float pairs for the compensated sums.
@@ -229,6 +239,24 @@ struct Tsit5Alg {
     }
 };
 
+// sol(t, Val{1}) of a Tsit5 step (interpolants.jl:143-178): sum_i k_i b_i'(theta),
+// FP64 (the dense-output evaluation).
+template <int C>
+__device__ __forceinline__ void tsit5_derivative(const double (*k)[C], double th, double* out) {
+    auto r = [](int i, int q) { return tab::TSIT5_R(i, q); };
+    double b[8];
+    b[1] = interp_dweight<5>(th, 1, r, true);
+#pragma unroll
+    for (int i = 2; i <= 7; ++i) b[i] = interp_dweight<5>(th, i, r, false);
+#pragma unroll
+    for (int i = 0; i < C; ++i) {
+        double acc = k[6][i] * b[7];
+#pragma unroll
+        for (int s = 6; s >= 1; --s) acc = fma(k[s - 1][i], b[s], acc);
+        out[i] = acc;
+    }
+}
+
 struct Vern7Alg {
     static constexpr int ORDER = 7;
     static constexpr bool IMPLICIT = false;
@@ -351,6 +379,27 @@ struct Vern7Alg {
                 for (int q = 0; q < 13; ++q) cs.add_pair(b[q].hi, b[q].lo, (float)c.s[Vern7Tab::slot(idx[q])][i]);
                 Acc<R>::update2(out[i], outlo[i], d, dl, (R)cs.value(), y0[i], y0lo[i]);
             }
+        }
+    }
+
+    // sol(t, Val{1}) (interpolants.jl:305-334): sum over the 13 stages of k_s b_s'(theta),
+    // the extra stages formed first; FP64 (the dense-output evaluation).
+    template <class Model, int L, int C>
+    __device__ static void derivative(Cache<double, C>& c, double* out, double th, double dt, double tprev,
+                                      const double* y0, const double* y0lo, const double* p, const Group<L>& g) {
+        if (!c.extra) extra_stages<Model, double, L, C>(c, tprev, dt, y0, y0lo, p, g);
+        constexpr int idx[13] = {1, 4, 5, 6, 7, 8, 9, 11, 12, 13, 14, 15, 16};
+        auto r = [](int i, int q) { return tab::VERN7_R(i, q); };
+        double b[13];
+        b[0] = interp_dweight<8>(th, 1, r, true);
+#pragma unroll
+        for (int q = 1; q < 13; ++q) b[q] = interp_dweight<8>(th, idx[q], r, false);
+#pragma unroll
+        for (int i = 0; i < C; ++i) {
+            double acc = c.s[Vern7Tab::slot(16)][i] * b[12];
+#pragma unroll
+            for (int q = 11; q >= 0; --q) acc = fma(c.s[Vern7Tab::slot(idx[q])][i], b[q], acc);
+            out[i] = acc;
         }
     }
 };

@@ -479,8 +479,10 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             StepStats uncounted = {0, 0, 0, 0, 0, 0};
             double eig = 0.0;
             if constexpr (is_composite_alg<Alg>::value) eig = cache.eigen_est;
+            // iter -1: the recomputation (a W-method keeps the step's J, as the in-place
+            // addsteps does, and its reuse state)
             Alg::template step<Model, R, L, C>(cache, ut, utlo, uprev, uprevlo, p, TM(tprev), TM(dt), abstol, reltol,
-                                               iter, false, g, uncounted);
+                                               -1, false, g, uncounted);
             if constexpr (is_composite_alg<Alg>::value) cache.eigen_est = eig;
         }
     };

@@ -75,19 +75,37 @@ __global__ void dense_eval_pointwise(DenseArgs a) {
             Tsit5Alg::Cache<double, 1> c;
 #pragma unroll
             for (int q = 0; q < NK; ++q) c.k[q][0] = kp[(size_t)q * n * N];
-            Tsit5Alg::interpolate<Linear, double, 1, 1>(c, &o, &olo, v.th, v.dt, v.tprev, &y0, &z, &y1, &z, nullptr,
-                                                        g);
+            if (a.deriv) tsit5_derivative<1>(c.k, v.th, &o);
+            else Tsit5Alg::interpolate<Linear, double, 1, 1>(c, &o, &olo, v.th, v.dt, v.tprev, &y0, &z, &y1, &z,
+                                                             nullptr, g);
         } else if constexpr (ALG == 2) {
             Rodas5PAlg::Cache<double, 1> c;
 #pragma unroll
             for (int q = 0; q < NK; ++q) c.dk[q][0] = kp[(size_t)q * n * N];
-            Rodas5PAlg::interp_dense<double, 1>(c, &o, &olo, v.th, &y0, &z, &y1, &z);
+            if (a.deriv) {
+                // rosenbrock_interpolants.jl:444-470 (interp_order 3):
+                // (k1 + th (-2 k1 + 2 k2 + th (-3 k2 + 3 k3 - 4 th k3)) - y0 + y1) / dt
+                const double k1 = c.dk[0][0], k2 = c.dk[1][0], k3 = c.dk[2][0], th = v.th;
+                const double in2 = fma(-3.0, k2, fma(3.0, k3, -4.0 * th * k3));
+                const double in1 = fma(th, in2, fma(-2.0, k1, 2.0 * k2));
+                o = ((fma(th, in1, k1) - y0) + y1) / v.dt;
+            } else {
+                Rodas5PAlg::interp_dense<double, 1>(c, &o, &olo, v.th, &y0, &z, &y1, &z);
+            }
         } else {
             Rosenbrock23Alg::Cache<double, 1> c;
 #pragma unroll
             for (int q = 0; q < NK; ++q) c.k[q][0] = kp[(size_t)q * n * N];
-            Rosenbrock23Alg::interpolate<Linear, double, 1, 1>(c, &o, &olo, v.th, v.dt, v.tprev, &y0, &z, &y1, &z,
-                                                               nullptr, g);
+            if (a.deriv) {
+                // rosenbrock_interpolants.jl:111-127: c1' k1 + c2' k2, c1' = (1 - 2 th)/(1 - 2d),
+                // c2' = (2 th - 2d)/(1 - 2d)
+                const double d = tab::ROS23_D, th = v.th;
+                const double c1 = (1.0 - 2.0 * th) / (1.0 - 2.0 * d), c2 = (2.0 * th - 2.0 * d) / (1.0 - 2.0 * d);
+                o = fma(c1, c.k[0][0], c2 * c.k[1][0]);
+            } else {
+                Rosenbrock23Alg::interpolate<Linear, double, 1, 1>(c, &o, &olo, v.th, v.dt, v.tprev, &y0, &z, &y1, &z,
+                                                                   nullptr, g);
+            }
         }
         a.out[((size_t)r * n + i) * N + j] = o;
     }
@@ -127,7 +145,8 @@ __global__ void dense_eval_vern7(DenseArgs a) {
                 a.ks[(((size_t)v.ip * Vern7Alg::NDENSE + q) * n + i) * N + j];
     }
     cache.extra = false;
-    Vern7Alg::interpolate<Model, double, L, C>(cache, out, outlo, v.th, v.dt, v.tprev, y0, z, y1, z, p, g);
+    if (a.deriv) Vern7Alg::derivative<Model, L, C>(cache, out, v.th, v.dt, v.tprev, y0, z, p, g);
+    else Vern7Alg::interpolate<Model, double, L, C>(cache, out, outlo, v.th, v.dt, v.tprev, y0, z, y1, z, p, g);
 #pragma unroll
     for (int c = 0; c < C; ++c) a.out[((size_t)r * n + g.lane * C + c) * N + j] = out[c];
 }

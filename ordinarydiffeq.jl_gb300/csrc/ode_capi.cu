@@ -264,6 +264,13 @@ int check_problem(const ode_problem_desc* d, const ode_options* o, int64_t N, co
         return bad(ODE_E_INVALID, "save_everystep needs max_step_saves > 0");
     if (o->ntstops < 0 || (o->ntstops > 0 && !o->tstops))
         return bad(ODE_E_INVALID, "ntstops < 0, or tstops is null");
+    if (o->max_jac_age < 0) return bad(ODE_E_INVALID, "max_jac_age must be >= 0");
+    // the kept J lives beside W in registers; the shared-memory LU (16-64 states)
+    // forms W in place of J
+    if (d->alg_id == ODE_ROSENBROCK23 && o->max_jac_age > 1 && d->n_states > 8)
+        return bad(ODE_E_UNSUPPORTED, "Rosenbrock23 Jacobian reuse (max_jac_age > 1) needs n_states <= 8");
+    if (o->jac_reuse_gamma_tol != o->jac_reuse_gamma_tol)
+        return bad(ODE_E_INVALID, "jac_reuse_gamma_tol is NaN");
     return ODE_OK;
 }
 
@@ -333,6 +340,8 @@ EnsembleArgs make_args(ode_handle* h, const ode_problem_desc* d, const ode_optio
     a.interp_points = o->interp_points;
     a.tstops = o->ntstops > 0 ? o->tstops : nullptr;   // device memory, ascending, at this point
     a.ntstops = o->ntstops > 0 ? o->ntstops : 0;
+    a.max_jac_age = o->max_jac_age;
+    a.jac_reuse_gamma_tol = o->jac_reuse_gamma_tol < 0 ? 0.03 : o->jac_reuse_gamma_tol;
     a.t_out = t_out;
     a.u_out = u_out;
     a.nsaved = nsaved;
@@ -1311,6 +1320,8 @@ void ode_options_default(ode_options* o) {
     o->save_end_user = -1;
     o->ir_sweeps = -1;
     o->interp_points = 10;
+    o->max_jac_age = 1;
+    o->jac_reuse_gamma_tol = 0.03;
 }
 
 size_t ode_options_size(void) { return sizeof(ode_options); }
@@ -1414,10 +1425,12 @@ int ode_solve_ensemble_dense(ode_handle* h, const ode_problem_desc* d, const ode
     return solve_host(h, d, o, N, nullptr, u0, p, tspan, nullptr, t_out, u_out, k_out, nsaved, retcode, stats);
 }
 
-int ode_dense_eval(ode_handle* h, const ode_problem_desc* d, int64_t N, const double* p, const double* t_saved,
-                   const double* u_saved, const double* k_saved, const int32_t* nsaved, int32_t cap, int32_t nq,
-                   const double* tq, int32_t tq_per_traj, double* out) {
+int ode_dense_eval_deriv(ode_handle* h, const ode_problem_desc* d, int64_t N, const double* p,
+                         const double* t_saved, const double* u_saved, const double* k_saved, const int32_t* nsaved,
+                         int32_t cap, int32_t nq, const double* tq, int32_t tq_per_traj, int32_t deriv, double* out) {
     if (!h || !d) return fail(h, ODE_E_INVALID, "null handle or problem");
+    if (deriv < 0) return fail(h, ODE_E_INVALID, "negative derivative order");
+    if (deriv > 1) return fail(h, ODE_E_UNSUPPORTED, "dense evaluation of the value (0) or first derivative (1) only");
     ode_options o;
     ode_options_default(&o);
     int rc = validate(h, d, &o, N);
@@ -1445,6 +1458,7 @@ int ode_dense_eval(ode_handle* h, const ode_problem_desc* d, int64_t N, const do
     a.nq = nq;
     a.tq_per_traj = tq_per_traj ? 1 : 0;
     a.cap = cap;
+    a.deriv = deriv;
     cudaStream_t s = h->main.stream;
     // The saves are copied in (the interval search reads them scattered, which is
     // slow from host memory: measured 30x slower in place over NVLink-C2C); a
@@ -1483,6 +1497,12 @@ int ode_dense_eval(ode_handle* h, const ode_problem_desc* d, int64_t N, const do
     float ms = 0;
     if (cudaEventElapsedTime(&ms, h->main.ev0, h->main.ev1) == cudaSuccess) h->last_ms = ms;
     return ODE_OK;
+}
+
+int ode_dense_eval(ode_handle* h, const ode_problem_desc* d, int64_t N, const double* p, const double* t_saved,
+                   const double* u_saved, const double* k_saved, const int32_t* nsaved, int32_t cap, int32_t nq,
+                   const double* tq, int32_t tq_per_traj, double* out) {
+    return ode_dense_eval_deriv(h, d, N, p, t_saved, u_saved, k_saved, nsaved, cap, nq, tq, tq_per_traj, 0, out);
 }
 
 int ode_submit(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int64_t N, const int32_t* npt,
@@ -1892,6 +1912,8 @@ extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_o
     a.interp_points = o->interp_points;
     a.tstops = o->ntstops > 0 ? o->tstops : nullptr;   // device memory, ascending
     a.ntstops = o->ntstops > 0 ? o->ntstops : 0;
+    a.max_jac_age = o->max_jac_age;
+    a.jac_reuse_gamma_tol = o->jac_reuse_gamma_tol < 0 ? 0.03 : o->jac_reuse_gamma_tol;
     a.t_out = t_out;
     a.u_out = u_out;
     a.nsaved = nsaved;

@@ -45,6 +45,7 @@ struct DenseArgs {
     const int32_t* nsaved;
     const double* tq;
     double* out;
+    int deriv;              // 0: sol(t); 1: sol(t, Val{1})
 };
 
 // Dense vectors stored per step, by ode_alg (Tsit5, Vern7, Rodas5P, Rosenbrock23,

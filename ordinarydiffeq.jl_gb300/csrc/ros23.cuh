@@ -5,10 +5,12 @@
 //  initialize! (FSAL, k = [k1, k2])   rosenbrock_perform_step.jl:1-14
 //  tableau                             rosenbrock_tableaus.jl:6-10 (c32 = 6 + sqrt(2), d = 1/(2 + sqrt(2)))
 //  interpolant                         rosenbrock_interpolants.jl:39-74
-//  J and W on every attempt            a W-method whose default max_jac_age = 1
-//                                      (algorithms.jl:108-115) makes _rosenbrock_jac_reuse_decision
+//  J reuse (a W-method)                _rosenbrock_jac_reuse_decision
 //                                      (OrdinaryDiffEqDifferentiation/src/derivative_utils.jl:46-170)
-//                                      return a fresh J and W each time, rejected or not
+//                                      with calc_rosenbrock_differentiation! (:1011-1041): the
+//                                      default max_jac_age = 1 (algorithms.jl:108-115) takes a fresh
+//                                      J on every attempt, rejected or not; a larger one keeps J
+//                                      (and dT) across accepted steps; W and its LU every attempt
 //  controller                          alg_order 2 (alg_utils.jl:1), qsteady_max 6/5 (AdaptiveImplicit)
 //
 // With W = J - I/(dt d) (the form the Rodas5P kernels factor), a solve x = W \ b
@@ -42,6 +44,11 @@ struct Rosenbrock23T {
         R dT[C];         // df/dt at (uprev, t), non-autonomous models
         ff pff[MAXP];
         int ir;
+        // Jacobian reuse (JacReuseState): dtgamma of the last fresh J once an accepted
+        // step has passed, the one pending, and naccept at the last age reset
+        int max_age;
+        double gamma_tol, last_dtg, pending_dtg;
+        long long last_naccept, last_step_iter;
     };
     template <class R, int L, int C> __host__ __device__ static constexpr int smem_bytes() {
         return LA::template smem_bytes<R, L, C>();
@@ -53,6 +60,10 @@ struct Rosenbrock23T {
     __device__ static void prepare(Cache<R, C>& c, const Group<L>& g, const EnsembleArgs& a, long long j) {
         LA::template init<R, L, C>(c.la, g);
         c.ir = a.ir_sweeps;
+        c.max_age = a.max_jac_age;
+        c.gamma_tol = a.jac_reuse_gamma_tol;
+        c.last_dtg = c.pending_dtg = 0.0;
+        c.last_naccept = c.last_step_iter = 0;
         if (sizeof(R) == 4) {
 #pragma unroll
             for (int i = 0; i < Model::NP; ++i) c.pff[i] = ff(a.p[(size_t)i * a.N + j]);
@@ -97,10 +108,37 @@ struct Rosenbrock23T {
         st.nf += 1;
     }
 
+    // _rosenbrock_jac_reuse_decision for this W-method (no mass matrix, adaptive, not
+    // inside a composite): a fresh J on the first attempt, after a rejected one, when
+    // no J has been committed yet, when an attempt was skipped since the last (a
+    // step below eps(t) onto a tstop), when dtgamma moved more than gamma_tol from
+    // the J's, and every max_age accepted steps (the age reset); else the J (and dT)
+    // kept.  iter < 0: an event's recomputation of the shortened step, which keeps
+    // the step's J (the in-place addsteps reuses it) and touches no reuse state.
+    template <class R, int C>
+    __device__ static bool fresh_jacobian(Cache<R, C>& c, double dt, long long iter, bool errorfail,
+                                          long long naccept) {
+        if (iter < 0) return false;
+        if (c.max_age <= 1) return true;   // the age check fires on every attempt
+        const double dtg = dt * tab::ROS23_D;
+        bool fresh = true;
+        if (iter > 1) {
+            if (naccept > c.last_naccept) c.last_dtg = c.pending_dtg;
+            const bool skipped = c.last_step_iter != 0 && iter > c.last_step_iter + 1;
+            if (c.last_dtg != 0.0 && !skipped && !errorfail && !(fabs(dtg / c.last_dtg - 1.0) > c.gamma_tol)) {
+                if (naccept - c.last_naccept >= c.max_age) c.last_naccept = naccept;
+                else fresh = false;
+            }
+        }
+        c.last_step_iter = iter;
+        if (fresh) c.pending_dtg = dtg;
+        return fresh;
+    }
+
     template <class Model, class R, int L, int C>
     __device__ static typename Ctl<R>::T step(Cache<R, C>& c, R* u, R* ulo, const R* up, const R* uplo,
-                                             const PR<R>* p, double t, double dt, R abstol, R reltol, long long,
-                                             bool, const Group<L>& g, StepStats& st) {
+                                             const PR<R>* p, double t, double dt, R abstol, R reltol, long long iter,
+                                             bool errorfail, const Group<L>& g, StepStats& st) {
         constexpr int NP = Model::NP;
         R dr, idg, ninv, dto2, dto6, c32;
         if constexpr (sizeof(R) == 8) {
@@ -121,14 +159,17 @@ struct Rosenbrock23T {
         }
         static_assert(Model::AUTONOMOUS || has_tgrad<Model>::value, "a non-autonomous model needs its tgrad");
         static_assert(Model::AUTONOMOUS || L == 1, "time derivatives are formed on one lane");
-        LA::template jacobian<Model, R, L, C>(c.la, up, p, t, true, g);
-        st.njacs += 1;
-        st.nf += jac_f_calls<Model>::value;
-        // the time derivative (calc_tderivative!, derivative_utils.jl:181-227): the model's
-        // analytic tgrad (not an f call); else dT = 0 for an autonomous model, whose AD
-        // evaluation in the reference counts as one f call
-        if constexpr (has_tgrad<Model>::value) Model::template tgrad<R, C>(c.dT, up, p, t);
-        else st.nf += 1;
+        const bool new_jac = fresh_jacobian(c, dt, iter, errorfail, st.naccept);
+        LA::template jacobian<Model, R, L, C>(c.la, up, p, t, new_jac, g);
+        if (new_jac) {
+            st.njacs += 1;
+            st.nf += jac_f_calls<Model>::value;
+            // the time derivative (calc_tderivative!, derivative_utils.jl:181-227), with a
+            // fresh J only: the model's analytic tgrad (not an f call); else dT = 0 for an
+            // autonomous model, whose AD evaluation in the reference counts as one f call
+            if constexpr (has_tgrad<Model>::value) Model::template tgrad<R, C>(c.dT, up, p, t);
+            else st.nf += 1;
+        }
         LA::template factor<R, L, C>(c.la, idg, g);
         st.nw += 1;
         R* k1 = c.k[0];

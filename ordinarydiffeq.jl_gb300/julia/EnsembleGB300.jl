@@ -101,7 +101,11 @@ mutable struct Options
     saveat_per_traj::Int32; qmax_first_step::Float64; qmax::Float64; lanes_per_traj::Int32
     scheduler::Int32; block_size::Int32; ir_sweeps::Int32; save_everystep::Int32; max_step_saves::Int32
     callback::Int32; interp_points::Int32; max_events::Int32; ntstops::Int32; tstops::Ptr{Float64}
+    max_jac_age::Int32; reserved2::Int32; jac_reuse_gamma_tol::Float64
 end
+# the W-method Jacobian reuse knobs of Rosenbrock23(max_jac_age, jac_reuse_gamma_tol)
+jac_reuse(alg::Rosenbrock23) = (Int32(alg.max_jac_age), Float64(alg.jac_reuse_gamma_tol))
+jac_reuse(alg) = (Int32(1), 0.03)
 struct Stats
     nf::Int64; njacs::Int64; nw::Int64; nsolve::Int64; naccept::Int64; nreject::Int64
 end
@@ -128,7 +132,7 @@ const RETCODES = (SciMLBase.ReturnCode.Default, SciMLBase.ReturnCode.Success, Sc
 """
 Interpolation of a dense GB300 solve (the reference's dense = true): sol(t)
 evaluates the method's interpolant on the saved steps on the device
-(ode_dense_eval), as ode_interpolation does on the host.  Holds one
+(ode_dense_eval_deriv; sol(t, Val{1}) too), as ode_interpolation does on the host.  Holds one
 trajectory's saves t (ns), u (n x ns) and interpolation vectors k (n x nk x ns).
 """
 struct GB300DenseInterpolation <: SciMLBase.AbstractDiffEqInterpolation
@@ -142,16 +146,17 @@ struct GB300DenseInterpolation <: SciMLBase.AbstractDiffEqInterpolation
 end
 
 function (id::GB300DenseInterpolation)(tvals, idxs, deriv, p, continuity::Symbol = :left)
-    deriv == Val{0} || error("GB300 dense output evaluates the solution (deriv = Val{0}) only")
+    order = deriv == Val{0} ? 0 : deriv == Val{1} ? 1 :
+            error("GB300 dense output evaluates the solution (Val{0}) and its first derivative (Val{1})")
     tq = tvals isa Number ? [Float64(tvals)] : collect(Float64, tvals)
     n, ns, nq = size(id.u, 1), length(id.t), length(tq)
     d = ProblemDesc(id.model, id.alg, n, length(id.p), 0, 0)
     out = zeros(n, nq)   # [(r*n + i)*N + j] with N = 1 -> out[i, r]
-    status = ccall((:ode_dense_eval, LIB), Cint,
+    status = ccall((:ode_dense_eval_deriv, LIB), Cint,
                    (Ptr{Cvoid}, Ref{ProblemDesc}, Int64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
-                    Ptr{Int32}, Int32, Int32, Ptr{Float64}, Int32, Ptr{Float64}),
-                   handle(id.device), d, 1, id.p, id.t, id.u, id.k, Int32[ns], ns, nq, tq, 0, out)
-    status == 0 || error("ode_dense_eval: ", unsafe_string(ccall((:ode_last_error, LIB), Cstring, (Ptr{Cvoid},), handle(id.device))))
+                    Ptr{Int32}, Int32, Int32, Ptr{Float64}, Int32, Int32, Ptr{Float64}),
+                   handle(id.device), d, 1, id.p, id.t, id.u, id.k, Int32[ns], ns, nq, tq, 0, order, out)
+    status == 0 || error("ode_dense_eval_deriv: ", unsafe_string(ccall((:ode_last_error, LIB), Cstring, (Ptr{Cvoid},), handle(id.device))))
     vals = [idxs === nothing ? out[:, r] : out[idxs, r] for r in 1:nq]
     tvals isa Number ? vals[1] : vals
 end
@@ -210,7 +215,7 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem,
     o = Options(reltol, abstol, dtmax, dtmin, dt, maxiters, ss, se, save_end === nothing ? -1 : Int32(save_end),
                 scalar, length(sv), 0, 0.0, 0.0, ens.lanes_per_traj, ens.scheduler, 0, -1, everystep,
                 everystep ? max_step_saves : 0, cb, cb ? callback.interp_points : 10, cb ? callback.max_events : 0,
-                length(tst), isempty(tst) ? Ptr{Float64}(C_NULL) : pointer(tst))
+                length(tst), isempty(tst) ? Ptr{Float64}(C_NULL) : pointer(tst), jac_reuse(alg)[1], Int32(0), jac_reuse(alg)[2])
     d = ProblemDesc(model, alg_id(alg), n, npar, ens.precision === :mixed ? 1 : 0, 0)
     cap = (everystep ? max_step_saves : length(sv)) + 2 + (cb ? 2 * callback.max_events : 0)
     t_out = fill(NaN, N, cap); u_out = fill(NaN, N, n, cap)   # [(s*n + i)*N + j] -> u_out[j, i, s]

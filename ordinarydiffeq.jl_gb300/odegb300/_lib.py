@@ -39,7 +39,8 @@ class Options(C.Structure):
                 ("scheduler", C.c_int32), ("block_size", C.c_int32), ("ir_sweeps", C.c_int32),
                 ("save_everystep", C.c_int32), ("max_step_saves", C.c_int32),
                 ("callback", C.c_int32), ("interp_points", C.c_int32), ("max_events", C.c_int32),
-                ("ntstops", C.c_int32), ("tstops", C.POINTER(C.c_double))]
+                ("ntstops", C.c_int32), ("tstops", C.POINTER(C.c_double)),
+                ("max_jac_age", C.c_int32), ("reserved2", C.c_int32), ("jac_reuse_gamma_tol", C.c_double)]
 
 
 class Stats(C.Structure):
@@ -74,6 +75,8 @@ SIGNATURES = {
                                            _DP, _DP, _DP, _DP, _IP, _IP, C.POINTER(Stats)]),
     "ode_dense_eval": (C.c_int, [_VP, C.POINTER(ProblemDesc), C.c_int64, _DP, _DP, _DP, _DP, _IP, C.c_int32,
                                  C.c_int32, _DP, C.c_int32, _DP]),
+    "ode_dense_eval_deriv": (C.c_int, [_VP, C.POINTER(ProblemDesc), C.c_int64, _DP, _DP, _DP, _DP, _IP, C.c_int32,
+                                       C.c_int32, _DP, C.c_int32, C.c_int32, _DP]),
     "ode_submit": (C.c_int, [_VP, C.POINTER(ProblemDesc), C.POINTER(Options), C.c_int64, _IP, _DP, _DP,
                              _DP, _DP, _DP, _DP, _IP, _IP, C.POINTER(Stats), C.POINTER(C.c_uint64)]),
     "ode_poll": (C.c_int, [_VP, C.c_uint64, _IP]),

@@ -90,9 +90,19 @@ class Rodas5P(_Alg):
 
 class Rosenbrock23(_Alg):
     """Rosenbrock23 (Shampine's ode23s W-method pair) with the analytic Jacobian of
-    the model, a fresh J and W on every step attempt (the reference's default
-    max_jac_age = 1; lib/OrdinaryDiffEqRosenbrock/src/algorithms.jl:108-146)."""
+    the model (lib/OrdinaryDiffEqRosenbrock/src/algorithms.jl:108-146).  As a
+    W-method it may keep J across accepted steps: max_jac_age = 1 (the
+    reference's default) takes a fresh J on every attempt; a larger value keeps
+    it for up to that many accepted steps while dt*gamma stays within
+    jac_reuse_gamma_tol of the J's (_rosenbrock_jac_reuse_decision)."""
     alg_id = _lib.ODE_ROSENBROCK23
+
+    def __init__(self, max_jac_age=1, jac_reuse_gamma_tol=0.03):
+        self.max_jac_age = int(max_jac_age)
+        self.jac_reuse_gamma_tol = float(jac_reuse_gamma_tol)
+
+    def __repr__(self):
+        return "Rosenbrock23(max_jac_age=%d)" % self.max_jac_age if self.max_jac_age != 1 else "Rosenbrock23()"
 
 
 class AutoTsit5(_Alg):
@@ -212,18 +222,21 @@ class ODESolution:
     def dense(self):
         return self._dense is not None
 
-    def __call__(self, t):
+    def __call__(self, t, deriv=0, idxs=None):
         """sol(t) as ode_interpolation (generic_dense.jl:1094-1190) evaluates it:
         the method's interpolant on the saved steps for a dense solve (on the
-        GPU), linear interpolation between saves otherwise.  Scalar t gives one
-        state vector, an array of times one row per time."""
+        GPU), linear interpolation between saves otherwise.  deriv=1 is
+        sol(t, Val{1}) (dense solves); idxs selects components.  Scalar t gives
+        one state vector, an array of times one row per time."""
         tq = np.atleast_1d(np.asarray(t, dtype=np.float64))
         if self._dense is not None:
             res, j = self._dense
             sub = {"t": res["t"][:, j:j + 1].copy(), "u": res["u"][:, :, j:j + 1].copy(),
                    "k": res["k"][..., j:j + 1].copy(), "nsaved": res["nsaved"][j:j + 1].copy(),
                    "dense": dict(res["dense"], p=res["dense"]["p"][:, j:j + 1].copy())}
-            vals = dense_eval(sub, tq)[:, :, 0]
+            vals = dense_eval(sub, tq, deriv=deriv)[:, :, 0]
+        elif deriv:
+            raise ValueError("derivatives of the interpolant need a dense solve")
         else:
             ts = np.asarray(self.t, dtype=np.float64)
             us = np.asarray(self.u, dtype=np.float64)
@@ -234,6 +247,8 @@ class ODESolution:
                 dt = ts[ip] - ts[im]
                 th = 1.0 if dt == 0 else (tv - ts[im]) / dt
                 vals[r] = (1 - th) * us[im] + th * us[ip]
+        if idxs is not None:
+            vals = vals[:, idxs]
         return vals[0] if np.ndim(t) == 0 else vals
 
     def __repr__(self):
@@ -293,10 +308,13 @@ def get_handle(device=0):
 
 
 def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax, callback=None,
-             tstops=None):
+             tstops=None, alg=None):
     o = _lib.Options()
     L = _lib.load()
     L.ode_options_default(C.byref(o))
+    if isinstance(alg, Rosenbrock23):   # its W-method Jacobian reuse knobs
+        o.max_jac_age = alg.max_jac_age
+        o.jac_reuse_gamma_tol = alg.jac_reuse_gamma_tol
     o.reltol, o.abstol = reltol, abstol
     o.dt = dt or 0.0
     o.dtmax = dtmax or 0.0
@@ -397,7 +415,7 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
     tspans = np.ascontiguousarray(tspans, dtype=np.float64)
     n, N = u0s.shape
     sv = resolve_saveat(saveat, tspans, save_start, save_end, save_everystep, max_step_saves)
-    o = _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax, callback, tstops)
+    o = _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax, callback, tstops, alg)
     d = _lib.ProblemDesc(model, alg.alg_id, n, ps.shape[0], ens.prec_id(), 0)
     cap = sv.cap + (2 * callback.max_events if callback is not None else 0)
     if dense and not sv.everystep:
@@ -445,10 +463,11 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
     return out
 
 
-def dense_eval(res, tq, device=None):
+def dense_eval(res, tq, device=None, deriv=0):
     """sol_j(t) of a dense solve (solve_arrays(..., dense=True)) for every
     trajectory j at the query times tq, shared (nq,) or per trajectory (nq, N),
-    evaluated on the GPU in FP64 (ode_dense_eval).  Returns (nq, n, N)."""
+    evaluated on the GPU in FP64 (ode_dense_eval_deriv).  deriv=1 gives
+    sol_j(t, Val{1}), the derivative of the interpolant.  Returns (nq, n, N)."""
     info = res.get("dense")
     if not info:
         raise ValueError("not a dense solve: pass dense=True")
@@ -465,8 +484,9 @@ def dense_eval(res, tq, device=None):
     d = _lib.ProblemDesc(info["model"], info["alg"], n, ps.shape[0], 0, 0)
     h = get_handle(info["device"] if device is None else device)
     dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
-    _lib.check(L.ode_dense_eval(h, C.byref(d), N, dp(ps), dp(t), dp(u), dp(k),
-                                ns.ctypes.data_as(C.POINTER(C.c_int32)), cap, nq, dp(tq), int(per), dp(out)), h)
+    _lib.check(L.ode_dense_eval_deriv(h, C.byref(d), N, dp(ps), dp(t), dp(u), dp(k),
+                                      ns.ctypes.data_as(C.POINTER(C.c_int32)), cap, nq, dp(tq), int(per), int(deriv),
+                                      dp(out)), h)
     return out
 
 

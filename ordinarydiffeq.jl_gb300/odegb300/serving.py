@@ -80,7 +80,7 @@ class Server:
         prec = pick_precision(precision, reltol, name)
         ens = EnsembleGB300(precision=prec, ir_sweeps=ir_sweeps if prec == "mixed" else -1)
         sv = saveat if hasattr(saveat, "nsave") else resolve_saveat(saveat, tspans)
-        o = _options(reltol, abstol, None, None, None, 1000000, sv, ens, None, None, tstops=tstops)
+        o = _options(reltol, abstol, None, None, None, 1000000, sv, ens, None, None, tstops=tstops, alg=alg)
         d = _lib.ProblemDesc(model, alg.alg_id, n, ps.shape[0], ens.prec_id(), 0)
         cap = sv.cap
         out = {"t": np.empty((cap, N)), "u": np.empty((cap, n, N)), "nsaved": np.empty(N, dtype=np.int32),

@@ -43,7 +43,7 @@ def test_struct_layouts_match_the_bindings():
 
 def test_abi_version_and_defaults_without_gpu():
     L = _lib.load()
-    assert L.ode_abi_version() == 4
+    assert L.ode_abi_version() == 5
     # dense vectors per step (Tsit5 k1..k7, Vern7 k1 and k4..k9, Rodas5P dense k1..k3)
     assert [L.ode_dense_nk(a) for a in (0, 1, 2)] == [7, 7, 3] and L.ode_dense_nk(9) == -1
     o = _lib.Options()
@@ -51,6 +51,7 @@ def test_abi_version_and_defaults_without_gpu():
     assert o.reltol == 1e-3 and o.abstol == 1e-6 and o.maxiters == 1000000
     assert o.save_start == 1 and o.save_end == 1 and o.save_end_user == -1
     assert o.ntstops == 0 and not o.tstops and o.interp_points == 10
+    assert o.max_jac_age == 1 and o.jac_reuse_gamma_tol == 0.03   # Rosenbrock23's defaults
     assert L.ode_status_string(-4).decode().startswith("unsupported")
 
 
@@ -84,6 +85,23 @@ def test_noalloc_applies_the_shared_problem_checks():
     d = _lib.ProblemDesc(_lib.MODEL_LORENZ, _lib.ODE_TSIT5, 4, 3, _lib.PREC_FP64, 0)   # Lorenz has 3 states
     assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == -1
     assert b"3 states" in L.ode_last_error(None)
+
+
+def test_jacobian_reuse_options_are_checked_on_the_host():
+    L = _lib.load()
+    o = _lib.Options()
+    L.ode_options_default(C.byref(o))
+    d = _lib.ProblemDesc(_lib.MODEL_LORENZ, _lib.ODE_ROSENBROCK23, 3, 3, _lib.PREC_FP64, 0)
+    o.max_jac_age = -1
+    assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == -1
+    o.max_jac_age = 20
+    o.jac_reuse_gamma_tol = float("nan")
+    assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == -1
+    # the kept J lives in registers beside W: not for the shared-memory LU (16-64 states)
+    o.jac_reuse_gamma_tol = 0.03
+    d = _lib.ProblemDesc(_lib.MODEL_BRUSSELATOR_1D, _lib.ODE_ROSENBROCK23, 16, 3, _lib.PREC_FP64, 0)
+    assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == -4
+    assert b"max_jac_age" in L.ode_last_error(None)
 
 
 def test_variant_registry_covers_the_workloads():

@@ -175,3 +175,53 @@ def test_page_locked_dense_eval_output_is_identical():
     _lib.check(L.ode_dense_eval(h, C.byref(d), N, ptr(h_p), ptr(h_t), ptr(h_u), ptr(h_k), ptr(h_ns, C.c_int32),
                                 g["t"].shape[0], tq.size, ptr(h_tq), 0, ptr(h_out)), h)
     assert np.array_equal(h_out.numpy(), staged)
+
+
+@pytest.mark.parametrize("model,alg,rt,at", [("lorenz", "tsit5", 1e-8, 1e-8), ("lorenz", "vern7", 1e-8, 1e-8),
+                                             ("robertson", "rodas5p", 1e-6, 1e-10),
+                                             ("lorenz", "rosenbrock23", 1e-6, 1e-8)])
+def test_dense_derivative_matches_oracle(model, alg, rt, at):
+    # sol(t, Val{1}) on the device (ode_dense_eval_deriv) against the oracle's, and
+    # against the derivative of the device's own interpolant (a polynomial in theta on
+    # each step, fitted from its values inside the step)
+    N = 32
+    u0, p, ts = inputs(model, N, 7)
+    n = u0.shape[0]
+    g = gpu(model, alg, u0, p, ts, None, rt, at, save_everystep=True, max_step_saves=4096, dense=True)
+    rng = np.random.default_rng(3)
+    tq = ts[0] + (ts[1] - ts[0]) * rng.uniform(0.0, 1.0, (16, N))
+    der = dense_eval(g, tq, deriv=1)
+    deg = {"tsit5": 4, "vern7": 7, "rodas5p": 4, "rosenbrock23": 2}[alg]
+    for j in range(N):
+        o = O.solve(ALG[alg][1], MODEL[model], u0[:, j], p[:, j], ts[:, j], dense=True, reltol=rt, abstol=at,
+                    saveat_given=False, save_everystep=True, max_step_saves=4096, save_start=True, save_end=True)
+        ref = o["dense"](tq[:, j], deriv=1)
+        scale = np.abs(ref).max(axis=0) + 1e-300
+        assert np.all(np.abs(der[:, :, j] - ref) <= 1e-4 * scale + 10 * at), j
+        ns = int(g["nsaved"][j])
+        tj = g["t"][:ns, j]
+        for r in range(0, 16, 5):
+            ip = max(1, int(np.searchsorted(tj, tq[r, j], side="left")))
+            a, b = tj[ip - 1], tj[ip]
+            x = a + (b - a) * np.linspace(0.1, 1.0, 3 * deg)
+            vals = dense_eval(g, np.tile(x[:, None], (1, N)))[:, :, j]
+            th = (tq[r, j] - a) / (b - a)
+            for i in range(n):
+                c = np.polyfit((x - a) / (b - a), vals[:, i], deg)
+                want = np.polyval(np.polyder(c), th) / (b - a)
+                assert der[r, i, j] == pytest.approx(want, rel=1e-7, abs=1e-9 * scale[i] + 1e-12), (j, r, i)
+
+
+def test_dense_derivative_order_checks():
+    from odegb300 import _lib
+    from odegb300.ensemble import get_handle
+    import ctypes as C
+    L = _lib.load()
+    d = _lib.ProblemDesc(_lib.MODEL_LORENZ, _lib.ODE_TSIT5, 3, 3, _lib.PREC_FP64, 0)
+    h = get_handle(0)
+    x = np.zeros(8)
+    dp = x.ctypes.data_as(C.POINTER(C.c_double))
+    ns = np.ones(1, dtype=np.int32)
+    ip = ns.ctypes.data_as(C.POINTER(C.c_int32))
+    assert L.ode_dense_eval_deriv(h, C.byref(d), 1, dp, dp, dp, dp, ip, 1, 1, dp, 0, 2, dp) == -4
+    assert L.ode_dense_eval_deriv(h, C.byref(d), 1, dp, dp, dp, dp, ip, 1, 1, dp, 0, -1, dp) == -1

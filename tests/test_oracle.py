@@ -734,3 +734,78 @@ def test_dense_output_with_events_follows_the_bounces(alg):
         hit = np.nonzero(np.abs(t - c) < 1e-8)[0]
         assert len(hit) == 2
         assert d([t[hit[0]]])[0][1] == pytest.approx(r["u"][hit[0]][1], rel=1e-12)
+
+
+# Rosenbrock23 as a W-method (Rosenbrock23(max_jac_age = ...), _rosenbrock_jac_reuse_decision,
+# lib/OrdinaryDiffEqDifferentiation/src/derivative_utils.jl:46-170): J is kept across
+# accepted steps while dtgamma stays within jac_reuse_gamma_tol of the J's and the age
+# is below max_jac_age; W and its LU are formed on every attempt.
+def test_jacobian_reuse_on_a_linear_problem_changes_nothing_but_the_count():
+    # J is constant: the kept J is the fresh one, so the steps are identical
+    kw = dict(saveat=[], saveat_given=False, save_everystep=True, max_step_saves=4096, save_start=True,
+              reltol=1e-5, abstol=1e-8)
+    a = O.solve(O.ROSENBROCK23, O.LINEAR, [1.0, 0.5], [-1.0], (0.0, 10.0), **kw)
+    b = O.solve(O.ROSENBROCK23, O.LINEAR, [1.0, 0.5], [-1.0], (0.0, 10.0), max_jac_age=20, **kw)
+    assert np.array_equal(a["t"], b["t"]) and np.array_equal(a["u"], b["u"])
+    assert a["stats"]["njacs"] == a["stats"]["naccept"] + a["stats"]["nreject"]
+    assert b["stats"]["njacs"] < a["stats"]["njacs"] // 3
+    # a wider gamma window keeps J longer
+    c = O.solve(O.ROSENBROCK23, O.LINEAR, [1.0, 0.5], [-1.0], (0.0, 10.0), max_jac_age=20,
+                jac_reuse_gamma_tol=0.2, **kw)
+    assert c["stats"]["njacs"] < b["stats"]["njacs"]
+
+
+def test_jacobian_reuse_keeps_the_accuracy_and_composites_ignore_it():
+    sv = np.linspace(1.0, 20.0, 20)
+    p = [0.3, 2.0, 0.0, 1.5, 1.7]
+    ex = forced_exact(sv, 0.4, -0.2, 0.3, 2.0, 1.5, 1.7)
+    errs = []
+    for age in (1, 20):
+        r = O.solve(O.ROSENBROCK23, O.FORCED_DUFFING, [0.4, -0.2], p, (0.0, 20.0), saveat=sv, reltol=1e-6,
+                    abstol=1e-6, max_jac_age=age)
+        assert r["retcode"] == 1
+        errs.append(np.abs(r["u"] - ex).max())
+        if age == 20:
+            assert r["stats"]["njacs"] < r["stats"]["naccept"]
+    assert errs[1] < 3 * errs[0] + 1e-6
+    kw = dict(saveat=sv, reltol=1e-6, abstol=1e-6)
+    a = O.solve(O.AUTOTSIT5_ROSENBROCK23, O.VANDERPOL, [2.0, 0.0], [100.0], (0.0, 5.0), **kw)
+    b = O.solve(O.AUTOTSIT5_ROSENBROCK23, O.VANDERPOL, [2.0, 0.0], [100.0], (0.0, 5.0), max_jac_age=20, **kw)
+    assert np.array_equal(a["u"], b["u"]) and a["stats"] == b["stats"]
+
+
+# test/Regression_I/ode_dense_tests.jl:47-106 (test_diff1): sol(t, Val{1}) is the derivative
+# of the interpolant sol(t, Val{0}) (the reference takes it by AD, left-continuously, at
+# 0:1/4:1).  Each interpolant is a polynomial in theta of known degree on its step, so
+# the derivative is checked against the exact derivative of a polynomial fit of the
+# values inside the step.
+@pytest.mark.parametrize("alg,deg", [(O.TSIT5, 4), (O.VERN7, 7), (O.RODAS5P, 4), (O.ROSENBROCK23, 2)])
+def test_dense_derivative_is_the_interpolants_derivative(alg, deg):
+    for u0 in ([0.5], [0.5, 0.25]):
+        r = O.solve(alg, O.LINEAR, u0, [1.01], (0.0, 1.0), saveat=[], saveat_given=False, dt=0.25, dense=True,
+                    save_start=True)
+        d, ts = r["dense"], r["t"]
+        for tp in np.linspace(0.0, 1.0, 5):
+            ip = max(1, int(np.searchsorted(ts, tp, side="left")))   # left continuity
+            a, b = ts[ip - 1], ts[ip]
+            x = a + (b - a) * np.linspace(0.1, 1.0, 3 * deg)
+            vals = d(x)
+            th = (tp - a) / (b - a)
+            got = d([tp], deriv=1)[0]
+            for i in range(len(u0)):
+                c = np.polyfit((x - a) / (b - a), vals[:, i], deg)
+                want = np.polyval(np.polyder(c), th) / (b - a)
+                assert got[i] == pytest.approx(want, rel=1e-9, abs=1e-12), (tp, i)
+
+
+def test_dense_derivative_follows_the_right_hand_side():
+    # on Lorenz the interpolant's derivative is f(sol(t)) to within the tolerance
+    p = [10.0, 28.0, 8 / 3]
+    for alg in (O.TSIT5, O.VERN7, O.RODAS5P):
+        r = O.solve(alg, O.LORENZ, [1.0, 0.0, 0.0], p, (0.0, 1.0), saveat=[], saveat_given=False, dense=True,
+                    save_start=True, reltol=1e-10, abstol=1e-10)
+        d = r["dense"]
+        tq = np.linspace(0.01, 0.99, 37)
+        der, val = d(tq, deriv=1), d(tq)
+        f = np.array([O.rhs(O.LORENZ, v, p, 0.0) for v in val])
+        assert np.abs(der - f).max() < 1e-5 * np.abs(f).max()
