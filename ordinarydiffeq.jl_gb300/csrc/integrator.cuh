@@ -424,6 +424,11 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
     double dtpropose = dt;
     CT EEst = CT(1), q11 = CT(1), errold = qoldinit;
     CT bank_errold = qoldinit, bank_q11 = CT(1);   // composite: the other method's controller state
+    // FP64 form: ln(errold) kept from the step that set errold, so errold^beta2 is one
+    // exp series instead of a ctrl_pow (the same value: ctrl_pow(x, y) is
+    // series_exp(y * series_ln(x)) for finite positive x); NaN when not kept
+    double ln_qoldinit = 0.0, ln_errold = 0.0, bank_ln_errold = 0.0;
+    if constexpr (sizeof(CT) == 8) ln_errold = bank_ln_errold = ln_qoldinit = series_ln((double)qoldinit);
     bool do_error_check = true;
     long long iter = 0, success_iter = 0;
     bool accept = false, next_tstop = false;
@@ -749,6 +754,9 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
                 q11 = bank_q11;
                 bank_errold = e_old;
                 bank_q11 = q_old;
+                const double l_old = ln_errold;
+                ln_errold = bank_ln_errold;
+                bank_ln_errold = l_old;
                 using NSA = typename Alg::NonStiff;
                 using SA = typename Alg::Stiff;
                 const Ctrl K2 = cur == 0 ? make_ctrl<NSA::ORDER, NSA::IMPLICIT>(a) : make_ctrl<SA::ORDER, SA::IMPLICIT>(a);
@@ -801,11 +809,21 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
         const double ttmp = t + dt;
         const CT inv_qmaxc = success_iter == 0 ? inv_qmax_first : inv_qmax;
         CT q;
+        double ln_eest = dnan();   // FP64 form: ln(EEst) of this attempt when EEst is finite and positive
         if (EEst == CT(0)) {
             q = inv_qmaxc;
         } else {
-            const CT qq = Ctl<R>::pw(EEst, beta1);
-            q = qq / Ctl<R>::pw(errold, beta2);
+            CT qq, den;
+            if constexpr (sizeof(CT) == 8) {
+                const bool fin = EEst > 0.0 && EEst < __longlong_as_double(0x7ff0000000000000LL);
+                if (fin) ln_eest = series_ln(EEst);
+                qq = fin ? series_exp(beta1 * ln_eest) : Ctl<R>::pw(EEst, beta1);
+                den = ln_errold == ln_errold ? series_exp(beta2 * ln_errold) : Ctl<R>::pw(errold, beta2);
+            } else {
+                qq = Ctl<R>::pw(EEst, beta1);
+                den = Ctl<R>::pw(errold, beta2);
+            }
+            q = qq / den;
             q11 = qq;
             const CT x = q / gam;
             q = x > qmin_inv ? qmin_inv : (x < inv_qmaxc ? inv_qmaxc : x);
@@ -823,6 +841,7 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             }
             if (CT(1) <= q && q <= qsteady_max) q = CT(1);
             errold = (EEst != EEst) ? EEst : (EEst > qoldinit ? EEst : qoldinit);
+            if constexpr (sizeof(CT) == 8) ln_errold = (EEst != EEst) ? dnan() : (EEst > qoldinit ? ln_eest : ln_qoldinit);
             const double dtnew = Ctl<R>::scale_dt(dt, q);
             const double dtp = pmin(pabs(dtmax), pabs(dtnew));
             dtpropose = pmax(pabs(dtp), pabs(pmax(peps(t), a.dtmin)));
