@@ -23,7 +23,8 @@
  *   tspan[j], tspan[N+j] t0 and tf of trajectory j          (2 x N; tf < t0 integrates backward)
  *   saveat[s] shared, or saveat[s*N + j] per trajectory     (nsave or nsave x N; ascending in s
  *                                                           whatever the direction)
- *   t_out[s*N + j], u_out[(s*n_states + i)*N + j]           (cap x N, cap x n_states x N)
+ *   t_out[s*N + j], u_out[(s*n_states + i)*N + j]         (cap x N, cap x n_states x N; with save_idxs
+ *                                                           nsave_idxs rows replace the n_states)
  * with cap = nsave + 2 save slots per trajectory (start and end saves), or
  * max_step_saves + 2 with save_everystep, plus 2 * max_events with a callback.
  */
@@ -190,6 +191,13 @@ typedef struct {
     int32_t reserved2;
     double jac_reuse_gamma_tol; /* reuse only while |dtgamma / dtgamma_J - 1| <= this (reference default
                                    0.03; < 0 means the default) */
+    int32_t nsave_idxs;         /* > 0: the reference's save_idxs: only these states are saved, u_out holds */
+    int32_t reserved3;          /* nsave_idxs rows per save (u_out[(s*nsave_idxs + r)*N + j] = state   */
+    const int32_t* save_idxs;   /* save_idxs[r] of trajectory j), in the given order, repeats allowed.
+                                   0-based.  Host memory for the host entry points (checked against
+                                   n_states), device memory for ode_solve_ensemble_device and
+                                   ode_solve_ensemble_noalloc (an index outside the trajectory's states
+                                   leaves its row unwritten).  Not with dense output */
 } ode_options;
 
 /* Fill o with the reference's defaults. */

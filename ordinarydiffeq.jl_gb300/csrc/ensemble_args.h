@@ -29,7 +29,9 @@ struct EnsembleArgs {
     int saveat_per_traj;
     int nsave_cap;          // save slots per trajectory in t_out/u_out
     double* t_out;
-    double* u_out;
+    double* u_out;          // u_out[(s*nmax + i)*N + j], or [(s*nsave_rows + r)*N + j] with save_idxs
+    const int32_t* save_idxs;  // the states saved, one row each (nullptr: every state)
+    int nsave_rows;
     int32_t* nsaved;
     int32_t* retcode;
     OdeStatsDev* stats;

@@ -364,9 +364,20 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
         const int slot = nsaved < a.nsave_cap ? nsaved : ((a.save_everystep || a.callback) ? a.nsave_cap - 1 : -1);
         if (slot >= 0) {
             if (g.lane == 0 && a.t_out) a.t_out[(size_t)slot * N + j] = TM(ts);
+            if (a.save_idxs) {   // save_idxs: row r holds state save_idxs[r], written by its lane
+#pragma unroll 1
+                for (int r = 0; r < a.nsave_rows; ++r) {
+                    const int si = a.save_idxs[r];
 #pragma unroll
-            for (int c = 0; c < C; ++c)
-                a.u_out[((size_t)slot * a.nmax + g.lane * C + c) * N + j] = Acc<R>::join(v[c], vlo[c]);
+                    for (int c = 0; c < C; ++c)
+                        if (si == g.lane * C + c)
+                            a.u_out[((size_t)slot * a.nsave_rows + r) * N + j] = Acc<R>::join(v[c], vlo[c]);
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < C; ++c)
+                    a.u_out[((size_t)slot * a.nmax + g.lane * C + c) * N + j] = Acc<R>::join(v[c], vlo[c]);
+            }
         }
         nsaved++;
         last_saved_t = ts;

@@ -170,6 +170,7 @@ struct ode_handle {
     DevBuf b_u0, b_p, b_tspan, b_saveat, b_t, b_u, b_ns, b_rc, b_st, b_npt;
     DevBuf b_k, b_tq, b_out;                 // dense output and its evaluation
     DevBuf b_tstops;                         // the host API's tstops, sorted
+    DevBuf b_idx;                            // the host API's save_idxs
     // copy streams and events of the chunked host-API pipeline
     cudaStream_t copy_in = nullptr, copy_out = nullptr;
     cudaEvent_t pipe_in[4] = {}, pipe_done[4] = {};
@@ -265,6 +266,8 @@ int check_problem(const ode_problem_desc* d, const ode_options* o, int64_t N, co
     if (o->ntstops < 0 || (o->ntstops > 0 && !o->tstops))
         return bad(ODE_E_INVALID, "ntstops < 0, or tstops is null");
     if (o->max_jac_age < 0) return bad(ODE_E_INVALID, "max_jac_age must be >= 0");
+    if (o->nsave_idxs < 0 || (o->nsave_idxs > 0 && !o->save_idxs))
+        return bad(ODE_E_INVALID, "nsave_idxs < 0, or save_idxs is null");
     // the kept J lives beside W in registers; the shared-memory LU (16-64 states)
     // forms W in place of J
     if (d->alg_id == ODE_ROSENBROCK23 && o->max_jac_age > 1 && d->n_states > 8)
@@ -289,6 +292,19 @@ int check_host_tstops(ode_handle* h, const ode_options* o) {
     return ODE_OK;
 }
 
+// ... and their save_idxs in host memory: each a state of the problem.
+int check_host_save_idxs(ode_handle* h, const ode_problem_desc* d, const ode_options* o) {
+    for (int32_t r = 0; r < o->nsave_idxs; ++r)
+        if (o->save_idxs[r] < 0 || o->save_idxs[r] >= d->n_states)
+            return fail(h, ODE_E_INVALID, "save_idxs entry outside [0, n_states)");
+    return ODE_OK;
+}
+
+// Output rows per save: the save_idxs, else every state.
+size_t out_rows(const ode_problem_desc* d, const ode_options* o) {
+    return o->nsave_idxs > 0 ? (size_t)o->nsave_idxs : (size_t)d->n_states;
+}
+
 std::vector<double> sorted_tstops(const ode_options* o) {
     std::vector<double> v;
     if (o->ntstops > 0) v.assign(o->tstops, o->tstops + o->ntstops);
@@ -304,12 +320,18 @@ int stage_tstops(ode_handle* h, const ode_options* o, cudaStream_t s, ode_option
     ot->tstops = nullptr;
     const std::vector<double> v = sorted_tstops(o);
     ot->ntstops = (int32_t)v.size();
-    if (v.empty()) return ODE_OK;
-    int rc = grow(h, h->b_tstops, v.size() * 8);
-    if (rc) return rc;
-    CUDA_TRY(h, cudaMemcpyAsync(h->b_tstops.p, v.data(), v.size() * 8, cudaMemcpyHostToDevice, s));
+    int rc = ODE_OK;
+    if (!v.empty()) {
+        if ((rc = grow(h, h->b_tstops, v.size() * 8))) return rc;
+        CUDA_TRY(h, cudaMemcpyAsync(h->b_tstops.p, v.data(), v.size() * 8, cudaMemcpyHostToDevice, s));
+        ot->tstops = (const double*)h->b_tstops.p;
+    }
+    if (o->nsave_idxs > 0) {   // the save_idxs too, as given
+        if ((rc = grow(h, h->b_idx, (size_t)o->nsave_idxs * 4))) return rc;
+        CUDA_TRY(h, cudaMemcpyAsync(h->b_idx.p, o->save_idxs, (size_t)o->nsave_idxs * 4, cudaMemcpyHostToDevice, s));
+        ot->save_idxs = (const int32_t*)h->b_idx.p;
+    }
     CUDA_TRY(h, cudaStreamSynchronize(s));
-    ot->tstops = (const double*)h->b_tstops.p;
     return ODE_OK;
 }
 
@@ -342,6 +364,8 @@ EnsembleArgs make_args(ode_handle* h, const ode_problem_desc* d, const ode_optio
     a.ntstops = o->ntstops > 0 ? o->ntstops : 0;
     a.max_jac_age = o->max_jac_age;
     a.jac_reuse_gamma_tol = o->jac_reuse_gamma_tol < 0 ? 0.03 : o->jac_reuse_gamma_tol;
+    a.save_idxs = o->nsave_idxs > 0 ? o->save_idxs : nullptr;   // device memory at this point
+    a.nsave_rows = o->nsave_idxs > 0 ? o->nsave_idxs : 0;
     a.t_out = t_out;
     a.u_out = u_out;
     a.nsaved = nsaved;
@@ -796,7 +820,7 @@ int solve_chunked(ode_handle* h, const ode_problem_desc* d, const ode_options* o
             CUDA_TRY(h, cudaEventCreateWithFlags(&h->pipe_done[k], cudaEventDisableTiming));
         }
     }
-    const size_t n = (size_t)d->n_states, np = (size_t)d->n_params, cap = save_cap(o);
+    const size_t n = (size_t)d->n_states, np = (size_t)d->n_params, cap = save_cap(o), rows = out_rows(d, o);
     const size_t pitch = (size_t)N * 8;
     const bool per_traj = o->saveat_per_traj && o->nsave > 0;
     cudaStream_t s = h->main.stream, ci = h->copy_in, co = h->copy_out;
@@ -836,7 +860,7 @@ int solve_chunked(ode_handle* h, const ode_problem_desc* d, const ode_options* o
         CUDA_TRY(h, cudaEventRecord(h->pipe_done[k], s));
         CUDA_TRY(h, cudaStreamWaitEvent(co, h->pipe_done[k], 0));
         if (t_out) CUDA_TRY(h, cudaMemcpy2DAsync(t_out + a0, pitch, dt + a0, pitch, w, cap, cudaMemcpyDeviceToHost, co));
-        CUDA_TRY(h, cudaMemcpy2DAsync(u_out + a0, pitch, du + a0, pitch, w, cap * n, cudaMemcpyDeviceToHost, co));
+        CUDA_TRY(h, cudaMemcpy2DAsync(u_out + a0, pitch, du + a0, pitch, w, cap * rows, cudaMemcpyDeviceToHost, co));
         CUDA_TRY(h, cudaMemcpyAsync(nsaved + a0, dns + a0, (size_t)cnt * 4, cudaMemcpyDeviceToHost, co));
         CUDA_TRY(h, cudaMemcpyAsync(retcode + a0, drc + a0, (size_t)cnt * 4, cudaMemcpyDeviceToHost, co));
         if (stats)
@@ -921,11 +945,11 @@ int solve_host(ode_handle* h, const ode_problem_desc* d, const ode_options* o, i
             return ODE_OK;
         }
     }
-    const size_t n = (size_t)d->n_states, np = (size_t)d->n_params, cap = save_cap(o);
+    const size_t n = (size_t)d->n_states, np = (size_t)d->n_params, cap = save_cap(o), rows = out_rows(d, o);
     const size_t nsv = (size_t)o->nsave * (o->saveat_per_traj ? (size_t)N : 1);
     if ((rc = grow(h, h->b_u0, n * N * 8)) || (rc = grow(h, h->b_p, np * N * 8)) ||
         (rc = grow(h, h->b_tspan, 2 * N * 8)) || (rc = grow(h, h->b_saveat, nsv * 8)) ||
-        (rc = grow(h, h->b_t, cap * N * 8)) || (rc = grow(h, h->b_u, cap * n * N * 8)) ||
+        (rc = grow(h, h->b_t, cap * N * 8)) || (rc = grow(h, h->b_u, cap * rows * N * 8)) ||
         (rc = grow(h, h->b_ns, N * 4)) || (rc = grow(h, h->b_rc, N * 4)) ||
         (rc = grow(h, h->b_st, N * sizeof(ode_stats))) || (npt && (rc = grow(h, h->b_npt, N * 4))))
         return rc;
@@ -948,7 +972,7 @@ int solve_host(ode_handle* h, const ode_problem_desc* d, const ode_options* o, i
         return rc;
     }
     if (t_out) CUDA_TRY(h, cudaMemcpyAsync(t_out, h->b_t.p, cap * N * 8, cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(h, cudaMemcpyAsync(u_out, h->b_u.p, cap * n * N * 8, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(h, cudaMemcpyAsync(u_out, h->b_u.p, cap * rows * N * 8, cudaMemcpyDeviceToHost, s));
     if (k_out) CUDA_TRY(h, cudaMemcpyAsync(k_out, h->b_k.p, kbytes, cudaMemcpyDeviceToHost, s));
     CUDA_TRY(h, cudaMemcpyAsync(nsaved, h->b_ns.p, N * 4, cudaMemcpyDeviceToHost, s));
     CUDA_TRY(h, cudaMemcpyAsync(retcode, h->b_rc.p, N * 4, cudaMemcpyDeviceToHost, s));
@@ -975,6 +999,7 @@ struct Request {
     int64_t N = 0;
     std::vector<double> u0, p, tspan, saveat, tstops;   // tstops sorted; o.tstops is unused
     std::vector<int32_t> npt;
+    std::vector<int32_t> save_idxs;                     // o.save_idxs is unused
     double* t_out = nullptr;
     double* u_out = nullptr;
     int32_t* nsaved = nullptr;
@@ -1018,7 +1043,7 @@ bool mergeable(const Request& a, const Request& b) {
     x.reltol = y.reltol = 0.0;
     x.abstol = y.abstol = 0.0;
     if (std::memcmp(&x, &y, sizeof(x)) != 0) return false;
-    return a.saveat == b.saveat && a.tstops == b.tstops;
+    return a.saveat == b.saveat && a.tstops == b.tstops && a.save_idxs == b.save_idxs;
 }
 
 // Byte offsets of one batch's block: inputs first, then outputs, so each
@@ -1026,10 +1051,11 @@ bool mergeable(const Request& a, const Request& b) {
 // device block share this layout.  Merged batches carry per-trajectory
 // tolerances.
 struct Layout {
-    size_t u0, p, ts, rtol, atol, sv, tst, npt, in_end, t, u, ns, rc, st, total;
+    size_t u0, p, ts, rtol, atol, sv, tst, idx, npt, in_end, t, u, ns, rc, st, total;
 };
 Layout layout(const Request& h, int64_t Ntot, bool per_traj_tol) {
     const size_t n = (size_t)h.d.n_states, np = (size_t)h.d.n_params, N = (size_t)Ntot, cap = save_cap(&h.o);
+    const size_t rows = out_rows(&h.d, &h.o);
     Layout L;
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off += align256(bytes); return o; };
@@ -1040,10 +1066,11 @@ Layout layout(const Request& h, int64_t Ntot, bool per_traj_tol) {
     L.atol = per_traj_tol ? take(N * 8) : (size_t)-1;
     L.sv = take(std::max<size_t>(h.saveat.size(), 1) * 8);
     L.tst = take(std::max<size_t>(h.tstops.size(), 1) * 8);
+    L.idx = take(std::max<size_t>(h.save_idxs.size(), 1) * 4);
     L.npt = h.npt.empty() ? (size_t)-1 : take(N * 4);
     L.in_end = off;
     L.t = take(cap * N * 8);
-    L.u = take(cap * n * N * 8);
+    L.u = take(cap * rows * N * 8);
     L.ns = take(N * 4);
     L.rc = take(N * 4);
     L.st = take(N * sizeof(ode_stats));
@@ -1090,6 +1117,7 @@ int admit(ode_handle* h, Batch& b, int k) {
     }
     if (!r0.saveat.empty()) std::memcpy(hs + L.sv, r0.saveat.data(), r0.saveat.size() * 8);
     if (!r0.tstops.empty()) std::memcpy(hs + L.tst, r0.tstops.data(), r0.tstops.size() * 8);
+    if (!r0.save_idxs.empty()) std::memcpy(hs + L.idx, r0.save_idxs.data(), r0.save_idxs.size() * 4);
     if (!r0.npt.empty()) std::memcpy(hs + L.npt, r0.npt.data(), N * 4);
     CUDA_TRY(h, cudaMallocAsync(&b.dmem, L.total, s));
     char* base = (char*)b.dmem;
@@ -1097,6 +1125,7 @@ int admit(ode_handle* h, Batch& b, int k) {
     ode_options o = r0.o;
     o.ntstops = (int32_t)r0.tstops.size();
     o.tstops = r0.tstops.empty() ? nullptr : (const double*)(base + L.tst);
+    o.save_idxs = r0.save_idxs.empty() ? nullptr : (const int32_t*)(base + L.idx);
     const bool pt = b.reqs.size() > 1;
     int rc = run_ensemble(h, c, &r0.d, &o, b.N, r0.npt.empty() ? nullptr : (const int32_t*)(base + L.npt),
                           (const double*)(base + L.u0), (const double*)(base + L.p), (const double*)(base + L.ts),
@@ -1115,7 +1144,7 @@ int admit(ode_handle* h, Batch& b, int k) {
 // Outputs from the slot's staging into each request's buffers.
 void finish(ode_handle* h, Batch& b) {
     const Request& r0 = b.head();
-    const size_t n = (size_t)r0.d.n_states, N = (size_t)b.N, cap = save_cap(&r0.o);
+    const size_t rows = out_rows(&r0.d, &r0.o), N = (size_t)b.N, cap = save_cap(&r0.o);
     if (b.status == ODE_OK && b.slot >= 0 && h->slot_pinned[b.slot]) {
         const Layout L = layout(b);
         const char* hs = (const char*)h->slot_pinned[b.slot];
@@ -1124,7 +1153,7 @@ void finish(ode_handle* h, Batch& b) {
             const size_t off = (size_t)b.offset[q], m = (size_t)r.N;
             if (r.t_out)
                 for (size_t i = 0; i < cap; ++i) std::memcpy(r.t_out + i * m, hs + L.t + (i * N + off) * 8, m * 8);
-            for (size_t i = 0; i < cap * n; ++i) std::memcpy(r.u_out + i * m, hs + L.u + (i * N + off) * 8, m * 8);
+            for (size_t i = 0; i < cap * rows; ++i) std::memcpy(r.u_out + i * m, hs + L.u + (i * N + off) * 8, m * 8);
             std::memcpy(r.nsaved, hs + L.ns + off * 4, m * 4);
             std::memcpy(r.retcode, hs + L.rc + off * 4, m * 4);
             if (r.stats) std::memcpy(r.stats, hs + L.st + off * sizeof(ode_stats), m * sizeof(ode_stats));
@@ -1357,7 +1386,7 @@ void ode_destroy(ode_handle* h) {
     cudaSetDevice(h->device);
     cudaDeviceSynchronize();
     for (auto& r : h->running) finish(h, *r);
-    for (DevBuf* b : {&h->b_u0, &h->b_p, &h->b_tspan, &h->b_saveat, &h->b_tstops, &h->b_t, &h->b_u, &h->b_ns, &h->b_rc,
+    for (DevBuf* b : {&h->b_u0, &h->b_p, &h->b_tspan, &h->b_saveat, &h->b_tstops, &h->b_idx, &h->b_t, &h->b_u, &h->b_ns, &h->b_rc,
                       &h->b_st, &h->b_npt})
         if (b->p) cudaFree(b->p);
     ctx_free(h->main);
@@ -1403,7 +1432,7 @@ int ode_solve_ensemble(ode_handle* h, const ode_problem_desc* d, const ode_optio
         return fail(h, ODE_E_INVALID, "null input or output buffer");
     if (o->nsave > 0 && !saveat) return fail(h, ODE_E_INVALID, "nsave > 0 but saveat is null");
     if ((rc = check_sizes(h, d, npt, N))) return rc;
-    if ((rc = check_host_tstops(h, o))) return rc;
+    if ((rc = check_host_tstops(h, o)) || (rc = check_host_save_idxs(h, d, o))) return rc;
     return solve_host(h, d, o, N, npt, u0, p, tspan, saveat, t_out, u_out, nullptr, nsaved, retcode, stats);
 }
 
@@ -1419,6 +1448,7 @@ int ode_solve_ensemble_dense(ode_handle* h, const ode_problem_desc* d, const ode
     if (!o->save_everystep || o->nsave != 0)
         return fail(h, ODE_E_INVALID, "dense output saves every step: save_everystep = 1 and nsave = 0");
     if (kDenseVectors[d->alg_id] == 0) return fail(h, ODE_E_UNSUPPORTED, "no dense output for this method");
+    if (o->nsave_idxs > 0) return fail(h, ODE_E_UNSUPPORTED, "save_idxs with dense output is not supported");
     if (N > 0 && (!u0 || !p || !tspan || !u_out || !k_out || !nsaved || !retcode))
         return fail(h, ODE_E_INVALID, "null input or output buffer");
     if ((rc = check_host_tstops(h, o))) return rc;
@@ -1515,13 +1545,15 @@ int ode_submit(ode_handle* h, const ode_problem_desc* d, const ode_options* o, i
         return fail(h, ODE_E_INVALID, "null input or output buffer");
     if (o->nsave > 0 && !saveat) return fail(h, ODE_E_INVALID, "nsave > 0 but saveat is null");
     if ((rc = check_sizes(h, d, npt, N))) return rc;
-    if ((rc = check_host_tstops(h, o))) return rc;
+    if ((rc = check_host_tstops(h, o)) || (rc = check_host_save_idxs(h, d, o))) return rc;
     auto r = std::make_shared<Request>();
     r->d = *d;
     r->o = *o;
     r->tstops = sorted_tstops(o);
     r->o.tstops = nullptr;
     r->o.ntstops = (int32_t)r->tstops.size();
+    if (o->nsave_idxs > 0) r->save_idxs.assign(o->save_idxs, o->save_idxs + o->nsave_idxs);
+    r->o.save_idxs = nullptr;
     r->N = N;
     const size_t n = (size_t)d->n_states, np = (size_t)d->n_params;
     r->u0.assign(u0, u0 + n * N);
@@ -1666,18 +1698,18 @@ int ode_autotune(ode_handle* h, const ode_problem_desc* d, const ode_options* o,
     if (rc) return rc;
     if (N <= 0 || !u0 || !p || !tspan) return fail(h, ODE_E_INVALID, "autotune needs a non-empty sample");
     if (o->nsave > 0 && !saveat) return fail(h, ODE_E_INVALID, "nsave > 0 but saveat is null");
-    if ((rc = check_host_tstops(h, o))) return rc;
+    if ((rc = check_host_tstops(h, o)) || (rc = check_host_save_idxs(h, d, o))) return rc;
     std::lock_guard<std::mutex> lk(h->api_mu);
     CUDA_TRY(h, cudaSetDevice(h->device));
     *h->h_abort = 0;
     ode_options ostaged;
     if ((rc = stage_tstops(h, o, h->main.stream, &ostaged))) return rc;
     o = &ostaged;
-    const size_t n = (size_t)d->n_states, np = (size_t)d->n_params, cap = save_cap(o);
+    const size_t n = (size_t)d->n_states, np = (size_t)d->n_params, cap = save_cap(o), rows = out_rows(d, o);
     const size_t nsv = (size_t)o->nsave * (o->saveat_per_traj ? (size_t)N : 1);
     if ((rc = grow(h, h->b_u0, n * N * 8)) || (rc = grow(h, h->b_p, np * N * 8)) ||
         (rc = grow(h, h->b_tspan, 2 * N * 8)) || (rc = grow(h, h->b_saveat, nsv * 8)) ||
-        (rc = grow(h, h->b_t, cap * N * 8)) || (rc = grow(h, h->b_u, cap * n * N * 8)) ||
+        (rc = grow(h, h->b_t, cap * N * 8)) || (rc = grow(h, h->b_u, cap * rows * N * 8)) ||
         (rc = grow(h, h->b_ns, N * 4)) || (rc = grow(h, h->b_rc, N * 4)) ||
         (rc = grow(h, h->b_st, N * sizeof(ode_stats))))
         return rc;
@@ -1914,6 +1946,8 @@ extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_o
     a.ntstops = o->ntstops > 0 ? o->ntstops : 0;
     a.max_jac_age = o->max_jac_age;
     a.jac_reuse_gamma_tol = o->jac_reuse_gamma_tol < 0 ? 0.03 : o->jac_reuse_gamma_tol;
+    a.save_idxs = o->nsave_idxs > 0 ? o->save_idxs : nullptr;   // device memory at this point
+    a.nsave_rows = o->nsave_idxs > 0 ? o->nsave_idxs : 0;
     a.t_out = t_out;
     a.u_out = u_out;
     a.nsaved = nsaved;

@@ -102,6 +102,7 @@ mutable struct Options
     scheduler::Int32; block_size::Int32; ir_sweeps::Int32; save_everystep::Int32; max_step_saves::Int32
     callback::Int32; interp_points::Int32; max_events::Int32; ntstops::Int32; tstops::Ptr{Float64}
     max_jac_age::Int32; reserved2::Int32; jac_reuse_gamma_tol::Float64
+    nsave_idxs::Int32; reserved3::Int32; save_idxs::Ptr{Int32}
 end
 # the W-method Jacobian reuse knobs of Rosenbrock23(max_jac_age, jac_reuse_gamma_tol)
 jac_reuse(alg::Rosenbrock23) = (Int32(alg.max_jac_age), Float64(alg.jac_reuse_gamma_tol))
@@ -180,7 +181,8 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem,
                            ens::EnsembleGB300; trajectories, saveat = Float64[], reltol = 1e-3, abstol = 1e-6,
                            dt = 0.0, dtmax = 0.0, dtmin = 0.0, maxiters = 1_000_000, save_start = nothing,
                            save_end = nothing, save_everystep = isempty(saveat), max_step_saves = 1024, seed = 0,
-                           callback = nothing, dense = save_everystep && isempty(saveat),
+                           save_idxs = nothing, callback = nothing,
+                           dense = save_everystep && isempty(saveat) && save_idxs === nothing,
                            tstops = Float64[], kwargs...)
     t0 = time()
     N = trajectories
@@ -212,17 +214,21 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem,
     cb = callback isa GB300Callback
     # the solve's tstops (solve.jl:1021-1040): the library keeps those inside each (t0, tf)
     tst = collect(Float64, tstops)
+    # save_idxs (1-based in Julia, 0-based in the library): the states kept, one row each
+    sidx = save_idxs === nothing ? Int32[] : Int32[i - 1 for i in save_idxs]
+    rows = save_idxs === nothing ? n : length(sidx)
     o = Options(reltol, abstol, dtmax, dtmin, dt, maxiters, ss, se, save_end === nothing ? -1 : Int32(save_end),
                 scalar, length(sv), 0, 0.0, 0.0, ens.lanes_per_traj, ens.scheduler, 0, -1, everystep,
                 everystep ? max_step_saves : 0, cb, cb ? callback.interp_points : 10, cb ? callback.max_events : 0,
-                length(tst), isempty(tst) ? Ptr{Float64}(C_NULL) : pointer(tst), jac_reuse(alg)[1], Int32(0), jac_reuse(alg)[2])
+                length(tst), isempty(tst) ? Ptr{Float64}(C_NULL) : pointer(tst), jac_reuse(alg)[1], Int32(0),
+                jac_reuse(alg)[2], length(sidx), Int32(0), isempty(sidx) ? Ptr{Int32}(C_NULL) : pointer(sidx))
     d = ProblemDesc(model, alg_id(alg), n, npar, ens.precision === :mixed ? 1 : 0, 0)
     cap = (everystep ? max_step_saves : length(sv)) + 2 + (cb ? 2 * callback.max_events : 0)
-    t_out = fill(NaN, N, cap); u_out = fill(NaN, N, n, cap)   # [(s*n + i)*N + j] -> u_out[j, i, s]
+    t_out = fill(NaN, N, cap); u_out = fill(NaN, N, rows, cap)   # [(s*rows + i)*N + j] -> u_out[j, i, s]
     nsaved = zeros(Int32, N); rc = zeros(Int32, N); st = Vector{Stats}(undef, N)
     # dense output (solve.jl:145-146) for every-step saves of one state count
-    isdense = dense && everystep && npt == C_NULL
-    GC.@preserve tst if isdense   # o holds a pointer into tst
+    isdense = dense && everystep && npt == C_NULL && save_idxs === nothing
+    GC.@preserve tst sidx if isdense   # o holds pointers into tst and sidx
         nk = ccall((:ode_dense_nk, LIB), Cint, (Cint,), alg_id(alg))
         k_out = zeros(N, n, nk, cap)   # [((s*nk + q)*n + i)*N + j] -> k_out[j, i, q, s]
         status = ccall((:ode_solve_ensemble_dense, LIB), Cint,
@@ -238,7 +244,7 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem,
     status == 0 || error("ode_solve_ensemble: ", unsafe_string(ccall((:ode_last_error, LIB), Cstring, (Ptr{Cvoid},), handle(ens.device))))
     sols = map(1:N) do j
         k = nsaved[j]
-        nj = length(probs[j].u0)
+        nj = save_idxs === nothing ? length(probs[j].u0) : rows
         us = [u_out[j, 1:nj, s] for s in 1:k]
         stats = SciMLBase.DEStats(st[j].nf, 0, 0, st[j].nsolve, st[j].nw, st[j].njacs, 0, 0, 0, 0,
                                   st[j].naccept, st[j].nreject, 0.0)

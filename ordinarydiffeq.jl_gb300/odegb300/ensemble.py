@@ -274,7 +274,8 @@ class _LazySolutions:
             j += len(self)
         r = self.r
         ns = int(r["nsaved"][j])
-        n = r["u"].shape[1] if self.npt is None else int(self.npt[j])
+        # with save_idxs every row (one for a state past a smaller trajectory's size is not written)
+        n = r["u"].shape[1] if (self.npt is None or r.get("save_idxs") is not None) else int(self.npt[j])
         t = r["t"][:ns, j].copy()
         u = [r["u"][s, :n, j].copy() for s in range(ns)]
         st = {k: int(r["stats"][k][j]) for k in r["stats"]}
@@ -308,7 +309,7 @@ def get_handle(device=0):
 
 
 def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax, callback=None,
-             tstops=None, alg=None):
+             tstops=None, alg=None, save_idxs=None):
     o = _lib.Options()
     L = _lib.load()
     L.ode_options_default(C.byref(o))
@@ -343,6 +344,11 @@ def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_ste
         o.ntstops = ts.size
         o.tstops = ts.ctypes.data_as(C.POINTER(C.c_double))
         o._tstops = ts   # the options hold the array while the call reads it
+    if save_idxs is not None:
+        ix = np.ascontiguousarray(np.atleast_1d(save_idxs), dtype=np.int32).ravel()
+        o.nsave_idxs = ix.size
+        o.save_idxs = ix.ctypes.data_as(C.POINTER(C.c_int32))
+        o._save_idxs = ix
     return o
 
 
@@ -396,7 +402,7 @@ def register_model(source, name, n_states, n_params, jac=False, tgrad=False, non
 def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=1e-6, dt=None,
                  dtmax=None, dtmin=None, maxiters=1000000, save_start=None, save_end=None, n_per_traj=None,
                  qmax_first_step=None, qmax=None, return_times=False, save_everystep=False, max_step_saves=1024,
-                 dense=False, callback=None, tstops=None):
+                 dense=False, callback=None, tstops=None, save_idxs=None):
     """Solve a packed ensemble.  u0s (n, N), ps (np, N), tspans (2, N).  Returns the
     raw structure-of-arrays outputs dict (t, u, nsaved, retcode, stats).
     save_everystep (without saveat) keeps every accepted step, up to
@@ -406,7 +412,8 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
     callback: the model's ContinuousCallback (ContinuousCallback(...)); a
     trajectory it terminates reports ReturnCode.Terminated.  tstops: times every
     trajectory steps to exactly (those inside its (t0, tf)), as the reference's
-    tstops keyword."""
+    tstops keyword.  save_idxs: the states saved (0-based, in order; the
+    reference's save_idxs): u is then (cap, len(save_idxs), N)."""
     L = _lib.load()
     if isinstance(model, str):
         model = MODELS[model]
@@ -415,15 +422,19 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
     tspans = np.ascontiguousarray(tspans, dtype=np.float64)
     n, N = u0s.shape
     sv = resolve_saveat(saveat, tspans, save_start, save_end, save_everystep, max_step_saves)
-    o = _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax, callback, tstops, alg)
+    o = _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax, callback, tstops, alg,
+                 save_idxs)
     d = _lib.ProblemDesc(model, alg.alg_id, n, ps.shape[0], ens.prec_id(), 0)
+    rows = n if save_idxs is None else int(np.size(save_idxs))
     cap = sv.cap + (2 * callback.max_events if callback is not None else 0)
     if dense and not sv.everystep:
         raise ValueError("dense output keeps every step: use it without saveat, with save_everystep")
     if dense and n_per_traj is not None:
         raise ValueError("dense output needs trajectories of one size")
+    if dense and save_idxs is not None:
+        raise ValueError("save_idxs with dense output is not supported")
     t_out = np.full((cap, N), np.nan)
-    u_out = np.full((cap, n, N), np.nan)
+    u_out = np.full((cap, rows, N), np.nan)
     k_out = np.empty((cap, L.ode_dense_nk(alg.alg_id), n, N)) if dense else None
     nsaved = np.zeros(N, dtype=np.int32)
     rc = np.zeros(N, dtype=np.int32)
@@ -457,6 +468,8 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
                           "dropped (the final point is kept)" % (lost, sv.max_step_saves))
     out = {"t": t_out, "u": u_out, "nsaved": nsaved, "retcode": rc,
            "stats": {k: stats[:, i] for i, k in enumerate(names)}, "elapsed": elapsed}
+    if save_idxs is not None:
+        out["save_idxs"] = np.atleast_1d(save_idxs).astype(np.int32)
     if dense:
         out["k"] = k_out
         out["dense"] = {"model": model, "alg": alg.alg_id, "p": ps, "device": ens.device}
@@ -518,20 +531,21 @@ def autotune(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=
 def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, saveat=None, reltol=1e-3,
           abstol=1e-6, dt=None, dtmax=None, dtmin=None, maxiters=1000000, save_start=None, save_end=None,
           seed=0, qmax_first_step=None, qmax=None, save_everystep=None, max_step_saves=1024, dense=None,
-          callback=None, tstops=None):
+          callback=None, tstops=None, save_idxs=None):
     """solve(EnsembleProblem, alg, EnsembleGB300(); trajectories, saveat, reltol, abstol, ...).
     As in the reference (solve.jl:138-146), save_everystep defaults to "no
     saveat given" (every accepted step is kept, up to max_step_saves per
     trajectory) and dense to save_everystep without saveat (each step's
     interpolant; a callback's saves keep them as well); ensembles of uneven
     sizes are not dense by default.  callback: the model's ContinuousCallback or
-    DiscreteCallback.  tstops: times every trajectory steps to exactly."""
+    DiscreteCallback.  tstops: times every trajectory steps to exactly.
+    save_idxs: the states saved (0-based); no dense output with it."""
     no_saveat = saveat is None or (not np.isscalar(saveat) and np.size(saveat) == 0)
     if save_everystep is None:
         save_everystep = no_saveat
     dense_default = dense is None
     if dense is None:
-        dense = bool(save_everystep and no_saveat)
+        dense = bool(save_everystep and no_saveat and save_idxs is None)
     ens = ensemblealg or EnsembleGB300()
     if not isinstance(ens, EnsembleGB300):
         raise TypeError("ensemble algorithm must be EnsembleGB300")
@@ -548,7 +562,7 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
                            maxiters, save_start, save_end, eprob.n_per_traj, qmax_first_step, qmax,
                            save_everystep=save_everystep, max_step_saves=max_step_saves,
                            dense=dense and not (dense_default and eprob.n_per_traj is not None), callback=callback,
-                           tstops=tstops)
+                           tstops=tstops, save_idxs=save_idxs)
         sols = _LazySolutions(res, alg, eprob.n_per_traj)
         return EnsembleSolution(sols, time.perf_counter() - t_start, True, res)
     if trajectories is None:
@@ -564,7 +578,7 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
         ids = list(range(done, min(trajectories, done + batch_size)))
         outs = _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, dtmin, maxiters,
                             save_start, save_end, output_func, qmax_first_step, qmax, save_everystep, max_step_saves,
-                            dense, dense_default, callback, tstops)
+                            dense, dense_default, callback, tstops, save_idxs)
         u, converged = reduction(u, outs, range(ids[0] + 1, ids[-1] + 2))
         done = ids[-1] + 1
         if converged:
@@ -574,7 +588,7 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
 
 def _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, dtmin, maxiters, save_start,
                  save_end, output_func, qmax_first_step, qmax, save_everystep=False, max_step_saves=1024,
-                 dense=False, dense_default=True, callback=None, tstops=None):
+                 dense=False, dense_default=True, callback=None, tstops=None, save_idxs=None):
     repeat = {i: 1 for i in ids}
     results = {}
     todo = list(ids)
@@ -602,7 +616,7 @@ def _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, 
                            maxiters, save_start, save_end, npt, qmax_first_step, qmax,
                            save_everystep=save_everystep, max_step_saves=max_step_saves,
                            dense=dense and not (dense_default and npt is not None), callback=callback,
-                           tstops=tstops)
+                           tstops=tstops, save_idxs=save_idxs)
         sols = _LazySolutions(res, alg, npt)
         again = []
         for k, i in enumerate(todo):

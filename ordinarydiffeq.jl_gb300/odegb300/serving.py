@@ -64,7 +64,7 @@ class Server:
         self.close()
 
     def submit(self, model, alg, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=1e-6, precision="fp64",
-               ir_sweeps=-1, tag=None, tstops=None):
+               ir_sweeps=-1, tag=None, tstops=None, save_idxs=None):
         """Queue one packed ensemble; returns its ticket at once (the library
         copies the inputs, tstops included, before this returns), or None when
         the server's queue is full (the request was shed)."""
@@ -80,10 +80,12 @@ class Server:
         prec = pick_precision(precision, reltol, name)
         ens = EnsembleGB300(precision=prec, ir_sweeps=ir_sweeps if prec == "mixed" else -1)
         sv = saveat if hasattr(saveat, "nsave") else resolve_saveat(saveat, tspans)
-        o = _options(reltol, abstol, None, None, None, 1000000, sv, ens, None, None, tstops=tstops, alg=alg)
+        o = _options(reltol, abstol, None, None, None, 1000000, sv, ens, None, None, tstops=tstops, alg=alg,
+                     save_idxs=save_idxs)
         d = _lib.ProblemDesc(model, alg.alg_id, n, ps.shape[0], ens.prec_id(), 0)
         cap = sv.cap
-        out = {"t": np.empty((cap, N)), "u": np.empty((cap, n, N)), "nsaved": np.empty(N, dtype=np.int32),
+        rows = n if save_idxs is None else int(np.size(save_idxs))
+        out = {"t": np.empty((cap, N)), "u": np.empty((cap, rows, N)), "nsaved": np.empty(N, dtype=np.int32),
                "retcode": np.empty(N, dtype=np.int32), "stats": np.empty((N, 6), dtype=np.int64)}
         dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
         ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))

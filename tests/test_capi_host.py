@@ -104,6 +104,19 @@ def test_jacobian_reuse_options_are_checked_on_the_host():
     assert b"max_jac_age" in L.ode_last_error(None)
 
 
+def test_save_idxs_are_checked_on_the_host():
+    L = _lib.load()
+    o = _lib.Options()
+    L.ode_options_default(C.byref(o))
+    assert o.nsave_idxs == 0 and not o.save_idxs
+    d = _lib.ProblemDesc(_lib.MODEL_LORENZ, _lib.ODE_TSIT5, 3, 3, _lib.PREC_FP64, 0)
+    o.nsave_idxs = -1
+    assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == -1
+    o.nsave_idxs = 2   # and save_idxs left null
+    assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == -1
+    assert b"save_idxs" in L.ode_last_error(None)
+
+
 def test_variant_registry_covers_the_workloads():
     L = _lib.load()
     buf = (C.c_int32 * 8)()
