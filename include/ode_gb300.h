@@ -198,6 +198,11 @@ typedef struct {
                                    n_states), device memory for ode_solve_ensemble_device and
                                    ode_solve_ensemble_noalloc (an index outside the trajectory's states
                                    leaves its row unwritten).  Not with dense output */
+    int32_t adaptive;           /* 1 (default): error-controlled steps; 0: fixed steps of |dt|, clipped to
+                                   land on the tstops and tf; with dt = 0 (then tstops are required)
+                                   every step runs to the next tstop (the reference's adaptive = false:
+                                   no error estimate is judged, every step is accepted) */
+    int32_t reserved4;
 } ode_options;
 
 /* Fill o with the reference's defaults. */

@@ -1031,6 +1031,10 @@ void modify_dt_for_tstops(Integ& I) {
             I.tstop_target = I.tdir * tdir_tstop;
         }
         I.dt = I.tdir * jmin(orig, dist);
+    } else if (I.dtcache == 0.0) {   // fixed steps without a dt: to the next tstop
+        I.next_step_tstop = true;
+        I.tstop_target = I.tdir * tdir_tstop;
+        I.dt = I.tdir * dist;
     } else {
         if (std::fabs(I.dtcache) + tol < dist) {
             I.next_step_tstop = false;
@@ -1741,7 +1745,9 @@ int solve_one(Integ& I, const double* u0) {
         f_eval(I, I.u.data(), I.t, I.fsalfirst.data());
         I.st.nf += 1;
     }
-    if (I.o.dt > 0.0) {
+    if (!I.o.adaptive) {
+        I.dt = I.tdir * std::fabs(I.o.dt);   // fixed steps: no heuristic (handle_dt!, solve.jl:968-985)
+    } else if (I.o.dt > 0.0) {
         I.dt = I.tdir * I.o.dt;   // a positive dt is taken in the direction (handle_dt!, solve.jl:949-966)
     } else {
         I.dt = initdt(I);

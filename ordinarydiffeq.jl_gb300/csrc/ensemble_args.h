@@ -50,6 +50,7 @@ struct EnsembleArgs {
                             // method's NDENSE interpolation vectors of the step ending at save s
     double qmax_first_step, qmax;
     int ir_sweeps;          // mixed Rosenbrock: refinement sweeps per solve
+    int adaptive;           // 0: fixed steps of dt, every step accepted
     int max_jac_age;        // Rosenbrock23: J kept for at most this many accepted steps (<= 1: never kept)
     double jac_reuse_gamma_tol;  // ... while |dtgamma / dtgamma_J - 1| <= this
     // scheduling

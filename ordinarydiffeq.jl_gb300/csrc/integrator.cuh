@@ -420,7 +420,9 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
     double t = t0, tprev = t0;
     Alg::template initialize<Model, R, L, C>(cache, u, p, TM(t), g, st, a, j);
     double dt;
-    if (a.dt > 0) {
+    if (!a.adaptive) {
+        dt = fabs(a.dt);   // fixed steps: no initial-step heuristic (handle_dt!, solve.jl:968-985)
+    } else if (a.dt > 0) {
         dt = a.dt;
     } else {
         // the initial step's dtmax is at most the distance to the first tstop
@@ -781,10 +783,11 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
         // dt and a positive dtmin: the lower bound applies forward only)
         dt = pmin(dtmax, dt);
         if (!bwd) dt = pmax(dt, pabs(pmax(peps(t), a.dtmin)));
-        {   // modify_dt_for_tstops!
+        {   // modify_dt_for_tstops!  (fixed steps: the given dt, dtcache, clipped instead;
+            // without one, every step runs to the next tstop)
             const double tol = ptol100(pmax(pabs(t), pabs(tnext)));
-            const double orig = pabs(dt);
-            dtpropose = orig;
+            const double orig = a.adaptive ? pabs(dt) : (a.dt != 0 ? fabs(a.dt) : dist);
+            if (a.adaptive) dtpropose = orig;
             next_tstop = !plt(orig + tol, dist);
             dt = pmin(orig, dist);
         }
@@ -797,9 +800,10 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             else if (bits_nan(db)) e = RC_DTNAN;
             else if (iter > a.maxiters) e = RC_MAXITERS;
             // t + dt < tdir * first(tstops) in the reference's own time
-            else if (ple(pabs(dt), pabs(a.dtmin)) && (!accept || (bwd ? t + dt > tnext : t + dt < tnext)))
+            else if (a.adaptive && ple(pabs(dt), pabs(a.dtmin)) &&
+                     (!accept || (bwd ? t + dt > tnext : t + dt < tnext)))
                 e = RC_DTLESSTHANMIN;
-            else if (!accept && ple(pabs(dt), peps(t))) e = RC_UNSTABLE;
+            else if (a.adaptive && !accept && ple(pabs(dt), peps(t))) e = RC_UNSTABLE;
             else if (accept) {
                 bool bad = false;
 #pragma unroll
@@ -819,9 +823,11 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
         if constexpr (is_composite_alg<Alg>::value) do_error_check = true;
         const double ttmp = t + dt;
         const CT inv_qmaxc = success_iter == 0 ? inv_qmax_first : inv_qmax;
-        CT q;
+        CT q = CT(1);
         double ln_eest = dnan();   // FP64 form: ln(EEst) of this attempt when EEst is finite and positive
-        if (EEst == CT(0)) {
+        if (!a.adaptive) {
+            // fixed steps: every step is accepted and no controller runs
+        } else if (EEst == CT(0)) {
             q = inv_qmaxc;
         } else {
             CT qq, den;
@@ -839,23 +845,28 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             const CT x = q / gam;
             q = x > qmin_inv ? qmin_inv : (x < inv_qmaxc ? inv_qmaxc : x);
         }
-        accept = EEst <= CT(1);
+        accept = !a.adaptive || EEst <= CT(1);
         if (accept) {
             st.naccept++;
             tprev = t;
             if (next_tstop) {
-                dt = dtpropose;
+                if (a.adaptive) dt = dtpropose;
                 next_tstop = false;
                 t = tnext;   // the tstop target
             } else {
                 t = ttmp;
             }
-            if (CT(1) <= q && q <= qsteady_max) q = CT(1);
-            errold = (EEst != EEst) ? EEst : (EEst > qoldinit ? EEst : qoldinit);
-            if constexpr (sizeof(CT) == 8) ln_errold = (EEst != EEst) ? dnan() : (EEst > qoldinit ? ln_eest : ln_qoldinit);
-            const double dtnew = Ctl<R>::scale_dt(dt, q);
-            const double dtp = pmin(pabs(dtmax), pabs(dtnew));
-            dtpropose = pmax(pabs(dtp), pabs(pmax(peps(t), a.dtmin)));
+            if (a.adaptive) {
+                if (CT(1) <= q && q <= qsteady_max) q = CT(1);
+                errold = (EEst != EEst) ? EEst : (EEst > qoldinit ? EEst : qoldinit);
+                if constexpr (sizeof(CT) == 8)
+                    ln_errold = (EEst != EEst) ? dnan() : (EEst > qoldinit ? ln_eest : ln_qoldinit);
+                const double dtnew = Ctl<R>::scale_dt(dt, q);
+                const double dtp = pmin(pabs(dtmax), pabs(dtnew));
+                dtpropose = pmax(pabs(dtp), pabs(pmax(peps(t), a.dtmin)));
+            } else {
+                dtpropose = dt;   // the non-adaptive footer (integrator_utils.jl:660-677)
+            }
             // ---- handle_callbacks! / savevalues!
             // handle_callbacks! (integrator_utils.jl:1081-1132): the continuous callback,
             // then the discrete one; savevalues! unless the last of them saved

@@ -268,6 +268,8 @@ int check_problem(const ode_problem_desc* d, const ode_options* o, int64_t N, co
     if (o->max_jac_age < 0) return bad(ODE_E_INVALID, "max_jac_age must be >= 0");
     if (o->nsave_idxs < 0 || (o->nsave_idxs > 0 && !o->save_idxs))
         return bad(ODE_E_INVALID, "nsave_idxs < 0, or save_idxs is null");
+    if (!o->adaptive && (std::isnan(o->dt) || std::isinf(o->dt) || (o->dt == 0 && o->ntstops == 0)))
+        return bad(ODE_E_INVALID, "fixed steps (adaptive = 0) need a finite dt or tstops");
     // the kept J lives beside W in registers; the shared-memory LU (16-64 states)
     // forms W in place of J
     if (d->alg_id == ODE_ROSENBROCK23 && o->max_jac_age > 1 && d->n_states > 8)
@@ -364,6 +366,7 @@ EnsembleArgs make_args(ode_handle* h, const ode_problem_desc* d, const ode_optio
     a.ntstops = o->ntstops > 0 ? o->ntstops : 0;
     a.max_jac_age = o->max_jac_age;
     a.jac_reuse_gamma_tol = o->jac_reuse_gamma_tol < 0 ? 0.03 : o->jac_reuse_gamma_tol;
+    a.adaptive = o->adaptive ? 1 : 0;
     a.save_idxs = o->nsave_idxs > 0 ? o->save_idxs : nullptr;   // device memory at this point
     a.nsave_rows = o->nsave_idxs > 0 ? o->nsave_idxs : 0;
     a.t_out = t_out;
@@ -1351,6 +1354,7 @@ void ode_options_default(ode_options* o) {
     o->interp_points = 10;
     o->max_jac_age = 1;
     o->jac_reuse_gamma_tol = 0.03;
+    o->adaptive = 1;
 }
 
 size_t ode_options_size(void) { return sizeof(ode_options); }
@@ -1946,6 +1950,7 @@ extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_o
     a.ntstops = o->ntstops > 0 ? o->ntstops : 0;
     a.max_jac_age = o->max_jac_age;
     a.jac_reuse_gamma_tol = o->jac_reuse_gamma_tol < 0 ? 0.03 : o->jac_reuse_gamma_tol;
+    a.adaptive = o->adaptive ? 1 : 0;
     a.save_idxs = o->nsave_idxs > 0 ? o->save_idxs : nullptr;   // device memory at this point
     a.nsave_rows = o->nsave_idxs > 0 ? o->nsave_idxs : 0;
     a.t_out = t_out;

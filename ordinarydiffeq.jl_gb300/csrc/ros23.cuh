@@ -47,6 +47,7 @@ struct Rosenbrock23T {
         // Jacobian reuse (JacReuseState): dtgamma of the last fresh J once an accepted
         // step has passed, the one pending, and naccept at the last age reset
         int max_age;
+        bool adaptive;
         double gamma_tol, last_dtg, pending_dtg;
         long long last_naccept, last_step_iter;
     };
@@ -61,6 +62,7 @@ struct Rosenbrock23T {
         LA::template init<R, L, C>(c.la, g);
         c.ir = a.ir_sweeps;
         c.max_age = a.max_jac_age;
+        c.adaptive = a.adaptive != 0;
         c.gamma_tol = a.jac_reuse_gamma_tol;
         c.last_dtg = c.pending_dtg = 0.0;
         c.last_naccept = c.last_step_iter = 0;
@@ -120,6 +122,7 @@ struct Rosenbrock23T {
                                           long long naccept) {
         if (iter < 0) return false;
         if (c.max_age <= 1) return true;   // the age check fires on every attempt
+        if (!c.adaptive) return true;      // non-adaptive solves always recompute
         const double dtg = dt * tab::ROS23_D;
         bool fresh = true;
         if (iter > 1) {
@@ -203,6 +206,7 @@ struct Rosenbrock23T {
         for (int i = 0; i < C; ++i) Acc<R>::update2(u[i], ulo[i], dr, dl, k2[i], up[i], uplo[i]);
         rhs_stage<Model, R, L, C, NP>(c.fsallast, u, ulo, p, c.pff, stage_time<Model>(1.0, dt, t), g);
         st.nf += 1;
+        if (!c.adaptive) return R(0);   // fixed steps: no k3, no error estimate
 #pragma unroll
         for (int i = 0; i < C; ++i) {
             R acc = FMA(-c32, k2[i] - c.f1[i], c.fsallast[i]);

@@ -103,6 +103,7 @@ mutable struct Options
     callback::Int32; interp_points::Int32; max_events::Int32; ntstops::Int32; tstops::Ptr{Float64}
     max_jac_age::Int32; reserved2::Int32; jac_reuse_gamma_tol::Float64
     nsave_idxs::Int32; reserved3::Int32; save_idxs::Ptr{Int32}
+    adaptive::Int32; reserved4::Int32
 end
 # the W-method Jacobian reuse knobs of Rosenbrock23(max_jac_age, jac_reuse_gamma_tol)
 jac_reuse(alg::Rosenbrock23) = (Int32(alg.max_jac_age), Float64(alg.jac_reuse_gamma_tol))
@@ -181,7 +182,7 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem,
                            ens::EnsembleGB300; trajectories, saveat = Float64[], reltol = 1e-3, abstol = 1e-6,
                            dt = 0.0, dtmax = 0.0, dtmin = 0.0, maxiters = 1_000_000, save_start = nothing,
                            save_end = nothing, save_everystep = isempty(saveat), max_step_saves = 1024, seed = 0,
-                           save_idxs = nothing, callback = nothing,
+                           save_idxs = nothing, adaptive = true, callback = nothing,
                            dense = save_everystep && isempty(saveat) && save_idxs === nothing,
                            tstops = Float64[], kwargs...)
     t0 = time()
@@ -217,11 +218,13 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem,
     # save_idxs (1-based in Julia, 0-based in the library): the states kept, one row each
     sidx = save_idxs === nothing ? Int32[] : Int32[i - 1 for i in save_idxs]
     rows = save_idxs === nothing ? n : length(sidx)
-    o = Options(reltol, abstol, dtmax, dtmin, dt, maxiters, ss, se, save_end === nothing ? -1 : Int32(save_end),
+    # a dt of either sign is taken in the direction of the span (handle_dt!, solve.jl:968-985)
+    o = Options(reltol, abstol, dtmax, dtmin, abs(dt), maxiters, ss, se, save_end === nothing ? -1 : Int32(save_end),
                 scalar, length(sv), 0, 0.0, 0.0, ens.lanes_per_traj, ens.scheduler, 0, -1, everystep,
                 everystep ? max_step_saves : 0, cb, cb ? callback.interp_points : 10, cb ? callback.max_events : 0,
                 length(tst), isempty(tst) ? Ptr{Float64}(C_NULL) : pointer(tst), jac_reuse(alg)[1], Int32(0),
-                jac_reuse(alg)[2], length(sidx), Int32(0), isempty(sidx) ? Ptr{Int32}(C_NULL) : pointer(sidx))
+                jac_reuse(alg)[2], length(sidx), Int32(0), isempty(sidx) ? Ptr{Int32}(C_NULL) : pointer(sidx),
+                Int32(adaptive), Int32(0))
     d = ProblemDesc(model, alg_id(alg), n, npar, ens.precision === :mixed ? 1 : 0, 0)
     cap = (everystep ? max_step_saves : length(sv)) + 2 + (cb ? 2 * callback.max_events : 0)
     t_out = fill(NaN, N, cap); u_out = fill(NaN, N, rows, cap)   # [(s*rows + i)*N + j] -> u_out[j, i, s]

@@ -41,7 +41,8 @@ class Options(C.Structure):
                 ("callback", C.c_int32), ("interp_points", C.c_int32), ("max_events", C.c_int32),
                 ("ntstops", C.c_int32), ("tstops", C.POINTER(C.c_double)),
                 ("max_jac_age", C.c_int32), ("reserved2", C.c_int32), ("jac_reuse_gamma_tol", C.c_double),
-                ("nsave_idxs", C.c_int32), ("reserved3", C.c_int32), ("save_idxs", C.POINTER(C.c_int32))]
+                ("nsave_idxs", C.c_int32), ("reserved3", C.c_int32), ("save_idxs", C.POINTER(C.c_int32)),
+                ("adaptive", C.c_int32), ("reserved4", C.c_int32)]
 
 
 class Stats(C.Structure):

@@ -309,7 +309,7 @@ def get_handle(device=0):
 
 
 def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax, callback=None,
-             tstops=None, alg=None, save_idxs=None):
+             tstops=None, alg=None, save_idxs=None, adaptive=True):
     o = _lib.Options()
     L = _lib.load()
     L.ode_options_default(C.byref(o))
@@ -317,7 +317,7 @@ def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_ste
         o.max_jac_age = alg.max_jac_age
         o.jac_reuse_gamma_tol = alg.jac_reuse_gamma_tol
     o.reltol, o.abstol = reltol, abstol
-    o.dt = dt or 0.0
+    o.dt = abs(dt or 0.0)   # either sign is taken in the span's direction (handle_dt!, solve.jl:968-985)
     o.dtmax = dtmax or 0.0
     o.dtmin = dtmin or 0.0
     o.maxiters = int(maxiters)
@@ -344,6 +344,7 @@ def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_ste
         o.ntstops = ts.size
         o.tstops = ts.ctypes.data_as(C.POINTER(C.c_double))
         o._tstops = ts   # the options hold the array while the call reads it
+    o.adaptive = int(bool(adaptive))
     if save_idxs is not None:
         ix = np.ascontiguousarray(np.atleast_1d(save_idxs), dtype=np.int32).ravel()
         o.nsave_idxs = ix.size
@@ -402,7 +403,7 @@ def register_model(source, name, n_states, n_params, jac=False, tgrad=False, non
 def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=1e-6, dt=None,
                  dtmax=None, dtmin=None, maxiters=1000000, save_start=None, save_end=None, n_per_traj=None,
                  qmax_first_step=None, qmax=None, return_times=False, save_everystep=False, max_step_saves=1024,
-                 dense=False, callback=None, tstops=None, save_idxs=None):
+                 dense=False, callback=None, tstops=None, save_idxs=None, adaptive=True):
     """Solve a packed ensemble.  u0s (n, N), ps (np, N), tspans (2, N).  Returns the
     raw structure-of-arrays outputs dict (t, u, nsaved, retcode, stats).
     save_everystep (without saveat) keeps every accepted step, up to
@@ -413,7 +414,8 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
     trajectory it terminates reports ReturnCode.Terminated.  tstops: times every
     trajectory steps to exactly (those inside its (t0, tf)), as the reference's
     tstops keyword.  save_idxs: the states saved (0-based, in order; the
-    reference's save_idxs): u is then (cap, len(save_idxs), N)."""
+    reference's save_idxs): u is then (cap, len(save_idxs), N).  adaptive=False:
+    fixed steps of dt (the reference's adaptive = false)."""
     L = _lib.load()
     if isinstance(model, str):
         model = MODELS[model]
@@ -423,7 +425,7 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
     n, N = u0s.shape
     sv = resolve_saveat(saveat, tspans, save_start, save_end, save_everystep, max_step_saves)
     o = _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax, callback, tstops, alg,
-                 save_idxs)
+                 save_idxs, adaptive)
     d = _lib.ProblemDesc(model, alg.alg_id, n, ps.shape[0], ens.prec_id(), 0)
     rows = n if save_idxs is None else int(np.size(save_idxs))
     cap = sv.cap + (2 * callback.max_events if callback is not None else 0)
@@ -531,7 +533,7 @@ def autotune(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=
 def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, saveat=None, reltol=1e-3,
           abstol=1e-6, dt=None, dtmax=None, dtmin=None, maxiters=1000000, save_start=None, save_end=None,
           seed=0, qmax_first_step=None, qmax=None, save_everystep=None, max_step_saves=1024, dense=None,
-          callback=None, tstops=None, save_idxs=None):
+          callback=None, tstops=None, save_idxs=None, adaptive=True):
     """solve(EnsembleProblem, alg, EnsembleGB300(); trajectories, saveat, reltol, abstol, ...).
     As in the reference (solve.jl:138-146), save_everystep defaults to "no
     saveat given" (every accepted step is kept, up to max_step_saves per
@@ -562,7 +564,7 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
                            maxiters, save_start, save_end, eprob.n_per_traj, qmax_first_step, qmax,
                            save_everystep=save_everystep, max_step_saves=max_step_saves,
                            dense=dense and not (dense_default and eprob.n_per_traj is not None), callback=callback,
-                           tstops=tstops, save_idxs=save_idxs)
+                           tstops=tstops, save_idxs=save_idxs, adaptive=adaptive)
         sols = _LazySolutions(res, alg, eprob.n_per_traj)
         return EnsembleSolution(sols, time.perf_counter() - t_start, True, res)
     if trajectories is None:
@@ -578,7 +580,7 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
         ids = list(range(done, min(trajectories, done + batch_size)))
         outs = _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, dtmin, maxiters,
                             save_start, save_end, output_func, qmax_first_step, qmax, save_everystep, max_step_saves,
-                            dense, dense_default, callback, tstops, save_idxs)
+                            dense, dense_default, callback, tstops, save_idxs, adaptive)
         u, converged = reduction(u, outs, range(ids[0] + 1, ids[-1] + 2))
         done = ids[-1] + 1
         if converged:
@@ -588,7 +590,7 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
 
 def _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, dtmin, maxiters, save_start,
                  save_end, output_func, qmax_first_step, qmax, save_everystep=False, max_step_saves=1024,
-                 dense=False, dense_default=True, callback=None, tstops=None, save_idxs=None):
+                 dense=False, dense_default=True, callback=None, tstops=None, save_idxs=None, adaptive=True):
     repeat = {i: 1 for i in ids}
     results = {}
     todo = list(ids)
@@ -616,7 +618,7 @@ def _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, 
                            maxiters, save_start, save_end, npt, qmax_first_step, qmax,
                            save_everystep=save_everystep, max_step_saves=max_step_saves,
                            dense=dense and not (dense_default and npt is not None), callback=callback,
-                           tstops=tstops, save_idxs=save_idxs)
+                           tstops=tstops, save_idxs=save_idxs, adaptive=adaptive)
         sols = _LazySolutions(res, alg, npt)
         again = []
         for k, i in enumerate(todo):

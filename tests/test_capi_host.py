@@ -117,6 +117,20 @@ def test_save_idxs_are_checked_on_the_host():
     assert b"save_idxs" in L.ode_last_error(None)
 
 
+def test_fixed_steps_are_checked_on_the_host():
+    # adaptive = false needs a dt or tstops (solve.jl:277-280); a NaN or infinite dt is rejected
+    L = _lib.load()
+    o = _lib.Options()
+    L.ode_options_default(C.byref(o))
+    assert o.adaptive == 1
+    d = _lib.ProblemDesc(_lib.MODEL_LORENZ, _lib.ODE_TSIT5, 3, 3, _lib.PREC_FP64, 0)
+    o.adaptive = 0
+    assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == -1
+    assert b"fixed steps" in L.ode_last_error(None)
+    o.dt = float("inf")
+    assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == -1
+
+
 def test_variant_registry_covers_the_workloads():
     L = _lib.load()
     buf = (C.c_int32 * 8)()

@@ -331,6 +331,29 @@ def test_every_tstop_is_in_sol_t(alg):
     assert np.all(np.diff(r["t"]) > 0)
 
 
+def _fixed(tstops, dt=0.0):
+    return O.solve(O.TSIT5, O.LINEAR, [0.5], [1.01], (0.0, 1.0), saveat=[], tstops=tstops, saveat_given=False,
+                   adaptive=False, dt=dt, save_everystep=True, max_step_saves=4096, save_start=True)
+
+
+def test_fixed_steps_land_on_the_tstops():
+    # ode_tstops_tests.jl:14-15: RK4, dt = 1//3, tstops = [1/2], adaptive = false
+    r = _fixed([0.5], dt=1 / 3)
+    assert list(r["t"]) == [0.0, 1 / 3, 1 / 2, 1 / 3 + 1 / 2, 1.0]
+    # :29-30 and :32-36: without a dt every step runs to the next tstop
+    ts = [1 / 5, 1 / 4, 1 / 3, 1 / 2, 3 / 4]
+    assert list(_fixed(ts)["t"]) == [0.0] + ts + [1.0]
+    assert list(_fixed([0.0] + ts + [1.0])["t"]) == [0.0] + ts + [1.0]
+    # :38-42: a range of tstops is the time grid
+    assert list(_fixed(np.arange(17) / 16)["t"]) == list(np.arange(17) / 16)
+    g = np.linspace(0.0, 1.0, 100)
+    assert list(_fixed(g)["t"]) == list(g)
+    # every step is accepted and no initial-step probe runs: one RHS call per stage
+    r = _fixed([0.5], dt=1 / 3)
+    assert r["stats"]["naccept"] == 4 and r["stats"]["nreject"] == 0
+    assert r["stats"]["nf"] == 1 + 6 * 4
+
+
 def test_tstops_from_a_range_are_a_subset_of_sol_t():
     # ode_tstops_tests.jl:97-105 ("Late binding tstops"): 0:0.1:1 is a subset of sol.t
     ts = np.arange(0, 11) * 0.1
