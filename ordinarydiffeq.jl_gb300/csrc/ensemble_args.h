@@ -55,6 +55,7 @@ struct EnsembleArgs {
     double jac_reuse_gamma_tol;  // ... while |dtgamma / dtgamma_J - 1| <= this
     // scheduling
     int persistent;
+    int refill_lanes;       // idle lanes of a warp that take new trajectories together (32: the whole warp)
     unsigned long long* queue;     // persistent work counter (zeroed before launch)
     const volatile int* abort_flag;  // host-settable early stop (nullptr: none)
     // size classes of an uneven ensemble (one launch over all classes):

@@ -319,33 +319,43 @@ __device__ double initdt(const R* u0, const PR<R>* p, double t, bool bwd, double
     return jmax(dtmin, jmin(jmin(100.0 * dt0, dt1), dtmax));
 }
 
-// One trajectory, start to finish, on lane group g.  Alg provides the cache,
-// the step, the interpolant and the FSAL hooks.
-template <class Alg, class Model, class R, int L, int C>
-__device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group<L>& g) {
+// Trajectories one after another on lane group g, as `next` hands them out
+// (a negative index: none left).  A group whose trajectory ends takes the next
+// one inside the same step loop, so its lanes step again with the rest of the
+// warp at the next iteration instead of idling until the warp's longest
+// trajectory ends (the trajectories of a warp differ in step counts by up to
+// the ratio of their spans or stiffness).  Every trajectory's arithmetic is
+// the same whichever group and slot runs it.  Alg provides the cache, the
+// step, the interpolant and the FSAL hooks.
+template <class Alg, class Model, class R, int L, int C, class Next>
+__device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Next next) {
     using CT = typename Ctl<R>::T;
     constexpr int NP = Model::NP;
     const long long N = a.N;
+    long long j = -1;   // the trajectory in hand
     R u[C], uprev[C], ulo[C], uprevlo[C];   // solution as (hi, lo) pairs, see Acc
     PR<R> p[NP > 0 ? NP : 1];   // FP64, or float pairs in the mixed form (fpair)
-#pragma unroll
-    for (int c = 0; c < C; ++c) Acc<R>::split(a.u0[(size_t)(g.lane * C + c) * N + j], u[c], ulo[c]);
-#pragma unroll
-    for (int i = 0; i < NP; ++i) p[i] = make_param<R>(a.p[(size_t)i * N + j]);
     // Backward integration (tf < t0) runs the loop on s = -t: its times, steps,
     // tstops and saveat points are those of the reference negated (the
     // reference's own heaps hold tdir * t), every comparison on them is the
     // reference's with tdir taken out, and the model and the method see the
     // model's time TM(s) = -s and signed step DT(h) = -h, so each stage and each
     // interpolation is the reference's arithmetic exactly (negation is exact).
-    const bool bwd = a.tspan[N + j] < a.tspan[j];
-    auto TM = [bwd](double x) -> double { return bwd ? -x : x; };
-    const double t0 = TM(a.tspan[j]), tf = TM(a.tspan[N + j]);
-    const double dtmax = a.dtmax > 0 ? a.dtmax : tf - t0;
+    // The direction is data, held in the step loop as one mask (bm = -1
+    // backward, 0 forward) from which everything direction-dependent is integer
+    // arithmetic: TM flips the sign bit, the reversed saveat and tstops indices
+    // are (s ^ bm) + (bm & n), and the forward-only dtmin bound is masked to zero
+    // (a runtime flag used through branches and selects on doubles cost the
+    // mixed Robertson kernel 30%).
+    bool bwd = false;
+    int bm = 0;
+    auto TM = [&bm](double x) -> double {
+        return __hiloint2double(__double2hiint(x) ^ (bm & (int)0x80000000u), __double2loint(x));
+    };
+    double t0 = 0.0, tf = 0.0, dtmax = 0.0;
     // the ensemble's tolerances, or per trajectory (requests merged into one
     // launch by the serving loop keep their own)
-    const R abstol = (R)(a.abstol_traj ? a.abstol_traj[j] : a.abstol);
-    const R reltol = (R)(a.reltol_traj ? a.reltol_traj[j] : a.reltol);
+    R abstol = R(0), reltol = R(0);
     const Ctrl K = make_ctrl<Alg::ORDER, Alg::IMPLICIT>(a);
     // beta1, beta2 and qsteady_max change with a composite's current method
     CT beta1 = (CT)K.beta1, beta2 = (CT)K.beta2, qsteady_max = (CT)K.qsteady_max;
@@ -402,51 +412,23 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
     };
     // the saveat points ascend; backward they are read from the end, negated
     auto saveat_at = [&](int s) -> double {
-        const int k = bwd ? a.nsave - 1 - s : s;
+        const int k = (s ^ bm) + (bm & a.nsave);
         return TM(a.saveat_per_traj ? a.saveat[(size_t)k * N + j] : a.saveat[k]);
     };
-    auto tstop_at = [&](int k) -> double { return TM(a.tstops[bwd ? a.ntstops - 1 - k : k]); };
+    auto tstop_at = [&](int k) -> double { return TM(a.tstops[(k ^ bm) + (bm & a.ntstops)]); };
 
-    // saveat entries outside (t0, tf] are skipped (initialize_saveat, solve.jl:1103-1124)
-    while (isave < a.nsave && !(saveat_at(isave) > t0)) isave++;
-
-#pragma unroll
-    for (int c = 0; c < C; ++c) { uprev[c] = u[c]; uprevlo[c] = ulo[c]; }
-    if (a.save_start) {
-        if (a.k_out) save_dense(false);
-        save_point(t0, u, ulo);
-    }
-
-    double t = t0, tprev = t0;
-    Alg::template initialize<Model, R, L, C>(cache, u, p, TM(t), g, st, a, j);
-    double dt;
-    if (!a.adaptive) {
-        dt = fabs(a.dt);   // fixed steps: no initial-step heuristic (handle_dt!, solve.jl:968-985)
-    } else if (a.dt > 0) {
-        dt = a.dt;
-    } else {
-        // the initial step's dtmax is at most the distance to the first tstop
-        // (_determine_initdt, integrator_interface.jl:644-656)
-        int k0 = 0;
-        while (k0 < a.ntstops && !(tstop_at(k0) > t0)) k0++;
-        const double first_tstop = (k0 < a.ntstops && tstop_at(k0) < tf) ? tstop_at(k0) : tf;
-        dt = initdt<Model, R, L, C, Alg::ORDER>(u, p, TM(t), bwd, jmin(fabs(dtmax), fabs(first_tstop - t0)), a.dtmin,
-                                                 abstol, reltol, Alg::template fsal_slot<R, C>(cache), g);
-        st.nf += 2;
-    }
-    double dtpropose = dt;
+    double t = 0.0, tprev = 0.0, dt = 0.0, dtpropose = 0.0;
     CT EEst = CT(1), q11 = CT(1), errold = qoldinit;
     CT bank_errold = qoldinit, bank_q11 = CT(1);   // composite: the other method's controller state
     // FP64 form: ln(errold) kept from the step that set errold, so errold^beta2 is one
     // exp series instead of a ctrl_pow (the same value: ctrl_pow(x, y) is
     // series_exp(y * series_ln(x)) for finite positive x); NaN when not kept
     double ln_qoldinit = 0.0, ln_errold = 0.0, bank_ln_errold = 0.0;
-    if constexpr (sizeof(CT) == 8) ln_errold = bank_ln_errold = ln_qoldinit = series_ln((double)qoldinit);
+    if constexpr (sizeof(CT) == 8) ln_qoldinit = series_ln((double)qoldinit);
     bool do_error_check = true;
     long long iter = 0, success_iter = 0;
     bool accept = false, next_tstop = false;
-    // a NaN span is not stepped
-    int rc = (tf >= t0) ? RC_DEFAULT : RC_INITIALFAILURE;
+    int rc = RC_DEFAULT;
 
     // _savevalues! (integrator_utils.jl:340-414) after an accepted step: saveat
     // points up to t by the step's interpolant, then the every-step save; true
@@ -734,7 +716,125 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
     // (handle_tstop!, integrator_utils.jl:1290-1313); NaNs and out-of-order
     // entries are dropped the same way.
     int itst = 0;
-    while (t < tf) {
+
+    // Load trajectory j: its state, parameters, span and tolerances, the start
+    // save, the method's initialisation and the initial step; every piece of
+    // per-trajectory state starts afresh.
+    auto start = [&]() {
+#pragma unroll
+        for (int c = 0; c < C; ++c) Acc<R>::split(a.u0[(size_t)(g.lane * C + c) * N + j], u[c], ulo[c]);
+#pragma unroll
+        for (int i = 0; i < NP; ++i) p[i] = make_param<R>(a.p[(size_t)i * N + j]);
+        bwd = a.tspan[N + j] < a.tspan[j];
+        bm = bwd ? -1 : 0;
+        t0 = TM(a.tspan[j]);
+        tf = TM(a.tspan[N + j]);
+        dtmax = a.dtmax > 0 ? a.dtmax : tf - t0;
+        abstol = (R)(a.abstol_traj ? a.abstol_traj[j] : a.abstol);
+        reltol = (R)(a.reltol_traj ? a.reltol_traj[j] : a.reltol);
+        beta1 = (CT)K.beta1;
+        beta2 = (CT)K.beta2;
+        qsteady_max = (CT)K.qsteady_max;
+        st = StepStats{0, 0, 0, 0, 0, 0};
+        nsaved = 0;
+        isave = 0;
+        last_saved_t = dnan();
+        // saveat entries outside (t0, tf] are skipped (initialize_saveat, solve.jl:1103-1124)
+        while (isave < a.nsave && !(saveat_at(isave) > t0)) isave++;
+#pragma unroll
+        for (int c = 0; c < C; ++c) { uprev[c] = u[c]; uprevlo[c] = ulo[c]; }
+        if (a.save_start) {
+            if (a.k_out) save_dense(false);
+            save_point(t0, u, ulo);
+        }
+        t = t0;
+        tprev = t0;
+        Alg::template initialize<Model, R, L, C>(cache, u, p, TM(t), g, st, a, j);
+        if (!a.adaptive) {
+            dt = fabs(a.dt);   // fixed steps: no initial-step heuristic (handle_dt!, solve.jl:968-985)
+        } else if (a.dt > 0) {
+            dt = a.dt;
+        } else {
+            // the initial step's dtmax is at most the distance to the first tstop
+            // (_determine_initdt, integrator_interface.jl:644-656)
+            int k0 = 0;
+            while (k0 < a.ntstops && !(tstop_at(k0) > t0)) k0++;
+            const double first_tstop = (k0 < a.ntstops && tstop_at(k0) < tf) ? tstop_at(k0) : tf;
+            dt = initdt<Model, R, L, C, Alg::ORDER>(u, p, TM(t), bwd, jmin(fabs(dtmax), fabs(first_tstop - t0)),
+                                                     a.dtmin, abstol, reltol, Alg::template fsal_slot<R, C>(cache), g);
+            st.nf += 2;
+        }
+        dtpropose = dt;
+        EEst = CT(1);
+        q11 = CT(1);
+        errold = qoldinit;
+        bank_errold = qoldinit;
+        bank_q11 = CT(1);
+        ln_errold = bank_ln_errold = ln_qoldinit;
+        do_error_check = true;
+        iter = 0;
+        success_iter = 0;
+        accept = false;
+        next_tstop = false;
+        rc = (tf >= t0) ? RC_DEFAULT : RC_INITIALFAILURE;   // a NaN span is not stepped
+        ev_last = false;
+        terminated = false;
+        last_event_error = 0.0;
+        prev_mask = 0;
+        itst = 0;
+    };
+
+    // The trajectory in hand has ended: the endpoint save
+    // (solution_endpoint_match_cur_integrator!) and its counts, retcode and stats.
+    auto finish = [&]() {
+        if (rc == RC_DEFAULT) rc = RC_SUCCESS;
+        if (a.save_end) {
+            bool need;
+            if (nsaved == 0) {
+                need = true;
+            } else {
+                bool in_saveat = false;
+                if (a.saveat_given && !a.saveat_scalar)
+                    for (int s = 0; s < a.nsave; ++s) in_saveat = in_saveat || (saveat_at(s) == t);
+                need = last_saved_t != t && (a.save_end_user == 1 || in_saveat || t == tf || !a.saveat_given);
+            }
+            if (need) {
+                if (a.k_out) save_dense(st.naccept > 0);
+                save_point(t, u, ulo);
+            }
+        }
+        if (g.lane == 0) {
+            a.nsaved[j] = nsaved < a.nsave_cap ? nsaved : a.nsave_cap;
+            a.retcode[j] = rc;
+            if (a.stats) {
+                OdeStatsDev* s = a.stats + j;
+                s->nf = st.nf; s->njacs = st.njacs; s->nw = st.nw; s->nsolve = st.nsolve;
+                s->naccept = st.naccept; s->nreject = st.nreject;
+            }
+        }
+    };
+
+    // One step attempt per iteration for every group of the warp that holds a
+    // trajectory; a group whose trajectory ended finishes it and loads the next.
+    bool done = true;   // no trajectory in hand
+    for (;;) {
+        // the idle lanes of the warp take their next trajectories together once
+        // a.refill_lanes of them are idle (or all are): loading one runs the
+        // initial-step probe and the method's start, which the stepping lanes would
+        // otherwise wait through once per trajectory.  Lanes also leave the loop
+        // only together: a warp whose lanes left one by one ran the mixed
+        // Robertson solve 3% slower than one that keeps them to the end.
+        const unsigned live = __activemask();
+        const unsigned idle = __ballot_sync(live, done);
+        if (done) {
+            if (__popc(idle) < a.refill_lanes && idle != live) continue;
+            if (j >= 0) finish();
+            j = next();
+            if (j < 0) break;
+            start();
+            done = !(t < tf);
+            continue;
+        }
         // ---- loopheader!
         while (itst < a.ntstops && !(tstop_at(itst) > t)) itst++;
         const double tnext = (itst < a.ntstops && tstop_at(itst) < tf) ? tstop_at(itst) : tf;   // first_tstop
@@ -782,7 +882,7 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
         // fix_dt_at_bounds!  (backward the reference takes min(dt, dtmin) of a negative
         // dt and a positive dtmin: the lower bound applies forward only)
         dt = pmin(dtmax, dt);
-        if (!bwd) dt = pmax(dt, pabs(pmax(peps(t), a.dtmin)));
+        dt = pmax(dt, __longlong_as_double(abs_bits(pmax(peps(t), a.dtmin)) & ~(long long)bm));
         {   // modify_dt_for_tstops!  (fixed steps: the given dt, dtcache, clipped instead;
             // without one, every step runs to the next tstop)
             const double tol = ptol100(pmax(pabs(t), pabs(tnext)));
@@ -812,7 +912,11 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             }
             if (e == RC_SUCCESS && a.abort_flag != nullptr && (iter & 63) == 0 && *a.abort_flag != 0)
                 e = RC_ABORTED;
-            if (e != RC_SUCCESS) { rc = e; break; }
+            if (e != RC_SUCCESS) {
+                rc = e;
+                done = true;
+                continue;
+            }
         }
         // ---- perform_step! (skipped for a step below eps(t) onto the tstop)
         if (!(next_tstop && plt(pabs(dt), peps(t)))) {
@@ -898,37 +1002,13 @@ __device__ void solve_trajectory(const EnsembleArgs& a, long long j, const Group
             Alg::template after_save<R, C>(cache);
             if (terminated) {   // terminate! (ReturnCode.Terminated)
                 rc = RC_TERMINATED;
-                break;
+                done = true;
+                continue;
             }
         } else {
             st.nreject++;
         }
-    }
-    if (rc == RC_DEFAULT) rc = RC_SUCCESS;
-    // ---- endpoint save (solution_endpoint_match_cur_integrator!)
-    if (a.save_end) {
-        bool need;
-        if (nsaved == 0) {
-            need = true;
-        } else {
-            bool in_saveat = false;
-            if (a.saveat_given && !a.saveat_scalar)
-                for (int s = 0; s < a.nsave; ++s) in_saveat = in_saveat || (saveat_at(s) == t);
-            need = last_saved_t != t && (a.save_end_user == 1 || in_saveat || t == tf || !a.saveat_given);
-        }
-        if (need) {
-            if (a.k_out) save_dense(st.naccept > 0);
-            save_point(t, u, ulo);
-        }
-    }
-    if (g.lane == 0) {
-        a.nsaved[j] = nsaved < a.nsave_cap ? nsaved : a.nsave_cap;
-        a.retcode[j] = rc;
-        if (a.stats) {
-            OdeStatsDev* s = a.stats + j;
-            s->nf = st.nf; s->njacs = st.njacs; s->nw = st.nw; s->nsolve = st.nsolve;
-            s->naccept = st.naccept; s->nreject = st.nreject;
-        }
+        done = !(t < tf);
     }
 }
 
@@ -946,20 +1026,20 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 && C <= 4) ? ODEGB_MIN_BL
     ensemble_kernel(EnsembleArgs a) {
     Group<L> g;
     const long long gid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / L;
-    if (!a.persistent) {
-        if (gid >= a.count) return;
-        long long j = a.order ? a.order[gid] : gid;
-        solve_trajectory<Alg, Model, R, L, C>(a, j, g);
-        return;
-    }
-    for (;;) {
-        unsigned long long idx = 0;
-        if (g.lane == 0) idx = atomicAdd(a.queue, 1ull);
-        idx = g.bcast(idx, 0);
-        if (idx >= (unsigned long long)a.count) break;
-        long long j = a.order ? a.order[idx] : (long long)idx;
-        solve_trajectory<Alg, Model, R, L, C>(a, j, g);
-    }
+    bool first = true;
+    solve_trajectories<Alg, Model, R, L, C>(a, g, [&]() -> long long {
+        unsigned long long idx;
+        if (!a.persistent) {   // static: this group's own trajectory, once
+            idx = first ? (unsigned long long)gid : ~0ull;
+            first = false;
+        } else {               // persistent: the next index of the device queue
+            idx = 0;
+            if (g.lane == 0) idx = atomicAdd(a.queue, 1ull);
+            idx = g.bcast(idx, 0);
+        }
+        if (idx >= (unsigned long long)a.count) return -1;
+        return a.order ? a.order[idx] : (long long)idx;
+    });
 }
 
 // Uneven-size ensembles in ONE persistent launch.  Trajectories were bucketed
@@ -973,13 +1053,12 @@ template <class Alg, class Model, class R, int L, int C>
 __device__ __forceinline__ void drain_class(const EnsembleArgs& a, int cls) {
     Group<L> g;
     const unsigned long long cnt = a.class_count[cls], off = a.class_offset[cls];
-    for (;;) {
+    solve_trajectories<Alg, Model, R, L, C>(a, g, [&]() -> long long {
         unsigned long long idx = 0;
         if (g.lane == 0) idx = atomicAdd(a.class_next + cls, 1ull);
         idx = g.bcast(idx, 0);
-        if (idx >= cnt) break;
-        solve_trajectory<Alg, Model, R, L, C>(a, a.order[off + idx], g);
-    }
+        return idx < cnt ? a.order[off + idx] : -1;
+    });
     __syncwarp();
 }
 

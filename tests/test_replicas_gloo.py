@@ -36,9 +36,12 @@ def _worker(rank, world, port, mode, q):
                 os._exit(3)
             try:
                 bench.max_over_ranks(1.0, dist)
-                q.put((r, "no error", None, None))
+                msg = (r, "no error", None, None)
             except Exception as e:   # noqa: BLE001 - any collective failure is the expected outcome
-                q.put((r, "error", type(e).__name__, None))
+                msg = (r, "error", type(e).__name__, None)
+            q.put(msg)
+            q.close()
+            q.join_thread()   # the message is in the pipe before the hard exit
             os._exit(0)
         dist.destroy_process_group()
     except Exception as e:   # noqa: BLE001
