@@ -112,7 +112,7 @@ def run_serving(args, rank, local):
 # capture (dram__bytes_read.sum + dram__bytes_write.sum) of the same kernel on
 # the full 100,000-trajectory Robertson ensemble.  Filled in only for kernels
 # captured at the benchmarked size; every other kernel reports null.
-NCU_TRAFFIC = {("robertson", "fp64"): 18.73e6, ("robertson", "mixed"): 18.70e6}
+NCU_TRAFFIC = {("robertson", "fp64"): 18.22e6, ("robertson", "mixed"): 17.04e6}
 METRIC = "trajectories/sec at equal accuracy, mixed vs plain FP64 GPU; p50/p99 latency"
 
 
