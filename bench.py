@@ -366,11 +366,14 @@ def measure(cfg, args, ctx, steps, warmup, headline=False):
     st_out = torch.empty((N, 6), dtype=torch.int64, device=dev)
     ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None
     ir_default = wl.get("ir_sweeps", -1)
+    fwd_spans = int(bool(np.all(wl["tspan"][1] >= wl["tspan"][0])))
 
     def solve_device(prec, ir=None, u0=None, p=None):
         ens = odegb300.EnsembleGB300(precision=prec, ir_sweeps=(ir_default if ir is None else ir)
                                      if prec == "mixed" else -1, lanes_per_traj=args.lanes)
         o = _options(wl["reltol"], wl["abstol"], None, None, None, 1000000, sv, ens, None, None, cb)
+        # the device entry point cannot see the spans: the caller states that all run forward
+        o.forward_only = fwd_spans
         if t_tst is not None:   # the device entry point takes tstops in device memory, sorted
             o.ntstops = int(t_tst.numel())
             o.tstops = C.cast(C.c_void_p(t_tst.data_ptr()), C.POINTER(C.c_double))

@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define ODE_ABI_VERSION 5
+#define ODE_ABI_VERSION 6
 
 typedef struct ode_handle ode_handle;
 
@@ -202,7 +202,11 @@ typedef struct {
                                    land on the tstops and tf; with dt = 0 (then tstops are required)
                                    every step runs to the next tstop (the reference's adaptive = false:
                                    no error estimate is judged, every step is accepted) */
-    int32_t reserved4;
+    int32_t forward_only;       /* 1: the caller guarantees tf >= t0 for every trajectory, so the kernels'
+                                   forward-only forms (no integration direction in their step loops) may
+                                   run; a backward span then reports ODE_RC_INITIALFAILURE.  0 (default):
+                                   either direction.  The host entry points (ode_solve_ensemble, _dense,
+                                   ode_submit) find it out themselves from the host spans */
 } ode_options;
 
 /* Fill o with the reference's defaults. */

@@ -51,6 +51,7 @@ struct EnsembleArgs {
     double qmax_first_step, qmax;
     int ir_sweeps;          // mixed Rosenbrock: refinement sweeps per solve
     int adaptive;           // 0: fixed steps of dt, every step accepted
+    int forward_only;       // every span runs forward: the kernel's forward-only form may run
     int max_jac_age;        // Rosenbrock23: J kept for at most this many accepted steps (<= 1: never kept)
     double jac_reuse_gamma_tol;  // ... while |dtgamma / dtgamma_J - 1| <= this
     // scheduling

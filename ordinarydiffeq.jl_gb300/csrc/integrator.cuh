@@ -326,8 +326,10 @@ __device__ double initdt(const R* u0, const PR<R>* p, double t, bool bwd, double
 // trajectory ends (the trajectories of a warp differ in step counts by up to
 // the ratio of their spans or stiffness).  Every trajectory's arithmetic is
 // the same whichever group and slot runs it.  Alg provides the cache, the
-// step, the interpolant and the FSAL hooks.
-template <class Alg, class Model, class R, int L, int C, class Next>
+// step, the interpolant and the FSAL hooks.  FWD: the caller guarantees
+// forward spans (tf >= t0) and the loop carries no direction at all; a
+// backward span then reports InitialFailure, as a NaN span does.
+template <class Alg, class Model, class R, int L, int C, bool FWD, class Next>
 __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Next next) {
     using CT = typename Ctl<R>::T;
     constexpr int NP = Model::NP;
@@ -725,8 +727,10 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
         for (int c = 0; c < C; ++c) Acc<R>::split(a.u0[(size_t)(g.lane * C + c) * N + j], u[c], ulo[c]);
 #pragma unroll
         for (int i = 0; i < NP; ++i) p[i] = make_param<R>(a.p[(size_t)i * N + j]);
-        bwd = a.tspan[N + j] < a.tspan[j];
-        bm = bwd ? -1 : 0;
+        if constexpr (!FWD) {
+            bwd = a.tspan[N + j] < a.tspan[j];
+            bm = bwd ? -1 : 0;
+        }
         t0 = TM(a.tspan[j]);
         tf = TM(a.tspan[N + j]);
         dtmax = a.dtmax > 0 ? a.dtmax : tf - t0;
@@ -1015,7 +1019,7 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
 // Ensemble kernel: static (one trajectory per group, the plain one-kernel-per-
 // ensemble form) or persistent (groups pop trajectory indices from a device
 // counter until the ensemble is exhausted).
-template <class Alg, class Model, class R, int L, int C>
+template <class Alg, class Model, class R, int L, int C, bool FWD = false>
 // Mixed kernels with up to 4 states per lane are held to 3 resident blocks of
 // 128 (<= 170 registers; measured 10% faster than 2 on Robertson, no spills);
 // wider or FP64 kernels keep their registers.
@@ -1027,7 +1031,7 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 && C <= 4) ? ODEGB_MIN_BL
     Group<L> g;
     const long long gid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / L;
     bool first = true;
-    solve_trajectories<Alg, Model, R, L, C>(a, g, [&]() -> long long {
+    solve_trajectories<Alg, Model, R, L, C, FWD>(a, g, [&]() -> long long {
         unsigned long long idx;
         if (!a.persistent) {   // static: this group's own trajectory, once
             idx = first ? (unsigned long long)gid : ~0ull;
@@ -1049,11 +1053,11 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 && C <= 4) ? ODEGB_MIN_BL
 // group that finishes a trajectory refills at once and the load balances
 // across classes.  At a class change the warp regroups its lanes (L depends
 // on the class), which needs the whole warp: __syncwarp between classes.
-template <class Alg, class Model, class R, int L, int C>
+template <class Alg, class Model, class R, int L, int C, bool FWD>
 __device__ __forceinline__ void drain_class(const EnsembleArgs& a, int cls) {
     Group<L> g;
     const unsigned long long cnt = a.class_count[cls], off = a.class_offset[cls];
-    solve_trajectories<Alg, Model, R, L, C>(a, g, [&]() -> long long {
+    solve_trajectories<Alg, Model, R, L, C, FWD>(a, g, [&]() -> long long {
         unsigned long long idx = 0;
         if (g.lane == 0) idx = atomicAdd(a.class_next + cls, 1ull);
         idx = g.bcast(idx, 0);
@@ -1068,14 +1072,14 @@ __device__ __forceinline__ void drain_class(const EnsembleArgs& a, int cls) {
 #ifndef ODEGB_MIN_BLOCKS_FUSED_F32
 #define ODEGB_MIN_BLOCKS_FUSED_F32 3
 #endif
-template <class Alg, class Model, class R, int C>
+template <class Alg, class Model, class R, int C, bool FWD = false>
 __global__ void __launch_bounds__(128, sizeof(R) == 4 ? ODEGB_MIN_BLOCKS_FUSED_F32 : 1) fused_class_kernel(EnsembleArgs a) {
     static_assert(C == 2 || C == 4, "class layouts hold 2 or 4 states per lane");
-    drain_class<Alg, Model, R, 64 / C, C>(a, 4);
-    drain_class<Alg, Model, R, 32 / C, C>(a, 3);
-    drain_class<Alg, Model, R, 16 / C, C>(a, 2);
-    drain_class<Alg, Model, R, 8 / C, C>(a, 1);
-    drain_class<Alg, Model, R, 4 / C, C>(a, 0);
+    drain_class<Alg, Model, R, 64 / C, C, FWD>(a, 4);
+    drain_class<Alg, Model, R, 32 / C, C, FWD>(a, 3);
+    drain_class<Alg, Model, R, 16 / C, C, FWD>(a, 2);
+    drain_class<Alg, Model, R, 8 / C, C, FWD>(a, 1);
+    drain_class<Alg, Model, R, 4 / C, C, FWD>(a, 0);
 }
 
 }  // namespace odegb

@@ -14,7 +14,11 @@ namespace odegb {
      [](const EnsembleArgs& a, int g, int b, size_t s, cudaStream_t st) {                          \
          launch_kernel(fused_class_kernel<Vern7Alg, MODEL, R, C>, a, g, b, s, st);                     \
      },                                                                                            \
-     "vern7-classes/" #MODEL "/" #R "/C" #C}
+     "vern7-classes/" #MODEL "/" #R "/C" #C,                                                        \
+     (const void*)fused_class_kernel<Vern7Alg, MODEL, R, C, true>,                                   \
+     [](const EnsembleArgs& a, int g, int b, size_t s, cudaStream_t st) {                          \
+         launch_kernel(fused_class_kernel<Vern7Alg, MODEL, R, C, true>, a, g, b, s, st);              \
+     }}
 
 static const FusedVariant kFused[] = {
     FUSED(Duffing, M_DUFFING, double, 0, 4),

@@ -12,6 +12,17 @@ namespace odegb {
      },                                                                                             \
      "rodas5p/" #MODEL "/" #R "/L" #L "C" #C}
 #define BOTH(MODEL, MID, L, C) VAR(MODEL, MID, double, 0, L, C), VAR(MODEL, MID, float, 1, L, C)
+// with the forward-only form (benchmarked workloads: a second copy of the step loop)
+#define VARF(MODEL, MID, R, PREC, L, C)                                                             \
+    {2, MID, PREC, (L) * (C), L, 0, (const void*)ensemble_kernel<Rodas5PAlg, MODEL, R, L, C>,        \
+     [](const EnsembleArgs& a, int g, int b, size_t s, cudaStream_t st) {                           \
+         launch_kernel(ensemble_kernel<Rodas5PAlg, MODEL, R, L, C>, a, g, b, s, st);                 \
+     },                                                                                             \
+     "rodas5p/" #MODEL "/" #R "/L" #L "C" #C,                                                       \
+     (const void*)ensemble_kernel<Rodas5PAlg, MODEL, R, L, C, true>,                                \
+     [](const EnsembleArgs& a, int g, int b, size_t s, cudaStream_t st) {                           \
+         launch_kernel(ensemble_kernel<Rodas5PAlg, MODEL, R, L, C, true>, a, g, b, s, st);           \
+     }}
 
 static const KernelVariant kVariants[] = {
     BOTH(BouncingBall, M_BOUNCING_BALL, 1, 2),
@@ -19,7 +30,8 @@ static const KernelVariant kVariants[] = {
     BOTH(PKOneCompartment, M_PK1, 1, 2),
     BOTH(ForcedDuffing, M_FORCED_DUFFING, 1, 2),
     BOTH(Linear, M_LINEAR, 1, 1), BOTH(Linear, M_LINEAR, 1, 2),
-    BOTH(Lorenz, M_LORENZ, 1, 3), BOTH(Robertson, M_ROBERTSON, 1, 3),
+    BOTH(Lorenz, M_LORENZ, 1, 3),
+    VARF(Robertson, M_ROBERTSON, double, 0, 1, 3), VARF(Robertson, M_ROBERTSON, float, 1, 1, 3),
     BOTH(Duffing, M_DUFFING, 1, 4),
 };
 

@@ -121,13 +121,30 @@ const KernelVariant* variant_for(const ode_problem_desc* d, int lanes, int* rc, 
 
 // Launch one ensemble kernel: through its typed launcher, or (a registered
 // model's run-time compiled kernel) through cudaLaunchKernel.
+// The kernel a launch runs: the forward-only form when every span runs forward
+// and the variant has one.
+const void* kernel_fn(const KernelVariant* v, const EnsembleArgs& a) {
+    return a.forward_only && v->fwd_fn ? v->fwd_fn : v->fn;
+}
+
 void launch_any(const KernelVariant* v, const EnsembleArgs& a, int grid, int block, size_t smem, cudaStream_t s) {
+    if (a.forward_only && v->fwd_launch) {
+        v->fwd_launch(a, grid, block, smem, s);
+        return;
+    }
     if (v->launch) {
         v->launch(a, grid, block, smem, s);
         return;
     }
     void* args[] = {const_cast<EnsembleArgs*>(&a)};
     cudaLaunchKernel(v->fn, dim3(grid), dim3(block), args, smem, s);
+}
+
+// Every span of a host tspan array runs forward (tf >= t0; NaN is not).
+bool all_forward(const double* tspan, int64_t N) {
+    for (int64_t j = 0; j < N; ++j)
+        if (!(tspan[N + j] >= tspan[j])) return false;
+    return true;
 }
 
 struct DevBuf {
@@ -367,6 +384,7 @@ EnsembleArgs make_args(ode_handle* h, const ode_problem_desc* d, const ode_optio
     a.max_jac_age = o->max_jac_age;
     a.jac_reuse_gamma_tol = o->jac_reuse_gamma_tol < 0 ? 0.03 : o->jac_reuse_gamma_tol;
     a.adaptive = o->adaptive ? 1 : 0;
+    a.forward_only = o->forward_only ? 1 : 0;
     a.save_idxs = o->nsave_idxs > 0 ? o->save_idxs : nullptr;   // device memory at this point
     a.nsave_rows = o->nsave_idxs > 0 ? o->nsave_idxs : 0;
     a.t_out = t_out;
@@ -503,7 +521,8 @@ cudaError_t launch_fused(const FusedVariant* fv, EnsembleArgs a, unsigned long l
                          cudaStream_t s) {
     const int block = 128;
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fv->fn, block, 0);
+    const bool fwd = a.forward_only && fv->fwd_fn;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fwd ? fv->fwd_fn : fv->fn, block, 0);
     if (e != cudaSuccess) return e;
     if (per_sm <= 0) per_sm = 1;
     long long want = (a.count * 16 + block - 1) / block;   // enough groups for the largest class
@@ -513,7 +532,7 @@ cudaError_t launch_fused(const FusedVariant* fv, EnsembleArgs a, unsigned long l
     a.class_count = ctr + kOffCounts;
     a.class_offset = ctr + kOffOffsets;
     a.class_next = ctr + kOffNext;
-    fv->launch(a, grid, block, 0, s);
+    (fwd ? fv->fwd_launch : fv->launch)(a, grid, block, 0, s);
     return cudaGetLastError();
 }
 constexpr int kBlock = 128;
@@ -535,6 +554,8 @@ cudaError_t launch_geometry(const KernelVariant* v, int block, int* block_out, s
     const size_t smem = (size_t)(block / v->lanes) * (size_t)v->smem_per_group;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(v->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess && v->fwd_fn)
+            e = cudaFuncSetAttribute(v->fwd_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
     *block_out = block;
@@ -555,7 +576,7 @@ int launch_variant(ode_handle* h, const KernelVariant* v, EnsembleArgs a, int sc
     int grid;
     if (persistent) {
         int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v->fn, block, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel_fn(v, a), block, smem);
         if (per_sm <= 0) per_sm = 1;
         long long want = (groups * v->lanes + block - 1) / block;
         grid = (int)std::min<long long>((long long)per_sm * h->sm_count, want);
@@ -929,6 +950,7 @@ int solve_host(ode_handle* h, const ode_problem_desc* d, const ode_options* o, i
     *h->h_abort = 0;
     ode_options ostaged;
     if ((rc = stage_tstops(h, o, h->main.stream, &ostaged))) return rc;
+    if (!ostaged.forward_only && N > 0) ostaged.forward_only = all_forward(tspan, N) ? 1 : 0;
     o = &ostaged;
     if (N > 0) {   // every buffer page-locked: the kernels work in place, no staging copies
         const double *mu0 = mapped_ptr(u0), *mp = mapped_ptr(p), *mts = mapped_ptr(tspan);
@@ -1566,6 +1588,7 @@ int ode_submit(ode_handle* h, const ode_problem_desc* d, const ode_options* o, i
     r->u0.assign(u0, u0 + n * N);
     r->p.assign(p, p + np * N);
     r->tspan.assign(tspan, tspan + 2 * N);
+    if (!r->o.forward_only && N > 0) r->o.forward_only = all_forward(tspan, N) ? 1 : 0;
     if (o->nsave > 0) r->saveat.assign(saveat, saveat + (size_t)o->nsave * (o->saveat_per_traj ? (size_t)N : 1));
     if (npt) r->npt.assign(npt, npt + N);
     r->t_out = t_out;
@@ -1711,6 +1734,7 @@ int ode_autotune(ode_handle* h, const ode_problem_desc* d, const ode_options* o,
     *h->h_abort = 0;
     ode_options ostaged;
     if ((rc = stage_tstops(h, o, h->main.stream, &ostaged))) return rc;
+    if (!ostaged.forward_only) ostaged.forward_only = all_forward(tspan, N) ? 1 : 0;
     o = &ostaged;
     const size_t n = (size_t)d->n_states, np = (size_t)d->n_params, cap = save_cap(o), rows = out_rows(d, o);
     const size_t nsv = (size_t)o->nsave * (o->saveat_per_traj ? (size_t)N : 1);
@@ -1887,7 +1911,7 @@ int noalloc_launch(const KernelVariant* v, EnsembleArgs a, unsigned long long* q
     cudaError_t e = launch_geometry(v, 0, &block, &smem);
     if (e != cudaSuccess) return fail(nullptr, ODE_E_CUDA, std::string("shared memory: ") + cudaGetErrorString(e));
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v->fn, block, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel_fn(v, a), block, smem);
     if (e != cudaSuccess) return fail(nullptr, ODE_E_CUDA, std::string("occupancy: ") + cudaGetErrorString(e));
     if (per_sm <= 0) per_sm = 1;
     long long want = (a.count * v->lanes + block - 1) / block;
@@ -1955,6 +1979,7 @@ extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_o
     a.max_jac_age = o->max_jac_age;
     a.jac_reuse_gamma_tol = o->jac_reuse_gamma_tol < 0 ? 0.03 : o->jac_reuse_gamma_tol;
     a.adaptive = o->adaptive ? 1 : 0;
+    a.forward_only = o->forward_only ? 1 : 0;
     a.save_idxs = o->nsave_idxs > 0 ? o->save_idxs : nullptr;   // device memory at this point
     a.nsave_rows = o->nsave_idxs > 0 ? o->nsave_idxs : 0;
     a.t_out = t_out;

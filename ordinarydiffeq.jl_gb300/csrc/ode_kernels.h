@@ -21,6 +21,9 @@ struct KernelVariant {
     const void* fn;         // __global__ function
     void (*launch)(const EnsembleArgs&, int grid, int block, size_t smem, cudaStream_t);
     const char* name;
+    // the same kernel for forward spans only (no direction in its step loop), or null
+    const void* fwd_fn;
+    void (*fwd_launch)(const EnsembleArgs&, int grid, int block, size_t smem, cudaStream_t);
 };
 
 // One launch integrating every size class of an uneven ensemble.
@@ -29,6 +32,8 @@ struct FusedVariant {
     const void* fn;
     void (*launch)(const EnsembleArgs&, int grid, int block, size_t smem, cudaStream_t);
     const char* name;
+    const void* fwd_fn;   // forward spans only, or null
+    void (*fwd_launch)(const EnsembleArgs&, int grid, int block, size_t smem, cudaStream_t);
 };
 
 // Dense-output evaluation sol(t) at query times (device pointers):

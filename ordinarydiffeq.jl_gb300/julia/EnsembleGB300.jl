@@ -103,7 +103,7 @@ mutable struct Options
     callback::Int32; interp_points::Int32; max_events::Int32; ntstops::Int32; tstops::Ptr{Float64}
     max_jac_age::Int32; reserved2::Int32; jac_reuse_gamma_tol::Float64
     nsave_idxs::Int32; reserved3::Int32; save_idxs::Ptr{Int32}
-    adaptive::Int32; reserved4::Int32
+    adaptive::Int32; forward_only::Int32
 end
 # the W-method Jacobian reuse knobs of Rosenbrock23(max_jac_age, jac_reuse_gamma_tol)
 jac_reuse(alg::Rosenbrock23) = (Int32(alg.max_jac_age), Float64(alg.jac_reuse_gamma_tol))

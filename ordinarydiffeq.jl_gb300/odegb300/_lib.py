@@ -42,7 +42,7 @@ class Options(C.Structure):
                 ("ntstops", C.c_int32), ("tstops", C.POINTER(C.c_double)),
                 ("max_jac_age", C.c_int32), ("reserved2", C.c_int32), ("jac_reuse_gamma_tol", C.c_double),
                 ("nsave_idxs", C.c_int32), ("reserved3", C.c_int32), ("save_idxs", C.POINTER(C.c_int32)),
-                ("adaptive", C.c_int32), ("reserved4", C.c_int32)]
+                ("adaptive", C.c_int32), ("forward_only", C.c_int32)]
 
 
 class Stats(C.Structure):
