@@ -165,9 +165,11 @@ typedef struct {
     int32_t block_size;         /* 0: tuned */
     int32_t ir_sweeps;          /* MIXED Rodas5P refinement sweeps (< 0: none) */
     int32_t save_everystep;     /* 1: save every accepted step, the reference's default without saveat
-                                   (integrator_utils.jl:397-404); needs nsave == 0 */
+                                   (integrator_utils.jl:397-404); with saveat points, both sets (each
+                                   step after the saveat points up to it, unless one landed on it) */
     int32_t max_step_saves;     /* save_everystep: step saves kept per trajectory; t_out/u_out hold
-                                   max_step_saves + 2 slots, and past that the last slot keeps the latest step */
+                                   nsave + max_step_saves + 2 slots, and past that the last slot keeps the
+                                   latest step */
     int32_t callback;           /* 1: the model's registered ContinuousCallback (models with an event;
                                    SciMLBase defaults: rootfind = LeftRootFind, save_positions = (true, true),
                                    abstol = 10eps(), repeat_nudge = 1//100, dtrelax = 1).  An event moves t

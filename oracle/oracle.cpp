@@ -1992,7 +1992,7 @@ int orc_solve_ensemble(int alg, int model, int nmax, const int32_t* n_per_traj, 
     if (nthreads <= 0) nthreads = (int)std::thread::hardware_concurrency();
     if (nthreads <= 0) nthreads = 1;
     // saves plus possible start and end saves, and two per event (before and after its affect)
-    int cap = (o->save_everystep ? o->max_step_saves : nsave) + 2 + (o->callback ? 2 * o->max_events : 0);
+    int cap = nsave + (o->save_everystep ? o->max_step_saves : 0) + 2 + (o->callback ? 2 * o->max_events : 0);
     std::atomic<int64_t> next(0);
     auto worker = [&]() {
         std::vector<double> uj(nmax), pj(np), sv(nsave > 0 ? nsave : 1), tl(cap), ul((size_t)cap * nmax);

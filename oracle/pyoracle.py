@@ -123,7 +123,7 @@ def solve(alg, model, u0, p, tspan, saveat=(), tstops=(), dense=False, **kw):
     if kw.get("saveat_given", True) is False or sv.size == 0:
         cap = 4
     if kw.get("save_everystep"):
-        cap = kw.get("max_step_saves", 0) + 2
+        cap = sv.size + kw.get("max_step_saves", 0) + 2
     if kw.get("callback"):
         cap += 2 * max(kw.get("max_events", 0), 64)
     t_out = np.zeros(cap)
@@ -188,7 +188,7 @@ def solve_ensemble(alg, model, u0, p, tspan, saveat, reltol, abstol, n_per_traj=
     sv = np.ascontiguousarray(saveat, dtype=np.float64)
     nmax, N = u0.shape
     nsave = sv.shape[0]
-    cap = (kw.get("max_step_saves", 0) if kw.get("save_everystep") else nsave) + 2 + \
+    cap = nsave + (kw.get("max_step_saves", 0) if kw.get("save_everystep") else 0) + 2 + \
         (2 * kw.get("max_events", 0) if kw.get("callback") else 0)
     t_out = np.full((cap, N), np.nan)
     u_out = np.full((cap, nmax, N), np.nan)

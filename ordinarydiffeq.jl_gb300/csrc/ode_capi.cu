@@ -276,8 +276,6 @@ int check_problem(const ode_problem_desc* d, const ode_options* o, int64_t N, co
         return bad(ODE_E_INVALID, "interp_points and max_events must be >= 0");
     if (!(o->reltol > 0) || !(o->abstol >= 0)) return bad(ODE_E_INVALID, "tolerances must be positive");
     if (o->nsave < 0) return bad(ODE_E_INVALID, "negative nsave");
-    if (o->save_everystep && o->nsave > 0)
-        return bad(ODE_E_UNSUPPORTED, "save_everystep together with saveat is not supported");
     if (o->save_everystep && o->max_step_saves <= 0)
         return bad(ODE_E_INVALID, "save_everystep needs max_step_saves > 0");
     if (o->ntstops < 0 || (o->ntstops > 0 && !o->tstops))
@@ -357,7 +355,8 @@ int stage_tstops(ode_handle* h, const ode_options* o, cudaStream_t s, ode_option
 // Output slots per trajectory: the saveat points (or the kept step saves)
 // plus the start and end saves.
 size_t save_cap(const ode_options* o) {
-    return (size_t)(o->save_everystep ? o->max_step_saves : o->nsave) + 2 + (o->callback ? 2 * (size_t)o->max_events : 0);
+    return (size_t)o->nsave + (o->save_everystep ? (size_t)o->max_step_saves : 0) + 2 +
+           (o->callback ? 2 * (size_t)o->max_events : 0);
 }
 
 EnsembleArgs make_args(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int64_t N,

@@ -207,9 +207,10 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem,
     t0, tf = probs[1].tspan
     sd = (tf < t0 ? -1 : 1) * abs(saveat isa Number ? saveat : 0.0)
     sv = scalar ? sort(collect(t0 + sd:sd:tf)) : sort(collect(Float64, saveat))
-    ss = save_start === nothing ? (isempty(saveat) || scalar || probs[1].tspan[1] in sv) : save_start
-    se = save_end === nothing ? (isempty(saveat) || scalar || probs[1].tspan[2] in sv) : save_end
-    everystep = save_everystep && isempty(sv)
+    ss = save_start === nothing ? (save_everystep || isempty(saveat) || scalar || probs[1].tspan[1] in sv) :
+         save_start
+    se = save_end === nothing ? (save_everystep || isempty(saveat) || scalar || probs[1].tspan[2] in sv) : save_end
+    everystep = save_everystep   # with saveat too: both sets are kept (_savevalues!)
     callback === nothing || callback isa GB300Callback ||
         error("EnsembleGB300 runs the model's registered callback only: pass GB300Callback(...)")
     cb = callback isa GB300Callback
@@ -226,7 +227,7 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem,
                 jac_reuse(alg)[2], length(sidx), Int32(0), isempty(sidx) ? Ptr{Int32}(C_NULL) : pointer(sidx),
                 Int32(adaptive), Int32(0))
     d = ProblemDesc(model, alg_id(alg), n, npar, ens.precision === :mixed ? 1 : 0, 0)
-    cap = (everystep ? max_step_saves : length(sv)) + 2 + (cb ? 2 * callback.max_events : 0)
+    cap = length(sv) + (everystep ? max_step_saves : 0) + 2 + (cb ? 2 * callback.max_events : 0)
     t_out = fill(NaN, N, cap); u_out = fill(NaN, N, rows, cap)   # [(s*rows + i)*N + j] -> u_out[j, i, s]
     nsaved = zeros(Int32, N); rc = zeros(Int32, N); st = Vector{Stats}(undef, N)
     # dense output (solve.jl:145-146) for every-step saves of one state count

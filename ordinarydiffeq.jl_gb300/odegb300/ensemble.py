@@ -406,9 +406,9 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
                  dense=False, callback=None, tstops=None, save_idxs=None, adaptive=True):
     """Solve a packed ensemble.  u0s (n, N), ps (np, N), tspans (2, N).  Returns the
     raw structure-of-arrays outputs dict (t, u, nsaved, retcode, stats).
-    save_everystep (without saveat) keeps every accepted step, up to
-    max_step_saves per trajectory (past that the last slot holds the final
-    point and a warning is issued).  dense (with save_everystep) also keeps
+    save_everystep keeps every accepted step, up to max_step_saves per
+    trajectory (past that the last slot holds the final point and a warning is
+    issued), beside the saveat points if any.  dense (with save_everystep) also keeps
     each step's interpolation vectors, k (cap, nk, n, N), for dense_eval.
     callback: the model's ContinuousCallback (ContinuousCallback(...)); a
     trajectory it terminates reports ReturnCode.Terminated.  tstops: times every
@@ -464,7 +464,7 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
         warnings.warn("some trajectories filled all %d save slots: raise max_events (their latest save is kept "
                       "in the last slot)" % cap)
     elif sv.everystep:
-        lost = int(np.sum(stats[:, 4] + int(sv.save_start) > cap))
+        lost = int(np.sum(stats[:, 4] + int(sv.save_start) + sv.nsave > cap))
         if lost:
             warnings.warn("%d trajectories took more than max_step_saves=%d steps; their middle steps were "
                           "dropped (the final point is kept)" % (lost, sv.max_step_saves))

@@ -8,8 +8,9 @@
   the rest).  The points are passed ascending whatever the direction.
 * Defaults (solve.jl:141-143, 596-599): save_start = isempty(saveat) || saveat is a
   number || t0 in saveat; save_end = isempty(saveat) || saveat is a number ||
-  tf in saveat.  Saving every step (empty saveat in the reference) is not
-  offered: without saveat only the start and end points are returned.
+  tf in saveat; save_everystep makes both true.  save_everystep with saveat
+  keeps both sets (_savevalues!: the saveat points up to t, then the step
+  unless a saveat point landed on it).
 """
 from dataclasses import dataclass
 from fractions import Fraction
@@ -85,24 +86,32 @@ class SaveSpec:
     save_start: bool
     save_end: bool
     save_end_user: int
-    everystep: bool = False      # save every accepted step (no saveat)
+    everystep: bool = False      # save every accepted step (beside the saveat points, if any)
     max_step_saves: int = 0      # step saves kept per trajectory when everystep
 
     @property
     def cap(self):
         """Output slots per trajectory: t_out is (cap, N), u_out (cap, n, N)."""
-        return (self.max_step_saves if self.everystep else self.nsave) + 2
+        return self.nsave + (self.max_step_saves if self.everystep else 0) + 2
 
 
 def resolve_saveat(saveat, tspans, save_start=None, save_end=None, save_everystep=False, max_step_saves=1024):
     """tspans: (2, N).  Returns the SaveSpec passed to the C ABI (a SaveSpec is
-    returned unchanged).  save_everystep (only without saveat) keeps every
-    accepted step, up to max_step_saves per trajectory."""
+    returned unchanged).  save_everystep keeps every accepted step, up to
+    max_step_saves per trajectory, beside the saveat points if any."""
     if isinstance(saveat, SaveSpec):
         return saveat
     no_saveat = saveat is None or (not np.isscalar(saveat) and np.size(saveat) == 0)
     if save_everystep and not no_saveat:
-        raise ValueError("save_everystep together with saveat is not supported")
+        if max_step_saves <= 0:
+            raise ValueError("save_everystep needs max_step_saves > 0")
+        # the saveat points as without it, with save_start and save_end true by default
+        sv = resolve_saveat(saveat, tspans, True if save_start is None else save_start,
+                            True if save_end is None else save_end)
+        sv.save_end_user = -1 if save_end is None else int(bool(save_end))
+        sv.everystep = True
+        sv.max_step_saves = int(max_step_saves)
+        return sv
     if save_everystep:
         if max_step_saves <= 0:
             raise ValueError("save_everystep needs max_step_saves > 0")

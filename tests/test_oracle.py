@@ -600,6 +600,31 @@ def test_backward_adaptive_with_a_tstop(alg):
     assert np.abs(r["u"] - ex).max() < 1e-3
 
 
+def _every(alg, tspan, saveat, **kw):
+    from odegb300.saveat import resolve_saveat
+    sv = resolve_saveat(saveat, np.array([[tspan[0]], [tspan[1]]]), save_everystep=True, max_step_saves=4096)
+    r = O.solve(alg, O.LINEAR, [0.5], [1.01], tspan, saveat=sv.values, save_start=sv.save_start,
+                save_end=sv.save_end, save_end_user=sv.save_end_user, saveat_given=sv.nsave > 0,
+                saveat_scalar=sv.scalar, save_everystep=True, max_step_saves=4096, **kw)
+    assert r["retcode"] == O.RC_SUCCESS
+    return r["t"]
+
+
+# test/InterfaceI/ode_saveat_tests.jl:44-124: save_everystep with saveat keeps both
+# sets; the saveat points are the only times not in the every-step solution
+@pytest.mark.parametrize("alg,kw", [(O.TSIT5, dict(adaptive=False)), (O.RODAS5P, {}), (O.ROSENBROCK23, {})])
+@pytest.mark.parametrize("tspan", [(0.0, 1.0), (1.0, 0.0)])
+def test_every_step_saves_with_saveat(alg, kw, tspan):
+    pts = [0.125, 0.6, 0.61, 0.8]
+    a = _every(alg, tspan, None, dt=0.25, **kw)
+    b = _every(alg, tspan, pts, dt=0.25, **kw)
+    assert sorted(set(b) ^ set(a)) == pts and len(b) == len(a) + len(pts)
+    assert np.all(np.diff(b) > 0) if tspan[1] > tspan[0] else np.all(np.diff(b) < 0)
+    # saveat points that are the endpoints add nothing (ode_saveat_tests.jl:99-106)
+    c = _every(alg, tspan, [0.0, 0.5, 1.0], dt=0.25, **kw)
+    assert sorted(set(c) ^ set(a)) == ([0.5] if 0.5 not in a else [])
+
+
 # test/InterfaceI/ode_saveat_tests.jl:5-42 on prob_reverse = (1.0, 0.0): the save times
 # mirror the forward ones
 def test_backward_saveat_rules():
