@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define ODE_ABI_VERSION 6
+#define ODE_ABI_VERSION 7
 
 typedef struct ode_handle ode_handle;
 
@@ -209,6 +209,14 @@ typedef struct {
                                    run; a backward span then reports ODE_RC_INITIALFAILURE.  0 (default):
                                    either direction.  The host entry points (ode_solve_ensemble, _dense,
                                    ode_submit) find it out themselves from the host spans */
+    /* The PI step-size controller's knobs (solve(...; controller = PIController(beta1, beta2;
+       qoldinit, qmin, gamma, qsteady_min, qsteady_max)), controllers.jl:745-843; qmax and
+       qmax_first_step above).  controller_given = 0: every knob at the method's default
+       (alg_utils.jl); 1: each field below that is not NaN replaces the default (for both
+       methods of a composite) */
+    int32_t controller_given;
+    int32_t reserved5;
+    double beta1, beta2, qoldinit, qmin, gamma, qsteady_min, qsteady_max;
 } ode_options;
 
 /* Fill o with the reference's defaults. */

@@ -1572,11 +1572,27 @@ void loopfooter(Integ& I) {
 
 // Controller defaults of one method (alg_utils.jl:407-879): beta1 = 7/(10 order),
 // beta2 = 2/(5 order), qsteady_max 6/5 for the adaptive implicit family.
+// The caller's PIController knobs (controllers.jl:751-774: beta1, beta2,
+// qoldinit and the CommonControllerOptions qmin, gamma, qsteady_min,
+// qsteady_max) over the defaults, for every method of a composite.
+void apply_controller_knobs(Integ& I) {
+    if (!I.o.ctrl_given) return;
+    auto set = [](double& f, double v) { if (!std::isnan(v)) f = v; };
+    set(I.beta1, I.o.c_beta1);
+    set(I.beta2, I.o.c_beta2);
+    set(I.qoldinit, I.o.c_qoldinit);
+    set(I.qmin, I.o.c_qmin);
+    set(I.gamma, I.o.c_gamma);
+    set(I.qsteady_min, I.o.c_qsteady_min);
+    set(I.qsteady_max, I.o.c_qsteady_max);
+}
+
 void set_controller(Integ& I, int order, bool implicit) {
     I.order = order;
     I.beta2 = 2.0 / (5.0 * order);
     I.beta1 = 7.0 / (10.0 * order);
     I.qsteady_max = implicit ? 1.2 : 1.0;
+    apply_controller_knobs(I);
 }
 
 // choose_algorithm! for AutoTsit5(Rosenbrock23()) (composite_perform_step.jl:181-221)
@@ -1810,6 +1826,7 @@ void setup(Integ& I, int alg, int model, int n, const double* p, double t0, doub
     I.qsteady_min = 1.0;
     I.qsteady_max = (alg == ORC_RODAS5P || alg == ORC_ROSENBROCK23) ? 1.2 : 1.0;   // AdaptiveImplicit: 6/5
     I.qoldinit = 1e-4;
+    apply_controller_knobs(I);
     // initialize_tstops / initialize_saveat (solve.jl:1021-1040, 1103-1124): tdir * t
     // inside the span, ascending
     const double d = I.tdir, dt0 = d * t0, dtf = d * tf;

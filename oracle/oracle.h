@@ -57,6 +57,8 @@ typedef struct {
     const double* tstops;     /* kept where t0 < ts < tf (initialize_tstops) */
     int32_t max_jac_age;      /* Rosenbrock23: J kept for at most this many accepted steps (1: never) */
     double jac_reuse_gamma_tol; /* ... while |dtgamma / dtgamma_J - 1| <= this (0.03) */
+    int32_t ctrl_given;       /* 1: the PIController knobs below replace the defaults where not NaN */
+    double c_beta1, c_beta2, c_qoldinit, c_qmin, c_gamma, c_qsteady_min, c_qsteady_max;
 } orc_opts;
 
 /* Solve one trajectory.  saveat: nsave_in times in (t0, tf] sorted ascending.

@@ -37,6 +37,9 @@ class Opts(C.Structure):
         ("save_everystep", C.c_int32), ("max_step_saves", C.c_int32),
         ("callback", C.c_int32), ("interp_points", C.c_int32), ("max_events", C.c_int32), ("ntstops", C.c_int32),
         ("tstops", C.POINTER(C.c_double)), ("max_jac_age", C.c_int32), ("jac_reuse_gamma_tol", C.c_double),
+        ("ctrl_given", C.c_int32), ("c_beta1", C.c_double), ("c_beta2", C.c_double), ("c_qoldinit", C.c_double),
+        ("c_qmin", C.c_double), ("c_gamma", C.c_double), ("c_qsteady_min", C.c_double),
+        ("c_qsteady_max", C.c_double),
     ]
 
 
@@ -95,13 +98,18 @@ def make_opts(reltol=1e-3, abstol=1e-6, dtmax=0.0, dtmin=0.0, dt=0.0, adaptive=T
               maxiters=1000000, save_start=False, save_end=True, save_end_user=-1,
               saveat_given=True, saveat_scalar=False, qmax_first_step=0.0, qmax=0.0, saveat_as_tstops=False,
               save_everystep=False, max_step_saves=0, callback=False, interp_points=10, max_events=0,
-              tstops=(), max_jac_age=1, jac_reuse_gamma_tol=0.03):
+              tstops=(), max_jac_age=1, jac_reuse_gamma_tol=0.03, controller=None):
     ts = np.ascontiguousarray(tstops, dtype=np.float64).ravel()
     o = Opts(reltol, abstol, dtmax, dtmin, dt, int(adaptive), maxiters, int(save_start),
              int(save_end), save_end_user, int(saveat_given), int(saveat_scalar),
              qmax_first_step, qmax, int(saveat_as_tstops), int(save_everystep), int(max_step_saves),
              int(callback), int(interp_points), int(max_events), int(ts.size), _dp(ts) if ts.size else None,
              int(max_jac_age), float(jac_reuse_gamma_tol))
+    if controller:   # dict of PIController knobs (beta1, beta2, qoldinit, qmin, gamma, qsteady_min, qsteady_max)
+        o.ctrl_given = 1
+        for k in ("beta1", "beta2", "qoldinit", "qmin", "gamma", "qsteady_min", "qsteady_max"):
+            v = controller.get(k)
+            setattr(o, "c_" + k, float("nan") if v is None else float(v))
     o._tstops = ts   # keeps the array alive as long as the options
     return o
 

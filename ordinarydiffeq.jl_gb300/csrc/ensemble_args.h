@@ -52,6 +52,9 @@ struct EnsembleArgs {
     int ir_sweeps;          // mixed Rosenbrock: refinement sweeps per solve
     int adaptive;           // 0: fixed steps of dt, every step accepted
     int forward_only;       // every span runs forward: the kernel's forward-only form may run
+    // user PI-controller knobs (ctrl_given; NaN: the method's default)
+    int ctrl_given;
+    double c_beta1, c_beta2, c_qoldinit, c_qmin, c_gamma, c_qsteady_min, c_qsteady_max;
     int max_jac_age;        // Rosenbrock23: J kept for at most this many accepted steps (<= 1: never kept)
     double jac_reuse_gamma_tol;  // ... while |dtgamma / dtgamma_J - 1| <= this
     // scheduling

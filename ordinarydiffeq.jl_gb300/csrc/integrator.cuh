@@ -205,7 +205,7 @@ template <> struct Ctl<float> {    // mixed: FP32 factors, FP64 dt
 };
 
 struct Ctrl {
-    double beta1, beta2, qmin_inv, qmax, qmax_first, gamma, qsteady_max, qoldinit;
+    double beta1, beta2, qmin_inv, qmax, qmax_first, gamma, qsteady_min, qsteady_max, qoldinit;
 };
 
 template <int ORDER, bool IMPLICIT>
@@ -217,8 +217,19 @@ __device__ __forceinline__ Ctrl make_ctrl(const EnsembleArgs& a) {
     c.qmax = a.qmax > 0 ? a.qmax : 10.0;
     c.qmax_first = a.qmax_first_step > 0 ? a.qmax_first_step : 10000.0;
     c.gamma = 0.9;
+    c.qsteady_min = 1.0;
     c.qsteady_max = IMPLICIT ? 1.2 : 1.0;
     c.qoldinit = 1e-4;
+    if (a.ctrl_given) {   // the caller's PIController knobs (NaN: the default)
+        auto set = [](double& f, double v) { if (v == v) f = v; };
+        set(c.beta1, a.c_beta1);
+        set(c.beta2, a.c_beta2);
+        set(c.qoldinit, a.c_qoldinit);
+        if (a.c_qmin == a.c_qmin) c.qmin_inv = 1.0 / a.c_qmin;
+        set(c.gamma, a.c_gamma);
+        set(c.qsteady_min, a.c_qsteady_min);
+        set(c.qsteady_max, a.c_qsteady_max);
+    }
     return c;
 }
 
@@ -360,7 +371,7 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
     R abstol = R(0), reltol = R(0);
     const Ctrl K = make_ctrl<Alg::ORDER, Alg::IMPLICIT>(a);
     // beta1, beta2 and qsteady_max change with a composite's current method
-    CT beta1 = (CT)K.beta1, beta2 = (CT)K.beta2, qsteady_max = (CT)K.qsteady_max;
+    CT beta1 = (CT)K.beta1, beta2 = (CT)K.beta2, qsteady_max = (CT)K.qsteady_max, qsteady_min = (CT)K.qsteady_min;
     const CT gam = (CT)K.gamma, qmin_inv = (CT)K.qmin_inv;
     const CT qoldinit = (CT)K.qoldinit;
     const CT inv_qmax = (CT)(1.0 / K.qmax), inv_qmax_first = (CT)(1.0 / K.qmax_first);
@@ -739,6 +750,7 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
         beta1 = (CT)K.beta1;
         beta2 = (CT)K.beta2;
         qsteady_max = (CT)K.qsteady_max;
+        qsteady_min = (CT)K.qsteady_min;
         st = StepStats{0, 0, 0, 0, 0, 0};
         nsaved = 0;
         isave = 0;
@@ -880,6 +892,7 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
                 beta1 = (CT)K2.beta1;
                 beta2 = (CT)K2.beta2;
                 qsteady_max = (CT)K2.qsteady_max;
+                qsteady_min = (CT)K2.qsteady_min;
                 Alg::template enter<Model, R, L, C>(cache, uprev, uprevlo, p, TM(t), g, st);
             }
         }
@@ -965,7 +978,7 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
                 t = ttmp;
             }
             if (a.adaptive) {
-                if (CT(1) <= q && q <= qsteady_max) q = CT(1);
+                if (qsteady_min <= q && q <= qsteady_max) q = CT(1);
                 errold = (EEst != EEst) ? EEst : (EEst > qoldinit ? EEst : qoldinit);
                 if constexpr (sizeof(CT) == 8)
                     ln_errold = (EEst != EEst) ? dnan() : (EEst > qoldinit ? ln_eest : ln_qoldinit);

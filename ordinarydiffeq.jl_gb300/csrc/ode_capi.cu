@@ -283,6 +283,13 @@ int check_problem(const ode_problem_desc* d, const ode_options* o, int64_t N, co
     if (o->max_jac_age < 0) return bad(ODE_E_INVALID, "max_jac_age must be >= 0");
     if (o->nsave_idxs < 0 || (o->nsave_idxs > 0 && !o->save_idxs))
         return bad(ODE_E_INVALID, "nsave_idxs < 0, or save_idxs is null");
+    if (o->controller_given) {
+        const double f[] = {o->beta1, o->beta2, o->qoldinit, o->qmin, o->gamma, o->qsteady_min, o->qsteady_max};
+        for (double v : f)
+            if (std::isinf(v)) return bad(ODE_E_INVALID, "controller knobs must be finite (NaN: the default)");
+        if (o->qmin <= 0 || o->gamma <= 0 || o->qoldinit <= 0)
+            return bad(ODE_E_INVALID, "controller qmin, gamma and qoldinit must be > 0");
+    }
     if (!o->adaptive && (std::isnan(o->dt) || std::isinf(o->dt) || (o->dt == 0 && o->ntstops == 0)))
         return bad(ODE_E_INVALID, "fixed steps (adaptive = 0) need a finite dt or tstops");
     // the kept J lives beside W in registers; the shared-memory LU (16-64 states)
@@ -384,6 +391,14 @@ EnsembleArgs make_args(ode_handle* h, const ode_problem_desc* d, const ode_optio
     a.jac_reuse_gamma_tol = o->jac_reuse_gamma_tol < 0 ? 0.03 : o->jac_reuse_gamma_tol;
     a.adaptive = o->adaptive ? 1 : 0;
     a.forward_only = o->forward_only ? 1 : 0;
+    a.ctrl_given = o->controller_given ? 1 : 0;
+    a.c_beta1 = o->beta1;
+    a.c_beta2 = o->beta2;
+    a.c_qoldinit = o->qoldinit;
+    a.c_qmin = o->qmin;
+    a.c_gamma = o->gamma;
+    a.c_qsteady_min = o->qsteady_min;
+    a.c_qsteady_max = o->qsteady_max;
     a.save_idxs = o->nsave_idxs > 0 ? o->save_idxs : nullptr;   // device memory at this point
     a.nsave_rows = o->nsave_idxs > 0 ? o->nsave_idxs : 0;
     a.t_out = t_out;
@@ -1379,6 +1394,8 @@ void ode_options_default(ode_options* o) {
     o->max_jac_age = 1;
     o->jac_reuse_gamma_tol = 0.03;
     o->adaptive = 1;
+    o->controller_given = 0;
+    o->beta1 = o->beta2 = o->qoldinit = o->qmin = o->gamma = o->qsteady_min = o->qsteady_max = std::nan("");
 }
 
 size_t ode_options_size(void) { return sizeof(ode_options); }
@@ -1979,6 +1996,14 @@ extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_o
     a.jac_reuse_gamma_tol = o->jac_reuse_gamma_tol < 0 ? 0.03 : o->jac_reuse_gamma_tol;
     a.adaptive = o->adaptive ? 1 : 0;
     a.forward_only = o->forward_only ? 1 : 0;
+    a.ctrl_given = o->controller_given ? 1 : 0;
+    a.c_beta1 = o->beta1;
+    a.c_beta2 = o->beta2;
+    a.c_qoldinit = o->qoldinit;
+    a.c_qmin = o->qmin;
+    a.c_gamma = o->gamma;
+    a.c_qsteady_min = o->qsteady_min;
+    a.c_qsteady_max = o->qsteady_max;
     a.save_idxs = o->nsave_idxs > 0 ? o->save_idxs : nullptr;   // device memory at this point
     a.nsave_rows = o->nsave_idxs > 0 ? o->nsave_idxs : 0;
     a.t_out = t_out;

@@ -29,7 +29,7 @@ using SciMLBase
 import OrdinaryDiffEqTsit5: Tsit5
 import OrdinaryDiffEqVerner: Vern7
 import OrdinaryDiffEqRosenbrock: Rodas5P, Rosenbrock23
-import OrdinaryDiffEqCore: CompositeAlgorithm, AutoSwitch
+import OrdinaryDiffEqCore: CompositeAlgorithm, AutoSwitch, PIController
 
 export EnsembleGB300, GB300Model, GB300Callback, register_model
 
@@ -104,6 +104,23 @@ mutable struct Options
     max_jac_age::Int32; reserved2::Int32; jac_reuse_gamma_tol::Float64
     nsave_idxs::Int32; reserved3::Int32; save_idxs::Ptr{Int32}
     adaptive::Int32; forward_only::Int32
+    controller_given::Int32; reserved5::Int32
+    beta1::Float64; beta2::Float64; qoldinit::Float64; qmin::Float64; gamma::Float64
+    qsteady_min::Float64; qsteady_max::Float64
+end
+# the knobs of solve(...; controller = PIController(beta1, beta2; qoldinit, qmin, qmax,
+# qmax_first_step, gamma, qsteady_min, qsteady_max)): beta1, beta2 and qoldinit on the
+# controller, the rest as overrides in its `basic` (a NamedTuple until resolved)
+_knob(b::NamedTuple, k) = haskey(b, k) && b[k] !== nothing ? Float64(b[k]) : NaN
+_knob(b, k) = Float64(getfield(b, k))
+function controller_knobs(c)
+    c === nothing && return (Int32(0), fill(NaN, 7), 0.0, 0.0)
+    c isa PIController || error("EnsembleGB300 runs the PI controller: pass controller = PIController(...)")
+    b = c.basic
+    qm, qmf = _knob(b, :qmax), _knob(b, :qmax_first_step)
+    return (Int32(1), [Float64(c.beta1), Float64(c.beta2), Float64(c.qoldinit), _knob(b, :qmin), _knob(b, :gamma),
+                       _knob(b, :qsteady_min), _knob(b, :qsteady_max)],
+            isnan(qm) ? 0.0 : qm, isnan(qmf) ? 0.0 : qmf)
 end
 # the W-method Jacobian reuse knobs of Rosenbrock23(max_jac_age, jac_reuse_gamma_tol)
 jac_reuse(alg::Rosenbrock23) = (Int32(alg.max_jac_age), Float64(alg.jac_reuse_gamma_tol))
@@ -182,7 +199,7 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem,
                            ens::EnsembleGB300; trajectories, saveat = Float64[], reltol = 1e-3, abstol = 1e-6,
                            dt = 0.0, dtmax = 0.0, dtmin = 0.0, maxiters = 1_000_000, save_start = nothing,
                            save_end = nothing, save_everystep = isempty(saveat), max_step_saves = 1024, seed = 0,
-                           save_idxs = nothing, adaptive = true, callback = nothing,
+                           save_idxs = nothing, adaptive = true, controller = nothing, callback = nothing,
                            dense = save_everystep && isempty(saveat) && save_idxs === nothing,
                            tstops = Float64[], kwargs...)
     t0 = time()
@@ -220,12 +237,13 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem,
     sidx = save_idxs === nothing ? Int32[] : Int32[i - 1 for i in save_idxs]
     rows = save_idxs === nothing ? n : length(sidx)
     # a dt of either sign is taken in the direction of the span (handle_dt!, solve.jl:968-985)
+    cg, ck, cqmax, cqmaxfirst = controller_knobs(controller)
     o = Options(reltol, abstol, dtmax, dtmin, abs(dt), maxiters, ss, se, save_end === nothing ? -1 : Int32(save_end),
-                scalar, length(sv), 0, 0.0, 0.0, ens.lanes_per_traj, ens.scheduler, 0, -1, everystep,
+                scalar, length(sv), 0, cqmaxfirst, cqmax, ens.lanes_per_traj, ens.scheduler, 0, -1, everystep,
                 everystep ? max_step_saves : 0, cb, cb ? callback.interp_points : 10, cb ? callback.max_events : 0,
                 length(tst), isempty(tst) ? Ptr{Float64}(C_NULL) : pointer(tst), jac_reuse(alg)[1], Int32(0),
                 jac_reuse(alg)[2], length(sidx), Int32(0), isempty(sidx) ? Ptr{Int32}(C_NULL) : pointer(sidx),
-                Int32(adaptive), Int32(0))
+                Int32(adaptive), Int32(0), cg, Int32(0), ck...)
     d = ProblemDesc(model, alg_id(alg), n, npar, ens.precision === :mixed ? 1 : 0, 0)
     cap = length(sv) + (everystep ? max_step_saves : 0) + 2 + (cb ? 2 * callback.max_events : 0)
     t_out = fill(NaN, N, cap); u_out = fill(NaN, N, rows, cap)   # [(s*rows + i)*N + j] -> u_out[j, i, s]

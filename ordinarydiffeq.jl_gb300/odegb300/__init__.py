@@ -7,13 +7,14 @@
     sim.u[0].t, sim.u[0].u, sim.u[0].retcode, sim.u[0].stats
 """
 from .ensemble import (AutoTsit5, ContinuousCallback, DiscreteCallback, EnsembleContext, EnsembleGB300,
-                       EnsembleProblem, EnsembleSolution, ODEProblem, ODESolution, ReturnCode, Rodas5P, Rosenbrock23,
+                       EnsembleProblem, EnsembleSolution, ODEProblem, ODESolution, PIController, ReturnCode, Rodas5P,
+                       Rosenbrock23,
                        Tsit5, Vern7, autotune, dense_eval, get_handle, register_model, remake, solve, solve_arrays)
 from .saveat import julia_float_range, resolve_saveat
 from .serving import Server, run_open_loop
 from . import _lib, build
 
 __all__ = ["AutoTsit5", "ContinuousCallback", "DiscreteCallback", "EnsembleContext", "EnsembleGB300", "EnsembleProblem",
-           "EnsembleSolution", "ODEProblem", "ODESolution", "ReturnCode", "Rodas5P", "Rosenbrock23", "Tsit5", "Vern7",
+           "EnsembleSolution", "ODEProblem", "ODESolution", "PIController", "ReturnCode", "Rodas5P", "Rosenbrock23", "Tsit5", "Vern7",
            "autotune", "dense_eval", "get_handle", "register_model", "remake", "solve", "solve_arrays", "julia_float_range",
            "resolve_saveat", "Server", "run_open_loop"]

@@ -128,6 +128,22 @@ ALG_BY_NAME = {"tsit5": Tsit5(), "vern7": Vern7(), "rodas5p": Rodas5P(), "rosenb
 
 
 @dataclass
+class PIController:
+    """The reference's PIController knobs (controllers.jl:745-843: beta1, beta2,
+    qoldinit and the CommonControllerOptions qmin, qmax, qmax_first_step, gamma,
+    qsteady_min, qsteady_max); None keeps the method's default."""
+    beta1: float = None
+    beta2: float = None
+    qoldinit: float = None
+    qmin: float = None
+    qmax: float = None
+    qmax_first_step: float = None
+    gamma: float = None
+    qsteady_min: float = None
+    qsteady_max: float = None
+
+
+@dataclass
 class EnsembleGB300:
     """Ensemble algorithm running every trajectory on one GB300.
 
@@ -309,7 +325,7 @@ def get_handle(device=0):
 
 
 def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax, callback=None,
-             tstops=None, alg=None, save_idxs=None, adaptive=True):
+             tstops=None, alg=None, save_idxs=None, adaptive=True, controller=None):
     o = _lib.Options()
     L = _lib.load()
     L.ode_options_default(C.byref(o))
@@ -327,6 +343,15 @@ def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_ste
     o.saveat_per_traj = int(sv.per_traj)
     o.qmax_first_step = qmax_first_step or 0.0
     o.qmax = qmax or 0.0
+    if controller is not None:   # solve(...; controller = PIController(...))
+        o.controller_given = 1
+        for k in ("beta1", "beta2", "qoldinit", "qmin", "gamma", "qsteady_min", "qsteady_max"):
+            v = getattr(controller, k)
+            setattr(o, k, float("nan") if v is None else float(v))
+        if controller.qmax is not None:
+            o.qmax = float(controller.qmax)
+        if controller.qmax_first_step is not None:
+            o.qmax_first_step = float(controller.qmax_first_step)
     o.lanes_per_traj = ens.lanes_per_traj
     o.scheduler = ens.sched_id()
     o.block_size = ens.block_size
@@ -403,7 +428,7 @@ def register_model(source, name, n_states, n_params, jac=False, tgrad=False, non
 def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=1e-6, dt=None,
                  dtmax=None, dtmin=None, maxiters=1000000, save_start=None, save_end=None, n_per_traj=None,
                  qmax_first_step=None, qmax=None, return_times=False, save_everystep=False, max_step_saves=1024,
-                 dense=False, callback=None, tstops=None, save_idxs=None, adaptive=True):
+                 dense=False, callback=None, tstops=None, save_idxs=None, adaptive=True, controller=None):
     """Solve a packed ensemble.  u0s (n, N), ps (np, N), tspans (2, N).  Returns the
     raw structure-of-arrays outputs dict (t, u, nsaved, retcode, stats).
     save_everystep keeps every accepted step, up to max_step_saves per
@@ -415,7 +440,8 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
     trajectory steps to exactly (those inside its (t0, tf)), as the reference's
     tstops keyword.  save_idxs: the states saved (0-based, in order; the
     reference's save_idxs): u is then (cap, len(save_idxs), N).  adaptive=False:
-    fixed steps of dt (the reference's adaptive = false)."""
+    fixed steps of dt (the reference's adaptive = false).  controller: a
+    PIController with the step-size controller's knobs."""
     L = _lib.load()
     if isinstance(model, str):
         model = MODELS[model]
@@ -425,7 +451,7 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
     n, N = u0s.shape
     sv = resolve_saveat(saveat, tspans, save_start, save_end, save_everystep, max_step_saves)
     o = _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax, callback, tstops, alg,
-                 save_idxs, adaptive)
+                 save_idxs, adaptive, controller)
     d = _lib.ProblemDesc(model, alg.alg_id, n, ps.shape[0], ens.prec_id(), 0)
     rows = n if save_idxs is None else int(np.size(save_idxs))
     cap = sv.cap + (2 * callback.max_events if callback is not None else 0)
@@ -533,7 +559,7 @@ def autotune(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=
 def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, saveat=None, reltol=1e-3,
           abstol=1e-6, dt=None, dtmax=None, dtmin=None, maxiters=1000000, save_start=None, save_end=None,
           seed=0, qmax_first_step=None, qmax=None, save_everystep=None, max_step_saves=1024, dense=None,
-          callback=None, tstops=None, save_idxs=None, adaptive=True):
+          callback=None, tstops=None, save_idxs=None, adaptive=True, controller=None):
     """solve(EnsembleProblem, alg, EnsembleGB300(); trajectories, saveat, reltol, abstol, ...).
     As in the reference (solve.jl:138-146), save_everystep defaults to "no
     saveat given" (every accepted step is kept, up to max_step_saves per
@@ -564,7 +590,7 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
                            maxiters, save_start, save_end, eprob.n_per_traj, qmax_first_step, qmax,
                            save_everystep=save_everystep, max_step_saves=max_step_saves,
                            dense=dense and not (dense_default and eprob.n_per_traj is not None), callback=callback,
-                           tstops=tstops, save_idxs=save_idxs, adaptive=adaptive)
+                           tstops=tstops, save_idxs=save_idxs, adaptive=adaptive, controller=controller)
         sols = _LazySolutions(res, alg, eprob.n_per_traj)
         return EnsembleSolution(sols, time.perf_counter() - t_start, True, res)
     if trajectories is None:
@@ -580,7 +606,7 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
         ids = list(range(done, min(trajectories, done + batch_size)))
         outs = _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, dtmin, maxiters,
                             save_start, save_end, output_func, qmax_first_step, qmax, save_everystep, max_step_saves,
-                            dense, dense_default, callback, tstops, save_idxs, adaptive)
+                            dense, dense_default, callback, tstops, save_idxs, adaptive, controller)
         u, converged = reduction(u, outs, range(ids[0] + 1, ids[-1] + 2))
         done = ids[-1] + 1
         if converged:
@@ -590,7 +616,8 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
 
 def _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, dtmin, maxiters, save_start,
                  save_end, output_func, qmax_first_step, qmax, save_everystep=False, max_step_saves=1024,
-                 dense=False, dense_default=True, callback=None, tstops=None, save_idxs=None, adaptive=True):
+                 dense=False, dense_default=True, callback=None, tstops=None, save_idxs=None, adaptive=True,
+                 controller=None):
     repeat = {i: 1 for i in ids}
     results = {}
     todo = list(ids)
@@ -618,7 +645,7 @@ def _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, 
                            maxiters, save_start, save_end, npt, qmax_first_step, qmax,
                            save_everystep=save_everystep, max_step_saves=max_step_saves,
                            dense=dense and not (dense_default and npt is not None), callback=callback,
-                           tstops=tstops, save_idxs=save_idxs, adaptive=adaptive)
+                           tstops=tstops, save_idxs=save_idxs, adaptive=adaptive, controller=controller)
         sols = _LazySolutions(res, alg, npt)
         again = []
         for k, i in enumerate(todo):

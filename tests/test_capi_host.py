@@ -43,7 +43,7 @@ def test_struct_layouts_match_the_bindings():
 
 def test_abi_version_and_defaults_without_gpu():
     L = _lib.load()
-    assert L.ode_abi_version() == 6
+    assert L.ode_abi_version() == 7
     # dense vectors per step (Tsit5 k1..k7, Vern7 k1 and k4..k9, Rodas5P dense k1..k3)
     assert [L.ode_dense_nk(a) for a in (0, 1, 2)] == [7, 7, 3] and L.ode_dense_nk(9) == -1
     o = _lib.Options()
@@ -128,6 +128,21 @@ def test_fixed_steps_are_checked_on_the_host():
     assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == -1
     assert b"fixed steps" in L.ode_last_error(None)
     o.dt = float("inf")
+    assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == -1
+
+
+def test_controller_knobs_are_checked_on_the_host():
+    L = _lib.load()
+    o = _lib.Options()
+    L.ode_options_default(C.byref(o))
+    assert o.controller_given == 0 and np.isnan(o.beta1) and np.isnan(o.qsteady_max)
+    d = _lib.ProblemDesc(_lib.MODEL_LORENZ, _lib.ODE_TSIT5, 3, 3, _lib.PREC_FP64, 0)
+    o.controller_given = 1
+    o.qmin = 0.0
+    assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == -1
+    assert b"qmin" in L.ode_last_error(None)
+    o.qmin = float("nan")
+    o.beta1 = float("inf")
     assert L.ode_solve_ensemble_noalloc(C.byref(d), C.byref(o), 0, *([None] * 11)) == -1
 
 

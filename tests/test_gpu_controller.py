@@ -1,0 +1,55 @@
+"""The PI controller's knobs (solve(...; controller = PIController(beta1, beta2;
+qoldinit, qmin, qmax, gamma, qsteady_min, qsteady_max)), controllers.jl:745-843)
+on the GPU: for every method the saves and step counts match the oracle's with
+the same knobs, in FP64 and in the mixed form, and the steady band pinned in
+the oracle (dt constant after the first step) holds on the device."""
+import numpy as np
+import pytest
+
+from gpu_common import compare, gpu, lorenz_inputs, oracle
+from odegb300 import PIController
+
+pytestmark = pytest.mark.gpu
+
+ALGS = ["tsit5", "vern7", "rodas5p", "rosenbrock23", "autotsit5_rosenbrock23"]
+KNOBS = dict(beta1=0.12, beta2=0.05, qoldinit=1e-3, qmin=0.3, qmax=5.0, gamma=0.8, qsteady_min=0.95,
+             qsteady_max=1.3)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from odegb300 import build
+    build.build()
+
+
+@pytest.mark.parametrize("alg", ALGS)
+def test_controller_knobs_match_oracle(alg):
+    N = 256
+    u0, p, ts = lorenz_inputs(N, seed=51)
+    rt = 1e-8 if alg in ("tsit5", "vern7") else 1e-6
+    ctl = PIController(**KNOBS)
+    g = gpu("lorenz", alg, u0, p, ts, 0.1, rt, rt, controller=ctl)
+    knobs = {k: v for k, v in KNOBS.items() if k != "qmax"}
+    o = oracle("lorenz", alg, u0, p, ts, 0.1, rt, rt, controller=knobs, qmax=KNOBS["qmax"])
+    assert (g["retcode"] == 1).all()
+    c = compare(g, o, rt, rt)
+    assert c["ok"] and c["steps_ok"], c
+    base = gpu("lorenz", alg, u0, p, ts, 0.1, rt, rt)
+    assert not np.array_equal(base["stats"]["naccept"], g["stats"]["naccept"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_steady_band_keeps_dt(precision):
+    N = 64
+    u0 = np.full((1, N), 0.5)
+    p = np.full((1, N), 1.01)
+    ts = np.tile([[0.0], [1.0]], (1, N))
+    g = gpu("linear", "tsit5", u0, p, ts, None, 1e-6, 1e-6, precision=precision, save_everystep=True,
+            max_step_saves=512, controller=PIController(qsteady_min=0.0, qsteady_max=1e9))
+    t = g["t"][:int(g["nsaved"][0]), 0]
+    d = np.diff(t)
+    assert (g["stats"]["nreject"] == 0).all() and len(d) > 5
+    assert np.allclose(d[:-1], d[0], rtol=1e-12, atol=0) and d[-1] <= d[0]

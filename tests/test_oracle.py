@@ -354,6 +354,30 @@ def test_fixed_steps_land_on_the_tstops():
     assert r["stats"]["nf"] == 1 + 6 * 4
 
 
+def test_controller_knobs():
+    # PIController(...; qsteady_min = 0, qsteady_max = 1e9): every accepted step's q is
+    # in the steady band, so dt never changes after the first step (controllers.jl:829)
+    kw = dict(saveat=[], saveat_given=False, save_everystep=True, max_step_saves=4096, save_start=True,
+              reltol=1e-6, abstol=1e-6)
+    steady = dict(qsteady_min=0.0, qsteady_max=1e9)
+    r = O.solve(O.TSIT5, O.LINEAR, [0.5], [1.01], (0.0, 1.0), controller=steady, **kw)
+    d = np.diff(r["t"])
+    assert r["stats"]["nreject"] == 0 and len(d) > 5
+    assert np.allclose(d[:-1], d[0], rtol=1e-12, atol=0) and d[-1] <= d[0]
+    # a smaller safety factor or a tighter qmax takes more steps; the defaults equal no knobs
+    base = O.solve(O.TSIT5, O.LORENZ, [1.0, 0.0, 0.0], [10.0, 28.0, 8 / 3], (0.0, 1.0), **kw)
+    same = O.solve(O.TSIT5, O.LORENZ, [1.0, 0.0, 0.0], [10.0, 28.0, 8 / 3], (0.0, 1.0),
+                   controller=dict(beta1=7.0 / (10.0 * 5), beta2=2.0 / (5.0 * 5), gamma=0.9, qmin=0.2), **kw)
+    assert np.array_equal(base["t"], same["t"]) and np.array_equal(base["u"], same["u"])
+    cautious = O.solve(O.TSIT5, O.LORENZ, [1.0, 0.0, 0.0], [10.0, 28.0, 8 / 3], (0.0, 1.0),
+                       controller=dict(gamma=0.5), **kw)
+    assert cautious["stats"]["naccept"] > 1.2 * base["stats"]["naccept"]
+    # beta2 = 0: the I controller (q = EEst^beta1 / gamma clipped)
+    icon = O.solve(O.TSIT5, O.LORENZ, [1.0, 0.0, 0.0], [10.0, 28.0, 8 / 3], (0.0, 1.0),
+                   controller=dict(beta1=1.0 / 5, beta2=0.0), **kw)
+    assert icon["retcode"] == O.RC_SUCCESS and icon["stats"]["naccept"] != base["stats"]["naccept"]
+
+
 def test_tstops_from_a_range_are_a_subset_of_sol_t():
     # ode_tstops_tests.jl:97-105 ("Late binding tstops"): 0:0.1:1 is a subset of sol.t
     ts = np.arange(0, 11) * 0.1
