@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define ODE_ABI_VERSION 7
+#define ODE_ABI_VERSION 8
 
 typedef struct ode_handle ode_handle;
 
@@ -217,6 +217,13 @@ typedef struct {
     int32_t controller_given;
     int32_t reserved5;
     double beta1, beta2, qoldinit, qmin, gamma, qsteady_min, qsteady_max;
+    /* Per-state tolerances (solve(...; abstol = [...], reltol = [...]): calculate_residuals with
+       array tolerances, calculate_residuals.jl:9-14,117-125, and the initial-step scale): n_states
+       entries each (abstol >= 0, reltol > 0), or NULL for the scalar above.  Host memory for the
+       host entry points, device memory for ode_solve_ensemble_device and ode_solve_ensemble_noalloc;
+       not with ode_submit */
+    const double* abstol_vec;
+    const double* reltol_vec;
 } ode_options;
 
 /* Fill o with the reference's defaults. */

@@ -384,11 +384,15 @@ inline void f_eval(Integ& I, const double* u, double t, double* du) {
 
 // calculate_residuals + ODE_DEFAULT_NORM:
 // lib/DiffEqBase/src/calculate_residuals.jl:9-14,117-125 and
-// lib/DiffEqBase/src/common_defaults.jl:69-75 (sqrt(sum(abs2)/n)).
+// lib/DiffEqBase/src/common_defaults.jl:69-75 (sqrt(sum(abs2)/n)).  Array
+// tolerances (the broadcast over abstol and reltol) give state i its own.
+inline double abstol_at(const Integ& I, int i) { return I.o.abstol_vec ? I.o.abstol_vec[i] : I.o.abstol; }
+inline double reltol_at(const Integ& I, int i) { return I.o.reltol_vec ? I.o.reltol_vec[i] : I.o.reltol; }
+
 double residual_norm(Integ& I, const double* ut, const double* u0, const double* u1) {
     double acc = 0.0;
     for (int i = 0; i < I.n; ++i) {
-        double sc = std::fma(jmax(std::fabs(u0[i]), std::fabs(u1[i])), I.o.reltol, I.o.abstol);
+        double sc = std::fma(jmax(std::fabs(u0[i]), std::fabs(u1[i])), reltol_at(I, i), abstol_at(I, i));
         double e = ut[i] / sc;
         acc = std::fma(e, e, acc);
     }
@@ -409,7 +413,7 @@ double initdt(Integ& I) {
     double dtmin = std::nextafter(jmax(I.o.dtmin, jeps(t)), INFINITY);
     double smalldt = jmax(dtmin, 1e-6);
     std::vector<double> sk(n), f0(n), f1(n), u1(n), tmp(n);
-    for (int i = 0; i < n; ++i) sk[i] = std::fma(std::fabs(u0[i]), I.o.reltol, I.o.abstol);
+    for (int i = 0; i < n; ++i) sk[i] = std::fma(std::fabs(u0[i]), reltol_at(I, i), abstol_at(I, i));
     f_eval(I, u0, t, f0.data());
     if (I.alg == ORC_TSIT5) I.fsallast = f0;
     auto nrm = [&](const std::vector<double>& v) {

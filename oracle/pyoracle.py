@@ -39,7 +39,7 @@ class Opts(C.Structure):
         ("tstops", C.POINTER(C.c_double)), ("max_jac_age", C.c_int32), ("jac_reuse_gamma_tol", C.c_double),
         ("ctrl_given", C.c_int32), ("c_beta1", C.c_double), ("c_beta2", C.c_double), ("c_qoldinit", C.c_double),
         ("c_qmin", C.c_double), ("c_gamma", C.c_double), ("c_qsteady_min", C.c_double),
-        ("c_qsteady_max", C.c_double),
+        ("c_qsteady_max", C.c_double), ("abstol_vec", C.POINTER(C.c_double)), ("reltol_vec", C.POINTER(C.c_double)),
     ]
 
 
@@ -100,6 +100,11 @@ def make_opts(reltol=1e-3, abstol=1e-6, dtmax=0.0, dtmin=0.0, dt=0.0, adaptive=T
               save_everystep=False, max_step_saves=0, callback=False, interp_points=10, max_events=0,
               tstops=(), max_jac_age=1, jac_reuse_gamma_tol=0.03, controller=None):
     ts = np.ascontiguousarray(tstops, dtype=np.float64).ravel()
+    # array tolerances: one per state (the scalars then stand unused)
+    av = np.ascontiguousarray(abstol, dtype=np.float64).ravel() if np.ndim(abstol) else None
+    rv = np.ascontiguousarray(reltol, dtype=np.float64).ravel() if np.ndim(reltol) else None
+    abstol = float(av[0]) if av is not None else abstol
+    reltol = float(rv[0]) if rv is not None else reltol
     o = Opts(reltol, abstol, dtmax, dtmin, dt, int(adaptive), maxiters, int(save_start),
              int(save_end), save_end_user, int(saveat_given), int(saveat_scalar),
              qmax_first_step, qmax, int(saveat_as_tstops), int(save_everystep), int(max_step_saves),
@@ -110,7 +115,11 @@ def make_opts(reltol=1e-3, abstol=1e-6, dtmax=0.0, dtmin=0.0, dt=0.0, adaptive=T
         for k in ("beta1", "beta2", "qoldinit", "qmin", "gamma", "qsteady_min", "qsteady_max"):
             v = controller.get(k)
             setattr(o, "c_" + k, float("nan") if v is None else float(v))
-    o._tstops = ts   # keeps the array alive as long as the options
+    if av is not None:
+        o.abstol_vec = _dp(av)
+    if rv is not None:
+        o.reltol_vec = _dp(rv)
+    o._keep = (ts, av, rv)   # keeps the arrays alive as long as the options
     return o
 
 

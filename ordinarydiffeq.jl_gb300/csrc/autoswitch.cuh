@@ -104,15 +104,15 @@ struct AutoSwitchAlg {
 
     template <class Model, class R, int L, int C>
     __device__ static typename Ctl<R>::T step(Cache<R, C>& c, R* u, R* ulo, const R* up, const R* uplo,
-                                             const PR<R>* p, double t, double dt, R abstol, R reltol, long long iter,
+                                             const PR<R>* p, double t, double dt, const Tol<R>& tol, long long iter,
                                              bool errorfail, const Group<L>& g, StepStats& st) {
         if (c.current == 0) {
             const typename Ctl<R>::T e = NS::template step<Model, R, L, C, true>(c.ns, u, ulo, up, uplo, p, t, dt,
-                                                                                abstol, reltol, iter, errorfail, g, st);
+                                                                                tol, iter, errorfail, g, st);
             c.eigen_est = c.ns.eig;
             return e;
         }
-        return S::template step<Model, R, L, C>(c.s, u, ulo, up, uplo, p, t, dt, abstol, reltol, iter, errorfail, g,
+        return S::template step<Model, R, L, C>(c.s, u, ulo, up, uplo, p, t, dt, tol, iter, errorfail, g,
                                                 st);
     }
 

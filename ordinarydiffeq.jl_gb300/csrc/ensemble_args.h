@@ -12,6 +12,10 @@ struct OdeStatsDev {
     long long nf, njacs, nw, nsolve, naccept, nreject;
 };
 
+// PI-controller values of EnsembleArgs::kd / kf: beta1, beta2, 1/qmin, gamma,
+// qsteady_min, qsteady_max, qoldinit, 1/qmax, 1/qmax_first_step.
+enum { KB1 = 0, KB2, KQMININV, KGAM, KQSMIN, KQSMAX, KQOLD, KIQMAX, KIQMAXF, KNCTRL };
+
 // Everything one ensemble launch needs.  Device pointers; SoA layouts:
 //   u0[i*N + j], p[i*N + j], tspan[j] / tspan[N + j],
 //   saveat[s] (shared) or saveat[s*N + j] (per trajectory),
@@ -52,9 +56,13 @@ struct EnsembleArgs {
     int ir_sweeps;          // mixed Rosenbrock: refinement sweeps per solve
     int adaptive;           // 0: fixed steps of dt, every step accepted
     int forward_only;       // every span runs forward: the kernel's forward-only form may run
-    // user PI-controller knobs (ctrl_given; NaN: the method's default)
-    int ctrl_given;
-    double c_beta1, c_beta2, c_qoldinit, c_qmin, c_gamma, c_qsteady_min, c_qsteady_max;
+    // The PI controller of each method (slot 1: a composite's stiff method), its
+    // defaults and the caller's knobs resolved on the host, in both precisions
+    // (kernel parameters: read where used, held in no register)
+    double kd[2][KNCTRL];
+    float kf[2][KNCTRL];
+    const double* abstol_vec;   // per-state tolerances (device, n entries), or null
+    const double* reltol_vec;
     int max_jac_age;        // Rosenbrock23: J kept for at most this many accepted steps (<= 1: never kept)
     double jac_reuse_gamma_tol;  // ... while |dtgamma / dtgamma_J - 1| <= this
     // scheduling

@@ -154,7 +154,7 @@ struct Tsit5Alg {
     // g6 the sixth stage's input, NaN propagating like Julia's maximum.
     template <class Model, class R, int L, int C, bool EIG = false>
     __device__ static typename Ctl<R>::T step(Cache<R, C>& c, R* u, R* ulo, const R* up, const R* uplo,
-                                             const PR<R>* p, double t, double dt, R abstol, R reltol, long long, bool,
+                                             const PR<R>* p, double t, double dt, const Tol<R>& tol, long long, bool,
                                              const Group<L>& g, StepStats& st) {
         static_assert(!EIG || L == 1, "the stiffness estimate is formed on one lane");
         using K = RK<Tsit5Tab, R, C>;
@@ -193,7 +193,7 @@ struct Tsit5Alg {
         K::weights(tmp, c.k, Tsit5Err());
 #pragma unroll
         for (int i = 0; i < C; ++i) tmp[i] = d * tmp[i];
-        return error_norm<R, L, C>(tmp, up, u, abstol, reltol, g);
+        return error_norm<R, L, C>(tmp, up, u, tol, g);
     }
 
     template <class Model, class R, int L, int C>
@@ -293,7 +293,7 @@ struct Vern7Alg {
 
     template <class Model, class R, int L, int C>
     __device__ static typename Ctl<R>::T step(Cache<R, C>& c, R* u, R* ulo, const R* up, const R* uplo,
-                                             const PR<R>* p, double t, double dt, R abstol, R reltol, long long, bool,
+                                             const PR<R>* p, double t, double dt, const Tol<R>& tol, long long, bool,
                                              const Group<L>& g, StepStats& st) {
         const R d = (R)dt;
         c.extra = false;
@@ -315,7 +315,7 @@ struct Vern7Alg {
         RK<Vern7Tab, R, C>::weights(c.tmp, c.s, Vern7Err());
 #pragma unroll
         for (int i = 0; i < C; ++i) c.tmp[i] = d * c.tmp[i];
-        return error_norm<R, L, C>(c.tmp, up, u, abstol, reltol, g);
+        return error_norm<R, L, C>(c.tmp, up, u, tol, g);
     }
 
     // Extra stages k11..k16 (verner_addsteps.jl:80-195) at (tprev, uprev, dt).

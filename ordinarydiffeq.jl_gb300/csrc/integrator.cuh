@@ -204,49 +204,42 @@ template <> struct Ctl<float> {    // mixed: FP32 factors, FP64 dt
     static __device__ __forceinline__ float theta(double num, double dt) { return (float)num / (float)dt; }
 };
 
-struct Ctrl {
-    double beta1, beta2, qmin_inv, qmax, qmax_first, gamma, qsteady_min, qsteady_max, qoldinit;
-};
-
-template <int ORDER, bool IMPLICIT>
-__device__ __forceinline__ Ctrl make_ctrl(const EnsembleArgs& a) {
-    Ctrl c;
-    c.beta2 = 2.0 / (5.0 * ORDER);
-    c.beta1 = 7.0 / (10.0 * ORDER);
-    c.qmin_inv = 1.0 / 0.2;
-    c.qmax = a.qmax > 0 ? a.qmax : 10.0;
-    c.qmax_first = a.qmax_first_step > 0 ? a.qmax_first_step : 10000.0;
-    c.gamma = 0.9;
-    c.qsteady_min = 1.0;
-    c.qsteady_max = IMPLICIT ? 1.2 : 1.0;
-    c.qoldinit = 1e-4;
-    if (a.ctrl_given) {   // the caller's PIController knobs (NaN: the default)
-        auto set = [](double& f, double v) { if (v == v) f = v; };
-        set(c.beta1, a.c_beta1);
-        set(c.beta2, a.c_beta2);
-        set(c.qoldinit, a.c_qoldinit);
-        if (a.c_qmin == a.c_qmin) c.qmin_inv = 1.0 / a.c_qmin;
-        set(c.gamma, a.c_gamma);
-        set(c.qsteady_min, a.c_qsteady_min);
-        set(c.qsteady_max, a.c_qsteady_max);
-    }
-    return c;
+// A PI-controller value of method slot s (ensemble_args.h: KB1 ... KIQMAXF), in
+// the controller's precision.
+template <class CT> __device__ __forceinline__ CT kval(const EnsembleArgs& a, int s, int k) {
+    if constexpr (sizeof(CT) == 8) return a.kd[s][k];
+    else return a.kf[s][k];
 }
 
-// Residual norm sqrt(sum_i (ut_i / (abstol + max(|u0_i|,|u1_i|) reltol))^2 / n).
+// A step's tolerances: the trajectory's scalars, or per state when the solve
+// gives vectors (abstol[i], reltol[i] of state i = lane*C + c, read from the
+// launch's device arrays where used, so no register holds them).
+template <class R> struct Tol {
+    R abstol, reltol;
+    const double* av;   // per-state abstol, or null
+    const double* rv;   // per-state reltol, or null
+    template <int C> __device__ __forceinline__ R a(int lane, int c) const {
+        return av ? (R)av[lane * C + c] : abstol;
+    }
+    template <int C> __device__ __forceinline__ R r(int lane, int c) const {
+        return rv ? (R)rv[lane * C + c] : reltol;
+    }
+};
+
+// Residual norm sqrt(sum_i (ut_i / (abstol_i + max(|u0_i|,|u1_i|) reltol_i))^2 / n).
 // FP64 mode: the sum in FP64 (sequentially within a lane, then across the
 // group).  Mixed mode: the same sum carried in double-float (an exact square
 // by fma, a two-sum per term; FP64-class precision on the FP32 pipe), since
 // on GB300 each FP64 add/fma or float<->double conversion per component would
 // cost the FP64 pipe more time than the whole FP32 stage work of a small system.
 template <class R, int L, int C>
-__device__ __forceinline__ typename Ctl<R>::T error_norm(const R* ut, const R* u0, const R* u1, R abstol, R reltol,
+__device__ __forceinline__ typename Ctl<R>::T error_norm(const R* ut, const R* u0, const R* u1, const Tol<R>& tol,
                                                          const Group<L>& g) {
     if (sizeof(R) == 8) {
         double acc = 0.0;
 #pragma unroll
         for (int c = 0; c < C; ++c) {
-            R sc = FMA(tmax(ABS(u0[c]), ABS(u1[c])), reltol, abstol);
+            R sc = FMA(tmax(ABS(u0[c]), ABS(u1[c])), tol.template r<C>(g.lane, c), tol.template a<C>(g.lane, c));
             double e = (double)(ut[c] / sc);
             acc = fma(e, e, acc);
         }
@@ -256,7 +249,8 @@ __device__ __forceinline__ typename Ctl<R>::T error_norm(const R* ut, const R* u
     float hi = 0.0f, lo = 0.0f;
 #pragma unroll
     for (int c = 0; c < C; ++c) {
-        const float sc = fmaf(tmax(fabsf((float)u0[c]), fabsf((float)u1[c])), (float)reltol, (float)abstol);
+        const float sc = fmaf(tmax(fabsf((float)u0[c]), fabsf((float)u1[c])), (float)tol.template r<C>(g.lane, c),
+                              (float)tol.template a<C>(g.lane, c));
         const float e = (float)ut[c] / sc;
         const float p = e * e;
         const float pe = fmaf(e, e, -p);
@@ -280,13 +274,13 @@ __device__ __forceinline__ typename Ctl<R>::T error_norm(const R* ut, const R* u
 // t is the model's time; bwd: the integration runs towards smaller t, so the
 // trial step goes to t - dt0 (dt0_tdir), and the magnitude is returned.
 template <class Model, class R, int L, int C, int ORDER>
-__device__ double initdt(const R* u0, const PR<R>* p, double t, bool bwd, double dtmax, double dtmin_user, R abstol,
-                         R reltol, R* f0, const Group<L>& g) {
+__device__ double initdt(const R* u0, const PR<R>* p, double t, bool bwd, double dtmax, double dtmin_user,
+                         const Tol<R>& tol, R* f0, const Group<L>& g) {
     double dtmin = nextafter(jmax(dtmin_user, jeps(t)), __longlong_as_double(0x7ff0000000000000LL));
     double smalldt = jmax(dtmin, 1e-6);
     R sk[C], f1[C], u1[C];
 #pragma unroll
-    for (int c = 0; c < C; ++c) sk[c] = FMA(ABS(u0[c]), reltol, abstol);
+    for (int c = 0; c < C; ++c) sk[c] = FMA(ABS(u0[c]), tol.template r<C>(g.lane, c), tol.template a<C>(g.lane, c));
     Model::template rhs<R, L, C>(f0, u0, p, t, g);
     double a0 = 0.0, a1 = 0.0;
 #pragma unroll
@@ -369,14 +363,14 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
     // the ensemble's tolerances, or per trajectory (requests merged into one
     // launch by the serving loop keep their own)
     R abstol = R(0), reltol = R(0);
-    const Ctrl K = make_ctrl<Alg::ORDER, Alg::IMPLICIT>(a);
-    // beta1, beta2 and qsteady_max change with a composite's current method
-    CT beta1 = (CT)K.beta1, beta2 = (CT)K.beta2, qsteady_max = (CT)K.qsteady_max, qsteady_min = (CT)K.qsteady_min;
-    const CT gam = (CT)K.gamma, qmin_inv = (CT)K.qmin_inv;
-    const CT qoldinit = (CT)K.qoldinit;
-    const CT inv_qmax = (CT)(1.0 / K.qmax), inv_qmax_first = (CT)(1.0 / K.qmax_first);
+    auto tol = [&]() { return Tol<R>{abstol, reltol, a.abstol_vec, a.reltol_vec}; };
 
     typename Alg::template Cache<R, C> cache;
+    // the PI controller's values: the method's own (a composite's current one)
+    auto KV = [&](int k) -> CT {
+        if constexpr (is_composite_alg<Alg>::value) return kval<CT>(a, cache.current, k);
+        else return kval<CT>(a, 0, k);
+    };
     StepStats st = {0, 0, 0, 0, 0, 0};
     int nsaved = 0;
     int isave = 0;
@@ -431,13 +425,13 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
     auto tstop_at = [&](int k) -> double { return TM(a.tstops[(k ^ bm) + (bm & a.ntstops)]); };
 
     double t = 0.0, tprev = 0.0, dt = 0.0, dtpropose = 0.0;
-    CT EEst = CT(1), q11 = CT(1), errold = qoldinit;
-    CT bank_errold = qoldinit, bank_q11 = CT(1);   // composite: the other method's controller state
+    CT EEst = CT(1), q11 = CT(1), errold = CT(1);
+    CT bank_errold = CT(1), bank_q11 = CT(1);   // composite: the other method's controller state
     // FP64 form: ln(errold) kept from the step that set errold, so errold^beta2 is one
     // exp series instead of a ctrl_pow (the same value: ctrl_pow(x, y) is
     // series_exp(y * series_ln(x)) for finite positive x); NaN when not kept
     double ln_qoldinit = 0.0, ln_errold = 0.0, bank_ln_errold = 0.0;
-    if constexpr (sizeof(CT) == 8) ln_qoldinit = series_ln((double)qoldinit);
+    if constexpr (sizeof(CT) == 8) ln_qoldinit = series_ln((double)kval<CT>(a, 0, KQOLD));
     bool do_error_check = true;
     long long iter = 0, success_iter = 0;
     bool accept = false, next_tstop = false;
@@ -494,7 +488,7 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
             if constexpr (is_composite_alg<Alg>::value) eig = cache.eigen_est;
             // iter -1: the recomputation (a W-method keeps the step's J, as the in-place
             // addsteps does, and its reuse state)
-            Alg::template step<Model, R, L, C>(cache, ut, utlo, uprev, uprevlo, p, TM(tprev), TM(dt), abstol, reltol,
+            Alg::template step<Model, R, L, C>(cache, ut, utlo, uprev, uprevlo, p, TM(tprev), TM(dt), tol(),
                                                -1, false, g, uncounted);
             if constexpr (is_composite_alg<Alg>::value) cache.eigen_est = eig;
         }
@@ -747,10 +741,6 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
         dtmax = a.dtmax > 0 ? a.dtmax : tf - t0;
         abstol = (R)(a.abstol_traj ? a.abstol_traj[j] : a.abstol);
         reltol = (R)(a.reltol_traj ? a.reltol_traj[j] : a.reltol);
-        beta1 = (CT)K.beta1;
-        beta2 = (CT)K.beta2;
-        qsteady_max = (CT)K.qsteady_max;
-        qsteady_min = (CT)K.qsteady_min;
         st = StepStats{0, 0, 0, 0, 0, 0};
         nsaved = 0;
         isave = 0;
@@ -777,14 +767,14 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
             while (k0 < a.ntstops && !(tstop_at(k0) > t0)) k0++;
             const double first_tstop = (k0 < a.ntstops && tstop_at(k0) < tf) ? tstop_at(k0) : tf;
             dt = initdt<Model, R, L, C, Alg::ORDER>(u, p, TM(t), bwd, jmin(fabs(dtmax), fabs(first_tstop - t0)),
-                                                     a.dtmin, abstol, reltol, Alg::template fsal_slot<R, C>(cache), g);
+                                                     a.dtmin, tol(), Alg::template fsal_slot<R, C>(cache), g);
             st.nf += 2;
         }
         dtpropose = dt;
         EEst = CT(1);
         q11 = CT(1);
-        errold = qoldinit;
-        bank_errold = qoldinit;
+        errold = kval<CT>(a, 0, KQOLD);
+        bank_errold = errold;
         bank_q11 = CT(1);
         ln_errold = bank_ln_errold = ln_qoldinit;
         do_error_check = true;
@@ -866,7 +856,8 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
                 Alg::template on_accept<R, C>(cache);
             } else {
                 // step_reject_controller!: dt /= min(1/qmin, q11/gamma)
-                const CT qq = q11 / gam;
+                const CT qmin_inv = KV(KQMININV);
+                const CT qq = q11 / KV(KGAM);
                 const CT f = (qmin_inv != qmin_inv || qq != qq) ? qq + qmin_inv : (qmin_inv < qq ? qmin_inv : qq);
                 dt = Ctl<R>::scale_dt(dt, f);
             }
@@ -888,11 +879,6 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
                 bank_ln_errold = l_old;
                 using NSA = typename Alg::NonStiff;
                 using SA = typename Alg::Stiff;
-                const Ctrl K2 = cur == 0 ? make_ctrl<NSA::ORDER, NSA::IMPLICIT>(a) : make_ctrl<SA::ORDER, SA::IMPLICIT>(a);
-                beta1 = (CT)K2.beta1;
-                beta2 = (CT)K2.beta2;
-                qsteady_max = (CT)K2.qsteady_max;
-                qsteady_min = (CT)K2.qsteady_min;
                 Alg::template enter<Model, R, L, C>(cache, uprev, uprevlo, p, TM(t), g, st);
             }
         }
@@ -937,13 +923,13 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
         }
         // ---- perform_step! (skipped for a step below eps(t) onto the tstop)
         if (!(next_tstop && plt(pabs(dt), peps(t)))) {
-            EEst = Alg::template step<Model, R, L, C>(cache, u, ulo, uprev, uprevlo, p, TM(t), TM(dt), abstol, reltol,
+            EEst = Alg::template step<Model, R, L, C>(cache, u, ulo, uprev, uprevlo, p, TM(t), TM(dt), tol(),
                                                       iter, EEst > CT(1), g, st);
         }
         // ---- loopfooter!
         if constexpr (is_composite_alg<Alg>::value) do_error_check = true;
         const double ttmp = t + dt;
-        const CT inv_qmaxc = success_iter == 0 ? inv_qmax_first : inv_qmax;
+        const CT inv_qmaxc = success_iter == 0 ? KV(KIQMAXF) : KV(KIQMAX);
         CT q = CT(1);
         double ln_eest = dnan();   // FP64 form: ln(EEst) of this attempt when EEst is finite and positive
         if (!a.adaptive) {
@@ -955,16 +941,16 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
             if constexpr (sizeof(CT) == 8) {
                 const bool fin = EEst > 0.0 && EEst < __longlong_as_double(0x7ff0000000000000LL);
                 if (fin) ln_eest = series_ln(EEst);
-                qq = fin ? series_exp(beta1 * ln_eest) : Ctl<R>::pw(EEst, beta1);
-                den = ln_errold == ln_errold ? series_exp(beta2 * ln_errold) : Ctl<R>::pw(errold, beta2);
+                qq = fin ? series_exp(KV(KB1) * ln_eest) : Ctl<R>::pw(EEst, KV(KB1));
+                den = ln_errold == ln_errold ? series_exp(KV(KB2) * ln_errold) : Ctl<R>::pw(errold, KV(KB2));
             } else {
-                qq = Ctl<R>::pw(EEst, beta1);
-                den = Ctl<R>::pw(errold, beta2);
+                qq = Ctl<R>::pw(EEst, KV(KB1));
+                den = Ctl<R>::pw(errold, KV(KB2));
             }
             q = qq / den;
             q11 = qq;
-            const CT x = q / gam;
-            q = x > qmin_inv ? qmin_inv : (x < inv_qmaxc ? inv_qmaxc : x);
+            const CT x = q / KV(KGAM);
+            q = x > KV(KQMININV) ? KV(KQMININV) : (x < inv_qmaxc ? inv_qmaxc : x);
         }
         accept = !a.adaptive || EEst <= CT(1);
         if (accept) {
@@ -978,10 +964,10 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
                 t = ttmp;
             }
             if (a.adaptive) {
-                if (qsteady_min <= q && q <= qsteady_max) q = CT(1);
-                errold = (EEst != EEst) ? EEst : (EEst > qoldinit ? EEst : qoldinit);
+                if (KV(KQSMIN) <= q && q <= KV(KQSMAX)) q = CT(1);
+                errold = (EEst != EEst) ? EEst : (EEst > KV(KQOLD) ? EEst : KV(KQOLD));
                 if constexpr (sizeof(CT) == 8)
-                    ln_errold = (EEst != EEst) ? dnan() : (EEst > qoldinit ? ln_eest : ln_qoldinit);
+                    ln_errold = (EEst != EEst) ? dnan() : (EEst > KV(KQOLD) ? ln_eest : ln_qoldinit);
                 const double dtnew = Ctl<R>::scale_dt(dt, q);
                 const double dtp = pmin(pabs(dtmax), pabs(dtnew));
                 dtpropose = pmax(pabs(dtp), pabs(pmax(peps(t), a.dtmin)));

@@ -188,6 +188,7 @@ struct ode_handle {
     DevBuf b_k, b_tq, b_out;                 // dense output and its evaluation
     DevBuf b_tstops;                         // the host API's tstops, sorted
     DevBuf b_idx;                            // the host API's save_idxs
+    DevBuf b_atol, b_rtol;                   // the host API's per-state tolerances
     // copy streams and events of the chunked host-API pipeline
     cudaStream_t copy_in = nullptr, copy_out = nullptr;
     cudaEvent_t pipe_in[4] = {}, pipe_done[4] = {};
@@ -324,6 +325,17 @@ int check_host_save_idxs(ode_handle* h, const ode_problem_desc* d, const ode_opt
     return ODE_OK;
 }
 
+// Per-state tolerances given in host memory: every entry finite, abstol >= 0, reltol > 0.
+int check_host_tolvec(ode_handle* h, const ode_problem_desc* d, const ode_options* o) {
+    for (int32_t i = 0; i < d->n_states; ++i) {
+        if (o->abstol_vec && !(o->abstol_vec[i] >= 0 && std::isfinite(o->abstol_vec[i])))
+            return fail(h, ODE_E_INVALID, "abstol_vec entries must be finite and >= 0");
+        if (o->reltol_vec && !(o->reltol_vec[i] > 0 && std::isfinite(o->reltol_vec[i])))
+            return fail(h, ODE_E_INVALID, "reltol_vec entries must be finite and > 0");
+    }
+    return ODE_OK;
+}
+
 // Output rows per save: the save_idxs, else every state.
 size_t out_rows(const ode_problem_desc* d, const ode_options* o) {
     return o->nsave_idxs > 0 ? (size_t)o->nsave_idxs : (size_t)d->n_states;
@@ -359,11 +371,74 @@ int stage_tstops(ode_handle* h, const ode_options* o, cudaStream_t s, ode_option
     return ODE_OK;
 }
 
+// The host API's per-state tolerances into the handle's buffers (ot's pointers
+// still the caller's host arrays), synchronously: n doubles each.
+int stage_tolvec(ode_handle* h, const ode_problem_desc* d, cudaStream_t s, ode_options* ot) {
+    int rc = ODE_OK;
+    const size_t bytes = (size_t)d->n_states * 8;
+    if (ot->abstol_vec) {
+        if ((rc = grow(h, h->b_atol, bytes))) return rc;
+        CUDA_TRY(h, cudaMemcpyAsync(h->b_atol.p, ot->abstol_vec, bytes, cudaMemcpyHostToDevice, s));
+        ot->abstol_vec = (const double*)h->b_atol.p;
+    }
+    if (ot->reltol_vec) {
+        if ((rc = grow(h, h->b_rtol, bytes))) return rc;
+        CUDA_TRY(h, cudaMemcpyAsync(h->b_rtol.p, ot->reltol_vec, bytes, cudaMemcpyHostToDevice, s));
+        ot->reltol_vec = (const double*)h->b_rtol.p;
+    }
+    if (ot->abstol_vec || ot->reltol_vec) CUDA_TRY(h, cudaStreamSynchronize(s));
+    return ODE_OK;
+}
+
 // Output slots per trajectory: the saveat points (or the kept step saves)
 // plus the start and end saves.
 size_t save_cap(const ode_options* o) {
     return (size_t)o->nsave + (o->save_everystep ? (size_t)o->max_step_saves : 0) + 2 +
            (o->callback ? 2 * (size_t)o->max_events : 0);
+}
+
+// The PI controller of each method of alg (slot 1: the composite's stiff method):
+// the method's defaults (alg_utils.jl: beta2 = 2/(5 order), beta1 = 7/(10 order),
+// qmin 1/5, qmax 10, qmax_first_step 10^4, gamma 9/10, qsteady_min 1, qsteady_max
+// 6/5 for the adaptive implicit family else 1, qoldinit 10^-4), then the caller's
+// knobs, in FP64 and FP32 for the two precisions' controllers.
+void resolve_controller(EnsembleArgs& a, int alg_id, const ode_options* o) {
+    struct Method { int order; bool implicit; };
+    Method m[2] = {{5, false}, {5, false}};
+    switch (alg_id) {
+        case ODE_VERN7: m[0] = {7, false}; break;
+        case ODE_RODAS5P: m[0] = {5, true}; break;
+        case ODE_ROSENBROCK23: m[0] = {2, true}; break;
+        case ODE_AUTOTSIT5_ROSENBROCK23: m[1] = {2, true}; break;   // Tsit5, then Rosenbrock23
+        default: break;
+    }
+    for (int s = 0; s < 2; ++s) {
+        double v[KNCTRL];
+        v[KB2] = 2.0 / (5.0 * m[s].order);
+        v[KB1] = 7.0 / (10.0 * m[s].order);
+        double qmin = 0.2, gamma = 0.9;
+        v[KQSMIN] = 1.0;
+        v[KQSMAX] = m[s].implicit ? 1.2 : 1.0;
+        v[KQOLD] = 1e-4;
+        if (o->controller_given) {   // each knob that is not NaN
+            auto set = [](double& f, double x) { if (!std::isnan(x)) f = x; };
+            set(v[KB1], o->beta1);
+            set(v[KB2], o->beta2);
+            set(v[KQOLD], o->qoldinit);
+            set(qmin, o->qmin);
+            set(gamma, o->gamma);
+            set(v[KQSMIN], o->qsteady_min);
+            set(v[KQSMAX], o->qsteady_max);
+        }
+        v[KQMININV] = 1.0 / qmin;
+        v[KGAM] = gamma;
+        v[KIQMAX] = 1.0 / (o->qmax > 0 ? o->qmax : 10.0);
+        v[KIQMAXF] = 1.0 / (o->qmax_first_step > 0 ? o->qmax_first_step : 10000.0);
+        for (int k = 0; k < KNCTRL; ++k) {
+            a.kd[s][k] = v[k];
+            a.kf[s][k] = (float)v[k];
+        }
+    }
 }
 
 EnsembleArgs make_args(ode_handle* h, const ode_problem_desc* d, const ode_options* o, int64_t N,
@@ -391,14 +466,9 @@ EnsembleArgs make_args(ode_handle* h, const ode_problem_desc* d, const ode_optio
     a.jac_reuse_gamma_tol = o->jac_reuse_gamma_tol < 0 ? 0.03 : o->jac_reuse_gamma_tol;
     a.adaptive = o->adaptive ? 1 : 0;
     a.forward_only = o->forward_only ? 1 : 0;
-    a.ctrl_given = o->controller_given ? 1 : 0;
-    a.c_beta1 = o->beta1;
-    a.c_beta2 = o->beta2;
-    a.c_qoldinit = o->qoldinit;
-    a.c_qmin = o->qmin;
-    a.c_gamma = o->gamma;
-    a.c_qsteady_min = o->qsteady_min;
-    a.c_qsteady_max = o->qsteady_max;
+    a.abstol_vec = o->abstol_vec;
+    a.reltol_vec = o->reltol_vec;
+    resolve_controller(a, d->alg_id, o);
     a.save_idxs = o->nsave_idxs > 0 ? o->save_idxs : nullptr;   // device memory at this point
     a.nsave_rows = o->nsave_idxs > 0 ? o->nsave_idxs : 0;
     a.t_out = t_out;
@@ -964,6 +1034,7 @@ int solve_host(ode_handle* h, const ode_problem_desc* d, const ode_options* o, i
     *h->h_abort = 0;
     ode_options ostaged;
     if ((rc = stage_tstops(h, o, h->main.stream, &ostaged))) return rc;
+    if ((rc = stage_tolvec(h, d, h->main.stream, &ostaged))) return rc;
     if (!ostaged.forward_only && N > 0) ostaged.forward_only = all_forward(tspan, N) ? 1 : 0;
     o = &ostaged;
     if (N > 0) {   // every buffer page-locked: the kernels work in place, no staging copies
@@ -1431,7 +1502,7 @@ void ode_destroy(ode_handle* h) {
     cudaSetDevice(h->device);
     cudaDeviceSynchronize();
     for (auto& r : h->running) finish(h, *r);
-    for (DevBuf* b : {&h->b_u0, &h->b_p, &h->b_tspan, &h->b_saveat, &h->b_tstops, &h->b_idx, &h->b_t, &h->b_u, &h->b_ns, &h->b_rc,
+    for (DevBuf* b : {&h->b_u0, &h->b_p, &h->b_tspan, &h->b_saveat, &h->b_tstops, &h->b_idx, &h->b_atol, &h->b_rtol, &h->b_t, &h->b_u, &h->b_ns, &h->b_rc,
                       &h->b_st, &h->b_npt})
         if (b->p) cudaFree(b->p);
     ctx_free(h->main);
@@ -1477,7 +1548,8 @@ int ode_solve_ensemble(ode_handle* h, const ode_problem_desc* d, const ode_optio
         return fail(h, ODE_E_INVALID, "null input or output buffer");
     if (o->nsave > 0 && !saveat) return fail(h, ODE_E_INVALID, "nsave > 0 but saveat is null");
     if ((rc = check_sizes(h, d, npt, N))) return rc;
-    if ((rc = check_host_tstops(h, o)) || (rc = check_host_save_idxs(h, d, o))) return rc;
+    if ((rc = check_host_tstops(h, o)) || (rc = check_host_save_idxs(h, d, o)) || (rc = check_host_tolvec(h, d, o)))
+        return rc;
     return solve_host(h, d, o, N, npt, u0, p, tspan, saveat, t_out, u_out, nullptr, nsaved, retcode, stats);
 }
 
@@ -1590,6 +1662,8 @@ int ode_submit(ode_handle* h, const ode_problem_desc* d, const ode_options* o, i
         return fail(h, ODE_E_INVALID, "null input or output buffer");
     if (o->nsave > 0 && !saveat) return fail(h, ODE_E_INVALID, "nsave > 0 but saveat is null");
     if ((rc = check_sizes(h, d, npt, N))) return rc;
+    if (o->abstol_vec || o->reltol_vec)
+        return fail(h, ODE_E_UNSUPPORTED, "per-state tolerances are not taken by the serving queue");
     if ((rc = check_host_tstops(h, o)) || (rc = check_host_save_idxs(h, d, o))) return rc;
     auto r = std::make_shared<Request>();
     r->d = *d;
@@ -1744,12 +1818,14 @@ int ode_autotune(ode_handle* h, const ode_problem_desc* d, const ode_options* o,
     if (rc) return rc;
     if (N <= 0 || !u0 || !p || !tspan) return fail(h, ODE_E_INVALID, "autotune needs a non-empty sample");
     if (o->nsave > 0 && !saveat) return fail(h, ODE_E_INVALID, "nsave > 0 but saveat is null");
-    if ((rc = check_host_tstops(h, o)) || (rc = check_host_save_idxs(h, d, o))) return rc;
+    if ((rc = check_host_tstops(h, o)) || (rc = check_host_save_idxs(h, d, o)) || (rc = check_host_tolvec(h, d, o)))
+        return rc;
     std::lock_guard<std::mutex> lk(h->api_mu);
     CUDA_TRY(h, cudaSetDevice(h->device));
     *h->h_abort = 0;
     ode_options ostaged;
     if ((rc = stage_tstops(h, o, h->main.stream, &ostaged))) return rc;
+    if ((rc = stage_tolvec(h, d, h->main.stream, &ostaged))) return rc;
     if (!ostaged.forward_only) ostaged.forward_only = all_forward(tspan, N) ? 1 : 0;
     o = &ostaged;
     const size_t n = (size_t)d->n_states, np = (size_t)d->n_params, cap = save_cap(o), rows = out_rows(d, o);
@@ -1996,14 +2072,9 @@ extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_o
     a.jac_reuse_gamma_tol = o->jac_reuse_gamma_tol < 0 ? 0.03 : o->jac_reuse_gamma_tol;
     a.adaptive = o->adaptive ? 1 : 0;
     a.forward_only = o->forward_only ? 1 : 0;
-    a.ctrl_given = o->controller_given ? 1 : 0;
-    a.c_beta1 = o->beta1;
-    a.c_beta2 = o->beta2;
-    a.c_qoldinit = o->qoldinit;
-    a.c_qmin = o->qmin;
-    a.c_gamma = o->gamma;
-    a.c_qsteady_min = o->qsteady_min;
-    a.c_qsteady_max = o->qsteady_max;
+    a.abstol_vec = o->abstol_vec;
+    a.reltol_vec = o->reltol_vec;
+    resolve_controller(a, d->alg_id, o);
     a.save_idxs = o->nsave_idxs > 0 ? o->save_idxs : nullptr;   // device memory at this point
     a.nsave_rows = o->nsave_idxs > 0 ? o->nsave_idxs : 0;
     a.t_out = t_out;

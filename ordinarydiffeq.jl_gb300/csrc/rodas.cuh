@@ -219,7 +219,7 @@ struct Rodas5PT {
 
     template <class Model, class R, int L, int C>
     __device__ static typename Ctl<R>::T step(Cache<R, C>& c, R* u, R* ulo, const R* up, const R* uplo,
-                                             const PR<R>* p, double t, double dt, R abstol, R reltol, long long iter,
+                                             const PR<R>* p, double t, double dt, const Tol<R>& tol, long long iter,
                                              bool errorfail, const Group<L>& g, StepStats& st) {
         constexpr int NP = Model::NP;
         // dt-derived coefficients: FP64 like the reference; in the mixed mode they
@@ -328,7 +328,7 @@ struct Rodas5PT {
                 Acc<R>::update(u[i], ulo[i], R(1), (R)cs.value(), up[i], uplo[i]);
             }
         }
-        return error_norm<R, L, C>(c.ks[7], up, u, abstol, reltol, g);
+        return error_norm<R, L, C>(c.ks[7], up, u, tol, g);
     }
 
     // Dense coefficients k_j = sum_i H[j,i] ks_i (rosenbrock_perform_step.jl:811-815),

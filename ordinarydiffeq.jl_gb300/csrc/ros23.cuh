@@ -140,7 +140,7 @@ struct Rosenbrock23T {
 
     template <class Model, class R, int L, int C>
     __device__ static typename Ctl<R>::T step(Cache<R, C>& c, R* u, R* ulo, const R* up, const R* uplo,
-                                             const PR<R>* p, double t, double dt, R abstol, R reltol, long long iter,
+                                             const PR<R>* p, double t, double dt, const Tol<R>& tol, long long iter,
                                              bool errorfail, const Group<L>& g, StepStats& st) {
         constexpr int NP = Model::NP;
         R dr, idg, ninv, dto2, dto6, c32;
@@ -220,7 +220,7 @@ struct Rosenbrock23T {
         R tmp[C];
 #pragma unroll
         for (int i = 0; i < C; ++i) tmp[i] = dto6 * (FMA(R(-2), k2[i], k1[i]) + k3[i]);
-        return error_norm<R, L, C>(tmp, up, u, abstol, reltol, g);
+        return error_norm<R, L, C>(tmp, up, u, tol, g);
     }
 
     // y0 + dt (c1 k1 + c2 k2), c1 = th (1 - th) / (1 - 2d), c2 = th (th - 2d) / (1 - 2d)

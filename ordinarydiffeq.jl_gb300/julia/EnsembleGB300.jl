@@ -107,6 +107,7 @@ mutable struct Options
     controller_given::Int32; reserved5::Int32
     beta1::Float64; beta2::Float64; qoldinit::Float64; qmin::Float64; gamma::Float64
     qsteady_min::Float64; qsteady_max::Float64
+    abstol_vec::Ptr{Float64}; reltol_vec::Ptr{Float64}
 end
 # the knobs of solve(...; controller = PIController(beta1, beta2; qoldinit, qmin, qmax,
 # qmax_first_step, gamma, qsteady_min, qsteady_max)): beta1, beta2 and qoldinit on the
@@ -238,19 +239,25 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem,
     rows = save_idxs === nothing ? n : length(sidx)
     # a dt of either sign is taken in the direction of the span (handle_dt!, solve.jl:968-985)
     cg, ck, cqmax, cqmaxfirst = controller_knobs(controller)
-    o = Options(reltol, abstol, dtmax, dtmin, abs(dt), maxiters, ss, se, save_end === nothing ? -1 : Int32(save_end),
+    # array tolerances: one per state (the scalar fields then hold their smallest entries)
+    atv = abstol isa AbstractVector ? collect(Float64, abstol) : Float64[]
+    rtv = reltol isa AbstractVector ? collect(Float64, reltol) : Float64[]
+    atol_s = isempty(atv) ? Float64(abstol) : minimum(atv)
+    rtol_s = isempty(rtv) ? Float64(reltol) : minimum(rtv)
+    o = Options(rtol_s, atol_s, dtmax, dtmin, abs(dt), maxiters, ss, se, save_end === nothing ? -1 : Int32(save_end),
                 scalar, length(sv), 0, cqmaxfirst, cqmax, ens.lanes_per_traj, ens.scheduler, 0, -1, everystep,
                 everystep ? max_step_saves : 0, cb, cb ? callback.interp_points : 10, cb ? callback.max_events : 0,
                 length(tst), isempty(tst) ? Ptr{Float64}(C_NULL) : pointer(tst), jac_reuse(alg)[1], Int32(0),
                 jac_reuse(alg)[2], length(sidx), Int32(0), isempty(sidx) ? Ptr{Int32}(C_NULL) : pointer(sidx),
-                Int32(adaptive), Int32(0), cg, Int32(0), ck...)
+                Int32(adaptive), Int32(0), cg, Int32(0), ck...,
+                isempty(atv) ? Ptr{Float64}(C_NULL) : pointer(atv), isempty(rtv) ? Ptr{Float64}(C_NULL) : pointer(rtv))
     d = ProblemDesc(model, alg_id(alg), n, npar, ens.precision === :mixed ? 1 : 0, 0)
     cap = length(sv) + (everystep ? max_step_saves : 0) + 2 + (cb ? 2 * callback.max_events : 0)
     t_out = fill(NaN, N, cap); u_out = fill(NaN, N, rows, cap)   # [(s*rows + i)*N + j] -> u_out[j, i, s]
     nsaved = zeros(Int32, N); rc = zeros(Int32, N); st = Vector{Stats}(undef, N)
     # dense output (solve.jl:145-146) for every-step saves of one state count
     isdense = dense && everystep && npt == C_NULL && save_idxs === nothing
-    GC.@preserve tst sidx if isdense   # o holds pointers into tst and sidx
+    GC.@preserve tst sidx atv rtv if isdense   # o holds pointers into tst, sidx, atv and rtv
         nk = ccall((:ode_dense_nk, LIB), Cint, (Cint,), alg_id(alg))
         k_out = zeros(N, n, nk, cap)   # [((s*nk + q)*n + i)*N + j] -> k_out[j, i, q, s]
         status = ccall((:ode_solve_ensemble_dense, LIB), Cint,

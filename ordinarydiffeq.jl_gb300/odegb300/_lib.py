@@ -45,7 +45,8 @@ class Options(C.Structure):
                 ("adaptive", C.c_int32), ("forward_only", C.c_int32),
                 ("controller_given", C.c_int32), ("reserved5", C.c_int32), ("beta1", C.c_double),
                 ("beta2", C.c_double), ("qoldinit", C.c_double), ("qmin", C.c_double), ("gamma", C.c_double),
-                ("qsteady_min", C.c_double), ("qsteady_max", C.c_double)]
+                ("qsteady_min", C.c_double), ("qsteady_max", C.c_double),
+                ("abstol_vec", C.POINTER(C.c_double)), ("reltol_vec", C.POINTER(C.c_double))]
 
 
 class Stats(C.Structure):

@@ -332,7 +332,18 @@ def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_ste
     if isinstance(alg, Rosenbrock23):   # its W-method Jacobian reuse knobs
         o.max_jac_age = alg.max_jac_age
         o.jac_reuse_gamma_tol = alg.jac_reuse_gamma_tol
-    o.reltol, o.abstol = reltol, abstol
+    # array tolerances: one per state (solve(...; abstol = [...])); the scalar fields
+    # then hold their smallest entries (checked, unused)
+    keep = []
+    for name, tol in (("abstol", abstol), ("reltol", reltol)):
+        if np.ndim(tol):
+            v = np.ascontiguousarray(tol, dtype=np.float64).ravel()
+            keep.append(v)
+            setattr(o, name + "_vec", v.ctypes.data_as(C.POINTER(C.c_double)))
+            setattr(o, name, float(v.min()))
+        else:
+            setattr(o, name, float(tol))
+    o._keep_tol = keep
     o.dt = abs(dt or 0.0)   # either sign is taken in the span's direction (handle_dt!, solve.jl:968-985)
     o.dtmax = dtmax or 0.0
     o.dtmin = dtmin or 0.0

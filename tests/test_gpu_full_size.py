@@ -57,6 +57,7 @@ def device_solve(wl, precision, ir=None):
     npt = t(wl["n_per_traj"]) if wl.get("n_per_traj") is not None else None
     vp = lambda x: C.c_void_p(x.data_ptr()) if x is not None else None
     stream = torch.cuda.Stream(dev)
+    torch.cuda.synchronize(dev)   # the inputs' copies are done before the solve's stream reads them
     _lib.check(L.ode_solve_ensemble_device(h, C.byref(d), C.byref(o), N, vp(npt), *[vp(x) for x in ins],
                                            vp(out["t"]), vp(out["u"]), vp(out["nsaved"]), vp(out["retcode"]),
                                            vp(out["stats"]), C.c_void_p(stream.cuda_stream)), h)

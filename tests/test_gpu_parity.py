@@ -312,6 +312,7 @@ def test_abort_stops_running_kernels():
     stream = torch.cuda.Stream(dev)
     vp = lambda x: C.c_void_p(x.data_ptr())
     t0 = time.perf_counter()
+    torch.cuda.synchronize(dev)   # the inputs' copies are done before the solve's stream reads them
     _lib.check(L.ode_solve_ensemble_device(h, C.byref(d), C.byref(o), N, None, vp(du0), vp(dp), vp(dts), None,
                                            vp(tout), vp(uout), vp(ns), vp(rc), vp(st),
                                            C.c_void_p(stream.cuda_stream)), h)
@@ -352,6 +353,7 @@ def _device_solve(model, alg, u0, p, ts, saveat, reltol, abstol, precision="fp64
     dn = t(npt) if npt is not None else None
     vp = lambda x: C.c_void_p(x.data_ptr()) if x is not None else None
     stream = torch.cuda.Stream(dev)
+    torch.cuda.synchronize(dev)   # the inputs' copies are done before the solve's stream reads them
     _lib.check(L.ode_solve_ensemble_device(h, C.byref(d), C.byref(o), N, vp(dn), *[vp(b) for b in bufs],
                                            C.c_void_p(stream.cuda_stream)), h)
     stream.synchronize()

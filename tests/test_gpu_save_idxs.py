@@ -93,6 +93,7 @@ def test_device_entry_and_serving_with_save_idxs():
             torch.empty((N, 6), dtype=torch.int64, device=dev)]
     vp = lambda x: C.c_void_p(x.data_ptr())
     stream = torch.cuda.Stream(dev)
+    torch.cuda.synchronize(dev)   # the inputs' copies are done before the solve's stream reads them
     _lib.check(L.ode_solve_ensemble_device(h, C.byref(d), C.byref(o), N, None, *[vp(b) for b in bufs],
                                            C.c_void_p(stream.cuda_stream)), h)
     stream.synchronize()

@@ -378,6 +378,24 @@ def test_controller_knobs():
     assert icon["retcode"] == O.RC_SUCCESS and icon["stats"]["naccept"] != base["stats"]["naccept"]
 
 
+def test_array_tolerances():
+    # calculate_residuals with array abstol/reltol (calculate_residuals.jl:117-125): equal
+    # entries are the scalar solve bit for bit; tightening one state's tolerance takes
+    # more steps; ROBER's classic per-species abstol runs to the end
+    kw = dict(saveat=[1.0, 10.0], saveat_given=True)
+    p = [0.04, 3e7, 1e4]
+    sc = O.solve(O.RODAS5P, O.ROBERTSON, [1.0, 0.0, 0.0], p, (0.0, 10.0), reltol=1e-6, abstol=1e-8, **kw)
+    vec = O.solve(O.RODAS5P, O.ROBERTSON, [1.0, 0.0, 0.0], p, (0.0, 10.0), reltol=[1e-6] * 3,
+                  abstol=[1e-8] * 3, **kw)
+    assert np.array_equal(sc["u"], vec["u"]) and sc["stats"] == vec["stats"]
+    tight = O.solve(O.RODAS5P, O.ROBERTSON, [1.0, 0.0, 0.0], p, (0.0, 10.0), reltol=1e-6,
+                    abstol=[1e-8, 1e-14, 1e-8], **kw)
+    assert tight["stats"]["naccept"] > sc["stats"]["naccept"]
+    rober = O.solve(O.RODAS5P, O.ROBERTSON, [1.0, 0.0, 0.0], p, (0.0, 1e5), reltol=1e-4,
+                    abstol=[1e-8, 1e-14, 1e-6], saveat=[1e5], saveat_given=True)
+    assert rober["retcode"] == O.RC_SUCCESS and abs(rober["u"][-1].sum() - 1.0) < 1e-6
+
+
 def test_tstops_from_a_range_are_a_subset_of_sol_t():
     # ode_tstops_tests.jl:97-105 ("Late binding tstops"): 0:0.1:1 is a subset of sol.t
     ts = np.arange(0, 11) * 0.1

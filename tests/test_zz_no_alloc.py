@@ -43,6 +43,7 @@ def _device_solve(entry, model, alg_id, prec, u0, p, ts, saveat, reltol, abstol,
     rc = torch.zeros(N, dtype=torch.int32, device=dev)
     st = torch.zeros((N, 6), dtype=torch.int64, device=dev)
     ptr = lambda x: C.c_void_p(x.data_ptr()) if x is not None else None
+    torch.cuda.synchronize(dev)   # the inputs' copies are done before the solve's stream reads them
     stream = torch.cuda.Stream(dev)
     args = (C.byref(d), C.byref(o), N, ptr(b_npt), ptr(b_u0), ptr(b_p), ptr(b_ts), ptr(b_sv), ptr(t_out),
             ptr(u_out), ptr(ns), ptr(rc), ptr(st), C.c_void_p(stream.cuda_stream))
