@@ -41,6 +41,32 @@ def test_struct_layouts_match_the_bindings():
     assert L.ode_problem_desc_size() == C.sizeof(_lib.ProblemDesc)
 
 
+def _julia_struct(name):
+    src = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "ordinarydiffeq.jl_gb300",
+                            "julia", "EnsembleGB300.jl")).read()
+    body = re.search(r"(?:mutable )?struct %s\n(.*?)\nend" % name, src, re.S).group(1)
+    out = []
+    for part in re.split(r"[;\n]", body):
+        if part.strip():
+            n, t = part.split("::")
+            out.append((n.strip(), t.strip()))
+    return out
+
+
+def test_julia_binding_mirrors_the_c_structs():
+    # the Julia ccall glue passes ode_options and ode_problem_desc by reference: its
+    # structs must hold the same fields, in order, with the same widths
+    width = {"Float64": C.c_double, "Int64": C.c_int64, "Int32": C.c_int32}
+    for jname, ctype in (("Options", _lib.Options), ("ProblemDesc", _lib.ProblemDesc)):
+        jl = _julia_struct(jname)
+        assert [n for n, _ in jl] == [n for n, _ in ctype._fields_], jname
+        for (n, jt), (_, ct) in zip(jl, ctype._fields_):
+            if jt.startswith("Ptr{"):
+                assert C.sizeof(ct) == C.sizeof(C.c_void_p), n
+            else:
+                assert C.sizeof(width[jt]) == C.sizeof(ct), n
+
+
 def test_abi_version_and_defaults_without_gpu():
     L = _lib.load()
     assert L.ode_abi_version() == 8
