@@ -125,6 +125,8 @@ def parse():
     ap.add_argument("--config", default="robertson", choices=sorted(CONFIGS))
     ap.add_argument("--trajectories", type=int, default=0)
     ap.add_argument("--lanes", type=int, default=0, help="lanes per trajectory of the device solves (0: default)")
+    ap.add_argument("--scheduler", default="auto", choices=["auto", "static", "persistent"],
+                    help="scheduler of the device solves")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU-baseline sample time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-small", action="store_true",
@@ -370,7 +372,7 @@ def measure(cfg, args, ctx, steps, warmup, headline=False):
 
     def solve_device(prec, ir=None, u0=None, p=None):
         ens = odegb300.EnsembleGB300(precision=prec, ir_sweeps=(ir_default if ir is None else ir)
-                                     if prec == "mixed" else -1, lanes_per_traj=args.lanes)
+                                     if prec == "mixed" else -1, lanes_per_traj=args.lanes, scheduler=args.scheduler)
         o = _options(wl["reltol"], wl["abstol"], None, None, None, 1000000, sv, ens, None, None, cb)
         # the device entry point cannot see the spans: the caller states that all run forward
         o.forward_only = fwd_spans
@@ -506,7 +508,7 @@ def measure(cfg, args, ctx, steps, warmup, headline=False):
     h_st = torch.empty((N, 6), dtype=torch.int64).pin_memory()
     best_prec = "fp64" if best == "fp64" else "mixed"
     ens_e2e = odegb300.EnsembleGB300(precision=best_prec, ir_sweeps=results[best]["ir_sweeps"]
-                                     if best_prec == "mixed" else -1)
+                                     if best_prec == "mixed" else -1, scheduler=args.scheduler)
     o_e2e = _options(wl["reltol"], wl["abstol"], None, None, None, 1000000, sv, ens_e2e, None, None, cb,
                      tstops=wl.get("tstops"))
     d_e2e = _lib.ProblemDesc(model, alg.alg_id, n, wl["p"].shape[0], ens_e2e.prec_id(), 0)
@@ -640,7 +642,8 @@ def run_profile_small(args, ctx):
     t_tst = T(np.sort(np.asarray(tst, dtype=np.float64))) if tst is not None else None
     ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None
     for prec in ("fp64", "mixed"):
-        ens = odegb300.EnsembleGB300(precision=prec, ir_sweeps=wl.get("ir_sweeps", -1) if prec == "mixed" else -1)
+        ens = odegb300.EnsembleGB300(precision=prec, ir_sweeps=wl.get("ir_sweeps", -1) if prec == "mixed" else -1,
+                                     scheduler=args.scheduler)
         o = _options(wl["reltol"], wl["abstol"], None, None, None, 1000000, sv, ens, None, None, cb)
         if t_tst is not None:
             o.ntstops = int(t_tst.numel())
