@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define ODE_ABI_VERSION 8
+#define ODE_ABI_VERSION 9
 
 typedef struct ode_handle ode_handle;
 
@@ -215,7 +215,9 @@ typedef struct {
        (alg_utils.jl); 1: each field below that is not NaN replaces the default (for both
        methods of a composite) */
     int32_t controller_given;
-    int32_t reserved5;
+    int32_t force_dtmin;        /* 1: the reference's force_dtmin = true: a step at or below max(eps(t), dtmin)
+                                   is accepted whatever its error, and no DtLessThanMin or Unstable exit is
+                                   taken on dt (check_error.jl:91-106, integrator_utils.jl:613-623) */
     double beta1, beta2, qoldinit, qmin, gamma, qsteady_min, qsteady_max;
     /* Per-state tolerances (solve(...; abstol = [...], reltol = [...]): calculate_residuals with
        array tolerances, calculate_residuals.jl:9-14,117-125, and the initial-step scale): n_states

@@ -1538,7 +1538,9 @@ void loopfooter(Integ& I) {
     double ttmp = I.t + I.dt;
     if (I.o.adaptive) {
         double q = stepsize_controller(I);
-        I.accept_step = I.EEst <= 1.0;
+        // accept_step_controller, or force_dtmin at abs(dt) <= timedepentdtmin
+        // (integrator_utils.jl:613-623, utils.jl:93: abs(max(eps(t), dtmin)))
+        I.accept_step = I.EEst <= 1.0 || (I.o.force_dtmin && std::fabs(I.dt) <= std::fabs(jmax(jeps(I.t), I.o.dtmin)));
         if (I.accept_step) {
             I.st.naccept++;
             I.tprev = I.t;
@@ -1670,7 +1672,7 @@ int check_error(Integ& I) {
     if (I.dt != I.dt) return ORC_RC_DTNAN;
     if (I.iter > I.o.maxiters) return ORC_RC_MAXITERS;
     bool acc = I.accept_step;
-    if (I.o.adaptive) {
+    if (I.o.adaptive && !I.o.force_dtmin) {   // check_error.jl:91
         // t + dt < tdir * first(tstops), as the reference writes it for either direction
         double next_tstop = I.itstop < I.tstops.size() ? I.tdir * I.tstops[I.itstop] : I.tdir * INFINITY;
         if (std::fabs(I.dt) <= std::fabs(I.o.dtmin) && (!acc || I.t + I.dt < next_tstop))

@@ -59,6 +59,7 @@ typedef struct {
     double jac_reuse_gamma_tol; /* ... while |dtgamma / dtgamma_J - 1| <= this (0.03) */
     int32_t ctrl_given;       /* 1: the PIController knobs below replace the defaults where not NaN */
     double c_beta1, c_beta2, c_qoldinit, c_qmin, c_gamma, c_qsteady_min, c_qsteady_max;
+    int32_t force_dtmin;       /* accept steps at max(eps(t), dtmin); no dt exits (check_error.jl:91) */
     const double* abstol_vec;  /* per-state tolerances (n entries), or NULL for the scalars */
     const double* reltol_vec;
 } orc_opts;

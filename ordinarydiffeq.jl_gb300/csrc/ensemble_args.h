@@ -56,6 +56,7 @@ struct EnsembleArgs {
     int ir_sweeps;          // mixed Rosenbrock: refinement sweeps per solve
     int adaptive;           // 0: fixed steps of dt, every step accepted
     int forward_only;       // every span runs forward: the kernel's forward-only form may run
+    int force_dtmin;        // accept steps at max(eps(t), dtmin) whatever their error
     // The PI controller of each method (slot 1: a composite's stiff method), its
     // defaults and the caller's knobs resolved on the host, in both precisions
     // (kernel parameters: read where used, held in no register)

@@ -903,10 +903,10 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
             else if (bits_nan(db)) e = RC_DTNAN;
             else if (iter > a.maxiters) e = RC_MAXITERS;
             // t + dt < tdir * first(tstops) in the reference's own time
-            else if (a.adaptive && ple(pabs(dt), pabs(a.dtmin)) &&
+            else if (a.adaptive && !a.force_dtmin && ple(pabs(dt), pabs(a.dtmin)) &&
                      (!accept || (bwd ? t + dt > tnext : t + dt < tnext)))
                 e = RC_DTLESSTHANMIN;
-            else if (a.adaptive && !accept && ple(pabs(dt), peps(t))) e = RC_UNSTABLE;
+            else if (a.adaptive && !a.force_dtmin && !accept && ple(pabs(dt), peps(t))) e = RC_UNSTABLE;
             else if (accept) {
                 bool bad = false;
 #pragma unroll
@@ -953,6 +953,8 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
             q = x > KV(KQMININV) ? KV(KQMININV) : (x < inv_qmaxc ? inv_qmaxc : x);
         }
         accept = !a.adaptive || EEst <= CT(1);
+        // force_dtmin: a step at the smallest dt is taken whatever its error
+        if (!accept && a.force_dtmin) accept = ple(pabs(dt), pabs(pmax(peps(t), a.dtmin)));
         if (accept) {
             st.naccept++;
             tprev = t;

@@ -468,6 +468,7 @@ EnsembleArgs make_args(ode_handle* h, const ode_problem_desc* d, const ode_optio
     a.forward_only = o->forward_only ? 1 : 0;
     a.abstol_vec = o->abstol_vec;
     a.reltol_vec = o->reltol_vec;
+    a.force_dtmin = o->force_dtmin ? 1 : 0;
     resolve_controller(a, d->alg_id, o);
     a.save_idxs = o->nsave_idxs > 0 ? o->save_idxs : nullptr;   // device memory at this point
     a.nsave_rows = o->nsave_idxs > 0 ? o->nsave_idxs : 0;
@@ -2074,6 +2075,7 @@ extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_o
     a.forward_only = o->forward_only ? 1 : 0;
     a.abstol_vec = o->abstol_vec;
     a.reltol_vec = o->reltol_vec;
+    a.force_dtmin = o->force_dtmin ? 1 : 0;
     resolve_controller(a, d->alg_id, o);
     a.save_idxs = o->nsave_idxs > 0 ? o->save_idxs : nullptr;   // device memory at this point
     a.nsave_rows = o->nsave_idxs > 0 ? o->nsave_idxs : 0;

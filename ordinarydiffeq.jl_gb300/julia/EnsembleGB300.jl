@@ -104,7 +104,7 @@ mutable struct Options
     max_jac_age::Int32; reserved2::Int32; jac_reuse_gamma_tol::Float64
     nsave_idxs::Int32; reserved3::Int32; save_idxs::Ptr{Int32}
     adaptive::Int32; forward_only::Int32
-    controller_given::Int32; reserved5::Int32
+    controller_given::Int32; force_dtmin::Int32
     beta1::Float64; beta2::Float64; qoldinit::Float64; qmin::Float64; gamma::Float64
     qsteady_min::Float64; qsteady_max::Float64
     abstol_vec::Ptr{Float64}; reltol_vec::Ptr{Float64}
@@ -200,7 +200,8 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem,
                            ens::EnsembleGB300; trajectories, saveat = Float64[], reltol = 1e-3, abstol = 1e-6,
                            dt = 0.0, dtmax = 0.0, dtmin = 0.0, maxiters = 1_000_000, save_start = nothing,
                            save_end = nothing, save_everystep = isempty(saveat), max_step_saves = 1024, seed = 0,
-                           save_idxs = nothing, adaptive = true, controller = nothing, callback = nothing,
+                           save_idxs = nothing, adaptive = true, controller = nothing, force_dtmin = false,
+                           callback = nothing,
                            dense = save_everystep && isempty(saveat) && save_idxs === nothing,
                            tstops = Float64[], kwargs...)
     t0 = time()
@@ -249,7 +250,7 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem,
                 everystep ? max_step_saves : 0, cb, cb ? callback.interp_points : 10, cb ? callback.max_events : 0,
                 length(tst), isempty(tst) ? Ptr{Float64}(C_NULL) : pointer(tst), jac_reuse(alg)[1], Int32(0),
                 jac_reuse(alg)[2], length(sidx), Int32(0), isempty(sidx) ? Ptr{Int32}(C_NULL) : pointer(sidx),
-                Int32(adaptive), Int32(0), cg, Int32(0), ck...,
+                Int32(adaptive), Int32(0), cg, Int32(force_dtmin), ck...,
                 isempty(atv) ? Ptr{Float64}(C_NULL) : pointer(atv), isempty(rtv) ? Ptr{Float64}(C_NULL) : pointer(rtv))
     d = ProblemDesc(model, alg_id(alg), n, npar, ens.precision === :mixed ? 1 : 0, 0)
     cap = length(sv) + (everystep ? max_step_saves : 0) + 2 + (cb ? 2 * callback.max_events : 0)

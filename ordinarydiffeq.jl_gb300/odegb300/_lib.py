@@ -43,7 +43,7 @@ class Options(C.Structure):
                 ("max_jac_age", C.c_int32), ("reserved2", C.c_int32), ("jac_reuse_gamma_tol", C.c_double),
                 ("nsave_idxs", C.c_int32), ("reserved3", C.c_int32), ("save_idxs", C.POINTER(C.c_int32)),
                 ("adaptive", C.c_int32), ("forward_only", C.c_int32),
-                ("controller_given", C.c_int32), ("reserved5", C.c_int32), ("beta1", C.c_double),
+                ("controller_given", C.c_int32), ("force_dtmin", C.c_int32), ("beta1", C.c_double),
                 ("beta2", C.c_double), ("qoldinit", C.c_double), ("qmin", C.c_double), ("gamma", C.c_double),
                 ("qsteady_min", C.c_double), ("qsteady_max", C.c_double),
                 ("abstol_vec", C.POINTER(C.c_double)), ("reltol_vec", C.POINTER(C.c_double))]

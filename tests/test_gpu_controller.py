@@ -53,3 +53,20 @@ def test_steady_band_keeps_dt(precision):
     d = np.diff(t)
     assert (g["stats"]["nreject"] == 0).all() and len(d) > 5
     assert np.allclose(d[:-1], d[0], rtol=1e-12, atol=0) and d[-1] <= d[0]
+
+
+@pytest.mark.parametrize("alg", ["tsit5", "vern7"])
+def test_force_dtmin_matches_oracle(alg):
+    # a tolerance that needs steps below dtmin: DtLessThanMin, or with force_dtmin
+    # every step at dtmin, as in the oracle
+    N = 128
+    u0, p, ts = lorenz_inputs(N, seed=52)
+    kw = dict(dtmin=2e-3 if alg == "tsit5" else 3e-2)   # above the steps each method takes at 1e-12
+    g0 = gpu("lorenz", alg, u0, p, ts, 0.1, 1e-12, 1e-12, **kw)
+    o0 = oracle("lorenz", alg, u0, p, ts, 0.1, 1e-12, 1e-12, **kw)
+    assert np.array_equal(g0["retcode"], o0["retcode"]) and (g0["retcode"] == 4).any()
+    g = gpu("lorenz", alg, u0, p, ts, 0.1, 1e-12, 1e-12, force_dtmin=True, **kw)
+    o = oracle("lorenz", alg, u0, p, ts, 0.1, 1e-12, 1e-12, force_dtmin=True, **kw)
+    assert (g["retcode"] == 1).all()
+    c = compare(g, o, 1e-9, 1e-9, step_slack=0)
+    assert c["ok"] and c["steps_ok"], c

@@ -396,6 +396,20 @@ def test_array_tolerances():
     assert rober["retcode"] == O.RC_SUCCESS and abs(rober["u"][-1].sum() - 1.0) < 1e-6
 
 
+def test_force_dtmin():
+    # force_dtmin (check_error.jl:91, integrator_utils.jl:613-623): a tolerance that
+    # needs steps below dtmin ends in DtLessThanMin; forced, every step is taken at
+    # dtmin (500 steps of 2e-3 over (0, 1)) and the solve succeeds
+    kw = dict(saveat=[0.5, 1.0], saveat_given=True, reltol=1e-12, abstol=1e-12, dtmin=2e-3)
+    a = O.solve(O.TSIT5, O.LORENZ, [1.0, 0.0, 0.0], [10.0, 28.0, 8 / 3], (0.0, 1.0), **kw)
+    assert a["retcode"] == O.RC_DTLESSTHANMIN
+    b = O.solve(O.TSIT5, O.LORENZ, [1.0, 0.0, 0.0], [10.0, 28.0, 8 / 3], (0.0, 1.0), force_dtmin=True, **kw)
+    assert b["retcode"] == O.RC_SUCCESS and b["stats"]["naccept"] == 500
+    ref = O.solve(O.TSIT5, O.LORENZ, [1.0, 0.0, 0.0], [10.0, 28.0, 8 / 3], (0.0, 1.0), saveat=[0.5, 1.0],
+                  saveat_given=True, reltol=1e-12, abstol=1e-12)
+    assert np.abs(b["u"] - ref["u"]).max() < 1e-6
+
+
 def test_tstops_from_a_range_are_a_subset_of_sol_t():
     # ode_tstops_tests.jl:97-105 ("Late binding tstops"): 0:0.1:1 is a subset of sol.t
     ts = np.arange(0, 11) * 0.1
