@@ -645,6 +645,7 @@ def run_profile_small(args, ctx):
         ens = odegb300.EnsembleGB300(precision=prec, ir_sweeps=wl.get("ir_sweeps", -1) if prec == "mixed" else -1,
                                      scheduler=args.scheduler)
         o = _options(wl["reltol"], wl["abstol"], None, None, None, 1000000, sv, ens, None, None, cb)
+        o.forward_only = int(bool(np.all(wl["tspan"][1] >= wl["tspan"][0])))   # the timed solves' kernels
         if t_tst is not None:
             o.ntstops = int(t_tst.numel())
             o.tstops = C.cast(C.c_void_p(t_tst.data_ptr()), C.POINTER(C.c_double))
