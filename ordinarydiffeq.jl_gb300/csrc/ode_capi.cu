@@ -669,7 +669,7 @@ int launch_variant(ode_handle* h, const KernelVariant* v, EnsembleArgs a, int sc
         CUDA_TRY(h, cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s));
         a.queue = queue;
         a.persistent = 1;
-        a.refill_lanes = 8;    // 100k van der Pol (AutoTsit5): 232 ms at 8 idle lanes, 276 at 16, 436 at 32
+        a.refill_lanes = 4;    // 100k van der Pol (AutoTsit5) FP64: 217 ms at 4 idle lanes, 215 at 2, 232 at 8, 276 at 16, 436 at 32
     } else {
         long long threads = groups * v->lanes;
         grid = (int)((threads + block - 1) / block);
