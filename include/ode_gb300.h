@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define ODE_ABI_VERSION 9
+#define ODE_ABI_VERSION 10
 
 typedef struct ode_handle ode_handle;
 
@@ -190,7 +190,10 @@ typedef struct {
                                    OrdinaryDiffEqDifferentiation/src/derivative_utils.jl:46-170): 0 or 1, the
                                    reference's default for Rosenbrock23, evaluates J on every attempt.
                                    W = J - I/(dt gamma) and its LU are formed on every attempt either way */
-    int32_t reserved2;
+    int32_t isoutofdomain;      /* solve(...; isoutofdomain): 0 (default) none; 1 the common
+                                   (u, p, t) -> any(x -> x < 0, u): an adaptive step whose end state has a
+                                   negative component is rejected and retried with dt * qmin
+                                   (integrator_utils.jl:135-137, 612-623) */
     double jac_reuse_gamma_tol; /* reuse only while |dtgamma / dtgamma_J - 1| <= this (reference default
                                    0.03; < 0 means the default) */
     int32_t nsave_idxs;         /* > 0: the reference's save_idxs: only these states are saved, u_out holds */
@@ -205,8 +208,9 @@ typedef struct {
                                    every step runs to the next tstop (the reference's adaptive = false:
                                    no error estimate is judged, every step is accepted) */
     int32_t forward_only;       /* 1: the caller guarantees tf >= t0 for every trajectory, so the kernels'
-                                   forward-only forms (no integration direction in their step loops) may
-                                   run; a backward span then reports ODE_RC_INITIALFAILURE.  0 (default):
+                                   plain forms (no integration direction, force_dtmin or isoutofdomain in
+                                   their step loops) may run when neither of those two is set; a backward
+                                   span then reports ODE_RC_INITIALFAILURE.  0 (default):
                                    either direction.  The host entry points (ode_solve_ensemble, _dense,
                                    ode_submit) find it out themselves from the host spans */
     /* The PI step-size controller's knobs (solve(...; controller = PIController(beta1, beta2;

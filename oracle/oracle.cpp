@@ -329,6 +329,7 @@ struct Integ {
     double beta1, beta2, qmin, qmax, qmax_first, gamma, qsteady_min, qsteady_max, qoldinit;
     int order;
     int64_t iter, success_iter;
+    bool isout = false;   // the last attempt ended out of the domain (isoutofdomain)
     bool accept_step, next_step_tstop;
     double tstop_target;
     std::vector<double> u, uprev, tmp, utilde, atmp, fsalfirst, fsallast;
@@ -1538,9 +1539,14 @@ void loopfooter(Integ& I) {
     double ttmp = I.t + I.dt;
     if (I.o.adaptive) {
         double q = stepsize_controller(I);
+        // isoutofdomain (here the common any(x -> x < 0, u)) at the step's end, then
         // accept_step_controller, or force_dtmin at abs(dt) <= timedepentdtmin
-        // (integrator_utils.jl:613-623, utils.jl:93: abs(max(eps(t), dtmin)))
-        I.accept_step = I.EEst <= 1.0 || (I.o.force_dtmin && std::fabs(I.dt) <= std::fabs(jmax(jeps(I.t), I.o.dtmin)));
+        // (integrator_utils.jl:612-623, utils.jl:93: abs(max(eps(t), dtmin)))
+        I.isout = false;
+        if (I.o.isoutofdomain)
+            for (int i = 0; i < I.n; ++i) I.isout = I.isout || I.u[i] < 0.0;
+        I.accept_step = (!I.isout && I.EEst <= 1.0) ||
+                        (I.o.force_dtmin && std::fabs(I.dt) <= std::fabs(jmax(jeps(I.t), I.o.dtmin)));
         if (I.accept_step) {
             I.st.naccept++;
             I.tprev = I.t;
@@ -1658,7 +1664,9 @@ void loopheader(Integ& I) {
             I.reeval_fsal = false;
             modify_dt_for_tstops(I);
         } else {
-            I.dt = I.dt / jmin(1.0 / I.qmin, I.q11 / I.gamma);
+            // handle_step_rejection! (integrator_utils.jl:135-139)
+            if (I.isout) I.dt = I.dt * I.qmin;
+            else I.dt = I.dt / jmin(1.0 / I.qmin, I.q11 / I.gamma);
         }
     }
     I.iter++;
@@ -1748,6 +1756,7 @@ int solve_one(Integ& I, const double* u0) {
     I.iter = 0;
     I.success_iter = 0;
     I.accept_step = false;
+    I.isout = false;
     I.next_step_tstop = false;
     I.EEst = 1.0;
     I.q11 = 1.0;

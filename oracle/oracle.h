@@ -62,6 +62,7 @@ typedef struct {
     int32_t force_dtmin;       /* accept steps at max(eps(t), dtmin); no dt exits (check_error.jl:91) */
     const double* abstol_vec;  /* per-state tolerances (n entries), or NULL for the scalars */
     const double* reltol_vec;
+    int32_t isoutofdomain;     /* 1: reject adaptive steps ending with a negative state (any(x -> x < 0, u)) */
 } orc_opts;
 
 /* Solve one trajectory.  saveat: nsave_in times in (t0, tf] sorted ascending.

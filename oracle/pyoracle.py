@@ -40,7 +40,7 @@ class Opts(C.Structure):
         ("ctrl_given", C.c_int32), ("c_beta1", C.c_double), ("c_beta2", C.c_double), ("c_qoldinit", C.c_double),
         ("c_qmin", C.c_double), ("c_gamma", C.c_double), ("c_qsteady_min", C.c_double),
         ("c_qsteady_max", C.c_double), ("force_dtmin", C.c_int32), ("abstol_vec", C.POINTER(C.c_double)),
-        ("reltol_vec", C.POINTER(C.c_double)),
+        ("reltol_vec", C.POINTER(C.c_double)), ("isoutofdomain", C.c_int32),
     ]
 
 
@@ -99,7 +99,8 @@ def make_opts(reltol=1e-3, abstol=1e-6, dtmax=0.0, dtmin=0.0, dt=0.0, adaptive=T
               maxiters=1000000, save_start=False, save_end=True, save_end_user=-1,
               saveat_given=True, saveat_scalar=False, qmax_first_step=0.0, qmax=0.0, saveat_as_tstops=False,
               save_everystep=False, max_step_saves=0, callback=False, interp_points=10, max_events=0,
-              tstops=(), max_jac_age=1, jac_reuse_gamma_tol=0.03, controller=None, force_dtmin=False):
+              tstops=(), max_jac_age=1, jac_reuse_gamma_tol=0.03, controller=None, force_dtmin=False,
+              isoutofdomain=0):
     ts = np.ascontiguousarray(tstops, dtype=np.float64).ravel()
     # array tolerances: one per state (the scalars then stand unused)
     av = np.ascontiguousarray(abstol, dtype=np.float64).ravel() if np.ndim(abstol) else None
@@ -117,6 +118,7 @@ def make_opts(reltol=1e-3, abstol=1e-6, dtmax=0.0, dtmin=0.0, dt=0.0, adaptive=T
             v = controller.get(k)
             setattr(o, "c_" + k, float("nan") if v is None else float(v))
     o.force_dtmin = int(bool(force_dtmin))
+    o.isoutofdomain = int(isoutofdomain)
     if av is not None:
         o.abstol_vec = _dp(av)
     if rv is not None:

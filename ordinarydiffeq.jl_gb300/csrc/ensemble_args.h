@@ -13,8 +13,8 @@ struct OdeStatsDev {
 };
 
 // PI-controller values of EnsembleArgs::kd / kf: beta1, beta2, 1/qmin, gamma,
-// qsteady_min, qsteady_max, qoldinit, 1/qmax, 1/qmax_first_step.
-enum { KB1 = 0, KB2, KQMININV, KGAM, KQSMIN, KQSMAX, KQOLD, KIQMAX, KIQMAXF, KNCTRL };
+// qsteady_min, qsteady_max, qoldinit, 1/qmax, 1/qmax_first_step, qmin.
+enum { KB1 = 0, KB2, KQMININV, KGAM, KQSMIN, KQSMAX, KQOLD, KIQMAX, KIQMAXF, KQMIN, KNCTRL };
 
 // Everything one ensemble launch needs.  Device pointers; SoA layouts:
 //   u0[i*N + j], p[i*N + j], tspan[j] / tspan[N + j],
@@ -55,8 +55,10 @@ struct EnsembleArgs {
     double qmax_first_step, qmax;
     int ir_sweeps;          // mixed Rosenbrock: refinement sweeps per solve
     int adaptive;           // 0: fixed steps of dt, every step accepted
-    int forward_only;       // every span runs forward: the kernel's forward-only form may run
+    int forward_only;       // the kernel's plain form may run: every span runs forward, and neither
+                            // force_dtmin nor isoutofdomain is asked for
     int force_dtmin;        // accept steps at max(eps(t), dtmin) whatever their error
+    int isoutofdomain;      // 1: reject adaptive steps ending with a negative state
     // The PI controller of each method (slot 1: a composite's stiff method), its
     // defaults and the caller's knobs resolved on the host, in both precisions
     // (kernel parameters: read where used, held in no register)

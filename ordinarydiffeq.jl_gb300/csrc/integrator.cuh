@@ -331,9 +331,10 @@ __device__ double initdt(const R* u0, const PR<R>* p, double t, bool bwd, double
 // trajectory ends (the trajectories of a warp differ in step counts by up to
 // the ratio of their spans or stiffness).  Every trajectory's arithmetic is
 // the same whichever group and slot runs it.  Alg provides the cache, the
-// step, the interpolant and the FSAL hooks.  FWD: the caller guarantees
-// forward spans (tf >= t0) and the loop carries no direction at all; a
-// backward span then reports InitialFailure, as a NaN span does.
+// step, the interpolant and the FSAL hooks.  FWD, the plain form: the caller
+// guarantees forward spans (tf >= t0) and uses neither force_dtmin nor
+// isoutofdomain, and the loop carries none of them (a backward span then
+// reports InitialFailure, as a NaN span does).
 template <class Alg, class Model, class R, int L, int C, bool FWD, class Next>
 __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Next next) {
     using CT = typename Ctl<R>::T;
@@ -435,6 +436,7 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
     bool do_error_check = true;
     long long iter = 0, success_iter = 0;
     bool accept = false, next_tstop = false;
+    bool isout = false;   // the last attempt ended out of the domain (isoutofdomain)
     int rc = RC_DEFAULT;
 
     // _savevalues! (integrator_utils.jl:340-414) after an accepted step: saveat
@@ -782,6 +784,7 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
         success_iter = 0;
         accept = false;
         next_tstop = false;
+        isout = false;
         rc = (tf >= t0) ? RC_DEFAULT : RC_INITIALFAILURE;   // a NaN span is not stepped
         ev_last = false;
         terminated = false;
@@ -854,6 +857,10 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
                 // dtpropose the second call below overwrites; only the clip survives)
                 dt = pmin(dtpropose, dist);
                 Alg::template on_accept<R, C>(cache);
+            } else if (!FWD && isout) {
+                // handle_step_rejection! after an out-of-domain step: dt * qmin
+                if constexpr (is_composite_alg<Alg>::value) dt = dt * a.kd[cache.current][KQMIN];
+                else dt = dt * a.kd[0][KQMIN];
             } else {
                 // step_reject_controller!: dt /= min(1/qmin, q11/gamma)
                 const CT qmin_inv = KV(KQMININV);
@@ -903,10 +910,10 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
             else if (bits_nan(db)) e = RC_DTNAN;
             else if (iter > a.maxiters) e = RC_MAXITERS;
             // t + dt < tdir * first(tstops) in the reference's own time
-            else if (a.adaptive && !a.force_dtmin && ple(pabs(dt), pabs(a.dtmin)) &&
+            else if (a.adaptive && (FWD || !a.force_dtmin) && ple(pabs(dt), pabs(a.dtmin)) &&
                      (!accept || (bwd ? t + dt > tnext : t + dt < tnext)))
                 e = RC_DTLESSTHANMIN;
-            else if (a.adaptive && !a.force_dtmin && !accept && ple(pabs(dt), peps(t))) e = RC_UNSTABLE;
+            else if (a.adaptive && (FWD || !a.force_dtmin) && !accept && ple(pabs(dt), peps(t))) e = RC_UNSTABLE;
             else if (accept) {
                 bool bad = false;
 #pragma unroll
@@ -952,9 +959,18 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
             const CT x = q / KV(KGAM);
             q = x > KV(KQMININV) ? KV(KQMININV) : (x < inv_qmaxc ? inv_qmaxc : x);
         }
-        accept = !a.adaptive || EEst <= CT(1);
+        // isoutofdomain (the common any(x -> x < 0, u)) at the step's end, adaptive
+        // steps only (integrator_utils.jl:612-615)
+        isout = false;
+        if (!FWD && a.isoutofdomain && a.adaptive) {
+            bool neg = false;
+#pragma unroll
+            for (int c = 0; c < C; ++c) neg = neg || u[c] < R(0) || (u[c] == R(0) && ulo[c] < R(0));
+            isout = g.any(neg);
+        }
+        accept = !a.adaptive || (!isout && EEst <= CT(1));
         // force_dtmin: a step at the smallest dt is taken whatever its error
-        if (!accept && a.force_dtmin) accept = ple(pabs(dt), pabs(pmax(peps(t), a.dtmin)));
+        if (!FWD && !accept && a.force_dtmin) accept = ple(pabs(dt), pabs(pmax(peps(t), a.dtmin)));
         if (accept) {
             st.naccept++;
             tprev = t;

@@ -282,6 +282,8 @@ int check_problem(const ode_problem_desc* d, const ode_options* o, int64_t N, co
     if (o->ntstops < 0 || (o->ntstops > 0 && !o->tstops))
         return bad(ODE_E_INVALID, "ntstops < 0, or tstops is null");
     if (o->max_jac_age < 0) return bad(ODE_E_INVALID, "max_jac_age must be >= 0");
+    if (o->isoutofdomain < 0 || o->isoutofdomain > 1)
+        return bad(ODE_E_INVALID, "isoutofdomain must be 0 (none) or 1 (any state < 0)");
     if (o->nsave_idxs < 0 || (o->nsave_idxs > 0 && !o->save_idxs))
         return bad(ODE_E_INVALID, "nsave_idxs < 0, or save_idxs is null");
     if (o->controller_given) {
@@ -431,6 +433,7 @@ void resolve_controller(EnsembleArgs& a, int alg_id, const ode_options* o) {
             set(v[KQSMAX], o->qsteady_max);
         }
         v[KQMININV] = 1.0 / qmin;
+        v[KQMIN] = qmin;
         v[KGAM] = gamma;
         v[KIQMAX] = 1.0 / (o->qmax > 0 ? o->qmax : 10.0);
         v[KIQMAXF] = 1.0 / (o->qmax_first_step > 0 ? o->qmax_first_step : 10000.0);
@@ -465,10 +468,11 @@ EnsembleArgs make_args(ode_handle* h, const ode_problem_desc* d, const ode_optio
     a.max_jac_age = o->max_jac_age;
     a.jac_reuse_gamma_tol = o->jac_reuse_gamma_tol < 0 ? 0.03 : o->jac_reuse_gamma_tol;
     a.adaptive = o->adaptive ? 1 : 0;
-    a.forward_only = o->forward_only ? 1 : 0;
+    a.forward_only = (o->forward_only && !o->force_dtmin && !o->isoutofdomain) ? 1 : 0;
     a.abstol_vec = o->abstol_vec;
     a.reltol_vec = o->reltol_vec;
     a.force_dtmin = o->force_dtmin ? 1 : 0;
+    a.isoutofdomain = o->isoutofdomain;
     resolve_controller(a, d->alg_id, o);
     a.save_idxs = o->nsave_idxs > 0 ? o->save_idxs : nullptr;   // device memory at this point
     a.nsave_rows = o->nsave_idxs > 0 ? o->nsave_idxs : 0;
@@ -2072,10 +2076,11 @@ extern "C" int ode_solve_ensemble_noalloc(const ode_problem_desc* d, const ode_o
     a.max_jac_age = o->max_jac_age;
     a.jac_reuse_gamma_tol = o->jac_reuse_gamma_tol < 0 ? 0.03 : o->jac_reuse_gamma_tol;
     a.adaptive = o->adaptive ? 1 : 0;
-    a.forward_only = o->forward_only ? 1 : 0;
+    a.forward_only = (o->forward_only && !o->force_dtmin && !o->isoutofdomain) ? 1 : 0;
     a.abstol_vec = o->abstol_vec;
     a.reltol_vec = o->reltol_vec;
     a.force_dtmin = o->force_dtmin ? 1 : 0;
+    a.isoutofdomain = o->isoutofdomain;
     resolve_controller(a, d->alg_id, o);
     a.save_idxs = o->nsave_idxs > 0 ? o->save_idxs : nullptr;   // device memory at this point
     a.nsave_rows = o->nsave_idxs > 0 ? o->nsave_idxs : 0;

@@ -101,7 +101,7 @@ mutable struct Options
     saveat_per_traj::Int32; qmax_first_step::Float64; qmax::Float64; lanes_per_traj::Int32
     scheduler::Int32; block_size::Int32; ir_sweeps::Int32; save_everystep::Int32; max_step_saves::Int32
     callback::Int32; interp_points::Int32; max_events::Int32; ntstops::Int32; tstops::Ptr{Float64}
-    max_jac_age::Int32; reserved2::Int32; jac_reuse_gamma_tol::Float64
+    max_jac_age::Int32; isoutofdomain::Int32; jac_reuse_gamma_tol::Float64
     nsave_idxs::Int32; reserved3::Int32; save_idxs::Ptr{Int32}
     adaptive::Int32; forward_only::Int32
     controller_given::Int32; force_dtmin::Int32
@@ -201,7 +201,7 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem,
                            dt = 0.0, dtmax = 0.0, dtmin = 0.0, maxiters = 1_000_000, save_start = nothing,
                            save_end = nothing, save_everystep = isempty(saveat), max_step_saves = 1024, seed = 0,
                            save_idxs = nothing, adaptive = true, controller = nothing, force_dtmin = false,
-                           callback = nothing,
+                           isoutofdomain = nothing, callback = nothing,
                            dense = save_everystep && isempty(saveat) && save_idxs === nothing,
                            tstops = Float64[], kwargs...)
     t0 = time()
@@ -240,6 +240,10 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem,
     rows = save_idxs === nothing ? n : length(sidx)
     # a dt of either sign is taken in the direction of the span (handle_dt!, solve.jl:968-985)
     cg, ck, cqmax, cqmaxfirst = controller_knobs(controller)
+    # isoutofdomain: the library runs the common (u, p, t) -> any(x -> x < 0, u), asked for by :negative
+    isoutofdomain === nothing || isoutofdomain === :negative ||
+        error("EnsembleGB300 runs isoutofdomain = :negative (any state < 0) only")
+    iood = isoutofdomain === :negative ? Int32(1) : Int32(0)
     # array tolerances: one per state (the scalar fields then hold their smallest entries)
     atv = abstol isa AbstractVector ? collect(Float64, abstol) : Float64[]
     rtv = reltol isa AbstractVector ? collect(Float64, reltol) : Float64[]
@@ -248,7 +252,7 @@ function SciMLBase.__solve(eprob::SciMLBase.AbstractEnsembleProblem,
     o = Options(rtol_s, atol_s, dtmax, dtmin, abs(dt), maxiters, ss, se, save_end === nothing ? -1 : Int32(save_end),
                 scalar, length(sv), 0, cqmaxfirst, cqmax, ens.lanes_per_traj, ens.scheduler, 0, -1, everystep,
                 everystep ? max_step_saves : 0, cb, cb ? callback.interp_points : 10, cb ? callback.max_events : 0,
-                length(tst), isempty(tst) ? Ptr{Float64}(C_NULL) : pointer(tst), jac_reuse(alg)[1], Int32(0),
+                length(tst), isempty(tst) ? Ptr{Float64}(C_NULL) : pointer(tst), jac_reuse(alg)[1], iood,
                 jac_reuse(alg)[2], length(sidx), Int32(0), isempty(sidx) ? Ptr{Int32}(C_NULL) : pointer(sidx),
                 Int32(adaptive), Int32(0), cg, Int32(force_dtmin), ck...,
                 isempty(atv) ? Ptr{Float64}(C_NULL) : pointer(atv), isempty(rtv) ? Ptr{Float64}(C_NULL) : pointer(rtv))

@@ -40,7 +40,7 @@ class Options(C.Structure):
                 ("save_everystep", C.c_int32), ("max_step_saves", C.c_int32),
                 ("callback", C.c_int32), ("interp_points", C.c_int32), ("max_events", C.c_int32),
                 ("ntstops", C.c_int32), ("tstops", C.POINTER(C.c_double)),
-                ("max_jac_age", C.c_int32), ("reserved2", C.c_int32), ("jac_reuse_gamma_tol", C.c_double),
+                ("max_jac_age", C.c_int32), ("isoutofdomain", C.c_int32), ("jac_reuse_gamma_tol", C.c_double),
                 ("nsave_idxs", C.c_int32), ("reserved3", C.c_int32), ("save_idxs", C.POINTER(C.c_int32)),
                 ("adaptive", C.c_int32), ("forward_only", C.c_int32),
                 ("controller_given", C.c_int32), ("force_dtmin", C.c_int32), ("beta1", C.c_double),

@@ -325,7 +325,8 @@ def get_handle(device=0):
 
 
 def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax, callback=None,
-             tstops=None, alg=None, save_idxs=None, adaptive=True, controller=None, force_dtmin=False):
+             tstops=None, alg=None, save_idxs=None, adaptive=True, controller=None, force_dtmin=False,
+             isoutofdomain=None):
     o = _lib.Options()
     L = _lib.load()
     L.ode_options_default(C.byref(o))
@@ -382,6 +383,10 @@ def _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_ste
         o._tstops = ts   # the options hold the array while the call reads it
     o.adaptive = int(bool(adaptive))
     o.force_dtmin = int(bool(force_dtmin))
+    # isoutofdomain: the common any(x -> x < 0, u) ("negative" or True), else none
+    if isoutofdomain not in (None, False, True, "negative"):
+        raise ValueError('isoutofdomain: "negative" (any state < 0) or None')
+    o.isoutofdomain = 1 if isoutofdomain in (True, "negative") else 0
     if save_idxs is not None:
         ix = np.ascontiguousarray(np.atleast_1d(save_idxs), dtype=np.int32).ravel()
         o.nsave_idxs = ix.size
@@ -441,7 +446,7 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
                  dtmax=None, dtmin=None, maxiters=1000000, save_start=None, save_end=None, n_per_traj=None,
                  qmax_first_step=None, qmax=None, return_times=False, save_everystep=False, max_step_saves=1024,
                  dense=False, callback=None, tstops=None, save_idxs=None, adaptive=True, controller=None,
-                 force_dtmin=False):
+                 force_dtmin=False, isoutofdomain=None):
     """Solve a packed ensemble.  u0s (n, N), ps (np, N), tspans (2, N).  Returns the
     raw structure-of-arrays outputs dict (t, u, nsaved, retcode, stats).
     save_everystep keeps every accepted step, up to max_step_saves per
@@ -455,7 +460,9 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
     reference's save_idxs): u is then (cap, len(save_idxs), N).  adaptive=False:
     fixed steps of dt (the reference's adaptive = false).  controller: a
     PIController with the step-size controller's knobs.  force_dtmin: steps at
-    the smallest dt are taken whatever their error (no DtLessThanMin exit)."""
+    the smallest dt are taken whatever their error (no DtLessThanMin exit).
+    isoutofdomain="negative": adaptive steps ending with a negative state are
+    rejected (the reference's isoutofdomain = (u, p, t) -> any(x -> x < 0, u))."""
     L = _lib.load()
     if isinstance(model, str):
         model = MODELS[model]
@@ -465,7 +472,7 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
     n, N = u0s.shape
     sv = resolve_saveat(saveat, tspans, save_start, save_end, save_everystep, max_step_saves)
     o = _options(reltol, abstol, dt, dtmax, dtmin, maxiters, sv, ens, qmax_first_step, qmax, callback, tstops, alg,
-                 save_idxs, adaptive, controller, force_dtmin)
+                 save_idxs, adaptive, controller, force_dtmin, isoutofdomain)
     d = _lib.ProblemDesc(model, alg.alg_id, n, ps.shape[0], ens.prec_id(), 0)
     rows = n if save_idxs is None else int(np.size(save_idxs))
     cap = sv.cap + (2 * callback.max_events if callback is not None else 0)
@@ -573,7 +580,8 @@ def autotune(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=
 def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, saveat=None, reltol=1e-3,
           abstol=1e-6, dt=None, dtmax=None, dtmin=None, maxiters=1000000, save_start=None, save_end=None,
           seed=0, qmax_first_step=None, qmax=None, save_everystep=None, max_step_saves=1024, dense=None,
-          callback=None, tstops=None, save_idxs=None, adaptive=True, controller=None, force_dtmin=False):
+          callback=None, tstops=None, save_idxs=None, adaptive=True, controller=None, force_dtmin=False,
+          isoutofdomain=None):
     """solve(EnsembleProblem, alg, EnsembleGB300(); trajectories, saveat, reltol, abstol, ...).
     As in the reference (solve.jl:138-146), save_everystep defaults to "no
     saveat given" (every accepted step is kept, up to max_step_saves per
@@ -605,7 +613,7 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
                            save_everystep=save_everystep, max_step_saves=max_step_saves,
                            dense=dense and not (dense_default and eprob.n_per_traj is not None), callback=callback,
                            tstops=tstops, save_idxs=save_idxs, adaptive=adaptive, controller=controller,
-                           force_dtmin=force_dtmin)
+                           force_dtmin=force_dtmin, isoutofdomain=isoutofdomain)
         sols = _LazySolutions(res, alg, eprob.n_per_traj)
         return EnsembleSolution(sols, time.perf_counter() - t_start, True, res)
     if trajectories is None:
@@ -621,7 +629,8 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
         ids = list(range(done, min(trajectories, done + batch_size)))
         outs = _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, dtmin, maxiters,
                             save_start, save_end, output_func, qmax_first_step, qmax, save_everystep, max_step_saves,
-                            dense, dense_default, callback, tstops, save_idxs, adaptive, controller, force_dtmin)
+                            dense, dense_default, callback, tstops, save_idxs, adaptive, controller, force_dtmin,
+                            isoutofdomain)
         u, converged = reduction(u, outs, range(ids[0] + 1, ids[-1] + 2))
         done = ids[-1] + 1
         if converged:
@@ -632,7 +641,7 @@ def solve(eprob, alg, ensemblealg=None, trajectories=None, batch_size=None, save
 def _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, dtmin, maxiters, save_start,
                  save_end, output_func, qmax_first_step, qmax, save_everystep=False, max_step_saves=1024,
                  dense=False, dense_default=True, callback=None, tstops=None, save_idxs=None, adaptive=True,
-                 controller=None, force_dtmin=False):
+                 controller=None, force_dtmin=False, isoutofdomain=None):
     repeat = {i: 1 for i in ids}
     results = {}
     todo = list(ids)
@@ -661,7 +670,7 @@ def _solve_batch(eprob, alg, ens, ids, root, saveat, reltol, abstol, dt, dtmax, 
                            save_everystep=save_everystep, max_step_saves=max_step_saves,
                            dense=dense and not (dense_default and npt is not None), callback=callback,
                            tstops=tstops, save_idxs=save_idxs, adaptive=adaptive, controller=controller,
-                           force_dtmin=force_dtmin)
+                           force_dtmin=force_dtmin, isoutofdomain=isoutofdomain)
         sols = _LazySolutions(res, alg, npt)
         again = []
         for k, i in enumerate(todo):

@@ -69,7 +69,7 @@ def test_julia_binding_mirrors_the_c_structs():
 
 def test_abi_version_and_defaults_without_gpu():
     L = _lib.load()
-    assert L.ode_abi_version() == 9
+    assert L.ode_abi_version() == 10
     # dense vectors per step (Tsit5 k1..k7, Vern7 k1 and k4..k9, Rodas5P dense k1..k3)
     assert [L.ode_dense_nk(a) for a in (0, 1, 2)] == [7, 7, 3] and L.ode_dense_nk(9) == -1
     o = _lib.Options()

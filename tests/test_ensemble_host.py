@@ -23,7 +23,8 @@ def exact_linear(monkeypatch):
     def fake(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abstol=1e-6, dt=None, dtmax=None,
              dtmin=None, maxiters=1000000, save_start=None, save_end=None, n_per_traj=None, qmax_first_step=None,
              qmax=None, return_times=False, save_everystep=False, max_step_saves=1024, dense=False, callback=None,
-             tstops=None, save_idxs=None, adaptive=True, controller=None, force_dtmin=False):
+             tstops=None, save_idxs=None, adaptive=True, controller=None, force_dtmin=False,
+             isoutofdomain=None):
         u0s, ps, tspans = np.asarray(u0s, float), np.asarray(ps, float), np.asarray(tspans, float)
         n, N = u0s.shape
         sv = resolve_saveat(saveat, tspans, save_start, save_end, save_everystep, max_step_saves)

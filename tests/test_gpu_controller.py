@@ -70,3 +70,26 @@ def test_force_dtmin_matches_oracle(alg):
     assert (g["retcode"] == 1).all()
     c = compare(g, o, 1e-9, 1e-9, step_slack=0)
     assert c["ok"] and c["steps_ok"], c
+
+
+@pytest.mark.parametrize("alg,precision", [("vern7", "fp64"), ("tsit5", "fp64"), ("rodas5p", "fp64"),
+                                           ("vern7", "mixed")])
+def test_isoutofdomain_negative_matches_oracle(alg, precision):
+    # u' = p u with p ~ -U(20, 80) at loose tolerance overshoots below zero; with
+    # isoutofdomain = "negative" such steps are rejected and retried at dt * qmin
+    N = 256
+    rng = np.random.default_rng(53)
+    u0 = rng.uniform(0.5, 2.0, (1, N))
+    p = -rng.uniform(20.0, 80.0, (1, N))
+    ts = np.tile([[0.0], [2.0]], (1, N))
+    kw = dict(save_everystep=True, max_step_saves=2048)
+    g = gpu("linear", alg, u0, p, ts, None, 1e-2, 1e-2, precision=precision, isoutofdomain="negative", **kw)
+    o = oracle("linear", alg, u0, p, ts, None, 1e-2, 1e-2, isoutofdomain=1, **kw)
+    assert (g["retcode"] == 1).all()
+    k = int(g["nsaved"].max())
+    m = np.arange(k)[:, None] < g["nsaved"][None, :]
+    assert g["u"][:k, 0][m].min() >= 0.0
+    if precision == "fp64":
+        c = compare(g, o, 1e-2, 1e-2, step_slack=0)
+        assert c["ok"] and c["steps_ok"], c
+        assert np.array_equal(g["stats"]["nreject"], o["stats"]["nreject"])

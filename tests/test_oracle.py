@@ -410,6 +410,23 @@ def test_force_dtmin():
     assert np.abs(b["u"] - ref["u"]).max() < 1e-6
 
 
+def test_isoutofdomain_negative():
+    # isoutofdomain = (u, p, t) -> any(x -> x < 0, u) (integrator_utils.jl:135-137,
+    # 612-615): Vern7 at reltol = abstol = 1e-2 on u' = -50 u dips below zero; with
+    # the check no saved state is negative, and the rejected steps are counted
+    kw = dict(saveat=[], saveat_given=False, save_everystep=True, max_step_saves=4096, save_start=True,
+              reltol=1e-2, abstol=1e-2)
+    a = O.solve(O.VERN7, O.LINEAR, [1.0], [-50.0], (0.0, 2.0), **kw)
+    assert a["u"].min() < 0.0
+    b = O.solve(O.VERN7, O.LINEAR, [1.0], [-50.0], (0.0, 2.0), isoutofdomain=1, **kw)
+    assert b["retcode"] == O.RC_SUCCESS and b["u"].min() >= 0.0
+    assert b["stats"]["nreject"] > a["stats"]["nreject"]
+    # a solution that stays positive is untouched
+    c = O.solve(O.TSIT5, O.LINEAR, [1.0], [-1.0], (0.0, 2.0), isoutofdomain=1, **kw)
+    d = O.solve(O.TSIT5, O.LINEAR, [1.0], [-1.0], (0.0, 2.0), **kw)
+    assert np.array_equal(c["u"], d["u"])
+
+
 def test_tstops_from_a_range_are_a_subset_of_sol_t():
     # ode_tstops_tests.jl:97-105 ("Late binding tstops"): 0:0.1:1 is a subset of sol.t
     ts = np.arange(0, 11) * 0.1
