@@ -97,3 +97,17 @@ def test_device_arrays_and_host_checks():
     assert np.array_equal(outs[1].cpu().numpy()[:k], host["u"][:k])
     with pytest.raises(_lib.OdeError):
         gpu("robertson", "rodas5p", u0, p, ts, ROBER_SAVEAT, 1e-6, np.array([1e-8, -1.0, 1e-6]))
+
+
+def test_uneven_chains_with_array_tolerances():
+    # the one-launch class kernel: each chain takes the first n entries of the arrays
+    from gpu_common import duffing_inputs
+    N = 4096
+    u0, p, ts, sv, npt = duffing_inputs(N, [2, 4, 8], tf_range=(1.0, 3.0), seed=64)
+    nmax = u0.shape[0]
+    at = np.where(np.arange(nmax) % 2 == 0, 1e-9, 1e-7)   # positions tighter than velocities
+    rt = np.full(nmax, 1e-8)
+    g = gpu("duffing_chain", "vern7", u0, p, ts, sv, rt, at, n_per_traj=npt)
+    o = oracle("duffing_chain", "vern7", u0, p, ts, sv, rt, at, n_per_traj=npt)
+    c = compare(g, o, 1e-8, 1e-8)
+    assert c["ok"] and c["steps_ok"], c

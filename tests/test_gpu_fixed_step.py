@@ -127,3 +127,23 @@ def test_fixed_step_events_match_oracle():
     mu = ~np.isnan(ou)
     assert np.all(np.abs(gu[mu] - ou[mu]) <= 1e-9 * np.abs(ou[mu]) + 1e-9)
     assert (g["nsaved"] > 15 * 4 + 1).all()   # every ball bounced at least once
+
+
+@pytest.mark.parametrize("alg", ["tsit5", "rodas5p"])
+def test_fixed_steps_with_dense_output(alg):
+    # the dense vectors of each fixed step: sol(t) between the steps matches the oracle's
+    from gpu_common import ALG, MODEL
+    import pyoracle as O
+    from odegb300 import dense_eval
+    N = 16
+    u0, p, ts = lorenz_inputs(N, seed=14)
+    g = gpu("lorenz", alg, u0, p, ts, None, 1e-6, 1e-6, adaptive=False, dt=1e-2, save_everystep=True,
+            max_step_saves=256, dense=True)
+    tq = np.linspace(0.0, 1.0, 37)[:, None] * np.ones((1, N))
+    ev = dense_eval(g, tq)
+    for j in range(N):
+        o = O.solve(ALG[alg][1], MODEL["lorenz"], u0[:, j], p[:, j], ts[:, j], dense=True, adaptive=False, dt=1e-2,
+                    reltol=1e-6, abstol=1e-6, saveat_given=False, save_everystep=True, max_step_saves=256,
+                    save_start=True, save_end=True)
+        ref = o["dense"](tq[:, j])
+        assert np.all(np.abs(ev[:, :, j] - ref) <= 1e-10 * (np.abs(ref) + 1.0)), j
