@@ -903,6 +903,30 @@ void tsit5_interp_d1(double th, const double* K, int n, double* out) {
     }
 }
 
+// Tsit5's second derivative (interpolants.jl: tsit5pre2, Val{2}): sum_i k_i b_i''(th) / dt,
+// b_i'' = evalpoly(th, 2 r_i2, 6 r_i3, 12 r_i4).
+void tsit5_interp_d2(double th, double dt, const double* K, int n, double* out) {
+    double b[8];
+    for (int s = 1; s <= 7; ++s)
+        b[s] = std::fma(th, std::fma(th, 12.0 * TSIT5_R[s][4], 6.0 * TSIT5_R[s][3]), 2.0 * TSIT5_R[s][2]);
+    const double invdt = 1.0 / dt;
+    for (int i = 0; i < n; ++i) {
+        double acc = K[6 * n + i] * b[7];
+        for (int s = 6; s >= 1; --s) acc = std::fma(K[(s - 1) * n + i], b[s], acc);
+        out[i] = acc * invdt;
+    }
+}
+
+// Rodas5P's second derivative (rosenbrock_interpolants.jl:544-560, interp_order 3):
+// (-2 k1 + 2 k2 + th (-6 k2 + 6 k3 - 12 th k3)) / dt^2
+void rodas_interp_d2(double th, double dt, const double* K, int n, double* out) {
+    for (int i = 0; i < n; ++i) {
+        const double k1 = K[i], k2 = K[n + i], k3 = K[2 * n + i];
+        const double in2 = std::fma(-6.0, k2, std::fma(6.0, k3, -12.0 * th * k3));
+        out[i] = std::fma(th, in2, std::fma(-2.0, k1, 2.0 * k2)) / (dt * dt);
+    }
+}
+
 // Vern7 (lib/OrdinaryDiffEqVerner/src/interpolants.jl:305-334), the extra stages formed.
 void vern7_interp_d1(double th, const double* K, int n, double* out) {
     static const int idx[13] = {1, 4, 5, 6, 7, 8, 9, 11, 12, 13, 14, 15, 16};
@@ -1949,8 +1973,9 @@ int orc_dense_eval_deriv(void* h, const double* tq, int nq, int deriv, double* o
 int orc_dense_eval(void* h, const double* tq, int nq, double* out) { return orc_dense_eval_deriv(h, tq, nq, 0, out); }
 
 int orc_dense_eval_deriv(void* h, const double* tq, int nq, int deriv, double* out) {
-    if (deriv < 0 || deriv > 1) return -2;
     Dense* D = (Dense*)h;
+    // Val{2}: the forms the reference has (Tsit5, Rodas5P)
+    if (deriv < 0 || deriv > 2 || (deriv == 2 && D->alg != ORC_TSIT5 && D->alg != ORC_RODAS5P)) return -2;
     const int n = D->n;
     if (D->steps.empty()) return -1;
     const size_t ns = D->steps.size() + 1;
@@ -1969,7 +1994,8 @@ int orc_dense_eval_deriv(void* h, const double* tq, int nq, int deriv, double* o
         double* o = out + (size_t)q * n;
         switch (D->alg) {
         case ORC_TSIT5:
-            if (deriv) tsit5_interp_d1(th, S.k.data(), n, o);
+            if (deriv == 2) tsit5_interp_d2(th, dt, S.k.data(), n, o);
+            else if (deriv) tsit5_interp_d1(th, S.k.data(), n, o);
             else tsit5_interp(th, dt, S.y0.data(), S.k.data(), n, o);
             break;
         case ORC_VERN7:
@@ -1980,7 +2006,8 @@ int orc_dense_eval_deriv(void* h, const double* tq, int nq, int deriv, double* o
             else vern7_interp(th, dt, S.y0.data(), K.data(), n, o);
             break;
         case ORC_RODAS5P:
-            if (deriv) rodas_interp_d1(th, dt, S.y0.data(), S.y1.data(), S.k.data(), n, o);
+            if (deriv == 2) rodas_interp_d2(th, dt, S.k.data(), n, o);
+            else if (deriv) rodas_interp_d1(th, dt, S.y0.data(), S.y1.data(), S.k.data(), n, o);
             else rodas_interp(th, S.y0.data(), S.y1.data(), S.k.data(), n, o);
             break;
         case ORC_ROSENBROCK23:

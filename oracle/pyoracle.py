@@ -175,7 +175,9 @@ class DenseSolution:
     def __call__(self, ts, deriv=0):
         ts = np.ascontiguousarray(np.atleast_1d(ts), dtype=np.float64)
         out = np.zeros((ts.size, self.n))
-        lib().orc_dense_eval_deriv(self.h, _dp(ts), ts.size, int(deriv), _dp(out))
+        rc = lib().orc_dense_eval_deriv(self.h, _dp(ts), ts.size, int(deriv), _dp(out))
+        if rc != 0:
+            raise ValueError("dense evaluation failed (%d): derivative order %d" % (rc, deriv))
         return out
 
     @property

@@ -257,6 +257,24 @@ __device__ __forceinline__ void tsit5_derivative(const double (*k)[C], double th
     }
 }
 
+// Tsit5's second derivative (interpolants.jl: tsit5pre2, the Val{2} form):
+// (sum_i k_i b_i''(th)) / dt with b_i'' = evalpoly(th, 2 r_i2, 6 r_i3, 12 r_i4).
+template <int C>
+__device__ __forceinline__ void tsit5_second_derivative(const double (*k)[C], double th, double dt, double* out) {
+    double b[8];
+#pragma unroll
+    for (int i = 1; i <= 7; ++i)
+        b[i] = fma(th, fma(th, 12.0 * tab::TSIT5_R(i, 4), 6.0 * tab::TSIT5_R(i, 3)), 2.0 * tab::TSIT5_R(i, 2));
+    const double invdt = 1.0 / dt;
+#pragma unroll
+    for (int i = 0; i < C; ++i) {
+        double acc = k[6][i] * b[7];
+#pragma unroll
+        for (int s = 6; s >= 1; --s) acc = fma(k[s - 1][i], b[s], acc);
+        out[i] = acc * invdt;
+    }
+}
+
 struct Vern7Alg {
     static constexpr int ORDER = 7;
     static constexpr bool IMPLICIT = false;

@@ -75,14 +75,21 @@ __global__ void dense_eval_pointwise(DenseArgs a) {
             Tsit5Alg::Cache<double, 1> c;
 #pragma unroll
             for (int q = 0; q < NK; ++q) c.k[q][0] = kp[(size_t)q * n * N];
-            if (a.deriv) tsit5_derivative<1>(c.k, v.th, &o);
+            if (a.deriv == 2) tsit5_second_derivative<1>(c.k, v.th, v.dt, &o);
+            else if (a.deriv) tsit5_derivative<1>(c.k, v.th, &o);
             else Tsit5Alg::interpolate<Linear, double, 1, 1>(c, &o, &olo, v.th, v.dt, v.tprev, &y0, &z, &y1, &z,
                                                              nullptr, g);
         } else if constexpr (ALG == 2) {
             Rodas5PAlg::Cache<double, 1> c;
 #pragma unroll
             for (int q = 0; q < NK; ++q) c.dk[q][0] = kp[(size_t)q * n * N];
-            if (a.deriv) {
+            if (a.deriv == 2) {
+                // the Val{2} form (rosenbrock_interpolants.jl:544-560, interp_order 3):
+                // (-2 k1 + 2 k2 + th (-6 k2 + 6 k3 - 12 th k3)) / dt^2
+                const double k1 = c.dk[0][0], k2 = c.dk[1][0], k3 = c.dk[2][0], th = v.th;
+                const double in2 = fma(-6.0, k2, fma(6.0, k3, -12.0 * th * k3));
+                o = fma(th, in2, fma(-2.0, k1, 2.0 * k2)) / (v.dt * v.dt);
+            } else if (a.deriv) {
                 // rosenbrock_interpolants.jl:444-470 (interp_order 3):
                 // (k1 + th (-2 k1 + 2 k2 + th (-3 k2 + 3 k3 - 4 th k3)) - y0 + y1) / dt
                 const double k1 = c.dk[0][0], k2 = c.dk[1][0], k3 = c.dk[2][0], th = v.th;

@@ -152,7 +152,7 @@ const RETCODES = (SciMLBase.ReturnCode.Default, SciMLBase.ReturnCode.Success, Sc
 """
 Interpolation of a dense GB300 solve (the reference's dense = true): sol(t)
 evaluates the method's interpolant on the saved steps on the device
-(ode_dense_eval_deriv; sol(t, Val{1}) too), as ode_interpolation does on the host.  Holds one
+(ode_dense_eval_deriv; sol(t, Val{1}) and, for Tsit5 and Rodas5P, sol(t, Val{2}) too), as ode_interpolation does on the host.  Holds one
 trajectory's saves t (ns), u (n x ns) and interpolation vectors k (n x nk x ns).
 """
 struct GB300DenseInterpolation <: SciMLBase.AbstractDiffEqInterpolation
@@ -166,8 +166,8 @@ struct GB300DenseInterpolation <: SciMLBase.AbstractDiffEqInterpolation
 end
 
 function (id::GB300DenseInterpolation)(tvals, idxs, deriv, p, continuity::Symbol = :left)
-    order = deriv == Val{0} ? 0 : deriv == Val{1} ? 1 :
-            error("GB300 dense output evaluates the solution (Val{0}) and its first derivative (Val{1})")
+    order = deriv == Val{0} ? 0 : deriv == Val{1} ? 1 : deriv == Val{2} ? 2 :
+            error("GB300 dense output evaluates the solution (Val{0}) and its derivatives Val{1}, Val{2}")
     tq = tvals isa Number ? [Float64(tvals)] : collect(Float64, tvals)
     n, ns, nq = size(id.u, 1), length(id.t), length(tq)
     d = ProblemDesc(id.model, id.alg, n, length(id.p), 0, 0)

@@ -427,6 +427,25 @@ def test_isoutofdomain_negative():
     assert np.array_equal(c["u"], d["u"])
 
 
+@pytest.mark.parametrize("alg", [O.TSIT5, O.RODAS5P])
+def test_dense_second_derivative(alg):
+    # sol(t, Val{2}) (Tsit5 tsit5pre2, Rodas5P rosenbrock_interpolants.jl:544-560): the
+    # derivative of the Val{1} interpolant, checked by central differences inside each
+    # step, and close to f'(u) = J f for the linear problem u' = p u (u'' = p^2 u)
+    r = O.solve(alg, O.LINEAR, [1.0], [-2.0], (0.0, 1.0), dense=True, reltol=1e-10, abstol=1e-10,
+                saveat_given=False, save_start=True, save_end=True)
+    sol = r["dense"]
+    t = r["t"]
+    mids = 0.5 * (t[:-1] + t[1:])
+    h = 1e-6 * np.diff(t).min()
+    fd = (sol(mids + h, deriv=1) - sol(mids - h, deriv=1)) / (2 * h)
+    d2 = sol(mids, deriv=2)
+    assert np.allclose(d2, fd, rtol=1e-4, atol=1e-6)
+    assert np.allclose(d2[:, 0], 4.0 * np.exp(-2.0 * mids), rtol=1e-3)
+    with pytest.raises(Exception):
+        O.solve(O.VERN7, O.LINEAR, [1.0], [-2.0], (0.0, 1.0), dense=True, saveat_given=False)["dense"](0.5, deriv=2)
+
+
 def test_tstops_from_a_range_are_a_subset_of_sol_t():
     # ode_tstops_tests.jl:97-105 ("Late binding tstops"): 0:0.1:1 is a subset of sol.t
     ts = np.arange(0, 11) * 0.1
