@@ -330,10 +330,11 @@ int ode_dense_eval(ode_handle* h, const ode_problem_desc* d, int64_t ntraj, cons
 /* The same with the derivative order: deriv 0 is sol(t) (ode_dense_eval), 1 is
  * sol(t, Val{1}), the time derivative of the method's interpolant on the same
  * interval (Tsit5 interpolants.jl:143-178, Vern7 :305-334, Rodas5P
- * rosenbrock_interpolants.jl:444-470, Rosenbrock23 :111-127), 2 is sol(t, Val{2})
- * for the methods whose interpolant has that form in the reference (Tsit5:
- * interpolants.jl tsit5pre2; Rodas5P: rosenbrock_interpolants.jl:544-560).
- * Other orders and methods: ODE_E_UNSUPPORTED. */
+ * rosenbrock_interpolants.jl:444-470, Rosenbrock23 :111-127), 2 and 3 are
+ * sol(t, Val{2}) and sol(t, Val{3}) for the methods whose interpolant has those
+ * forms in the reference (Tsit5: interpolants.jl tsit5pre2, tsit5pre3; Rodas5P:
+ * rosenbrock_interpolants.jl:544-560, 644-653).  Other orders and methods:
+ * ODE_E_UNSUPPORTED. */
 int ode_dense_eval_deriv(ode_handle* h, const ode_problem_desc* d, int64_t ntraj, const double* p,
                          const double* t_saved, const double* u_saved, const double* k_saved, const int32_t* nsaved,
                          int32_t cap, int32_t nq, const double* tq, int32_t tq_per_traj, int32_t deriv, double* out);

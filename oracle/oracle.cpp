@@ -917,6 +917,28 @@ void tsit5_interp_d2(double th, double dt, const double* K, int n, double* out) 
     }
 }
 
+// Tsit5's third derivative (tsit5pre3, Val{3}): sum_i k_i b_i'''(th) inv(dt)^2,
+// b_i''' = evalpoly(th, 6 r_i3, 24 r_i4).
+void tsit5_interp_d3(double th, double dt, const double* K, int n, double* out) {
+    double b[8];
+    for (int s = 1; s <= 7; ++s) b[s] = std::fma(th, 24.0 * TSIT5_R[s][4], 6.0 * TSIT5_R[s][3]);
+    const double invdt = 1.0 / dt, invdt2 = invdt * invdt;
+    for (int i = 0; i < n; ++i) {
+        double acc = K[6 * n + i] * b[7];
+        for (int s = 6; s >= 1; --s) acc = std::fma(K[(s - 1) * n + i], b[s], acc);
+        out[i] = acc * invdt2;
+    }
+}
+
+// Rodas5P's third derivative (rosenbrock_interpolants.jl:644-653, interp_order 3):
+// (-6 k2 + 6 k3 - 24 th k3) / dt^3
+void rodas_interp_d3(double th, double dt, const double* K, int n, double* out) {
+    for (int i = 0; i < n; ++i) {
+        const double k2 = K[n + i], k3 = K[2 * n + i];
+        out[i] = std::fma(-6.0, k2, std::fma(6.0, k3, -24.0 * th * k3)) / (dt * dt * dt);
+    }
+}
+
 // Rodas5P's second derivative (rosenbrock_interpolants.jl:544-560, interp_order 3):
 // (-2 k1 + 2 k2 + th (-6 k2 + 6 k3 - 12 th k3)) / dt^2
 void rodas_interp_d2(double th, double dt, const double* K, int n, double* out) {
@@ -1975,7 +1997,7 @@ int orc_dense_eval(void* h, const double* tq, int nq, double* out) { return orc_
 int orc_dense_eval_deriv(void* h, const double* tq, int nq, int deriv, double* out) {
     Dense* D = (Dense*)h;
     // Val{2}: the forms the reference has (Tsit5, Rodas5P)
-    if (deriv < 0 || deriv > 2 || (deriv == 2 && D->alg != ORC_TSIT5 && D->alg != ORC_RODAS5P)) return -2;
+    if (deriv < 0 || deriv > 3 || (deriv >= 2 && D->alg != ORC_TSIT5 && D->alg != ORC_RODAS5P)) return -2;
     const int n = D->n;
     if (D->steps.empty()) return -1;
     const size_t ns = D->steps.size() + 1;
@@ -1994,7 +2016,8 @@ int orc_dense_eval_deriv(void* h, const double* tq, int nq, int deriv, double* o
         double* o = out + (size_t)q * n;
         switch (D->alg) {
         case ORC_TSIT5:
-            if (deriv == 2) tsit5_interp_d2(th, dt, S.k.data(), n, o);
+            if (deriv == 3) tsit5_interp_d3(th, dt, S.k.data(), n, o);
+            else if (deriv == 2) tsit5_interp_d2(th, dt, S.k.data(), n, o);
             else if (deriv) tsit5_interp_d1(th, S.k.data(), n, o);
             else tsit5_interp(th, dt, S.y0.data(), S.k.data(), n, o);
             break;
@@ -2006,7 +2029,8 @@ int orc_dense_eval_deriv(void* h, const double* tq, int nq, int deriv, double* o
             else vern7_interp(th, dt, S.y0.data(), K.data(), n, o);
             break;
         case ORC_RODAS5P:
-            if (deriv == 2) rodas_interp_d2(th, dt, S.k.data(), n, o);
+            if (deriv == 3) rodas_interp_d3(th, dt, S.k.data(), n, o);
+            else if (deriv == 2) rodas_interp_d2(th, dt, S.k.data(), n, o);
             else if (deriv) rodas_interp_d1(th, dt, S.y0.data(), S.y1.data(), S.k.data(), n, o);
             else rodas_interp(th, S.y0.data(), S.y1.data(), S.k.data(), n, o);
             break;

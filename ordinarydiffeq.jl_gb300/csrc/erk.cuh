@@ -275,6 +275,23 @@ __device__ __forceinline__ void tsit5_second_derivative(const double (*k)[C], do
     }
 }
 
+// Tsit5's third derivative (tsit5pre3, the Val{3} form): (sum_i k_i b_i'''(th)) /
+// dt^2 with b_i''' = evalpoly(th, 6 r_i3, 24 r_i4) and inv(dt)^2.
+template <int C>
+__device__ __forceinline__ void tsit5_third_derivative(const double (*k)[C], double th, double dt, double* out) {
+    double b[8];
+#pragma unroll
+    for (int i = 1; i <= 7; ++i) b[i] = fma(th, 24.0 * tab::TSIT5_R(i, 4), 6.0 * tab::TSIT5_R(i, 3));
+    const double invdt = 1.0 / dt, invdt2 = invdt * invdt;
+#pragma unroll
+    for (int i = 0; i < C; ++i) {
+        double acc = k[6][i] * b[7];
+#pragma unroll
+        for (int s = 6; s >= 1; --s) acc = fma(k[s - 1][i], b[s], acc);
+        out[i] = acc * invdt2;
+    }
+}
+
 struct Vern7Alg {
     static constexpr int ORDER = 7;
     static constexpr bool IMPLICIT = false;

@@ -75,7 +75,8 @@ __global__ void dense_eval_pointwise(DenseArgs a) {
             Tsit5Alg::Cache<double, 1> c;
 #pragma unroll
             for (int q = 0; q < NK; ++q) c.k[q][0] = kp[(size_t)q * n * N];
-            if (a.deriv == 2) tsit5_second_derivative<1>(c.k, v.th, v.dt, &o);
+            if (a.deriv == 3) tsit5_third_derivative<1>(c.k, v.th, v.dt, &o);
+            else if (a.deriv == 2) tsit5_second_derivative<1>(c.k, v.th, v.dt, &o);
             else if (a.deriv) tsit5_derivative<1>(c.k, v.th, &o);
             else Tsit5Alg::interpolate<Linear, double, 1, 1>(c, &o, &olo, v.th, v.dt, v.tprev, &y0, &z, &y1, &z,
                                                              nullptr, g);
@@ -83,7 +84,12 @@ __global__ void dense_eval_pointwise(DenseArgs a) {
             Rodas5PAlg::Cache<double, 1> c;
 #pragma unroll
             for (int q = 0; q < NK; ++q) c.dk[q][0] = kp[(size_t)q * n * N];
-            if (a.deriv == 2) {
+            if (a.deriv == 3) {
+                // the Val{3} form (rosenbrock_interpolants.jl:644-653, interp_order 3):
+                // (-6 k2 + 6 k3 - 24 th k3) / dt^3
+                const double k2 = c.dk[1][0], k3 = c.dk[2][0], th = v.th;
+                o = fma(-6.0, k2, fma(6.0, k3, -24.0 * th * k3)) / (v.dt * v.dt * v.dt);
+            } else if (a.deriv == 2) {
                 // the Val{2} form (rosenbrock_interpolants.jl:544-560, interp_order 3):
                 // (-2 k1 + 2 k2 + th (-6 k2 + 6 k3 - 12 th k3)) / dt^2
                 const double k1 = c.dk[0][0], k2 = c.dk[1][0], k3 = c.dk[2][0], th = v.th;

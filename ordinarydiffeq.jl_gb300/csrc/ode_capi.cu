@@ -1582,11 +1582,11 @@ int ode_dense_eval_deriv(ode_handle* h, const ode_problem_desc* d, int64_t N, co
                          int32_t cap, int32_t nq, const double* tq, int32_t tq_per_traj, int32_t deriv, double* out) {
     if (!h || !d) return fail(h, ODE_E_INVALID, "null handle or problem");
     if (deriv < 0) return fail(h, ODE_E_INVALID, "negative derivative order");
-    if (deriv > 2) return fail(h, ODE_E_UNSUPPORTED, "dense evaluation of the value (0) or derivative 1 or 2 only");
-    // the reference's interpolants have a Val{2} form for Tsit5 and the Rosenbrock
-    // combined tableaus (Rodas5P), not for Vern7 or Rosenbrock23
-    if (deriv == 2 && d->alg_id != ODE_TSIT5 && d->alg_id != ODE_RODAS5P)
-        return fail(h, ODE_E_UNSUPPORTED, "the second derivative is for Tsit5 and Rodas5P solutions");
+    if (deriv > 3) return fail(h, ODE_E_UNSUPPORTED, "dense evaluation of the value (0) or derivatives 1 to 3 only");
+    // the reference's interpolants have Val{2} and Val{3} forms for Tsit5 and the
+    // Rosenbrock combined tableaus (Rodas5P), not for Vern7 or Rosenbrock23
+    if (deriv >= 2 && d->alg_id != ODE_TSIT5 && d->alg_id != ODE_RODAS5P)
+        return fail(h, ODE_E_UNSUPPORTED, "derivatives 2 and 3 are for Tsit5 and Rodas5P solutions");
     ode_options o;
     ode_options_default(&o);
     int rc = validate(h, d, &o, N);

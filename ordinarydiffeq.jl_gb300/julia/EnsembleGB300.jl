@@ -166,8 +166,8 @@ struct GB300DenseInterpolation <: SciMLBase.AbstractDiffEqInterpolation
 end
 
 function (id::GB300DenseInterpolation)(tvals, idxs, deriv, p, continuity::Symbol = :left)
-    order = deriv == Val{0} ? 0 : deriv == Val{1} ? 1 : deriv == Val{2} ? 2 :
-            error("GB300 dense output evaluates the solution (Val{0}) and its derivatives Val{1}, Val{2}")
+    order = deriv == Val{0} ? 0 : deriv == Val{1} ? 1 : deriv == Val{2} ? 2 : deriv == Val{3} ? 3 :
+            error("GB300 dense output evaluates the solution (Val{0}) and its derivatives Val{1} to Val{3}")
     tq = tvals isa Number ? [Float64(tvals)] : collect(Float64, tvals)
     n, ns, nq = size(id.u, 1), length(id.t), length(tq)
     d = ProblemDesc(id.model, id.alg, n, length(id.p), 0, 0)

@@ -529,8 +529,9 @@ def dense_eval(res, tq, device=None, deriv=0):
     """sol_j(t) of a dense solve (solve_arrays(..., dense=True)) for every
     trajectory j at the query times tq, shared (nq,) or per trajectory (nq, N),
     evaluated on the GPU in FP64 (ode_dense_eval_deriv).  deriv=1 gives
-    sol_j(t, Val{1}), the derivative of the interpolant; deriv=2 sol_j(t, Val{2})
-    for Tsit5 and Rodas5P solutions.  Returns (nq, n, N)."""
+    sol_j(t, Val{1}), the derivative of the interpolant; deriv=2 and 3
+    sol_j(t, Val{2}) and sol_j(t, Val{3}) for Tsit5 and Rodas5P solutions.
+    Returns (nq, n, N)."""
     info = res.get("dense")
     if not info:
         raise ValueError("not a dense solve: pass dense=True")

@@ -223,7 +223,7 @@ def test_dense_derivative_order_checks():
     dp = x.ctypes.data_as(C.POINTER(C.c_double))
     ns = np.ones(1, dtype=np.int32)
     ip = ns.ctypes.data_as(C.POINTER(C.c_int32))
-    assert L.ode_dense_eval_deriv(h, C.byref(d), 1, dp, dp, dp, dp, ip, 1, 1, dp, 0, 3, dp) == -4
+    assert L.ode_dense_eval_deriv(h, C.byref(d), 1, dp, dp, dp, dp, ip, 1, 1, dp, 0, 4, dp) == -4
     assert L.ode_dense_eval_deriv(h, C.byref(d), 1, dp, dp, dp, dp, ip, 1, 1, dp, 0, -1, dp) == -1
     # Val{2} exists for Tsit5 and Rodas5P only, as in the reference's interpolants
     for alg in (_lib.ODE_VERN7, _lib.ODE_ROSENBROCK23):
@@ -242,12 +242,13 @@ def test_dense_second_derivative_matches_oracle(model, alg, rt):
     rng = np.random.default_rng(4)
     tq = ts[0] + (ts[1] - ts[0]) * rng.uniform(0.05, 0.95, (12, N))
     d2 = dense_eval(g, tq, deriv=2)
+    d3 = dense_eval(g, tq, deriv=3)
     for j in range(N):
         o = O.solve(ALG[alg][1], MODEL[model], u0[:, j], p[:, j], ts[:, j], dense=True, reltol=rt, abstol=rt,
                     saveat_given=False, save_everystep=True, max_step_saves=4096, save_start=True, save_end=True)
-        ref = o["dense"](tq[:, j], deriv=2)
-        scale = np.abs(ref).max(axis=0) + 1e-300
-        assert np.all(np.abs(d2[:, :, j] - ref) <= 1e-4 * scale + 10 * rt), j
+        for dv, ref in ((d2, o["dense"](tq[:, j], deriv=2)), (d3, o["dense"](tq[:, j], deriv=3))):
+            scale = np.abs(ref).max(axis=0) + 1e-300
+            assert np.all(np.abs(dv[:, :, j] - ref) <= 1e-4 * scale + 10 * rt), j
     h = 1e-7 * np.abs(ts[1] - ts[0]).max()
     fd = (dense_eval(g, tq + h, deriv=1) - dense_eval(g, tq - h, deriv=1)) / (2 * h)
     sc = np.abs(d2).max(axis=0, keepdims=True) + 1e-300

@@ -442,6 +442,9 @@ def test_dense_second_derivative(alg):
     d2 = sol(mids, deriv=2)
     assert np.allclose(d2, fd, rtol=1e-4, atol=1e-6)
     assert np.allclose(d2[:, 0], 4.0 * np.exp(-2.0 * mids), rtol=1e-3)
+    # Val{3}: the derivative of Val{2} (a low-degree polynomial in theta per step)
+    fd3 = (sol(mids + h, deriv=2) - sol(mids - h, deriv=2)) / (2 * h)
+    assert np.allclose(sol(mids, deriv=3), fd3, rtol=1e-3, atol=1e-5)
     with pytest.raises(Exception):
         O.solve(O.VERN7, O.LINEAR, [1.0], [-2.0], (0.0, 1.0), dense=True, saveat_given=False)["dense"](0.5, deriv=2)
 
