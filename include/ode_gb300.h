@@ -338,6 +338,15 @@ int ode_dense_eval(ode_handle* h, const ode_problem_desc* d, int64_t ntraj, cons
 int ode_dense_eval_deriv(ode_handle* h, const ode_problem_desc* d, int64_t ntraj, const double* p,
                          const double* t_saved, const double* u_saved, const double* k_saved, const int32_t* nsaved,
                          int32_t cap, int32_t nq, const double* tq, int32_t tq_per_traj, int32_t deriv, double* out);
+/* The same with the continuity of sol(t, continuity): a query equal to a saved
+ * time returns that save (ode_interpolation's exact-time rule), the first one at
+ * that time, or with continuity_right = 1 (continuity = :right) the next save
+ * when it is at the same time (an event's post-affect save).  deriv > 0 always
+ * interpolates, as the reference does. */
+int ode_dense_eval_ex(ode_handle* h, const ode_problem_desc* d, int64_t ntraj, const double* p,
+                      const double* t_saved, const double* u_saved, const double* k_saved, const int32_t* nsaved,
+                      int32_t cap, int32_t nq, const double* tq, int32_t tq_per_traj, int32_t deriv,
+                      int32_t continuity_right, double* out);
 
 /* Continuous-batching serving API.  ode_submit copies the request's inputs
  * into handle-owned pinned/device memory and returns a ticket at once; the

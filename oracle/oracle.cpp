@@ -1990,11 +1990,18 @@ int orc_dense_nsteps(void* h) { return h ? (int)((Dense*)h)->steps.size() : 0; }
 // index >= 1 (0-based) with ts[i+] >= t, clamped to the last; dt = ts[i+] -
 // ts[i-] and theta = (t - ts[i-]) / dt; Vern7's extra stages are formed by
 // _ode_addsteps! with that dt (verner_addsteps.jl:137-193).
-int orc_dense_eval_deriv(void* h, const double* tq, int nq, int deriv, double* out);
+// A query equal to a saved time returns that save for deriv 0 (the first at
+// that time; with `right`, continuity = :right, the next one when it is at the
+// same time), as ode_interpolation does before interpolating.
+int orc_dense_eval_ex(void* h, const double* tq, int nq, int deriv, int right, double* out);
 
-int orc_dense_eval(void* h, const double* tq, int nq, double* out) { return orc_dense_eval_deriv(h, tq, nq, 0, out); }
+int orc_dense_eval(void* h, const double* tq, int nq, double* out) { return orc_dense_eval_ex(h, tq, nq, 0, 0, out); }
 
 int orc_dense_eval_deriv(void* h, const double* tq, int nq, int deriv, double* out) {
+    return orc_dense_eval_ex(h, tq, nq, deriv, 0, out);
+}
+
+int orc_dense_eval_ex(void* h, const double* tq, int nq, int deriv, int right, double* out) {
     Dense* D = (Dense*)h;
     // Val{2}: the forms the reference has (Tsit5, Rodas5P)
     if (deriv < 0 || deriv > 3 || (deriv >= 2 && D->alg != ORC_TSIT5 && D->alg != ORC_RODAS5P)) return -2;
@@ -2006,6 +2013,16 @@ int orc_dense_eval_deriv(void* h, const double* tq, int nq, int deriv, double* o
     std::vector<double> K;
     for (int q = 0; q < nq; ++q) {
         const double t = tq[q];
+        if (deriv == 0) {   // the exact-time rule (searchsortedfirst, then ts[i] == t)
+            size_t i0 = 0;
+            while (i0 < ns && tdir * ts(i0) < tdir * t) ++i0;
+            if (i0 < ns && ts(i0) == t) {
+                const size_t k = (right && i0 + 1 < ns && ts(i0 + 1) == t) ? i0 + 1 : i0;
+                const double* v = k == 0 ? D->steps[0].y0.data() : D->steps[k - 1].y1.data();
+                std::copy(v, v + n, out + (size_t)q * n);
+                continue;
+            }
+        }
         size_t ip = 1;
         while (ip < ns && tdir * ts(ip) < tdir * t) ++ip;
         if (ip > ns - 1) ip = ns - 1;

@@ -85,6 +85,7 @@ double orc_initdt(int alg, int model, int n, const double* p, double t0, double 
 int orc_dense_eval(void* dense_handle, const double* tq, int nq, double* out);
 /* The same with the derivative order (0 the value, 1 sol(t, Val{1})). */
 int orc_dense_eval_deriv(void* dense_handle, const double* tq, int nq, int deriv, double* out);
+int orc_dense_eval_ex(void* dense_handle, const double* tq, int nq, int deriv, int right, double* out);
 /* Step s: t2 = (tprev, tend), y0, y1 (n each), k (returned count x n): the
  * interpolation vectors in the library's dense order. */
 int orc_dense_step(void* dense_handle, int s, double* t2, double* y0, double* y1, double* k);

@@ -64,6 +64,7 @@ def lib():
                                 C.POINTER(C.c_int32), C.POINTER(Stats), C.POINTER(C.c_void_p)]
         L.orc_dense_eval.argtypes = [C.c_void_p, dp, C.c_int, dp]
         L.orc_dense_eval_deriv.argtypes = [C.c_void_p, dp, C.c_int, C.c_int, dp]
+        L.orc_dense_eval_ex.argtypes = [C.c_void_p, dp, C.c_int, C.c_int, C.c_int, dp]
         L.orc_dense_free.argtypes = [C.c_void_p]
         L.orc_dense_nsteps.argtypes = [C.c_void_p]
         L.orc_dense_step.restype = C.c_int
@@ -172,10 +173,10 @@ class DenseSolution:
     def __init__(self, h, n):
         self.h, self.n = h, n
 
-    def __call__(self, ts, deriv=0):
+    def __call__(self, ts, deriv=0, continuity="left"):
         ts = np.ascontiguousarray(np.atleast_1d(ts), dtype=np.float64)
         out = np.zeros((ts.size, self.n))
-        rc = lib().orc_dense_eval_deriv(self.h, _dp(ts), ts.size, int(deriv), _dp(out))
+        rc = lib().orc_dense_eval_ex(self.h, _dp(ts), ts.size, int(deriv), int(continuity == "right"), _dp(out))
         if rc != 0:
             raise ValueError("dense evaluation failed (%d): derivative order %d" % (rc, deriv))
         return out

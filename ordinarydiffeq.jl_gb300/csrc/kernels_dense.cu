@@ -47,6 +47,24 @@ __device__ __forceinline__ Interval dense_locate(const DenseArgs& a, long long j
     return v;
 }
 
+// ode_interpolation's exact-time rule for sol(t) (generic_dense.jl:1094-1190): a
+// query equal to a saved time returns that save, not the interpolant -- the
+// first save at that time, or with continuity = :right the next one when it is
+// at the same time (an event's post-affect save).  Returns the save index, or -1.
+__device__ __forceinline__ int exact_save(const DenseArgs& a, long long j, int ns, double t) {
+    const long long N = a.N;
+    const bool bwd = a.ts[(size_t)(ns - 1) * N + j] < a.ts[j];
+    int lo = 0, hi = ns;   // first s with tdir ts[s] >= tdir t (searchsortedfirst)
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const double ts = a.ts[(size_t)mid * N + j];
+        if (bwd ? ts <= t : ts >= t) hi = mid;
+        else lo = mid + 1;
+    }
+    if (lo >= ns || a.ts[(size_t)lo * N + j] != t) return -1;
+    return (a.right && lo + 1 < ns && a.ts[(size_t)(lo + 1) * N + j] == t) ? lo + 1 : lo;
+}
+
 __device__ __forceinline__ double query_time(const DenseArgs& a, long long j, int r) {
     return a.tq_per_traj ? a.tq[(size_t)r * a.N + j] : a.tq[r];
 }
@@ -64,7 +82,15 @@ __global__ void dense_eval_pointwise(DenseArgs a) {
         for (int i = 0; i < n; ++i) a.out[((size_t)r * n + i) * N + j] = dnan();
         return;
     }
-    const Interval v = dense_locate(a, j, ns, query_time(a, j, r));
+    const double tq = query_time(a, j, r);
+    if (a.deriv == 0) {
+        const int k = exact_save(a, j, ns, tq);
+        if (k >= 0) {
+            for (int i = 0; i < n; ++i) a.out[((size_t)r * n + i) * N + j] = a.us[((size_t)k * n + i) * N + j];
+            return;
+        }
+    }
+    const Interval v = dense_locate(a, j, ns, tq);
     constexpr int NK = kDenseVectors[ALG];
     Group<1> g;
     for (int i = 0; i < n; ++i) {
@@ -140,7 +166,17 @@ __global__ void dense_eval_vern7(DenseArgs a) {
         for (int c = 0; c < C; ++c) a.out[((size_t)r * n + g.lane * C + c) * N + j] = dnan();
         return;
     }
-    const Interval v = dense_locate(a, j, ns, query_time(a, j, r));
+    const double tq = query_time(a, j, r);
+    if (a.deriv == 0) {
+        const int k = exact_save(a, j, ns, tq);
+        if (k >= 0) {
+#pragma unroll
+            for (int c = 0; c < C; ++c)
+                a.out[((size_t)r * n + g.lane * C + c) * N + j] = a.us[((size_t)k * n + g.lane * C + c) * N + j];
+            return;
+        }
+    }
+    const Interval v = dense_locate(a, j, ns, tq);
     double p[Model::NP];
 #pragma unroll
     for (int k = 0; k < Model::NP; ++k) p[k] = a.p[(size_t)k * N + j];

@@ -1580,6 +1580,13 @@ int ode_solve_ensemble_dense(ode_handle* h, const ode_problem_desc* d, const ode
 int ode_dense_eval_deriv(ode_handle* h, const ode_problem_desc* d, int64_t N, const double* p,
                          const double* t_saved, const double* u_saved, const double* k_saved, const int32_t* nsaved,
                          int32_t cap, int32_t nq, const double* tq, int32_t tq_per_traj, int32_t deriv, double* out) {
+    return ode_dense_eval_ex(h, d, N, p, t_saved, u_saved, k_saved, nsaved, cap, nq, tq, tq_per_traj, deriv, 0, out);
+}
+
+int ode_dense_eval_ex(ode_handle* h, const ode_problem_desc* d, int64_t N, const double* p,
+                      const double* t_saved, const double* u_saved, const double* k_saved, const int32_t* nsaved,
+                      int32_t cap, int32_t nq, const double* tq, int32_t tq_per_traj, int32_t deriv,
+                      int32_t continuity_right, double* out) {
     if (!h || !d) return fail(h, ODE_E_INVALID, "null handle or problem");
     if (deriv < 0) return fail(h, ODE_E_INVALID, "negative derivative order");
     if (deriv > 3) return fail(h, ODE_E_UNSUPPORTED, "dense evaluation of the value (0) or derivatives 1 to 3 only");
@@ -1615,6 +1622,7 @@ int ode_dense_eval_deriv(ode_handle* h, const ode_problem_desc* d, int64_t N, co
     a.tq_per_traj = tq_per_traj ? 1 : 0;
     a.cap = cap;
     a.deriv = deriv;
+    a.right = continuity_right ? 1 : 0;
     cudaStream_t s = h->main.stream;
     // The saves are copied in (the interval search reads them scattered, which is
     // slow from host memory: measured 30x slower in place over NVLink-C2C); a

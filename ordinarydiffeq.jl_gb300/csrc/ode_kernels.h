@@ -50,7 +50,8 @@ struct DenseArgs {
     const int32_t* nsaved;
     const double* tq;
     double* out;
-    int deriv;              // 0: sol(t); 1: sol(t, Val{1})
+    int deriv;              // 0: sol(t); 1-3: sol(t, Val{deriv})
+    int right;              // continuity = :right (a query at a time saved twice takes the later save)
 };
 
 // Dense vectors stored per step, by ode_alg (Tsit5, Vern7, Rodas5P, Rosenbrock23,

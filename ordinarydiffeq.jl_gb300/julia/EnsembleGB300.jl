@@ -172,11 +172,13 @@ function (id::GB300DenseInterpolation)(tvals, idxs, deriv, p, continuity::Symbol
     n, ns, nq = size(id.u, 1), length(id.t), length(tq)
     d = ProblemDesc(id.model, id.alg, n, length(id.p), 0, 0)
     out = zeros(n, nq)   # [(r*n + i)*N + j] with N = 1 -> out[i, r]
-    status = ccall((:ode_dense_eval_deriv, LIB), Cint,
+    continuity in (:left, :right) || error("continuity: :left or :right")
+    status = ccall((:ode_dense_eval_ex, LIB), Cint,
                    (Ptr{Cvoid}, Ref{ProblemDesc}, Int64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
-                    Ptr{Int32}, Int32, Int32, Ptr{Float64}, Int32, Int32, Ptr{Float64}),
-                   handle(id.device), d, 1, id.p, id.t, id.u, id.k, Int32[ns], ns, nq, tq, 0, order, out)
-    status == 0 || error("ode_dense_eval_deriv: ", unsafe_string(ccall((:ode_last_error, LIB), Cstring, (Ptr{Cvoid},), handle(id.device))))
+                    Ptr{Int32}, Int32, Int32, Ptr{Float64}, Int32, Int32, Int32, Ptr{Float64}),
+                   handle(id.device), d, 1, id.p, id.t, id.u, id.k, Int32[ns], ns, nq, tq, 0, order,
+                   Int32(continuity === :right), out)
+    status == 0 || error("ode_dense_eval_ex: ", unsafe_string(ccall((:ode_last_error, LIB), Cstring, (Ptr{Cvoid},), handle(id.device))))
     vals = [idxs === nothing ? out[:, r] : out[idxs, r] for r in 1:nq]
     tvals isa Number ? vals[1] : vals
 end

@@ -83,6 +83,8 @@ SIGNATURES = {
                                  C.c_int32, _DP, C.c_int32, _DP]),
     "ode_dense_eval_deriv": (C.c_int, [_VP, C.POINTER(ProblemDesc), C.c_int64, _DP, _DP, _DP, _DP, _IP, C.c_int32,
                                        C.c_int32, _DP, C.c_int32, C.c_int32, _DP]),
+    "ode_dense_eval_ex": (C.c_int, [_VP, C.POINTER(ProblemDesc), C.c_int64, _DP, _DP, _DP, _DP, _IP, C.c_int32,
+                                    C.c_int32, _DP, C.c_int32, C.c_int32, C.c_int32, _DP]),
     "ode_submit": (C.c_int, [_VP, C.POINTER(ProblemDesc), C.POINTER(Options), C.c_int64, _IP, _DP, _DP,
                              _DP, _DP, _DP, _DP, _IP, _IP, C.POINTER(Stats), C.POINTER(C.c_uint64)]),
     "ode_poll": (C.c_int, [_VP, C.c_uint64, _IP]),

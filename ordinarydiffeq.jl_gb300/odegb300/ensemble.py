@@ -238,19 +238,21 @@ class ODESolution:
     def dense(self):
         return self._dense is not None
 
-    def __call__(self, t, deriv=0, idxs=None):
+    def __call__(self, t, deriv=0, idxs=None, continuity="left"):
         """sol(t) as ode_interpolation (generic_dense.jl:1094-1190) evaluates it:
         the method's interpolant on the saved steps for a dense solve (on the
         GPU), linear interpolation between saves otherwise.  deriv=1 is
-        sol(t, Val{1}) (dense solves); idxs selects components.  Scalar t gives
-        one state vector, an array of times one row per time."""
+        sol(t, Val{1}) (dense solves); idxs selects components.  A time equal
+        to a saved one returns that save; continuity="right" the later of two
+        saves at one time.  Scalar t gives one state vector, an array of times
+        one row per time."""
         tq = np.atleast_1d(np.asarray(t, dtype=np.float64))
         if self._dense is not None:
             res, j = self._dense
             sub = {"t": res["t"][:, j:j + 1].copy(), "u": res["u"][:, :, j:j + 1].copy(),
                    "k": res["k"][..., j:j + 1].copy(), "nsaved": res["nsaved"][j:j + 1].copy(),
                    "dense": dict(res["dense"], p=res["dense"]["p"][:, j:j + 1].copy())}
-            vals = dense_eval(sub, tq, deriv=deriv)[:, :, 0]
+            vals = dense_eval(sub, tq, deriv=deriv, continuity=continuity)[:, :, 0]
         elif deriv:
             raise ValueError("derivatives of the interpolant need a dense solve")
         else:
@@ -258,6 +260,11 @@ class ODESolution:
             us = np.asarray(self.u, dtype=np.float64)
             vals = np.empty((tq.size, us.shape[1]))
             for r, tv in enumerate(tq):
+                i0 = int(np.searchsorted(ts, tv, side="left"))   # the exact-time rule first
+                if i0 < len(ts) and ts[i0] == tv:
+                    k = i0 + 1 if continuity == "right" and i0 + 1 < len(ts) and ts[i0 + 1] == tv else i0
+                    vals[r] = us[k]
+                    continue
                 ip = min(len(ts) - 1, 1 + int(np.searchsorted(ts[1:], tv, side="left")))
                 im = ip - 1 if ip > 0 else ip
                 dt = ts[ip] - ts[im]
@@ -525,13 +532,14 @@ def solve_arrays(model, alg, ens, u0s, ps, tspans, saveat=None, reltol=1e-3, abs
     return out
 
 
-def dense_eval(res, tq, device=None, deriv=0):
+def dense_eval(res, tq, device=None, deriv=0, continuity="left"):
     """sol_j(t) of a dense solve (solve_arrays(..., dense=True)) for every
     trajectory j at the query times tq, shared (nq,) or per trajectory (nq, N),
     evaluated on the GPU in FP64 (ode_dense_eval_deriv).  deriv=1 gives
     sol_j(t, Val{1}), the derivative of the interpolant; deriv=2 and 3
-    sol_j(t, Val{2}) and sol_j(t, Val{3}) for Tsit5 and Rodas5P solutions.
-    Returns (nq, n, N)."""
+    sol_j(t, Val{2}) and sol_j(t, Val{3}) for Tsit5 and Rodas5P solutions.  A
+    query at a saved time returns that save; continuity="right" takes the later
+    of two saves at one time (an event's post-affect state).  Returns (nq, n, N)."""
     info = res.get("dense")
     if not info:
         raise ValueError("not a dense solve: pass dense=True")
@@ -548,9 +556,11 @@ def dense_eval(res, tq, device=None, deriv=0):
     d = _lib.ProblemDesc(info["model"], info["alg"], n, ps.shape[0], 0, 0)
     h = get_handle(info["device"] if device is None else device)
     dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
-    _lib.check(L.ode_dense_eval_deriv(h, C.byref(d), N, dp(ps), dp(t), dp(u), dp(k),
-                                      ns.ctypes.data_as(C.POINTER(C.c_int32)), cap, nq, dp(tq), int(per), int(deriv),
-                                      dp(out)), h)
+    if continuity not in ("left", "right"):
+        raise ValueError('continuity: "left" or "right"')
+    _lib.check(L.ode_dense_eval_ex(h, C.byref(d), N, dp(ps), dp(t), dp(u), dp(k),
+                                   ns.ctypes.data_as(C.POINTER(C.c_int32)), cap, nq, dp(tq), int(per), int(deriv),
+                                   int(continuity == "right"), dp(out)), h)
     return out
 
 

@@ -142,3 +142,7 @@ def test_linear_interpolation_between_saves_without_dense():
     # left continuity: t == ts[i] takes the interval ending at ts[i]; outside the
     # range the first or last interval's line continues
     assert np.allclose(s(4.0), [7.0, -10.0]) and np.allclose(s(-1.0), [-1.0, 0.0])
+    # a time saved twice (an event): the first save, or with continuity = :right the second
+    e = ODESolution(np.array([0.0, 1.0, 1.0, 2.0]), [np.array([0.0]), np.array([1.0]), np.array([-1.0]),
+                                                     np.array([0.0])], 1, {})
+    assert e(1.0)[0] == 1.0 and e(1.0, continuity="right")[0] == -1.0 and e(0.5)[0] == 0.5

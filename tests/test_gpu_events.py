@@ -134,3 +134,37 @@ def test_events_with_dense_output_match_oracle(alg):
         assert np.all(np.abs(g["t"][:ns, j] - o["t"]) <= 1e-12 * np.abs(o["t"]) + 1e-14), j
         ref = o["dense"](tq[:, j])
         assert np.all(np.abs(ev[:, :, j] - ref) <= 10 * (rt * np.abs(ref) + at)), j
+
+
+@pytest.mark.parametrize("alg", ["tsit5", "rodas5p"])
+def test_dense_output_at_event_times_takes_the_saves(alg):
+    # ode_interpolation's exact-time rule: sol(t) at a saved time is that save; at a
+    # contact (saved twice) the pre-affect state, and with continuity = :right the
+    # post-affect one (ode_event_tests.jl:170-172: sol(t, continuity = :right)[2] > 0)
+    from odegb300 import dense_eval
+    N = 32
+    wl = balls(N, seed=6)
+    rt = at = 1e-8
+    cb = ContinuousCallback(interp_points=10, max_events=16)
+    g = gpu("bouncing_ball", alg, wl["u0"], wl["p"], wl["tspan"], None, rt, at, callback=cb, save_everystep=True,
+            max_step_saves=4096, dense=True)
+    ns = g["nsaved"]
+    k = int(ns.min())
+    tq = g["t"][:k]                       # (k, N): every trajectory's own first k saved times
+    left = dense_eval(g, tq)
+    right = dense_eval(g, tq, continuity="right")
+    dup = np.zeros((k, N), dtype=bool)          # save r is followed by a save at the same time
+    dup[:-1] = g["t"][:k - 1] == g["t"][1:k]
+    second = np.zeros((k, N), dtype=bool)       # save r repeats the time of save r - 1
+    second[1:] = dup[:-1]
+    assert dup.any()
+    m = ~second
+    assert np.array_equal(left.transpose(1, 0, 2)[:, m], g["u"][:k].transpose(1, 0, 2)[:, m])
+    r, j = np.nonzero(dup)
+    assert np.array_equal(left[r + 1, :, j], g["u"][r, :, j])      # either query time: the first save
+    assert np.array_equal(right[r, :, j], g["u"][r + 1, :, j])     # :right, the second
+    assert np.array_equal(right[r + 1, :, j], g["u"][r + 1, :, j])
+    # falling into the floor before, rising after (a ball that terminate!s at its
+    # contact keeps its velocity in the post-affect save)
+    live = g["retcode"][j] == 1
+    assert live.any() and (left[r, 1, j] <= 0).all() and (right[r[live], 1, j[live]] >= 0).all()

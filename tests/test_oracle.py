@@ -877,6 +877,11 @@ def test_dense_output_with_events_follows_the_bounces(alg):
         hit = np.nonzero(np.abs(t - c) < 1e-8)[0]
         assert len(hit) == 2
         assert d([t[hit[0]]])[0][1] == pytest.approx(r["u"][hit[0]][1], rel=1e-12)
+        # the exact-time rule: a saved time returns the save itself; continuity = :right
+        # the post-affect save (ode_event_tests.jl:170-172: sol(t, continuity = :right)[2] > 0)
+        assert np.array_equal(d([t[hit[0]]])[0], r["u"][hit[0]])
+        right = d([t[hit[0]]], continuity="right")[0]
+        assert np.array_equal(right, r["u"][hit[1]]) and right[1] > 0 > r["u"][hit[0]][1]
 
 
 # Rosenbrock23 as a W-method (Rosenbrock23(max_jac_age = ...), _rosenbrock_jac_reuse_decision,
