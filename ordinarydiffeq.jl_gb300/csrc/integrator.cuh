@@ -1038,7 +1038,8 @@ __device__ void solve_trajectories(const EnsembleArgs& a, const Group<L>& g, Nex
 // counter until the ensemble is exhausted).
 template <class Alg, class Model, class R, int L, int C, bool FWD = false>
 // Mixed kernels with up to 4 states per lane are held to 3 resident blocks of
-// 128 (<= 170 registers; measured 10% faster than 2 on Robertson, no spills);
+// 128 (<= 170 registers; measured 10% faster than 2 on Robertson, no spills;
+// 4 blocks cap them at 128 registers and spill 316 bytes: 4.92 against 4.24 ms);
 // wider or FP64 kernels keep their registers.
 #ifndef ODEGB_MIN_BLOCKS_F32
 #define ODEGB_MIN_BLOCKS_F32 3
